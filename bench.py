@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 prover backend.
+
+Default workload (`--workload kernels`): the kernel microbench on synthetic seeded inputs —
+interpolate then evaluate 256 columns of 2^20 M31 words (canonic coset, log 20) at blowup 4
+(2^22 points each), Blake2s Merkle commit over the 256 x 2^22 evaluations, and one FRI fold of a
+2^22-point QM31 circle evaluation down to a 2^4 line with seeded alphas. One step = that whole
+pass. Inputs (1 GiB) are larger than L2 (129 MB), so no explicit flush is needed between steps.
+
+`value` is trace cells/s (256 x 2^20 input cells per step) with inputs resident in HBM when the
+timed region starts; `e2e` is the same metric through the public C ABI with the inputs copied
+from pinned host memory and the Merkle root + last FRI layer read back inside the timed region.
+
+`--impl reference` times the oracle (C++ restatement of the reference CPU backend; the reference
+Rust crate cannot be built without a Rust toolchain) on all host cores over a bounded sample.
+Multi-GPU (torchrun): independent replicas per rank, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+P = (1 << 31) - 1
+GAMMA = 0x9E3779B97F4A7C15
+MASK64 = (1 << 64) - 1
+
+
+def gen_words(k: int, c: int, n: int):
+    """Word i of column c of workload k: splitmix64(k + (c*2^32 + i + 1) * GAMMA) mod P."""
+    import numpy as np
+
+    i = np.arange(n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = np.uint64(k) + (np.uint64(c << 32) + i + np.uint64(1)) * np.uint64(GAMMA)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z % np.uint64(P)).astype(np.uint32)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------- kernel microbench
+class KernelsWorkload:
+    N_COLS, LOG, BLOWUP, FRI_LOG, FRI_LAST = 256, 20, 2, 22, 4
+
+    def __init__(self, n_cols=None):
+        import numpy as np
+        import torch
+
+        from stwo_gb300 import _lib
+        from stwo_gb300.backend import CudaBackend, SecureColumn, TwiddleTree
+        from stwo_gb300.circle import canonic_half_coset
+
+        self.B, self.SC = CudaBackend, SecureColumn
+        if n_cols:
+            self.N_COLS = n_cols
+        L = self.LOG + self.BLOWUP
+        self.L = L
+        n, N = 1 << self.LOG, 1 << L
+        self.host_in = torch.empty((self.N_COLS, n), dtype=torch.int32).pin_memory()
+        hv = self.host_in.numpy().view(np.uint32)
+        for c in range(self.N_COLS):
+            hv[c] = gen_words(1, c, n)
+        self.inp = self.host_in.cuda()
+        self.work = torch.empty_like(self.inp)
+        self.evals = torch.empty((self.N_COLS, N), dtype=torch.int32, device="cuda")
+        self.tw = TwiddleTree(canonic_half_coset(L))
+        self.small, self.big = canonic_half_coset(self.LOG), canonic_half_coset(L)
+        self.fri_half = canonic_half_coset(self.FRI_LOG)
+        self.fri_tw = self.tw if self.FRI_LOG <= L else TwiddleTree(self.fri_half)
+        self.fsrc = SecureColumn([torch.from_numpy(gen_words(1, 1000 + k, 1 << self.FRI_LOG).view(np.int32)).cuda()
+                                  for k in range(4)])
+        self.alphas = [tuple(int(x) for x in gen_words(1, 2000, 4 * self.FRI_LOG)[4 * j:4 * j + 4])
+                       for j in range(self.FRI_LOG)]
+        self.layers = [torch.empty(((1 << lg), 8), dtype=torch.int32, device="cuda") for lg in range(L + 1)]
+        self.line = SecureColumn([torch.empty(1 << (self.FRI_LOG - 1), dtype=torch.int32, device="cuda")
+                                  for _ in range(4)])
+        self.work_cols = [self.work[c] for c in range(self.N_COLS)]
+        self.eval_cols = [self.evals[c] for c in range(self.N_COLS)]
+        self.cells = self.N_COLS * n
+        self.root_host = torch.empty(8, dtype=torch.int32).pin_memory()
+        self.fri_host = torch.empty((4, 1 << self.FRI_LAST), dtype=torch.int32).pin_memory()
+        self.lib = _lib.load()
+
+    def restore(self):
+        self.work.copy_(self.inp)
+
+    def stages(self, ev=None):
+        """The hot path; `ev` (list of CUDA events) brackets interpolate / evaluate / merkle / fri."""
+        import torch
+
+        from stwo_gb300.circle import double
+
+        B = self.B
+        mark = (lambda i: ev[i].record()) if ev else (lambda i: None)
+        mark(0)
+        B.interpolate_columns(self.work_cols, self.small, self.tw)
+        mark(1)
+        B.evaluate_polynomials(self.work_cols, self.big, self.tw, out=self.eval_cols)
+        mark(2)
+        B.commit_on_layer(self.L, None, self.eval_cols, out=self.layers[self.L])
+        mark(3)
+        for lg in range(self.L - 1, -1, -1):
+            B.commit_on_layer(lg, self.layers[lg + 1], [], out=self.layers[lg])
+        mark(4)
+        for c in self.line.cols:
+            c.zero_()
+        B.fold_circle_into_line(self.line, self.fsrc, self.fri_half, self.alphas[0], self.fri_tw)
+        cur, dom = self.line, self.fri_half
+        j = 1
+        while len(cur) > (1 << self.FRI_LAST):
+            cur = B.fold_line(cur, dom, self.alphas[j], self.fri_tw)
+            dom = double(dom)
+            j += 1
+        self.last = cur
+        mark(5)
+        del torch
+
+    def readback(self):
+        self.root_host.copy_(self.layers[0][0], non_blocking=True)
+        for k in range(4):
+            self.fri_host[k].copy_(self.last.cols[k], non_blocking=True)
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from stwo_gb300 import _lib
+    from stwo_gb300.build import build_backend
+
+    if rank == 0 or world == 1:
+        build_backend()
+    if world > 1:
+        torch.distributed.barrier()
+    _lib.call("stwo_device_init", local)
+    wl = KernelsWorkload()
+    lib = wl.lib
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # Warm-up.
+    for _ in range(args.warmup):
+        wl.restore()
+        wl.stages()
+    barrier()
+
+    # Timed: device-resident inputs; per-stage CUDA events on the launching stream.
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
+    launches0 = lib.stwo_kernel_launches()
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for s in range(args.steps):
+            wl.restore()
+            wl.stages(evs[s])
+        barrier()
+        wall = time.perf_counter() - t0
+    launches = lib.stwo_kernel_launches() - launches0
+    stage_ms = np.zeros(5)
+    for s in range(args.steps):
+        for i in range(5):
+            stage_ms[i] += evs[s][i].elapsed_time(evs[s][i + 1])
+    stage_ms /= args.steps
+    step_ms = float(stage_ms.sum())
+    if world > 1:
+        t = torch.tensor([step_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+
+    # End to end through the public API: pinned host inputs -> HBM -> hot path -> root + FRI layer.
+    for _ in range(max(1, args.warmup)):
+        wl.work.copy_(wl.host_in, non_blocking=True)
+        wl.stages()
+        wl.readback()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        wl.work.copy_(wl.host_in, non_blocking=True)
+        wl.stages()
+        wl.readback()
+    e1.record()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    N, n = 1 << wl.L, 1 << wl.LOG
+    # Dominant HBM-bound kernel: the evaluate pass (4n read + 4N written per column).
+    eval_bytes = wl.N_COLS * (4 * n + 4 * N)
+    eval_s = stage_ms[1] / 1e3
+    achieved = eval_bytes / eval_s / 1e9
+    interp_gbs = wl.N_COLS * 8 * n / (stage_ms[0] / 1e3) / 1e9
+    comp = wl.N_COLS * N * (wl.N_COLS // 16) // wl.N_COLS  # leaf compressions = N * ceil(256/16)
+    comp = N * ((wl.N_COLS + 15) // 16)
+    line = {
+        "metric": "trace cells/s (kernel microbench: interpolate+evaluate 256x2^20 @ blowup 4, "
+                  "Blake2s Merkle 256x2^22, FRI fold 2^22->2^4)",
+        "value": wl.cells * world / (step_ms / 1e3),
+        "unit": "cells/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32 (M31 field words)",
+        "data": "synthetic seeded (splitmix64 mod P), shapes of the kernel microbench config",
+        "config": {"workload": "kernels: 256 cols x 2^20 -> 2^22 (blowup 4) + Merkle + FRI 2^22->2^4",
+                   "n_cols": wl.N_COLS, "log_size": wl.LOG, "log_blowup": wl.BLOWUP, "fri_log": wl.FRI_LOG,
+                   "l2": "inputs (1 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
+        "stages_ms": {"interpolate": stage_ms[0], "evaluate": stage_ms[1], "merkle_leaves": stage_ms[2],
+                      "merkle_nodes": stage_ms[3], "fri_folds": stage_ms[4]},
+        "roofline": {"bound": "hbm", "kernel": "k_fft_pass<evaluate> (2 passes per call)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_call": eval_bytes},
+        "interpolate_gbs": interp_gbs,
+        "merkle_leaf_compressions_per_s": comp / (stage_ms[2] / 1e3),
+        "e2e": {"value": wl.cells * world / (e2e_ms / 1e3), "unit": "cells/s",
+                "h2d_bytes_per_step": wl.cells * 4, "d2h_bytes_per_step": 32 + 4 * 4 * (1 << wl.FRI_LAST),
+                "ms_per_step": e2e_ms},
+        "gpu_launches": int(launches // args.steps) * args.steps,
+        "wall_s": wall,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_kernels(args.cpu_threads)
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_kernels(threads=0, n_cols=16):
+    """The oracle on all host cores over a bounded sample (n_cols columns at full sizes)."""
+    import numpy as np
+
+    import oracle.pyoracle as O
+
+    lib = O.lib()
+    lib.oracle_bench_cfg2.restype = C.c_double
+    root = np.zeros(8, np.uint32)
+    fri = np.zeros(64, np.uint32)
+    nthreads = threads or os.cpu_count() or 1
+    secs = lib.oracle_bench_cfg2(C.c_uint32(n_cols), C.c_uint32(20), C.c_uint32(2), C.c_uint32(22),
+                                 C.c_int(nthreads), root.ctypes.data_as(C.c_void_p), fri.ctypes.data_as(C.c_void_p))
+    return {"value": n_cols * (1 << 20) / secs, "unit": "cells/s", "cores": nthreads, "kind": "port",
+            "sample": f"{n_cols} of 256 columns at full sizes (2^20 -> 2^22, Merkle over {n_cols} cols, "
+                      f"FRI 2^22->2^4): {secs:.2f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from stwo_gb300.build import build_oracle
+
+    build_oracle()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline_kernels(args.cpu_threads, n_cols=4)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline_kernels(args.cpu_threads, n_cols=8))
+    v = sorted(x["value"] for x in vals)[len(vals) // 2]
+    cb = dict(vals[0])
+    cb["value"] = v
+    out = {
+        "impl": "reference",
+        "metric": "trace cells/s (kernel microbench: interpolate+evaluate 256x2^20 @ blowup 4, "
+                  "Blake2s Merkle 256x2^22, FRI fold 2^22->2^4)",
+        "value": v, "unit": "cells/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 8 * (1 << 20) / v * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
+        "data": "synthetic seeded (splitmix64 mod P)",
+        "config": {"workload": "kernels: 256 cols x 2^20 -> 2^22 (blowup 4) + Merkle + FRI 2^22->2^4",
+                   "sample_cols_per_step": 8},
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "C++ restatement of the reference CPU backend (the Rust reference needs cargo, absent here)",
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

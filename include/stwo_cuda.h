@@ -1,0 +1,164 @@
+/*
+ * stwo_cuda.h — C ABI of the GB300 (sm_103a) prover backend.
+ *
+ * Each entry point replaces one method of the reference's backend trait family
+ * (crates/prover/src/core/backend/mod.rs:19-65 and the trait homes cited per function).
+ * Conventions:
+ *   - Every function returns stwo_status; nothing aborts and nothing throws across the ABI.
+ *     Preconditions the reference `assert!`s return STWO_ERR_INVALID_ARG.
+ *   - `d_` pointers are device (HBM) pointers owned by the caller; `h_` pointers are host.
+ *     Base-field columns are arrays of canonical M31 words (u32 < 2^31 - 1). A secure
+ *     (QM31) column is four such coordinate columns, as SecureColumnByCoords
+ *     (crates/prover/src/core/fields/secure_column.rs:15).
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream). Calls are stream ordered;
+ *     results written to host memory are complete when the call returns.
+ *   - Evaluations are in bit-reversed circle-domain order, as the reference's
+ *     CircleEvaluation<_, _, BitReversedOrder>; coefficients are in the reference CPU
+ *     backend's order (crates/prover/src/core/backend/cpu/circle.rs:18-135).
+ */
+#ifndef STWO_CUDA_H
+#define STWO_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t stwo_status;
+#define STWO_OK 0
+#define STWO_ERR_INVALID_ARG 1
+#define STWO_ERR_OOM 2
+#define STWO_ERR_TIMEOUT 3
+#define STWO_ERR_CUDA 4
+#define STWO_ERR_UNSUPPORTED 5
+
+/* Coset `initial + <step>` of size 2^log_size, by circle-group indices modulo 2^31
+ * (crates/prover/src/core/circle.rs:307-330). A CircleDomain is given by its half coset
+ * (crates/prover/src/core/poly/circle/domain.rs:14-20). */
+typedef struct {
+  uint32_t initial_index;
+  uint32_t step_size;
+  uint32_t log_size;
+} stwo_coset;
+
+/* QM31 element (a + b i) + (c + d i) u as {a, b, c, d} (crates/prover/src/core/fields/qm31.rs:21-45). */
+typedef struct {
+  uint32_t v[4];
+} stwo_qm31;
+
+/* CirclePoint<SecureField> (crates/prover/src/core/circle.rs:13-17). */
+typedef struct {
+  stwo_qm31 x;
+  stwo_qm31 y;
+} stwo_qm31_point;
+
+typedef struct stwo_twiddle_tree_s* stwo_twiddle_tree;
+
+/* ------------------------------------------------------------------ runtime */
+const char* stwo_status_string(stwo_status status);
+/* Detail of the last failure on the calling host thread. */
+const char* stwo_last_error(void);
+/* Selects the device for the calling thread and warms the context. */
+stwo_status stwo_device_init(int device);
+stwo_status stwo_sync(void* stream);
+/* Diagnostic without a reference counterpart: kernels launched by this library so far
+ * (benchmarks report the count inside their timed region). */
+uint64_t stwo_kernel_launches(void);
+
+/* Column storage: Column::zeros / uninitialized / to_cpu / at
+ * (crates/prover/src/core/backend/mod.rs:46-65). */
+stwo_status stwo_buf_alloc(void** d_ptr, size_t bytes, void* stream);
+stwo_status stwo_buf_free(void* d_ptr, void* stream);
+stwo_status stwo_buf_upload(void* d_dst, const void* h_src, size_t bytes, void* stream);
+stwo_status stwo_buf_download(void* h_dst, const void* d_src, size_t bytes, void* stream);
+stwo_status stwo_buf_zero(void* d_dst, size_t bytes, void* stream);
+/* Column::at for a list of indices (Merkle decommitment reads,
+ * crates/prover/src/core/vcs/prover.rs:80-149). */
+stwo_status stwo_read_words(const uint32_t* d_col, const uint64_t* h_idx, size_t n, uint32_t* h_out,
+                            void* stream);
+
+/* ------------------------------------------------------------------ twiddles */
+/* PolyOps::precompute_twiddles (crates/prover/src/core/poly/circle/ops.rs:68;
+ * layout of crates/prover/src/core/backend/cpu/circle.rs:137-188, not doubled). */
+stwo_status stwo_twiddles_precompute(stwo_coset root, stwo_twiddle_tree* out, void* stream);
+stwo_status stwo_twiddles_free(stwo_twiddle_tree tree);
+stwo_status stwo_twiddles_info(stwo_twiddle_tree tree, stwo_coset* root, const uint32_t** d_twiddles,
+                               const uint32_t** d_itwiddles, size_t* size);
+
+/* ------------------------------------------------------------------ PolyOps */
+/* PolyOps::interpolate_columns (crates/prover/src/core/poly/circle/ops.rs:20-33), in place:
+ * each column holds 2^(domain.log_size+1) bit-reversed evaluations and receives the
+ * coefficients. `domain_half_coset` must be a doubling of the tree's root coset. */
+stwo_status stwo_interpolate_columns(stwo_twiddle_tree tree, stwo_coset domain_half_coset,
+                                     uint32_t* const* d_cols, uint32_t n_cols, void* stream);
+/* PolyOps::evaluate_polynomials / evaluate (ops.rs:41-65): polynomials with 2^coeff_log_size
+ * coefficients evaluated on the circle domain of `domain_half_coset` (log size >= coeff_log_size). */
+stwo_status stwo_evaluate_columns(stwo_twiddle_tree tree, stwo_coset domain_half_coset,
+                                  const uint32_t* const* d_coeffs, uint32_t coeff_log_size,
+                                  uint32_t* const* d_out, uint32_t n_cols, void* stream);
+/* PolyOps::extend (ops.rs:39-40): coefficients zero-padded to 2^log_size. */
+stwo_status stwo_extend(const uint32_t* d_coeffs, uint32_t coeff_log_size, uint32_t* d_out, uint32_t log_size,
+                        void* stream);
+/* PolyOps::eval_at_point (ops.rs:37) batched: h_out[i] = poly[poly_of[i]](points[i]). */
+stwo_status stwo_eval_at_points(const uint32_t* const* d_coeffs, const uint32_t* h_log_sizes, uint32_t n_polys,
+                                const uint32_t* h_poly_of, const stwo_qm31_point* h_points, uint32_t n_evals,
+                                stwo_qm31* h_out, void* stream);
+
+/* ColumnOps::bit_reverse_column (crates/prover/src/core/backend/mod.rs:40). */
+stwo_status stwo_bit_reverse_column(uint32_t* d_col, uint32_t log_size, void* stream);
+
+/* ------------------------------------------------------------------ MerkleOps */
+/* MerkleOps<Blake2sMerkleHasher>::commit_on_layer (crates/prover/src/core/vcs/ops.rs:41-45;
+ * backend/simd/blake2s.rs:60-145). Hashes are 8 little-endian u32 words. `d_prev_layer` is
+ * NULL for the leaf layer, else 2^(log_size+1) hashes. Columns have 2^log_size values. */
+stwo_status stwo_merkle_commit_layer(uint32_t log_size, const uint32_t* d_prev_layer,
+                                     const uint32_t* const* d_cols, uint32_t n_cols, uint32_t* d_out,
+                                     void* stream);
+
+/* ------------------------------------------------------------------ FriOps */
+/* FriOps::fold_line (crates/prover/src/core/fri.rs:103-107): evaluation on the line domain
+ * `line_domain` (2^log_size values) folded into 2^(log_size-1) values. */
+stwo_status stwo_fri_fold_line(stwo_twiddle_tree tree, stwo_coset line_domain, const uint32_t* const d_eval[4],
+                               stwo_qm31 alpha, uint32_t* const d_out[4], void* stream);
+/* FriOps::fold_circle_into_line (fri.rs:124-129): dst = dst * alpha^2 + fold(src). */
+stwo_status stwo_fri_fold_circle_into_line(stwo_twiddle_tree tree, stwo_coset src_half_coset,
+                                           uint32_t* const d_dst[4], const uint32_t* const d_src[4],
+                                           stwo_qm31 alpha, void* stream);
+/* FriOps::decompose (fri.rs:136-138; backend/simd/fri.rs:111-161). */
+stwo_status stwo_fri_decompose(const uint32_t* const d_eval[4], uint32_t log_size, uint32_t* const d_g[4],
+                               stwo_qm31* h_lambda, void* stream);
+
+/* ------------------------------------------------------------------ QuotientOps */
+/* One ColumnSampleBatch (crates/prover/src/core/pcs/quotients.rs:37-68). */
+typedef struct {
+  stwo_qm31_point point;
+  uint32_t n_columns;
+  const uint32_t* h_column_indices;
+  const stwo_qm31* h_values;
+} stwo_sample_batch;
+/* QuotientOps::accumulate_quotients (pcs/quotients.rs:21-35; backend/simd/quotients.rs:31-100),
+ * on CanonicCoset(domain_log_size).circle_domain(). Columns hold 2^domain_log_size values. */
+stwo_status stwo_accumulate_quotients(uint32_t domain_log_size, const uint32_t* const* d_cols, uint32_t n_cols,
+                                      stwo_qm31 random_coeff, const stwo_sample_batch* h_batches,
+                                      uint32_t n_batches, uint32_t log_blowup_factor, uint32_t* const d_out[4],
+                                      void* stream);
+
+/* ------------------------------------------------------------------ AccumulationOps */
+/* AccumulationOps::accumulate (crates/prover/src/core/air/accumulation.rs:151-158). */
+stwo_status stwo_secure_accumulate(uint32_t* const d_acc[4], const uint32_t* const d_other[4], size_t n,
+                                   void* stream);
+/* AccumulationOps::generate_secure_powers (accumulation.rs:156-157). */
+stwo_status stwo_generate_secure_powers(stwo_qm31 felt, uint32_t n_powers, stwo_qm31* h_out, void* stream);
+
+/* ------------------------------------------------------------------ GrindOps */
+/* GrindOps<Blake2sChannel>::grind (crates/prover/src/core/proof_of_work.rs:3-7;
+ * backend/simd/grind.rs:21-63): the smallest nonce whose raw Blake2s compression of
+ * (digest, [nonce_lo, nonce_hi, 0...]) has >= pow_bits trailing zeros in word 0. */
+stwo_status stwo_grind_blake2s(const uint32_t h_digest[8], uint32_t pow_bits, uint64_t* h_nonce, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STWO_CUDA_H */

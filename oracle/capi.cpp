@@ -1,0 +1,167 @@
+// ORACLE — test infrastructure only. C entry points over the oracle restatement, loaded by the
+// tests (ctypes) as the checker for the CUDA backend and by bench.py as the CPU baseline.
+// Nothing in the product links this library.
+#include "ops.h"
+#include <cstring>
+
+using namespace oracle;
+
+static Coset mk_coset(const uint32_t c[3]) { return Coset::raw(c[0], c[1], c[2]); }
+static QM31 q_of(const uint32_t* v) { return QM31::from_u32(v[0], v[1], v[2], v[3]); }
+static void q_to(QM31 q, uint32_t* v) {
+  v[0] = q.a.a.v; v[1] = q.a.b.v; v[2] = q.b.a.v; v[3] = q.b.b.v;
+}
+static Column col_of(const uint32_t* p, size_t n) {
+  Column c(n);
+  for (size_t i = 0; i < n; i++) c[i] = M31(p[i]);
+  return c;
+}
+
+extern "C" {
+
+// Twiddle tree of `root` (size 2^root.log_size): x-coordinates and inverses.
+void oracle_twiddles(const uint32_t root[3], uint32_t* tw, uint32_t* itw) {
+  TwiddleTree t = precompute_twiddles(mk_coset(root));
+  for (size_t i = 0; i < t.twiddles.size(); i++) {
+    tw[i] = t.twiddles[i].v;
+    itw[i] = t.itwiddles[i].v;
+  }
+}
+
+// In-place interpolation of n = 2^(half.log_size+1) bit-reversed values on the domain with
+// half coset `half`, using the tree of `tree_root`.
+int oracle_interpolate(const uint32_t half[3], const uint32_t tree_root[3], uint32_t* values) {
+  try {
+    CircleDomain d{mk_coset(half)};
+    TwiddleTree t = precompute_twiddles(mk_coset(tree_root));
+    std::vector<M31> v = interpolate(d, col_of(values, d.size()), t);
+    for (size_t i = 0; i < v.size(); i++) values[i] = v[i].v;
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+int oracle_evaluate(const uint32_t half[3], const uint32_t tree_root[3], const uint32_t* coeffs,
+                    uint32_t coeff_log, uint32_t* out) {
+  try {
+    CircleDomain d{mk_coset(half)};
+    TwiddleTree t = precompute_twiddles(mk_coset(tree_root));
+    std::vector<M31> v = evaluate(d, col_of(coeffs, (size_t)1 << coeff_log), t);
+    for (size_t i = 0; i < v.size(); i++) out[i] = v[i].v;
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+void oracle_eval_at_point(const uint32_t* coeffs, uint32_t log_size, const uint32_t point[8], uint32_t out[4]) {
+  CirclePointQM31 p{q_of(point), q_of(point + 4)};
+  q_to(eval_at_point(col_of(coeffs, (size_t)1 << log_size), p), out);
+}
+
+// Merkle layer: prev (8 words per hash, 2^(log+1) hashes) or NULL.
+void oracle_commit_on_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols, uint32_t n_cols,
+                            uint32_t* out) {
+  size_t n = (size_t)1 << log_size;
+  std::vector<Column> cs;
+  for (uint32_t c = 0; c < n_cols; c++) cs.push_back(col_of(cols[c], n));
+  std::vector<const Column*> cp;
+  for (auto& c : cs) cp.push_back(&c);
+  std::vector<Hash32> pv;
+  if (prev) {
+    pv.resize(2 * n);
+    for (size_t i = 0; i < 2 * n; i++) pv[i] = Hash32::from_words(prev + 8 * i);
+  }
+  std::vector<Hash32> r = commit_on_layer(log_size, prev ? &pv : nullptr, cp);
+  for (size_t i = 0; i < n; i++) r[i].words(out + 8 * i);
+}
+
+void oracle_blake2s(const uint8_t* data, size_t len, uint8_t out[32]) {
+  Hash32 h = Blake2s::hash(data, len);
+  std::memcpy(out, h.b, 32);
+}
+
+void oracle_fold_line(const uint32_t domain[3], const uint32_t* const src[4], const uint32_t alpha[4],
+                      uint32_t* const out[4]) {
+  Coset d = mk_coset(domain);
+  size_t n = d.size();
+  SecureColumn e(n);
+  for (int k = 0; k < 4; k++) e.c[k] = col_of(src[k], n);
+  SecureColumn r = fold_line(e, d, q_of(alpha));
+  for (int k = 0; k < 4; k++)
+    for (size_t i = 0; i < n / 2; i++) out[k][i] = r.c[k][i].v;
+}
+
+void oracle_fold_circle_into_line(const uint32_t half[3], uint32_t* const dst[4], const uint32_t* const src[4],
+                                  const uint32_t alpha[4]) {
+  CircleDomain d{mk_coset(half)};
+  size_t n = d.size();
+  SecureColumn s(n), t(n / 2);
+  for (int k = 0; k < 4; k++) {
+    s.c[k] = col_of(src[k], n);
+    t.c[k] = col_of(dst[k], n / 2);
+  }
+  fold_circle_into_line(t, s, d, q_of(alpha));
+  for (int k = 0; k < 4; k++)
+    for (size_t i = 0; i < n / 2; i++) dst[k][i] = t.c[k][i].v;
+}
+
+void oracle_decompose(const uint32_t* const src[4], uint32_t log_size, uint32_t* const g[4], uint32_t lambda[4]) {
+  size_t n = (size_t)1 << log_size;
+  SecureColumn e(n);
+  for (int k = 0; k < 4; k++) e.c[k] = col_of(src[k], n);
+  auto r = decompose(e);
+  for (int k = 0; k < 4; k++)
+    for (size_t i = 0; i < n; i++) g[k][i] = r.first.c[k][i].v;
+  q_to(r.second, lambda);
+}
+
+// Quotients on CanonicCoset(log_n).circle_domain(). Batches: n_batches points (8 words each),
+// batch_offsets[n_batches+1] into entry_cols / entry_values (4 words each).
+void oracle_accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols,
+                                 const uint32_t random_coeff[4], uint32_t n_batches, const uint32_t* batch_points,
+                                 const uint32_t* batch_offsets, const uint32_t* entry_cols,
+                                 const uint32_t* entry_values, uint32_t log_blowup, uint32_t* const out[4]) {
+  size_t n = (size_t)1 << log_n;
+  std::vector<Column> cs;
+  for (uint32_t c = 0; c < n_cols; c++) cs.push_back(col_of(cols[c], n));
+  std::vector<const Column*> cp;
+  for (auto& c : cs) cp.push_back(&c);
+  std::vector<ColumnSampleBatch> batches;
+  for (uint32_t b = 0; b < n_batches; b++) {
+    ColumnSampleBatch sb;
+    sb.point = {q_of(batch_points + 8 * b), q_of(batch_points + 8 * b + 4)};
+    for (uint32_t e = batch_offsets[b]; e < batch_offsets[b + 1]; e++)
+      sb.columns_and_values.push_back({entry_cols[e], q_of(entry_values + 4 * e)});
+    batches.push_back(sb);
+  }
+  SecureColumn r = accumulate_quotients(canonic_domain(log_n), cp, q_of(random_coeff), batches, log_blowup);
+  for (int k = 0; k < 4; k++)
+    for (size_t i = 0; i < n; i++) out[k][i] = r.c[k][i].v;
+}
+
+void oracle_secure_powers(const uint32_t felt[4], uint32_t n, uint32_t* out) {
+  auto v = generate_secure_powers(q_of(felt), n);
+  for (uint32_t i = 0; i < n; i++) q_to(v[i], out + 4 * i);
+}
+
+uint64_t oracle_grind(const uint32_t digest[8], uint32_t pow_bits) { return grind(digest, pow_bits); }
+
+void oracle_raw_compress(const uint32_t h[8], const uint32_t m[16], uint32_t t0, uint32_t t1, uint32_t f0,
+                         uint32_t f1, uint32_t out[8]) {
+  auto r = b2s_compress(h, m, t0, t1, f0, f1);
+  for (int i = 0; i < 8; i++) out[i] = r[i];
+}
+
+void oracle_qm31_mul(const uint32_t a[4], const uint32_t b[4], uint32_t out[4]) { q_to(q_of(a) * q_of(b), out); }
+void oracle_qm31_inv(const uint32_t a[4], uint32_t out[4]) { q_to(inv(q_of(a)), out); }
+
+// Circle point i * M31_CIRCLE_GEN.
+void oracle_index_to_point(uint32_t idx, uint32_t out[2]) {
+  CirclePointM31 p = index_to_point(idx);
+  out[0] = p.x.v;
+  out[1] = p.y.v;
+}
+
+}  // extern "C"

@@ -1,0 +1,180 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper of oracle/_build/liboracle.so, the C++ restatement of the reference's CPU
+algorithms. Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg only;
+the product (stwo_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+P = (1 << 31) - 1
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            import sys
+
+            sys.path.insert(0, os.path.dirname(HERE))
+            from stwo_gb300.build import build_oracle
+
+            build_oracle()
+        _lib = C.CDLL(LIB)
+        _lib.oracle_grind.restype = C.c_uint64
+        _lib.oracle_interpolate.restype = C.c_int
+        _lib.oracle_evaluate.restype = C.c_int
+    return _lib
+
+
+def _u32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint32))
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _c3(c):
+    return (C.c_uint32 * 3)(*c)
+
+
+def _arr4(cols):
+    return (C.c_void_p * 4)(*[c.ctypes.data for c in cols])
+
+
+def _ptr_table(cols):
+    return (C.c_void_p * max(1, len(cols)))(*[c.ctypes.data for c in cols])
+
+
+def twiddles(root):
+    n = 1 << root[2]
+    tw = np.zeros(n, np.uint32)
+    itw = np.zeros(n, np.uint32)
+    lib().oracle_twiddles(_c3(root), _p(tw), _p(itw))
+    return tw, itw
+
+
+def interpolate(half, tree_root, values):
+    v = _u32(values).copy()
+    rc = lib().oracle_interpolate(_c3(half), _c3(tree_root), _p(v))
+    assert rc == 0, "oracle interpolate rejected its arguments"
+    return v
+
+
+def evaluate(half, tree_root, coeffs):
+    c = _u32(coeffs)
+    out = np.zeros(1 << (half[2] + 1), np.uint32)
+    rc = lib().oracle_evaluate(_c3(half), _c3(tree_root), _p(c), C.c_uint32(c.size.bit_length() - 1), _p(out))
+    assert rc == 0, "oracle evaluate rejected its arguments"
+    return out
+
+
+def eval_at_point(coeffs, point):
+    c = _u32(coeffs)
+    pt = _u32(list(point[0]) + list(point[1]))
+    out = np.zeros(4, np.uint32)
+    lib().oracle_eval_at_point(_p(c), C.c_uint32(c.size.bit_length() - 1), _p(pt), _p(out))
+    return tuple(int(x) for x in out)
+
+
+def commit_on_layer(log_size, prev, cols):
+    cols = [_u32(c) for c in cols]
+    out = np.zeros((1 << log_size) * 8, np.uint32)
+    prev_p = _p(_u32(prev).reshape(-1)) if prev is not None else None
+    keep = _u32(prev).reshape(-1) if prev is not None else None
+    if keep is not None:
+        prev_p = _p(keep)
+    lib().oracle_commit_on_layer(C.c_uint32(log_size), prev_p, _ptr_table(cols), C.c_uint32(len(cols)), _p(out))
+    return out.reshape(-1, 8)
+
+
+def blake2s(data: bytes) -> bytes:
+    out = (C.c_uint8 * 32)()
+    buf = (C.c_uint8 * max(1, len(data))).from_buffer_copy(data if data else b"\0")
+    lib().oracle_blake2s(buf, C.c_size_t(len(data)), out)
+    return bytes(out)
+
+
+def fold_line(domain, src4, alpha):
+    src = [_u32(c) for c in src4]
+    n = src[0].size
+    out = [np.zeros(n // 2, np.uint32) for _ in range(4)]
+    lib().oracle_fold_line(_c3(domain), _arr4(src), _p(_u32(alpha)), _arr4(out))
+    return out
+
+
+def fold_circle_into_line(half, dst4, src4, alpha):
+    dst = [_u32(c).copy() for c in dst4]
+    src = [_u32(c) for c in src4]
+    lib().oracle_fold_circle_into_line(_c3(half), _arr4(dst), _arr4(src), _p(_u32(alpha)))
+    return dst
+
+
+def decompose(src4):
+    src = [_u32(c) for c in src4]
+    g = [np.zeros_like(c) for c in src]
+    lam = np.zeros(4, np.uint32)
+    lib().oracle_decompose(_arr4(src), C.c_uint32(src[0].size.bit_length() - 1), _arr4(g), _p(lam))
+    return g, tuple(int(x) for x in lam)
+
+
+def accumulate_quotients(log_n, cols, random_coeff, batches, log_blowup):
+    cols = [_u32(c) for c in cols]
+    pts, offs, ecols, evals = [], [0], [], []
+    for (pt, cv) in batches:
+        pts += list(pt[0]) + list(pt[1])
+        for c, v in cv:
+            ecols.append(c)
+            evals += list(v)
+        offs.append(len(ecols))
+    pts, offs, ecols, evals = _u32(pts), _u32(offs), _u32(ecols + [0]), _u32(evals + [0, 0, 0, 0])
+    n = 1 << log_n
+    out = [np.zeros(n, np.uint32) for _ in range(4)]
+    lib().oracle_accumulate_quotients(
+        C.c_uint32(log_n), _ptr_table(cols), C.c_uint32(len(cols)), _p(_u32(random_coeff)),
+        C.c_uint32(len(batches)), _p(pts), _p(offs), _p(ecols), _p(evals), C.c_uint32(log_blowup), _arr4(out))
+    return out
+
+
+def secure_powers(felt, n):
+    out = np.zeros(4 * max(n, 1), np.uint32)
+    lib().oracle_secure_powers(_p(_u32(felt)), C.c_uint32(n), _p(out))
+    return [tuple(int(x) for x in out[4 * i:4 * i + 4]) for i in range(n)]
+
+
+def grind(digest, pow_bits):
+    return int(lib().oracle_grind(_p(_u32(digest)), C.c_uint32(pow_bits)))
+
+
+def raw_compress(h, m, t0=0, t1=0, f0=0, f1=0):
+    out = np.zeros(8, np.uint32)
+    lib().oracle_raw_compress(_p(_u32(h)), _p(_u32(m)), C.c_uint32(t0), C.c_uint32(t1), C.c_uint32(f0),
+                              C.c_uint32(f1), _p(out))
+    return [int(x) for x in out]
+
+
+def qm31_mul(a, b):
+    out = np.zeros(4, np.uint32)
+    lib().oracle_qm31_mul(_p(_u32(a)), _p(_u32(b)), _p(out))
+    return tuple(int(x) for x in out)
+
+
+def qm31_inv(a):
+    out = np.zeros(4, np.uint32)
+    lib().oracle_qm31_inv(_p(_u32(a)), _p(out))
+    return tuple(int(x) for x in out)
+
+
+def index_to_point(idx):
+    out = np.zeros(2, np.uint32)
+    lib().oracle_index_to_point(C.c_uint32(idx), _p(out))
+    return int(out[0]), int(out[1])

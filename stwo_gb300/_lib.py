@@ -1,0 +1,109 @@
+"""ctypes binding of include/stwo_cuda.h (libstwo_gb300.so, built in-tree for sm_103a).
+
+Loading fails loudly: there is no CPU fallback for any backend operation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libstwo_gb300.so")
+
+STWO_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "TIMEOUT", 4: "CUDA_ERROR", 5: "UNSUPPORTED"}
+
+
+class StwoError(RuntimeError):
+    def __init__(self, status: int, fn: str, detail: str):
+        super().__init__(f"{fn} failed: {STATUS_NAMES.get(status, status)}: {detail}")
+        self.status = status
+
+
+class Coset(C.Structure):
+    _fields_ = [("initial_index", C.c_uint32), ("step_size", C.c_uint32), ("log_size", C.c_uint32)]
+
+
+class QM31(C.Structure):
+    _fields_ = [("v", C.c_uint32 * 4)]
+
+
+class QM31Point(C.Structure):
+    _fields_ = [("x", QM31), ("y", QM31)]
+
+
+class SampleBatch(C.Structure):
+    _fields_ = [
+        ("point", QM31Point),
+        ("n_columns", C.c_uint32),
+        ("h_column_indices", C.POINTER(C.c_uint32)),
+        ("h_values", C.POINTER(QM31)),
+    ]
+
+
+P4 = C.c_void_p * 4
+VP = C.c_void_p
+U32 = C.c_uint32
+PVP = C.POINTER(C.c_void_p)
+
+# name -> (restype, argtypes); every symbol declared in include/stwo_cuda.h.
+SIGNATURES = {
+    "stwo_status_string": (C.c_char_p, [C.c_int32]),
+    "stwo_last_error": (C.c_char_p, []),
+    "stwo_device_init": (C.c_int32, [C.c_int]),
+    "stwo_sync": (C.c_int32, [VP]),
+    "stwo_kernel_launches": (C.c_uint64, []),
+    "stwo_buf_alloc": (C.c_int32, [PVP, C.c_size_t, VP]),
+    "stwo_buf_free": (C.c_int32, [VP, VP]),
+    "stwo_buf_upload": (C.c_int32, [VP, VP, C.c_size_t, VP]),
+    "stwo_buf_download": (C.c_int32, [VP, VP, C.c_size_t, VP]),
+    "stwo_buf_zero": (C.c_int32, [VP, C.c_size_t, VP]),
+    "stwo_read_words": (C.c_int32, [VP, C.POINTER(C.c_uint64), C.c_size_t, C.POINTER(C.c_uint32), VP]),
+    "stwo_twiddles_precompute": (C.c_int32, [Coset, PVP, VP]),
+    "stwo_twiddles_free": (C.c_int32, [VP]),
+    "stwo_twiddles_info": (C.c_int32, [VP, C.POINTER(Coset), PVP, PVP, C.POINTER(C.c_size_t)]),
+    "stwo_interpolate_columns": (C.c_int32, [VP, Coset, PVP, U32, VP]),
+    "stwo_evaluate_columns": (C.c_int32, [VP, Coset, PVP, U32, PVP, U32, VP]),
+    "stwo_extend": (C.c_int32, [VP, U32, VP, U32, VP]),
+    "stwo_eval_at_points": (C.c_int32, [PVP, C.POINTER(C.c_uint32), U32, C.POINTER(C.c_uint32),
+                                        C.POINTER(QM31Point), U32, C.POINTER(QM31), VP]),
+    "stwo_bit_reverse_column": (C.c_int32, [VP, U32, VP]),
+    "stwo_merkle_commit_layer": (C.c_int32, [U32, VP, PVP, U32, VP, VP]),
+    "stwo_fri_fold_line": (C.c_int32, [VP, Coset, PVP, QM31, PVP, VP]),
+    "stwo_fri_fold_circle_into_line": (C.c_int32, [VP, Coset, PVP, PVP, QM31, VP]),
+    "stwo_fri_decompose": (C.c_int32, [PVP, U32, PVP, C.POINTER(QM31), VP]),
+    "stwo_accumulate_quotients": (C.c_int32, [U32, PVP, U32, QM31, C.POINTER(SampleBatch), U32, U32, PVP, VP]),
+    "stwo_secure_accumulate": (C.c_int32, [PVP, PVP, C.c_size_t, VP]),
+    "stwo_generate_secure_powers": (C.c_int32, [QM31, U32, C.POINTER(QM31), VP]),
+    "stwo_grind_blake2s": (C.c_int32, [C.POINTER(C.c_uint32), U32, C.POINTER(C.c_uint64), VP]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Loads the backend library (raises if it is missing: no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+        )
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int, fn: str) -> None:
+    if status != STWO_OK:
+        detail = load().stwo_last_error().decode(errors="replace")
+        raise StwoError(status, fn, detail)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(load(), name)(*args), name)

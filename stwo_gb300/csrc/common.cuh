@@ -1,0 +1,150 @@
+// Shared runtime for the sm_103a backend: status codes, error capture, the per-device
+// context (twiddle-tree cache, stream-ordered scratch) and launch helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <mutex>
+#include <map>
+#include <vector>
+#include <tuple>
+#include <algorithm>
+#include "../../include/stwo_cuda.h"
+#include "field.cuh"
+
+namespace stwo {
+
+// Last error detail, per host thread (the status code is the contract; this is for humans).
+void set_error(const char* fmt, ...);
+
+#define STWO_CHECK_CUDA(expr)                                                        \
+  do {                                                                               \
+    cudaError_t _e = (expr);                                                         \
+    if (_e != cudaSuccess) {                                                         \
+      ::stwo::set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(_e)); \
+      return (_e == cudaErrorMemoryAllocation) ? STWO_ERR_OOM : STWO_ERR_CUDA;       \
+    }                                                                                \
+  } while (0)
+
+#define STWO_REQUIRE(cond, ...)                 \
+  do {                                          \
+    if (!(cond)) {                              \
+      ::stwo::set_error(__VA_ARGS__);           \
+      return STWO_ERR_INVALID_ARG;              \
+    }                                           \
+  } while (0)
+
+#define STWO_LAUNCH_CHECK()                                                          \
+  do {                                                                               \
+    cudaError_t _e = cudaGetLastError();                                             \
+    if (_e != cudaSuccess) {                                                         \
+      ::stwo::set_error("%s:%d launch: %s", __FILE__, __LINE__, cudaGetErrorString(_e)); \
+      return STWO_ERR_CUDA;                                                          \
+    }                                                                                \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Index arithmetic on the circle group (indices mod 2^31), host side.
+constexpr uint32_t IDX_MASK = (1u << 31) - 1;
+inline uint32_t idx_reduce(uint64_t i) { return (uint32_t)(i & IDX_MASK); }
+
+inline stwo_coset coset_double(stwo_coset c) {
+  return {idx_reduce((uint64_t)c.initial_index * 2), idx_reduce((uint64_t)c.step_size * 2),
+          c.log_size ? c.log_size - 1 : 0};
+}
+inline bool coset_eq(stwo_coset a, stwo_coset b) {
+  return a.initial_index == b.initial_index && a.step_size == b.step_size && a.log_size == b.log_size;
+}
+inline bool coset_is_doubling_of(stwo_coset small, stwo_coset big) {
+  if (small.log_size > big.log_size) return false;
+  stwo_coset c = big;
+  for (uint32_t i = small.log_size; i < big.log_size; i++) c = coset_double(c);
+  return coset_eq(c, small);
+}
+inline stwo_coset coset_new(uint32_t initial_index, uint32_t log_size) {
+  return {idx_reduce(initial_index), idx_reduce(1ull << (31 - log_size)), log_size};
+}
+// CanonicCoset(log).half_coset() = Coset::half_odds(log - 1)
+inline stwo_coset canonic_half_coset(uint32_t log) {
+  return coset_new(1u << (31 - (log - 1 + 2)), log - 1);
+}
+
+// Host-side M31 helpers for O(1) setup scalars (never per-element work).
+inline uint32_t h_add(uint32_t a, uint32_t b) { uint32_t s = a + b; return s >= P ? s - P : s; }
+inline uint32_t h_sub(uint32_t a, uint32_t b) { return a >= b ? a - b : a + P - b; }
+inline uint32_t h_mul(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) % P); }
+inline uint32_t h_pow(uint32_t b, uint64_t e) { uint32_t r = 1; while (e) { if (e & 1) r = h_mul(r, b); b = h_mul(b, b); e >>= 1; } return r; }
+inline uint32_t h_inv(uint32_t a) { return h_pow(a, P - 2); }
+struct hpoint { uint32_t x, y; };
+inline hpoint h_padd(hpoint p, hpoint q) {
+  return {h_sub(h_mul(p.x, q.x), h_mul(p.y, q.y)), h_add(h_mul(p.x, q.y), h_mul(p.y, q.x))};
+}
+hpoint h_index_to_point(uint32_t idx);
+
+// Host QM31 for O(#columns) setup constants (line coefficients, powers, mappings).
+struct hq { uint32_t v[4]; };
+inline hq hq_make(uint32_t a, uint32_t b, uint32_t c, uint32_t d) { return hq{{a, b, c, d}}; }
+inline hq hq_from(const stwo_qm31& x) { return hq{{x.v[0], x.v[1], x.v[2], x.v[3]}}; }
+inline hq hq_add(hq x, hq y) { hq r; for (int i = 0; i < 4; i++) r.v[i] = h_add(x.v[i], y.v[i]); return r; }
+inline hq hq_sub(hq x, hq y) { hq r; for (int i = 0; i < 4; i++) r.v[i] = h_sub(x.v[i], y.v[i]); return r; }
+inline void h_cmul(uint32_t x0, uint32_t x1, uint32_t y0, uint32_t y1, uint32_t* r0, uint32_t* r1) {
+  uint32_t a = h_sub(h_mul(x0, y0), h_mul(x1, y1));
+  uint32_t b = h_add(h_mul(x0, y1), h_mul(x1, y0));
+  *r0 = a;
+  *r1 = b;
+}
+inline hq hq_mul(hq x, hq y) {
+  uint32_t ac0, ac1, bd0, bd1, ad0, ad1, bc0, bc1;
+  h_cmul(x.v[0], x.v[1], y.v[0], y.v[1], &ac0, &ac1);
+  h_cmul(x.v[2], x.v[3], y.v[2], y.v[3], &bd0, &bd1);
+  h_cmul(x.v[0], x.v[1], y.v[2], y.v[3], &ad0, &ad1);
+  h_cmul(x.v[2], x.v[3], y.v[0], y.v[1], &bc0, &bc1);
+  uint32_t rb0 = h_sub(h_add(bd0, bd0), bd1), rb1 = h_add(bd0, h_add(bd1, bd1));  // (2+i) bd
+  return hq{{h_add(ac0, rb0), h_add(ac1, rb1), h_add(ad0, bc0), h_add(ad1, bc1)}};
+}
+inline hq hq_conj(hq x) { return hq{{x.v[0], x.v[1], h_sub(0, x.v[2]), h_sub(0, x.v[3])}}; }
+inline hq hq_pow(hq b, uint64_t e) { hq r = hq_make(1, 0, 0, 0); while (e) { if (e & 1) r = hq_mul(r, b); b = hq_mul(b, b); e >>= 1; } return r; }
+
+// A twiddle tree resident in HBM: x-coordinates of every coset in the doubling tower of
+// `root`, bit-reversed per level, padded with one 1 (cpu/circle.rs:171-188), and inverses.
+struct TwiddleTree {
+  stwo_coset root;
+  uint32_t* d_tw = nullptr;
+  uint32_t* d_itw = nullptr;
+  size_t size = 0;  // 2^root.log_size (>= 1)
+};
+
+// Per-device state: cached twiddle trees (keyed by root coset) and the device id.
+struct DeviceContext {
+  int device = 0;
+  std::mutex mu;
+  std::map<std::tuple<uint32_t, uint32_t, uint32_t>, TwiddleTree*> trees;
+};
+DeviceContext& ctx();
+
+// Builds (or returns the cached) tree for `root` on `stream`.
+int32_t get_tree(stwo_coset root, cudaStream_t stream, TwiddleTree** out);
+int32_t build_tree(stwo_coset root, cudaStream_t stream, TwiddleTree* t);
+// The tree behind a caller-owned handle.
+const TwiddleTree* tree_of(stwo_twiddle_tree t);
+
+// Stream-ordered scratch allocation (cudaMallocAsync on the device's default pool).
+int32_t scratch_alloc(void** p, size_t bytes, cudaStream_t s);
+void scratch_free(void* p, cudaStream_t s);
+
+// Kernel-parameter tables of column pointers. Kernel parameters may be up to 32 KB on
+// sm_70+, so batches of this many columns travel in the launch itself and need no copy.
+constexpr int MAX_PARAM_COLS = 1024;
+struct ColPtrs { uint32_t* p[MAX_PARAM_COLS]; };
+struct ConstColPtrs { const uint32_t* p[MAX_PARAM_COLS]; };
+
+// Count of kernel launches issued by this library (diagnostic, read by benchmarks).
+void note_launch();
+
+// Number of SMs of the current device (152 on GB300).
+int sm_count();
+
+}  // namespace stwo

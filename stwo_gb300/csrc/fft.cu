@@ -1,0 +1,251 @@
+// Circle FFT / IFFT over M31 (PolyOps::interpolate_columns / evaluate_polynomials).
+//
+// Transform: the reference CPU backend's layer order (crates/prover/src/core/backend/cpu/
+// circle.rs:18-135): evaluate runs line layers L-1..1 with the twiddle-tree slices of
+// poly/utils.rs:62-77 and then the circle layer 0 whose twiddles are derived from the first
+// line layer as [y, -y, -x, x] (cpu/circle.rs:209-229); interpolate runs them in reverse with
+// inverse twiddles and scales by 1/2^L. Any correct schedule gives identical words because
+// every operation is exact in the field.
+//
+// GB300 schedule: a column of 2^L words is processed in passes. Each pass moves tiles of
+// 2^T words (T <= 13) HBM -> shared memory -> HBM; inside a tile, each thread holds 2^4
+// words in registers and applies 4 butterfly layers per round, exchanging through shared
+// memory between rounds. A contiguous pass covers layers [0, 13); strided passes cover
+// higher layers with the 2^c lowest address bits kept contiguous for coalesced access.
+// Evaluation on a larger domain (blowup) fuses the zero-extension into the first pass: each
+// of the 2^(L-F) sub-domain chunks reads the 2^F coefficients and applies the big domain's
+// twiddles, exactly as the reference SIMD backend's sub-domain evaluation
+// (backend/simd/circle.rs:230-294).
+#include "common.cuh"
+
+namespace stwo {
+
+constexpr uint32_t FFT_TMAX = 13;
+constexpr uint32_t FFT_R = 4;
+constexpr uint32_t FFT_MAX_THREADS = 512;
+
+struct FftPass {
+  uint32_t L;        // log size of the destination column (domain log size)
+  uint32_t F;        // number of FFT layers = log size of the source column
+  uint32_t lo, nl;   // this pass covers layers [lo, lo + nl)
+  uint32_t c;        // number of low address bits kept contiguous in a tile
+  uint32_t T;        // tile log size = c + nl
+  const uint32_t* tw;  // twiddles (forward) or inverse twiddles
+  uint32_t tw_size;    // tree size 2^root.log_size
+  uint32_t small_y;    // circle-layer twiddle when L <= 2 (inverted for interpolate)
+  uint32_t scale;      // output multiplier (1 = none)
+  uint32_t read_src;   // read from src (masked to 2^F) instead of dst
+};
+
+__device__ __forceinline__ uint32_t pad_idx(uint32_t e) { return e + (e >> 5); }
+
+__device__ __forceinline__ uint32_t fft_twiddle(const FftPass& p, uint32_t layer, uint32_t idx0) {
+  if (layer >= 1) {
+    uint32_t off = p.tw_size - (1u << (p.L - layer));
+    return __ldg(&p.tw[off + (idx0 >> (layer + 1))]);
+  }
+  uint32_t h = idx0 >> 1;
+  if (p.L <= 2) return (h & 1) ? m31_neg(p.small_y) : p.small_y;
+  uint32_t off = p.tw_size - (1u << (p.L - 1));
+  uint32_t t = __ldg(&p.tw[off + ((h >> 1) ^ 1)]);
+  return ((h ^ (h >> 1)) & 1) ? m31_neg(t) : t;
+}
+
+template <bool INV, int RB>
+__device__ __forceinline__ void fft_round(const FftPass& p, uint32_t* sm, uint32_t a, uint32_t fixed) {
+  const uint32_t n_tile = 1u << p.T;
+  const uint32_t G = n_tile >> RB;
+  const uint32_t cmask = (1u << p.c) - 1;
+  for (uint32_t grp = threadIdx.x; grp < G; grp += blockDim.x) {
+    uint32_t base = (grp & ((1u << a) - 1)) | ((grp >> a) << (a + RB));
+    uint32_t v[1 << RB];
+#pragma unroll
+    for (int k = 0; k < (1 << RB); k++) v[k] = sm[pad_idx(base | ((uint32_t)k << a))];
+#pragma unroll
+    for (int jj = 0; jj < RB; jj++) {
+      const int j = INV ? jj : (RB - 1 - jj);
+      const uint32_t layer = p.lo + (a + j - p.c);
+#pragma unroll
+      for (int k = 0; k < (1 << RB); k++) {
+        if (k & (1 << j)) continue;
+        uint32_t e0 = base | ((uint32_t)k << a);
+        uint32_t g0 = (e0 & cmask) | ((e0 >> p.c) << p.lo) | fixed;
+        uint32_t t = fft_twiddle(p, layer, g0);
+        if (INV) ibfly(v[k], v[k | (1 << j)], t);
+        else bfly(v[k], v[k | (1 << j)], t);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < (1 << RB); k++) sm[pad_idx(base | ((uint32_t)k << a))] = v[k];
+  }
+  __syncthreads();
+}
+
+template <bool INV>
+__device__ __forceinline__ void fft_round_dispatch(const FftPass& p, uint32_t* sm, uint32_t a, uint32_t rb,
+                                                   uint32_t fixed) {
+  switch (rb) {
+    case 4: fft_round<INV, 4>(p, sm, a, fixed); break;
+    case 3: fft_round<INV, 3>(p, sm, a, fixed); break;
+    case 2: fft_round<INV, 2>(p, sm, a, fixed); break;
+    default: fft_round<INV, 1>(p, sm, a, fixed); break;
+  }
+}
+
+template <bool INV>
+__global__ void __launch_bounds__(FFT_MAX_THREADS) k_fft_pass(FftPass p, ConstColPtrs src, ColPtrs dst) {
+  extern __shared__ uint32_t sm[];
+  const uint32_t col = blockIdx.y;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t n_tile = 1u << p.T;
+  const uint32_t mid_bits = p.lo - p.c;
+  const uint32_t fixed = ((tile & ((1u << mid_bits) - 1)) << p.c) | ((tile >> mid_bits) << (p.lo + p.nl));
+  const uint32_t cmask = (1u << p.c) - 1;
+  const uint32_t* s = p.read_src ? src.p[col] : dst.p[col];
+  const uint32_t smask = p.read_src ? ((1u << p.F) - 1) : 0xffffffffu;
+  uint32_t* d = dst.p[col];
+
+  for (uint32_t e = threadIdx.x; e < n_tile; e += blockDim.x) {
+    uint32_t g = (e & cmask) | ((e >> p.c) << p.lo) | fixed;
+    sm[pad_idx(e)] = s[g & smask];
+  }
+  __syncthreads();
+
+  if (!INV) {
+    uint32_t top = p.c + p.nl;
+    while (top > p.c) {
+      uint32_t rb = min(FFT_R, top - p.c);
+      uint32_t a = top - rb;
+      fft_round_dispatch<INV>(p, sm, a, rb, fixed);
+      top = a;
+    }
+  } else {
+    uint32_t bot = p.c;
+    while (bot < p.c + p.nl) {
+      uint32_t rb = min(FFT_R, p.c + p.nl - bot);
+      fft_round_dispatch<INV>(p, sm, bot, rb, fixed);
+      bot += rb;
+    }
+  }
+
+  for (uint32_t e = threadIdx.x; e < n_tile; e += blockDim.x) {
+    uint32_t g = (e & cmask) | ((e >> p.c) << p.lo) | fixed;
+    uint32_t v = sm[pad_idx(e)];
+    if (p.scale != 1u) v = m31_mul(v, p.scale);
+    d[g] = v;
+  }
+}
+
+struct PassPlan {
+  uint32_t lo, nl, c;
+};
+
+// Contiguous pass over [0, min(F, 13)), strided passes (<= 9 layers, >= 16 contiguous
+// words per row) above it.
+static std::vector<PassPlan> plan_passes(uint32_t F) {
+  std::vector<PassPlan> v;
+  if (F == 0) return v;
+  uint32_t low = F < FFT_TMAX ? F : FFT_TMAX;
+  v.push_back({0, low, 0});
+  uint32_t lo = low;
+  while (lo < F) {
+    uint32_t rem = F - lo;
+    uint32_t n_passes = (rem + 8) / 9;
+    uint32_t nl = (rem + n_passes - 1) / n_passes;
+    uint32_t c = FFT_TMAX - nl;
+    if (c > lo) c = lo;
+    v.push_back({lo, nl, c});
+    lo += nl;
+  }
+  return v;
+}
+
+// Runs the layers [0, F) of a 2^L-point circle FFT (F == L for interpolation).
+static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, const uint32_t* const* src,
+                       uint32_t F, uint32_t* const* dst, uint32_t n_cols, cudaStream_t s) {
+  const uint32_t L = half.log_size + 1;
+  STWO_REQUIRE(tree, "null twiddle tree");
+  STWO_REQUIRE(L <= 30, "domain log size %u > 30", L);
+  STWO_REQUIRE(F <= L, "Can only evaluate on larger domains");
+  STWO_REQUIRE(coset_is_doubling_of(half, tree->root), "domain half coset is not a doubling of the twiddle root");
+  if (n_cols == 0) return STWO_OK;
+
+  FftPass base{};
+  base.L = L;
+  base.F = F;
+  base.tw = inverse ? tree->d_itw : tree->d_tw;
+  base.tw_size = (uint32_t)tree->size;
+  base.scale = 1u;
+  base.small_y = 0;
+  if (L <= 2) {
+    uint32_t y = h_index_to_point(half.initial_index).y;
+    base.small_y = inverse ? h_inv(y) : y;
+  }
+
+  std::vector<PassPlan> plan = plan_passes(F);
+  if (!inverse) std::reverse(plan.begin(), plan.end());
+  if (F == 0) {
+    // A single coefficient: the constant polynomial, evaluated everywhere to that value.
+    STWO_REQUIRE(!inverse, "empty interpolation");
+    plan.push_back({0, 0, 0});
+  }
+
+  for (uint32_t c0 = 0; c0 < n_cols; c0 += MAX_PARAM_COLS) {
+    uint32_t nc = std::min<uint32_t>(MAX_PARAM_COLS, n_cols - c0);
+    ConstColPtrs sp;
+    ColPtrs dp;
+    for (uint32_t i = 0; i < nc; i++) {
+      sp.p[i] = src ? src[c0 + i] : dst[c0 + i];
+      dp.p[i] = dst[c0 + i];
+    }
+    for (size_t pi = 0; pi < plan.size(); pi++) {
+      FftPass p = base;
+      p.lo = plan[pi].lo;
+      p.nl = plan[pi].nl;
+      p.c = plan[pi].c;
+      p.T = p.c + p.nl;
+      p.read_src = (pi == 0 && src) ? 1u : 0u;
+      if (inverse && pi + 1 == plan.size()) p.scale = h_inv((uint32_t)((1ull << L) % P));
+      uint32_t tiles_log = L - p.T;
+      STWO_REQUIRE(tiles_log < 31, "too many tiles");
+      dim3 grid(1u << tiles_log, nc);
+      uint32_t groups = (1u << p.T) >> std::min(FFT_R, p.T);
+      uint32_t threads = std::max<uint32_t>(32, std::min<uint32_t>(FFT_MAX_THREADS, groups));
+      size_t smem = ((size_t)(1u << p.T) + ((1u << p.T) >> 5) + 1) * 4;
+      if (inverse) k_fft_pass<true><<<grid, threads, smem, s>>>(p, sp, dp);
+      else k_fft_pass<false><<<grid, threads, smem, s>>>(p, sp, dp);
+      note_launch();
+      STWO_LAUNCH_CHECK();
+    }
+  }
+  return STWO_OK;
+}
+
+int32_t fft_interpolate(const TwiddleTree* tree, stwo_coset half, uint32_t* const* cols, uint32_t n, cudaStream_t s) {
+  return run_fft(tree, half, true, nullptr, half.log_size + 1, cols, n, s);
+}
+int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* const* coeffs, uint32_t coeff_log,
+                     uint32_t* const* out, uint32_t n, cudaStream_t s) {
+  return run_fft(tree, half, false, coeffs, coeff_log, out, n, s);
+}
+
+}  // namespace stwo
+
+using namespace stwo;
+
+extern "C" {
+
+stwo_status stwo_interpolate_columns(stwo_twiddle_tree tree, stwo_coset domain_half_coset, uint32_t* const* d_cols,
+                                     uint32_t n_cols, void* stream) {
+  STWO_REQUIRE(n_cols == 0 || d_cols, "null column table");
+  return fft_interpolate(tree_of(tree), domain_half_coset, d_cols, n_cols, as_stream(stream));
+}
+
+stwo_status stwo_evaluate_columns(stwo_twiddle_tree tree, stwo_coset domain_half_coset,
+                                  const uint32_t* const* d_coeffs, uint32_t coeff_log_size, uint32_t* const* d_out,
+                                  uint32_t n_cols, void* stream) {
+  STWO_REQUIRE(n_cols == 0 || (d_coeffs && d_out), "null column table");
+  return fft_evaluate(tree_of(tree), domain_half_coset, d_coeffs, coeff_log_size, d_out, n_cols, as_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,237 @@
+// FriOps: fold_line, fold_circle_into_line, decompose.
+//
+// fold_line (crates/prover/src/core/fri.rs:1132-1157): out[i] = f0 + alpha * f1 with
+// (f0, f1) = ibutterfly(f(x), f(-x), 1/x), x = domain.at(bitrev(2i)).x. 1/x is entry i of the
+// line domain's level of the inverse twiddle tree (backend/simd/fri.rs:24-59).
+// fold_circle_into_line (fri.rs:1162-1189): dst[i] = dst[i] * alpha^2 + (f0 + alpha * f1) with
+// (f0, f1) = ibutterfly(f(p), f(-p), 1/p.y); 1/p.y is the circle-layer twiddle derived from the
+// half coset's level as [y, -y, -x, x] (backend/simd/fri.rs:61-109).
+// decompose (backend/simd/fri.rs:111-161): lambda = (sum(first half) - sum(second half)) / N,
+// g = f -+ lambda.
+// Each kernel is one streaming pass over four coordinate columns: HBM-bound.
+#include "common.cuh"
+
+namespace stwo {
+
+struct Secure4 { const uint32_t* p[4]; };
+struct Secure4M { uint32_t* p[4]; };
+
+__device__ __forceinline__ qm31 load_q(const Secure4& s, size_t i) {
+  return qm31_from_u32(__ldg(s.p[0] + i), __ldg(s.p[1] + i), __ldg(s.p[2] + i), __ldg(s.p[3] + i));
+}
+__device__ __forceinline__ void store_q(const Secure4M& s, size_t i, qm31 v) {
+  s.p[0][i] = v.a.a;
+  s.p[1][i] = v.a.b;
+  s.p[2][i] = v.b.a;
+  s.p[3][i] = v.b.b;
+}
+
+__device__ __forceinline__ void ibfly_q(qm31& v0, qm31& v1, uint32_t it) {
+  qm31 tmp = v0;
+  v0 = qm31_add(tmp, v1);
+  v1 = qm31_mul_m31(qm31_sub(tmp, v1), it);
+}
+
+// Two consecutive values of each coordinate are read as one 8-byte load.
+__device__ __forceinline__ void load_pair(const Secure4& s, size_t i, qm31& a, qm31& b) {
+  uint2 w0 = __ldg(reinterpret_cast<const uint2*>(s.p[0]) + i);
+  uint2 w1 = __ldg(reinterpret_cast<const uint2*>(s.p[1]) + i);
+  uint2 w2 = __ldg(reinterpret_cast<const uint2*>(s.p[2]) + i);
+  uint2 w3 = __ldg(reinterpret_cast<const uint2*>(s.p[3]) + i);
+  a = qm31_from_u32(w0.x, w1.x, w2.x, w3.x);
+  b = qm31_from_u32(w0.y, w1.y, w2.y, w3.y);
+}
+
+__global__ void k_fold_line(Secure4 src, Secure4M dst, uint32_t n_out, const uint32_t* __restrict__ itw_level,
+                            qm31 alpha) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
+    qm31 f0, f1;
+    load_pair(src, i, f0, f1);
+    ibfly_q(f0, f1, __ldg(itw_level + i));
+    store_q(dst, i, qm31_add(f0, qm31_mul(alpha, f1)));
+  }
+}
+
+// `itw_level` = inverse twiddles of the half coset's level (2^(n-2) entries), used when
+// n >= 3. For n <= 2 the y-coordinates come from the domain points directly.
+__global__ void k_fold_circle(Secure4 src, Secure4M dst, uint32_t n_out, const uint32_t* __restrict__ itw_level,
+                              uint32_t log_src, uint32_t half_init, uint32_t half_step, qm31 alpha, qm31 alpha_sq) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
+    uint32_t yinv;
+    if (log_src >= 3) {
+      uint32_t t = __ldg(itw_level + ((i >> 1) ^ 1));
+      yinv = ((i ^ (i >> 1)) & 1) ? m31_neg(t) : t;
+    } else {
+      // domain.at(bitrev(2i)): the half coset point bitrev(2i) when < half, else its conjugate.
+      uint32_t k = brev(2 * i, log_src);
+      uint32_t half = 1u << (log_src - 1);
+      uint32_t idx = k < half ? half_init + half_step * k : (0u - (half_init + half_step * (k - half)));
+      yinv = m31_inv(index_to_point(idx & 0x7fffffffu).y);
+    }
+    qm31 f0, f1;
+    load_pair(src, i, f0, f1);
+    ibfly_q(f0, f1, yinv);
+    qm31 fp = qm31_add(qm31_mul(alpha, f1), f0);
+    qm31 d = qm31_from_u32(dst.p[0][i], dst.p[1][i], dst.p[2][i], dst.p[3][i]);
+    store_q(dst, i, qm31_add(qm31_mul(d, alpha_sq), fp));
+  }
+}
+
+// Per-block partial sums of +f (first half) and -f (second half), four coordinates, reduced
+// into 64-bit accumulators (each partial is < P, so 2^33 of them cannot overflow).
+__global__ void k_decompose_sum(Secure4 src, uint32_t n, unsigned long long* acc) {
+  __shared__ uint32_t part[4][32];
+  uint32_t s[4] = {0, 0, 0, 0};
+  uint32_t half = n >> 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      uint32_t v = __ldg(src.p[k] + i);
+      s[k] = i < half ? m31_add(s[k], v) : m31_sub(s[k], v);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    uint32_t v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v = m31_add(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) part[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    uint32_t v = 0;
+    for (uint32_t w = 0; w < blockDim.x / 32; w++) v = m31_add(v, part[threadIdx.x][w]);
+    atomicAdd(acc + threadIdx.x, (unsigned long long)v);
+  }
+}
+
+__device__ __forceinline__ uint32_t m31_reduce64(unsigned long long x) {
+  x = (x & P) + (x >> 31);
+  x = (x & P) + (x >> 31);
+  uint32_t r = (uint32_t)x;
+  return r >= P ? r - P : r;
+}
+
+__global__ void k_decompose_apply(Secure4 src, Secure4M dst, uint32_t n, const unsigned long long* acc,
+                                  uint32_t inv_n, uint32_t* lambda_out) {
+  qm31 lambda = qm31_mul_m31(qm31_from_u32(m31_reduce64(acc[0]), m31_reduce64(acc[1]), m31_reduce64(acc[2]),
+                                           m31_reduce64(acc[3])),
+                             inv_n);
+  uint32_t half = n >> 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    lambda_out[0] = lambda.a.a;
+    lambda_out[1] = lambda.a.b;
+    lambda_out[2] = lambda.b.a;
+    lambda_out[3] = lambda.b.b;
+  }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    qm31 v = load_q(src, i);
+    store_q(dst, i, i < half ? qm31_sub(v, lambda) : qm31_add(v, lambda));
+  }
+}
+
+static qm31 to_q(stwo_qm31 a) { return {{a.v[0], a.v[1]}, {a.v[2], a.v[3]}}; }
+static uint32_t grid_for(size_t n, uint32_t threads) {
+  size_t b = (n + threads - 1) / threads;
+  size_t cap = (size_t)sm_count() * 16;
+  return (uint32_t)std::max<size_t>(1, std::min(b, cap));
+}
+
+// Offset of the level of coset `c` in a tree whose root it is a doubling of.
+static bool level_offset(const TwiddleTree* t, stwo_coset c, size_t* off) {
+  if (!t || !coset_is_doubling_of(c, t->root)) return false;
+  *off = t->size - ((size_t)1 << c.log_size);
+  return true;
+}
+
+int32_t fri_fold_line(const TwiddleTree* tree, stwo_coset line_domain, const uint32_t* const src[4],
+                      qm31 alpha, uint32_t* const out[4], cudaStream_t s) {
+  STWO_REQUIRE(line_domain.log_size >= 1, "Evaluation too small");
+  size_t off;
+  STWO_REQUIRE(level_offset(tree, line_domain, &off), "line domain is not a doubling of the twiddle root");
+  uint32_t n_out = 1u << (line_domain.log_size - 1);
+  Secure4 sp{{src[0], src[1], src[2], src[3]}};
+  Secure4M dp{{out[0], out[1], out[2], out[3]}};
+  k_fold_line<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, tree->d_itw + off, alpha); note_launch();
+  STWO_LAUNCH_CHECK();
+  return STWO_OK;
+}
+
+int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* const dst[4],
+                        const uint32_t* const src[4], qm31 alpha, cudaStream_t s) {
+  uint32_t log_src = half.log_size + 1;
+  size_t off = 0;
+  const uint32_t* lvl = nullptr;
+  if (log_src >= 3) {
+    STWO_REQUIRE(level_offset(tree, half, &off), "domain is not a doubling of the twiddle root");
+    lvl = tree->d_itw + off;
+  }
+  uint32_t n_out = 1u << (log_src - 1);
+  Secure4 sp{{src[0], src[1], src[2], src[3]}};
+  Secure4M dp{{dst[0], dst[1], dst[2], dst[3]}};
+  // alpha^2 computed on the device side of the arithmetic is identical; do it on the host once.
+  uint32_t a[4] = {alpha.a.a, alpha.a.b, alpha.b.a, alpha.b.b};
+  // (a + bu)^2 = a^2 + (2+i) b^2 + 2ab u over CM31.
+  auto cmul = [](uint32_t x0, uint32_t x1, uint32_t y0, uint32_t y1, uint32_t* r0, uint32_t* r1) {
+    *r0 = h_sub(h_mul(x0, y0), h_mul(x1, y1));
+    *r1 = h_add(h_mul(x0, y1), h_mul(x1, y0));
+  };
+  uint32_t aa0, aa1, bb0, bb1, ab0, ab1;
+  cmul(a[0], a[1], a[0], a[1], &aa0, &aa1);
+  cmul(a[2], a[3], a[2], a[3], &bb0, &bb1);
+  cmul(a[0], a[1], a[2], a[3], &ab0, &ab1);
+  uint32_t rb0 = h_sub(h_add(bb0, bb0), bb1), rb1 = h_add(bb0, h_add(bb1, bb1));
+  qm31 a2 = {{h_add(aa0, rb0), h_add(aa1, rb1)}, {h_add(ab0, ab0), h_add(ab1, ab1)}};
+  k_fold_circle<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, lvl, log_src, half.initial_index,
+                                                     half.step_size, alpha, a2); note_launch();
+  STWO_LAUNCH_CHECK();
+  return STWO_OK;
+}
+
+int32_t fri_decompose(const uint32_t* const src[4], uint32_t log_size, uint32_t* const g[4], stwo_qm31* lambda,
+                      cudaStream_t s) {
+  STWO_REQUIRE(log_size >= 1 && log_size <= 30, "bad log size %u", log_size);
+  uint32_t n = 1u << log_size;
+  unsigned long long* acc = nullptr;
+  int32_t st = scratch_alloc((void**)&acc, 4 * sizeof(unsigned long long) + 16, s);
+  if (st) return st;
+  uint32_t* lam = reinterpret_cast<uint32_t*>(acc + 4);
+  cudaMemsetAsync(acc, 0, 4 * sizeof(unsigned long long), s);
+  Secure4 sp{{src[0], src[1], src[2], src[3]}};
+  Secure4M dp{{g[0], g[1], g[2], g[3]}};
+  k_decompose_sum<<<grid_for(n, 256), 256, 0, s>>>(sp, n, acc); note_launch();
+  k_decompose_apply<<<grid_for(n, 256), 256, 0, s>>>(sp, dp, n, acc, h_inv(n % P), lam); note_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(lambda->v, lam, 16, cudaMemcpyDeviceToHost, s);
+  scratch_free(acc, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_error("decompose: %s", cudaGetErrorString(e));
+    return STWO_ERR_CUDA;
+  }
+  return STWO_OK;
+}
+
+}  // namespace stwo
+
+using namespace stwo;
+
+extern "C" {
+
+stwo_status stwo_fri_fold_line(stwo_twiddle_tree tree, stwo_coset line_domain, const uint32_t* const d_eval[4],
+                               stwo_qm31 alpha, uint32_t* const d_out[4], void* stream) {
+  return fri_fold_line(tree_of(tree), line_domain, d_eval, to_q(alpha), d_out, as_stream(stream));
+}
+
+stwo_status stwo_fri_fold_circle_into_line(stwo_twiddle_tree tree, stwo_coset src_half_coset,
+                                           uint32_t* const d_dst[4], const uint32_t* const d_src[4],
+                                           stwo_qm31 alpha, void* stream) {
+  return fri_fold_circle(tree_of(tree), src_half_coset, d_dst, d_src, to_q(alpha), as_stream(stream));
+}
+
+stwo_status stwo_fri_decompose(const uint32_t* const d_eval[4], uint32_t log_size, uint32_t* const d_g[4],
+                               stwo_qm31* h_lambda, void* stream) {
+  STWO_REQUIRE(h_lambda, "null lambda");
+  return fri_decompose(d_eval, log_size, d_g, h_lambda, as_stream(stream));
+}
+
+}  // extern "C"

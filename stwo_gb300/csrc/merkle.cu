@@ -1,0 +1,177 @@
+// MerkleOps<Blake2sMerkleHasher>::commit_on_layer and GrindOps<Blake2sChannel>::grind.
+//
+// Node i of a layer = BLAKE2s-256( [prev[2i] || prev[2i+1]] || col_0[i] || ... || col_{k-1}[i] )
+// with u32 little-endian column words (crates/prover/src/core/vcs/blake2_merkle.rs:14-30,
+// backend/simd/blake2s.rs:60-145; the empty message when there is neither). One thread per node:
+// a warp reads each column as one coalesced 128-byte line and streams 16 columns per
+// compression, so a leaf costs ceil(k/16) compressions on the INT pipes.
+#include "common.cuh"
+#include "blake2s.cuh"
+
+namespace stwo {
+
+constexpr int MERKLE_MAX_COLS = 3072;  // 24 KB of column pointers in the launch parameters
+struct MerkleCols { const uint32_t* p[MERKLE_MAX_COLS]; };
+
+// Hashes nodes [0, n_nodes) of a layer. When `n_cols` spans several launches the running
+// chaining value and byte count persist in `state` (8 words + 1 per node); `first`/`last`
+// mark the launch that starts / finishes the message.
+__global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const uint32_t* __restrict__ prev,
+                                                      MerkleCols cols, uint32_t n_cols, uint32_t* __restrict__ out,
+                                                      uint32_t* __restrict__ state, uint32_t first, uint32_t last,
+                                                      uint32_t total_bytes) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes) return;
+  uint32_t h[8];
+  uint32_t m[16];
+  uint32_t t = 0;
+  if (first) {
+    b2s_init(h);
+    if (prev) {
+      const uint4* pp = reinterpret_cast<const uint4*>(prev + (size_t)16 * i);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        uint4 w = pp[q];
+        m[4 * q] = w.x;
+        m[4 * q + 1] = w.y;
+        m[4 * q + 2] = w.z;
+        m[4 * q + 3] = w.w;
+      }
+      t = 64;
+      bool fin = last && n_cols == 0;
+      b2s_compress(h, m, t, fin);
+    } else if (n_cols == 0 && last) {
+#pragma unroll
+      for (int q = 0; q < 16; q++) m[q] = 0;
+      b2s_compress(h, m, 0, true);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; q++) h[q] = state[(size_t)9 * i + q];
+    t = state[(size_t)9 * i + 8];
+  }
+  uint32_t c = 0;
+  while (c < n_cols) {
+    uint32_t k = n_cols - c < 16 ? n_cols - c : 16;
+    bool fin = last && (c + k == n_cols);
+#pragma unroll
+    for (int q = 0; q < 16; q++) m[q] = (uint32_t)q < k ? __ldg(cols.p[c + q] + i) : 0u;
+    t += 4 * k;
+    b2s_compress(h, m, t, fin);
+    c += k;
+  }
+  if (last) {
+    uint4* po = reinterpret_cast<uint4*>(out + (size_t)8 * i);
+    po[0] = make_uint4(h[0], h[1], h[2], h[3]);
+    po[1] = make_uint4(h[4], h[5], h[6], h[7]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; q++) state[(size_t)9 * i + q] = h[q];
+    state[(size_t)9 * i + 8] = t;
+  }
+  (void)total_bytes;
+}
+
+int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols, uint32_t n_cols,
+                            uint32_t* out, cudaStream_t s) {
+  STWO_REQUIRE(log_size <= 30, "layer log size %u > 30", log_size);
+  STWO_REQUIRE(out, "null output");
+  STWO_REQUIRE(n_cols == 0 || cols, "null column table");
+  uint32_t n = 1u << log_size;
+  // Columns are consumed 16 at a time; a launch takes a multiple of 16 so that only the last
+  // launch sees a partial block.
+  const uint32_t per_launch = (MERKLE_MAX_COLS / 16) * 16;
+  uint32_t n_launch = n_cols <= per_launch ? 1 : (n_cols + per_launch - 1) / per_launch;
+  uint32_t* state = nullptr;
+  if (n_launch > 1) {
+    int32_t st = scratch_alloc((void**)&state, (size_t)n * 9 * 4, s);
+    if (st) return st;
+  }
+  uint32_t threads = 256;
+  uint32_t blocks = (n + threads - 1) / threads;
+  for (uint32_t l = 0; l < n_launch; l++) {
+    uint32_t c0 = l * per_launch;
+    uint32_t nc = n_cols - c0 < per_launch ? n_cols - c0 : per_launch;
+    MerkleCols mc;
+    for (uint32_t q = 0; q < nc; q++) mc.p[q] = cols[c0 + q];
+    k_merkle_layer<<<blocks, threads, 0, s>>>(n, prev, mc, nc, out, state, l == 0, l + 1 == n_launch, 0); note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      scratch_free(state, s);
+      set_error("merkle launch: %s", cudaGetErrorString(e));
+      return STWO_ERR_CUDA;
+    }
+  }
+  scratch_free(state, s);
+  return STWO_OK;
+}
+
+// ---------------------------------------------------------------- grind
+// Tests nonces [base, base + n): the smallest with >= pow_bits trailing zeros in word 0 of the
+// raw compression (digest, [lo, hi, 0, ...], t = 0, f = 0) is folded into *best by atomicMin.
+__global__ void k_grind(uint32_t d0, uint32_t d1, uint32_t d2, uint32_t d3, uint32_t d4, uint32_t d5, uint32_t d6,
+                        uint32_t d7, uint64_t base, uint32_t n, uint32_t pow_bits,
+                        unsigned long long* best) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t nonce = base + i;
+  uint32_t h[8] = {d0, d1, d2, d3, d4, d5, d6, d7};
+  uint32_t m[16];
+#pragma unroll
+  for (int q = 0; q < 16; q++) m[q] = 0;
+  m[0] = (uint32_t)nonce;
+  m[1] = (uint32_t)(nonce >> 32);
+  b2s_compress(h, m, 0, false);
+  uint32_t tz = h[0] == 0 ? 32u : (uint32_t)__ffs(h[0]) - 1;
+  if (tz >= pow_bits) atomicMin(best, (unsigned long long)nonce);
+}
+
+}  // namespace stwo
+
+using namespace stwo;
+
+extern "C" {
+
+stwo_status stwo_merkle_commit_layer(uint32_t log_size, const uint32_t* d_prev_layer, const uint32_t* const* d_cols,
+                                     uint32_t n_cols, uint32_t* d_out, void* stream) {
+  return merkle_commit_layer(log_size, d_prev_layer, d_cols, n_cols, d_out, as_stream(stream));
+}
+
+stwo_status stwo_grind_blake2s(const uint32_t h_digest[8], uint32_t pow_bits, uint64_t* h_nonce, void* stream) {
+  STWO_REQUIRE(h_digest && h_nonce, "null argument");
+  STWO_REQUIRE(pow_bits <= 32, "pow_bits > 32 is not supported");
+  cudaStream_t s = as_stream(stream);
+  unsigned long long* d_best = nullptr;
+  int32_t st = scratch_alloc((void**)&d_best, sizeof(unsigned long long), s);
+  if (st) return st;
+  const unsigned long long none = ~0ull;
+  // Batches grow geometrically: small proofs of work finish after one short launch.
+  uint64_t base = 0;
+  uint32_t batch = 1u << 14;
+  unsigned long long best = none;
+  stwo_status rc = STWO_OK;
+  while (true) {
+    if (cudaMemcpyAsync(d_best, &none, sizeof(none), cudaMemcpyHostToDevice, s) != cudaSuccess) { rc = STWO_ERR_CUDA; break; }
+    uint32_t threads = 256;
+    k_grind<<<(batch + threads - 1) / threads, threads, 0, s>>>(h_digest[0], h_digest[1], h_digest[2], h_digest[3],
+                                                                 h_digest[4], h_digest[5], h_digest[6], h_digest[7],
+                                                                 base, batch, pow_bits, d_best); note_launch();
+    if (cudaGetLastError() != cudaSuccess) { rc = STWO_ERR_CUDA; break; }
+    if (cudaMemcpyAsync(&best, d_best, sizeof(best), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { rc = STWO_ERR_CUDA; break; }
+    if (best != none) break;
+    base += batch;
+    if (batch < (1u << 26)) batch <<= 2;
+    if (base >= (1ull << 44)) { rc = STWO_ERR_TIMEOUT; break; }
+  }
+  scratch_free(d_best, s);
+  cudaStreamSynchronize(s);
+  if (rc) {
+    set_error("grind failed (status %d)", rc);
+    return rc;
+  }
+  *h_nonce = best;
+  return STWO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,313 @@
+// PolyOps::eval_at_point / extend, ColumnOps::bit_reverse_column, AccumulationOps,
+// and Column::at gathers.
+//
+// eval_at_point (crates/prover/src/core/backend/cpu/circle.rs:73-87): sum_i coeff_i * t_i(point),
+// t_i = y^{i_0} x^{i_1} pi(x)^{i_2} ... pi^{L-2}(x)^{i_{L-1}}, pi(x) = 2x^2 - 1. The index is split
+// as (top | mid 6 bits | low 8 bits): thread t of a block owns low = t, accumulates
+// sum_mid coeff * Mid[mid] (4 IMAD per coefficient), multiplies once by Low[t]; the block sum is
+// scaled by Top[block] and folded into 64-bit accumulators. One pass over the coefficients,
+// coalesced; HBM-bound for large polynomials.
+#include "common.cuh"
+
+namespace stwo {
+
+constexpr uint32_t EP_LOW = 8, EP_MID = 6;
+
+struct EvalJob {
+  const uint32_t* coeffs;
+  uint32_t log_size;
+  uint32_t pad;
+};
+
+__device__ __forceinline__ qm31 qm31_double_x(qm31 x) {
+  qm31 s = qm31_mul(x, x);
+  return qm31_sub(qm31_add(s, s), qm31_from_u32(1, 0, 0, 0));
+}
+
+// Mapping j of the point: j = 0 -> y, j >= 1 -> pi^{j-1}(x).
+__device__ __forceinline__ void point_mappings(const stwo_qm31_point& pt, uint32_t L, qm31* m) {
+  m[0] = qm31_from_u32(pt.y.v[0], pt.y.v[1], pt.y.v[2], pt.y.v[3]);
+  qm31 x = qm31_from_u32(pt.x.v[0], pt.x.v[1], pt.x.v[2], pt.x.v[3]);
+  for (uint32_t j = 1; j < L; j++) {
+    m[j] = x;
+    x = qm31_double_x(x);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict__ jobs, const uint32_t* __restrict__ poly_of,
+                                                       const stwo_qm31_point* __restrict__ points,
+                                                       unsigned long long* __restrict__ acc) {
+  __shared__ qm31 s_map[32];
+  __shared__ qm31 s_mid[1 << EP_MID];
+  __shared__ qm31 s_part[8];
+  const uint32_t e = blockIdx.y;
+  const EvalJob job = jobs[poly_of[e]];
+  const uint32_t L = job.log_size;
+  const uint32_t lo_bits = L < EP_LOW ? L : EP_LOW;
+  const uint32_t mid_bits = L - lo_bits < EP_MID ? L - lo_bits : EP_MID;
+  const uint32_t chunk_bits = lo_bits + mid_bits;
+  const uint32_t n_chunks = 1u << (L - chunk_bits);
+  if (blockIdx.x >= n_chunks) return;
+  if (threadIdx.x == 0) point_mappings(points[e], L, s_map);
+  __syncthreads();
+  if (threadIdx.x < (1u << mid_bits)) {
+    qm31 t = qm31_from_u32(1, 0, 0, 0);
+    for (uint32_t b = 0; b < mid_bits; b++)
+      if ((threadIdx.x >> b) & 1) t = qm31_mul(t, s_map[lo_bits + b]);
+    s_mid[threadIdx.x] = t;
+  }
+  __syncthreads();
+  qm31 res = qm31_zero();
+  const uint32_t t = threadIdx.x;
+  if (t < (1u << lo_bits)) {
+    const uint32_t* c = job.coeffs + ((size_t)blockIdx.x << chunk_bits);
+    unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    uint32_t cnt = 0;
+    for (uint32_t m = 0; m < (1u << mid_bits); m++) {
+      uint32_t v = __ldg(c + (m << lo_bits) + t);
+      qm31 w = s_mid[m];
+      a0 += (unsigned long long)w.a.a * v;
+      a1 += (unsigned long long)w.a.b * v;
+      a2 += (unsigned long long)w.b.a * v;
+      a3 += (unsigned long long)w.b.b * v;
+      if (++cnt == 3) {
+        a0 = (a0 & P) + (a0 >> 31);
+        a1 = (a1 & P) + (a1 >> 31);
+        a2 = (a2 & P) + (a2 >> 31);
+        a3 = (a3 & P) + (a3 >> 31);
+        cnt = 0;
+      }
+    }
+    auto red = [](unsigned long long x) {
+      x = (x & P) + (x >> 31);
+      x = (x & P) + (x >> 31);
+      uint32_t r = (uint32_t)x;
+      return r >= P ? r - P : r;
+    };
+    res = qm31_from_u32(red(a0), red(a1), red(a2), red(a3));
+    qm31 low = qm31_from_u32(1, 0, 0, 0);
+    for (uint32_t b = 0; b < lo_bits; b++)
+      if ((t >> b) & 1) low = qm31_mul(low, s_map[b]);
+    res = qm31_mul(res, low);
+  }
+  // Block reduction of the QM31 partials.
+  uint32_t w[4] = {res.a.a, res.a.b, res.b.a, res.b.b};
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    for (int o = 16; o > 0; o >>= 1) w[q] = m31_add(w[q], __shfl_xor_sync(0xffffffffu, w[q], o));
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = qm31_from_u32(w[0], w[1], w[2], w[3]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    qm31 sum = qm31_zero();
+    for (uint32_t i = 0; i < blockDim.x / 32; i++) sum = qm31_add(sum, s_part[i]);
+    qm31 top = qm31_from_u32(1, 0, 0, 0);
+    for (uint32_t b = chunk_bits; b < L; b++)
+      if ((blockIdx.x >> (b - chunk_bits)) & 1) top = qm31_mul(top, s_map[b]);
+    sum = qm31_mul(sum, top);
+    atomicAdd(acc + 4 * e + 0, (unsigned long long)sum.a.a);
+    atomicAdd(acc + 4 * e + 1, (unsigned long long)sum.a.b);
+    atomicAdd(acc + 4 * e + 2, (unsigned long long)sum.b.a);
+    atomicAdd(acc + 4 * e + 3, (unsigned long long)sum.b.b);
+  }
+}
+
+__global__ void k_reduce_acc(const unsigned long long* acc, uint32_t n, uint32_t* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned long long x = acc[i];
+  x = (x & P) + (x >> 31);
+  x = (x & P) + (x >> 31);
+  uint32_t r = (uint32_t)x;
+  out[i] = r >= P ? r - P : r;
+}
+
+int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
+                       const uint32_t* poly_of, const stwo_qm31_point* points, uint32_t n_evals, stwo_qm31* out,
+                       cudaStream_t s) {
+  if (n_evals == 0) return STWO_OK;
+  STWO_REQUIRE(coeffs && log_sizes && poly_of && points && out, "null argument");
+  std::vector<EvalJob> jobs(n_polys);
+  uint32_t max_chunks = 1;
+  for (uint32_t i = 0; i < n_polys; i++) {
+    STWO_REQUIRE(log_sizes[i] <= 30, "poly log size %u > 30", log_sizes[i]);
+    jobs[i] = {coeffs[i], log_sizes[i], 0};
+  }
+  for (uint32_t e = 0; e < n_evals; e++) {
+    STWO_REQUIRE(poly_of[e] < n_polys, "poly index out of range");
+    uint32_t L = log_sizes[poly_of[e]];
+    uint32_t cb = std::min(L, EP_LOW) + std::min(L - std::min(L, EP_LOW), EP_MID);
+    max_chunks = std::max(max_chunks, 1u << (L - cb));
+  }
+  STWO_REQUIRE(n_evals <= 65535, "too many evaluations in one call");
+  size_t off_jobs = 0;
+  size_t off_polyof = off_jobs + ((jobs.size() * sizeof(EvalJob) + 255) / 256) * 256;
+  size_t off_pts = off_polyof + (((size_t)n_evals * 4 + 255) / 256) * 256;
+  size_t off_acc = off_pts + (((size_t)n_evals * sizeof(stwo_qm31_point) + 255) / 256) * 256;
+  size_t off_out = off_acc + (size_t)n_evals * 4 * 8;
+  size_t total = off_out + (size_t)n_evals * 16;
+  char* buf = nullptr;
+  int32_t st = scratch_alloc((void**)&buf, total, s);
+  if (st) return st;
+  cudaError_t err = cudaSuccess;
+  if (!jobs.empty()) err = cudaMemcpyAsync(buf + off_jobs, jobs.data(), jobs.size() * sizeof(EvalJob), cudaMemcpyHostToDevice, s);
+  if (!err) err = cudaMemcpyAsync(buf + off_polyof, poly_of, (size_t)n_evals * 4, cudaMemcpyHostToDevice, s);
+  if (!err) err = cudaMemcpyAsync(buf + off_pts, points, (size_t)n_evals * sizeof(stwo_qm31_point), cudaMemcpyHostToDevice, s);
+  if (!err) err = cudaMemsetAsync(buf + off_acc, 0, (size_t)n_evals * 32, s);
+  if (!err) {
+    dim3 grid(max_chunks, n_evals);
+    k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<EvalJob*>(buf + off_jobs),
+                                         reinterpret_cast<uint32_t*>(buf + off_polyof),
+                                         reinterpret_cast<stwo_qm31_point*>(buf + off_pts),
+                                         reinterpret_cast<unsigned long long*>(buf + off_acc)); note_launch();
+    err = cudaGetLastError();
+  }
+  if (!err) {
+    k_reduce_acc<<<(n_evals * 4 + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned long long*>(buf + off_acc),
+                                                            n_evals * 4, reinterpret_cast<uint32_t*>(buf + off_out)); note_launch();
+    err = cudaGetLastError();
+  }
+  if (!err) err = cudaMemcpyAsync(out, buf + off_out, (size_t)n_evals * 16, cudaMemcpyDeviceToHost, s);
+  scratch_free(buf, s);
+  if (!err) err = cudaStreamSynchronize(s);
+  if (err) {
+    set_error("eval_at_points: %s", cudaGetErrorString(err));
+    return STWO_ERR_CUDA;
+  }
+  return STWO_OK;
+}
+
+// ---------------------------------------------------------------- bit reverse
+__global__ void k_bit_reverse(uint32_t* col, uint32_t log_n) {
+  uint32_t n = 1u << log_n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t j = brev(i, log_n);
+    if (i < j) {
+      uint32_t a = col[i];
+      col[i] = col[j];
+      col[j] = a;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- accumulation
+__global__ void k_secure_accumulate(uint32_t* a0, uint32_t* a1, uint32_t* a2, uint32_t* a3, const uint32_t* b0,
+                                    const uint32_t* b1, const uint32_t* b2, const uint32_t* b3, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    a0[i] = m31_add(a0[i], __ldg(b0 + i));
+    a1[i] = m31_add(a1[i], __ldg(b1 + i));
+    a2[i] = m31_add(a2[i], __ldg(b2 + i));
+    a3[i] = m31_add(a3[i], __ldg(b3 + i));
+  }
+}
+
+__global__ void k_secure_powers(qm31 felt, uint32_t n, uint32_t* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  qm31 r = qm31_from_u32(1, 0, 0, 0), b = felt;
+  uint32_t e = i;
+  while (e) {
+    if (e & 1) r = qm31_mul(r, b);
+    b = qm31_mul(b, b);
+    e >>= 1;
+  }
+  out[4 * i] = r.a.a;
+  out[4 * i + 1] = r.a.b;
+  out[4 * i + 2] = r.b.a;
+  out[4 * i + 3] = r.b.b;
+}
+
+__global__ void k_gather(const uint32_t* col, const unsigned long long* idx, size_t n, uint32_t* out) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = col[idx[i]];
+}
+
+static uint32_t grid_cap(size_t n, uint32_t threads) {
+  size_t b = (n + threads - 1) / threads;
+  size_t cap = (size_t)sm_count() * 16;
+  return (uint32_t)std::max<size_t>(1, std::min(b, cap));
+}
+
+}  // namespace stwo
+
+using namespace stwo;
+
+extern "C" {
+
+stwo_status stwo_eval_at_points(const uint32_t* const* d_coeffs, const uint32_t* h_log_sizes, uint32_t n_polys,
+                                const uint32_t* h_poly_of, const stwo_qm31_point* h_points, uint32_t n_evals,
+                                stwo_qm31* h_out, void* stream) {
+  return eval_at_points(d_coeffs, h_log_sizes, n_polys, h_poly_of, h_points, n_evals, h_out, as_stream(stream));
+}
+
+stwo_status stwo_extend(const uint32_t* d_coeffs, uint32_t coeff_log_size, uint32_t* d_out, uint32_t log_size,
+                        void* stream) {
+  STWO_REQUIRE(log_size >= coeff_log_size && log_size <= 30, "extend to a smaller size");
+  cudaStream_t s = as_stream(stream);
+  size_t n0 = (size_t)1 << coeff_log_size, n1 = (size_t)1 << log_size;
+  if (d_out != d_coeffs) STWO_CHECK_CUDA(cudaMemcpyAsync(d_out, d_coeffs, n0 * 4, cudaMemcpyDeviceToDevice, s));
+  if (n1 > n0) STWO_CHECK_CUDA(cudaMemsetAsync(d_out + n0, 0, (n1 - n0) * 4, s));
+  return STWO_OK;
+}
+
+stwo_status stwo_bit_reverse_column(uint32_t* d_col, uint32_t log_size, void* stream) {
+  STWO_REQUIRE(log_size <= 30, "log size > 30");
+  k_bit_reverse<<<grid_cap((size_t)1 << log_size, 256), 256, 0, as_stream(stream)>>>(d_col, log_size); note_launch();
+  STWO_LAUNCH_CHECK();
+  return STWO_OK;
+}
+
+stwo_status stwo_secure_accumulate(uint32_t* const d_acc[4], const uint32_t* const d_other[4], size_t n,
+                                   void* stream) {
+  if (n == 0) return STWO_OK;
+  k_secure_accumulate<<<grid_cap(n, 256), 256, 0, as_stream(stream)>>>(d_acc[0], d_acc[1], d_acc[2], d_acc[3],
+                                                                       d_other[0], d_other[1], d_other[2],
+                                                                       d_other[3], n); note_launch();
+  STWO_LAUNCH_CHECK();
+  return STWO_OK;
+}
+
+stwo_status stwo_generate_secure_powers(stwo_qm31 felt, uint32_t n_powers, stwo_qm31* h_out, void* stream) {
+  if (n_powers == 0) return STWO_OK;
+  STWO_REQUIRE(h_out, "null output");
+  cudaStream_t s = as_stream(stream);
+  uint32_t* d = nullptr;
+  int32_t st = scratch_alloc((void**)&d, (size_t)n_powers * 16, s);
+  if (st) return st;
+  qm31 f = {{felt.v[0], felt.v[1]}, {felt.v[2], felt.v[3]}};
+  k_secure_powers<<<(n_powers + 255) / 256, 256, 0, s>>>(f, n_powers, d); note_launch();
+  cudaError_t e = cudaGetLastError();
+  if (!e) e = cudaMemcpyAsync(h_out, d, (size_t)n_powers * 16, cudaMemcpyDeviceToHost, s);
+  scratch_free(d, s);
+  if (!e) e = cudaStreamSynchronize(s);
+  if (e) {
+    set_error("secure powers: %s", cudaGetErrorString(e));
+    return STWO_ERR_CUDA;
+  }
+  return STWO_OK;
+}
+
+stwo_status stwo_read_words(const uint32_t* d_col, const uint64_t* h_idx, size_t n, uint32_t* h_out, void* stream) {
+  if (n == 0) return STWO_OK;
+  STWO_REQUIRE(d_col && h_idx && h_out, "null argument");
+  cudaStream_t s = as_stream(stream);
+  char* buf = nullptr;
+  int32_t st = scratch_alloc((void**)&buf, n * 12 + 16, s);
+  if (st) return st;
+  unsigned long long* d_idx = reinterpret_cast<unsigned long long*>(buf);
+  uint32_t* d_out = reinterpret_cast<uint32_t*>(buf + n * 8);
+  cudaError_t e = cudaMemcpyAsync(d_idx, h_idx, n * 8, cudaMemcpyHostToDevice, s);
+  if (!e) {
+    k_gather<<<(uint32_t)((n + 255) / 256), 256, 0, s>>>(d_col, d_idx, n, d_out); note_launch();
+    e = cudaGetLastError();
+  }
+  if (!e) e = cudaMemcpyAsync(h_out, d_out, n * 4, cudaMemcpyDeviceToHost, s);
+  scratch_free(buf, s);
+  if (!e) e = cudaStreamSynchronize(s);
+  if (e) {
+    set_error("read_words: %s", cudaGetErrorString(e));
+    return STWO_ERR_CUDA;
+  }
+  return STWO_OK;
+}
+
+}  // extern "C"

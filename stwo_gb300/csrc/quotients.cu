@@ -1,0 +1,197 @@
+// QuotientOps::accumulate_quotients.
+//
+// Per row (crates/prover/src/core/backend/cpu/quotients.rs:43-76):
+//   acc = sum over batches k, in BTreeMap order:  acc * batch_coeff_k + num_k * den_k^-1
+//   num_k = sum_j (c_j * f_j(p) - (a_j * p.y + b_j))      [(a, b, c) of constraints.rs:98-115]
+//   den_k = (Re(P.x) - p.x) * Im(P.y) - (Re(P.y) - p.y) * Im(P.x)   (CM31)
+// As the reference SIMD backend does (backend/simd/quotients.rs:31-100), rows are computed on
+// the sub-domain (the first 2^(n - log_blowup) bit-reversed rows) and the result is extended to
+// the full domain through an interpolation and an evaluation; below a sub-domain of 2^6 points
+// every row is computed directly (the CPU fallback at simd/quotients.rs:41-58).
+//
+// GB300 mapping: one thread per row, columns streamed with coalesced 128-byte warp loads;
+// sum_j c_j * f_j is accumulated in 64-bit lanes (3 products per partial reduction) and the
+// linear terms are hoisted per batch (sum_j a_j, sum_j b_j), which leaves ~4 IMAD.WIDE + 4 IADD
+// per (column, row). The batch tables travel in a small device buffer.
+#include "common.cuh"
+
+namespace stwo {
+
+int32_t fft_interpolate(const TwiddleTree* tree, stwo_coset half, uint32_t* const* cols, uint32_t n, cudaStream_t s);
+int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* const* coeffs, uint32_t coeff_log,
+                     uint32_t* const* out, uint32_t n, cudaStream_t s);
+
+struct QBatch {
+  uint32_t prx[2], pix[2], pry[2], piy[2];  // CM31 parts of the sample point
+  uint32_t sum_a[4], sum_b[4], coeff[4];    // sum of a_j, sum of b_j, random_coeff^(n_j)
+  uint32_t e0, e1;                          // entry range
+};
+struct QEntry {
+  uint32_t col;
+  uint32_t c[4];
+};
+
+constexpr int Q_MAX_COLS = 2048;
+struct QCols { const uint32_t* p[Q_MAX_COLS]; };
+
+__device__ __forceinline__ uint32_t red64(unsigned long long x) {
+  x = (x & P) + (x >> 31);
+  x = (x & P) + (x >> 31);
+  uint32_t r = (uint32_t)x;
+  return r >= P ? r - P : r;
+}
+__device__ __forceinline__ unsigned long long fold64(unsigned long long x) { return (x & P) + (x >> 31); }
+
+__global__ void __launch_bounds__(256) k_quotient_rows(uint32_t rows, uint32_t log_n, uint32_t half_init,
+                                                       uint32_t half_step, QCols cols,
+                                                       const QBatch* __restrict__ batches, uint32_t n_batches,
+                                                       const QEntry* __restrict__ entries, uint32_t* o0, uint32_t* o1,
+                                                       uint32_t* o2, uint32_t* o3) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  // Domain point of bit-reversed row r of the circle domain with half coset (init, step).
+  uint32_t k = brev(r, log_n);
+  uint32_t half = 1u << (log_n - 1);
+  uint32_t idx = k < half ? half_init + half_step * k : (0u - (half_init + half_step * (k - half)));
+  cpoint p = index_to_point(idx & 0x7fffffffu);
+
+  qm31 acc = qm31_zero();
+  for (uint32_t b = 0; b < n_batches; b++) {
+    const QBatch& B = batches[b];
+    unsigned long long s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    uint32_t cnt = 0;
+    for (uint32_t e = B.e0; e < B.e1; e++) {
+      const QEntry& E = entries[e];
+      uint32_t v = __ldg(cols.p[E.col] + r);
+      s0 += (unsigned long long)E.c[0] * v;
+      s1 += (unsigned long long)E.c[1] * v;
+      s2 += (unsigned long long)E.c[2] * v;
+      s3 += (unsigned long long)E.c[3] * v;
+      if (++cnt == 3) {
+        s0 = fold64(s0);
+        s1 = fold64(s1);
+        s2 = fold64(s2);
+        s3 = fold64(s3);
+        cnt = 0;
+      }
+    }
+    qm31 cv = qm31_from_u32(red64(s0), red64(s1), red64(s2), red64(s3));
+    qm31 lin = qm31_add(qm31_mul_m31(qm31_from_u32(B.sum_a[0], B.sum_a[1], B.sum_a[2], B.sum_a[3]), p.y),
+                        qm31_from_u32(B.sum_b[0], B.sum_b[1], B.sum_b[2], B.sum_b[3]));
+    qm31 num = qm31_sub(cv, lin);
+    cm31 px = {p.x, 0u}, py = {p.y, 0u};
+    cm31 den = cm31_sub(cm31_mul(cm31_sub({B.prx[0], B.prx[1]}, px), {B.piy[0], B.piy[1]}),
+                        cm31_mul(cm31_sub({B.pry[0], B.pry[1]}, py), {B.pix[0], B.pix[1]}));
+    acc = qm31_add(qm31_mul(acc, qm31_from_u32(B.coeff[0], B.coeff[1], B.coeff[2], B.coeff[3])),
+                   qm31_mul_cm31(num, cm31_inv(den)));
+  }
+  o0[r] = acc.a.a;
+  o1[r] = acc.a.b;
+  o2[r] = acc.b.a;
+  o3[r] = acc.b.b;
+}
+
+int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, stwo_qm31 rc_in,
+                             const stwo_sample_batch* batches, uint32_t n_batches, uint32_t log_blowup,
+                             uint32_t* const out[4], cudaStream_t s) {
+  STWO_REQUIRE(log_n >= 1 && log_n <= 30, "bad domain log size %u", log_n);
+  STWO_REQUIRE(log_blowup < log_n, "log_blowup_factor %u >= domain log size %u", log_blowup, log_n);
+  STWO_REQUIRE(n_cols <= Q_MAX_COLS, "more than %d columns in one quotient group", Q_MAX_COLS);
+  STWO_REQUIRE(n_batches == 0 || batches, "null batches");
+  hq rc = hq_from(rc_in);
+
+  // Host constants: O(#samples) (cpu/quotients.rs:78-125).
+  std::vector<QBatch> hb(n_batches);
+  std::vector<QEntry> he;
+  for (uint32_t b = 0; b < n_batches; b++) {
+    const stwo_sample_batch& sb = batches[b];
+    hq px = hq_from(sb.point.x), py = hq_from(sb.point.y);
+    STWO_REQUIRE(!(py.v[2] == 0 && py.v[3] == 0), "Cannot evaluate a line with a single point");
+    QBatch& B = hb[b];
+    B.prx[0] = px.v[0]; B.prx[1] = px.v[1]; B.pix[0] = px.v[2]; B.pix[1] = px.v[3];
+    B.pry[0] = py.v[0]; B.pry[1] = py.v[1]; B.piy[0] = py.v[2]; B.piy[1] = py.v[3];
+    hq alpha = hq_make(1, 0, 0, 0), sa = hq_make(0, 0, 0, 0), sbb = hq_make(0, 0, 0, 0);
+    B.e0 = (uint32_t)he.size();
+    for (uint32_t j = 0; j < sb.n_columns; j++) {
+      STWO_REQUIRE(sb.h_column_indices[j] < n_cols, "sample column index out of range");
+      alpha = hq_mul(alpha, rc);
+      hq value = hq_from(sb.h_values[j]);
+      hq a = hq_sub(hq_conj(value), value);
+      hq c = hq_sub(hq_conj(py), py);
+      hq bcoef = hq_sub(hq_mul(value, c), hq_mul(a, py));
+      sa = hq_add(sa, hq_mul(alpha, a));
+      sbb = hq_add(sbb, hq_mul(alpha, bcoef));
+      hq ca = hq_mul(alpha, c);
+      QEntry e;
+      e.col = sb.h_column_indices[j];
+      for (int q = 0; q < 4; q++) e.c[q] = ca.v[q];
+      he.push_back(e);
+    }
+    B.e1 = (uint32_t)he.size();
+    hq bc = hq_pow(rc, sb.n_columns);
+    for (int q = 0; q < 4; q++) {
+      B.sum_a[q] = sa.v[q];
+      B.sum_b[q] = sbb.v[q];
+      B.coeff[q] = bc.v[q];
+    }
+  }
+
+  stwo_coset dom_half = canonic_half_coset(log_n);
+  uint32_t sub_log = log_n - log_blowup;
+  bool direct = sub_log < 6;
+  uint32_t rows = 1u << (direct ? log_n : sub_log);
+
+  size_t tbl_bytes = hb.size() * sizeof(QBatch) + he.size() * sizeof(QEntry);
+  size_t sub_bytes = direct ? 0 : (size_t)4 * rows * 4;
+  char* scratch = nullptr;
+  int32_t st = scratch_alloc((void**)&scratch, tbl_bytes + sub_bytes + 256, s);
+  if (st) return st;
+  QBatch* d_b = reinterpret_cast<QBatch*>(scratch);
+  QEntry* d_e = reinterpret_cast<QEntry*>(scratch + hb.size() * sizeof(QBatch));
+  uint32_t* d_sub = reinterpret_cast<uint32_t*>(scratch + ((tbl_bytes + 255) / 256) * 256);
+  auto fail = [&](int32_t code) {
+    scratch_free(scratch, s);
+    return code;
+  };
+  if (!hb.empty() && cudaMemcpyAsync(d_b, hb.data(), hb.size() * sizeof(QBatch), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return fail(STWO_ERR_CUDA);
+  if (!he.empty() && cudaMemcpyAsync(d_e, he.data(), he.size() * sizeof(QEntry), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return fail(STWO_ERR_CUDA);
+
+  QCols qc;
+  for (uint32_t c = 0; c < n_cols; c++) qc.p[c] = cols[c];
+  uint32_t* o[4];
+  for (int q = 0; q < 4; q++) o[q] = direct ? out[q] : d_sub + (size_t)q * rows;
+  k_quotient_rows<<<(rows + 255) / 256, 256, 0, s>>>(rows, log_n, dom_half.initial_index, dom_half.step_size, qc,
+                                                     d_b, n_batches, d_e, o[0], o[1], o[2], o[3]); note_launch();
+  if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
+
+  if (!direct) {
+    // Interpolate on the sub-domain (its own tree), then evaluate on the full canonic domain.
+    stwo_coset sub_half = coset_new(dom_half.initial_index, sub_log - 1);
+    TwiddleTree* t_sub = nullptr;
+    TwiddleTree* t_dom = nullptr;
+    st = get_tree(sub_half, s, &t_sub);
+    if (!st) st = get_tree(dom_half, s, &t_dom);
+    if (!st) st = fft_interpolate(t_sub, sub_half, o, 4, s);
+    if (!st) {
+      const uint32_t* co[4] = {o[0], o[1], o[2], o[3]};
+      st = fft_evaluate(t_dom, dom_half, co, sub_log, out, 4, s);
+    }
+    if (st) return fail(st);
+  }
+  scratch_free(scratch, s);
+  return STWO_OK;
+}
+
+}  // namespace stwo
+
+using namespace stwo;
+
+extern "C" stwo_status stwo_accumulate_quotients(uint32_t domain_log_size, const uint32_t* const* d_cols,
+                                                 uint32_t n_cols, stwo_qm31 random_coeff,
+                                                 const stwo_sample_batch* h_batches, uint32_t n_batches,
+                                                 uint32_t log_blowup_factor, uint32_t* const d_out[4], void* stream) {
+  return accumulate_quotients(domain_log_size, d_cols, n_cols, random_coeff, h_batches, n_batches, log_blowup_factor,
+                              d_out, as_stream(stream));
+}

@@ -1,0 +1,217 @@
+// Runtime: errors, device context, stream-ordered buffers and twiddle trees.
+#include "common.cuh"
+#include <cstdarg>
+#include <atomic>
+
+namespace stwo {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+DeviceContext& ctx() {
+  static DeviceContext c;
+  return c;
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+int32_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
+  *p = nullptr;
+  if (bytes == 0) return STWO_OK;
+  STWO_CHECK_CUDA(cudaMallocAsync(p, bytes, s));
+  return STWO_OK;
+}
+void scratch_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+hpoint h_index_to_point(uint32_t idx) {
+  static hpoint tower[31];
+  static bool init = false;
+  if (!init) {
+    tower[0] = {2u, 1268011823u};  // M31_CIRCLE_GEN, crates/prover/src/core/circle.rs:203-206
+    for (int b = 1; b < 31; b++) tower[b] = h_padd(tower[b - 1], tower[b - 1]);
+    init = true;
+  }
+  hpoint r = {1u, 0u};
+  idx &= IDX_MASK;
+  for (int b = 0; b < 31; b++)
+    if ((idx >> b) & 1) r = h_padd(r, tower[b]);
+  return r;
+}
+
+
+// One thread per tree entry. Entry `pos` of level k (the root doubled k times, log R-k)
+// lies at offset 2^R - 2^(R-k); it is the x-coordinate of the coset point with index
+// bitrev_{R-k-1}(pos - offset). The final entry is the padding value 1.
+__global__ void k_twiddle_tree(uint32_t init, uint32_t step, uint32_t R, uint32_t* tw, uint32_t* itw) {
+  uint32_t n = 1u << R;
+  for (uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x; pos < n; pos += gridDim.x * blockDim.x) {
+    if (pos == n - 1) {
+      tw[pos] = 1u;
+      itw[pos] = 1u;
+      continue;
+    }
+    uint32_t q = n - 1 - pos;              // = 2^(R-k) - 1 - j, in [2^(R-k-1), 2^(R-k) - 1]
+    uint32_t k = R - 1 - (31 - __clz(q));  // floor(log2(q)) = R-k-1
+    uint32_t lvl_log = R - k;                      // coset log size at this level
+    uint32_t off = n - (1u << lvl_log);
+    uint32_t j = pos - off;
+    uint32_t ik = (uint32_t)(((uint64_t)init << k) & IDX_MASK);
+    uint32_t sk = (uint32_t)(((uint64_t)step << k) & IDX_MASK);
+    uint32_t idx = (uint32_t)(((uint64_t)ik + (uint64_t)sk * brev(j, lvl_log - 1)) & IDX_MASK);
+    uint32_t x = index_to_point(idx).x;
+    tw[pos] = x;
+    itw[pos] = m31_inv(x);
+  }
+}
+
+int32_t build_tree(stwo_coset root, cudaStream_t stream, TwiddleTree* t) {
+  STWO_REQUIRE(root.log_size <= 30, "twiddle root log_size %u > 30", root.log_size);
+  t->root = root;
+  t->size = (size_t)1 << root.log_size;
+  STWO_CHECK_CUDA(cudaMalloc(&t->d_tw, t->size * 4));
+  STWO_CHECK_CUDA(cudaMalloc(&t->d_itw, t->size * 4));
+  uint32_t threads = 256;
+  uint32_t blocks = (uint32_t)((t->size + threads - 1) / threads);
+  if (blocks > 65535u) blocks = 65535u;
+  k_twiddle_tree<<<blocks, threads, 0, stream>>>(root.initial_index, root.step_size, root.log_size, t->d_tw,
+                                                 t->d_itw); note_launch();
+  STWO_LAUNCH_CHECK();
+  return STWO_OK;
+}
+
+int32_t get_tree(stwo_coset root, cudaStream_t stream, TwiddleTree** out) {
+  DeviceContext& c = ctx();
+  std::lock_guard<std::mutex> g(c.mu);
+  auto key = std::make_tuple(root.initial_index, root.step_size, root.log_size);
+  auto it = c.trees.find(key);
+  if (it != c.trees.end()) {
+    *out = it->second;
+    return STWO_OK;
+  }
+  TwiddleTree* t = new TwiddleTree();
+  int32_t st = build_tree(root, stream, t);
+  if (st) {
+    delete t;
+    return st;
+  }
+  c.trees[key] = t;
+  *out = t;
+  return STWO_OK;
+}
+
+}  // namespace stwo
+
+using namespace stwo;
+
+struct stwo_twiddle_tree_s {
+  TwiddleTree t;
+};
+
+extern "C" {
+
+const char* stwo_status_string(stwo_status s) {
+  switch (s) {
+    case STWO_OK: return "ok";
+    case STWO_ERR_INVALID_ARG: return "invalid argument";
+    case STWO_ERR_OOM: return "out of device memory";
+    case STWO_ERR_TIMEOUT: return "timeout";
+    case STWO_ERR_CUDA: return "cuda error";
+    case STWO_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char* stwo_last_error(void) { return g_err; }
+
+uint64_t stwo_kernel_launches(void) { return g_launches.load(); }
+
+stwo_status stwo_device_init(int device) {
+  STWO_CHECK_CUDA(cudaSetDevice(device));
+  STWO_CHECK_CUDA(cudaFree(nullptr));
+  ctx().device = device;
+  return STWO_OK;
+}
+
+stwo_status stwo_sync(void* stream) {
+  STWO_CHECK_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  return STWO_OK;
+}
+
+stwo_status stwo_buf_alloc(void** d_ptr, size_t bytes, void* stream) {
+  STWO_REQUIRE(d_ptr, "null out pointer");
+  return scratch_alloc(d_ptr, bytes, as_stream(stream));
+}
+stwo_status stwo_buf_free(void* d_ptr, void* stream) {
+  if (d_ptr) STWO_CHECK_CUDA(cudaFreeAsync(d_ptr, as_stream(stream)));
+  return STWO_OK;
+}
+stwo_status stwo_buf_upload(void* d_dst, const void* h_src, size_t bytes, void* stream) {
+  STWO_CHECK_CUDA(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, as_stream(stream)));
+  STWO_CHECK_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  return STWO_OK;
+}
+stwo_status stwo_buf_download(void* h_dst, const void* d_src, size_t bytes, void* stream) {
+  STWO_CHECK_CUDA(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, as_stream(stream)));
+  STWO_CHECK_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  return STWO_OK;
+}
+stwo_status stwo_buf_zero(void* d_dst, size_t bytes, void* stream) {
+  STWO_CHECK_CUDA(cudaMemsetAsync(d_dst, 0, bytes, as_stream(stream)));
+  return STWO_OK;
+}
+
+stwo_status stwo_twiddles_precompute(stwo_coset root, stwo_twiddle_tree* out, void* stream) {
+  STWO_REQUIRE(out, "null out pointer");
+  stwo_twiddle_tree_s* t = new stwo_twiddle_tree_s();
+  int32_t st = build_tree(root, as_stream(stream), &t->t);
+  if (st) {
+    delete t;
+    return st;
+  }
+  *out = t;
+  return STWO_OK;
+}
+
+stwo_status stwo_twiddles_free(stwo_twiddle_tree tree) {
+  if (!tree) return STWO_OK;
+  cudaFree(tree->t.d_tw);
+  cudaFree(tree->t.d_itw);
+  delete tree;
+  return STWO_OK;
+}
+
+stwo_status stwo_twiddles_info(stwo_twiddle_tree tree, stwo_coset* root, const uint32_t** d_tw,
+                               const uint32_t** d_itw, size_t* size) {
+  STWO_REQUIRE(tree, "null tree");
+  if (root) *root = tree->t.root;
+  if (d_tw) *d_tw = tree->t.d_tw;
+  if (d_itw) *d_itw = tree->t.d_itw;
+  if (size) *size = tree->t.size;
+  return STWO_OK;
+}
+
+}  // extern "C"
+
+namespace stwo {
+const TwiddleTree* tree_of(stwo_twiddle_tree t) { return t ? &t->t : nullptr; }
+}
