@@ -20,9 +20,9 @@
 
 namespace stwo {
 
-constexpr uint32_t FFT_TMAX = 13;
-constexpr uint32_t FFT_R = 4;
-constexpr uint32_t FFT_MAX_THREADS = 512;
+constexpr uint32_t FFT_TMAX = 12;   // contiguous tile: 2^12 words = 16 KB (+ padding)
+constexpr uint32_t FFT_TMAX_STRIDED = 13;
+constexpr uint32_t FFT_R = 4;        // 2^4 words per thread, 4 layers per register round
 
 struct FftPass {
   uint32_t L;        // log size of the destination column (domain log size)
@@ -51,13 +51,33 @@ __device__ __forceinline__ uint32_t fft_twiddle(const FftPass& p, uint32_t layer
   return ((h ^ (h >> 1)) & 1) ? m31_neg(t) : t;
 }
 
+// Global index of tile element e: its low c bits are global bits [0, c), the next nl bits are
+// the layer bits [lo, lo + nl); `fixed` carries every other bit of the tile.
+__device__ __forceinline__ uint32_t tile_to_global(const FftPass& p, uint32_t e, uint32_t fixed) {
+  return (e & ((1u << p.c) - 1)) | ((e >> p.c) << p.lo) | fixed;
+}
+
+// Bits of the tile id, lowest first: the sub-domain chunk bits [F, L) (so that the chunks that
+// read the same source tile run back to back and share it through L2), then [c, lo), then
+// [lo + nl, F).
+__device__ __forceinline__ uint32_t tile_fixed_bits(const FftPass& p, uint32_t tile) {
+  uint32_t nchunk = p.L - p.F;
+  uint32_t chunk = tile & ((1u << nchunk) - 1);
+  tile >>= nchunk;
+  uint32_t mid_bits = p.lo - p.c;
+  uint32_t mid = tile & ((1u << mid_bits) - 1);
+  uint32_t top = tile >> mid_bits;
+  return (chunk << p.F) | (mid << p.c) | (top << (p.lo + p.nl));
+}
+
+// One register round over tile bits [a, a + RB): each thread owns groups of 2^RB words differing
+// in those bits, applies RB butterfly layers in registers (one twiddle load per distinct
+// twiddle), and writes the group back.
 template <bool INV, int RB>
 __device__ __forceinline__ void fft_round(const FftPass& p, uint32_t* sm, uint32_t a, uint32_t fixed) {
-  const uint32_t n_tile = 1u << p.T;
-  const uint32_t G = n_tile >> RB;
-  const uint32_t cmask = (1u << p.c) - 1;
+  const uint32_t G = (1u << p.T) >> RB;
   for (uint32_t grp = threadIdx.x; grp < G; grp += blockDim.x) {
-    uint32_t base = (grp & ((1u << a) - 1)) | ((grp >> a) << (a + RB));
+    const uint32_t base = (grp & ((1u << a) - 1)) | ((grp >> a) << (a + RB));
     uint32_t v[1 << RB];
 #pragma unroll
     for (int k = 0; k < (1 << RB); k++) v[k] = sm[pad_idx(base | ((uint32_t)k << a))];
@@ -66,13 +86,15 @@ __device__ __forceinline__ void fft_round(const FftPass& p, uint32_t* sm, uint32
       const int j = INV ? jj : (RB - 1 - jj);
       const uint32_t layer = p.lo + (a + j - p.c);
 #pragma unroll
-      for (int k = 0; k < (1 << RB); k++) {
-        if (k & (1 << j)) continue;
-        uint32_t e0 = base | ((uint32_t)k << a);
-        uint32_t g0 = (e0 & cmask) | ((e0 >> p.c) << p.lo) | fixed;
-        uint32_t t = fft_twiddle(p, layer, g0);
-        if (INV) ibfly(v[k], v[k | (1 << j)], t);
-        else bfly(v[k], v[k | (1 << j)], t);
+      for (int kh = 0; kh < (1 << (RB - 1 - j)); kh++) {
+        const int k0 = kh << (j + 1);
+        const uint32_t g0 = tile_to_global(p, base | ((uint32_t)k0 << a), fixed);
+        const uint32_t t = fft_twiddle(p, layer, g0);
+#pragma unroll
+        for (int kl = 0; kl < (1 << j); kl++) {
+          if (INV) ibfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+          else bfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+        }
       }
     }
 #pragma unroll
@@ -92,23 +114,18 @@ __device__ __forceinline__ void fft_round_dispatch(const FftPass& p, uint32_t* s
   }
 }
 
-template <bool INV>
-__global__ void __launch_bounds__(FFT_MAX_THREADS) k_fft_pass(FftPass p, ConstColPtrs src, ColPtrs dst) {
+template <bool INV, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_fft_pass(FftPass p, ConstColPtrs src, ColPtrs dst) {
   extern __shared__ uint32_t sm[];
   const uint32_t col = blockIdx.y;
-  const uint32_t tile = blockIdx.x;
   const uint32_t n_tile = 1u << p.T;
-  const uint32_t mid_bits = p.lo - p.c;
-  const uint32_t fixed = ((tile & ((1u << mid_bits) - 1)) << p.c) | ((tile >> mid_bits) << (p.lo + p.nl));
-  const uint32_t cmask = (1u << p.c) - 1;
+  const uint32_t fixed = tile_fixed_bits(p, blockIdx.x);
   const uint32_t* s = p.read_src ? src.p[col] : dst.p[col];
   const uint32_t smask = p.read_src ? ((1u << p.F) - 1) : 0xffffffffu;
   uint32_t* d = dst.p[col];
 
-  for (uint32_t e = threadIdx.x; e < n_tile; e += blockDim.x) {
-    uint32_t g = (e & cmask) | ((e >> p.c) << p.lo) | fixed;
-    sm[pad_idx(e)] = s[g & smask];
-  }
+  for (uint32_t e = threadIdx.x; e < n_tile; e += blockDim.x)
+    sm[pad_idx(e)] = __ldg(&s[tile_to_global(p, e, fixed) & smask]);
   __syncthreads();
 
   if (!INV) {
@@ -129,10 +146,9 @@ __global__ void __launch_bounds__(FFT_MAX_THREADS) k_fft_pass(FftPass p, ConstCo
   }
 
   for (uint32_t e = threadIdx.x; e < n_tile; e += blockDim.x) {
-    uint32_t g = (e & cmask) | ((e >> p.c) << p.lo) | fixed;
     uint32_t v = sm[pad_idx(e)];
     if (p.scale != 1u) v = m31_mul(v, p.scale);
-    d[g] = v;
+    d[tile_to_global(p, e, fixed)] = v;
   }
 }
 
@@ -140,8 +156,8 @@ struct PassPlan {
   uint32_t lo, nl, c;
 };
 
-// Contiguous pass over [0, min(F, 13)), strided passes (<= 9 layers, >= 16 contiguous
-// words per row) above it.
+// A contiguous pass over [0, min(F, 12)); strided passes above it with tiles of <= 2^13 words
+// whose rows keep >= 8 contiguous words (32 bytes).
 static std::vector<PassPlan> plan_passes(uint32_t F) {
   std::vector<PassPlan> v;
   if (F == 0) return v;
@@ -150,9 +166,10 @@ static std::vector<PassPlan> plan_passes(uint32_t F) {
   uint32_t lo = low;
   while (lo < F) {
     uint32_t rem = F - lo;
-    uint32_t n_passes = (rem + 8) / 9;
+    uint32_t max_nl = FFT_TMAX_STRIDED - 3;  // c >= 3
+    uint32_t n_passes = (rem + max_nl - 1) / max_nl;
     uint32_t nl = (rem + n_passes - 1) / n_passes;
-    uint32_t c = FFT_TMAX - nl;
+    uint32_t c = (nl <= FFT_TMAX - 4) ? FFT_TMAX - nl : FFT_TMAX_STRIDED - nl;
     if (c > lo) c = lo;
     v.push_back({lo, nl, c});
     lo += nl;
@@ -210,10 +227,15 @@ static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, c
       STWO_REQUIRE(tiles_log < 31, "too many tiles");
       dim3 grid(1u << tiles_log, nc);
       uint32_t groups = (1u << p.T) >> std::min(FFT_R, p.T);
-      uint32_t threads = std::max<uint32_t>(32, std::min<uint32_t>(FFT_MAX_THREADS, groups));
+      uint32_t threads = std::max<uint32_t>(32, groups);
       size_t smem = ((size_t)(1u << p.T) + ((1u << p.T) >> 5) + 1) * 4;
-      if (inverse) k_fft_pass<true><<<grid, threads, smem, s>>>(p, sp, dp);
-      else k_fft_pass<false><<<grid, threads, smem, s>>>(p, sp, dp);
+      if (threads <= 256) {
+        if (inverse) k_fft_pass<true, 256><<<grid, threads, smem, s>>>(p, sp, dp);
+        else k_fft_pass<false, 256><<<grid, threads, smem, s>>>(p, sp, dp);
+      } else {
+        if (inverse) k_fft_pass<true, 512><<<grid, threads, smem, s>>>(p, sp, dp);
+        else k_fft_pass<false, 512><<<grid, threads, smem, s>>>(p, sp, dp);
+      }
       note_launch();
       STWO_LAUNCH_CHECK();
     }

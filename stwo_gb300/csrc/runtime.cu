@@ -62,7 +62,8 @@ hpoint h_index_to_point(uint32_t idx) {
 // One thread per tree entry. Entry `pos` of level k (the root doubled k times, log R-k)
 // lies at offset 2^R - 2^(R-k); it is the x-coordinate of the coset point with index
 // bitrev_{R-k-1}(pos - offset). The final entry is the padding value 1.
-__global__ void k_twiddle_tree(uint32_t init, uint32_t step, uint32_t R, uint32_t* tw, uint32_t* itw) {
+__global__ void k_twiddle_tree(uint32_t init, uint32_t step, uint32_t R, uint32_t* tw, uint32_t* itw,
+                               uint32_t* zero_flag) {
   uint32_t n = 1u << R;
   for (uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x; pos < n; pos += gridDim.x * blockDim.x) {
     if (pos == n - 1) {
@@ -79,6 +80,7 @@ __global__ void k_twiddle_tree(uint32_t init, uint32_t step, uint32_t R, uint32_
     uint32_t sk = (uint32_t)(((uint64_t)step << k) & IDX_MASK);
     uint32_t idx = (uint32_t)(((uint64_t)ik + (uint64_t)sk * brev(j, lvl_log - 1)) & IDX_MASK);
     uint32_t x = index_to_point(idx).x;
+    if (x == 0) atomicOr(zero_flag, 1u);  // "0 has no inverse" (fields/m31.rs:66)
     tw[pos] = x;
     itw[pos] = m31_inv(x);
   }
@@ -88,14 +90,28 @@ int32_t build_tree(stwo_coset root, cudaStream_t stream, TwiddleTree* t) {
   STWO_REQUIRE(root.log_size <= 30, "twiddle root log_size %u > 30", root.log_size);
   t->root = root;
   t->size = (size_t)1 << root.log_size;
-  STWO_CHECK_CUDA(cudaMalloc(&t->d_tw, t->size * 4));
+  STWO_CHECK_CUDA(cudaMalloc(&t->d_tw, t->size * 4 + 4));
   STWO_CHECK_CUDA(cudaMalloc(&t->d_itw, t->size * 4));
+  // One word past the twiddles flags an x-coordinate equal to 0: such a coset has no inverse
+  // twiddles and is rejected, as the reference panics on it.
+  uint32_t* flag = t->d_tw + t->size;
+  STWO_CHECK_CUDA(cudaMemsetAsync(flag, 0, 4, stream));
   uint32_t threads = 256;
   uint32_t blocks = (uint32_t)((t->size + threads - 1) / threads);
   if (blocks > 65535u) blocks = 65535u;
   k_twiddle_tree<<<blocks, threads, 0, stream>>>(root.initial_index, root.step_size, root.log_size, t->d_tw,
-                                                 t->d_itw); note_launch();
+                                                 t->d_itw, flag); note_launch();
   STWO_LAUNCH_CHECK();
+  uint32_t h_flag = 0;
+  STWO_CHECK_CUDA(cudaMemcpyAsync(&h_flag, flag, 4, cudaMemcpyDeviceToHost, stream));
+  STWO_CHECK_CUDA(cudaStreamSynchronize(stream));
+  if (h_flag) {
+    cudaFree(t->d_tw);
+    cudaFree(t->d_itw);
+    t->d_tw = t->d_itw = nullptr;
+    set_error("coset has a point with x = 0: 0 has no inverse");
+    return STWO_ERR_INVALID_ARG;
+  }
   return STWO_OK;
 }
 

@@ -34,7 +34,7 @@ def rand_point(oracle, rng):
 
 
 @pytest.mark.parametrize("root", [F.canonic_half(1), F.canonic_half(5), F.canonic_half(14),
-                                  (12345, 1 << 22, 9), (1 << 20, 1 << 21, 10)])
+                                  (12345, 1 << 22, 9), (3 << 18, 1 << 22, 9)])
 def test_twiddle_tree(cuda, oracle, root):
     import ctypes as C
 
@@ -229,6 +229,11 @@ def test_bit_reverse_and_extend(cuda):
 def test_invalid_arguments_return_status(cuda):
     from stwo_gb300 import _lib
     from stwo_gb300.backend import TwiddleTree
+
+    # A coset containing a point with x = 0 has no inverse twiddles (the reference panics).
+    with pytest.raises(_lib.StwoError) as e:
+        TwiddleTree(_lib.Coset(1 << 20, 1 << 21, 10))
+    assert e.value.status == 1
 
     t = TwiddleTree(_lib.Coset(*F.canonic_half(5)))
     # A domain that is not a doubling of the tree's root is rejected, not computed.
