@@ -211,7 +211,7 @@ def run_gb300(args):
     if world > 1:
         torch.distributed.barrier()
     _lib.call("stwo_device_init", local)
-    wl = KernelsWorkload()
+    wl = KernelsWorkload(n_cols=args.n_cols)
     lib = wl.lib
 
     def barrier():
@@ -375,6 +375,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-cols", type=int, default=0, help="columns of the kernel workload (default 256; "
+                    "smaller only for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -55,8 +55,10 @@ inline stwo_coset coset_double(stwo_coset c) {
   return {idx_reduce((uint64_t)c.initial_index * 2), idx_reduce((uint64_t)c.step_size * 2),
           c.log_size ? c.log_size - 1 : 0};
 }
+// Indices compare modulo 2^31 (a log-0 coset's step 2^31 equals a doubled step 0).
 inline bool coset_eq(stwo_coset a, stwo_coset b) {
-  return a.initial_index == b.initial_index && a.step_size == b.step_size && a.log_size == b.log_size;
+  return idx_reduce(a.initial_index) == idx_reduce(b.initial_index) &&
+         idx_reduce(a.step_size) == idx_reduce(b.step_size) && a.log_size == b.log_size;
 }
 inline bool coset_is_doubling_of(stwo_coset small, stwo_coset big) {
   if (small.log_size > big.log_size) return false;

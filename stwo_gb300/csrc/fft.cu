@@ -184,7 +184,15 @@ static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, c
   STWO_REQUIRE(tree, "null twiddle tree");
   STWO_REQUIRE(L <= 30, "domain log size %u > 30", L);
   STWO_REQUIRE(F <= L, "Can only evaluate on larger domains");
-  STWO_REQUIRE(coset_is_doubling_of(half, tree->root), "domain half coset is not a doubling of the twiddle root");
+  if (!coset_is_doubling_of(half, tree->root)) {
+    // Domains below 2^5 take their own twiddles, as the reference SIMD backend's CPU path for
+    // them does (backend/simd/circle.rs:137-140, 247-255); larger ones must match the tree.
+    STWO_REQUIRE(L < 5, "domain half coset is not a doubling of the twiddle root");
+    TwiddleTree* own = nullptr;
+    int32_t st = get_tree(half, s, &own);
+    if (st) return st;
+    tree = own;
+  }
   if (n_cols == 0) return STWO_OK;
 
   FftPass base{};
