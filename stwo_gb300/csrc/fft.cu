@@ -152,6 +152,135 @@ __global__ void __launch_bounds__(MAXT) k_fft_pass(FftPass p, ConstColPtrs src, 
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Specialised pass kernel: the tile shape (C contiguous low bits, NL layer bits) is a template
+// parameter, so every shared-memory offset and twiddle offset is an immediate and each
+// butterfly costs the field arithmetic plus ~1 issue slot of addressing. Requires L >= 3 (the
+// circle layer's twiddles come from the tree) and a tile of >= 2^4 words; other shapes use the
+// generic kernel above.
+
+template <bool INV, int C, int NL, int A, int RB>
+__device__ __forceinline__ void fft_round_ct(const FftPass& p, uint32_t* sm, uint32_t fixed_hi, uint32_t llo) {
+  constexpr int T = C + NL;
+  constexpr int THREADS = 1 << (T - 4);
+  constexpr int G = 1 << (T - RB);
+#pragma unroll
+  for (int it = 0; it < G / THREADS; it++) {
+    const uint32_t grp = threadIdx.x + it * THREADS;
+    const uint32_t base = (grp & ((1u << A) - 1)) | ((grp >> A) << (A + RB));
+    const uint32_t pb = base + (base >> 5);
+    uint32_t v[1 << RB];
+#pragma unroll
+    for (int k = 0; k < (1 << RB); k++) v[k] = sm[pb + (k << A) + ((k << A) >> 5)];
+#pragma unroll
+    for (int jj = 0; jj < RB; jj++) {
+      const int j = INV ? jj : (RB - 1 - jj);
+      const int lt = A + j - C;  // layer - lo
+      // Twiddle index of the pair group: (tile bits above the layer) | (fixed bits above the tile).
+      const uint32_t hb = (base >> (A + j + 1)) | (fixed_hi << (T - A - j - 1));
+      const bool circle = (lt == 0) && (C == 0) && (p.lo == 0);
+      const uint32_t* twp;
+      if (circle) twp = p.tw + (p.tw_size - (llo >> 1)) + (hb >> 1);
+      else twp = p.tw + (p.tw_size - (llo >> lt)) + hb;
+#pragma unroll
+      for (int kh = 0; kh < (1 << (RB - 1 - j)); kh++) {
+        uint32_t t;
+        if (circle) {
+          // [y, -y, -x, x] from the first line layer (cpu/circle.rs:209-229); the low bits of the
+          // pair index are kh, so the entry and the sign are compile-time.
+          uint32_t raw = __ldg(twp + ((kh >> 1) ^ 1));
+          t = ((kh ^ (kh >> 1)) & 1) ? m31_neg(raw) : raw;
+        } else {
+          t = __ldg(twp + kh);
+        }
+        const int k0 = kh << (j + 1);
+#pragma unroll
+        for (int kl = 0; kl < (1 << j); kl++) {
+          if (INV) ibfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+          else bfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < (1 << RB); k++) sm[pb + (k << A) + ((k << A) >> 5)] = v[k];
+  }
+  __syncthreads();
+}
+
+template <bool INV, int C, int NL, int TOP>
+__device__ __forceinline__ void fft_rounds_fwd(const FftPass& p, uint32_t* sm, uint32_t fixed_hi, uint32_t llo) {
+  if constexpr (TOP > C) {
+    constexpr int RB = (TOP - C) < 4 ? (TOP - C) : 4;
+    fft_round_ct<INV, C, NL, TOP - RB, RB>(p, sm, fixed_hi, llo);
+    fft_rounds_fwd<INV, C, NL, TOP - RB>(p, sm, fixed_hi, llo);
+  }
+}
+template <bool INV, int C, int NL, int BOT>
+__device__ __forceinline__ void fft_rounds_inv(const FftPass& p, uint32_t* sm, uint32_t fixed_hi, uint32_t llo) {
+  if constexpr (BOT < C + NL) {
+    constexpr int RB = (C + NL - BOT) < 4 ? (C + NL - BOT) : 4;
+    fft_round_ct<INV, C, NL, BOT, RB>(p, sm, fixed_hi, llo);
+    fft_rounds_inv<INV, C, NL, BOT + RB>(p, sm, fixed_hi, llo);
+  }
+}
+
+template <bool INV, int C, int NL>
+__global__ void __launch_bounds__(1 << (C + NL - 4)) k_fft_tile(FftPass p, ConstColPtrs src, ColPtrs dst) {
+  constexpr int T = C + NL;
+  constexpr int THREADS = 1 << (T - 4);
+  constexpr int PADW = THREADS + THREADS / 32;  // padded stride of consecutive thread rows
+  __shared__ uint32_t sm[(1 << T) + (1 << T) / 32 + 1];
+  const uint32_t col = blockIdx.y;
+  const uint32_t fixed = tile_fixed_bits(p, blockIdx.x);
+  const uint32_t fixed_hi = fixed >> (p.lo + NL);
+  const uint32_t llo = 1u << (p.L - p.lo);
+  const uint32_t* s = p.read_src ? src.p[col] : dst.p[col];
+  const uint32_t smask = p.read_src ? ((1u << p.F) - 1) : 0xffffffffu;
+  uint32_t* d = dst.p[col];
+  const uint32_t t = threadIdx.x;
+  const uint32_t pt = t + (t >> 5);
+  // Global index of element e = t + i * THREADS. When THREADS is a multiple of 2^C it is
+  // g_t + i * gstep; otherwise it is computed per element.
+  constexpr bool kStep = C <= T - 4;
+  const uint32_t gt = (t & ((1u << C) - 1)) | ((t >> C) << p.lo) | fixed;
+  const uint32_t gstep = kStep ? ((uint32_t)(THREADS >> C) << p.lo) : 0u;
+  auto gidx = [&](int i) -> uint32_t {
+    if constexpr (kStep) {
+      return gt + i * gstep;
+    } else {
+      uint32_t e = t + i * THREADS;
+      return (e & ((1u << C) - 1)) | ((e >> C) << p.lo) | fixed;
+    }
+  };
+#pragma unroll
+  for (int i = 0; i < 16; i++) sm[pt + i * PADW] = __ldg(&s[gidx(i) & smask]);
+  __syncthreads();
+  if (!INV) fft_rounds_fwd<INV, C, NL, C + NL>(p, sm, fixed_hi, llo);
+  else fft_rounds_inv<INV, C, NL, C>(p, sm, fixed_hi, llo);
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    uint32_t v = sm[pt + i * PADW];
+    if (p.scale != 1u) v = m31_mul(v, p.scale);
+    d[gidx(i)] = v;
+  }
+}
+
+// Launches the specialised kernel when one exists for (c, nl); returns false otherwise.
+template <bool INV>
+static bool launch_tile(const FftPass& p, dim3 grid, cudaStream_t s, const ConstColPtrs& sp, const ColPtrs& dp) {
+#define STWO_FFT_CASE(CC, NN)                                                          \
+  if (p.c == CC && p.nl == NN) {                                                       \
+    k_fft_tile<INV, CC, NN><<<grid, 1 << (CC + NN - 4), 0, s>>>(p, sp, dp);          \
+    return true;                                                                       \
+  }
+  STWO_FFT_CASE(0, 4) STWO_FFT_CASE(0, 5) STWO_FFT_CASE(0, 6) STWO_FFT_CASE(0, 7) STWO_FFT_CASE(0, 8)
+  STWO_FFT_CASE(0, 9) STWO_FFT_CASE(0, 10) STWO_FFT_CASE(0, 11) STWO_FFT_CASE(0, 12)
+  STWO_FFT_CASE(11, 1) STWO_FFT_CASE(10, 2) STWO_FFT_CASE(9, 3) STWO_FFT_CASE(8, 4) STWO_FFT_CASE(7, 5)
+  STWO_FFT_CASE(6, 6) STWO_FFT_CASE(5, 7) STWO_FFT_CASE(4, 8)
+#undef STWO_FFT_CASE
+  return false;
+}
+
 struct PassPlan {
   uint32_t lo, nl, c;
 };
@@ -166,10 +295,10 @@ static std::vector<PassPlan> plan_passes(uint32_t F) {
   uint32_t lo = low;
   while (lo < F) {
     uint32_t rem = F - lo;
-    uint32_t max_nl = FFT_TMAX_STRIDED - 3;  // c >= 3
+    uint32_t max_nl = FFT_TMAX - 4;  // rows of >= 16 contiguous words (64 bytes)
     uint32_t n_passes = (rem + max_nl - 1) / max_nl;
     uint32_t nl = (rem + n_passes - 1) / n_passes;
-    uint32_t c = (nl <= FFT_TMAX - 4) ? FFT_TMAX - nl : FFT_TMAX_STRIDED - nl;
+    uint32_t c = FFT_TMAX - nl;
     if (c > lo) c = lo;
     v.push_back({lo, nl, c});
     lo += nl;
@@ -237,7 +366,10 @@ static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, c
       uint32_t groups = (1u << p.T) >> std::min(FFT_R, p.T);
       uint32_t threads = std::max<uint32_t>(32, groups);
       size_t smem = ((size_t)(1u << p.T) + ((1u << p.T) >> 5) + 1) * 4;
-      if (threads <= 256) {
+      bool done = false;
+      if (L >= 3 && p.T >= 4) done = inverse ? launch_tile<true>(p, grid, s, sp, dp) : launch_tile<false>(p, grid, s, sp, dp);
+      if (done) {
+      } else if (threads <= 256) {
         if (inverse) k_fft_pass<true, 256><<<grid, threads, smem, s>>>(p, sp, dp);
         else k_fft_pass<false, 256><<<grid, threads, smem, s>>>(p, sp, dp);
       } else {

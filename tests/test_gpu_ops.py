@@ -55,7 +55,7 @@ def test_twiddle_tree(cuda, oracle, root):
     assert np.array_equal(igot, itw)
 
 
-@pytest.mark.parametrize("log", [1, 2, 3, 4, 5, 6, 8, 12, 13, 14, 16, 17, 20])
+@pytest.mark.parametrize("log", [1, 2, 3, 4, 5, 6, 7, 8, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22])
 def test_interpolate(cuda, oracle, log):
     from stwo_gb300 import _lib
     from stwo_gb300.backend import TwiddleTree
