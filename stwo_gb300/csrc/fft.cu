@@ -186,10 +186,17 @@ __device__ __forceinline__ void fft_round_ct(const FftPass& p, uint32_t* sm, uin
       for (int kh = 0; kh < (1 << (RB - 1 - j)); kh++) {
         uint32_t t;
         if (circle) {
-          // [y, -y, -x, x] from the first line layer (cpu/circle.rs:209-229); the low bits of the
-          // pair index are kh, so the entry and the sign are compile-time.
-          uint32_t raw = __ldg(twp + ((kh >> 1) ^ 1));
-          t = ((kh ^ (kh >> 1)) & 1) ? m31_neg(raw) : raw;
+          // [y, -y, -x, x] from the first line layer (cpu/circle.rs:209-229). In a round of >= 3
+          // bits the low two bits of the pair index are those of kh: entry and sign are
+          // compile-time; otherwise they come from the full index.
+          if (RB - 1 - j >= 2) {
+            uint32_t raw = __ldg(twp + ((kh >> 1) ^ 1));
+            t = ((kh ^ (kh >> 1)) & 1) ? m31_neg(raw) : raw;
+          } else {
+            const uint32_t h = hb + kh;
+            uint32_t raw = __ldg(p.tw + (p.tw_size - (llo >> 1)) + ((h >> 1) ^ 1));
+            t = ((h ^ (h >> 1)) & 1) ? m31_neg(raw) : raw;
+          }
         } else {
           t = __ldg(twp + kh);
         }
@@ -210,7 +217,9 @@ __device__ __forceinline__ void fft_round_ct(const FftPass& p, uint32_t* sm, uin
 template <bool INV, int C, int NL, int TOP>
 __device__ __forceinline__ void fft_rounds_fwd(const FftPass& p, uint32_t* sm, uint32_t fixed_hi, uint32_t llo) {
   if constexpr (TOP > C) {
-    constexpr int RB = (TOP - C) < 4 ? (TOP - C) : 4;
+    // The partial round (if NL is not a multiple of 4) goes first, at the top, so that the
+    // lowest round is always a full 4-layer one.
+    constexpr int RB = ((TOP - C - 1) % 4) + 1;
     fft_round_ct<INV, C, NL, TOP - RB, RB>(p, sm, fixed_hi, llo);
     fft_rounds_fwd<INV, C, NL, TOP - RB>(p, sm, fixed_hi, llo);
   }
@@ -252,14 +261,19 @@ __global__ void __launch_bounds__(1 << (C + NL - 4)) k_fft_tile(FftPass p, Const
       return (e & ((1u << C) - 1)) | ((e >> C) << p.lo) | fixed;
     }
   };
+  // Padded shared-memory slot of element t + i * THREADS.
+  auto sidx = [&](int i) -> uint32_t {
+    if constexpr (THREADS >= 32) return pt + i * PADW;
+    else return pad_idx(t + i * THREADS);
+  };
 #pragma unroll
-  for (int i = 0; i < 16; i++) sm[pt + i * PADW] = __ldg(&s[gidx(i) & smask]);
+  for (int i = 0; i < 16; i++) sm[sidx(i)] = __ldg(&s[gidx(i) & smask]);
   __syncthreads();
   if (!INV) fft_rounds_fwd<INV, C, NL, C + NL>(p, sm, fixed_hi, llo);
   else fft_rounds_inv<INV, C, NL, C>(p, sm, fixed_hi, llo);
 #pragma unroll
   for (int i = 0; i < 16; i++) {
-    uint32_t v = sm[pt + i * PADW];
+    uint32_t v = sm[sidx(i)];
     if (p.scale != 1u) v = m31_mul(v, p.scale);
     d[gidx(i)] = v;
   }
