@@ -165,3 +165,53 @@ void oracle_index_to_point(uint32_t idx, uint32_t out[2]) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- proofs
+#include "air_wide_fib.h"
+
+extern "C" {
+
+// Proves the wide-Fibonacci AIR (log_n rows, n_cols columns, row r starting from (a[r], b[r])) as
+// the reference's test_wide_fib_prove_with_blake does; writes the canonical proof bytes.
+// Returns the proof length, or 0 on failure (message in err).
+size_t oracle_prove_wide_fib(uint32_t log_n, uint32_t n_cols, const uint32_t* a, const uint32_t* b,
+                             const uint32_t cfg[4], uint8_t* out, size_t cap, char* err, size_t err_cap) {
+  try {
+    PcsConfig config{cfg[0], cfg[1], cfg[2], cfg[3]};
+    TwiddleTree tw = precompute_twiddles(canonic_domain(log_n + 1 + config.log_blowup).half_coset);
+    Channel ch;
+    CommitmentSchemeProver pcs;
+    pcs.config = config;
+    pcs.twiddles = &tw;
+    pcs.commit({}, ch);
+    pcs.commit_evals(wide_fib_trace(log_n, n_cols, a, b), log_n, ch);
+    WideFibAir air(log_n, n_cols);
+    StarkProof proof = prove(air, ch, pcs);
+    std::vector<uint8_t> bytes = serialize(proof);
+    if (bytes.size() > cap) throw std::runtime_error("output buffer too small");
+    std::memcpy(out, bytes.data(), bytes.size());
+    return bytes.size();
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+// Verifies canonical proof bytes of the wide-Fibonacci AIR; returns 1 when accepted.
+int oracle_verify_wide_fib(uint32_t log_n, uint32_t n_cols, const uint8_t* proof, size_t len, char* err,
+                           size_t err_cap) {
+  try {
+    StarkProof p;
+    if (!deserialize(proof, len, p)) throw std::runtime_error("malformed proof bytes");
+    Channel ch;
+    WideFibAir air(log_n, n_cols);
+    std::string r = verify(air, ch, p, {{}, std::vector<uint32_t>(n_cols, log_n)});
+    if (!r.empty()) throw std::runtime_error(r);
+    return 1;
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+}  // extern "C"

@@ -178,3 +178,27 @@ def index_to_point(idx):
     out = np.zeros(2, np.uint32)
     lib().oracle_index_to_point(C.c_uint32(idx), _p(out))
     return int(out[0]), int(out[1])
+
+
+def prove_wide_fib(log_n, n_cols, a, b, config=(5, 1, 0, 3)):
+    """Canonical proof bytes of the wide-Fibonacci AIR (oracle prover)."""
+    a, b = _u32(a), _u32(b)
+    cap = 64 << 20
+    out = np.zeros(cap, np.uint8)
+    err = C.create_string_buffer(512)
+    f = lib().oracle_prove_wide_fib
+    f.restype = C.c_size_t
+    n = f(C.c_uint32(log_n), C.c_uint32(n_cols), _p(a), _p(b), _p(_u32(config)), _p(out), C.c_size_t(cap), err,
+          C.c_size_t(512))
+    if n == 0:
+        raise RuntimeError("oracle prove failed: " + err.value.decode())
+    return bytes(out[:n])
+
+
+def verify_wide_fib(log_n, n_cols, proof: bytes):
+    """(accepted, reason) for canonical proof bytes of the wide-Fibonacci AIR."""
+    buf = np.frombuffer(proof, dtype=np.uint8).copy()
+    err = C.create_string_buffer(512)
+    ok = lib().oracle_verify_wide_fib(C.c_uint32(log_n), C.c_uint32(n_cols), _p(buf), C.c_size_t(len(proof)), err,
+                                      C.c_size_t(512))
+    return bool(ok), err.value.decode()

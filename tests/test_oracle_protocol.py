@@ -1,0 +1,37 @@
+"""The oracle's prover and verifier agree (CPU): wide-Fibonacci proofs at the reference test's
+sizes (crates/prover/src/examples/wide_fibonacci/mod.rs:174-227, log 2..6 with inputs a = 1,
+b = row index) are accepted, and tampered proofs are rejected."""
+import numpy as np
+import pytest
+
+
+@pytest.mark.parametrize("log_n", [2, 3, 4, 5, 6, 8])
+def test_wide_fib_prove_verify(oracle, log_n):
+    n = 1 << log_n
+    a = np.ones(n, np.uint32)
+    b = np.arange(n, dtype=np.uint32)
+    proof = oracle.prove_wide_fib(log_n, 100, a, b)
+    ok, why = oracle.verify_wide_fib(log_n, 100, proof)
+    assert ok, why
+
+
+def test_wide_fib_tampered_proofs_rejected(oracle):
+    n = 1 << 5
+    proof = oracle.prove_wide_fib(5, 100, np.ones(n, np.uint32), np.arange(n, dtype=np.uint32))
+    rng = np.random.default_rng(0)
+    for pos in rng.integers(0, len(proof), size=12):
+        bad = bytearray(proof)
+        bad[int(pos)] ^= 0x04
+        ok, _ = oracle.verify_wide_fib(5, 100, bytes(bad))
+        assert not ok, int(pos)
+    assert not oracle.verify_wide_fib(5, 100, proof[:-1])[0]
+
+
+def test_wide_fib_other_configs(oracle):
+    n = 1 << 6
+    a = np.full(n, 7, np.uint32)
+    b = (np.arange(n, dtype=np.uint32) * 13) % ((1 << 31) - 1)
+    for cfg in [(0, 1, 0, 3), (8, 2, 1, 5), (5, 1, 2, 10)]:
+        proof = oracle.prove_wide_fib(6, 40, a, b, cfg)
+        ok, why = oracle.verify_wide_fib(6, 40, proof)
+        assert ok, (cfg, why)
