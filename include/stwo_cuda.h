@@ -158,6 +158,29 @@ stwo_status stwo_generate_secure_powers(stwo_qm31 felt, uint32_t n_powers, stwo_
  * (digest, [nonce_lo, nonce_hi, 0...]) has >= pow_bits trailing zeros in word 0. */
 stwo_status stwo_grind_blake2s(const uint32_t h_digest[8], uint32_t pow_bits, uint64_t* h_nonce, void* stream);
 
+/* ------------------------------------------------------------------ proving */
+/* PcsConfig { pow_bits, fri_config: FriConfig { log_last_layer_degree_bound, log_blowup_factor,
+ * n_queries } } (crates/prover/src/core/pcs/mod.rs:33-59, fri.rs:37-70). */
+typedef struct {
+  uint32_t pow_bits;
+  uint32_t log_blowup_factor;
+  uint32_t log_last_layer_degree_bound;
+  uint32_t n_queries;
+} stwo_pcs_config;
+
+/* generate_trace of the wide-Fibonacci example (crates/prover/src/examples/wide_fibonacci/mod.rs:46-68):
+ * row r of the n_cols device columns starts from (d_a[r], d_b[r]). */
+stwo_status stwo_gen_wide_fib_trace(uint32_t log_n_rows, uint32_t n_cols, const uint32_t* d_a, const uint32_t* d_b,
+                                    uint32_t* const* d_cols, void* stream);
+/* prove::<CudaBackend, Blake2sMerkleChannel> (crates/prover/src/core/prover/mod.rs:27-79) of the
+ * wide-Fibonacci AIR, with an empty preprocessed tree and the trace committed as in
+ * test_wide_fib_prove_with_blake (wide_fibonacci/mod.rs:174-227). The trace columns (bit-reversed
+ * evaluations) are consumed: they hold the trace coefficients afterwards. Writes the canonical
+ * proof bytes (u32 words and u64 lengths little-endian, fields in StarkProof order) to h_proof and
+ * their count to *h_len (also when the buffer is too small, which returns INVALID_ARG). */
+stwo_status stwo_prove_wide_fib(uint32_t log_n_rows, uint32_t n_cols, uint32_t* const* d_trace, stwo_pcs_config cfg,
+                                uint8_t* h_proof, size_t capacity, size_t* h_len, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

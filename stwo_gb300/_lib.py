@@ -32,6 +32,11 @@ class QM31Point(C.Structure):
     _fields_ = [("x", QM31), ("y", QM31)]
 
 
+class PcsConfig(C.Structure):
+    _fields_ = [("pow_bits", C.c_uint32), ("log_blowup_factor", C.c_uint32),
+                ("log_last_layer_degree_bound", C.c_uint32), ("n_queries", C.c_uint32)]
+
+
 class SampleBatch(C.Structure):
     _fields_ = [
         ("point", QM31Point),
@@ -76,6 +81,8 @@ SIGNATURES = {
     "stwo_secure_accumulate": (C.c_int32, [PVP, PVP, C.c_size_t, VP]),
     "stwo_generate_secure_powers": (C.c_int32, [QM31, U32, C.POINTER(QM31), VP]),
     "stwo_grind_blake2s": (C.c_int32, [C.POINTER(C.c_uint32), U32, C.POINTER(C.c_uint64), VP]),
+    "stwo_gen_wide_fib_trace": (C.c_int32, [U32, U32, VP, VP, PVP, VP]),
+    "stwo_prove_wide_fib": (C.c_int32, [U32, U32, PVP, PcsConfig, VP, C.c_size_t, C.POINTER(C.c_size_t), VP]),
 }
 
 _lib = None

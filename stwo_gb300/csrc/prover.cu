@@ -1,0 +1,721 @@
+// GPU prover host: prove() of the reference (crates/prover/src/core/prover/mod.rs:27-79) over this
+// backend, with every O(trace) stage on the device:
+//   commitment trees  pcs/prover.rs:208-227  (FFT extension + Blake2s Merkle, trees kept in HBM)
+//   composition       air/components.rs:122-137, constraint_framework/component.rs:278-416
+//                     (one constraint kernel per AIR; accumulation, denominators, interpolation)
+//   opening           pcs/prover.rs:83-148 (batched eval_at_point, quotients per log size)
+//   FRI               fri.rs:168-336 (folds and layer Merkle trees on the device)
+//   decommitment      vcs/prover.rs:80-149 and fri.rs:295-336: query positions and witness
+//                     structure are computed on the host, the words themselves are gathered from
+//                     HBM in one kernel launch
+// The transcript (Blake2s channel) and the O(1)-size last FRI layer interpolation stay on the host,
+// as in the reference. Proofs are written in the canonical byte form (little-endian u32 words,
+// u64 lengths, struct order).
+#include "common.cuh"
+#include "host_channel.h"
+#include "prover.cuh"
+#include <set>
+
+namespace stwo {
+
+int32_t fft_interpolate(const TwiddleTree* tree, stwo_coset half, uint32_t* const* cols, uint32_t n, cudaStream_t s);
+int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* const* coeffs, uint32_t coeff_log,
+                     uint32_t* const* out, uint32_t n, cudaStream_t s);
+int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols, uint32_t n_cols,
+                            uint32_t* out, cudaStream_t s);
+int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, stwo_qm31 rc_in,
+                             const stwo_sample_batch* batches, uint32_t n_batches, uint32_t log_blowup,
+                             uint32_t* const out[4], cudaStream_t s);
+int32_t fri_fold_line(const TwiddleTree* tree, stwo_coset line_domain, const uint32_t* const src[4], qm31 alpha,
+                      uint32_t* const out[4], cudaStream_t s);
+int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* const dst[4], const uint32_t* const src[4],
+                        qm31 alpha, cudaStream_t s);
+int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
+                       const uint32_t* poly_of, const stwo_qm31_point* points, uint32_t n_evals, stwo_qm31* out,
+                       cudaStream_t s);
+
+// ------------------------------------------------------------------------------------------------
+Arena::~Arena() {
+  for (void* p : ptrs) cudaFreeAsync(p, s);
+}
+uint32_t* Arena::alloc(size_t words) {
+  void* p = nullptr;
+  if (cudaMallocAsync(&p, std::max<size_t>(words, 1) * 4, s) != cudaSuccess) {
+    failed = true;
+    return nullptr;
+  }
+  ptrs.push_back(p);
+  return reinterpret_cast<uint32_t*>(p);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Gather of words from HBM: each request is (device pointer, element index), 1 or 8 words.
+__global__ void k_gather(const unsigned long long* ptr, const unsigned long long* idx, uint32_t n, uint32_t words,
+                         uint32_t* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t* p = reinterpret_cast<const uint32_t*>(ptr[i]) + idx[i] * words;
+  for (uint32_t w = 0; w < words; w++) out[(size_t)i * words + w] = p[w];
+}
+
+int32_t Gather::run(cudaStream_t s) {
+  for (int kind = 0; kind < 2; kind++) {
+    auto& ptr = kind ? hptr : vptr;
+    auto& idx = kind ? hidx : vidx;
+    auto& res = kind ? hres : vres;
+    uint32_t words = kind ? 8 : 1;
+    size_t n = ptr.size();
+    res.assign(n * words, 0);
+    if (!n) continue;
+    char* buf = nullptr;
+    int32_t st = scratch_alloc((void**)&buf, n * 16 + n * words * 4, s);
+    if (st) return st;
+    unsigned long long* dptr = reinterpret_cast<unsigned long long*>(buf);
+    unsigned long long* didx = dptr + n;
+    uint32_t* dout = reinterpret_cast<uint32_t*>(didx + n);
+    cudaError_t e = cudaMemcpyAsync(dptr, ptr.data(), n * 8, cudaMemcpyHostToDevice, s);
+    if (!e) e = cudaMemcpyAsync(didx, idx.data(), n * 8, cudaMemcpyHostToDevice, s);
+    if (!e) {
+      k_gather<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>(dptr, didx, (uint32_t)n, words, dout);
+      note_launch();
+      e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpyAsync(res.data(), dout, n * words * 4, cudaMemcpyDeviceToHost, s);
+    if (!e) e = cudaStreamSynchronize(s);
+    scratch_free(buf, s);
+    if (e) {
+      set_error("gather: %s", cudaGetErrorString(e));
+      return STWO_ERR_CUDA;
+    }
+  }
+  return STWO_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+static uint32_t ilog2u(size_t n) {
+  uint32_t l = 0;
+  while (((size_t)1 << (l + 1)) <= n) l++;
+  return l;
+}
+
+int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s) {
+  sorted = columns;
+  std::stable_sort(sorted.begin(), sorted.end(), [](const ColRef& a, const ColRef& b) { return a.log > b.log; });
+  uint32_t max_log = sorted.empty() ? 0 : sorted[0].log;
+  layers.assign(max_log + 1, nullptr);
+  size_t ci = 0;
+  for (int lg = (int)max_log; lg >= 0; lg--) {
+    std::vector<const uint32_t*> lc;
+    while (ci < sorted.size() && sorted[ci].log == (uint32_t)lg) lc.push_back(sorted[ci++].p);
+    layers[lg] = arena.alloc((size_t)8 << lg);
+    if (!layers[lg]) return STWO_ERR_OOM;
+    const uint32_t* prev = (uint32_t)lg < max_log ? layers[lg + 1] : nullptr;
+    int32_t st = merkle_commit_layer((uint32_t)lg, prev, lc.data(), (uint32_t)lc.size(), layers[lg], s);
+    if (st) return st;
+  }
+  uint32_t w[8];
+  STWO_CHECK_CUDA(cudaMemcpyAsync(w, layers[0], 32, cudaMemcpyDeviceToHost, s));
+  STWO_CHECK_CUDA(cudaStreamSynchronize(s));
+  root = Digest::from_words(w);
+  return STWO_OK;
+}
+
+// vcs/prover.rs:80-149, recording gather requests instead of reading values.
+void DevMerkle::decommit(const std::map<uint32_t, std::vector<size_t>>& queries, Gather& g, DecommitRecipe& out) const {
+  size_t ci = 0;
+  std::vector<size_t> last;
+  static const std::vector<size_t> empty;
+  for (int lg = (int)layers.size() - 1; lg >= 0; lg--) {
+    std::vector<const uint32_t*> lc;
+    while (ci < sorted.size() && sorted[ci].log == (uint32_t)lg) lc.push_back(sorted[ci++].p);
+    const uint32_t* prev = (size_t)lg + 1 < layers.size() ? layers[lg + 1] : nullptr;
+    auto it = queries.find((uint32_t)lg);
+    const std::vector<size_t>& cq = it == queries.end() ? empty : it->second;
+    std::vector<size_t> total;
+    size_t pi = 0, qi = 0;
+    while (true) {
+      bool have = false;
+      size_t node = 0;
+      if (pi < last.size()) { node = last[pi] / 2; have = true; }
+      if (qi < cq.size()) { node = have ? std::min(node, cq[qi]) : cq[qi]; have = true; }
+      if (!have) break;
+      if (prev) {
+        if (pi < last.size() && last[pi] == 2 * node) pi++;
+        else out.hash_witness.push_back(g.hash(prev, 2 * node));
+        if (pi < last.size() && last[pi] == 2 * node + 1) pi++;
+        else out.hash_witness.push_back(g.hash(prev, 2 * node + 1));
+      }
+      bool q = qi < cq.size() && cq[qi] == node;
+      if (q) qi++;
+      for (auto* c : lc) (q ? out.queried : out.column_witness).push_back(g.val(c, node));
+      total.push_back(node);
+    }
+    last = total;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Canonical proof bytes (same layout as the oracle's serialiser).
+struct ByteWriter {
+  std::vector<uint8_t> b;
+  void u32(uint32_t v) { for (int i = 0; i < 4; i++) b.push_back((uint8_t)(v >> (8 * i))); }
+  void u64(uint64_t v) { for (int i = 0; i < 8; i++) b.push_back((uint8_t)(v >> (8 * i))); }
+  void digest(const Digest& d) { b.insert(b.end(), d.b, d.b + 32); }
+  void q(const hq& x) { for (int i = 0; i < 4; i++) u32(x.v[i]); }
+  void hashes(const std::vector<size_t>& idx, const Gather& g) {
+    u64(idx.size());
+    for (size_t i : idx) {
+      uint32_t w[8];
+      for (int k = 0; k < 8; k++) w[k] = g.hres[8 * i + k];
+      digest(Digest::from_words(w));
+    }
+  }
+  void vals(const std::vector<size_t>& idx, const Gather& g) {
+    u64(idx.size());
+    for (size_t i : idx) u32(g.vres[i]);
+  }
+  void dec(const DecommitRecipe& d, const Gather& g) {
+    hashes(d.hash_witness, g);
+    vals(d.column_witness, g);
+  }
+};
+
+// ------------------------------------------------------------------------------------------------
+struct Queries {
+  std::vector<size_t> pos;
+  uint32_t log = 0;
+  Queries fold(uint32_t n) const {
+    Queries q;
+    q.log = log - n;
+    for (size_t p : pos) {
+      size_t v = p >> n;
+      if (q.pos.empty() || q.pos.back() != v) q.pos.push_back(v);
+    }
+    return q;
+  }
+};
+static Queries generate_queries(HostChannel& ch, uint32_t log, uint32_t n_queries) {
+  std::set<size_t> qs;
+  uint32_t cnt = 0;
+  uint32_t mask = (uint32_t)((1ull << log) - 1);
+  while (true) {
+    Digest d = ch.draw_random_bytes();
+    uint32_t w[8];
+    d.words(w);
+    for (int i = 0; i < 8; i++) {
+      qs.insert(w[i] & mask);
+      if (++cnt == n_queries) return Queries{std::vector<size_t>(qs.begin(), qs.end()), log};
+    }
+  }
+}
+
+// Decommitment positions and witness requests of a 2-folding layer (fri.rs:943-976).
+static void fri_positions_and_witness(const SecureCols& col, const std::vector<size_t>& queries, Gather& g,
+                                      std::vector<size_t>& positions, std::vector<size_t>& witness) {
+  size_t i = 0;
+  while (i < queries.size()) {
+    size_t start = (queries[i] >> 1) << 1;
+    size_t j = i;
+    while (j < queries.size() && (queries[j] >> 1) == (queries[i] >> 1)) j++;
+    size_t k = i;
+    for (size_t pos = start; pos < start + 2; pos++) {
+      positions.push_back(pos);
+      if (k < j && queries[k] == pos) {
+        k++;
+        continue;
+      }
+      for (int c = 0; c < 4; c++) witness.push_back(g.val(col.c[c], pos));
+    }
+    i = j;
+  }
+}
+
+static qm31 to_dq(hq x) { return {{x.v[0], x.v[1]}, {x.v[2], x.v[3]}}; }
+static stwo_qm31 to_sq(hq x) { stwo_qm31 r; for (int i = 0; i < 4; i++) r.v[i] = x.v[i]; return r; }
+static hq from_sq(const stwo_qm31& x) { return hq_make(x.v[0], x.v[1], x.v[2], x.v[3]); }
+
+// Circle point over QM31 on the host.
+struct HPointQ { hq x, y; };
+static HPointQ hpq_add_m31(const HPointQ& a, hpoint b) {
+  hq bx = hq_make(b.x, 0, 0, 0), by = hq_make(b.y, 0, 0, 0);
+  return {hq_sub(hq_mul(a.x, bx), hq_mul(a.y, by)), hq_add(hq_mul(a.x, by), hq_mul(a.y, bx))};
+}
+static bool hpq_less(const HPointQ& a, const HPointQ& b) {
+  for (int i = 0; i < 4; i++) if (a.x.v[i] != b.x.v[i]) return a.x.v[i] < b.x.v[i];
+  for (int i = 0; i < 4; i++) if (a.y.v[i] != b.y.v[i]) return a.y.v[i] < b.y.v[i];
+  return false;
+}
+static bool hpq_eq(const HPointQ& a, const HPointQ& b) { return !hpq_less(a, b) && !hpq_less(b, a); }
+static hq hq_inv(hq x) {
+  // (a + bu)^-1 = (a - bu) / (a^2 - (2+i) b^2), CM31 inverse via the norm (fields/qm31.rs:121-129).
+  uint32_t b2r, b2i, a2r, a2i;
+  h_cmul(x.v[2], x.v[3], x.v[2], x.v[3], &b2r, &b2i);
+  h_cmul(x.v[0], x.v[1], x.v[0], x.v[1], &a2r, &a2i);
+  uint32_t rb_r = h_sub(h_add(b2r, b2r), b2i), rb_i = h_add(b2r, h_add(b2i, b2i));
+  uint32_t dr = h_sub(a2r, rb_r), di = h_sub(a2i, rb_i);
+  uint32_t nrm = h_inv(h_add(h_mul(dr, dr), h_mul(di, di)));
+  uint32_t ir = h_mul(dr, nrm), ii = h_mul(h_sub(0, di), nrm);
+  uint32_t r0, r1, r2, r3;
+  h_cmul(x.v[0], x.v[1], ir, ii, &r0, &r1);
+  h_cmul(h_sub(0, x.v[2]), h_sub(0, x.v[3]), ir, ii, &r2, &r3);
+  return hq_make(r0, r1, r2, r3);
+}
+static HPointQ random_point(HostChannel& ch) {
+  hq t = ch.draw_felt();
+  hq t2 = hq_mul(t, t);
+  hq d = hq_inv(hq_add(t2, hq_make(1, 0, 0, 0)));
+  return {hq_mul(hq_sub(hq_make(1, 0, 0, 0), t2), d), hq_mul(hq_add(t, t), d)};
+}
+
+// ------------------------------------------------------------------------------------------------
+// Commitment scheme prover state on the device.
+struct Tree {
+  std::vector<uint32_t*> polys;     // device coefficient columns
+  std::vector<uint32_t> poly_logs;
+  std::vector<uint32_t*> evals;     // device evaluations on the blown-up canonic domains
+  std::vector<uint32_t> eval_logs;
+  DevMerkle merkle;
+};
+
+int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t> logs) {
+  trees.emplace_back();
+  Tree& t = trees.back();
+  t.polys = std::move(polys);
+  t.poly_logs = std::move(logs);
+  std::vector<ColRef> refs;
+  // Evaluate all polynomials of the same log size in one batched call.
+  std::map<uint32_t, std::vector<size_t>> by_log;
+  for (size_t i = 0; i < t.polys.size(); i++) by_log[t.poly_logs[i]].push_back(i);
+  t.evals.assign(t.polys.size(), nullptr);
+  t.eval_logs.assign(t.polys.size(), 0);
+  for (auto& kv : by_log) {
+    uint32_t el = kv.first + cfg.log_blowup_factor;
+    std::vector<const uint32_t*> src;
+    std::vector<uint32_t*> dst;
+    for (size_t i : kv.second) {
+      t.evals[i] = arena.alloc((size_t)1 << el);
+      if (!t.evals[i]) return STWO_ERR_OOM;
+      t.eval_logs[i] = el;
+      src.push_back(t.polys[i]);
+      dst.push_back(t.evals[i]);
+    }
+    int32_t st = fft_evaluate(tree, canonic_half_coset(el), src.data(), kv.first, dst.data(), (uint32_t)src.size(), s);
+    if (st) return st;
+  }
+  for (size_t i = 0; i < t.evals.size(); i++) refs.push_back({t.evals[i], t.eval_logs[i]});
+  int32_t st = t.merkle.commit(refs, arena, s);
+  if (st) return st;
+  ch.mix_root(t.merkle.root);
+  return STWO_OK;
+}
+
+int32_t Prover::commit_evals(const std::vector<uint32_t*>& cols, uint32_t log_size) {
+  // Interpolate in place (the evaluation is consumed, as PolyOps::interpolate takes it by value).
+  if (!cols.empty()) {
+    int32_t st = fft_interpolate(tree, canonic_half_coset(log_size), cols.data(), (uint32_t)cols.size(), s);
+    if (st) return st;
+  }
+  return commit_polys(cols, std::vector<uint32_t>(cols.size(), log_size));
+}
+
+Prover::Prover(const stwo_pcs_config& c, uint32_t max_log, cudaStream_t st) : cfg(c), s(st), arena(st) {
+  init_status = get_tree(canonic_half_coset(max_log), s, &tree);
+}
+Prover::~Prover() = default;
+
+// Composition polynomial (air/accumulation.rs:49-149 for one component): the AIR kernel
+// accumulates row_res * denom_inv on the evaluation domain; the four coordinate columns are then
+// interpolated and committed as a tree.
+int32_t Prover::commit_composition(const GpuAir& air, hq rc) {
+  uint32_t eval_log = air.max_constraint_log_degree_bound();
+  uint32_t trace_log = air.log_size();
+  size_t n = air.n_constraints();
+  // Random coefficient powers, highest first: constraint k gets rc^(n-1-k).
+  std::vector<uint32_t> coeffs(4 * n);
+  hq p = hq_make(1, 0, 0, 0);
+  for (size_t k = 0; k < n; k++) {
+    for (int i = 0; i < 4; i++) coeffs[4 * (n - 1 - k) + i] = p.v[i];
+    p = hq_mul(p, rc);
+  }
+  // Denominator inverses: 1 / coset_vanishing(trace coset, eval_domain.at(i)), bit-reversed.
+  uint32_t expand = eval_log - trace_log;
+  std::vector<uint32_t> dinv((size_t)1 << expand);
+  {
+    stwo_coset tc = coset_new(1u << (31 - (trace_log + 1)), trace_log);  // Coset::odds(trace_log)
+    hpoint init = h_index_to_point(tc.initial_index);
+    hpoint half = h_index_to_point(tc.step_size >> 1);
+    hpoint shift = h_padd({init.x, h_sub(0, init.y)}, half);
+    stwo_coset eh = canonic_half_coset(eval_log);
+    for (size_t i = 0; i < dinv.size(); i++) {
+      uint32_t idx = idx_reduce((uint64_t)eh.initial_index + (uint64_t)eh.step_size * i);  // i < half size
+      hpoint pt = h_padd(h_index_to_point(idx), shift);
+      uint32_t x = pt.x;
+      for (uint32_t k = 1; k < trace_log; k++) x = h_sub(h_add(h_mul(x, x), h_mul(x, x)), 1);
+      dinv[i] = h_inv(x);
+    }
+    // bit-reverse
+    uint32_t lb = expand;
+    std::vector<uint32_t> tmp(dinv.size());
+    for (size_t i = 0; i < dinv.size(); i++) {
+      size_t r = 0;
+      for (uint32_t b = 0; b < lb; b++) r |= ((i >> b) & 1) << (lb - 1 - b);
+      tmp[r] = dinv[i];
+    }
+    dinv.swap(tmp);
+  }
+  uint32_t* d_coeffs = arena.alloc(coeffs.size() + dinv.size());
+  if (!d_coeffs) return STWO_ERR_OOM;
+  uint32_t* d_dinv = d_coeffs + coeffs.size();
+  STWO_CHECK_CUDA(cudaMemcpyAsync(d_coeffs, coeffs.data(), coeffs.size() * 4, cudaMemcpyHostToDevice, s));
+  STWO_CHECK_CUDA(cudaMemcpyAsync(d_dinv, dinv.data(), dinv.size() * 4, cudaMemcpyHostToDevice, s));
+  // Trace columns on the evaluation domain, per tree (extension when the committed domain differs).
+  std::vector<std::vector<const uint32_t*>> tcols(trees.size());
+  for (size_t ti = 0; ti < trees.size(); ti++) {
+    Tree& t = trees[ti];
+    std::vector<const uint32_t*> src;
+    std::vector<uint32_t*> ext;
+    for (size_t c = 0; c < t.evals.size(); c++) {
+      if (t.eval_logs[c] == eval_log) {
+        tcols[ti].push_back(t.evals[c]);
+      } else {
+        uint32_t* e = arena.alloc((size_t)1 << eval_log);
+        if (!e) return STWO_ERR_OOM;
+        src.push_back(t.polys[c]);
+        ext.push_back(e);
+        tcols[ti].push_back(e);
+      }
+    }
+    if (!src.empty()) {
+      // All columns of a component share one log size.
+      int32_t st = fft_evaluate(tree, canonic_half_coset(eval_log), src.data(), t.poly_logs[0], ext.data(),
+                                (uint32_t)src.size(), s);
+      if (st) return st;
+    }
+  }
+  uint32_t* acc[4];
+  for (int k = 0; k < 4; k++) {
+    acc[k] = arena.alloc((size_t)1 << eval_log);
+    if (!acc[k]) return STWO_ERR_OOM;
+  }
+  int32_t st = air.eval_composition(tcols, d_coeffs, d_dinv, acc, s);
+  if (st) return st;
+  st = fft_interpolate(tree, canonic_half_coset(eval_log), acc, 4, s);
+  if (st) return st;
+  return commit_polys({acc[0], acc[1], acc[2], acc[3]}, std::vector<uint32_t>(4, eval_log));
+}
+
+static void write_config(ByteWriter& w, const stwo_pcs_config& c) {
+  w.u32(c.pow_bits);
+  w.u32(c.log_blowup_factor);
+  w.u32(c.log_last_layer_degree_bound);
+  w.u64(c.n_queries);
+}
+
+int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
+  // Composition polynomial and OODS point (prover/mod.rs:41-61).
+  hq rc = ch.draw_felt();
+  int32_t st = commit_composition(air, rc);
+  if (st) return st;
+  HPointQ oods = random_point(ch);
+
+  // Sample points: mask offsets of the AIR, then four times the OODS point for the composition.
+  auto mask = air.mask_offsets();
+  std::vector<std::vector<std::vector<HPointQ>>> pts(trees.size());
+  uint32_t step = 1u << (31 - air.log_size());
+  for (size_t t = 0; t + 1 < trees.size(); t++) {
+    pts[t].resize(trees[t].polys.size());
+    if (t == 0 || t >= mask.size()) continue;
+    for (size_t c = 0; c < mask[t].size(); c++)
+      for (int off : mask[t][c]) {
+        uint32_t idx = idx_reduce((uint64_t)step * (uint64_t)(off >= 0 ? off : -off));
+        if (off < 0) idx = idx_reduce((1ull << 31) - idx);
+        pts[t][c].push_back(hpq_add_m31(oods, h_index_to_point(idx)));
+      }
+  }
+  pts.back().assign(4, {oods});
+
+  // Batched OODS evaluation of every sampled polynomial (pcs/prover.rs:89-101).
+  std::vector<const uint32_t*> polys;
+  std::vector<uint32_t> plogs, poly_of;
+  std::vector<stwo_qm31_point> qpts;
+  for (size_t t = 0; t < trees.size(); t++)
+    for (size_t c = 0; c < pts[t].size(); c++) {
+      polys.push_back(trees[t].polys[c]);
+      plogs.push_back(trees[t].poly_logs[c]);
+      for (auto& p : pts[t][c]) {
+        poly_of.push_back((uint32_t)polys.size() - 1);
+        qpts.push_back({to_sq(p.x), to_sq(p.y)});
+      }
+    }
+  std::vector<stwo_qm31> svals(qpts.size());
+  st = eval_at_points(polys.data(), plogs.data(), (uint32_t)polys.size(), poly_of.data(), qpts.data(),
+                      (uint32_t)qpts.size(), svals.data(), s);
+  if (st) return st;
+  std::vector<hq> flat;
+  for (auto& v : svals) flat.push_back(from_sq(v));
+  ch.mix_felts(flat);
+
+  // Sanity check of the composition at the OODS point (prover/mod.rs:70-76).
+  {
+    std::vector<std::vector<std::vector<hq>>> mv(trees.size() - 1);
+    size_t k = 0;
+    for (size_t t = 0; t + 1 < trees.size(); t++) {
+      mv[t].resize(pts[t].size());
+      for (size_t c = 0; c < pts[t].size(); c++)
+        for (size_t j = 0; j < pts[t][c].size(); j++) mv[t][c].push_back(flat[k++]);
+    }
+    hq comp[4];
+    for (int i = 0; i < 4; i++) comp[i] = flat[k++];
+    hq lhs = hq_add(hq_add(comp[0], hq_mul(comp[1], hq_make(0, 1, 0, 0))),
+                    hq_add(hq_mul(comp[2], hq_make(0, 0, 1, 0)), hq_mul(comp[3], hq_make(0, 0, 0, 1))));
+    // denom inverse 1 / coset_vanishing(CanonicCoset(log).coset, oods)
+    stwo_coset tc = coset_new(1u << (31 - (air.log_size() + 1)), air.log_size());
+    hpoint init = h_index_to_point(tc.initial_index);
+    hpoint half = h_index_to_point(tc.step_size >> 1);
+    hpoint shift = h_padd({init.x, h_sub(0, init.y)}, half);
+    HPointQ q = hpq_add_m31(oods, shift);
+    hq x = q.x;
+    for (uint32_t i = 1; i < air.log_size(); i++) x = hq_sub(hq_add(hq_mul(x, x), hq_mul(x, x)), hq_make(1, 0, 0, 0));
+    hq rhs = air.eval_at_point(mv, rc, hq_inv(x));
+    for (int i = 0; i < 4; i++)
+      if (lhs.v[i] != rhs.v[i]) {
+        set_error("ConstraintsNotSatisfied");
+        return STWO_ERR_INVALID_ARG;
+      }
+  }
+
+  // FRI quotients per log size, descending (pcs/quotients.rs:76-101).
+  struct ColS { const uint32_t* p; uint32_t log; std::vector<std::pair<HPointQ, hq>> samples; };
+  std::vector<ColS> cols;
+  {
+    size_t k = 0;
+    for (size_t t = 0; t < trees.size(); t++)
+      for (size_t c = 0; c < trees[t].evals.size(); c++) {
+        ColS cs{trees[t].evals[c], trees[t].eval_logs[c], {}};
+        for (auto& p : pts[t][c]) cs.samples.push_back({p, flat[k++]});
+        cols.push_back(cs);
+      }
+  }
+  std::stable_sort(cols.begin(), cols.end(), [](const ColS& a, const ColS& b) { return a.log > b.log; });
+  hq qrc = ch.draw_felt();
+  std::vector<SecureCols> quotients;
+  std::vector<uint32_t> qlogs;
+  for (size_t i = 0; i < cols.size();) {
+    size_t j = i;
+    while (j < cols.size() && cols[j].log == cols[i].log) j++;
+    // ColumnSampleBatch::new_vec: group by point in CirclePoint<QM31> order.
+    std::vector<HPointQ> points;
+    for (size_t c = i; c < j; c++)
+      for (auto& sp : cols[c].samples) {
+        bool found = false;
+        for (auto& q : points) found = found || hpq_eq(q, sp.first);
+        if (!found) points.push_back(sp.first);
+      }
+    std::sort(points.begin(), points.end(), hpq_less);
+    std::vector<std::vector<uint32_t>> bidx(points.size());
+    std::vector<std::vector<stwo_qm31>> bval(points.size());
+    for (size_t c = i; c < j; c++)
+      for (auto& sp : cols[c].samples)
+        for (size_t b = 0; b < points.size(); b++)
+          if (hpq_eq(points[b], sp.first)) {
+            bidx[b].push_back((uint32_t)(c - i));
+            bval[b].push_back(to_sq(sp.second));
+          }
+    std::vector<stwo_sample_batch> batches(points.size());
+    for (size_t b = 0; b < points.size(); b++)
+      batches[b] = {{to_sq(points[b].x), to_sq(points[b].y)}, (uint32_t)bidx[b].size(), bidx[b].data(), bval[b].data()};
+    std::vector<const uint32_t*> gc;
+    for (size_t c = i; c < j; c++) gc.push_back(cols[c].p);
+    SecureCols q;
+    for (int k = 0; k < 4; k++) {
+      q.c[k] = arena.alloc((size_t)1 << cols[i].log);
+      if (!q.c[k]) return STWO_ERR_OOM;
+    }
+    st = accumulate_quotients(cols[i].log, gc.data(), (uint32_t)gc.size(), to_sq(qrc), batches.data(),
+                              (uint32_t)batches.size(), cfg.log_blowup_factor, q.c, s);
+    if (st) return st;
+    quotients.push_back(q);
+    qlogs.push_back(cols[i].log);
+    i = j;
+  }
+
+  // FRI commitment (fri.rs:168-290).
+  std::vector<ColRef> first_cols;
+  for (size_t i = 0; i < quotients.size(); i++)
+    for (int k = 0; k < 4; k++) first_cols.push_back({quotients[i].c[k], qlogs[i]});
+  DevMerkle first_tree;
+  st = first_tree.commit(first_cols, arena, s);
+  if (st) return st;
+  ch.mix_root(first_tree.root);
+  struct Layer { SecureCols eval; stwo_coset dom; DevMerkle merkle; };
+  std::vector<Layer> layers;
+  stwo_coset dom = coset_new(1u << (31 - (qlogs[0] - 1 + 2)), qlogs[0] - 1);  // Coset::half_odds(log-1)
+  SecureCols cur;
+  for (int k = 0; k < 4; k++) {
+    cur.c[k] = arena.alloc((size_t)1 << dom.log_size);
+    if (!cur.c[k]) return STWO_ERR_OOM;
+    STWO_CHECK_CUDA(cudaMemsetAsync(cur.c[k], 0, ((size_t)4) << dom.log_size, s));
+  }
+  hq alpha = ch.draw_felt();
+  size_t next = 0;
+  st = fri_fold_circle(tree, canonic_half_coset(qlogs[0]), cur.c, const_cast<const uint32_t* const*>(quotients[0].c),
+                       to_dq(alpha), s);
+  if (st) return st;
+  next = 1;
+  size_t last_size = (size_t)1 << (cfg.log_last_layer_degree_bound + cfg.log_blowup_factor);
+  while (((size_t)1 << dom.log_size) > last_size) {
+    Layer L;
+    L.eval = cur;
+    L.dom = dom;
+    std::vector<ColRef> lc;
+    for (int k = 0; k < 4; k++) lc.push_back({cur.c[k], dom.log_size});
+    st = L.merkle.commit(lc, arena, s);
+    if (st) return st;
+    ch.mix_root(L.merkle.root);
+    alpha = ch.draw_felt();
+    SecureCols nxt;
+    for (int k = 0; k < 4; k++) {
+      nxt.c[k] = arena.alloc((size_t)1 << (dom.log_size - 1));
+      if (!nxt.c[k]) return STWO_ERR_OOM;
+    }
+    st = fri_fold_line(tree, dom, const_cast<const uint32_t* const*>(cur.c), to_dq(alpha), nxt.c, s);
+    if (st) return st;
+    dom = coset_double(dom);
+    if (next < quotients.size() && qlogs[next] - 1 == dom.log_size) {
+      st = fri_fold_circle(tree, canonic_half_coset(qlogs[next]), nxt.c,
+                           const_cast<const uint32_t* const*>(quotients[next].c), to_dq(alpha), s);
+      if (st) return st;
+      next++;
+    }
+    layers.push_back(L);
+    cur = nxt;
+  }
+  STWO_REQUIRE(next == quotients.size(), "not all FRI columns consumed");
+  // Last layer: read back and interpolate on the host (fri.rs:272-290).
+  std::vector<hq> last(last_size);
+  {
+    std::vector<uint32_t> w(4 * last_size);
+    for (int k = 0; k < 4; k++)
+      STWO_CHECK_CUDA(cudaMemcpyAsync(w.data() + k * last_size, cur.c[k], last_size * 4, cudaMemcpyDeviceToHost, s));
+    STWO_CHECK_CUDA(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < last_size; i++) last[i] = hq_make(w[i], w[last_size + i], w[2 * last_size + i], w[3 * last_size + i]);
+  }
+  std::vector<hq> coeffs = line_interpolate_host(dom, last);
+  size_t bound = (size_t)1 << cfg.log_last_layer_degree_bound;
+  for (size_t i = bound; i < coeffs.size(); i++)
+    for (int k = 0; k < 4; k++)
+      if (coeffs[i].v[k]) {
+        set_error("invalid degree");
+        return STWO_ERR_INVALID_ARG;
+      }
+  coeffs.resize(bound);
+  bit_reverse_host(coeffs);
+  ch.mix_felts(coeffs);
+
+  // Proof of work (pcs/prover.rs:122-125).
+  uint64_t nonce = 0;
+  {
+    uint32_t d[8];
+    ch.digest.words(d);
+    st = stwo_grind_blake2s(d, cfg.pow_bits, &nonce, s);
+    if (st) return st;
+  }
+  ch.mix_u64(nonce);
+
+  // Decommitment (fri.rs:295-334, pcs/prover.rs:127-137): record every word to read, gather.
+  Gather g;
+  Queries q = generate_queries(ch, qlogs[0], cfg.n_queries);
+  std::map<uint32_t, std::vector<size_t>> by_log;
+  for (uint32_t l : std::set<uint32_t>(qlogs.begin(), qlogs.end())) by_log[l] = q.fold(qlogs[0] - l).pos;
+  std::vector<size_t> first_witness;
+  std::map<uint32_t, std::vector<size_t>> dpos;
+  for (size_t c = 0; c < quotients.size(); c++) {
+    Queries cq = q.fold(qlogs[0] - qlogs[c]);
+    std::vector<size_t> pos;
+    fri_positions_and_witness(quotients[c], cq.pos, g, pos, first_witness);
+    dpos[qlogs[c]] = pos;
+  }
+  DecommitRecipe first_dec;
+  first_tree.decommit(dpos, g, first_dec);
+  std::vector<std::vector<size_t>> layer_witness(layers.size());
+  std::vector<DecommitRecipe> layer_dec(layers.size());
+  Queries lq = q.fold(1);
+  for (size_t li = 0; li < layers.size(); li++) {
+    std::vector<size_t> pos;
+    fri_positions_and_witness(layers[li].eval, lq.pos, g, pos, layer_witness[li]);
+    std::map<uint32_t, std::vector<size_t>> m;
+    m[layers[li].dom.log_size] = pos;
+    layers[li].merkle.decommit(m, g, layer_dec[li]);
+    lq = lq.fold(1);
+  }
+  std::vector<DecommitRecipe> tree_dec(trees.size());
+  for (size_t t = 0; t < trees.size(); t++) trees[t].merkle.decommit(by_log, g, tree_dec[t]);
+  st = g.run(s);
+  if (st) return st;
+
+  // Canonical bytes: config, commitments, sampled values, decommitments, queried values, pow, FRI.
+  ByteWriter w;
+  write_config(w, cfg);
+  w.u64(trees.size());
+  for (auto& t : trees) w.digest(t.merkle.root);
+  w.u64(trees.size());
+  {
+    size_t k = 0;
+    for (size_t t = 0; t < trees.size(); t++) {
+      w.u64(pts[t].size());
+      for (auto& c : pts[t]) {
+        w.u64(c.size());
+        for (size_t j = 0; j < c.size(); j++) w.q(flat[k++]);
+      }
+    }
+  }
+  w.u64(trees.size());
+  for (auto& d : tree_dec) w.dec(d, g);
+  w.u64(trees.size());
+  for (auto& d : tree_dec) w.vals(d.queried, g);
+  w.u64(nonce);
+  auto write_witness = [&](const std::vector<size_t>& wi) {
+    w.u64(wi.size() / 4);
+    for (size_t i = 0; i < wi.size(); i++) w.u32(g.vres[wi[i]]);
+  };
+  write_witness(first_witness);
+  w.dec(first_dec, g);
+  w.digest(first_tree.root);
+  w.u64(layers.size());
+  for (size_t li = 0; li < layers.size(); li++) {
+    write_witness(layer_witness[li]);
+    w.dec(layer_dec[li], g);
+    w.digest(layers[li].merkle.root);
+  }
+  w.u64(coeffs.size());
+  for (auto& c : coeffs) w.q(c);
+  out.swap(w.b);
+  return arena.failed ? STWO_ERR_OOM : STWO_OK;
+}
+
+// Line polynomial coefficients from a bit-reversed evaluation on the line domain `dom`
+// (poly/line.rs:225-290); the last FRI layer has 2^(log_last_layer + log_blowup) points.
+std::vector<hq> line_interpolate_host(stwo_coset dom, std::vector<hq> v) {
+  bit_reverse_host(v);
+  stwo_coset d = dom;
+  while (((size_t)1 << d.log_size) > 1) {
+    size_t n = (size_t)1 << d.log_size, half = n / 2;
+    for (size_t c = 0; c < v.size(); c += n)
+      for (size_t i = 0; i < half; i++) {
+        uint32_t x = h_index_to_point(idx_reduce((uint64_t)d.initial_index + (uint64_t)d.step_size * i)).x;
+        uint32_t xi = h_inv(x);
+        hq a = v[c + i], b = v[c + half + i];
+        v[c + i] = hq_add(a, b);
+        hq diff = hq_sub(a, b);
+        for (int k = 0; k < 4; k++) diff.v[k] = h_mul(diff.v[k], xi);
+        v[c + half + i] = diff;
+      }
+    d = coset_double(d);
+  }
+  uint32_t li = h_inv((uint32_t)(v.size() % P));
+  for (auto& x : v)
+    for (int k = 0; k < 4; k++) x.v[k] = h_mul(x.v[k], li);
+  return v;
+}
+
+}  // namespace stwo

@@ -1,0 +1,113 @@
+// Declarations of the GPU prover host (prover.cu) and of the AIR interface its constraint
+// kernels implement.
+#pragma once
+#include <map>
+#include <vector>
+#include "common.cuh"
+#include "host_channel.h"
+
+namespace stwo {
+
+// Stream-ordered device allocations released together (one proof's working set).
+struct Arena {
+  cudaStream_t s;
+  std::vector<void*> ptrs;
+  bool failed = false;
+  explicit Arena(cudaStream_t st) : s(st) {}
+  ~Arena();
+  uint32_t* alloc(size_t words);
+};
+
+// Words to read back from HBM, collected while walking decommitment structures on the host and
+// fetched in one launch per word size.
+struct Gather {
+  std::vector<unsigned long long> vptr, vidx, hptr, hidx;
+  std::vector<uint32_t> vres, hres;
+  size_t val(const uint32_t* col, size_t i) {
+    vptr.push_back((unsigned long long)(uintptr_t)col);
+    vidx.push_back(i);
+    return vptr.size() - 1;
+  }
+  size_t hash(const uint32_t* layer, size_t node) {
+    hptr.push_back((unsigned long long)(uintptr_t)layer);
+    hidx.push_back(node);
+    return hptr.size() - 1;
+  }
+  int32_t run(cudaStream_t s);
+};
+
+struct ColRef {
+  const uint32_t* p;
+  uint32_t log;
+};
+
+// A Merkle decommitment as indices into a Gather's results.
+struct DecommitRecipe {
+  std::vector<size_t> hash_witness, column_witness, queried;
+};
+
+// MerkleProver (crates/prover/src/core/vcs/prover.rs:13-154) with layers resident in HBM.
+struct DevMerkle {
+  std::vector<uint32_t*> layers;  // layers[l]: 2^l hashes of 8 words
+  std::vector<ColRef> sorted;     // columns, stable-sorted by descending log size
+  Digest root;
+  int32_t commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s);
+  void decommit(const std::map<uint32_t, std::vector<size_t>>& queries, Gather& g, DecommitRecipe& out) const;
+};
+
+struct SecureCols {
+  uint32_t* c[4];
+};
+
+// One FrameworkComponent-like AIR (constraint_framework/component.rs:126-416).
+struct GpuAir {
+  virtual ~GpuAir() {}
+  virtual uint32_t log_size() const = 0;
+  virtual uint32_t max_constraint_log_degree_bound() const = 0;
+  virtual size_t n_constraints() const = 0;
+  // [tree][column] -> mask offsets (tree 0 = preprocessed, 1 = trace, 2 = interaction).
+  virtual std::vector<std::vector<std::vector<int>>> mask_offsets() const = 0;
+  // Writes row_res * denom_inv for every row of the evaluation domain into acc (4 coordinate
+  // columns); `cols[tree][col]` are the trace columns on that domain, `coeffs` the reversed powers
+  // of the random coefficient (4 words each), `dinv` the bit-reversed denominator inverses.
+  virtual int32_t eval_composition(const std::vector<std::vector<const uint32_t*>>& cols, const uint32_t* coeffs,
+                                   const uint32_t* dinv, uint32_t* const acc[4], cudaStream_t s) const = 0;
+  // The constraint quotient sum at a point from the sampled mask values (PointEvaluator).
+  virtual hq eval_at_point(const std::vector<std::vector<std::vector<hq>>>& mask, hq rc, hq denom_inv) const = 0;
+};
+
+struct Tree;
+
+// CommitmentSchemeProver + prove() for one AIR.
+struct Prover {
+  stwo_pcs_config cfg;
+  cudaStream_t s;
+  Arena arena;
+  TwiddleTree* tree = nullptr;
+  int32_t init_status = 0;
+  HostChannel ch;
+  std::vector<Tree> trees;
+
+  Prover(const stwo_pcs_config& c, uint32_t max_log, cudaStream_t st);
+  ~Prover();
+  int32_t commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t> logs);
+  int32_t commit_evals(const std::vector<uint32_t*>& cols, uint32_t log_size);
+  int32_t commit_composition(const GpuAir& air, hq rc);
+  int32_t prove(const GpuAir& air, std::vector<uint8_t>& out);
+};
+
+std::vector<hq> line_interpolate_host(stwo_coset dom, std::vector<hq> v);
+
+template <class T>
+inline void bit_reverse_host(std::vector<T>& v) {
+  size_t n = v.size();
+  uint32_t log = 0;
+  while (((size_t)1 << log) < n) log++;
+  for (size_t i = 0; i < n; i++) {
+    size_t r = 0;
+    for (uint32_t b = 0; b < log; b++) r |= ((i >> b) & 1) << (log - 1 - b);
+    if (r > i) std::swap(v[i], v[r]);
+  }
+}
+
+}  // namespace stwo

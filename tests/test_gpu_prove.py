@@ -1,0 +1,43 @@
+"""Whole proofs on the GPU are byte-identical to the oracle's and accepted by its verifier."""
+import numpy as np
+import pytest
+
+from tests import m31 as F
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(x):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(x, np.uint32)).view(np.int32)).cuda()
+
+
+@pytest.mark.parametrize("log_n,n_cols,cfg", [(2, 100, (5, 1, 0, 3)), (3, 100, (5, 1, 0, 3)),
+                                              (5, 100, (5, 1, 0, 3)), (6, 100, (5, 1, 0, 3)),
+                                              (8, 100, (5, 1, 0, 3)), (10, 32, (10, 1, 0, 3)),
+                                              (7, 20, (3, 2, 1, 5)), (9, 50, (0, 1, 2, 8)),
+                                              (12, 100, (5, 1, 0, 3))])
+def test_wide_fib_proof_bytes_match_oracle(cuda, oracle, log_n, n_cols, cfg):
+    from stwo_gb300.prover import prove_wide_fib, wide_fib_trace
+
+    rng = np.random.default_rng(log_n * 1000 + n_cols)
+    a = F.rand_m31(rng, 1 << log_n)
+    b = F.rand_m31(rng, 1 << log_n)
+    want = oracle.prove_wide_fib(log_n, n_cols, a, b, cfg)
+    got = prove_wide_fib(log_n, wide_fib_trace(log_n, n_cols, dev(a), dev(b)), cfg)
+    assert len(got) == len(want)
+    assert got == want
+    ok, why = oracle.verify_wide_fib(log_n, n_cols, got)
+    assert ok, why
+
+
+def test_wide_fib_reference_inputs(cuda, oracle):
+    # The reference test's inputs (a = 1, b = row index) at log 2..6.
+    from stwo_gb300.prover import prove_wide_fib, wide_fib_trace
+
+    for log_n in range(2, 7):
+        n = 1 << log_n
+        a, b = np.ones(n, np.uint32), np.arange(n, dtype=np.uint32)
+        got = prove_wide_fib(log_n, wide_fib_trace(log_n, 100, dev(a), dev(b)))
+        assert got == oracle.prove_wide_fib(log_n, 100, a, b)
