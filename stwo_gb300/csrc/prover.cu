@@ -600,7 +600,8 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     STWO_CHECK_CUDA(cudaStreamSynchronize(s));
     for (size_t i = 0; i < last_size; i++) last[i] = hq_make(w[i], w[last_size + i], w[2 * last_size + i], w[3 * last_size + i]);
   }
-  std::vector<hq> coeffs = line_interpolate_host(dom, last);
+  std::vector<hq> coeffs = line_interpolate_host(dom, last);  // bit-reversed coefficient order
+  bit_reverse_host(coeffs);                                   // natural order
   size_t bound = (size_t)1 << cfg.log_last_layer_degree_bound;
   for (size_t i = bound; i < coeffs.size(); i++)
     for (int k = 0; k < 4; k++)
