@@ -106,6 +106,22 @@ stwo_status stwo_eval_at_points(const uint32_t* const* d_coeffs, const uint32_t*
                                 const uint32_t* h_poly_of, const stwo_qm31_point* h_points, uint32_t n_evals,
                                 stwo_qm31* h_out, void* stream);
 
+/* No counterpart in the reference. The same result as stwo_eval_at_points for callers that
+ * cannot allocate device memory (their HBM is owned by a pool manager that forbids other
+ * allocations, or an allocation would stall or synchronise work they run on other streams). It
+ * calls no cudaMalloc/cudaFree or allocating library routine: its scratch is a fixed
+ * 256-byte-aligned static device array of about 200 KB, held by every GPU that loads this library
+ * until the process exits. Limits: n_evals <= STWO_NOALLOC_MAX_EVALS and
+ * n_polys <= STWO_NOALLOC_MAX_POLYS, else STWO_ERR_INVALID_ARG. The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture. All calls share the one array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the caller. */
+#define STWO_NOALLOC_MAX_EVALS 2048
+#define STWO_NOALLOC_MAX_POLYS 2048
+stwo_status stwo_eval_at_points_noalloc(const uint32_t* const* d_coeffs, const uint32_t* h_log_sizes,
+                                        uint32_t n_polys, const uint32_t* h_poly_of, const stwo_qm31_point* h_points,
+                                        uint32_t n_evals, stwo_qm31* h_out, void* stream);
+
 /* ColumnOps::bit_reverse_column (crates/prover/src/core/backend/mod.rs:40). */
 stwo_status stwo_bit_reverse_column(uint32_t* d_col, uint32_t log_size, void* stream);
 

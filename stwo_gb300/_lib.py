@@ -72,6 +72,8 @@ SIGNATURES = {
     "stwo_extend": (C.c_int32, [VP, U32, VP, U32, VP]),
     "stwo_eval_at_points": (C.c_int32, [PVP, C.POINTER(C.c_uint32), U32, C.POINTER(C.c_uint32),
                                         C.POINTER(QM31Point), U32, C.POINTER(QM31), VP]),
+    "stwo_eval_at_points_noalloc": (C.c_int32, [PVP, C.POINTER(C.c_uint32), U32, C.POINTER(C.c_uint32),
+                                                C.POINTER(QM31Point), U32, C.POINTER(QM31), VP]),
     "stwo_bit_reverse_column": (C.c_int32, [VP, U32, VP]),
     "stwo_merkle_commit_layer": (C.c_int32, [U32, VP, PVP, U32, VP, VP]),
     "stwo_fri_fold_line": (C.c_int32, [VP, Coset, PVP, QM31, PVP, VP]),

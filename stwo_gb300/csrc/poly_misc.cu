@@ -176,6 +176,101 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
   return STWO_OK;
 }
 
+// ---------------------------------------------------------------- eval_at_points without allocation
+// Same computation as eval_at_points, for callers that must not allocate device memory: a process
+// whose HBM is handed out by its own pool manager (a serving loop that reserves its budget up
+// front and forbids any other allocation), or code running where cudaMalloc/cudaFree would stall
+// other streams or device-wide synchronise. Its scratch is a fixed static device array instead of
+// a stream-ordered allocation. Every GPU that loads this library keeps the array until exit.
+constexpr uint32_t NOALLOC_MAX_EVALS = STWO_NOALLOC_MAX_EVALS;
+constexpr uint32_t NOALLOC_MAX_POLYS = STWO_NOALLOC_MAX_POLYS;
+constexpr size_t NA_OFF_JOBS = 0;
+constexpr size_t NA_OFF_POLYOF = NA_OFF_JOBS + (size_t)NOALLOC_MAX_POLYS * sizeof(EvalJob);
+constexpr size_t NA_OFF_PTS = NA_OFF_POLYOF + (size_t)NOALLOC_MAX_EVALS * 4;
+constexpr size_t NA_OFF_ACC = NA_OFF_PTS + (size_t)NOALLOC_MAX_EVALS * sizeof(stwo_qm31_point);
+constexpr size_t NA_OFF_OUT = NA_OFF_ACC + (size_t)NOALLOC_MAX_EVALS * 4 * 8;
+constexpr size_t NA_BYTES = NA_OFF_OUT + (size_t)NOALLOC_MAX_EVALS * 16;
+static_assert(NA_OFF_POLYOF % 8 == 0 && NA_OFF_PTS % 8 == 0 && NA_OFF_ACC % 8 == 0, "scratch alignment");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+// Device address of g_noalloc_scratch, looked up once per device with that device current (the
+// host-side symbol is only a stand-in and must never reach a kernel).
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[256] = {};
+
+static int32_t noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  STWO_CHECK_CUDA(cudaGetDevice(&dev));
+  STWO_REQUIRE(dev >= 0 && dev < 256, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("cudaGetSymbolAddress of the no-alloc scratch: %s", cudaGetErrorString(e));
+      return STWO_ERR_CUDA;
+    }
+    g_noalloc_addr[dev] = p;
+  }
+  *out = reinterpret_cast<unsigned char*>(g_noalloc_addr[dev]);
+  return STWO_OK;
+}
+
+int32_t eval_at_points_noalloc(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
+                               const uint32_t* poly_of, const stwo_qm31_point* points, uint32_t n_evals,
+                               stwo_qm31* out, cudaStream_t s) {
+  if (n_evals == 0) return STWO_OK;
+  STWO_REQUIRE(coeffs && log_sizes && poly_of && points && out, "null argument");
+  STWO_REQUIRE(n_evals <= NOALLOC_MAX_EVALS, "n_evals %u exceeds the no-alloc maximum of %u", n_evals,
+               NOALLOC_MAX_EVALS);
+  STWO_REQUIRE(n_polys <= NOALLOC_MAX_POLYS, "n_polys %u exceeds the no-alloc maximum of %u", n_polys,
+               NOALLOC_MAX_POLYS);
+  EvalJob jobs[NOALLOC_MAX_POLYS];
+  uint32_t max_chunks = 1;
+  for (uint32_t i = 0; i < n_polys; i++) {
+    STWO_REQUIRE(log_sizes[i] <= 30, "poly log size %u > 30", log_sizes[i]);
+    jobs[i] = {coeffs[i], log_sizes[i], 0};
+  }
+  for (uint32_t e = 0; e < n_evals; e++) {
+    STWO_REQUIRE(poly_of[e] < n_polys, "poly index out of range");
+    uint32_t L = log_sizes[poly_of[e]];
+    uint32_t cb = std::min(L, EP_LOW) + std::min(L - std::min(L, EP_LOW), EP_MID);
+    max_chunks = std::max(max_chunks, 1u << (L - cb));
+  }
+  unsigned char* buf = nullptr;
+  int32_t st = noalloc_scratch(&buf);
+  if (st) return st;
+  cudaError_t err = cudaSuccess;
+  if (n_polys) err = cudaMemcpyAsync(buf + NA_OFF_JOBS, jobs, n_polys * sizeof(EvalJob), cudaMemcpyHostToDevice, s);
+  if (!err) err = cudaMemcpyAsync(buf + NA_OFF_POLYOF, poly_of, (size_t)n_evals * 4, cudaMemcpyHostToDevice, s);
+  if (!err) err = cudaMemcpyAsync(buf + NA_OFF_PTS, points, (size_t)n_evals * sizeof(stwo_qm31_point), cudaMemcpyHostToDevice, s);
+  // The accumulators keep the previous call's sums: they must start at zero.
+  if (!err) err = cudaMemsetAsync(buf + NA_OFF_ACC, 0, (size_t)n_evals * 32, s);
+  if (!err) {
+    dim3 grid(max_chunks, n_evals);
+    k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<EvalJob*>(buf + NA_OFF_JOBS),
+                                         reinterpret_cast<uint32_t*>(buf + NA_OFF_POLYOF),
+                                         reinterpret_cast<stwo_qm31_point*>(buf + NA_OFF_PTS),
+                                         reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC));
+    note_launch();
+    err = cudaGetLastError();
+  }
+  if (!err) {
+    k_reduce_acc<<<(n_evals * 4 + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC),
+                                                            n_evals * 4, reinterpret_cast<uint32_t*>(buf + NA_OFF_OUT));
+    note_launch();
+    err = cudaGetLastError();
+  }
+  if (!err) err = cudaMemcpyAsync(out, buf + NA_OFF_OUT, (size_t)n_evals * 16, cudaMemcpyDeviceToHost, s);
+  if (!err) err = cudaStreamSynchronize(s);
+  if (err) {
+    set_error("eval_at_points_noalloc: %s", cudaGetErrorString(err));
+    return STWO_ERR_CUDA;
+  }
+  return STWO_OK;
+}
+
 // ---------------------------------------------------------------- bit reverse
 __global__ void k_bit_reverse(uint32_t* col, uint32_t log_n) {
   uint32_t n = 1u << log_n;
@@ -237,6 +332,13 @@ stwo_status stwo_eval_at_points(const uint32_t* const* d_coeffs, const uint32_t*
                                 const uint32_t* h_poly_of, const stwo_qm31_point* h_points, uint32_t n_evals,
                                 stwo_qm31* h_out, void* stream) {
   return eval_at_points(d_coeffs, h_log_sizes, n_polys, h_poly_of, h_points, n_evals, h_out, as_stream(stream));
+}
+
+stwo_status stwo_eval_at_points_noalloc(const uint32_t* const* d_coeffs, const uint32_t* h_log_sizes,
+                                        uint32_t n_polys, const uint32_t* h_poly_of, const stwo_qm31_point* h_points,
+                                        uint32_t n_evals, stwo_qm31* h_out, void* stream) {
+  return eval_at_points_noalloc(d_coeffs, h_log_sizes, n_polys, h_poly_of, h_points, n_evals, h_out,
+                                as_stream(stream));
 }
 
 stwo_status stwo_extend(const uint32_t* d_coeffs, uint32_t coeff_log_size, uint32_t* d_out, uint32_t log_size,
