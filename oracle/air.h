@@ -38,6 +38,17 @@ struct DomainEvaluator {
     return out;
   }
   M31 next_trace_mask() { return next_interaction_mask(1, {0})[0]; }
+  // Four consecutive columns combined into QM31 values (EvalAtRow::next_extension_interaction_mask).
+  std::vector<QM31> next_extension_interaction_mask(size_t tree, const std::vector<int>& offsets) {
+    std::vector<M31> c[4];
+    for (int k = 0; k < 4; k++) c[k] = next_interaction_mask(tree, offsets);
+    std::vector<QM31> out;
+    for (size_t j = 0; j < offsets.size(); j++) {
+      M31 v[4] = {c[0][j], c[1][j], c[2][j], c[3][j]};
+      out.push_back(combine_ef(v));
+    }
+    return out;
+  }
   template <class G>
   void add_constraint(const G& c) { row_res = row_res + coeffs[ci++] * c; }
   static QM31 combine_ef(const M31 v[4]) { return QM31::from_m31(v[0], v[1], v[2], v[3]); }
@@ -58,6 +69,16 @@ struct PointEvaluator {
     return v;
   }
   QM31 next_trace_mask() { return next_interaction_mask(1, {0})[0]; }
+  std::vector<QM31> next_extension_interaction_mask(size_t tree, const std::vector<int>& offsets) {
+    std::vector<QM31> c[4];
+    for (int k = 0; k < 4; k++) c[k] = next_interaction_mask(tree, offsets);
+    std::vector<QM31> out;
+    for (size_t j = 0; j < offsets.size(); j++) {
+      QM31 v[4] = {c[0][j], c[1][j], c[2][j], c[3][j]};
+      out.push_back(combine_ef(v));
+    }
+    return out;
+  }
   void add_constraint(const QM31& c) { *acc = *acc * rc + denom_inv * c; }
   static QM31 combine_ef(const QM31 v[4]) {
     // QM31::from_partial_evals (fields/qm31.rs:52-58)
@@ -120,9 +141,13 @@ inline std::vector<Column> composition_polynomial(const Air& air, const Commitme
       if (ev.size() == ed.size()) {
         tr[t].push_back(&ev);
       } else {
-        if (!have_etw) { etw = precompute_twiddles(ed.half_coset); have_etw = true; }
-        ext[t].push_back(evaluate(ed, pcs.trees[t].polys[c], etw));
+        ext[t].emplace_back();
       }
+    }
+    if (!ext[t].empty()) {
+      if (!have_etw) { etw = precompute_twiddles(ed.half_coset); have_etw = true; }
+#pragma omp parallel for schedule(dynamic)
+      for (long c = 0; c < (long)ext[t].size(); c++) ext[t][c] = evaluate(ed, pcs.trees[t].polys[c], etw);
     }
     if (!ext[t].empty()) {
       tr[t].clear();
@@ -136,7 +161,8 @@ inline std::vector<Column> composition_polynomial(const Air& air, const Commitme
   for (size_t i = 0; i < ((size_t)1 << expand); i++) dinv.push_back(inv(coset_vanishing(tc, ed.at(i))));
   bit_reverse(dinv);
   SecureColumn acc(ed.size());
-  for (size_t r = 0; r < ed.size(); r++) {
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < (long)ed.size(); r++) {
     DomainEvaluator e(&tr, r, trace_log, eval_log, coeffs.data());
     QM31 rr = air.eval_row(e);
     acc.set(r, rr * dinv[r >> trace_log]);
@@ -209,13 +235,15 @@ inline bool rebuild_evals(const std::vector<size_t>& queries, const std::vector<
 // `trace_log_sizes[t]` are the committed trees' column log sizes before blowup (trees before
 // the composition tree). Returns "" on success, else the failure reason.
 inline std::string verify(const Air& air, Channel& ch, const StarkProof& proof,
-                          const std::vector<std::vector<uint32_t>>& trace_log_sizes) {
+                          const std::vector<std::vector<uint32_t>>& trace_log_sizes,
+                          const std::function<void(size_t, Channel&)>& after_tree = nullptr) {
   const PcsConfig& cfg = proof.config;
   size_t n_trees = trace_log_sizes.size();
   if (proof.commitments.size() != n_trees + 1) return "commitments";
   std::vector<std::vector<uint32_t>> tree_logs;  // extended log sizes
   for (size_t t = 0; t < n_trees; t++) {
     ch.mix_root(proof.commitments[t]);
+    if (after_tree) after_tree(t, ch);
     std::vector<uint32_t> l;
     for (auto x : trace_log_sizes[t]) l.push_back(x + cfg.log_blowup);
     tree_logs.push_back(l);

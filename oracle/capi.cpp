@@ -215,3 +215,65 @@ int oracle_verify_wide_fib(uint32_t log_n, uint32_t n_cols, const uint8_t* proof
 }
 
 }  // extern "C"
+
+#include "air_poseidon.h"
+
+extern "C" {
+
+// Proves the Poseidon2 AIR (2^log_n rows, 8 permutations per row) as prove_poseidon does
+// (poseidon/mod.rs:327-389). `init` holds the initial states ((row * 8 + rep) * 16 + i), or is NULL
+// for the reference's deterministic inputs. Writes the proof bytes; claimed_sum (4 words) out.
+size_t oracle_prove_poseidon(uint32_t log_n, const uint32_t* init, const uint32_t cfg[4], uint8_t* out, size_t cap,
+                             uint32_t claimed_sum[4], char* err, size_t err_cap) {
+  try {
+    PcsConfig config{cfg[0], cfg[1], cfg[2], cfg[3]};
+    std::vector<uint32_t> ref;
+    if (!init) {
+      ref = poseidon_reference_inputs(log_n);
+      init = ref.data();
+    }
+    TwiddleTree tw = precompute_twiddles(canonic_domain(log_n + PS_LOG_EXPAND + config.log_blowup).half_coset);
+    Channel ch;
+    CommitmentSchemeProver pcs;
+    pcs.config = config;
+    pcs.twiddles = &tw;
+    pcs.commit({}, ch);
+    std::vector<std::vector<M31>> lookups;
+    pcs.commit_evals(poseidon_trace(log_n, init, lookups), log_n, ch);
+    LookupElements le = LookupElements::draw(ch);
+    QM31 cs;
+    pcs.commit_evals(poseidon_interaction_trace(log_n, lookups, le, cs), log_n, ch);
+    PoseidonAir air(log_n, le, cs);
+    StarkProof proof = prove(air, ch, pcs);
+    std::vector<uint8_t> bytes = serialize(proof);
+    if (bytes.size() > cap) throw std::runtime_error("output buffer too small");
+    std::memcpy(out, bytes.data(), bytes.size());
+    q_to(cs, claimed_sum);
+    return bytes.size();
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+int oracle_verify_poseidon(uint32_t log_n, const uint32_t claimed_sum[4], const uint8_t* proof, size_t len, char* err,
+                           size_t err_cap) {
+  try {
+    StarkProof p;
+    if (!deserialize(proof, len, p)) throw std::runtime_error("malformed proof bytes");
+    Channel ch;
+    PoseidonAir air(log_n, LookupElements{}, q_of(claimed_sum));
+    auto hook = [&](size_t t, Channel& c) {
+      if (t == 1) air.le = LookupElements::draw(c);
+    };
+    std::string r = verify(air, ch, p,
+                           {{}, std::vector<uint32_t>(PS_COLUMNS, log_n), std::vector<uint32_t>(32, log_n)}, hook);
+    if (!r.empty()) throw std::runtime_error(r);
+    return 1;
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+}  // extern "C"

@@ -25,8 +25,9 @@ inline std::vector<Hash32> commit_on_layer(uint32_t log_size, const std::vector<
                                            const std::vector<const Column*>& cols) {
   size_t n = (size_t)1 << log_size;
   std::vector<Hash32> out(n);
-  std::vector<uint32_t> vals(cols.size());
-  for (size_t i = 0; i < n; i++) {
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)n; i++) {
+    std::vector<uint32_t> vals(cols.size());
     for (size_t c = 0; c < cols.size(); c++) vals[c] = (*cols[c])[i].v;
     if (prev) out[i] = hash_node(&(*prev)[2 * i], &(*prev)[2 * i + 1], vals.data(), vals.size());
     else out[i] = hash_node(nullptr, nullptr, vals.data(), vals.size());
@@ -319,8 +320,9 @@ inline SecureColumn accumulate_quotients(const CircleDomain& domain, const std::
   QuotientConstants qc = quotient_constants(batches, rc);
   std::vector<CirclePointM31> pts = domain_points_bitrev(sub);
   SecureColumn subv(sub.size());
-  std::vector<M31> row(cols.size());
-  for (size_t r = 0; r < sub.size(); r++) {
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < (long)sub.size(); r++) {
+    std::vector<M31> row(cols.size());
     for (size_t c = 0; c < cols.size(); c++) row[c] = (*cols[c])[r];
     subv.set(r, accumulate_row_quotients(batches, row, qc, pts[r]));
   }

@@ -17,6 +17,7 @@
 #include <set>
 #include <stdexcept>
 #include <cstring>
+#include <functional>
 
 namespace oracle {
 
@@ -411,9 +412,11 @@ struct CommitmentSchemeProver {
   void commit(std::vector<Column> polys, Channel& ch) {
     CommitmentTree t;
     t.polys = std::move(polys);
-    for (auto& p : t.polys) {
-      uint32_t log = ilog2(p.size()) + config.log_blowup;
-      t.evals.push_back(evaluate(canonic_domain(log), p, *twiddles));
+    t.evals.resize(t.polys.size());
+#pragma omp parallel for schedule(dynamic)
+    for (long i = 0; i < (long)t.polys.size(); i++) {
+      uint32_t log = ilog2(t.polys[i].size()) + config.log_blowup;
+      t.evals[i] = evaluate(canonic_domain(log), t.polys[i], *twiddles);
     }
     std::vector<const Column*> ec;
     for (auto& e : t.evals) ec.push_back(&e);
@@ -423,8 +426,9 @@ struct CommitmentSchemeProver {
   }
   // TreeBuilder::extend_evals: interpolate then commit.
   void commit_evals(const std::vector<Column>& evals, uint32_t log_size, Channel& ch) {
-    std::vector<Column> polys;
-    for (auto& e : evals) polys.push_back(interpolate(canonic_domain(log_size), e, *twiddles));
+    std::vector<Column> polys(evals.size());
+#pragma omp parallel for schedule(dynamic)
+    for (long i = 0; i < (long)evals.size(); i++) polys[i] = interpolate(canonic_domain(log_size), evals[i], *twiddles);
     commit(std::move(polys), ch);
   }
 
@@ -435,19 +439,17 @@ struct CommitmentSchemeProver {
     std::vector<std::vector<std::vector<PointSample>>> samples(trees.size());
     std::vector<QM31> flat;
     for (size_t t = 0; t < trees.size(); t++) {
-      proof.sampled_values.emplace_back();
-      for (size_t c = 0; c < trees[t].polys.size(); c++) {
-        std::vector<PointSample> s;
-        std::vector<QM31> vals;
+      proof.sampled_values.emplace_back(trees[t].polys.size());
+      samples[t].resize(trees[t].polys.size());
+#pragma omp parallel for schedule(dynamic)
+      for (long c = 0; c < (long)trees[t].polys.size(); c++) {
         for (auto& pt : points[t][c]) {
           QM31 v = eval_at_point(trees[t].polys[c], pt);
-          s.push_back({pt, v});
-          vals.push_back(v);
-          flat.push_back(v);
+          samples[t][c].push_back({pt, v});
+          proof.sampled_values[t][c].push_back(v);
         }
-        samples[t].push_back(s);
-        proof.sampled_values.back().push_back(vals);
       }
+      for (auto& col : proof.sampled_values[t]) flat.insert(flat.end(), col.begin(), col.end());
     }
     ch.mix_felts(flat);
     // compute_fri_quotients (pcs/quotients.rs:76-101): stable sort by descending log size.

@@ -202,3 +202,29 @@ def verify_wide_fib(log_n, n_cols, proof: bytes):
     ok = lib().oracle_verify_wide_fib(C.c_uint32(log_n), C.c_uint32(n_cols), _p(buf), C.c_size_t(len(proof)), err,
                                       C.c_size_t(512))
     return bool(ok), err.value.decode()
+
+
+def prove_poseidon(log_n, init=None, config=(5, 1, 0, 3)):
+    """(proof bytes, claimed_sum) of the Poseidon2 AIR; init = None for the reference's inputs."""
+    cap = 256 << 20
+    out = np.zeros(cap, np.uint8)
+    cs = np.zeros(4, np.uint32)
+    err = C.create_string_buffer(512)
+    f = lib().oracle_prove_poseidon
+    f.restype = C.c_size_t
+    ip = _p(_u32(init).reshape(-1)) if init is not None else None
+    keep = _u32(init).reshape(-1) if init is not None else None
+    if keep is not None:
+        ip = _p(keep)
+    n = f(C.c_uint32(log_n), ip, _p(_u32(config)), _p(out), C.c_size_t(cap), _p(cs), err, C.c_size_t(512))
+    if n == 0:
+        raise RuntimeError("oracle prove failed: " + err.value.decode())
+    return bytes(out[:n]), tuple(int(x) for x in cs)
+
+
+def verify_poseidon(log_n, claimed_sum, proof: bytes):
+    buf = np.frombuffer(proof, dtype=np.uint8).copy()
+    err = C.create_string_buffer(512)
+    ok = lib().oracle_verify_poseidon(C.c_uint32(log_n), _p(_u32(claimed_sum)), _p(buf), C.c_size_t(len(proof)),
+                                      err, C.c_size_t(512))
+    return bool(ok), err.value.decode()

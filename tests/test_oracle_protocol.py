@@ -35,3 +35,20 @@ def test_wide_fib_other_configs(oracle):
         proof = oracle.prove_wide_fib(6, 40, a, b, cfg)
         ok, why = oracle.verify_wide_fib(6, 40, proof)
         assert ok, (cfg, why)
+
+
+@pytest.mark.parametrize("log_n", [3, 4, 5, 7])
+def test_poseidon_prove_verify(oracle, log_n):
+    proof, claimed_sum = oracle.prove_poseidon(log_n)
+    ok, why = oracle.verify_poseidon(log_n, claimed_sum, proof)
+    assert ok, why
+    # A wrong claimed sum is rejected by the constraint check at the OODS point.
+    bad = ((claimed_sum[0] + 1) % ((1 << 31) - 1),) + claimed_sum[1:]
+    assert not oracle.verify_poseidon(log_n, bad, proof)[0]
+
+
+def test_poseidon_seeded_inputs(oracle):
+    rng = np.random.default_rng(3)
+    init = rng.integers(0, (1 << 31) - 1, size=(1 << 5) * 8 * 16, dtype=np.int64).astype(np.uint32)
+    proof, cs = oracle.prove_poseidon(5, init)
+    assert oracle.verify_poseidon(5, cs, proof)[0]
