@@ -85,6 +85,8 @@ SIGNATURES = {
     "stwo_grind_blake2s": (C.c_int32, [C.POINTER(C.c_uint32), U32, C.POINTER(C.c_uint64), VP]),
     "stwo_gen_wide_fib_trace": (C.c_int32, [U32, U32, VP, VP, PVP, VP]),
     "stwo_prove_wide_fib": (C.c_int32, [U32, U32, PVP, PcsConfig, VP, C.c_size_t, C.POINTER(C.c_size_t), VP]),
+    "stwo_prove_poseidon": (C.c_int32, [U32, VP, PcsConfig, VP, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(QM31),
+                                        VP]),
 }
 
 _lib = None

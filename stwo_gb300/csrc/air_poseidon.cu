@@ -1,0 +1,624 @@
+// Poseidon2 AIR on the device (crates/prover/src/examples/poseidon/mod.rs:30-389): 8 width-16
+// permutations per row (4 full, 14 partial, 4 full rounds; 1264 trace columns), plus the LogUp
+// interaction trace of their initial/final states (constraint_framework/logup.rs:123-260) and
+// the composition constraints (1136 round constraints + 8 LogUp constraints, finalize_logup_in_pairs
+// of constraint_framework/mod.rs:182-248).
+//
+// Kernels (one thread per row each):
+//   k_poseidon_trace        trace generation; also keeps the lookup states, since committing the
+//                           trace replaces it by its coefficients
+//   k_poseidon_interaction  8 cumulative LogUp secure columns (QM31 inverses per row)
+//   k_coset_scan_*          inclusive prefix sum in coset order of the last column
+//                           (backend/simd/prefix_sum.rs:19-139)
+//   k_poseidon_composition  all constraints on the 4x evaluation domain, random-coefficient
+//                           accumulation in 64-bit lanes, times the vanishing inverse
+// Multiplication by 2^k (internal matrix) is a 31-bit rotation, exact modulo 2^31 - 1.
+#include "common.cuh"
+#include "prover.cuh"
+
+namespace stwo {
+
+constexpr int PS_REPS = 8, PS_ST = 16, PS_PARTIAL = 14, PS_HALF = 4;
+constexpr int PS_COLS_PER_REP = PS_ST * (1 + 2 * PS_HALF) + PS_PARTIAL;  // 158
+constexpr int PS_COLS = PS_REPS * PS_COLS_PER_REP;                       // 1264
+constexpr int PS_INTERACTION_COLS = 4 * PS_REPS;                         // 32
+constexpr int PS_N_CONSTRAINTS = PS_REPS * (2 * PS_HALF * PS_ST + PS_PARTIAL) + PS_REPS;  // 1144
+constexpr uint32_t PS_RC = 1234;  // round constants of the reference example
+constexpr uint32_t PS_LOG_EXPAND = 2;
+
+__device__ __forceinline__ uint32_t m31_mul_pow2(uint32_t x, int k) { return ((x << k) | (x >> (31 - k))) & P; }
+__device__ __forceinline__ uint32_t pow5(uint32_t x) {
+  uint32_t x2 = m31_sqr(x);
+  return m31_mul(m31_sqr(x2), x);
+}
+// M4 of Poseidon2 section 5.1 (poseidon/mod.rs:72-94).
+__device__ __forceinline__ void apply_m4(uint32_t* x) {
+  uint32_t t0 = m31_add(x[0], x[1]);
+  uint32_t t02 = m31_add(t0, t0);
+  uint32_t t1 = m31_add(x[2], x[3]);
+  uint32_t t12 = m31_add(t1, t1);
+  uint32_t t2 = m31_add(m31_add(x[1], x[1]), t1);
+  uint32_t t3 = m31_add(m31_add(x[3], x[3]), t0);
+  uint32_t t4 = m31_add(m31_add(t12, t12), t3);
+  uint32_t t5 = m31_add(m31_add(t02, t02), t2);
+  x[0] = m31_add(t3, t5);
+  x[1] = t5;
+  x[2] = m31_add(t2, t4);
+  x[3] = t4;
+}
+__device__ __forceinline__ void external_matrix(uint32_t* s) {
+#pragma unroll
+  for (int i = 0; i < 4; i++) apply_m4(s + 4 * i);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    uint32_t t = m31_add(m31_add(s[j], s[j + 4]), m31_add(s[j + 8], s[j + 12]));
+#pragma unroll
+    for (int i = 0; i < 4; i++) s[4 * i + j] = m31_add(s[4 * i + j], t);
+  }
+}
+__device__ __forceinline__ void internal_matrix(uint32_t* s) {
+  uint32_t sum = s[0];
+#pragma unroll
+  for (int i = 1; i < 16; i++) sum = m31_add(sum, s[i]);
+#pragma unroll
+  for (int i = 0; i < 16; i++) s[i] = m31_add(m31_mul_pow2(s[i], i + 1), sum);
+}
+
+// ------------------------------------------------------------------------------------------ trace
+// init: ((row * 8 + rep) * 16 + i) or NULL for the reference inputs (row + i + rep).
+__global__ void __launch_bounds__(128) k_poseidon_trace(uint32_t n_rows, const uint32_t* __restrict__ init,
+                                                        uint32_t* __restrict__ trace, uint32_t* __restrict__ lookups) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  size_t n = n_rows;
+  int col = 0;
+  for (int rep = 0; rep < PS_REPS; rep++) {
+    uint32_t s[PS_ST];
+#pragma unroll
+    for (int i = 0; i < PS_ST; i++) {
+      s[i] = init ? init[((size_t)r * PS_REPS + rep) * PS_ST + i] : (r + i + rep);
+      trace[(size_t)col++ * n + r] = s[i];
+      lookups[((size_t)rep * 32 + i) * n + r] = s[i];
+    }
+    for (int round = 0; round < 2 * PS_HALF + PS_PARTIAL; round++) {
+      bool full = round < PS_HALF || round >= PS_HALF + PS_PARTIAL;
+      if (full) {
+#pragma unroll
+        for (int i = 0; i < PS_ST; i++) s[i] = m31_add(s[i], PS_RC);
+        external_matrix(s);
+#pragma unroll
+        for (int i = 0; i < PS_ST; i++) {
+          s[i] = pow5(s[i]);
+          trace[(size_t)col++ * n + r] = s[i];
+        }
+      } else {
+        s[0] = m31_add(s[0], PS_RC);
+        internal_matrix(s);
+        s[0] = pow5(s[0]);
+        trace[(size_t)col++ * n + r] = s[0];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < PS_ST; i++) lookups[((size_t)rep * 32 + 16 + i) * n + r] = s[i];
+  }
+}
+
+// ------------------------------------------------------------------------------------ interaction
+struct LookupConsts {
+  uint32_t z[4];
+  uint32_t alpha_pow[PS_ST][4];
+};
+
+__device__ __forceinline__ qm31 qm31_inv(qm31 x) {
+  // (a + bu)^-1 = (a - bu) / (a^2 - (2+i) b^2)  (fields/qm31.rs:121-129)
+  cm31 b2 = cm31_mul(x.b, x.b);
+  cm31 denom = cm31_sub(cm31_mul(x.a, x.a), cm31_mul_r(b2));
+  cm31 di = cm31_inv(denom);
+  return {cm31_mul(x.a, di), cm31_mul(cm31_sub({0u, 0u}, x.b), di)};
+}
+
+__device__ __forceinline__ uint32_t fold64_p(unsigned long long x) {
+  x = (x & P) + (x >> 31);
+  x = (x & P) + (x >> 31);
+  uint32_t r = (uint32_t)x;
+  return r >= P ? r - P : r;
+}
+
+// sum_i alpha^i * v_i - z  (LookupElements::combine, logup.rs:90-105)
+__device__ __forceinline__ qm31 combine16(const LookupConsts& lc, const uint32_t* v) {
+  unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+  for (int i = 0; i < PS_ST; i++) {
+    a0 += (unsigned long long)lc.alpha_pow[i][0] * v[i];
+    a1 += (unsigned long long)lc.alpha_pow[i][1] * v[i];
+    a2 += (unsigned long long)lc.alpha_pow[i][2] * v[i];
+    a3 += (unsigned long long)lc.alpha_pow[i][3] * v[i];
+    if (i % 3 == 2) {
+      a0 = (a0 & P) + (a0 >> 31);
+      a1 = (a1 & P) + (a1 >> 31);
+      a2 = (a2 & P) + (a2 >> 31);
+      a3 = (a3 & P) + (a3 >> 31);
+    }
+  }
+  qm31 s = qm31_from_u32(fold64_p(a0), fold64_p(a1), fold64_p(a2), fold64_p(a3));
+  return qm31_sub(s, qm31_from_u32(lc.z[0], lc.z[1], lc.z[2], lc.z[3]));
+}
+
+__global__ void __launch_bounds__(128) k_poseidon_interaction(uint32_t n_rows, const uint32_t* __restrict__ lookups,
+                                                              LookupConsts lc, uint32_t* __restrict__ out) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  size_t n = n_rows;
+  qm31 cum = qm31_zero();
+  for (int rep = 0; rep < PS_REPS; rep++) {
+    uint32_t a[PS_ST], b[PS_ST];
+#pragma unroll
+    for (int i = 0; i < PS_ST; i++) {
+      a[i] = __ldg(lookups + ((size_t)rep * 32 + i) * n + r);
+      b[i] = __ldg(lookups + ((size_t)rep * 32 + 16 + i) * n + r);
+    }
+    qm31 d0 = combine16(lc, a), d1 = combine16(lc, b);
+    // 1/d0 - 1/d1 = (d1 - d0) / (d0 d1)
+    qm31 frac = qm31_mul(qm31_sub(d1, d0), qm31_inv(qm31_mul(d0, d1)));
+    cum = qm31_add(cum, frac);
+    out[((size_t)4 * rep + 0) * n + r] = cum.a.a;
+    out[((size_t)4 * rep + 1) * n + r] = cum.a.b;
+    out[((size_t)4 * rep + 2) * n + r] = cum.b.a;
+    out[((size_t)4 * rep + 3) * n + r] = cum.b.b;
+  }
+}
+
+// Per-coordinate column sums into 64-bit accumulators.
+__global__ void k_column_sums(const uint32_t* __restrict__ cols, uint32_t n_rows, unsigned long long* acc) {
+  uint32_t k = blockIdx.y;
+  const uint32_t* c = cols + (size_t)k * n_rows;
+  unsigned long long s = 0;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += gridDim.x * blockDim.x) s += c[r];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc + k, s);
+}
+
+// Coset order position k <-> bit-reversed circle-domain storage row (utils.rs:96-115):
+// coset[2i] = natural[i], coset[2i+1] = natural[n-1-i].
+__device__ __forceinline__ uint32_t coset_to_storage(uint32_t k, uint32_t log_n) {
+  uint32_t n = 1u << log_n;
+  uint32_t nat = (k & 1) ? (n - 1 - (k >> 1)) : (k >> 1);
+  return brev(nat, log_n);
+}
+
+// tmp[k] = col[storage(k)] - shift  (four coordinate columns, blockIdx.y)
+__global__ void k_coset_gather(uint32_t* cols, uint32_t log_n, uint4 shift, uint32_t* tmp) {
+  uint32_t k = blockIdx.y;
+  uint32_t n = 1u << log_n;
+  uint32_t sh = k == 0 ? shift.x : k == 1 ? shift.y : k == 2 ? shift.z : shift.w;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    tmp[(size_t)k * n + i] = m31_sub(cols[(size_t)k * n + coset_to_storage(i, log_n)], sh);
+}
+__global__ void k_coset_scatter(uint32_t* cols, uint32_t log_n, const uint32_t* tmp) {
+  uint32_t k = blockIdx.y;
+  uint32_t n = 1u << log_n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    cols[(size_t)k * n + coset_to_storage(i, log_n)] = tmp[(size_t)k * n + i];
+}
+
+// Inclusive M31 scan of `len` words per row (blockIdx.y) in tiles of 4096 (256 threads x 16).
+// Tile totals go to `sums` (exclusive offsets are applied by k_scan_add).
+__global__ void __launch_bounds__(256) k_scan_tiles(uint32_t* data, uint32_t len, uint32_t* sums, uint32_t n_tiles) {
+  __shared__ uint32_t warp_tot[8];
+  uint32_t* d = data + (size_t)blockIdx.y * len;
+  uint32_t base = blockIdx.x * 4096 + threadIdx.x * 16;
+  uint32_t v[16];
+  uint32_t run = 0;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    uint32_t x = base + i < len ? d[base + i] : 0;
+    run = m31_add(run, x);
+    v[i] = run;
+  }
+  // Exclusive scan of the thread totals within the block.
+  uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t incl = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl = m31_add(incl, y);
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  uint32_t wpre = 0;
+  for (uint32_t j = 0; j < w; j++) wpre = m31_add(wpre, warp_tot[j]);
+  uint32_t excl = m31_add(wpre, m31_sub(incl, run));
+#pragma unroll
+  for (int i = 0; i < 16; i++)
+    if (base + i < len) d[base + i] = m31_add(v[i], excl);
+  if (threadIdx.x == 255) sums[(size_t)blockIdx.y * n_tiles + blockIdx.x] = m31_add(excl, run);
+}
+__global__ void k_scan_add(uint32_t* data, uint32_t len, const uint32_t* tile_offsets, uint32_t n_tiles) {
+  uint32_t* d = data + (size_t)blockIdx.y * len;
+  uint32_t t = blockIdx.x;
+  if (t == 0) return;
+  uint32_t off = tile_offsets[(size_t)blockIdx.y * n_tiles + t - 1];
+  for (uint32_t i = threadIdx.x; i < 4096; i += blockDim.x) {
+    uint32_t idx = t * 4096 + i;
+    if (idx < len) d[idx] = m31_add(d[idx], off);
+  }
+}
+
+// Inclusive scan of `rows` arrays of `len` words (len <= 4096^2), in place.
+static int32_t scan_rows(uint32_t* data, uint32_t len, uint32_t rows, Arena& arena, cudaStream_t s) {
+  uint32_t n_tiles = (len + 4095) / 4096;
+  STWO_REQUIRE(n_tiles <= 4096, "scan length too large");
+  uint32_t* sums = arena.alloc((size_t)n_tiles * rows);
+  if (!sums) return STWO_ERR_OOM;
+  k_scan_tiles<<<dim3(n_tiles, rows), 256, 0, s>>>(data, len, sums, n_tiles);
+  note_launch();
+  STWO_LAUNCH_CHECK();
+  if (n_tiles > 1) {
+    uint32_t* sums2 = arena.alloc(rows);
+    if (!sums2) return STWO_ERR_OOM;
+    k_scan_tiles<<<dim3(1, rows), 256, 0, s>>>(sums, n_tiles, sums2, 1);
+    note_launch();
+    STWO_LAUNCH_CHECK();
+    k_scan_add<<<dim3(n_tiles, rows), 256, 0, s>>>(data, len, sums, n_tiles);
+    note_launch();
+    STWO_LAUNCH_CHECK();
+  }
+  return STWO_OK;
+}
+
+// ------------------------------------------------------------------------------------ composition
+struct PoseidonParams {
+  uint32_t trace_log, eval_log;
+  uint32_t shift[4];  // claimed_sum / 2^trace_log
+  LookupConsts lc;
+};
+
+__device__ __forceinline__ uint32_t prev_row_index(uint32_t r, uint32_t trace_log, uint32_t eval_log) {
+  // offset_bit_reversed_circle_domain_index(r, trace_log, eval_log, -1) (core/utils.rs:74-90)
+  uint32_t prev = brev(r, eval_log);
+  uint32_t half = 1u << (eval_log - 1);
+  uint32_t step = 1u << (eval_log - trace_log - 1);
+  if (prev < half) prev = (prev + half - step) & (half - 1);
+  else prev = ((prev - half + step) & (half - 1)) + half;
+  return brev(prev, eval_log);
+}
+
+__global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* const* __restrict__ cols,
+                                                              uint32_t n_rows, PoseidonParams pp,
+                                                              const uint32_t* __restrict__ coeffs,
+                                                              const uint32_t* __restrict__ dinv, uint32_t* o0,
+                                                              uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+  __shared__ uint32_t s_coeffs[4 * PS_N_CONSTRAINTS];
+  for (uint32_t i = threadIdx.x; i < 4 * PS_N_CONSTRAINTS; i += blockDim.x) s_coeffs[i] = coeffs[i];
+  __syncthreads();
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  uint32_t cnt = 0;
+  int ci = 0;
+  auto acc = [&](uint32_t cons) {
+    const uint32_t* k = s_coeffs + 4 * ci++;
+    a0 += (unsigned long long)k[0] * cons;
+    a1 += (unsigned long long)k[1] * cons;
+    a2 += (unsigned long long)k[2] * cons;
+    a3 += (unsigned long long)k[3] * cons;
+    if (++cnt == 3) {
+      a0 = (a0 & P) + (a0 >> 31);
+      a1 = (a1 & P) + (a1 >> 31);
+      a2 = (a2 & P) + (a2 >> 31);
+      a3 = (a3 & P) + (a3 >> 31);
+      cnt = 0;
+    }
+  };
+  qm31 logup = qm31_zero();
+  qm31 prev_col = qm31_zero();
+  uint32_t rp = prev_row_index(r, pp.trace_log, pp.eval_log);
+  for (int rep = 0; rep < PS_REPS; rep++) {
+    const uint32_t* const* c = cols + rep * PS_COLS_PER_REP;
+    uint32_t s[PS_ST], init[PS_ST];
+#pragma unroll
+    for (int i = 0; i < PS_ST; i++) {
+      s[i] = __ldg(c[i] + r);
+      init[i] = s[i];
+    }
+    int mc = PS_ST;
+    for (int round = 0; round < 2 * PS_HALF + PS_PARTIAL; round++) {
+      bool full = round < PS_HALF || round >= PS_HALF + PS_PARTIAL;
+      if (full) {
+#pragma unroll
+        for (int i = 0; i < PS_ST; i++) s[i] = m31_add(s[i], PS_RC);
+        external_matrix(s);
+#pragma unroll
+        for (int i = 0; i < PS_ST; i++) {
+          uint32_t m = __ldg(c[mc++] + r);
+          acc(m31_sub(pow5(s[i]), m));
+          s[i] = m;
+        }
+      } else {
+        s[0] = m31_add(s[0], PS_RC);
+        internal_matrix(s);
+        uint32_t m = __ldg(c[mc++] + r);
+        acc(m31_sub(pow5(s[0]), m));
+        s[0] = m;
+      }
+    }
+    // LogUp batch `rep`: fraction (1/d0 - 1/d1) = (d1 - d0) / (d0 d1).
+    qm31 d0 = combine16(pp.lc, init), d1 = combine16(pp.lc, s);
+    qm31 num = qm31_sub(d1, d0), den = qm31_mul(d0, d1);
+    const uint32_t* const* ic = cols + PS_COLS + 4 * rep;
+    qm31 cur = qm31_from_u32(__ldg(ic[0] + r), __ldg(ic[1] + r), __ldg(ic[2] + r), __ldg(ic[3] + r));
+    qm31 diff;
+    if (rep + 1 < PS_REPS) {
+      diff = qm31_sub(cur, prev_col);
+      prev_col = cur;
+    } else {
+      qm31 prev = qm31_from_u32(__ldg(ic[0] + rp), __ldg(ic[1] + rp), __ldg(ic[2] + rp), __ldg(ic[3] + rp));
+      diff = qm31_add(qm31_sub(qm31_sub(cur, prev), prev_col),
+                      qm31_from_u32(pp.shift[0], pp.shift[1], pp.shift[2], pp.shift[3]));
+    }
+    qm31 cons = qm31_sub(qm31_mul(diff, den), num);
+    const uint32_t* k = s_coeffs + 4 * (PS_N_CONSTRAINTS - PS_REPS + rep);
+    logup = qm31_add(logup, qm31_mul(qm31_from_u32(k[0], k[1], k[2], k[3]), cons));
+  }
+  qm31 res = qm31_add(qm31_from_u32(fold64_p(a0), fold64_p(a1), fold64_p(a2), fold64_p(a3)), logup);
+  uint32_t d = __ldg(dinv + (r >> pp.trace_log));
+  o0[r] = m31_mul(res.a.a, d);
+  o1[r] = m31_mul(res.a.b, d);
+  o2[r] = m31_mul(res.b.a, d);
+  o3[r] = m31_mul(res.b.b, d);
+}
+
+// ------------------------------------------------------------------------------------ host side
+static hq hq_m(hq x, uint32_t m) {
+  for (int i = 0; i < 4; i++) x.v[i] = h_mul(x.v[i], m);
+  return x;
+}
+
+struct HLookup {
+  hq z, alpha_pow[PS_ST];
+  template <class V>
+  hq combine(const V* v) const;
+};
+template <>
+hq HLookup::combine<hq>(const hq* v) const {
+  hq acc = hq_make(0, 0, 0, 0);
+  for (int i = 0; i < PS_ST; i++) acc = hq_add(acc, hq_mul(alpha_pow[i], v[i]));
+  return hq_sub(acc, z);
+}
+
+struct PoseidonGpuAir : GpuAir {
+  uint32_t log_n;
+  HLookup le;
+  hq claimed_sum;
+  PoseidonGpuAir(uint32_t l, const HLookup& e, hq cs) : log_n(l), le(e), claimed_sum(cs) {}
+  uint32_t log_size() const override { return log_n; }
+  uint32_t max_constraint_log_degree_bound() const override { return log_n + PS_LOG_EXPAND; }
+  size_t n_constraints() const override { return PS_N_CONSTRAINTS; }
+  std::vector<std::vector<std::vector<int>>> mask_offsets() const override {
+    std::vector<std::vector<std::vector<int>>> m(3);
+    m[1].assign(PS_COLS, {0});
+    for (int b = 0; b + 1 < PS_REPS; b++)
+      for (int k = 0; k < 4; k++) m[2].push_back({0});
+    for (int k = 0; k < 4; k++) m[2].push_back({-1, 0});
+    return m;
+  }
+  hq shift() const { return hq_m(claimed_sum, h_inv((uint32_t)((1ull << log_n) % P))); }
+  int32_t eval_composition(const std::vector<std::vector<const uint32_t*>>& cols, const uint32_t* coeffs,
+                           const uint32_t* dinv, uint32_t* const acc[4], cudaStream_t s) const override {
+    STWO_REQUIRE(cols.size() >= 3 && cols[1].size() == PS_COLS && cols[2].size() == PS_INTERACTION_COLS,
+                 "trace trees mismatch");
+    std::vector<const uint32_t*> table(cols[1]);
+    table.insert(table.end(), cols[2].begin(), cols[2].end());
+    const uint32_t** d_table = nullptr;
+    int32_t st = scratch_alloc((void**)&d_table, table.size() * sizeof(void*), s);
+    if (st) return st;
+    STWO_CHECK_CUDA(cudaMemcpyAsync(d_table, table.data(), table.size() * sizeof(void*), cudaMemcpyHostToDevice, s));
+    PoseidonParams pp;
+    pp.trace_log = log_n;
+    pp.eval_log = log_n + PS_LOG_EXPAND;
+    hq sh = shift();
+    for (int i = 0; i < 4; i++) pp.shift[i] = sh.v[i];
+    for (int i = 0; i < 4; i++) pp.lc.z[i] = le.z.v[i];
+    for (int j = 0; j < PS_ST; j++)
+      for (int i = 0; i < 4; i++) pp.lc.alpha_pow[j][i] = le.alpha_pow[j].v[i];
+    uint32_t n_rows = 1u << pp.eval_log;
+    k_poseidon_composition<<<(n_rows + 127) / 128, 128, 0, s>>>(d_table, n_rows, pp, coeffs, dinv, acc[0], acc[1],
+                                                                acc[2], acc[3]);
+    note_launch();
+    cudaError_t e = cudaGetLastError();
+    scratch_free(d_table, s);
+    if (e) {
+      set_error("poseidon composition: %s", cudaGetErrorString(e));
+      return STWO_ERR_CUDA;
+    }
+    return STWO_OK;
+  }
+  // The same constraints over QM31 at the OODS point (PointEvaluator).
+  hq eval_at_point(const std::vector<std::vector<std::vector<hq>>>& mask, hq rc, hq denom_inv) const override {
+    hq acc = hq_make(0, 0, 0, 0);
+    auto add = [&](hq c) { acc = hq_add(hq_mul(acc, rc), hq_mul(denom_inv, c)); };
+    auto m4 = [](hq* x) {
+      hq t0 = hq_add(x[0], x[1]), t02 = hq_add(t0, t0), t1 = hq_add(x[2], x[3]), t12 = hq_add(t1, t1);
+      hq t2 = hq_add(hq_add(x[1], x[1]), t1), t3 = hq_add(hq_add(x[3], x[3]), t0);
+      hq t4 = hq_add(hq_add(t12, t12), t3), t5 = hq_add(hq_add(t02, t02), t2);
+      x[0] = hq_add(t3, t5);
+      x[1] = t5;
+      x[2] = hq_add(t2, t4);
+      x[3] = t4;
+    };
+    auto ext = [&](hq* st) {
+      for (int i = 0; i < 4; i++) m4(st + 4 * i);
+      for (int j = 0; j < 4; j++) {
+        hq t = hq_add(hq_add(st[j], st[j + 4]), hq_add(st[j + 8], st[j + 12]));
+        for (int i = 0; i < 4; i++) st[4 * i + j] = hq_add(st[4 * i + j], t);
+      }
+    };
+    auto p5 = [](hq x) {
+      hq x2 = hq_mul(x, x);
+      return hq_mul(hq_mul(x2, x2), x);
+    };
+    const hq rcq = hq_make(PS_RC, 0, 0, 0);
+    const auto& t = mask[1];
+    const auto& it = mask[2];
+    std::vector<std::pair<hq, hq>> fr;  // (num, den) per batch
+    size_t mc = 0;
+    for (int rep = 0; rep < PS_REPS; rep++) {
+      hq s[PS_ST], init[PS_ST];
+      for (int i = 0; i < PS_ST; i++) init[i] = s[i] = t[mc++][0];
+      for (int round = 0; round < 2 * PS_HALF + PS_PARTIAL; round++) {
+        bool full = round < PS_HALF || round >= PS_HALF + PS_PARTIAL;
+        if (full) {
+          for (int i = 0; i < PS_ST; i++) s[i] = hq_add(s[i], rcq);
+          ext(s);
+          for (int i = 0; i < PS_ST; i++) {
+            hq m = t[mc++][0];
+            add(hq_sub(p5(s[i]), m));
+            s[i] = m;
+          }
+        } else {
+          s[0] = hq_add(s[0], rcq);
+          hq sum = s[0];
+          for (int i = 1; i < 16; i++) sum = hq_add(sum, s[i]);
+          for (int i = 0; i < 16; i++) s[i] = hq_add(hq_m(s[i], 1u << (i + 1)), sum);
+          hq m = t[mc++][0];
+          add(hq_sub(p5(s[0]), m));
+          s[0] = m;
+        }
+      }
+      hq d0 = le.combine(init), d1 = le.combine(s);
+      fr.push_back({hq_sub(d1, d0), hq_mul(d0, d1)});
+    }
+    auto comb = [](const std::vector<hq>& c0, const std::vector<hq>& c1, const std::vector<hq>& c2,
+                   const std::vector<hq>& c3, size_t j) {
+      return hq_add(hq_add(c0[j], hq_mul(c1[j], hq_make(0, 1, 0, 0))),
+                    hq_add(hq_mul(c2[j], hq_make(0, 0, 1, 0)), hq_mul(c3[j], hq_make(0, 0, 0, 1))));
+    };
+    hq prev_col = hq_make(0, 0, 0, 0);
+    for (int b = 0; b < PS_REPS; b++) {
+      const auto& c0 = it[4 * b];
+      const auto& c1 = it[4 * b + 1];
+      const auto& c2 = it[4 * b + 2];
+      const auto& c3 = it[4 * b + 3];
+      hq diff;
+      if (b + 1 < PS_REPS) {
+        hq cur = comb(c0, c1, c2, c3, 0);
+        diff = hq_sub(cur, prev_col);
+        prev_col = cur;
+      } else {
+        hq prev = comb(c0, c1, c2, c3, 0), cur = comb(c0, c1, c2, c3, 1);
+        diff = hq_add(hq_sub(hq_sub(cur, prev), prev_col), shift());
+      }
+      add(hq_sub(hq_mul(diff, fr[b].second), fr[b].first));
+    }
+    return acc;
+  }
+};
+
+}  // namespace stwo
+
+using namespace stwo;
+
+extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* d_init, stwo_pcs_config cfg,
+                                           uint8_t* h_proof, size_t capacity, size_t* h_len,
+                                           stwo_qm31* h_claimed_sum, void* stream) {
+  STWO_REQUIRE(log_n_rows >= 4 && log_n_rows + PS_LOG_EXPAND + cfg.log_blowup_factor <= 28, "bad log_n_rows");
+  STWO_REQUIRE(cfg.log_blowup_factor >= 1 && cfg.log_blowup_factor <= 16, "log_blowup_factor out of [1, 16]");
+  STWO_REQUIRE(cfg.log_last_layer_degree_bound <= 10, "log_last_layer_degree_bound > 10");
+  STWO_REQUIRE(h_len, "null length");
+  cudaStream_t s = as_stream(stream);
+  std::vector<uint8_t> bytes;
+  hq claimed = hq_make(0, 0, 0, 0);
+  int32_t st;
+  {
+    Prover pv(cfg, log_n_rows + PS_LOG_EXPAND + cfg.log_blowup_factor, s);
+    if (pv.init_status) return pv.init_status;
+    size_t n = (size_t)1 << log_n_rows;
+    st = pv.commit_polys({}, {});
+    uint32_t* trace = nullptr;
+    uint32_t* lookups = nullptr;
+    uint32_t* inter = nullptr;
+    if (!st) {
+      trace = pv.arena.alloc(n * PS_COLS);
+      lookups = pv.arena.alloc(n * 32 * PS_REPS);
+      inter = pv.arena.alloc(n * PS_INTERACTION_COLS);
+      if (!trace || !lookups || !inter) st = STWO_ERR_OOM;
+    }
+    if (!st) {
+      k_poseidon_trace<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_init, trace, lookups);
+      note_launch();
+      if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
+    }
+    if (!st) {
+      std::vector<uint32_t*> cols(PS_COLS);
+      for (int c = 0; c < PS_COLS; c++) cols[c] = trace + (size_t)c * n;
+      st = pv.commit_evals(cols, log_n_rows);
+    }
+    HLookup le;
+    if (!st) {
+      // PoseidonElements::draw: draw_felts(2) = one draw of 8 base felts (logup.rs:74-88).
+      auto f = pv.ch.draw_base_felts();
+      le.z = hq_make(f[0], f[1], f[2], f[3]);
+      hq alpha = hq_make(f[4], f[5], f[6], f[7]);
+      hq cur = hq_make(1, 0, 0, 0);
+      for (int i = 0; i < PS_ST; i++) {
+        le.alpha_pow[i] = cur;
+        cur = hq_mul(cur, alpha);
+      }
+      LookupConsts lc;
+      for (int i = 0; i < 4; i++) lc.z[i] = le.z.v[i];
+      for (int j = 0; j < PS_ST; j++)
+        for (int i = 0; i < 4; i++) lc.alpha_pow[j][i] = le.alpha_pow[j].v[i];
+      k_poseidon_interaction<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, lookups, lc, inter);
+      note_launch();
+      if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
+    }
+    if (!st) {
+      // Claimed sum of the last column, its shift, and the coset-order prefix sum (logup.rs:155-195).
+      uint32_t* last = inter + (size_t)(PS_INTERACTION_COLS - 4) * n;
+      unsigned long long* d_sums = reinterpret_cast<unsigned long long*>(pv.arena.alloc(8));
+      uint32_t* tmp = pv.arena.alloc(4 * n);
+      if (!d_sums || !tmp) st = STWO_ERR_OOM;
+      unsigned long long h_sums[4] = {0, 0, 0, 0};
+      if (!st && cudaMemsetAsync(d_sums, 0, 32, s) != cudaSuccess) st = STWO_ERR_CUDA;
+      if (!st) {
+        k_column_sums<<<dim3(std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024), 4), 256, 0, s>>>(last, (uint32_t)n, d_sums);
+        note_launch();
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(h_sums, d_sums, 32, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+          st = STWO_ERR_CUDA;
+      }
+      if (!st) {
+        claimed = hq_make((uint32_t)(h_sums[0] % P), (uint32_t)(h_sums[1] % P), (uint32_t)(h_sums[2] % P),
+                          (uint32_t)(h_sums[3] % P));
+        hq sh = hq_m(claimed, h_inv((uint32_t)(n % P)));
+        uint4 shv = make_uint4(sh.v[0], sh.v[1], sh.v[2], sh.v[3]);
+        uint32_t g = std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024);
+        k_coset_gather<<<dim3(g, 4), 256, 0, s>>>(last, log_n_rows, shv, tmp);
+        note_launch();
+        st = cudaGetLastError() ? STWO_ERR_CUDA : STWO_OK;
+        if (!st) st = scan_rows(tmp, (uint32_t)n, 4, pv.arena, s);
+        if (!st) {
+          k_coset_scatter<<<dim3(g, 4), 256, 0, s>>>(last, log_n_rows, tmp);
+          note_launch();
+          st = cudaGetLastError() ? STWO_ERR_CUDA : STWO_OK;
+        }
+      }
+    }
+    if (!st) {
+      std::vector<uint32_t*> cols(PS_INTERACTION_COLS);
+      for (int c = 0; c < PS_INTERACTION_COLS; c++) cols[c] = inter + (size_t)c * n;
+      st = pv.commit_evals(cols, log_n_rows);
+    }
+    if (!st) {
+      PoseidonGpuAir air(log_n_rows, le, claimed);
+      st = pv.prove(air, bytes);
+    }
+    cudaStreamSynchronize(s);
+  }
+  if (st) return st;
+  if (h_claimed_sum)
+    for (int i = 0; i < 4; i++) h_claimed_sum->v[i] = claimed.v[i];
+  *h_len = bytes.size();
+  STWO_REQUIRE(bytes.size() <= capacity, "proof buffer too small (%zu bytes needed)", bytes.size());
+  if (h_proof) memcpy(h_proof, bytes.data(), bytes.size());
+  return STWO_OK;
+}

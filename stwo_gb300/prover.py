@@ -36,3 +36,17 @@ def prove_wide_fib(log_n_rows: int, trace: Sequence[torch.Tensor], cfg=DEFAULT_C
     call("stwo_prove_wide_fib", log_n_rows, len(trace), _ptrs(trace), pcs_config(cfg), buf, cap, C.byref(n),
          _stream())
     return bytes(buf[: n.value])
+
+
+def prove_poseidon(log_n_rows: int, init=None, cfg=DEFAULT_CONFIG):
+    """Proves the Poseidon2 AIR; `init` is None (reference inputs) or a device int32 tensor of
+    initial states. Returns (proof bytes, claimed LogUp sum)."""
+    from ._lib import QM31
+
+    cap = 1 << 26
+    buf = (C.c_uint8 * cap)()
+    n = C.c_size_t()
+    cs = QM31()
+    call("stwo_prove_poseidon", log_n_rows, init.data_ptr() if init is not None else None, pcs_config(cfg), buf,
+         cap, C.byref(n), C.byref(cs), _stream())
+    return bytes(buf[: n.value]), tuple(cs.v)

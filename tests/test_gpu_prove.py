@@ -41,3 +41,22 @@ def test_wide_fib_reference_inputs(cuda, oracle):
         a, b = np.ones(n, np.uint32), np.arange(n, dtype=np.uint32)
         got = prove_wide_fib(log_n, wide_fib_trace(log_n, 100, dev(a), dev(b)))
         assert got == oracle.prove_wide_fib(log_n, 100, a, b)
+
+
+@pytest.mark.parametrize("log_n,seeded,cfg", [(4, False, (5, 1, 0, 3)), (5, False, (10, 1, 0, 3)),
+                                              (6, True, (5, 1, 0, 3)), (8, True, (3, 2, 1, 4)),
+                                              (10, False, (10, 1, 0, 3))])
+def test_poseidon_proof_bytes_match_oracle(cuda, oracle, log_n, seeded, cfg):
+    from stwo_gb300.prover import prove_poseidon
+
+    init = None
+    if seeded:
+        rng = np.random.default_rng(log_n)
+        init = F.rand_m31(rng, (1 << log_n) * 8 * 16)
+    want, want_cs = oracle.prove_poseidon(log_n, init, cfg)
+    got, cs = prove_poseidon(log_n, dev(init) if seeded else None, cfg)
+    assert cs == want_cs
+    assert len(got) == len(want)
+    assert got == want
+    ok, why = oracle.verify_poseidon(log_n, cs, got)
+    assert ok, why
