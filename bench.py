@@ -1,7 +1,15 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 prover backend.
 
-Default workload (`--workload kernels`): the kernel microbench on synthetic seeded inputs —
+Default workload (`--workload poseidon`): one proof of the Poseidon2 AIR with 2^16 rows (2^19
+permutations, 1264 trace + 32 LogUp interaction columns), seeded uniform initial states,
+PcsConfig { pow_bits 10, FriConfig(0, 1, 3) }. One step = one proof through the C ABI
+(stwo_prove_poseidon). `value` is trace cells/s = 2^16 x 1296 / proof time with the initial
+states resident in HBM; `e2e` copies them from pinned host memory inside the timed region (the
+proof bytes always come back to the host). Per-stage device times come from one extra,
+separately timed proof.
+
+Kernel workload (`--workload kernels`): the kernel microbench on synthetic seeded inputs —
 interpolate then evaluate 256 columns of 2^20 M31 words (canonic coset, log 20) at blowup 4
 (2^22 points each), Blake2s Merkle commit over the 256 x 2^22 evaluations, and one FRI fold of a
 2^22-point QM31 circle evaluation down to a 2^4 line with seeded alphas. One step = that whole
@@ -191,6 +199,48 @@ class KernelsWorkload:
             self.fri_host[k].copy_(self.last.cols[k], non_blocking=True)
 
 
+class PoseidonWorkload:
+    """Single proof of the Poseidon2 AIR: 2^16 rows x 8 permutations (2^19 permutations), seeded
+    uniform initial states, LogUp interaction trace, pow_bits 10, blowup 2, 3 FRI queries."""
+
+    LOG = 16
+    CFG = (10, 1, 0, 3)
+    TRACE_COLS = 1264 + 32
+
+    def __init__(self, log=None):
+        import numpy as np
+        import torch
+
+        if log:
+            self.LOG = log
+        n = (1 << self.LOG) * 8 * 16
+        self.host_in = torch.empty(n, dtype=torch.int32).pin_memory()
+        self.host_in.numpy().view(np.uint32)[:] = gen_words(3, 0, n)
+        self.inp = self.host_in.cuda()
+        self.work = torch.empty_like(self.inp)
+        self.cells = (1 << self.LOG) * self.TRACE_COLS
+
+    def step(self, from_host=False):
+        from stwo_gb300.prover import prove_poseidon
+
+        src = self.work if from_host else self.inp
+        if from_host:
+            self.work.copy_(self.host_in, non_blocking=True)
+        self.proof, self.claimed_sum = prove_poseidon(self.LOG, src, self.CFG)
+        return self.proof
+
+    def stage_bytes(self):
+        """Algorithmic HBM bytes of the HBM-bound stages (reads + writes of the column data)."""
+        n = 1 << self.LOG
+        cols = self.TRACE_COLS
+        return {
+            "Composition extension": cols * (4 * n + 4 * 4 * n),
+            "Constraint point-wise eval": cols * 4 * 4 * n + 4 * 4 * 4 * n,
+            "Interpolation for commitment": cols * 8 * n,
+            "Compute FRI quotients": cols * 4 * n + 4 * 4 * 2 * n + 4 * 4 * 8 * n,
+        }
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -211,13 +261,129 @@ def run_gb300(args):
     if world > 1:
         torch.distributed.barrier()
     _lib.call("stwo_device_init", local)
-    wl = KernelsWorkload(n_cols=args.n_cols)
-    lib = wl.lib
+    lib = _lib.load()
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
+
+    def max_over_ranks(v):
+        if world > 1:
+            t = torch.tensor([v], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    if args.workload == "kernels":
+        return run_kernels(args, world, rank, local, lib, barrier, max_over_ranks)
+
+    wl = PoseidonWorkload()
+    for _ in range(args.warmup):
+        wl.step()
+    barrier()
+    launches0 = lib.stwo_kernel_launches()
+    times = []
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            wl.step()
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        barrier()
+        wall = time.perf_counter() - t0
+    launches = lib.stwo_kernel_launches() - launches0
+    step_ms = max_over_ranks(float(np.mean(times)))
+    # End to end: initial states from pinned host memory, proof bytes back on the host.
+    for _ in range(max(1, args.warmup // 2)):
+        wl.step(from_host=True)
+    barrier()
+    et = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        wl.step(from_host=True)
+        torch.cuda.synchronize()
+        et.append((time.perf_counter() - t1) * 1e3)
+    e2e_ms = max_over_ranks(float(np.mean(et)))
+    # One extra proof with per-stage device timing (outside the timed region).
+    _lib.call("stwo_set_stage_timing", 1)
+    wl.step()
+    names = (C.c_char_p * 64)()
+    ms = (C.c_float * 64)()
+    k = lib.stwo_stage_times(names, ms, 64)
+    _lib.call("stwo_set_stage_timing", 0)
+    stages = {names[i].decode(): float(ms[i]) for i in range(min(k, 64))}
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    sbytes = wl.stage_bytes()
+    hbm_stages = {k2: v for k2, v in stages.items() if k2 in sbytes and v > 0}
+    dom = max(hbm_stages, key=hbm_stages.get) if hbm_stages else None
+    roof = None
+    if dom:
+        ach = sbytes[dom] / (hbm_stages[dom] / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": sbytes[dom],
+                "stage_ms": hbm_stages[dom]}
+    line = {
+        "metric": "proof s & trace cells/s (Poseidon2 2^16 rows)",
+        "value": wl.cells * world / (step_ms / 1e3),
+        "unit": "trace cells/s",
+        "proof_s": step_ms / 1e3,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32 (M31 field words)",
+        "data": "synthetic: seeded uniform M31 initial states (splitmix64 mod P)",
+        "config": {"workload": "Poseidon2 AIR proof, 2^16 rows x 8 permutations, LogUp interaction trace",
+                   "log_n_rows": wl.LOG, "trace_cells": wl.cells, "pow_bits": wl.CFG[0], "log_blowup": wl.CFG[1],
+                   "log_last_layer": wl.CFG[2], "n_queries": wl.CFG[3],
+                   "l2": "working set (~3 GB) far larger than L2; no flush", "parallelism": f"replicas x{world}"},
+        "proof_bytes": len(wl.proof),
+        "stages_ms": stages,
+        "roofline": roof,
+        "e2e": {"value": wl.cells * world / (e2e_ms / 1e3), "unit": "trace cells/s", "proof_s": e2e_ms / 1e3,
+                "h2d_bytes_per_step": wl.host_in.numel() * 4, "d2h_bytes_per_step": len(wl.proof)},
+        "gpu_launches": int(launches),
+        "wall_s": wall,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_poseidon(args.cpu_threads, log=15)
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_poseidon(threads=0, log=15):
+    """The oracle's Poseidon2 proof on all host cores (OpenMP), a bounded sample of 2^log rows."""
+    import oracle.pyoracle as O
+
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    nthreads = threads or os.cpu_count() or 1
+    init = gen_words(3, 0, (1 << log) * 8 * 16)
+    t0 = time.perf_counter()
+    O.prove_poseidon(log, init, PoseidonWorkload.CFG)
+    secs = time.perf_counter() - t0
+    cells = (1 << log) * PoseidonWorkload.TRACE_COLS
+    return {"value": cells / secs, "unit": "trace cells/s", "cores": nthreads, "kind": "port",
+            "proof_s": secs, "sample": f"one full Poseidon2 proof of 2^{log} rows (the same AIR, config and "
+                                        f"input generator; 1/{1 << (16 - log)} of the rows): {secs:.2f} s"}
+
+
+def run_kernels(args, world, rank, local, lib, barrier, max_over_ranks):
+    import numpy as np
+    import torch
+
+    wl = KernelsWorkload(n_cols=args.n_cols)
 
     # Warm-up.
     for _ in range(args.warmup):
@@ -242,11 +408,7 @@ def run_gb300(args):
         for i in range(5):
             stage_ms[i] += evs[s][i].elapsed_time(evs[s][i + 1])
     stage_ms /= args.steps
-    step_ms = float(stage_ms.sum())
-    if world > 1:
-        t = torch.tensor([step_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(float(stage_ms.sum()))
 
     # End to end through the public API: pinned host inputs -> HBM -> hot path -> root + FRI layer.
     for _ in range(max(1, args.warmup)):
@@ -263,11 +425,7 @@ def run_gb300(args):
         wl.readback()
     e1.record()
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
 
     if rank != 0:
         return
@@ -336,33 +494,43 @@ def cpu_baseline_kernels(threads=0, n_cols=16):
 
 
 def run_reference(args):
+    """The reference arm: the oracle (C++ restatement of the reference CPU prover; the Rust crate
+    needs cargo, which this image lacks) on all host cores. Rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from stwo_gb300.build import build_oracle
 
     build_oracle()
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline_kernels(args.cpu_threads, n_cols=4)
-    for _ in range(args.steps):
-        vals.append(cpu_baseline_kernels(args.cpu_threads, n_cols=8))
+    if args.workload == "kernels":
+        for _ in range(args.warmup):
+            cpu_baseline_kernels(args.cpu_threads, n_cols=4)
+        vals = [cpu_baseline_kernels(args.cpu_threads, n_cols=8) for _ in range(args.steps)]
+        metric = ("trace cells/s (kernel microbench: interpolate+evaluate 256x2^20 @ blowup 4, "
+                  "Blake2s Merkle 256x2^22, FRI fold 2^22->2^4)")
+        unit = "cells/s"
+        config = {"workload": "kernels: 256 cols x 2^20 -> 2^22 (blowup 4) + Merkle + FRI 2^22->2^4",
+                  "sample_cols_per_step": 8}
+    else:
+        log = 14
+        for _ in range(min(args.warmup, 1)):
+            cpu_baseline_poseidon(args.cpu_threads, log=log)
+        vals = [cpu_baseline_poseidon(args.cpu_threads, log=log) for _ in range(args.steps)]
+        metric = "proof s & trace cells/s (Poseidon2 2^16 rows)"
+        unit = "trace cells/s"
+        config = {"workload": "Poseidon2 AIR proof, 2^16 rows x 8 permutations, LogUp interaction trace",
+                  "sample_rows_per_step": 1 << log}
     v = sorted(x["value"] for x in vals)[len(vals) // 2]
     cb = dict(vals[0])
     cb["value"] = v
     out = {
-        "impl": "reference",
-        "metric": "trace cells/s (kernel microbench: interpolate+evaluate 256x2^20 @ blowup 4, "
-                  "Blake2s Merkle 256x2^22, FRI fold 2^22->2^4)",
-        "value": v, "unit": "cells/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 8 * (1 << 20) / v * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
-        "data": "synthetic seeded (splitmix64 mod P)",
-        "config": {"workload": "kernels: 256 cols x 2^20 -> 2^22 (blowup 4) + Merkle + FRI 2^22->2^4",
-                   "sample_cols_per_step": 8},
-        "cpu_baseline": cb,
-        "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "C++ restatement of the reference CPU backend (the Rust reference needs cargo, absent here)",
+        "impl": "reference", "metric": metric, "value": v, "unit": unit,
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(sorted(x.get("proof_s", 0) for x in vals)[len(vals) // 2]) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
+        "data": "synthetic seeded (splitmix64 mod P)", "config": config, "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "C++ restatement of the reference CPU prover (the Rust reference needs cargo, absent here)",
     }
     print(json.dumps(out), flush=True)
 
@@ -373,6 +541,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="poseidon", choices=["poseidon", "kernels"],
+                    help="poseidon: the headline Poseidon2 2^16-row proof; kernels: the kernel microbench")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-cols", type=int, default=0, help="columns of the kernel workload (default 256; "

@@ -66,6 +66,12 @@ stwo_status stwo_sync(void* stream);
 /* Diagnostic without a reference counterpart: kernels launched by this library so far
  * (benchmarks report the count inside their timed region). */
 uint64_t stwo_kernel_launches(void);
+/* Diagnostics without a reference counterpart: per-stage device times of the prover on the
+ * calling thread, named after the reference's tracing spans ("Extension", "Merkle", ...).
+ * stwo_set_stage_timing(1) enables recording (and clears earlier records); stwo_stage_times
+ * returns the number of distinct stages and fills up to `cap` names / summed milliseconds. */
+stwo_status stwo_set_stage_timing(int enable);
+uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap);
 
 /* Column storage: Column::zeros / uninitialized / to_cpu / at
  * (crates/prover/src/core/backend/mod.rs:46-65). */

@@ -58,6 +58,8 @@ SIGNATURES = {
     "stwo_device_init": (C.c_int32, [C.c_int]),
     "stwo_sync": (C.c_int32, [VP]),
     "stwo_kernel_launches": (C.c_uint64, []),
+    "stwo_set_stage_timing": (C.c_int32, [C.c_int]),
+    "stwo_stage_times": (C.c_uint32, [C.POINTER(C.c_char_p), C.POINTER(C.c_float), U32]),
     "stwo_buf_alloc": (C.c_int32, [PVP, C.c_size_t, VP]),
     "stwo_buf_free": (C.c_int32, [VP, VP]),
     "stwo_buf_upload": (C.c_int32, [VP, VP, C.c_size_t, VP]),

@@ -543,6 +543,7 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
       if (!trace || !lookups || !inter) st = STWO_ERR_OOM;
     }
     if (!st) {
+      StageScope stage("Generation", s);
       k_poseidon_trace<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_init, trace, lookups);
       note_launch();
       if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
@@ -563,6 +564,7 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
         le.alpha_pow[i] = cur;
         cur = hq_mul(cur, alpha);
       }
+      StageScope stage("Interaction", s);
       LookupConsts lc;
       for (int i = 0; i < 4; i++) lc.z[i] = le.z.v[i];
       for (int j = 0; j < PS_ST; j++)

@@ -146,6 +146,16 @@ struct ConstColPtrs { const uint32_t* p[MAX_PARAM_COLS]; };
 // Count of kernel launches issued by this library (diagnostic, read by benchmarks).
 void note_launch();
 
+// Optional per-stage device timing of the prover (names follow the reference's tracing spans).
+// Disabled by default; when enabled, each scope records a pair of CUDA events on its stream.
+void stage_begin(const char* name, cudaStream_t s);
+void stage_end(cudaStream_t s);
+struct StageScope {
+  cudaStream_t s;
+  StageScope(const char* name, cudaStream_t st) : s(st) { stage_begin(name, st); }
+  ~StageScope() { stage_end(s); }
+};
+
 // Number of SMs of the current device (152 on GB300).
 int sm_count();
 

@@ -288,6 +288,7 @@ int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t>
   for (size_t i = 0; i < t.polys.size(); i++) by_log[t.poly_logs[i]].push_back(i);
   t.evals.assign(t.polys.size(), nullptr);
   t.eval_logs.assign(t.polys.size(), 0);
+  StageScope stage_ext("Extension", s);
   for (auto& kv : by_log) {
     uint32_t el = kv.first + cfg.log_blowup_factor;
     std::vector<const uint32_t*> src;
@@ -303,6 +304,7 @@ int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t>
     if (st) return st;
   }
   for (size_t i = 0; i < t.evals.size(); i++) refs.push_back({t.evals[i], t.eval_logs[i]});
+  StageScope stage_merkle("Merkle", s);
   int32_t st = t.merkle.commit(refs, arena, s);
   if (st) return st;
   ch.mix_root(t.merkle.root);
@@ -312,6 +314,7 @@ int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t>
 int32_t Prover::commit_evals(const std::vector<uint32_t*>& cols, uint32_t log_size) {
   // Interpolate in place (the evaluation is consumed, as PolyOps::interpolate takes it by value).
   if (!cols.empty()) {
+    StageScope stage("Interpolation for commitment", s);
     int32_t st = fft_interpolate(tree, canonic_half_coset(log_size), cols.data(), (uint32_t)cols.size(), s);
     if (st) return st;
   }
@@ -368,6 +371,7 @@ int32_t Prover::commit_composition(const GpuAir& air, hq rc) {
   uint32_t* d_dinv = d_coeffs + coeffs.size();
   STWO_CHECK_CUDA(cudaMemcpyAsync(d_coeffs, coeffs.data(), coeffs.size() * 4, cudaMemcpyHostToDevice, s));
   STWO_CHECK_CUDA(cudaMemcpyAsync(d_dinv, dinv.data(), dinv.size() * 4, cudaMemcpyHostToDevice, s));
+  StageScope stage_cext("Composition extension", s);
   // Trace columns on the evaluation domain, per tree (extension when the committed domain differs).
   std::vector<std::vector<const uint32_t*>> tcols(trees.size());
   for (size_t ti = 0; ti < trees.size(); ti++) {
@@ -397,8 +401,10 @@ int32_t Prover::commit_composition(const GpuAir& air, hq rc) {
     acc[k] = arena.alloc((size_t)1 << eval_log);
     if (!acc[k]) return STWO_ERR_OOM;
   }
+  StageScope stage_cons("Constraint point-wise eval", s);
   int32_t st = air.eval_composition(tcols, d_coeffs, d_dinv, acc, s);
   if (st) return st;
+  StageScope stage_ci("Constraints interpolation", s);
   st = fft_interpolate(tree, canonic_half_coset(eval_log), acc, 4, s);
   if (st) return st;
   return commit_polys({acc[0], acc[1], acc[2], acc[3]}, std::vector<uint32_t>(4, eval_log));
@@ -448,6 +454,7 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
       }
     }
   std::vector<stwo_qm31> svals(qpts.size());
+  StageScope stage_oods("Evaluate columns out of domain", s);
   st = eval_at_points(polys.data(), plogs.data(), (uint32_t)polys.size(), poly_of.data(), qpts.data(),
                       (uint32_t)qpts.size(), svals.data(), s);
   if (st) return st;
@@ -498,6 +505,7 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   }
   std::stable_sort(cols.begin(), cols.end(), [](const ColS& a, const ColS& b) { return a.log > b.log; });
   hq qrc = ch.draw_felt();
+  StageScope stage_q("Compute FRI quotients", s);
   std::vector<SecureCols> quotients;
   std::vector<uint32_t> qlogs;
   for (size_t i = 0; i < cols.size();) {
@@ -539,6 +547,7 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     i = j;
   }
 
+  StageScope stage_fri("FRI commitment", s);
   // FRI commitment (fri.rs:168-290).
   std::vector<ColRef> first_cols;
   for (size_t i = 0; i < quotients.size(); i++)
@@ -616,6 +625,7 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   // Proof of work (pcs/prover.rs:122-125).
   uint64_t nonce = 0;
   {
+    StageScope stage_g("Grind", s);
     uint32_t d[8];
     ch.digest.words(d);
     st = stwo_grind_blake2s(d, cfg.pow_bits, &nonce, s);
@@ -623,6 +633,7 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   }
   ch.mix_u64(nonce);
 
+  StageScope stage_dec("Decommitment", s);
   // Decommitment (fri.rs:295-334, pcs/prover.rs:127-137): record every word to read, gather.
   Gather g;
   Queries q = generate_queries(ch, qlogs[0], cfg.n_queries);

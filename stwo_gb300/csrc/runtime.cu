@@ -17,6 +17,29 @@ void set_error(const char* fmt, ...) {
 static std::atomic<unsigned long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+struct StageRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+static thread_local bool g_stage_on = false;
+static thread_local std::vector<StageRec> g_stages;
+static thread_local int g_stage_open = -1;
+
+void stage_begin(const char* name, cudaStream_t s) {
+  if (!g_stage_on) return;
+  if (g_stage_open >= 0) stage_end(s);
+  StageRec r{name, nullptr, nullptr};
+  if (cudaEventCreate(&r.a) != cudaSuccess || cudaEventCreate(&r.b) != cudaSuccess) return;
+  cudaEventRecord(r.a, s);
+  g_stages.push_back(r);
+  g_stage_open = (int)g_stages.size() - 1;
+}
+void stage_end(cudaStream_t s) {
+  if (!g_stage_on || g_stage_open < 0) return;
+  cudaEventRecord(g_stages[g_stage_open].b, s);
+  g_stage_open = -1;
+}
+
 DeviceContext& ctx() {
   static DeviceContext c;
   return c;
@@ -160,6 +183,45 @@ const char* stwo_status_string(stwo_status s) {
 const char* stwo_last_error(void) { return g_err; }
 
 uint64_t stwo_kernel_launches(void) { return g_launches.load(); }
+
+stwo_status stwo_set_stage_timing(int enable) {
+  g_stage_on = enable != 0;
+  for (auto& r : g_stages) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  g_stages.clear();
+  g_stage_open = -1;
+  return STWO_OK;
+}
+
+uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap) {
+  std::vector<std::pair<const char*, float>> agg;
+  for (auto& r : g_stages) {
+    float t = 0;
+    if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&t, r.a, r.b) != cudaSuccess) t = -1;
+    bool found = false;
+    for (auto& a : agg)
+      if (strcmp(a.first, r.name) == 0) {
+        a.second += t;
+        found = true;
+      }
+    if (!found) agg.push_back({r.name, t});
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  g_stages.clear();
+  g_stage_open = -1;
+  uint32_t n = 0;
+  for (auto& a : agg) {
+    if (n < cap) {
+      if (names) names[n] = a.first;
+      if (ms) ms[n] = a.second;
+    }
+    n++;
+  }
+  return n;
+}
 
 stwo_status stwo_device_init(int device) {
   STWO_CHECK_CUDA(cudaSetDevice(device));
