@@ -40,7 +40,7 @@ Arena::~Arena() {
 }
 uint32_t* Arena::alloc(size_t words) {
   void* p = nullptr;
-  if (cudaMallocAsync(&p, std::max<size_t>(words, 1) * 4, s) != cudaSuccess) {
+  if (scratch_alloc(&p, std::max<size_t>(words, 1) * 4, s) != STWO_OK) {
     failed = true;
     return nullptr;
   }
@@ -293,9 +293,10 @@ int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t>
     uint32_t el = kv.first + cfg.log_blowup_factor;
     std::vector<const uint32_t*> src;
     std::vector<uint32_t*> dst;
+    uint32_t* block = arena.alloc(kv.second.size() << el);
+    if (!block) return STWO_ERR_OOM;
     for (size_t i : kv.second) {
-      t.evals[i] = arena.alloc((size_t)1 << el);
-      if (!t.evals[i]) return STWO_ERR_OOM;
+      t.evals[i] = block + (dst.size() << el);
       t.eval_logs[i] = el;
       src.push_back(t.polys[i]);
       dst.push_back(t.evals[i]);
@@ -378,12 +379,15 @@ int32_t Prover::commit_composition(const GpuAir& air, hq rc) {
     Tree& t = trees[ti];
     std::vector<const uint32_t*> src;
     std::vector<uint32_t*> ext;
+    size_t n_ext = 0;
+    for (size_t c = 0; c < t.evals.size(); c++) n_ext += t.eval_logs[c] != eval_log;
+    uint32_t* block = n_ext ? arena.alloc(n_ext << eval_log) : nullptr;
+    if (n_ext && !block) return STWO_ERR_OOM;
     for (size_t c = 0; c < t.evals.size(); c++) {
       if (t.eval_logs[c] == eval_log) {
         tcols[ti].push_back(t.evals[c]);
       } else {
-        uint32_t* e = arena.alloc((size_t)1 << eval_log);
-        if (!e) return STWO_ERR_OOM;
+        uint32_t* e = block + (ext.size() << eval_log);
         src.push_back(t.polys[c]);
         ext.push_back(e);
         tcols[ti].push_back(e);

@@ -56,9 +56,25 @@ int sm_count() {
   return n;
 }
 
+// Keeps freed stream-ordered memory cached in the device's default pool instead of returning it
+// at every synchronisation (the default release threshold is 0), so repeated proofs reuse their
+// working set without re-mapping it.
+static void keep_pool_memory() {
+  static thread_local int done_dev = -1;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev == done_dev) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done_dev = dev;
+}
+
 int32_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
   *p = nullptr;
   if (bytes == 0) return STWO_OK;
+  keep_pool_memory();
   STWO_CHECK_CUDA(cudaMallocAsync(p, bytes, s));
   return STWO_OK;
 }

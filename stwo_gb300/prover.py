@@ -15,6 +15,17 @@ from .backend import _ptrs, _stream
 
 DEFAULT_CONFIG = (5, 1, 0, 3)  # PcsConfig::default(): pow_bits 5, FriConfig::new(0, 1, 3)
 
+_OUT_CAP = 1 << 26
+_out_buf = None
+
+
+def _out():
+    """A reusable host buffer for proof bytes (allocated once; proofs are far smaller)."""
+    global _out_buf
+    if _out_buf is None:
+        _out_buf = (C.c_uint8 * _OUT_CAP)()
+    return _out_buf
+
 
 def pcs_config(cfg: Tuple[int, int, int, int] = DEFAULT_CONFIG) -> PcsConfig:
     """(pow_bits, log_blowup_factor, log_last_layer_degree_bound, n_queries)."""
@@ -30,12 +41,11 @@ def wide_fib_trace(log_n_rows: int, n_cols: int, a: torch.Tensor, b: torch.Tenso
 
 def prove_wide_fib(log_n_rows: int, trace: Sequence[torch.Tensor], cfg=DEFAULT_CONFIG) -> bytes:
     """Proves the wide-Fibonacci AIR over `trace` (consumed: it holds coefficients afterwards)."""
-    cap = 1 << 24
-    buf = (C.c_uint8 * cap)()
+    buf = _out()
     n = C.c_size_t()
-    call("stwo_prove_wide_fib", log_n_rows, len(trace), _ptrs(trace), pcs_config(cfg), buf, cap, C.byref(n),
+    call("stwo_prove_wide_fib", log_n_rows, len(trace), _ptrs(trace), pcs_config(cfg), buf, _OUT_CAP, C.byref(n),
          _stream())
-    return bytes(buf[: n.value])
+    return C.string_at(buf, n.value)
 
 
 def prove_poseidon(log_n_rows: int, init=None, cfg=DEFAULT_CONFIG):
@@ -43,10 +53,9 @@ def prove_poseidon(log_n_rows: int, init=None, cfg=DEFAULT_CONFIG):
     initial states. Returns (proof bytes, claimed LogUp sum)."""
     from ._lib import QM31
 
-    cap = 1 << 26
-    buf = (C.c_uint8 * cap)()
+    buf = _out()
     n = C.c_size_t()
     cs = QM31()
     call("stwo_prove_poseidon", log_n_rows, init.data_ptr() if init is not None else None, pcs_config(cfg), buf,
-         cap, C.byref(n), C.byref(cs), _stream())
-    return bytes(buf[: n.value]), tuple(cs.v)
+         _OUT_CAP, C.byref(n), C.byref(cs), _stream())
+    return C.string_at(buf, n.value), tuple(cs.v)
