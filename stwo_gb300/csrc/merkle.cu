@@ -106,6 +106,94 @@ int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint3
   return STWO_OK;
 }
 
+// ---------------------------------------------------------------- node subtrees
+// Layers made only of child hashes (no columns of that size): each block hashes 2^k nodes of the
+// first output layer from their children, then keeps halving in shared memory, writing every
+// level, so one launch covers up to 8 levels of the tree (vcs/prover.rs:39-61 layer by layer).
+constexpr int SUBTREE_LOG = 8;
+
+struct LayerPtrs {
+  uint32_t* p[SUBTREE_LOG + 1];
+};
+
+__device__ __forceinline__ void hash_children(const uint32_t* l, const uint32_t* r, uint32_t h[8]) {
+  uint32_t m[16];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    m[q] = l[q];
+    m[8 + q] = r[q];
+  }
+  b2s_init(h);
+  b2s_compress(h, m, 64, true);
+}
+
+__global__ void __launch_bounds__(256) k_merkle_subtrees(const uint32_t* __restrict__ prev, uint32_t first_log,
+                                                         uint32_t levels, LayerPtrs outs) {
+  __shared__ uint32_t sm[256 * 8];
+  const uint32_t t = threadIdx.x;
+  const uint32_t node = blockIdx.x * blockDim.x + t;  // node of layer first_log
+  uint32_t h[8];
+  if (node < (1u << first_log)) {
+    const uint4* pp = reinterpret_cast<const uint4*>(prev + (size_t)16 * node);
+    uint32_t m[16];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      uint4 w = pp[q];
+      m[4 * q] = w.x;
+      m[4 * q + 1] = w.y;
+      m[4 * q + 2] = w.z;
+      m[4 * q + 3] = w.w;
+    }
+    b2s_init(h);
+    b2s_compress(h, m, 64, true);
+    uint4* po = reinterpret_cast<uint4*>(outs.p[0] + (size_t)8 * node);
+    po[0] = make_uint4(h[0], h[1], h[2], h[3]);
+    po[1] = make_uint4(h[4], h[5], h[6], h[7]);
+#pragma unroll
+    for (int q = 0; q < 8; q++) sm[t * 8 + q] = h[q];
+  }
+  __syncthreads();
+  uint32_t width = blockDim.x;
+  for (uint32_t lv = 1; lv < levels; lv++) {
+    width >>= 1;
+    uint32_t out_node = blockIdx.x * width + t;
+    if (t < width) {
+      hash_children(sm + (2 * t) * 8, sm + (2 * t + 1) * 8, h);
+      uint4* po = reinterpret_cast<uint4*>(outs.p[lv] + (size_t)8 * out_node);
+      po[0] = make_uint4(h[0], h[1], h[2], h[3]);
+      po[1] = make_uint4(h[4], h[5], h[6], h[7]);
+    }
+    __syncthreads();
+    if (t < width) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) sm[t * 8 + q] = h[q];
+    }
+    __syncthreads();
+  }
+}
+
+// Hashes the pure node layers first_log, first_log - 1, ..., first_log - n_levels + 1 from `prev`
+// (layer first_log + 1). out[i] receives layer first_log - i.
+int32_t merkle_node_layers(const uint32_t* prev, uint32_t first_log, uint32_t n_levels, uint32_t* const* out,
+                           cudaStream_t s) {
+  uint32_t done = 0;
+  while (done < n_levels) {
+    uint32_t lg = first_log - done;
+    uint32_t block_log = lg < (uint32_t)SUBTREE_LOG ? lg : (uint32_t)SUBTREE_LOG;
+    uint32_t lv = std::min<uint32_t>(n_levels - done, block_log + 1);
+    LayerPtrs lp;
+    for (uint32_t i = 0; i < lv; i++) lp.p[i] = out[done + i];
+    uint32_t threads = 1u << block_log;
+    uint32_t blocks = 1u << (lg - block_log);
+    k_merkle_subtrees<<<blocks, threads, 0, s>>>(prev, lg, lv, lp);
+    note_launch();
+    STWO_LAUNCH_CHECK();
+    prev = out[done + lv - 1];
+    done += lv;
+  }
+  return STWO_OK;
+}
+
 // ---------------------------------------------------------------- grind
 // Tests nonces [base, base + n): the smallest with >= pow_bits trailing zeros in word 0 of the
 // raw compression (digest, [lo, hi, 0, ...], t = 0, f = 0) is folded into *best by atomicMin.

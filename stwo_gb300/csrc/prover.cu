@@ -23,6 +23,8 @@ int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* c
                      uint32_t* const* out, uint32_t n, cudaStream_t s);
 int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols, uint32_t n_cols,
                             uint32_t* out, cudaStream_t s);
+int32_t merkle_node_layers(const uint32_t* prev, uint32_t first_log, uint32_t n_levels, uint32_t* const* out,
+                           cudaStream_t s);
 int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, stwo_qm31 rc_in,
                              const stwo_sample_batch* batches, uint32_t n_batches, uint32_t log_blowup,
                              uint32_t* const out[4], cudaStream_t s);
@@ -103,15 +105,30 @@ int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cuda
   std::stable_sort(sorted.begin(), sorted.end(), [](const ColRef& a, const ColRef& b) { return a.log > b.log; });
   uint32_t max_log = sorted.empty() ? 0 : sorted[0].log;
   layers.assign(max_log + 1, nullptr);
+  // One block for all layers: 2^(max_log + 1) - 1 hashes.
+  uint32_t* all = arena.alloc((size_t)8 * ((2ull << max_log) - 1));
+  if (!all) return STWO_ERR_OOM;
+  for (uint32_t lg = 0; lg <= max_log; lg++) layers[lg] = all + (size_t)8 * ((1ull << lg) - 1);
   size_t ci = 0;
-  for (int lg = (int)max_log; lg >= 0; lg--) {
+  int lg = (int)max_log;
+  while (lg >= 0) {
     std::vector<const uint32_t*> lc;
     while (ci < sorted.size() && sorted[ci].log == (uint32_t)lg) lc.push_back(sorted[ci++].p);
-    layers[lg] = arena.alloc((size_t)8 << lg);
-    if (!layers[lg]) return STWO_ERR_OOM;
     const uint32_t* prev = (uint32_t)lg < max_log ? layers[lg + 1] : nullptr;
-    int32_t st = merkle_commit_layer((uint32_t)lg, prev, lc.data(), (uint32_t)lc.size(), layers[lg], s);
+    if (!lc.empty() || !prev) {
+      int32_t st = merkle_commit_layer((uint32_t)lg, prev, lc.data(), (uint32_t)lc.size(), layers[lg], s);
+      if (st) return st;
+      lg--;
+      continue;
+    }
+    // A run of layers made only of child hashes, down to the next layer with columns.
+    int stop = lg;
+    while (stop - 1 >= 0 && !(ci < sorted.size() && sorted[ci].log == (uint32_t)(stop - 1))) stop--;
+    std::vector<uint32_t*> outs;
+    for (int l = lg; l >= stop; l--) outs.push_back(layers[l]);
+    int32_t st = merkle_node_layers(prev, (uint32_t)lg, (uint32_t)outs.size(), outs.data(), s);
     if (st) return st;
+    lg = stop - 1;
   }
   uint32_t w[8];
   STWO_CHECK_CUDA(cudaMemcpyAsync(w, layers[0], 32, cudaMemcpyDeviceToHost, s));

@@ -42,53 +42,123 @@ __device__ __forceinline__ uint32_t red64(unsigned long long x) {
 }
 __device__ __forceinline__ unsigned long long fold64(unsigned long long x) { return (x & P) + (x >> 31); }
 
+// Entry staged in shared memory: the column pointer itself and the coefficient c_j.
+struct QStage {
+  const uint32_t* col;
+  uint32_t c[4];
+};
+
+constexpr int Q_ROWS = 32;    // rows per block (one warp-width of consecutive rows)
+constexpr int Q_SLICES = 8;   // column slices per row; 256 threads
+constexpr int Q_STAGE = 512;  // entries staged in shared memory at a time
+
+// One block = 32 consecutive rows x 8 column slices: a warp reads 32 consecutive words of one
+// column, the 8 warps stream disjoint columns of the same rows, and the 8 partial sums of a
+// batch meet in shared memory. Slice 0 then finishes the batch (line term, denominator).
 __global__ void __launch_bounds__(256) k_quotient_rows(uint32_t rows, uint32_t log_n, uint32_t half_init,
                                                        uint32_t half_step, QCols cols,
                                                        const QBatch* __restrict__ batches, uint32_t n_batches,
                                                        const QEntry* __restrict__ entries, uint32_t* o0, uint32_t* o1,
                                                        uint32_t* o2, uint32_t* o3) {
-  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
-  // Domain point of bit-reversed row r of the circle domain with half coset (init, step).
-  uint32_t k = brev(r, log_n);
-  uint32_t half = 1u << (log_n - 1);
-  uint32_t idx = k < half ? half_init + half_step * k : (0u - (half_init + half_step * (k - half)));
-  cpoint p = index_to_point(idx & 0x7fffffffu);
-
+  __shared__ QStage st[Q_STAGE];
+  __shared__ uint32_t part[Q_SLICES][Q_ROWS][4];
+  const uint32_t lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
+  const uint32_t r = blockIdx.x * Q_ROWS + lane;
+  const bool live = r < rows;
+  cpoint p = {0u, 0u};
+  if (slice == 0 && live) {
+    // Domain point of bit-reversed row r of the circle domain with half coset (init, step).
+    uint32_t k = brev(r, log_n);
+    uint32_t half = 1u << (log_n - 1);
+    uint32_t idx = k < half ? half_init + half_step * k : (0u - (half_init + half_step * (k - half)));
+    p = index_to_point(idx & 0x7fffffffu);
+  }
   qm31 acc = qm31_zero();
   for (uint32_t b = 0; b < n_batches; b++) {
     const QBatch& B = batches[b];
     unsigned long long s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-    uint32_t cnt = 0;
-    for (uint32_t e = B.e0; e < B.e1; e++) {
-      const QEntry& E = entries[e];
-      uint32_t v = __ldg(cols.p[E.col] + r);
-      s0 += (unsigned long long)E.c[0] * v;
-      s1 += (unsigned long long)E.c[1] * v;
-      s2 += (unsigned long long)E.c[2] * v;
-      s3 += (unsigned long long)E.c[3] * v;
-      if (++cnt == 3) {
-        s0 = fold64(s0);
-        s1 = fold64(s1);
-        s2 = fold64(s2);
-        s3 = fold64(s3);
-        cnt = 0;
+    for (uint32_t e0 = B.e0; e0 < B.e1; e0 += Q_STAGE) {
+      uint32_t ne = min((uint32_t)Q_STAGE, B.e1 - e0);
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < ne; i += blockDim.x) {
+        const QEntry& E = entries[e0 + i];
+        st[i].col = cols.p[E.col];
+        st[i].c[0] = E.c[0];
+        st[i].c[1] = E.c[1];
+        st[i].c[2] = E.c[2];
+        st[i].c[3] = E.c[3];
+      }
+      __syncthreads();
+      if (live) {
+        uint32_t cnt = 0;
+        uint32_t i = slice;
+        // Four independent column loads in flight per iteration.
+        for (; i + 3 * Q_SLICES < ne; i += 4 * Q_SLICES) {
+          uint32_t v[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) v[u] = __ldg(st[i + u * Q_SLICES].col + r);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const QStage& q = st[i + u * Q_SLICES];
+            s0 += (unsigned long long)q.c[0] * v[u];
+            s1 += (unsigned long long)q.c[1] * v[u];
+            s2 += (unsigned long long)q.c[2] * v[u];
+            s3 += (unsigned long long)q.c[3] * v[u];
+            if (u == 1 || u == 3) {
+              s0 = fold64(s0);
+              s1 = fold64(s1);
+              s2 = fold64(s2);
+              s3 = fold64(s3);
+            }
+          }
+        }
+        for (; i < ne; i += Q_SLICES) {
+          uint32_t v = __ldg(st[i].col + r);
+          s0 += (unsigned long long)st[i].c[0] * v;
+          s1 += (unsigned long long)st[i].c[1] * v;
+          s2 += (unsigned long long)st[i].c[2] * v;
+          s3 += (unsigned long long)st[i].c[3] * v;
+          if (++cnt == 2) {
+            s0 = fold64(s0);
+            s1 = fold64(s1);
+            s2 = fold64(s2);
+            s3 = fold64(s3);
+            cnt = 0;
+          }
+        }
       }
     }
-    qm31 cv = qm31_from_u32(red64(s0), red64(s1), red64(s2), red64(s3));
-    qm31 lin = qm31_add(qm31_mul_m31(qm31_from_u32(B.sum_a[0], B.sum_a[1], B.sum_a[2], B.sum_a[3]), p.y),
-                        qm31_from_u32(B.sum_b[0], B.sum_b[1], B.sum_b[2], B.sum_b[3]));
-    qm31 num = qm31_sub(cv, lin);
-    cm31 px = {p.x, 0u}, py = {p.y, 0u};
-    cm31 den = cm31_sub(cm31_mul(cm31_sub({B.prx[0], B.prx[1]}, px), {B.piy[0], B.piy[1]}),
-                        cm31_mul(cm31_sub({B.pry[0], B.pry[1]}, py), {B.pix[0], B.pix[1]}));
-    acc = qm31_add(qm31_mul(acc, qm31_from_u32(B.coeff[0], B.coeff[1], B.coeff[2], B.coeff[3])),
-                   qm31_mul_cm31(num, cm31_inv(den)));
+    part[slice][lane][0] = red64(s0);
+    part[slice][lane][1] = red64(s1);
+    part[slice][lane][2] = red64(s2);
+    part[slice][lane][3] = red64(s3);
+    __syncthreads();
+    if (slice == 0 && live) {
+      uint32_t cv[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int sl = 0; sl < Q_SLICES; sl++) t = m31_add(t, part[sl][lane][q]);
+        cv[q] = t;
+      }
+      qm31 lin = qm31_add(qm31_mul_m31(qm31_from_u32(B.sum_a[0], B.sum_a[1], B.sum_a[2], B.sum_a[3]), p.y),
+                          qm31_from_u32(B.sum_b[0], B.sum_b[1], B.sum_b[2], B.sum_b[3]));
+      qm31 num = qm31_sub(qm31_from_u32(cv[0], cv[1], cv[2], cv[3]), lin);
+      cm31 px = {p.x, 0u}, py = {p.y, 0u};
+      cm31 den = cm31_sub(cm31_mul(cm31_sub({B.prx[0], B.prx[1]}, px), {B.piy[0], B.piy[1]}),
+                          cm31_mul(cm31_sub({B.pry[0], B.pry[1]}, py), {B.pix[0], B.pix[1]}));
+      acc = qm31_add(qm31_mul(acc, qm31_from_u32(B.coeff[0], B.coeff[1], B.coeff[2], B.coeff[3])),
+                     qm31_mul_cm31(num, cm31_inv(den)));
+    }
+    __syncthreads();  // `part` is rewritten by the next batch
   }
-  o0[r] = acc.a.a;
-  o1[r] = acc.a.b;
-  o2[r] = acc.b.a;
-  o3[r] = acc.b.b;
+  if (slice == 0 && live) {
+    o0[r] = acc.a.a;
+    o1[r] = acc.a.b;
+    o2[r] = acc.b.a;
+    o3[r] = acc.b.b;
+  }
 }
 
 int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, stwo_qm31 rc_in,
@@ -162,7 +232,7 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
   for (uint32_t c = 0; c < n_cols; c++) qc.p[c] = cols[c];
   uint32_t* o[4];
   for (int q = 0; q < 4; q++) o[q] = direct ? out[q] : d_sub + (size_t)q * rows;
-  k_quotient_rows<<<(rows + 255) / 256, 256, 0, s>>>(rows, log_n, dom_half.initial_index, dom_half.step_size, qc,
+  k_quotient_rows<<<(rows + Q_ROWS - 1) / Q_ROWS, 256, 0, s>>>(rows, log_n, dom_half.initial_index, dom_half.step_size, qc,
                                                      d_b, n_batches, d_e, o[0], o[1], o[2], o[3]); note_launch();
   if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
 
