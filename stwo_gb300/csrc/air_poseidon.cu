@@ -287,9 +287,8 @@ __global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* co
                                                               const uint32_t* __restrict__ coeffs,
                                                               const uint32_t* __restrict__ dinv, uint32_t* o0,
                                                               uint32_t* o1, uint32_t* o2, uint32_t* o3) {
-  __shared__ uint4 s_coeffs[PS_N_CONSTRAINTS];
-  for (uint32_t i = threadIdx.x; i < PS_N_CONSTRAINTS; i += blockDim.x)
-    s_coeffs[i] = make_uint4(coeffs[4 * i], coeffs[4 * i + 1], coeffs[4 * i + 2], coeffs[4 * i + 3]);
+  __shared__ uint32_t s_coeffs[4 * PS_N_CONSTRAINTS];
+  for (uint32_t i = threadIdx.x; i < 4 * PS_N_CONSTRAINTS; i += blockDim.x) s_coeffs[i] = coeffs[i];
   __syncthreads();
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
@@ -297,11 +296,11 @@ __global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* co
   uint32_t cnt = 0;
   int ci = 0;
   auto acc = [&](uint32_t cons) {
-    const uint4 k = s_coeffs[ci++];
-    a0 += (unsigned long long)k.x * cons;
-    a1 += (unsigned long long)k.y * cons;
-    a2 += (unsigned long long)k.z * cons;
-    a3 += (unsigned long long)k.w * cons;
+    const uint32_t* k = s_coeffs + 4 * ci++;
+    a0 += (unsigned long long)k[0] * cons;
+    a1 += (unsigned long long)k[1] * cons;
+    a2 += (unsigned long long)k[2] * cons;
+    a3 += (unsigned long long)k[3] * cons;
     if (++cnt == 3) {
       a0 = (a0 & P) + (a0 >> 31);
       a1 = (a1 & P) + (a1 >> 31);
@@ -357,8 +356,8 @@ __global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* co
                       qm31_from_u32(pp.shift[0], pp.shift[1], pp.shift[2], pp.shift[3]));
     }
     qm31 cons = qm31_sub(qm31_mul(diff, den), num);
-    const uint4 k = s_coeffs[PS_N_CONSTRAINTS - PS_REPS + rep];
-    logup = qm31_add(logup, qm31_mul(qm31_from_u32(k.x, k.y, k.z, k.w), cons));
+    const uint32_t* k = s_coeffs + 4 * (PS_N_CONSTRAINTS - PS_REPS + rep);
+    logup = qm31_add(logup, qm31_mul(qm31_from_u32(k[0], k[1], k[2], k[3]), cons));
   }
   qm31 res = qm31_add(qm31_from_u32(fold64_p(a0), fold64_p(a1), fold64_p(a2), fold64_p(a3)), logup);
   uint32_t d = __ldg(dinv + (r >> pp.trace_log));

@@ -279,6 +279,46 @@ __global__ void __launch_bounds__(1 << (C + NL - 4)) k_fft_tile(FftPass p, Const
   }
 }
 
+// Strided pass of RB <= 4 layers [lo, lo + RB) straight from HBM to registers: each thread owns
+// the 2^RB words g0 + k * 2^lo (k < 2^RB) where g0 has zero layer bits; consecutive threads take
+// consecutive low bits, so every load and store of a warp is one 128-byte line. No shared memory
+// and no barrier. Requires lo >= 5.
+template <bool INV, int RB>
+__global__ void __launch_bounds__(256) k_fft_reg(FftPass p, ConstColPtrs src, ColPtrs dst) {
+  const uint32_t col = blockIdx.y;
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;  // < 2^(L - RB)
+  // Insert RB zero bits at position lo.
+  const uint32_t g0 = (gid & ((1u << p.lo) - 1)) | ((gid >> p.lo) << (p.lo + RB));
+  const uint32_t* s = p.read_src ? src.p[col] : dst.p[col];
+  const uint32_t smask = p.read_src ? ((1u << p.F) - 1) : 0xffffffffu;
+  uint32_t* d = dst.p[col];
+  uint32_t v[1 << RB];
+#pragma unroll
+  for (int k = 0; k < (1 << RB); k++) v[k] = __ldg(&s[(g0 + ((uint32_t)k << p.lo)) & smask]);
+#pragma unroll
+  for (int jj = 0; jj < RB; jj++) {
+    const int j = INV ? jj : (RB - 1 - jj);
+    const uint32_t layer = p.lo + j;
+    const uint32_t* twp = p.tw + (p.tw_size - (1u << (p.L - layer))) + (g0 >> (layer + 1));
+#pragma unroll
+    for (int kh = 0; kh < (1 << (RB - 1 - j)); kh++) {
+      const uint32_t t = __ldg(twp + kh);
+      const int k0 = kh << (j + 1);
+#pragma unroll
+      for (int kl = 0; kl < (1 << j); kl++) {
+        if (INV) ibfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+        else bfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < (1 << RB); k++) {
+    uint32_t x = v[k];
+    if (p.scale != 1u) x = m31_mul(x, p.scale);
+    d[g0 + ((uint32_t)k << p.lo)] = x;
+  }
+}
+
 // Launches the specialised kernel when one exists for (c, nl); returns false otherwise.
 template <bool INV>
 static bool launch_tile(const FftPass& p, dim3 grid, cudaStream_t s, const ConstColPtrs& sp, const ColPtrs& dp) {
@@ -381,7 +421,19 @@ static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, c
       uint32_t threads = std::max<uint32_t>(32, groups);
       size_t smem = ((size_t)(1u << p.T) + ((1u << p.T) >> 5) + 1) * 4;
       bool done = false;
-      if (L >= 3 && p.T >= 4) done = inverse ? launch_tile<true>(p, grid, s, sp, dp) : launch_tile<false>(p, grid, s, sp, dp);
+      if (p.lo >= 5 && p.nl >= 1 && p.nl <= 4 && L - p.nl >= 8) {
+        // Register-only strided pass.
+        dim3 g2(1u << (L - p.nl - 8), nc);
+#define STWO_REG_CASE(RB)                                                       \
+  if (p.nl == RB) {                                                             \
+    if (inverse) k_fft_reg<true, RB><<<g2, 256, 0, s>>>(p, sp, dp);             \
+    else k_fft_reg<false, RB><<<g2, 256, 0, s>>>(p, sp, dp);                    \
+  }
+        STWO_REG_CASE(1) STWO_REG_CASE(2) STWO_REG_CASE(3) STWO_REG_CASE(4)
+#undef STWO_REG_CASE
+        done = true;
+      }
+      if (!done && L >= 3 && p.T >= 4) done = inverse ? launch_tile<true>(p, grid, s, sp, dp) : launch_tile<false>(p, grid, s, sp, dp);
       if (done) {
       } else if (threads <= 256) {
         if (inverse) k_fft_pass<true, 256><<<grid, threads, smem, s>>>(p, sp, dp);
