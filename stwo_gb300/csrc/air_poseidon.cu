@@ -282,9 +282,12 @@ __device__ __forceinline__ uint32_t prev_row_index(uint32_t r, uint32_t trace_lo
   return brev(prev, eval_log);
 }
 
-__global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* const* __restrict__ cols,
-                                                              uint32_t n_rows, PoseidonParams pp,
-                                                              const uint32_t* __restrict__ coeffs,
+// Trace (1264) and interaction (32) columns are contiguous blocks with a stride of 2^eval_log
+// words, so a mask value is one load at base + (col << eval_log) + row. Each round's masks are
+// loaded before its arithmetic so that their latency hides behind the matrix and S-box work.
+__global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* __restrict__ trace,
+                                                              const uint32_t* __restrict__ inter, uint32_t n_rows,
+                                                              PoseidonParams pp, const uint32_t* __restrict__ coeffs,
                                                               const uint32_t* __restrict__ dinv, uint32_t* o0,
                                                               uint32_t* o1, uint32_t* o2, uint32_t* o3) {
   __shared__ uint32_t s_coeffs[4 * PS_N_CONSTRAINTS];
@@ -292,6 +295,8 @@ __global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* co
   __syncthreads();
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
+  const uint32_t el = pp.eval_log;
+  auto col = [&](const uint32_t* base, uint32_t c, uint32_t row) { return __ldg(base + ((size_t)c << el) + row); };
   unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
   uint32_t cnt = 0;
   int ci = 0;
@@ -313,45 +318,55 @@ __global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* co
   qm31 prev_col = qm31_zero();
   uint32_t rp = prev_row_index(r, pp.trace_log, pp.eval_log);
   for (int rep = 0; rep < PS_REPS; rep++) {
-    const uint32_t* const* c = cols + rep * PS_COLS_PER_REP;
+    const uint32_t c0 = rep * PS_COLS_PER_REP;
     uint32_t s[PS_ST], init[PS_ST];
 #pragma unroll
     for (int i = 0; i < PS_ST; i++) {
-      s[i] = __ldg(c[i] + r);
+      s[i] = col(trace, c0 + i, r);
       init[i] = s[i];
     }
-    int mc = PS_ST;
-    for (int round = 0; round < 2 * PS_HALF + PS_PARTIAL; round++) {
-      bool full = round < PS_HALF || round >= PS_HALF + PS_PARTIAL;
-      if (full) {
+    uint32_t mc = c0 + PS_ST;
+    auto full_round = [&]() {
+      uint32_t m[PS_ST];
 #pragma unroll
-        for (int i = 0; i < PS_ST; i++) s[i] = m31_add(s[i], PS_RC);
-        external_matrix(s);
+      for (int i = 0; i < PS_ST; i++) m[i] = col(trace, mc + i, r);
+      mc += PS_ST;
 #pragma unroll
-        for (int i = 0; i < PS_ST; i++) {
-          uint32_t m = __ldg(c[mc++] + r);
-          acc(m31_sub(pow5(s[i]), m));
-          s[i] = m;
-        }
-      } else {
+      for (int i = 0; i < PS_ST; i++) s[i] = m31_add(s[i], PS_RC);
+      external_matrix(s);
+#pragma unroll
+      for (int i = 0; i < PS_ST; i++) {
+        acc(m31_sub(pow5(s[i]), m[i]));
+        s[i] = m[i];
+      }
+    };
+    for (int round = 0; round < PS_HALF; round++) full_round();
+    {
+      uint32_t m[PS_PARTIAL];
+#pragma unroll
+      for (int i = 0; i < PS_PARTIAL; i++) m[i] = col(trace, mc + i, r);
+      mc += PS_PARTIAL;
+#pragma unroll
+      for (int round = 0; round < PS_PARTIAL; round++) {
         s[0] = m31_add(s[0], PS_RC);
         internal_matrix(s);
-        uint32_t m = __ldg(c[mc++] + r);
-        acc(m31_sub(pow5(s[0]), m));
-        s[0] = m;
+        acc(m31_sub(pow5(s[0]), m[round]));
+        s[0] = m[round];
       }
     }
+    for (int round = 0; round < PS_HALF; round++) full_round();
     // LogUp batch `rep`: fraction (1/d0 - 1/d1) = (d1 - d0) / (d0 d1).
     qm31 d0 = combine16(pp.lc, init), d1 = combine16(pp.lc, s);
     qm31 num = qm31_sub(d1, d0), den = qm31_mul(d0, d1);
-    const uint32_t* const* ic = cols + PS_COLS + 4 * rep;
-    qm31 cur = qm31_from_u32(__ldg(ic[0] + r), __ldg(ic[1] + r), __ldg(ic[2] + r), __ldg(ic[3] + r));
+    const uint32_t ic = 4 * rep;
+    qm31 cur = qm31_from_u32(col(inter, ic, r), col(inter, ic + 1, r), col(inter, ic + 2, r), col(inter, ic + 3, r));
     qm31 diff;
     if (rep + 1 < PS_REPS) {
       diff = qm31_sub(cur, prev_col);
       prev_col = cur;
     } else {
-      qm31 prev = qm31_from_u32(__ldg(ic[0] + rp), __ldg(ic[1] + rp), __ldg(ic[2] + rp), __ldg(ic[3] + rp));
+      qm31 prev = qm31_from_u32(col(inter, ic, rp), col(inter, ic + 1, rp), col(inter, ic + 2, rp),
+                                col(inter, ic + 3, rp));
       diff = qm31_add(qm31_sub(qm31_sub(cur, prev), prev_col),
                       qm31_from_u32(pp.shift[0], pp.shift[1], pp.shift[2], pp.shift[3]));
     }
@@ -406,12 +421,12 @@ struct PoseidonGpuAir : GpuAir {
                            const uint32_t* dinv, uint32_t* const acc[4], cudaStream_t s) const override {
     STWO_REQUIRE(cols.size() >= 3 && cols[1].size() == PS_COLS && cols[2].size() == PS_INTERACTION_COLS,
                  "trace trees mismatch");
-    std::vector<const uint32_t*> table(cols[1]);
-    table.insert(table.end(), cols[2].begin(), cols[2].end());
-    const uint32_t** d_table = nullptr;
-    int32_t st = scratch_alloc((void**)&d_table, table.size() * sizeof(void*), s);
-    if (st) return st;
-    STWO_CHECK_CUDA(cudaMemcpyAsync(d_table, table.data(), table.size() * sizeof(void*), cudaMemcpyHostToDevice, s));
+    // The prover hands each tree's columns on the evaluation domain as one contiguous block.
+    const uint32_t el = log_n + PS_LOG_EXPAND;
+    for (int c = 0; c < PS_COLS; c++)
+      STWO_REQUIRE(cols[1][c] == cols[1][0] + ((size_t)c << el), "trace columns are not one contiguous block");
+    for (int c = 0; c < PS_INTERACTION_COLS; c++)
+      STWO_REQUIRE(cols[2][c] == cols[2][0] + ((size_t)c << el), "interaction columns are not one contiguous block");
     PoseidonParams pp;
     pp.trace_log = log_n;
     pp.eval_log = log_n + PS_LOG_EXPAND;
@@ -421,11 +436,10 @@ struct PoseidonGpuAir : GpuAir {
     for (int j = 0; j < PS_ST; j++)
       for (int i = 0; i < 4; i++) pp.lc.alpha_pow[j][i] = le.alpha_pow[j].v[i];
     uint32_t n_rows = 1u << pp.eval_log;
-    k_poseidon_composition<<<(n_rows + 127) / 128, 128, 0, s>>>(d_table, n_rows, pp, coeffs, dinv, acc[0], acc[1],
-                                                                acc[2], acc[3]);
+    k_poseidon_composition<<<(n_rows + 127) / 128, 128, 0, s>>>(cols[1][0], cols[2][0], n_rows, pp, coeffs, dinv,
+                                                                acc[0], acc[1], acc[2], acc[3]);
     note_launch();
     cudaError_t e = cudaGetLastError();
-    scratch_free(d_table, s);
     if (e) {
       set_error("poseidon composition: %s", cudaGetErrorString(e));
       return STWO_ERR_CUDA;
