@@ -174,6 +174,55 @@ stwo_status stwo_secure_accumulate(uint32_t* const d_acc[4], const uint32_t* con
 /* AccumulationOps::generate_secure_powers (accumulation.rs:156-157). */
 stwo_status stwo_generate_secure_powers(stwo_qm31 felt, uint32_t n_powers, stwo_qm31* h_out, void* stream);
 
+/* ------------------------------------------------------------------ GkrOps / MleOps */
+/* Mle columns (crates/prover/src/core/lookups/mle.rs:16-19) hold values on the boolean hypercube,
+ * first variable = most significant index bit. Layer kinds of gkr_prover.rs:94-108: */
+#define STWO_GKR_GRAND_PRODUCT 0u        /* d_num = the secure column, d_den unused */
+#define STWO_GKR_LOGUP_GENERIC 1u        /* d_num, d_den secure */
+#define STWO_GKR_LOGUP_MULTIPLICITIES 2u /* d_num[0] = base-field numerators, d_den secure */
+#define STWO_GKR_LOGUP_SINGLES 3u        /* numerators implicitly 1 (d_num unused), d_den secure */
+
+/* GkrOps::gen_eq_evals (gkr_prover.rs:28; backend/simd/lookups/gkr.rs:22-54): eq(x, y) * v for
+ * every x in {0,1}^n_y (n_y <= 30), into 2^n_y secure values. */
+stwo_status stwo_gkr_gen_eq_evals(const stwo_qm31* h_y, uint32_t n_y, stwo_qm31 v, uint32_t* const d_out[4],
+                                  void* stream);
+/* GkrOps::next_layer (gkr_prover.rs:31; backend/simd/lookups/gkr.rs:56-74): the layer of
+ * 2^(log_n-1) gates above a layer of 2^log_n. A grand product writes d_next_num only; every LogUp
+ * kind writes a generic layer (d_next_num, d_next_den). */
+stwo_status stwo_gkr_next_layer(uint32_t kind, uint32_t log_n, const uint32_t* const d_num[4],
+                                const uint32_t* const d_den[4], uint32_t* const d_next_num[4],
+                                uint32_t* const d_next_den[4], void* stream);
+/* GkrOps::sum_as_poly_in_first_variable (gkr_prover.rs:36-41; backend/simd/lookups/gkr.rs:76-127)
+ * for the GkrMultivariatePolyOracle (gkr_prover.rs:285-318) of a layer of 2^log_n gates (log_n >=
+ * 2): eq evaluations d_eq_evals (at least 2^(log_n-2) values) generated from y = h_y[0..n_y),
+ * lambda and eq_fixed_var_correction. Writes the round polynomial's monomial coefficients
+ * (leading zeros dropped, at most 4) and their count. Synchronous. */
+stwo_status stwo_gkr_sum_as_poly_in_first_variable(uint32_t kind, uint32_t log_n, const uint32_t* const d_num[4],
+                                                   const uint32_t* const d_den[4],
+                                                   const uint32_t* const d_eq_evals[4], const stwo_qm31* h_y,
+                                                   uint32_t n_y, stwo_qm31 lambda,
+                                                   stwo_qm31 eq_fixed_var_correction, stwo_qm31 claim,
+                                                   stwo_qm31* h_coeffs, uint32_t* h_n_coeffs, void* stream);
+/* MleOps<BaseField>::fix_first_variable (mle.rs:9-14; backend/simd/lookups/mle.rs:14-45):
+ * out[i] = a * (in[i + h] - in[i]) + in[i], h = 2^(log_n-1), into a secure column. */
+stwo_status stwo_mle_fix_first_variable_base(uint32_t log_n, const uint32_t* d_mle, stwo_qm31 assignment,
+                                             uint32_t* const d_out[4], void* stream);
+/* MleOps<SecureField>::fix_first_variable (backend/simd/lookups/mle.rs:47-91); d_out may equal
+ * d_mle (the reference folds in place). */
+stwo_status stwo_mle_fix_first_variable_secure(uint32_t log_n, const uint32_t* const d_mle[4], stwo_qm31 assignment,
+                                               uint32_t* const d_out[4], void* stream);
+/* gkr_prover::prove_batch (gkr_prover.rs:401-506) over n_instances input layers: instance i has
+ * kind h_kinds[i], 2^h_log_sizes[i] gates (log size >= 1), numerators h_num[4i..4i+4) and
+ * denominators h_den[4i..4i+4) (device pointers; entries a kind does not use may be NULL). The
+ * Blake2s channel starts from digest h_digest_in (NULL: the default channel) and its final digest is
+ * written to h_digest_out (if not NULL). Writes the canonical bytes of the GkrBatchProof followed by
+ * the GkrArtifact (u64 lengths, QM31 as four LE u32 words, fields in struct order). Inputs are not
+ * modified. Synchronous. */
+stwo_status stwo_gkr_prove_batch(uint32_t n_instances, const uint32_t* h_kinds, const uint32_t* h_log_sizes,
+                                 const uint32_t* const* h_num, const uint32_t* const* h_den,
+                                 const uint8_t* h_digest_in, uint8_t* h_out, size_t capacity, size_t* h_len,
+                                 uint8_t* h_digest_out, void* stream);
+
 /* ------------------------------------------------------------------ GrindOps */
 /* GrindOps<Blake2sChannel>::grind (crates/prover/src/core/proof_of_work.rs:3-7;
  * backend/simd/grind.rs:21-63): the smallest nonce whose raw Blake2s compression of

@@ -277,3 +277,175 @@ int oracle_verify_poseidon(uint32_t log_n, const uint32_t claimed_sum[4], const 
 }
 
 }  // extern "C"
+
+#include "gkr.h"
+
+namespace {
+std::vector<QM31> secure_of(const uint32_t* soa, size_t n) {
+  std::vector<QM31> v(n);
+  for (size_t i = 0; i < n; i++) v[i] = QM31::from_u32(soa[i], soa[n + i], soa[2 * n + i], soa[3 * n + i]);
+  return v;
+}
+void secure_to(const std::vector<QM31>& v, uint32_t* soa) {
+  size_t n = v.size();
+  for (size_t i = 0; i < n; i++) {
+    soa[i] = v[i].a.a.v;
+    soa[n + i] = v[i].a.b.v;
+    soa[2 * n + i] = v[i].b.a.v;
+    soa[3 * n + i] = v[i].b.b.v;
+  }
+}
+std::vector<QM31> qs_of(const uint32_t* aos, size_t n) {
+  std::vector<QM31> v(n);
+  for (size_t i = 0; i < n; i++) v[i] = q_of(aos + 4 * i);
+  return v;
+}
+// Reads one layer from `data`: the grand-product column, or numerators then denominators, each
+// secure column as four coordinate arrays and the multiplicities as one base array.
+GkrLayer layer_of(uint32_t kind, uint32_t log_n, const uint32_t*& data) {
+  size_t n = (size_t)1 << log_n;
+  GkrLayer l;
+  l.kind = (GkrKind)kind;
+  if (kind == GKR_GRAND_PRODUCT || kind == GKR_LOGUP_GENERIC) {
+    l.num = secure_of(data, n);
+    data += 4 * n;
+  } else if (kind == GKR_LOGUP_MULTIPLICITIES) {
+    for (size_t i = 0; i < n; i++) l.num_base.push_back(M31(data[i]));
+    data += n;
+  }
+  if (kind != GKR_GRAND_PRODUCT) {
+    l.den = secure_of(data, n);
+    data += 4 * n;
+  }
+  return l;
+}
+std::vector<GkrLayer> layers_of(size_t n_inst, const uint32_t* kinds, const uint32_t* logs, const uint32_t* data) {
+  std::vector<GkrLayer> v;
+  for (size_t i = 0; i < n_inst; i++) v.push_back(layer_of(kinds[i], logs[i], data));
+  return v;
+}
+}  // namespace
+
+extern "C" {
+
+// GkrOps::gen_eq_evals: eq(x, y) * v over {0,1}^n_y into four coordinate arrays of 2^n_y.
+void oracle_gkr_gen_eq_evals(const uint32_t* y, uint32_t n_y, const uint32_t v[4], uint32_t* out) {
+  secure_to(gen_eq_evals(qs_of(y, n_y), q_of(v)), out);
+}
+
+// GkrOps::next_layer for a layer of 2^log_n gates; writes the next layer's columns in the same
+// packing (a grand product stays one column, every LogUp kind becomes generic: numerators then
+// denominators).
+void oracle_gkr_next_layer(uint32_t kind, uint32_t log_n, const uint32_t* data, uint32_t* out) {
+  GkrLayer l = next_layer(layer_of(kind, log_n, data));
+  secure_to(l.num, out);
+  if (l.kind != GKR_GRAND_PRODUCT) secure_to(l.den, out + 4 * l.num.size());
+}
+
+// GkrOps::sum_as_poly_in_first_variable for the oracle of a layer of 2^log_n gates with eq
+// evaluations generated from y (EqEvals::generate), lambda and the accumulated eq correction.
+// Writes the round polynomial's coefficients (up to 4) and returns their number.
+uint32_t oracle_gkr_sum_as_poly(uint32_t kind, uint32_t log_n, const uint32_t* data, const uint32_t* y, uint32_t n_y,
+                                const uint32_t lambda[4], const uint32_t correction[4], const uint32_t claim[4],
+                                uint32_t* coeffs) {
+  EqEvals eq = EqEvals::generate(qs_of(y, n_y));
+  GkrPolyOracle o;
+  o.eq = &eq;
+  o.layer = layer_of(kind, log_n, data);
+  o.lambda = q_of(lambda);
+  o.correction = q_of(correction);
+  UPoly p = o.sum_as_poly_in_first_variable(q_of(claim));
+  for (size_t i = 0; i < p.size(); i++) q_to(p[i], coeffs + 4 * i);
+  return (uint32_t)p.size();
+}
+
+// MleOps::fix_first_variable of a base (is_base = 1, one array) or secure (four coordinate
+// arrays) column of 2^log_n values; writes 2^(log_n-1) secure values.
+void oracle_mle_fix_first_variable(int is_base, uint32_t log_n, const uint32_t* in, const uint32_t a[4],
+                                   uint32_t* out) {
+  size_t n = (size_t)1 << log_n;
+  if (is_base) {
+    std::vector<M31> m(n);
+    for (size_t i = 0; i < n; i++) m[i] = M31(in[i]);
+    secure_to(fix_first_variable(m, q_of(a)), out);
+  } else {
+    secure_to(fix_first_variable(secure_of(in, n), q_of(a)), out);
+  }
+}
+
+// gkr_prover::prove_batch over n_inst input layers (kinds / log sizes / packed data as above)
+// on a channel whose digest is `digest` (NULL: the default channel). Writes the proof followed by
+// the artifact; returns the byte count, or 0 with `err` set.
+size_t oracle_gkr_prove(size_t n_inst, const uint32_t* kinds, const uint32_t* logs, const uint32_t* data,
+                        const uint8_t* digest, uint8_t* out, size_t cap, uint8_t* digest_out, char* err,
+                        size_t err_cap) {
+  try {
+    Channel ch;
+    if (digest) std::memcpy(ch.digest.b, digest, 32);
+    auto [proof, art] = gkr_prove_batch(ch, layers_of(n_inst, kinds, logs, data));
+    Writer w;
+    write_gkr(w, proof, art);
+    if (w.b.size() > cap) throw std::runtime_error("output buffer too small");
+    std::memcpy(out, w.b.data(), w.b.size());
+    if (digest_out) std::memcpy(digest_out, ch.digest.b, 32);
+    return w.b.size();
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+// partially_verify_batch on the proof bytes, then the checks of the reference's GKR tests: the
+// recomputed artifact equals the one written after the proof, and each instance's claims equal
+// its input layer's columns at the artifact's point (gkr.rs tests, cpu/lookups/gkr.rs:315-470).
+// `data` may be NULL to skip the input-layer check. Returns 1 on success.
+int oracle_gkr_verify(size_t n_inst, const uint32_t* kinds, const uint32_t* logs, const uint32_t* data,
+                      const uint8_t* digest, const uint8_t* bytes, size_t len, char* err, size_t err_cap) {
+  try {
+    GkrBatchProof proof;
+    GkrArtifact claimed, art;
+    if (!read_gkr(bytes, len, proof, claimed)) throw std::runtime_error("malformed proof bytes");
+    Channel ch;
+    if (digest) std::memcpy(ch.digest.b, digest, 32);
+    std::vector<GkrGate> gates;
+    for (size_t i = 0; i < n_inst; i++) gates.push_back(kinds[i] == GKR_GRAND_PRODUCT ? GATE_GRAND_PRODUCT : GATE_LOGUP);
+    std::string r = gkr_partially_verify_batch(gates, proof, ch, art);
+    if (!r.empty()) throw std::runtime_error(r);
+    if (art.ood_point != claimed.ood_point || art.claims_to_verify_by_instance != claimed.claims_to_verify_by_instance ||
+        art.n_variables_by_instance != claimed.n_variables_by_instance)
+      throw std::runtime_error("artifact differs from the verifier's");
+    if (data) {
+      std::vector<GkrLayer> layers = layers_of(n_inst, kinds, logs, data);
+      size_t n_layers = 0;
+      for (auto& l : layers) n_layers = std::max(n_layers, l.n_variables());
+      for (size_t i = 0; i < n_inst; i++) {
+        const GkrLayer& l = layers[i];
+        std::vector<QM31> pt(art.ood_point.begin() + (n_layers - l.n_variables()), art.ood_point.end());
+        std::vector<QM31> want;
+        if (l.kind == GKR_GRAND_PRODUCT) {
+          want = {mle_eval_at_point(l.num, pt)};
+        } else {
+          std::vector<QM31> num;
+          if (l.kind == GKR_LOGUP_SINGLES) num.assign(l.den.size(), q_one());
+          else if (l.kind == GKR_LOGUP_MULTIPLICITIES) for (auto x : l.num_base) num.push_back(QM31(x));
+          else num = l.num;
+          want = {mle_eval_at_point(num, pt), mle_eval_at_point(l.den, pt)};
+        }
+        if (want != art.claims_to_verify_by_instance[i]) throw std::runtime_error("input layer claim mismatch");
+      }
+    }
+    return 1;
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+// Draws n secure felts from the default channel (test_channel().draw_felts(n)), four words each.
+void oracle_channel_draw_felts(size_t n, uint32_t* out) {
+  Channel ch;
+  std::vector<QM31> v = ch.draw_felts(n);
+  for (size_t i = 0; i < n; i++) q_to(v[i], out + 4 * i);
+}
+
+}  // extern "C"

@@ -228,3 +228,92 @@ def verify_poseidon(log_n, claimed_sum, proof: bytes):
     ok = lib().oracle_verify_poseidon(C.c_uint32(log_n), _p(_u32(claimed_sum)), _p(buf), C.c_size_t(len(proof)),
                                       err, C.c_size_t(512))
     return bool(ok), err.value.decode()
+
+
+# ---------------------------------------------------------------- GKR / MLE
+GRAND_PRODUCT, LOGUP_GENERIC, LOGUP_MULTIPLICITIES, LOGUP_SINGLES = 0, 1, 2, 3
+
+
+def gkr_pack(kind, cols):
+    """Flat words of one layer: secure columns as (4, n) coordinate arrays, multiplicities (n,)."""
+    return np.concatenate([_u32(c).reshape(-1) for c in cols])
+
+
+def _layer_args(layers):
+    kinds = _u32([k for k, _ in layers])
+    logs = _u32([(np.asarray(cols[-1]).shape[-1]).bit_length() - 1 for _, cols in layers])
+    data = np.concatenate([gkr_pack(k, cols) for k, cols in layers])
+    return kinds, logs, data
+
+
+def gkr_gen_eq_evals(y, v):
+    y = _u32(y).reshape(-1, 4)
+    out = np.zeros((4, 1 << len(y)), np.uint32)
+    lib().oracle_gkr_gen_eq_evals(_p(y), C.c_uint32(len(y)), _p(_u32(v)), _p(out))
+    return out
+
+
+def gkr_next_layer(kind, cols):
+    """Next layer's columns: [prod (4, n/2)] or [num (4, n/2), den (4, n/2)]."""
+    n = np.asarray(cols[-1]).shape[-1]
+    data = gkr_pack(kind, cols)
+    ncols = 1 if kind == GRAND_PRODUCT else 2
+    out = np.zeros((ncols, 4, n // 2), np.uint32)
+    lib().oracle_gkr_next_layer(C.c_uint32(kind), C.c_uint32(n.bit_length() - 1), _p(data), _p(out))
+    return [out[i] for i in range(ncols)]
+
+
+def gkr_sum_as_poly(kind, cols, y, lam, correction, claim):
+    n = np.asarray(cols[-1]).shape[-1]
+    data = gkr_pack(kind, cols)
+    y = _u32(y).reshape(-1, 4)
+    coeffs = np.zeros((4, 4), np.uint32)
+    f = lib().oracle_gkr_sum_as_poly
+    f.restype = C.c_uint32
+    k = f(C.c_uint32(kind), C.c_uint32(n.bit_length() - 1), _p(data), _p(y), C.c_uint32(len(y)), _p(_u32(lam)),
+          _p(_u32(correction)), _p(_u32(claim)), _p(coeffs))
+    return [tuple(int(x) for x in coeffs[i]) for i in range(k)]
+
+
+def mle_fix_first_variable(col, a):
+    col = _u32(col)
+    is_base = col.ndim == 1
+    n = col.shape[-1]
+    out = np.zeros((4, n // 2), np.uint32)
+    lib().oracle_mle_fix_first_variable(C.c_int(int(is_base)), C.c_uint32(n.bit_length() - 1), _p(col),
+                                        _p(_u32(a)), _p(out))
+    return out
+
+
+def gkr_prove(layers, digest=None):
+    """(proof+artifact bytes, final channel digest) of prove_batch over [(kind, cols), ...]."""
+    kinds, logs, data = _layer_args(layers)
+    cap = 16 << 20
+    out = np.zeros(cap, np.uint8)
+    dout = np.zeros(32, np.uint8)
+    err = C.create_string_buffer(512)
+    f = lib().oracle_gkr_prove
+    f.restype = C.c_size_t
+    dg = np.frombuffer(digest, np.uint8).copy() if digest is not None else None
+    n = f(C.c_size_t(len(layers)), _p(kinds), _p(logs), _p(data), _p(dg) if dg is not None else None, _p(out),
+          C.c_size_t(cap), _p(dout), err, C.c_size_t(512))
+    if n == 0:
+        raise RuntimeError("oracle GKR prove failed: " + err.value.decode())
+    return bytes(out[:n]), bytes(dout)
+
+
+def gkr_verify(layers, proof: bytes, digest=None, check_inputs=True):
+    kinds, logs, data = _layer_args(layers)
+    buf = np.frombuffer(proof, dtype=np.uint8).copy()
+    err = C.create_string_buffer(512)
+    dg = np.frombuffer(digest, np.uint8).copy() if digest is not None else None
+    ok = lib().oracle_gkr_verify(C.c_size_t(len(layers)), _p(kinds), _p(logs), _p(data) if check_inputs else None,
+                                 _p(dg) if dg is not None else None, _p(buf), C.c_size_t(len(proof)), err,
+                                 C.c_size_t(512))
+    return bool(ok), err.value.decode()
+
+
+def channel_draw_felts(n):
+    out = np.zeros((n, 4), np.uint32)
+    lib().oracle_channel_draw_felts(C.c_size_t(n), _p(out))
+    return out

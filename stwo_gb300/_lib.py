@@ -84,6 +84,14 @@ SIGNATURES = {
     "stwo_accumulate_quotients": (C.c_int32, [U32, PVP, U32, QM31, C.POINTER(SampleBatch), U32, U32, PVP, VP]),
     "stwo_secure_accumulate": (C.c_int32, [PVP, PVP, C.c_size_t, VP]),
     "stwo_generate_secure_powers": (C.c_int32, [QM31, U32, C.POINTER(QM31), VP]),
+    "stwo_gkr_gen_eq_evals": (C.c_int32, [C.POINTER(QM31), U32, QM31, PVP, VP]),
+    "stwo_gkr_next_layer": (C.c_int32, [U32, U32, PVP, PVP, PVP, PVP, VP]),
+    "stwo_gkr_sum_as_poly_in_first_variable": (C.c_int32, [U32, U32, PVP, PVP, PVP, C.POINTER(QM31), U32, QM31, QM31,
+                                                           QM31, C.POINTER(QM31), C.POINTER(C.c_uint32), VP]),
+    "stwo_mle_fix_first_variable_base": (C.c_int32, [U32, VP, QM31, PVP, VP]),
+    "stwo_mle_fix_first_variable_secure": (C.c_int32, [U32, PVP, QM31, PVP, VP]),
+    "stwo_gkr_prove_batch": (C.c_int32, [U32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), PVP, PVP, VP, VP,
+                                         C.c_size_t, C.POINTER(C.c_size_t), VP, VP]),
     "stwo_grind_blake2s": (C.c_int32, [C.POINTER(C.c_uint32), U32, C.POINTER(C.c_uint64), VP]),
     "stwo_gen_wide_fib_trace": (C.c_int32, [U32, U32, VP, VP, PVP, VP]),
     "stwo_prove_wide_fib": (C.c_int32, [U32, U32, PVP, PcsConfig, VP, C.c_size_t, C.POINTER(C.c_size_t), VP]),

@@ -205,6 +205,110 @@ class CudaBackend:
         return nonce.value
 
 
+GRAND_PRODUCT, LOGUP_GENERIC, LOGUP_MULTIPLICITIES, LOGUP_SINGLES = 0, 1, 2, 3
+
+
+@dataclass
+class GkrLayer:
+    """Layer (crates/prover/src/core/lookups/gkr_prover.rs:94-108): `num` is the grand product's
+    column, the secure numerators, or (multiplicities) a base column; `den` the denominators."""
+
+    kind: int
+    num: Optional[object] = None
+    den: Optional[SecureColumn] = None
+
+    def __len__(self) -> int:
+        col = self.num if self.kind == GRAND_PRODUCT else self.den
+        return col.numel() if isinstance(col, torch.Tensor) else len(col)
+
+    def n_variables(self) -> int:
+        return len(self).bit_length() - 1
+
+    def _num_ptrs(self):
+        if self.kind == LOGUP_SINGLES:
+            return None
+        if self.kind == LOGUP_MULTIPLICITIES:
+            return _ptrs([self.num] * 4)
+        return _ptrs(self.num.cols)
+
+    def _den_ptrs(self):
+        return None if self.kind == GRAND_PRODUCT else _ptrs(self.den.cols)
+
+
+class GkrOps:
+    """GkrOps (gkr_prover.rs:22-42) and MleOps (lookups/mle.rs:9-14) on the GPU."""
+
+    @staticmethod
+    def gen_eq_evals(y: Sequence[QM31T], v: QM31T) -> SecureColumn:
+        out = SecureColumn([empty(1 << len(y)) for _ in range(4)])
+        arr = (QM31 * max(1, len(y)))(*[_q(x) for x in y])
+        call("stwo_gkr_gen_eq_evals", arr, len(y), _q(v), _ptrs(out.cols), _stream())
+        return out
+
+    @staticmethod
+    def next_layer(layer: GkrLayer) -> GkrLayer:
+        h = len(layer) // 2
+        num = SecureColumn([empty(h) for _ in range(4)])
+        if layer.kind == GRAND_PRODUCT:
+            call("stwo_gkr_next_layer", layer.kind, layer.n_variables(), layer._num_ptrs(), None, _ptrs(num.cols),
+                 None, _stream())
+            return GkrLayer(GRAND_PRODUCT, num)
+        den = SecureColumn([empty(h) for _ in range(4)])
+        call("stwo_gkr_next_layer", layer.kind, layer.n_variables(), layer._num_ptrs(), layer._den_ptrs(),
+             _ptrs(num.cols), _ptrs(den.cols), _stream())
+        return GkrLayer(LOGUP_GENERIC, num, den)
+
+    @staticmethod
+    def sum_as_poly_in_first_variable(layer: GkrLayer, eq_evals: SecureColumn, y: Sequence[QM31T], lam: QM31T,
+                                      eq_fixed_var_correction: QM31T, claim: QM31T) -> List[QM31T]:
+        ys = (QM31 * max(1, len(y)))(*[_q(x) for x in y])
+        coeffs = (QM31 * 4)()
+        n = C.c_uint32()
+        call("stwo_gkr_sum_as_poly_in_first_variable", layer.kind, layer.n_variables(), layer._num_ptrs(),
+             layer._den_ptrs(), _ptrs(eq_evals.cols), ys, len(y), _q(lam), _q(eq_fixed_var_correction), _q(claim),
+             coeffs, C.byref(n), _stream())
+        return [tuple(coeffs[i].v) for i in range(n.value)]
+
+    @staticmethod
+    def fix_first_variable(mle, assignment: QM31T) -> SecureColumn:
+        if isinstance(mle, torch.Tensor):
+            n = mle.numel()
+            out = SecureColumn([empty(n // 2) for _ in range(4)])
+            call("stwo_mle_fix_first_variable_base", n.bit_length() - 1, C.c_void_p(mle.data_ptr()), _q(assignment),
+                 _ptrs(out.cols), _stream())
+            return out
+        n = len(mle)
+        out = SecureColumn([empty(n // 2) for _ in range(4)])
+        call("stwo_mle_fix_first_variable_secure", n.bit_length() - 1, _ptrs(mle.cols), _q(assignment),
+             _ptrs(out.cols), _stream())
+        return out
+
+    @staticmethod
+    def prove_batch(layers: Sequence[GkrLayer], digest: Optional[bytes] = None,
+                    capacity: int = 16 << 20) -> Tuple[bytes, bytes]:
+        """gkr_prover::prove_batch: (canonical proof + artifact bytes, final channel digest)."""
+        k = len(layers)
+        kinds = (C.c_uint32 * k)(*[l.kind for l in layers])
+        logs = (C.c_uint32 * k)(*[l.n_variables() for l in layers])
+        nums = (C.c_void_p * (4 * k))()
+        dens = (C.c_void_p * (4 * k))()
+        for i, l in enumerate(layers):
+            if l.kind == LOGUP_MULTIPLICITIES:
+                nums[4 * i] = l.num.data_ptr()
+            elif l.kind != LOGUP_SINGLES:
+                for c in range(4):
+                    nums[4 * i + c] = l.num.cols[c].data_ptr()
+            if l.kind != GRAND_PRODUCT:
+                for c in range(4):
+                    dens[4 * i + c] = l.den.cols[c].data_ptr()
+        out = (C.c_uint8 * capacity)()
+        n = C.c_size_t()
+        din = (C.c_uint8 * 32).from_buffer_copy(digest) if digest is not None else None
+        dout = (C.c_uint8 * 32)()
+        call("stwo_gkr_prove_batch", k, kinds, logs, nums, dens, din, out, capacity, C.byref(n), dout, _stream())
+        return bytes(out[:n.value]), bytes(dout)
+
+
 def canonic_twiddles(log_size: int) -> TwiddleTree:
     """Twiddles for CanonicCoset(log_size).circle_domain() and every domain it doubles into."""
     return TwiddleTree(canonic_half_coset(log_size))

@@ -109,6 +109,20 @@ inline hq hq_mul(hq x, hq y) {
 }
 inline hq hq_conj(hq x) { return hq{{x.v[0], x.v[1], h_sub(0, x.v[2]), h_sub(0, x.v[3])}}; }
 inline hq hq_pow(hq b, uint64_t e) { hq r = hq_make(1, 0, 0, 0); while (e) { if (e & 1) r = hq_mul(r, b); b = hq_mul(b, b); e >>= 1; } return r; }
+inline hq hq_inv(hq x) {
+  // (a + bu)^-1 = (a - bu) / (a^2 - (2+i) b^2), CM31 inverse via the norm (fields/qm31.rs:121-129).
+  uint32_t b2r, b2i, a2r, a2i;
+  h_cmul(x.v[2], x.v[3], x.v[2], x.v[3], &b2r, &b2i);
+  h_cmul(x.v[0], x.v[1], x.v[0], x.v[1], &a2r, &a2i);
+  uint32_t rb_r = h_sub(h_add(b2r, b2r), b2i), rb_i = h_add(b2r, h_add(b2i, b2i));
+  uint32_t dr = h_sub(a2r, rb_r), di = h_sub(a2i, rb_i);
+  uint32_t nrm = h_inv(h_add(h_mul(dr, dr), h_mul(di, di)));
+  uint32_t ir = h_mul(dr, nrm), ii = h_mul(h_sub(0, di), nrm);
+  uint32_t r0, r1, r2, r3;
+  h_cmul(x.v[0], x.v[1], ir, ii, &r0, &r1);
+  h_cmul(h_sub(0, x.v[2]), h_sub(0, x.v[3]), ir, ii, &r2, &r3);
+  return hq_make(r0, r1, r2, r3);
+}
 
 // A twiddle tree resident in HBM: x-coordinates of every coset in the doubling tower of
 // `root`, bit-reversed per level, padded with one 1 (cpu/circle.rs:171-188), and inverses.

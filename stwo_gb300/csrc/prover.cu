@@ -263,20 +263,6 @@ static bool hpq_less(const HPointQ& a, const HPointQ& b) {
   return false;
 }
 static bool hpq_eq(const HPointQ& a, const HPointQ& b) { return !hpq_less(a, b) && !hpq_less(b, a); }
-static hq hq_inv(hq x) {
-  // (a + bu)^-1 = (a - bu) / (a^2 - (2+i) b^2), CM31 inverse via the norm (fields/qm31.rs:121-129).
-  uint32_t b2r, b2i, a2r, a2i;
-  h_cmul(x.v[2], x.v[3], x.v[2], x.v[3], &b2r, &b2i);
-  h_cmul(x.v[0], x.v[1], x.v[0], x.v[1], &a2r, &a2i);
-  uint32_t rb_r = h_sub(h_add(b2r, b2r), b2i), rb_i = h_add(b2r, h_add(b2i, b2i));
-  uint32_t dr = h_sub(a2r, rb_r), di = h_sub(a2i, rb_i);
-  uint32_t nrm = h_inv(h_add(h_mul(dr, dr), h_mul(di, di)));
-  uint32_t ir = h_mul(dr, nrm), ii = h_mul(h_sub(0, di), nrm);
-  uint32_t r0, r1, r2, r3;
-  h_cmul(x.v[0], x.v[1], ir, ii, &r0, &r1);
-  h_cmul(h_sub(0, x.v[2]), h_sub(0, x.v[3]), ir, ii, &r2, &r3);
-  return hq_make(r0, r1, r2, r3);
-}
 static HPointQ random_point(HostChannel& ch) {
   hq t = ch.draw_felt();
   hq t2 = hq_mul(t, t);
