@@ -241,6 +241,163 @@ class PoseidonWorkload:
         }
 
 
+class GkrWorkload:
+    """GKR batch proof (gkr_prover::prove_batch) of one LogUp-generic input layer of 2^20 leaves: the
+    shape of the Poseidon2 relation at 2^16 rows (8 permutations x 2 fractions per row), with
+    seeded uniform QM31 numerators and denominators. One step = one prove_batch through the C ABI
+    (stwo_gkr_prove_batch) from a default channel."""
+
+    LOG = 20
+
+    def __init__(self, log=None):
+        import numpy as np
+        import torch
+
+        from stwo_gb300 import _lib
+
+        if log:
+            self.LOG = log
+        n = 1 << self.LOG
+        self.host_in = torch.empty(8 * n, dtype=torch.int32).pin_memory()
+        self.host_in.numpy().view(np.uint32)[:] = gen_words(6, 0, 8 * n)
+        self.dev = self.host_in.cuda()
+        self.work = torch.empty_like(self.dev)
+        self.cap = 1 << 20
+        self.out = (C.c_uint8 * self.cap)()
+        self.len = C.c_size_t()
+        self.lib = _lib
+
+    def _ptrs(self, t):
+        n = 1 << self.LOG
+        base = t.data_ptr()
+        nums = (C.c_void_p * 4)(*[base + 4 * c * n for c in range(4)])
+        dens = (C.c_void_p * 4)(*[base + 4 * (4 + c) * n for c in range(4)])
+        return nums, dens
+
+    def step(self, from_host=False):
+        import torch
+
+        src = self.work if from_host else self.dev
+        if from_host:
+            self.work.copy_(self.host_in, non_blocking=True)
+        nums, dens = self._ptrs(src)
+        kinds = (C.c_uint32 * 1)(1)
+        logs = (C.c_uint32 * 1)(self.LOG)
+        self.lib.call("stwo_gkr_prove_batch", 1, kinds, logs, nums, dens, None, self.out, self.cap,
+                      C.byref(self.len), None, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        return bytes(self.out[:self.len.value])
+
+    def algorithmic_bytes(self):
+        """Compulsory HBM bytes of one proof: building the circuit (each next_layer reads 2m gates
+        and writes m, 32 B per gate) and every sum-check round (the first round of a layer reads
+        its 2^k gates; later rounds read the previous 2m folded gates and write m; plus the eq
+        evaluations each round reads and the per-layer eq table writes)."""
+        total = 0
+        for k in range(self.LOG, 0, -1):
+            total += 32 * (1 << k) + 32 * (1 << (k - 1))
+        for k in range(1, self.LOG + 1):  # oracle over the layer with k variables
+            total += 16 * (1 << max(k - 2, 0))  # eq table of 2^(k-2) written
+            cur = 1 << k
+            total += 32 * cur + 16 * (cur // 4)
+            while cur > 2:
+                cur //= 2
+                total += 32 * 2 * cur + 32 * cur + (16 * (cur // 4) if cur >= 4 else 0)
+        return total
+
+
+def run_gkr(args, world, rank, local, lib, barrier, max_over_ranks):
+    import numpy as np
+    import torch
+
+    wl = GkrWorkload()
+    # The input (32 MiB) fits in L2, so L2 is flushed by a 256 MiB write before every timed step.
+    flush = torch.empty(64 << 20, dtype=torch.int32, device="cuda")
+    for _ in range(args.warmup):
+        wl.step()
+    barrier()
+    launches0 = lib.stwo_kernel_launches()
+    times = []
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            proof = wl.step()
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        barrier()
+        wall = time.perf_counter() - t0
+    launches = lib.stwo_kernel_launches() - launches0
+    step_ms = max_over_ranks(float(np.mean(times)))
+    for _ in range(max(1, args.warmup // 2)):
+        wl.step(from_host=True)
+    barrier()
+    et = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        wl.step(from_host=True)
+        torch.cuda.synchronize()
+        et.append((time.perf_counter() - t1) * 1e3)
+    e2e_ms = max_over_ranks(float(np.mean(et)))
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    leaves = 1 << wl.LOG
+    ab = wl.algorithmic_bytes()
+    ach = ab / (step_ms / 1e3) / 1e9
+    line = {
+        "metric": "GKR prove_batch leaves/s (LogUp generic, 2^20 leaves)",
+        "value": leaves * world / (step_ms / 1e3),
+        "unit": "leaves/s",
+        "proof_s": step_ms / 1e3,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (QM31 as 4 M31 words)",
+        "data": "synthetic: seeded uniform QM31 numerators and denominators (splitmix64 mod P)",
+        "config": {"workload": "GKR batch proof, one LogUp-generic layer of 2^20 leaves (Poseidon2 relation shape "
+                               "at 2^16 rows)", "log_leaves": wl.LOG,
+                   "l2": "input (32 MiB) fits in L2: flushed by a 256 MiB write before each timed step",
+                   "parallelism": f"replicas x{world}"},
+        "proof_bytes": len(proof),
+        "roofline": {"bound": "hbm", "kernel": "whole prove_batch (latency-bound: one host round trip per "
+                                               "sum-check round)", "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak, "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": ab},
+        "e2e": {"value": leaves * world / (e2e_ms / 1e3), "unit": "leaves/s", "proof_s": e2e_ms / 1e3,
+                "h2d_bytes_per_step": 32 * leaves, "d2h_bytes_per_step": len(proof)},
+        "gpu_launches": int(launches),
+        "wall_s": wall,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_gkr(args.cpu_threads)
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_gkr(threads=0, log=20):
+    """The oracle's GKR batch proof (OpenMP on all host cores) of the same 2^20-leaf layer."""
+    import numpy as np
+
+    import oracle.pyoracle as O
+
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    nthreads = threads or os.cpu_count() or 1
+    n = 1 << log
+    w = gen_words(6, 0, 8 * n).reshape(8, n)
+    layers = [(O.LOGUP_GENERIC, [np.ascontiguousarray(w[:4]), np.ascontiguousarray(w[4:])])]
+    t0 = time.perf_counter()
+    O.gkr_prove(layers)
+    secs = time.perf_counter() - t0
+    return {"value": n / secs, "unit": "leaves/s", "cores": nthreads, "kind": "port", "proof_s": secs,
+            "sample": f"one full GKR batch proof of the same 2^{log}-leaf layer: {secs:.2f} s"}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -277,6 +434,8 @@ def run_gb300(args):
 
     if args.workload == "kernels":
         return run_kernels(args, world, rank, local, lib, barrier, max_over_ranks)
+    if args.workload == "gkr":
+        return run_gkr(args, world, rank, local, lib, barrier, max_over_ranks)
 
     wl = PoseidonWorkload()
     for _ in range(args.warmup):
@@ -511,6 +670,14 @@ def run_reference(args):
         unit = "cells/s"
         config = {"workload": "kernels: 256 cols x 2^20 -> 2^22 (blowup 4) + Merkle + FRI 2^22->2^4",
                   "sample_cols_per_step": 8}
+    elif args.workload == "gkr":
+        for _ in range(min(args.warmup, 1)):
+            cpu_baseline_gkr(args.cpu_threads)
+        vals = [cpu_baseline_gkr(args.cpu_threads) for _ in range(args.steps)]
+        metric = "GKR prove_batch leaves/s (LogUp generic, 2^20 leaves)"
+        unit = "leaves/s"
+        config = {"workload": "GKR batch proof, one LogUp-generic layer of 2^20 leaves (Poseidon2 relation shape "
+                              "at 2^16 rows)", "log_leaves": 20}
     else:
         log = 14
         for _ in range(min(args.warmup, 1)):
@@ -541,8 +708,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="poseidon", choices=["poseidon", "kernels"],
-                    help="poseidon: the headline Poseidon2 2^16-row proof; kernels: the kernel microbench")
+    ap.add_argument("--workload", default="poseidon", choices=["poseidon", "kernels", "gkr"],
+                    help="poseidon: the headline Poseidon2 2^16-row proof; kernels: the kernel microbench; "
+                         "gkr: GKR batch proof of 2^20 LogUp leaves")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-cols", type=int, default=0, help="columns of the kernel workload (default 256; "

@@ -120,9 +120,11 @@ inline std::vector<QM31> gen_eq_evals(const std::vector<QM31>& y, QM31 v) {
   e.reserve(size_t(1) << y.size());
   for (size_t k = y.size(); k-- > 0;) {
     size_t n = e.size();
+    e.resize(2 * n);
+#pragma omp parallel for if (n >= 4096)
     for (size_t j = 0; j < n; j++) {
       QM31 t = e[j] * y[k];
-      e.push_back(t);
+      e[n + j] = t;
       e[j] = e[j] - t;
     }
   }
@@ -133,12 +135,14 @@ inline std::vector<QM31> gen_eq_evals(const std::vector<QM31>& y, QM31 v) {
 inline std::vector<QM31> fix_first_variable(const std::vector<QM31>& m, QM31 a) {
   size_t h = m.size() / 2;
   std::vector<QM31> r(h);
+#pragma omp parallel for if (h >= 4096)
   for (size_t i = 0; i < h; i++) r[i] = fold_mle_evals(a, m[i], m[i + h]);
   return r;
 }
 inline std::vector<QM31> fix_first_variable(const std::vector<M31>& m, QM31 a) {
   size_t h = m.size() / 2;
   std::vector<QM31> r(h);
+#pragma omp parallel for if (h >= 4096)
   for (size_t i = 0; i < h; i++) r[i] = fold_mle_evals(a, QM31(m[i]), QM31(m[i + h]));
   return r;
 }
@@ -170,12 +174,14 @@ inline GkrLayer next_layer(const GkrLayer& l) {
   if (l.kind == GKR_GRAND_PRODUCT) {
     r.kind = GKR_GRAND_PRODUCT;
     r.num.resize(h);
+#pragma omp parallel for if (h >= 4096)
     for (size_t i = 0; i < h; i++) r.num[i] = l.num[2 * i] * l.num[2 * i + 1];
     return r;
   }
   r.kind = GKR_LOGUP_GENERIC;
   r.num.resize(h);
   r.den.resize(h);
+#pragma omp parallel for if (h >= 4096)
   for (size_t i = 0; i < h; i++) {
     QM31 n0 = l.numer(2 * i), n1 = l.numer(2 * i + 1), d0 = l.den[2 * i], d1 = l.den[2 * i + 1];
     r.num[i] = d1 * n0 + d0 * n1;
@@ -254,14 +260,19 @@ inline UPoly correct_sum_as_poly_in_first_variable(QM31 f0, QM31 f2, QM31 claim,
 inline std::pair<QM31, QM31> gkr_eval_sums(const std::vector<QM31>& eq_evals, const GkrLayer& l, QM31 lambda) {
   size_t n_terms = l.len() / 4;
   QM31 e0, e2;
+  // Field sums are exact, so any split across threads gives the same result.
+#pragma omp parallel if (n_terms >= 4096)
+  {
+  QM31 s0, s2;
+#pragma omp for nowait
   for (size_t i = 0; i < n_terms; i++) {
     size_t a0 = 2 * i, a1 = 2 * i + 1, b0 = 2 * (n_terms + i), b1 = 2 * (n_terms + i) + 1;
     QM31 eqv = eq_evals[i];
     if (l.kind == GKR_GRAND_PRODUCT) {
       QM31 r2a = l.num[b0] + l.num[b0] - l.num[a0];
       QM31 r2b = l.num[b1] + l.num[b1] - l.num[a1];
-      e0 = e0 + eqv * (l.num[a0] * l.num[a1]);
-      e2 = e2 + eqv * (r2a * r2b);
+      s0 = s0 + eqv * (l.num[a0] * l.num[a1]);
+      s2 = s2 + eqv * (r2a * r2b);
       continue;
     }
     QM31 n00 = l.numer(a0), n01 = l.numer(a1), n10 = l.numer(b0), n11 = l.numer(b1);
@@ -270,8 +281,14 @@ inline std::pair<QM31, QM31> gkr_eval_sums(const std::vector<QM31>& eq_evals, co
     QM31 d20 = d10 + d10 - d00, d21 = d11 + d11 - d01;
     QM31 num0 = d01 * n00 + d00 * n01, den0 = d00 * d01;
     QM31 num2 = d21 * n20 + d20 * n21, den2 = d20 * d21;
-    e0 = e0 + eqv * (num0 + lambda * den0);
-    e2 = e2 + eqv * (num2 + lambda * den2);
+    s0 = s0 + eqv * (num0 + lambda * den0);
+    s2 = s2 + eqv * (num2 + lambda * den2);
+  }
+#pragma omp critical
+  {
+    e0 = e0 + s0;
+    e2 = e2 + s2;
+  }
   }
   return {e0, e2};
 }
