@@ -133,11 +133,11 @@ struct TwiddleTree {
   size_t size = 0;  // 2^root.log_size (>= 1)
 };
 
-// Per-device state: cached twiddle trees (keyed by root coset) and the device id.
+// Process state: cached twiddle trees keyed by (device, root coset). A tree is complete (its
+// build synchronised) before it enters the cache, so any stream may use a cached tree.
 struct DeviceContext {
-  int device = 0;
   std::mutex mu;
-  std::map<std::tuple<uint32_t, uint32_t, uint32_t>, TwiddleTree*> trees;
+  std::map<std::tuple<int, uint32_t, uint32_t, uint32_t>, TwiddleTree*> trees;
 };
 DeviceContext& ctx();
 

@@ -46,13 +46,12 @@ DeviceContext& ctx() {
 }
 
 int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
+  static const int n = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 152;
-  }
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 152;
+  }();
   return n;
 }
 
@@ -83,13 +82,15 @@ void scratch_free(void* p, cudaStream_t s) {
 }
 
 hpoint h_index_to_point(uint32_t idx) {
-  static hpoint tower[31];
-  static bool init = false;
-  if (!init) {
-    tower[0] = {2u, 1268011823u};  // M31_CIRCLE_GEN, crates/prover/src/core/circle.rs:203-206
-    for (int b = 1; b < 31; b++) tower[b] = h_padd(tower[b - 1], tower[b - 1]);
-    init = true;
-  }
+  struct Tower {
+    hpoint p[31];
+    Tower() {
+      p[0] = {2u, 1268011823u};  // M31_CIRCLE_GEN, crates/prover/src/core/circle.rs:203-206
+      for (int b = 1; b < 31; b++) p[b] = h_padd(p[b - 1], p[b - 1]);
+    }
+  };
+  static const Tower tw;  // thread-safe one-time initialisation
+  const hpoint* tower = tw.p;
   hpoint r = {1u, 0u};
   idx &= IDX_MASK;
   for (int b = 0; b < 31; b++)
@@ -157,7 +158,9 @@ int32_t build_tree(stwo_coset root, cudaStream_t stream, TwiddleTree* t) {
 int32_t get_tree(stwo_coset root, cudaStream_t stream, TwiddleTree** out) {
   DeviceContext& c = ctx();
   std::lock_guard<std::mutex> g(c.mu);
-  auto key = std::make_tuple(root.initial_index, root.step_size, root.log_size);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto key = std::make_tuple(dev, root.initial_index, root.step_size, root.log_size);
   auto it = c.trees.find(key);
   if (it != c.trees.end()) {
     *out = it->second;
@@ -242,7 +245,6 @@ uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap) {
 stwo_status stwo_device_init(int device) {
   STWO_CHECK_CUDA(cudaSetDevice(device));
   STWO_CHECK_CUDA(cudaFree(nullptr));
-  ctx().device = device;
   return STWO_OK;
 }
 
