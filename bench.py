@@ -398,6 +398,192 @@ def cpu_baseline_gkr(threads=0, log=20):
             "sample": f"one full GKR batch proof of the same 2^{log}-leaf layer: {secs:.2f} s"}
 
 
+class BatchWorkload:
+    """Mixed batch of whole proofs: n jobs, half wide-Fibonacci (100 columns, 2^log rows) and half
+    Poseidon2 (2^log instances = 2^(log-3) rows), log sizes uniform in [lo, hi] from `seed`, each
+    with its seeded inputs resident in HBM. Wide-Fibonacci uses PcsConfig::default(); Poseidon2
+    pow_bits 10."""
+
+    def __init__(self, n=64, lo=10, hi=18, seed=4, arrivals=None):
+        import numpy as np
+        import torch
+
+        from stwo_gb300.prover import AIR_POSEIDON, AIR_WIDE_FIB
+
+        rng = np.random.default_rng(seed)
+        if arrivals is None:
+            airs = rng.permutation([AIR_WIDE_FIB] * (n // 2) + [AIR_POSEIDON] * (n - n // 2))
+        else:
+            airs = rng.integers(0, 2, n)
+        logs = rng.integers(lo, hi + 1, n)
+        self.arrivals = arrivals
+        self.specs = []
+        self.host = []
+        for i, (air, log) in enumerate(zip(airs, logs)):
+            if air == AIR_WIDE_FIB:
+                rows = int(log)
+                words = gen_words(40 + seed, i, 2 << rows)
+                cfg, cols = (5, 1, 0, 3), 100
+            else:
+                rows = int(log) - 3
+                words = gen_words(40 + seed, i, (1 << rows) * 128)
+                cfg, cols = (10, 1, 0, 3), 0
+            h = torch.empty(len(words), dtype=torch.int32).pin_memory()
+            h.numpy().view(np.uint32)[:] = words
+            self.host.append(h)
+            self.specs.append((int(air), rows, cols, cfg))
+        self.dev = [h.cuda() for h in self.host]
+        self.cells = sum((1 << r) * (c if a == AIR_WIDE_FIB else 1296) for a, r, c, _ in self.specs)
+
+    def jobs(self, from_host=False):
+        from stwo_gb300.prover import AIR_WIDE_FIB, Job
+
+        if from_host:
+            for d, h in zip(self.dev, self.host):
+                d.copy_(h, non_blocking=True)
+        out = []
+        for (air, rows, cols, cfg), d in zip(self.specs, self.dev):
+            if air == AIR_WIDE_FIB:
+                n = 1 << rows
+                out.append(Job(air, rows, cfg, n_cols=cols, a=d[:n], b=d[n:]))
+            else:
+                out.append(Job(air, rows, cfg, init=d))
+        return out
+
+
+def run_batch(args, world, rank, local, lib, barrier, max_over_ranks):
+    """Batched proofs/s of 64 mixed proofs on a worker pool, beside the same jobs one at a time."""
+    import numpy as np
+    import torch
+
+    from stwo_gb300.prover import prove_batch
+
+    wl = BatchWorkload()
+    workers = args.workers or 8
+
+    def run(n_workers, from_host=False):
+        jobs = wl.jobs(from_host)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = prove_batch(jobs, n_workers=n_workers)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, res
+
+    for _ in range(args.warmup):
+        run(workers)
+    barrier()
+    launches0 = lib.stwo_kernel_launches()
+    with ClockSampler(local) as clk:
+        ts = [run(workers)[0] for _ in range(args.steps)]
+    launches = lib.stwo_kernel_launches() - launches0
+    step_s = max_over_ranks(float(np.mean(ts)))
+    plain_s, plain_res = run(1)
+    e2e_s = float(np.mean([run(workers, from_host=True)[0] for _ in range(max(1, args.steps // 2))]))
+    _, res = run(workers)
+    same = all(a.proof == b.proof for a, b in zip(res, plain_res))
+    if rank != 0:
+        return
+    n = len(wl.specs)
+    lat = sorted(r.latency_ms for r in res)
+    line = {
+        "metric": "batched proofs/s (64 mixed wide-Fibonacci / Poseidon2 proofs, log sizes 10..18)",
+        "value": n * world / step_s, "unit": "proofs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
+        "data": "synthetic: seeded inputs (splitmix64 mod P), sizes from seed 4",
+        "config": {"workload": "64 proofs: 32 wide-Fibonacci (100 cols, 2^10..2^18 rows, PcsConfig default) + "
+                               "32 Poseidon2 (2^10..2^18 instances, pow 10)", "workers": workers,
+                   "trace_cells_per_batch": wl.cells,
+                   "l2": "working set (GBs) larger than L2; no flush", "timing": "host wall clock around the "
+                   "synchronous batch call (every stream complete at return)", "parallelism": f"replicas x{world}"},
+        "plain": {"value": n / plain_s, "unit": "proofs/s", "ms": plain_s * 1e3,
+                  "note": "the same jobs one at a time (one worker)"},
+        "speedup_vs_plain": plain_s / step_s,
+        "proofs_identical_to_plain": same,
+        "trace_cells_per_s": wl.cells * world / step_s,
+        "latency_ms_in_batch": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+        "e2e": {"value": n * world / e2e_s, "unit": "proofs/s", "ms": e2e_s * 1e3,
+                "h2d_bytes_per_step": sum(h.numel() * 4 for h in wl.host),
+                "d2h_bytes_per_step": sum(len(r.proof) for r in res)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args, world, rank, local, lib, barrier, max_over_ranks):
+    """Served proving: Poisson arrivals (rate 200/s, seed 5), wide-Fibonacci or Poseidon2 uniform,
+    log sizes 12..20, HBM budget 150 GB; latency percentiles beside a plain one-at-a-time server."""
+    import numpy as np
+    import torch
+
+    from stwo_gb300.prover import Server
+
+    n_req = args.requests or 200
+    rate = 200.0
+    rng = np.random.default_rng(5)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    wl = BatchWorkload(n=n_req, lo=12, hi=20, seed=5, arrivals=arrivals)
+    workers = args.workers or 8
+    budget = 150 << 30
+
+    def serve(n_workers):
+        jobs = wl.jobs()
+        torch.cuda.synchronize()
+        with Server(n_workers=n_workers, hbm_budget=budget) as srv:
+            t0 = time.perf_counter()
+            tickets = []
+            for j, at in zip(jobs, arrivals):
+                delay = t0 + at - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append(srv.submit(j))
+            res = [srv.wait(t) for t in tickets]
+            wall = time.perf_counter() - t0
+        return res, wall
+
+    for _ in range(args.warmup):
+        serve(workers)
+    barrier()
+    with ClockSampler(local) as clk:
+        runs = [serve(workers) for _ in range(args.steps)]
+    plain, plain_wall = serve(1)
+    if rank != 0:
+        return
+
+    def pct(res, q):
+        lat = sorted(r.latency_ms for r in res)
+        return lat[min(len(lat) - 1, int(q * len(lat)))]
+
+    p99 = float(np.median([pct(r, 0.99) for r, _ in runs]))
+    p50 = float(np.median([pct(r, 0.50) for r, _ in runs]))
+    same = all(a.proof == b.proof for a, b in zip(runs[-1][0], plain))
+    line = {
+        "metric": "served p99 latency vs plain (Poisson 200/s, wide-Fibonacci / Poseidon2, log 12..20)",
+        "value": p99, "unit": "ms (p99 latency)",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean([w for _, w in runs])) * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
+        "data": "synthetic: Poisson arrivals and sizes from seed 5, seeded inputs (splitmix64 mod P)",
+        "config": {"workload": f"{n_req} requests, Poisson rate 200/s, AIR uniform in {{wide-Fibonacci (100 cols), "
+                               f"Poseidon2}}, log size uniform 12..20, HBM budget 150 GB", "workers": workers,
+                   "blake_round_air": "not built (constraint kernel for the Blake round AIR is a next step)",
+                   "l2": "working set larger than L2; no flush", "parallelism": f"replicas x{world}"},
+        "p50_ms": p50,
+        "plain": {"p99_ms": pct(plain, 0.99), "p50_ms": pct(plain, 0.50), "wall_s": plain_wall,
+                  "note": "the same arrivals served one at a time (one worker)"},
+        "p99_vs_plain": p99 / pct(plain, 0.99),
+        "throughput_proofs_per_s": n_req / float(np.mean([w for _, w in runs])),
+        "proofs_identical_to_plain": same,
+        "e2e": {"value": p99, "unit": "ms (p99 latency)", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": sum(len(r.proof) for r in plain),
+                "note": "inputs resident; proof bytes returned to the host per request"},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -436,8 +622,12 @@ def run_gb300(args):
         return run_kernels(args, world, rank, local, lib, barrier, max_over_ranks)
     if args.workload == "gkr":
         return run_gkr(args, world, rank, local, lib, barrier, max_over_ranks)
+    if args.workload == "batch":
+        return run_batch(args, world, rank, local, lib, barrier, max_over_ranks)
+    if args.workload == "serve":
+        return run_serve(args, world, rank, local, lib, barrier, max_over_ranks)
 
-    wl = PoseidonWorkload()
+    wl = PoseidonWorkload(log=args.log_rows)
     for _ in range(args.warmup):
         wl.step()
     barrier()
@@ -708,12 +898,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="poseidon", choices=["poseidon", "kernels", "gkr"],
+    ap.add_argument("--workload", default="poseidon", choices=["poseidon", "kernels", "gkr", "batch", "serve"],
                     help="poseidon: the headline Poseidon2 2^16-row proof; kernels: the kernel microbench; "
-                         "gkr: GKR batch proof of 2^20 LogUp leaves")
+                         "gkr: GKR batch proof of 2^20 LogUp leaves; batch: 64 mixed proofs on a worker pool; "
+                         "serve: Poisson-arrival serving with latency percentiles")
+    ap.add_argument("--workers", type=int, default=0, help="worker streams of the batch / serve workloads (8)")
+    ap.add_argument("--requests", type=int, default=0, help="requests of the serve workload (200)")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-cols", type=int, default=0, help="columns of the kernel workload (default 256; "
+                    "smaller only for profiling captures)")
+    ap.add_argument("--log-rows", type=int, default=0, help="log2 rows of the Poseidon2 workload (default 16; "
                     "smaller only for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -260,6 +260,51 @@ stwo_status stwo_prove_wide_fib(uint32_t log_n_rows, uint32_t n_cols, uint32_t* 
 stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* d_init, stwo_pcs_config cfg, uint8_t* h_proof,
                                 size_t capacity, size_t* h_len, stwo_qm31* h_claimed_sum, void* stream);
 
+/* ------------------------------------------------------------------ batched and served proving */
+/* No counterpart in the reference, which proves one statement per call (prover/mod.rs:27-79).
+ * A server owns a pool of host workers, each with its own CUDA stream, that run whole-proof jobs
+ * (stwo_prove_wide_fib / stwo_prove_poseidon) concurrently. A job starts when its estimated
+ * device bytes (stwo_job_hbm_bytes) fit in the HBM budget beside the running jobs; among queued
+ * jobs the first in submission order that fits starts next. Proof bytes equal those of the
+ * single-call entry points. */
+#define STWO_AIR_WIDE_FIB 0u
+#define STWO_AIR_POSEIDON 1u
+typedef struct {
+  uint32_t air;
+  uint32_t log_n_rows;
+  uint32_t n_cols;        /* wide-Fibonacci columns */
+  const uint32_t* d_a;    /* wide-Fibonacci: per-row first two values (device, 2^log_n_rows each) */
+  const uint32_t* d_b;
+  const uint32_t* d_init; /* Poseidon2 initial states (device) or NULL for the reference inputs */
+  stwo_pcs_config cfg;
+  uint8_t* h_proof;       /* host buffer for the proof bytes */
+  size_t capacity;
+} stwo_proof_job;
+typedef struct {
+  stwo_status status;
+  size_t len;
+  stwo_qm31 claimed_sum;  /* Poseidon2 LogUp claimed sum */
+  double queue_ms;        /* submission to start */
+  double run_ms;          /* start to completion */
+  double latency_ms;      /* submission to completion */
+  char error[256];
+} stwo_proof_result;
+typedef struct stwo_server_s* stwo_server;
+
+/* n_workers streams on `device`; hbm_budget_bytes = 0 takes 90% of the free device memory. */
+stwo_status stwo_server_create(uint32_t n_workers, size_t hbm_budget_bytes, int device, stwo_server* out);
+/* Queues a job (its buffers must stay valid until its wait returns); returns at once. */
+stwo_status stwo_server_submit(stwo_server server, const stwo_proof_job* job, uint64_t* ticket);
+/* Blocks until the job of `ticket` has finished; each ticket is waited for once. */
+stwo_status stwo_server_wait(stwo_server server, uint64_t ticket, stwo_proof_result* out);
+/* Runs every queued job to completion, then stops the workers. */
+stwo_status stwo_server_destroy(stwo_server server);
+/* The admission estimate of a job, in bytes. */
+size_t stwo_job_hbm_bytes(const stwo_proof_job* job);
+/* All n_jobs on a temporary server; results[i] belongs to jobs[i]. Returns the first failure. */
+stwo_status stwo_prove_batch(const stwo_proof_job* jobs, uint32_t n_jobs, uint32_t n_workers,
+                             size_t hbm_budget_bytes, stwo_proof_result* results);
+
 #ifdef __cplusplus
 }
 #endif

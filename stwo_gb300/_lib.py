@@ -52,6 +52,17 @@ U32 = C.c_uint32
 PVP = C.POINTER(C.c_void_p)
 
 # name -> (restype, argtypes); every symbol declared in include/stwo_cuda.h.
+class ProofJob(C.Structure):
+    _fields_ = [("air", C.c_uint32), ("log_n_rows", C.c_uint32), ("n_cols", C.c_uint32), ("d_a", C.c_void_p),
+                ("d_b", C.c_void_p), ("d_init", C.c_void_p), ("cfg", PcsConfig), ("h_proof", C.c_void_p),
+                ("capacity", C.c_size_t)]
+
+
+class ProofResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("len", C.c_size_t), ("claimed_sum", QM31), ("queue_ms", C.c_double),
+                ("run_ms", C.c_double), ("latency_ms", C.c_double), ("error", C.c_char * 256)]
+
+
 SIGNATURES = {
     "stwo_status_string": (C.c_char_p, [C.c_int32]),
     "stwo_last_error": (C.c_char_p, []),
@@ -97,6 +108,12 @@ SIGNATURES = {
     "stwo_prove_wide_fib": (C.c_int32, [U32, U32, PVP, PcsConfig, VP, C.c_size_t, C.POINTER(C.c_size_t), VP]),
     "stwo_prove_poseidon": (C.c_int32, [U32, VP, PcsConfig, VP, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(QM31),
                                         VP]),
+    "stwo_server_create": (C.c_int32, [U32, C.c_size_t, C.c_int, PVP]),
+    "stwo_server_submit": (C.c_int32, [VP, C.POINTER(ProofJob), C.POINTER(C.c_uint64)]),
+    "stwo_server_wait": (C.c_int32, [VP, C.c_uint64, C.POINTER(ProofResult)]),
+    "stwo_server_destroy": (C.c_int32, [VP]),
+    "stwo_job_hbm_bytes": (C.c_size_t, [C.POINTER(ProofJob)]),
+    "stwo_prove_batch": (C.c_int32, [C.POINTER(ProofJob), U32, U32, C.c_size_t, C.POINTER(ProofResult)]),
 }
 
 _lib = None

@@ -293,12 +293,12 @@ class GkrOps:
         nums = (C.c_void_p * (4 * k))()
         dens = (C.c_void_p * (4 * k))()
         for i, l in enumerate(layers):
-            if l.kind == LOGUP_MULTIPLICITIES:
+            if isinstance(l.num, torch.Tensor):
                 nums[4 * i] = l.num.data_ptr()
-            elif l.kind != LOGUP_SINGLES:
+            elif l.num is not None:
                 for c in range(4):
                     nums[4 * i + c] = l.num.cols[c].data_ptr()
-            if l.kind != GRAND_PRODUCT:
+            if l.den is not None:
                 for c in range(4):
                     dens[4 * i + c] = l.den.cols[c].data_ptr()
         out = (C.c_uint8 * capacity)()

@@ -59,3 +59,77 @@ def prove_poseidon(log_n_rows: int, init=None, cfg=DEFAULT_CONFIG):
     call("stwo_prove_poseidon", log_n_rows, init.data_ptr() if init is not None else None, pcs_config(cfg), buf,
          _OUT_CAP, C.byref(n), C.byref(cs), _stream())
     return C.string_at(buf, n.value), tuple(cs.v)
+
+
+# ------------------------------------------------------------------ batched and served proving
+AIR_WIDE_FIB, AIR_POSEIDON = 0, 1
+
+
+class Job:
+    """One whole-proof job: wide-Fibonacci (a, b device tensors of 2^log_n_rows words) or
+    Poseidon2 (init device tensor, or None for the reference inputs)."""
+
+    def __init__(self, air: int, log_n_rows: int, cfg=DEFAULT_CONFIG, n_cols: int = 0, a=None, b=None, init=None,
+                 capacity: int = 1 << 22):
+        self.air, self.log_n_rows, self.cfg, self.n_cols = air, log_n_rows, cfg, n_cols
+        self.a, self.b, self.init = a, b, init  # kept alive while the job runs
+        self.buf = (C.c_uint8 * capacity)()
+        self.c = _lib.ProofJob(air, log_n_rows, n_cols, a.data_ptr() if a is not None else None,
+                               b.data_ptr() if b is not None else None,
+                               init.data_ptr() if init is not None else None, pcs_config(cfg),
+                               C.cast(self.buf, C.c_void_p), capacity)
+
+    def hbm_bytes(self) -> int:
+        return _lib.load().stwo_job_hbm_bytes(C.byref(self.c))
+
+
+class Result:
+    def __init__(self, job: Job, r):
+        self.proof = C.string_at(job.buf, r.len)
+        self.claimed_sum = tuple(r.claimed_sum.v)
+        self.queue_ms, self.run_ms, self.latency_ms = r.queue_ms, r.run_ms, r.latency_ms
+
+
+class Server:
+    """A pool of workers, one CUDA stream each, running submitted jobs with HBM-budget
+    admission (stwo_server_*)."""
+
+    def __init__(self, n_workers: int = 8, hbm_budget: int = 0, device: int = None):
+        dev = torch.cuda.current_device() if device is None else device
+        h = C.c_void_p()
+        call("stwo_server_create", n_workers, hbm_budget, dev, C.byref(h))
+        self.h = h
+        self.jobs = {}
+
+    def submit(self, job: Job) -> int:
+        t = C.c_uint64()
+        call("stwo_server_submit", self.h, C.byref(job.c), C.byref(t))
+        self.jobs[t.value] = job
+        return t.value
+
+    def wait(self, ticket: int) -> Result:
+        r = _lib.ProofResult()
+        call("stwo_server_wait", self.h, ticket, C.byref(r))
+        job = self.jobs.pop(ticket)
+        if r.status != 0:
+            raise _lib.StwoError(r.status, "server job", r.error.decode(errors="replace"))
+        return Result(job, r)
+
+    def close(self):
+        if self.h:
+            _lib.load().stwo_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def prove_batch(jobs: Sequence[Job], n_workers: int = 8, hbm_budget: int = 0):
+    """Runs all jobs on a temporary server (stwo_prove_batch); results in job order."""
+    arr = (_lib.ProofJob * max(1, len(jobs)))(*[j.c for j in jobs])
+    res = (_lib.ProofResult * max(1, len(jobs)))()
+    call("stwo_prove_batch", arr, len(jobs), n_workers, hbm_budget, res)
+    return [Result(j, res[i]) for i, j in enumerate(jobs)]
