@@ -648,6 +648,7 @@ def run_gb300(args):
         wall = time.perf_counter() - t0
     launches = lib.stwo_kernel_launches() - launches0
     step_ms = max_over_ranks(float(np.mean(times)))
+    step_spread = {"min": float(np.min(times)), "median": float(np.median(times)), "max": float(np.max(times))}
     # End to end: initial states from pinned host memory, proof bytes back on the host.
     for _ in range(max(1, args.warmup // 2)):
         wl.step(from_host=True)
@@ -698,6 +699,7 @@ def run_gb300(args):
                    "log_last_layer": wl.CFG[2], "n_queries": wl.CFG[3],
                    "l2": "working set (~3 GB) far larger than L2; no flush", "parallelism": f"replicas x{world}"},
         "proof_bytes": len(wl.proof),
+        "ms_per_step_spread": step_spread,
         "stages_ms": stages,
         "roofline": roof,
         "e2e": {"value": wl.cells * world / (e2e_ms / 1e3), "unit": "trace cells/s", "proof_s": e2e_ms / 1e3,

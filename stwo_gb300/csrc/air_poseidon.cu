@@ -109,13 +109,6 @@ struct LookupConsts {
   uint32_t alpha_pow[PS_ST][4];
 };
 
-__device__ __forceinline__ qm31 qm31_inv(qm31 x) {
-  // (a + bu)^-1 = (a - bu) / (a^2 - (2+i) b^2)  (fields/qm31.rs:121-129)
-  cm31 b2 = cm31_mul(x.b, x.b);
-  cm31 denom = cm31_sub(cm31_mul(x.a, x.a), cm31_mul_r(b2));
-  cm31 di = cm31_inv(denom);
-  return {cm31_mul(x.a, di), cm31_mul(cm31_sub({0u, 0u}, x.b), di)};
-}
 
 __device__ __forceinline__ uint32_t fold64_p(unsigned long long x) {
   x = (x & P) + (x >> 31);

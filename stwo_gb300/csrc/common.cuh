@@ -77,7 +77,13 @@ inline stwo_coset canonic_half_coset(uint32_t log) {
 // Host-side M31 helpers for O(1) setup scalars (never per-element work).
 inline uint32_t h_add(uint32_t a, uint32_t b) { uint32_t s = a + b; return s >= P ? s - P : s; }
 inline uint32_t h_sub(uint32_t a, uint32_t b) { return a >= b ? a - b : a + P - b; }
-inline uint32_t h_mul(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) % P); }
+inline uint32_t h_mul(uint32_t a, uint32_t b) {
+  // (a b) mod P for canonical a, b by folding the 62-bit product at bit 31 twice.
+  uint64_t x = (uint64_t)a * b;
+  x = (x & P) + (x >> 31);
+  uint32_t r = (uint32_t)((x & P) + (x >> 31));
+  return r >= P ? r - P : r;
+}
 inline uint32_t h_pow(uint32_t b, uint64_t e) { uint32_t r = 1; while (e) { if (e & 1) r = h_mul(r, b); b = h_mul(b, b); e >>= 1; } return r; }
 inline uint32_t h_inv(uint32_t a) { return h_pow(a, P - 2); }
 struct hpoint { uint32_t x, y; };
@@ -172,5 +178,14 @@ struct StageScope {
 
 // Number of SMs of the current device (152 on GB300).
 int sm_count();
+
+// Pinned host words mapped into the device address space, one growable buffer per host thread:
+// kernels write small results straight into host memory, read after a stream synchronisation.
+struct Mapped {
+  uint32_t* host = nullptr;
+  uint32_t* dev = nullptr;
+  size_t words = 0;
+};
+int32_t mapped_words(size_t words, Mapped& m);
 
 }  // namespace stwo

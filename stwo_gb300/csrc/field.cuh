@@ -70,6 +70,13 @@ __device__ __forceinline__ qm31 qm31_mul_m31(qm31 x, uint32_t y) { return {cm31_
 __device__ __forceinline__ qm31 qm31_mul_cm31(qm31 x, cm31 y) { return {cm31_mul(x.a, y), cm31_mul(x.b, y)}; }
 __device__ __forceinline__ qm31 qm31_from_u32(uint32_t a, uint32_t b, uint32_t c, uint32_t d) { return {{a, b}, {c, d}}; }
 __device__ __forceinline__ qm31 qm31_zero() { return {{0u, 0u}, {0u, 0u}}; }
+__device__ __forceinline__ qm31 qm31_inv(qm31 x) {
+  // (a + bu)^-1 = (a - bu) / (a^2 - (2+i) b^2)  (fields/qm31.rs:121-129)
+  cm31 b2 = cm31_mul(x.b, x.b);
+  cm31 denom = cm31_sub(cm31_mul(x.a, x.a), cm31_mul_r(b2));
+  cm31 di = cm31_inv(denom);
+  return {cm31_mul(x.a, di), cm31_mul(cm31_sub({0u, 0u}, x.b), di)};
+}
 
 // Circle point over M31.
 struct cpoint { uint32_t x, y; };

@@ -10,6 +10,7 @@
 // g = f -+ lambda.
 // Each kernel is one streaming pass over four coordinate columns: HBM-bound.
 #include "common.cuh"
+#include "dchannel.cuh"
 
 namespace stwo {
 
@@ -42,8 +43,16 @@ __device__ __forceinline__ void load_pair(const Secure4& s, size_t i, qm31& a, q
   b = qm31_from_u32(w0.y, w1.y, w2.y, w3.y);
 }
 
+// alpha (and alpha^2) from `alpha_dev` when it is set: the transcript then lives on the device.
+__device__ __forceinline__ void load_alpha(const uint32_t* alpha_dev, qm31& alpha, qm31* alpha_sq) {
+  if (!alpha_dev) return;
+  alpha = qm31_from_u32(__ldg(alpha_dev), __ldg(alpha_dev + 1), __ldg(alpha_dev + 2), __ldg(alpha_dev + 3));
+  if (alpha_sq) *alpha_sq = qm31_from_u32(__ldg(alpha_dev + 4), __ldg(alpha_dev + 5), __ldg(alpha_dev + 6), __ldg(alpha_dev + 7));
+}
+
 __global__ void k_fold_line(Secure4 src, Secure4M dst, uint32_t n_out, const uint32_t* __restrict__ itw_level,
-                            qm31 alpha) {
+                            qm31 alpha, const uint32_t* alpha_dev) {
+  load_alpha(alpha_dev, alpha, nullptr);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
     qm31 f0, f1;
     load_pair(src, i, f0, f1);
@@ -55,7 +64,9 @@ __global__ void k_fold_line(Secure4 src, Secure4M dst, uint32_t n_out, const uin
 // `itw_level` = inverse twiddles of the half coset's level (2^(n-2) entries), used when
 // n >= 3. For n <= 2 the y-coordinates come from the domain points directly.
 __global__ void k_fold_circle(Secure4 src, Secure4M dst, uint32_t n_out, const uint32_t* __restrict__ itw_level,
-                              uint32_t log_src, uint32_t half_init, uint32_t half_step, qm31 alpha, qm31 alpha_sq) {
+                              uint32_t log_src, uint32_t half_init, uint32_t half_step, qm31 alpha, qm31 alpha_sq,
+                              const uint32_t* alpha_dev) {
+  load_alpha(alpha_dev, alpha, &alpha_sq);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
     uint32_t yinv;
     if (log_src >= 3) {
@@ -75,6 +86,25 @@ __global__ void k_fold_circle(Secure4 src, Secure4M dst, uint32_t n_out, const u
     qm31 d = qm31_from_u32(dst.p[0][i], dst.p[1][i], dst.p[2][i], dst.p[3][i]);
     store_q(dst, i, qm31_add(qm31_mul(d, alpha_sq), fp));
   }
+}
+
+// One FRI transcript step on the device (fri.rs:198-214): mix the layer's Merkle root, draw the
+// folding alpha; alpha and alpha^2 go to `alpha_out` (8 words).
+__global__ void k_fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_t* alpha_out) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  d_ch_mix_root(ch, root);
+  qm31 a = d_ch_draw_felt(ch);
+  qm31 a2 = qm31_mul(a, a);
+  alpha_out[0] = a.a.a; alpha_out[1] = a.a.b; alpha_out[2] = a.b.a; alpha_out[3] = a.b.b;
+  alpha_out[4] = a2.a.a; alpha_out[5] = a2.a.b; alpha_out[6] = a2.b.a; alpha_out[7] = a2.b.b;
+}
+
+struct Digest8 { uint32_t w[8]; };
+__global__ void k_channel_set(DevChannel* ch, Digest8 d, uint64_t n_sent) {
+  for (int i = 0; i < 8; i++) ch->digest[i] = d.w[i];
+  ch->n_sent_lo = (uint32_t)n_sent;
+  ch->n_sent_hi = (uint32_t)(n_sent >> 32);
+  ch->error = 0u;
 }
 
 // Per-block partial sums of +f (first half) and -f (second half), four coordinates, reduced
@@ -144,20 +174,21 @@ static bool level_offset(const TwiddleTree* t, stwo_coset c, size_t* off) {
 }
 
 int32_t fri_fold_line(const TwiddleTree* tree, stwo_coset line_domain, const uint32_t* const src[4],
-                      qm31 alpha, uint32_t* const out[4], cudaStream_t s) {
+                      qm31 alpha, uint32_t* const out[4], cudaStream_t s, const uint32_t* alpha_dev) {
   STWO_REQUIRE(line_domain.log_size >= 1, "Evaluation too small");
   size_t off;
   STWO_REQUIRE(level_offset(tree, line_domain, &off), "line domain is not a doubling of the twiddle root");
   uint32_t n_out = 1u << (line_domain.log_size - 1);
   Secure4 sp{{src[0], src[1], src[2], src[3]}};
   Secure4M dp{{out[0], out[1], out[2], out[3]}};
-  k_fold_line<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, tree->d_itw + off, alpha); note_launch();
+  k_fold_line<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, tree->d_itw + off, alpha, alpha_dev);
+  note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
 }
 
 int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* const dst[4],
-                        const uint32_t* const src[4], qm31 alpha, cudaStream_t s) {
+                        const uint32_t* const src[4], qm31 alpha, cudaStream_t s, const uint32_t* alpha_dev) {
   uint32_t log_src = half.log_size + 1;
   size_t off = 0;
   const uint32_t* lvl = nullptr;
@@ -182,7 +213,8 @@ int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* cons
   uint32_t rb0 = h_sub(h_add(bb0, bb0), bb1), rb1 = h_add(bb0, h_add(bb1, bb1));
   qm31 a2 = {{h_add(aa0, rb0), h_add(aa1, rb1)}, {h_add(ab0, ab0), h_add(ab1, ab1)}};
   k_fold_circle<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, lvl, log_src, half.initial_index,
-                                                     half.step_size, alpha, a2); note_launch();
+                                                     half.step_size, alpha, a2, alpha_dev);
+  note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
 }
@@ -211,6 +243,22 @@ int32_t fri_decompose(const uint32_t* const src[4], uint32_t log_size, uint32_t*
   return STWO_OK;
 }
 
+int32_t fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_t* alpha_out, cudaStream_t s) {
+  k_fri_channel_step<<<1, 32, 0, s>>>(ch, root, alpha_out);
+  note_launch();
+  STWO_LAUNCH_CHECK();
+  return STWO_OK;
+}
+
+int32_t channel_set(DevChannel* ch, const uint32_t digest[8], uint64_t n_sent, cudaStream_t s) {
+  Digest8 d;
+  for (int i = 0; i < 8; i++) d.w[i] = digest[i];
+  k_channel_set<<<1, 1, 0, s>>>(ch, d, n_sent);
+  note_launch();
+  STWO_LAUNCH_CHECK();
+  return STWO_OK;
+}
+
 }  // namespace stwo
 
 using namespace stwo;
@@ -219,13 +267,13 @@ extern "C" {
 
 stwo_status stwo_fri_fold_line(stwo_twiddle_tree tree, stwo_coset line_domain, const uint32_t* const d_eval[4],
                                stwo_qm31 alpha, uint32_t* const d_out[4], void* stream) {
-  return fri_fold_line(tree_of(tree), line_domain, d_eval, to_q(alpha), d_out, as_stream(stream));
+  return fri_fold_line(tree_of(tree), line_domain, d_eval, to_q(alpha), d_out, as_stream(stream), nullptr);
 }
 
 stwo_status stwo_fri_fold_circle_into_line(stwo_twiddle_tree tree, stwo_coset src_half_coset,
                                            uint32_t* const d_dst[4], const uint32_t* const d_src[4],
                                            stwo_qm31 alpha, void* stream) {
-  return fri_fold_circle(tree_of(tree), src_half_coset, d_dst, d_src, to_q(alpha), as_stream(stream));
+  return fri_fold_circle(tree_of(tree), src_half_coset, d_dst, d_src, to_q(alpha), as_stream(stream), nullptr);
 }
 
 stwo_status stwo_fri_decompose(const uint32_t* const d_eval[4], uint32_t log_size, uint32_t* const d_g[4],

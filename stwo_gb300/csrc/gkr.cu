@@ -16,6 +16,8 @@
 // the reference.
 #include "common.cuh"
 #include "host_channel.h"
+#include <atomic>
+#include <chrono>
 
 namespace stwo {
 namespace {
@@ -151,7 +153,15 @@ struct RoundOut {
   uint32_t* partials;  // 8 words per block
   unsigned int* ticket;
   uint32_t* result;    // 8 words: f(0), f(2) before the eq correction
+  uint32_t* flag;      // optional (mapped host memory): set to `seq` once `result` is written
+  uint32_t seq;
 };
+
+// Publishes a completion flag to the host polling mapped memory, after every earlier write.
+__device__ __forceinline__ void publish_flag(uint32_t* flag, uint32_t seq) {
+  __threadfence_system();
+  *reinterpret_cast<volatile uint32_t*>(flag) = seq;
+}
 
 // (f(0), f(2)) of sum_x eq((0, x), y) P(t, x) over the current layer (cpu/lookups/gkr.rs:38-212).
 template <uint32_t KIND, bool FIX>
@@ -238,20 +248,26 @@ __global__ void __launch_bounds__(256) k_gkr_round(Cols src, ColsM dst, qm31 c, 
     r[0] = s0[0].a.a; r[1] = s0[0].a.b; r[2] = s0[0].b.a; r[3] = s0[0].b.b;
     r[4] = s2[0].a.a; r[5] = s2[0].a.b; r[6] = s2[0].b.a; r[7] = s2[0].b.b;
     *ro.ticket = 0u;
+    if (ro.flag) publish_flag(ro.flag, ro.seq);
+    else __threadfence_system();
   }
 }
 
 // The gates at positions 0..cur-1 (cur <= 2) into `out`: numerators at words 4j, denominators at
 // 8 + 4j. Used for output layer values and for the masks of constant oracles.
 template <uint32_t KIND, bool FIX>
-__global__ void k_gkr_gates(Cols src, ColsM dst, qm31 c, uint32_t cur, uint32_t* out) {
-  uint32_t j = threadIdx.x;
-  if (j >= cur) return;
-  qm31 n, d = qm31_zero();
-  gate<KIND, FIX>(src, dst, c, cur, j, n, d);
-  uint32_t* o = out + 4 * j;
-  o[0] = n.a.a; o[1] = n.a.b; o[2] = n.b.a; o[3] = n.b.b;
-  o[8] = d.a.a; o[9] = d.a.b; o[10] = d.b.a; o[11] = d.b.b;
+__global__ void k_gkr_gates(Cols src, ColsM dst, qm31 c, uint32_t cur, uint32_t* out, uint32_t* flag, uint32_t seq) {
+  const uint32_t j = threadIdx.x;
+  if (j < cur) {
+    qm31 n, d = qm31_zero();
+    gate<KIND, FIX>(src, dst, c, cur, j, n, d);
+    uint32_t* o = out + 4 * j;
+    o[0] = n.a.a; o[1] = n.a.b; o[2] = n.b.a; o[3] = n.b.b;
+    o[8] = d.a.a; o[9] = d.a.b; o[10] = d.b.a; o[11] = d.b.b;
+    __threadfence_system();
+  }
+  __syncthreads();
+  if (j == 0 && flag) publish_flag(flag, seq);
 }
 
 // ------------------------------------------------------------------------------ MleOps
@@ -301,11 +317,6 @@ using HPoly = std::vector<hq>;
 void hp_trunc(HPoly& p) {
   while (!p.empty() && hq_is_zero(p.back())) p.pop_back();
 }
-bool hp_is_zero(const HPoly& p) {
-  for (auto& c : p)
-    if (!hq_is_zero(c)) return false;
-  return true;
-}
 hq hp_eval(const HPoly& p, hq x) {
   hq acc = HQ_ZERO;
   for (size_t i = p.size(); i-- > 0;) acc = hq_add(hq_mul(acc, x), p[i]);
@@ -323,73 +334,53 @@ HPoly hp_scale(HPoly a, hq s) {
   for (auto& c : a) c = hq_mul(c, s);
   return a;
 }
-HPoly hp_mul(HPoly a, HPoly b) {
-  if (hp_is_zero(a) || hp_is_zero(b)) return {};
-  hp_trunc(a);
-  hp_trunc(b);
-  HPoly r(a.size() + b.size() - 1, HQ_ZERO);
-  for (size_t i = 0; i < a.size(); i++)
-    for (size_t j = 0; j < b.size(); j++) r[i + j] = hq_add(r[i + j], hq_mul(a[i], b[j]));
-  hp_trunc(r);
-  return r;
-}
 HPoly hp_new(HPoly p) {
   hp_trunc(p);
   return p;
 }
-HPoly interpolate_lagrange(const hq* xs, const hq* ys, size_t n) {
-  HPoly acc;
-  for (size_t i = 0; i < n; i++) {
-    hq prod = ys[i];
-    for (size_t j = 0; j < n; j++)
-      if (i != j) prod = hq_mul(prod, hq_inv(hq_sub(xs[i], xs[j])));
-    HPoly term = hp_new({prod});
-    for (size_t j = 0; j < n; j++) {
-      if (i == j) continue;
-      HPoly lin = hp_add({HQ_ZERO, HQ_ONE}, hp_scale(hp_new({xs[j]}), hq_sub(HQ_ZERO, HQ_ONE)));
-      term = hp_mul(term, lin);
-    }
-    acc = hp_add(acc, term);
-  }
-  hp_trunc(acc);
-  return acc;
-}
-
-// gkr_prover.rs:527-566.
+// gkr_prover.rs:527-566. The round polynomial interpolates (0, r0), (1, r1), (2, r2), (b, 0); the
+// interpolant is unique, so the Lagrange basis on {0, 1, 2, b} expanded in closed form gives the
+// reference's coefficients (leading zeros dropped) with two batched inversions.
 int32_t correct_sum(hq f0, hq f2, hq claim, const std::vector<hq>& y, size_t k, HPoly& out) {
-  size_t n = y.size();
+  const size_t n = y.size();
   STWO_REQUIRE(k != 0 && k <= n, "sum_as_poly: %zu variables with %zu eq coordinates", k, n);
-  std::vector<hq> zeros(n - k + 1, HQ_ZERO);
-  hq a = hq_inv(h_eq(zeros.data(), y.data(), n - k + 1));
-  hq yk = y[n - k];
-  hq b = hq_mul(hq_sub(HQ_ONE, yk), hq_inv(hq_sub(HQ_ONE, hq_add(yk, yk))));
-  hq zero = HQ_ZERO, two = hq_make(2, 0, 0, 0);
-  hq r0 = hq_mul(hq_mul(f0, h_eq(&zero, &yk, 1)), a);
-  hq r1 = hq_sub(claim, r0);
-  hq r2 = hq_mul(hq_mul(f2, h_eq(&two, &yk, 1)), a);
-  hq xs[4] = {HQ_ZERO, HQ_ONE, two, b};
-  hq ys[4] = {r0, r1, r2, HQ_ZERO};
-  out = interpolate_lagrange(xs, ys, 4);
-  return STWO_OK;
-}
-
-// Pinned, device-mapped words that kernels write results into (one buffer per host thread).
-struct Mapped {
-  uint32_t* host = nullptr;
-  uint32_t* dev = nullptr;
-  size_t words = 0;
-};
-int32_t mapped_words(size_t words, Mapped& m) {
-  thread_local Mapped tl;
-  if (tl.words < words) {
-    if (tl.host) cudaFreeHost(tl.host);
-    tl = Mapped{};
-    size_t w = std::max<size_t>(words, 4096);
-    STWO_CHECK_CUDA(cudaHostAlloc((void**)&tl.host, w * 4, cudaHostAllocMapped));
-    STWO_CHECK_CUDA(cudaHostGetDevicePointer((void**)&tl.dev, tl.host, 0));
-    tl.words = w;
+  hq prod = HQ_ONE;  // eq(0^(n-k+1), y[..n-k+1])
+  for (size_t j = 0; j <= n - k; j++) prod = hq_mul(prod, hq_sub(HQ_ONE, y[j]));
+  const hq yk = y[n - k];
+  const hq omy = hq_sub(HQ_ONE, yk);
+  const hq bden = hq_sub(HQ_ONE, hq_add(yk, yk));
+  const hq t = hq_mul(prod, bden);
+  if (hq_is_zero(t)) {
+    set_error("sum_as_poly: zero has no inverse");
+    return STWO_ERR_INVALID_ARG;
   }
-  m = tl;
+  const hq ti = hq_inv(t);
+  const hq a = hq_mul(ti, bden);
+  const hq b = hq_mul(omy, hq_mul(ti, prod));
+  const hq two = hq_make(2, 0, 0, 0), three = hq_make(3, 0, 0, 0);
+  const hq r0 = hq_mul(hq_mul(f0, omy), a);
+  const hq r1 = hq_sub(claim, r0);
+  const hq r2 = hq_mul(hq_mul(f2, hq_sub(hq_mul(three, yk), HQ_ONE)), a);  // eq([2], [yk]) = 3 yk - 1
+  const hq bm1 = hq_sub(b, HQ_ONE), tmb = hq_sub(two, b);
+  const hq p1 = hq_mul(b, bm1), p2 = hq_mul(p1, tmb);
+  if (hq_is_zero(p2)) {
+    set_error("sum_as_poly: zero has no inverse");
+    return STWO_ERR_INVALID_ARG;
+  }
+  const hq ip2 = hq_inv(p2), ip1 = hq_mul(ip2, tmb);
+  const hq inv_b = hq_mul(ip1, bm1), inv_bm1 = hq_mul(ip1, b), inv_tmb = hq_mul(ip2, p1);
+  const hq half = hq_make((P + 1) / 2, 0, 0, 0);
+  const hq A = hq_sub(HQ_ZERO, hq_mul(hq_mul(r0, inv_b), half));  // r0 / (-2b)
+  const hq B = hq_mul(r1, inv_bm1);                              // r1 / (b - 1)
+  const hq Cc = hq_mul(hq_mul(r2, inv_tmb), half);               // r2 / (2 (2 - b))
+  const hq b2 = hq_add(b, b), b3 = hq_add(b2, b);
+  out.assign(4, HQ_ZERO);
+  out[3] = hq_add(hq_add(A, B), Cc);
+  out[2] = hq_sub(HQ_ZERO, hq_add(hq_add(hq_mul(hq_add(three, b), A), hq_mul(hq_add(two, b), B)),
+                                  hq_mul(hq_add(HQ_ONE, b), Cc)));
+  out[1] = hq_add(hq_add(hq_mul(hq_add(two, b3), A), hq_mul(b2, B)), hq_mul(b, Cc));
+  out[0] = r0;
+  hp_trunc(out);
   return STWO_OK;
 }
 
@@ -421,14 +412,43 @@ void round_dispatch(uint32_t kind, const Cols& src, const ColsM& dst, qm31 c, ui
 
 template <bool FIX>
 void gates_dispatch(uint32_t kind, const Cols& src, const ColsM& dst, qm31 c, uint32_t cur, uint32_t* out,
-                    cudaStream_t s) {
+                    cudaStream_t s, uint32_t* flag = nullptr, uint32_t seq = 0) {
   switch (kind) {
-    case K_GP: k_gkr_gates<K_GP, FIX><<<1, 32, 0, s>>>(src, dst, c, cur, out); break;
-    case K_GENERIC: k_gkr_gates<K_GENERIC, FIX><<<1, 32, 0, s>>>(src, dst, c, cur, out); break;
-    case K_MULT: k_gkr_gates<K_MULT, FIX><<<1, 32, 0, s>>>(src, dst, c, cur, out); break;
-    default: k_gkr_gates<K_SINGLES, FIX><<<1, 32, 0, s>>>(src, dst, c, cur, out); break;
+    case K_GP: k_gkr_gates<K_GP, FIX><<<1, 32, 0, s>>>(src, dst, c, cur, out, flag, seq); break;
+    case K_GENERIC: k_gkr_gates<K_GENERIC, FIX><<<1, 32, 0, s>>>(src, dst, c, cur, out, flag, seq); break;
+    case K_MULT: k_gkr_gates<K_MULT, FIX><<<1, 32, 0, s>>>(src, dst, c, cur, out, flag, seq); break;
+    default: k_gkr_gates<K_SINGLES, FIX><<<1, 32, 0, s>>>(src, dst, c, cur, out, flag, seq); break;
   }
   note_launch();
+}
+
+// Waits until a kernel publishes `seq` in the mapped word `flag`: a host spin of about a
+// microsecond per round instead of a stream synchronisation. Bounded: a stream error, or no flag
+// after 30 s, ends the wait with an error.
+int32_t wait_flag(const uint32_t* flag, uint32_t seq, cudaStream_t s) {
+  const volatile uint32_t* f = flag;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (uint64_t it = 1;; it++) {
+    if (*f == seq) {
+      std::atomic_thread_fence(std::memory_order_acquire);
+      return STWO_OK;
+    }
+    if ((it & 4095) == 0) {
+      cudaError_t e = cudaStreamQuery(s);
+      if (e != cudaSuccess && e != cudaErrorNotReady) {
+        set_error("GKR round: %s", cudaGetErrorString(e));
+        return STWO_ERR_CUDA;
+      }
+      if (e == cudaSuccess && *f != seq) {
+        set_error("GKR round: stream finished without publishing its result");
+        return STWO_ERR_CUDA;
+      }
+      if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(30)) {
+        set_error("GKR round: no result after 30 s");
+        return STWO_ERR_TIMEOUT;
+      }
+    }
+  }
 }
 
 int32_t launch_eq_evals(const std::vector<hq>& y, hq v, const SecM& out, cudaStream_t s) {
@@ -532,8 +552,13 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
   STWO_CHECK_CUDA(cudaMemsetAsync(ro.ticket, 0, 4, s));
 
   Mapped mp;
-  st = mapped_words((size_t)n_inst * 24, mp);
+  st = mapped_words((size_t)n_inst * 24 + 1, mp);
   if (st) return st;
+  // Completion flag of the round and mask kernels, polled by the host (wait_flag).
+  uint32_t* const flag_dev = mp.dev + (size_t)n_inst * 24;
+  const uint32_t* const flag_host = mp.host + (size_t)n_inst * 24;
+  mp.host[(size_t)n_inst * 24] = 0;
+  uint32_t seq = 0;
 
   // Circuit layers (gen_layers, gkr_prover.rs:508-516): layers[n] is the caller's input.
   for (uint32_t i = 0; i < n_inst; i++) {
@@ -628,13 +653,20 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
     std::vector<hq> assignment;
     for (uint32_t r = 0; r < sc_vars; r++) {
       const uint32_t rem = sc_vars - r;
-      bool any = false;
+      size_t last_live = act.size();
+      for (size_t a = 0; a < act.size(); a++)
+        if (inst[act[a]].oracle_vars == rem) last_live = a;
+      const bool any = last_live < act.size();
+      if (any) seq++;
       for (size_t a = 0; a < act.size(); a++) {
         Instance& I = inst[act[a]];
         if (I.oracle_vars != rem) continue;
-        any = true;
         RoundOut o = ro;
         o.result = mp.dev + 24 * act[a];
+        if (a == last_live) {
+          o.flag = flag_dev;
+          o.seq = seq;
+        }
         ColsM dst{I.work_num, I.work_den};
         if (I.fix_pending) {
           round_dispatch<true>(I.kind, I.src, dst, to_q(I.pending), I.cur, as_const(eq), to_q(lambda), o, s);
@@ -647,7 +679,8 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
       }
       if (any) {
         STWO_LAUNCH_CHECK();
-        STWO_CHECK_CUDA(cudaStreamSynchronize(s));
+        st = wait_flag(flag_host, seq, s);
+        if (st) return st;
       }
       std::vector<HPoly> polys;
       for (size_t a = 0; a < act.size(); a++) {
@@ -688,15 +721,18 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
     }
     rounds_per_layer.push_back(sc_vars);
     // Masks of the now constant oracles (gkr_prover.rs:320-346).
+    seq++;
     for (size_t a = 0; a < act.size(); a++) {
       Instance& I = inst[act[a]];
       ColsM dst{I.work_num, I.work_den};
-      if (I.fix_pending) gates_dispatch<true>(I.kind, I.src, dst, to_q(I.pending), 2, mp.dev + 24 * act[a], s);
-      else gates_dispatch<false>(I.kind, I.src, dst, QZ, 2, mp.dev + 24 * act[a], s);
+      uint32_t* f = a + 1 == act.size() ? flag_dev : nullptr;
+      if (I.fix_pending) gates_dispatch<true>(I.kind, I.src, dst, to_q(I.pending), 2, mp.dev + 24 * act[a], s, f, seq);
+      else gates_dispatch<false>(I.kind, I.src, dst, QZ, 2, mp.dev + 24 * act[a], s, f, seq);
       if (I.fix_pending && I.kind == K_MULT) I.kind = K_GENERIC;
     }
     STWO_LAUNCH_CHECK();
-    STWO_CHECK_CUDA(cudaStreamSynchronize(s));
+    st = wait_flag(flag_host, seq, s);
+    if (st) return st;
     for (size_t a = 0; a < act.size(); a++) {
       Instance& I = inst[act[a]];
       const uint32_t* w = mp.host + 24 * act[a];

@@ -14,6 +14,8 @@
 #include "common.cuh"
 #include "host_channel.h"
 #include "prover.cuh"
+#include "dchannel.cuh"
+#include <future>
 #include <set>
 
 namespace stwo {
@@ -29,9 +31,26 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
                              const stwo_sample_batch* batches, uint32_t n_batches, uint32_t log_blowup,
                              uint32_t* const out[4], cudaStream_t s);
 int32_t fri_fold_line(const TwiddleTree* tree, stwo_coset line_domain, const uint32_t* const src[4], qm31 alpha,
-                      uint32_t* const out[4], cudaStream_t s);
+                      uint32_t* const out[4], cudaStream_t s, const uint32_t* alpha_dev);
 int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* const dst[4], const uint32_t* const src[4],
-                        qm31 alpha, cudaStream_t s);
+                        qm31 alpha, cudaStream_t s, const uint32_t* alpha_dev);
+int32_t fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_t* alpha_out, cudaStream_t s);
+int32_t channel_set(DevChannel* ch, const uint32_t digest[8], uint64_t n_sent, cudaStream_t s);
+
+// Copies segments of device words into one destination (mapped host memory) in one launch.
+constexpr int COLLECT_MAX = 48;
+struct CollectList {
+  const uint32_t* src[COLLECT_MAX];
+  uint32_t n[COLLECT_MAX];
+  uint32_t count;
+};
+__global__ void k_collect(CollectList l, uint32_t* out) {
+  uint32_t base = 0;
+  for (uint32_t k = 0; k < l.count; k++) {
+    for (uint32_t i = threadIdx.x; i < l.n[k]; i += blockDim.x) out[base + i] = l.src[k][i];
+    base += l.n[k];
+  }
+}
 int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
                        const uint32_t* poly_of, const stwo_qm31_point* points, uint32_t n_evals, stwo_qm31* out,
                        cudaStream_t s);
@@ -100,7 +119,7 @@ static uint32_t ilog2u(size_t n) {
   return l;
 }
 
-int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s) {
+int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root) {
   sorted = columns;
   std::stable_sort(sorted.begin(), sorted.end(), [](const ColRef& a, const ColRef& b) { return a.log > b.log; });
   uint32_t max_log = sorted.empty() ? 0 : sorted[0].log;
@@ -130,10 +149,13 @@ int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cuda
     if (st) return st;
     lg = stop - 1;
   }
-  uint32_t w[8];
-  STWO_CHECK_CUDA(cudaMemcpyAsync(w, layers[0], 32, cudaMemcpyDeviceToHost, s));
+  if (!read_root) return STWO_OK;
+  Mapped mp;
+  int32_t st = mapped_words(8, mp);
+  if (st) return st;
+  STWO_CHECK_CUDA(cudaMemcpyAsync(mp.host, layers[0], 32, cudaMemcpyDeviceToHost, s));
   STWO_CHECK_CUDA(cudaStreamSynchronize(s));
-  root = Digest::from_words(w);
+  root = Digest::from_words(mp.host);
   return STWO_OK;
 }
 
@@ -469,7 +491,10 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   for (auto& v : svals) flat.push_back(from_sq(v));
   ch.mix_felts(flat);
 
-  // Sanity check of the composition at the OODS point (prover/mod.rs:70-76).
+  // Sanity check of the composition at the OODS point (prover/mod.rs:70-76). It is host
+  // arithmetic only, so it runs on another host thread while the stream computes the quotients
+  // and the FRI layers; its verdict is collected before the proof is written.
+  std::future<bool> sanity;
   {
     std::vector<std::vector<std::vector<hq>>> mv(trees.size() - 1);
     size_t k = 0;
@@ -490,13 +515,19 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     HPointQ q = hpq_add_m31(oods, shift);
     hq x = q.x;
     for (uint32_t i = 1; i < air.log_size(); i++) x = hq_sub(hq_add(hq_mul(x, x), hq_mul(x, x)), hq_make(1, 0, 0, 0));
-    hq rhs = air.eval_at_point(mv, rc, hq_inv(x));
-    for (int i = 0; i < 4; i++)
-      if (lhs.v[i] != rhs.v[i]) {
-        set_error("ConstraintsNotSatisfied");
-        return STWO_ERR_INVALID_ARG;
-      }
+    hq dinv = hq_inv(x);
+    sanity = std::async(std::launch::async, [&air, mv = std::move(mv), rc, dinv, lhs]() {
+      hq rhs = air.eval_at_point(mv, rc, dinv);
+      return std::memcmp(lhs.v, rhs.v, sizeof(lhs.v)) == 0;
+    });
   }
+  // Every return below first waits for the check (it reads `air`).
+  struct JoinCheck {
+    std::future<bool>& f;
+    ~JoinCheck() {
+      if (f.valid()) f.wait();
+    }
+  } join_check{sanity};
 
   // FRI quotients per log size, descending (pcs/quotients.rs:76-101).
   struct ColS { const uint32_t* p; uint32_t log; std::vector<std::pair<HPointQ, hq>> samples; };
@@ -559,10 +590,25 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   std::vector<ColRef> first_cols;
   for (size_t i = 0; i < quotients.size(); i++)
     for (int k = 0; k < 4; k++) first_cols.push_back({quotients[i].c[k], qlogs[i]});
+  // The transcript of the commit phase runs on the device: each layer's root is mixed and its
+  // alpha drawn by one thread on the stream, so the layers follow one another with no host round
+  // trip; the roots, the channel state and the last layer come back together at the end.
+  DevChannel* dch = reinterpret_cast<DevChannel*>(arena.alloc(sizeof(DevChannel) / 4));
+  constexpr size_t FRI_MAX_STEPS = 40;
+  uint32_t* alphas = arena.alloc(8 * FRI_MAX_STEPS);
+  if (!dch || !alphas) return STWO_ERR_OOM;
+  {
+    uint32_t d[8];
+    ch.digest.words(d);
+    st = channel_set(dch, d, ch.n_sent, s);
+    if (st) return st;
+  }
   DevMerkle first_tree;
-  st = first_tree.commit(first_cols, arena, s);
+  st = first_tree.commit(first_cols, arena, s, false);
   if (st) return st;
-  ch.mix_root(first_tree.root);
+  size_t fstep = 0;
+  st = fri_channel_step(dch, first_tree.layers[0], alphas + 8 * fstep, s);
+  if (st) return st;
   struct Layer { SecureCols eval; stwo_coset dom; DevMerkle merkle; };
   std::vector<Layer> layers;
   stwo_coset dom = coset_new(1u << (31 - (qlogs[0] - 1 + 2)), qlogs[0] - 1);  // Coset::half_odds(log-1)
@@ -572,10 +618,10 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     if (!cur.c[k]) return STWO_ERR_OOM;
     STWO_CHECK_CUDA(cudaMemsetAsync(cur.c[k], 0, ((size_t)4) << dom.log_size, s));
   }
-  hq alpha = ch.draw_felt();
+  const qm31 unused_alpha = {{0u, 0u}, {0u, 0u}};
   size_t next = 0;
   st = fri_fold_circle(tree, canonic_half_coset(qlogs[0]), cur.c, const_cast<const uint32_t* const*>(quotients[0].c),
-                       to_dq(alpha), s);
+                       unused_alpha, s, alphas + 8 * fstep);
   if (st) return st;
   next = 1;
   size_t last_size = (size_t)1 << (cfg.log_last_layer_degree_bound + cfg.log_blowup_factor);
@@ -585,21 +631,23 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     L.dom = dom;
     std::vector<ColRef> lc;
     for (int k = 0; k < 4; k++) lc.push_back({cur.c[k], dom.log_size});
-    st = L.merkle.commit(lc, arena, s);
+    st = L.merkle.commit(lc, arena, s, false);
     if (st) return st;
-    ch.mix_root(L.merkle.root);
-    alpha = ch.draw_felt();
+    STWO_REQUIRE(++fstep < FRI_MAX_STEPS, "too many FRI layers");
+    st = fri_channel_step(dch, L.merkle.layers[0], alphas + 8 * fstep, s);
+    if (st) return st;
     SecureCols nxt;
     for (int k = 0; k < 4; k++) {
       nxt.c[k] = arena.alloc((size_t)1 << (dom.log_size - 1));
       if (!nxt.c[k]) return STWO_ERR_OOM;
     }
-    st = fri_fold_line(tree, dom, const_cast<const uint32_t* const*>(cur.c), to_dq(alpha), nxt.c, s);
+    st = fri_fold_line(tree, dom, const_cast<const uint32_t* const*>(cur.c), unused_alpha, nxt.c, s,
+                       alphas + 8 * fstep);
     if (st) return st;
     dom = coset_double(dom);
     if (next < quotients.size() && qlogs[next] - 1 == dom.log_size) {
       st = fri_fold_circle(tree, canonic_half_coset(qlogs[next]), nxt.c,
-                           const_cast<const uint32_t* const*>(quotients[next].c), to_dq(alpha), s);
+                           const_cast<const uint32_t* const*>(quotients[next].c), unused_alpha, s, alphas + 8 * fstep);
       if (st) return st;
       next++;
     }
@@ -607,14 +655,45 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     cur = nxt;
   }
   STWO_REQUIRE(next == quotients.size(), "not all FRI columns consumed");
-  // Last layer: read back and interpolate on the host (fri.rs:272-290).
+  STWO_REQUIRE(layers.size() + 1 + 5 <= (size_t)COLLECT_MAX, "too many FRI layers");
+  // Roots, channel state and the last layer (fri.rs:272-290) in one copy to mapped host memory.
   std::vector<hq> last(last_size);
   {
-    std::vector<uint32_t> w(4 * last_size);
-    for (int k = 0; k < 4; k++)
-      STWO_CHECK_CUDA(cudaMemcpyAsync(w.data() + k * last_size, cur.c[k], last_size * 4, cudaMemcpyDeviceToHost, s));
+    CollectList cl{};
+    auto add = [&](const uint32_t* p, uint32_t n) {
+      cl.src[cl.count] = p;
+      cl.n[cl.count++] = n;
+    };
+    add(first_tree.layers[0], 8);
+    for (auto& L : layers) add(L.merkle.layers[0], 8);
+    add(reinterpret_cast<const uint32_t*>(dch), sizeof(DevChannel) / 4);
+    for (int k = 0; k < 4; k++) add(cur.c[k], (uint32_t)last_size);
+    size_t total = 8 * (1 + layers.size()) + sizeof(DevChannel) / 4 + 4 * last_size;
+    Mapped mp;
+    st = mapped_words(total, mp);
+    if (st) return st;
+    k_collect<<<1, 256, 0, s>>>(cl, mp.dev);
+    note_launch();
+    STWO_LAUNCH_CHECK();
     STWO_CHECK_CUDA(cudaStreamSynchronize(s));
-    for (size_t i = 0; i < last_size; i++) last[i] = hq_make(w[i], w[last_size + i], w[2 * last_size + i], w[3 * last_size + i]);
+    const uint32_t* w = mp.host;
+    first_tree.root = Digest::from_words(w);
+    w += 8;
+    for (auto& L : layers) {
+      L.merkle.root = Digest::from_words(w);
+      w += 8;
+    }
+    DevChannel dc;
+    std::memcpy(&dc, w, sizeof(DevChannel));
+    w += sizeof(DevChannel) / 4;
+    if (dc.error) {
+      set_error("FRI channel: felt draw exhausted its retries");
+      return STWO_ERR_CUDA;
+    }
+    ch.digest = Digest::from_words(dc.digest);
+    ch.n_sent = (uint64_t)dc.n_sent_lo | ((uint64_t)dc.n_sent_hi << 32);
+    for (size_t i = 0; i < last_size; i++)
+      last[i] = hq_make(w[i], w[last_size + i], w[2 * last_size + i], w[3 * last_size + i]);
   }
   std::vector<hq> coeffs = line_interpolate_host(dom, last);  // bit-reversed coefficient order
   bit_reverse_host(coeffs);                                   // natural order
@@ -708,6 +787,10 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   }
   w.u64(coeffs.size());
   for (auto& c : coeffs) w.q(c);
+  if (!sanity.get()) {
+    set_error("ConstraintsNotSatisfied");
+    return STWO_ERR_INVALID_ARG;
+  }
   out.swap(w.b);
   return arena.failed ? STWO_ERR_OOM : STWO_OK;
 }

@@ -51,7 +51,8 @@ struct DevMerkle {
   std::vector<uint32_t*> layers;  // layers[l]: 2^l hashes of 8 words
   std::vector<ColRef> sorted;     // columns, stable-sorted by descending log size
   Digest root;
-  int32_t commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s);
+  // With read_root false the root stays on the device (layers[0]) and `root` is left unset.
+  int32_t commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root = true);
   void decommit(const std::map<uint32_t, std::vector<size_t>>& queries, Gather& g, DecommitRecipe& out) const;
 };
 

@@ -81,6 +81,20 @@ void scratch_free(void* p, cudaStream_t s) {
   if (p) cudaFreeAsync(p, s);
 }
 
+int32_t mapped_words(size_t words, Mapped& m) {
+  thread_local Mapped tl;
+  if (tl.words < words) {
+    if (tl.host) cudaFreeHost(tl.host);
+    tl = Mapped{};
+    size_t w = std::max<size_t>(words, 4096);
+    STWO_CHECK_CUDA(cudaHostAlloc((void**)&tl.host, w * 4, cudaHostAllocMapped));
+    STWO_CHECK_CUDA(cudaHostGetDevicePointer((void**)&tl.dev, tl.host, 0));
+    tl.words = w;
+  }
+  m = tl;
+  return STWO_OK;
+}
+
 hpoint h_index_to_point(uint32_t idx) {
   struct Tower {
     hpoint p[31];

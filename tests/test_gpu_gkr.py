@@ -214,3 +214,11 @@ def test_rejects_bad_arguments(cuda):
         GkrOps.prove_batch([GkrLayer(2, _dev(rng.integers(0, F.P, 2, dtype=np.uint32)), _sec(_rand(rng, 2)))])
     with pytest.raises(_lib.StwoError):
         GkrOps.prove_batch([GkrLayer(7, None, _sec(_rand(rng, 4)))])
+
+
+def test_large_mixed_batch(cuda, oracle):
+    # 66 instances of three kinds and sizes 2..4 in one batch.
+    rng = np.random.default_rng(65)
+    layers = [(k % 4 if k % 4 != 2 else 1, _layer(rng, k % 4 if k % 4 != 2 else 1, 2 + k % 3)) for k in range(66)]
+    got, want, dg, dw = _prove_both(oracle, layers)
+    assert got == want and dg == dw
