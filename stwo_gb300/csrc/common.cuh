@@ -136,6 +136,10 @@ struct TwiddleTree {
   stwo_coset root;
   uint32_t* d_tw = nullptr;
   uint32_t* d_itw = nullptr;
+  // The same twiddles doubled (2t as a 32-bit word) for the FFT butterflies: a product a * 2t
+  // splits at bit 32, so its reduction mod P needs one shift fewer (d_itw2 = d_tw2 + size).
+  uint32_t* d_tw2 = nullptr;
+  uint32_t* d_itw2 = nullptr;
   size_t size = 0;  // 2^root.log_size (>= 1)
 };
 

@@ -20,6 +20,27 @@
 
 namespace stwo {
 
+// Butterflies with doubled twiddles t2 = 2t (a 32-bit word): the 64-bit product a * t2 = 2at
+// splits at bit 32 into floor(at / 2^31) (the high word) and (at mod 2^31) (the low word shifted
+// right once), whose sum is at mod P up to one subtraction. The results equal those of
+// bfly / ibfly (crates/prover/src/core/fft.rs:5-21) with t.
+__device__ __forceinline__ uint32_t mul_tw2(uint32_t a, uint32_t t2) {
+  const uint64_t p = (uint64_t)a * t2;
+  const uint32_t s = (uint32_t)(p >> 32) + ((uint32_t)p >> 1);  // < 2P
+  return min(s, s - P);
+}
+__device__ __forceinline__ uint32_t neg_tw2(uint32_t t2) { return t2 ? 0xFFFFFFFEu - t2 : 0u; }  // 2(P - t)
+__device__ __forceinline__ void bfly2(uint32_t& v0, uint32_t& v1, uint32_t t2) {
+  const uint32_t tmp = mul_tw2(v1, t2);
+  v1 = m31_sub(v0, tmp);
+  v0 = m31_add(v0, tmp);
+}
+__device__ __forceinline__ void ibfly2(uint32_t& v0, uint32_t& v1, uint32_t it2) {
+  const uint32_t tmp = v0;
+  v0 = m31_add(tmp, v1);
+  v1 = mul_tw2(m31_sub(tmp, v1), it2);
+}
+
 constexpr uint32_t FFT_TMAX = 12;   // contiguous tile: 2^12 words = 16 KB (+ padding)
 constexpr uint32_t FFT_TMAX_STRIDED = 13;
 constexpr uint32_t FFT_R = 4;        // 2^4 words per thread, 4 layers per register round
@@ -32,7 +53,7 @@ struct FftPass {
   uint32_t T;        // tile log size = c + nl
   const uint32_t* tw;  // twiddles (forward) or inverse twiddles
   uint32_t tw_size;    // tree size 2^root.log_size
-  uint32_t small_y;    // circle-layer twiddle when L <= 2 (inverted for interpolate)
+  uint32_t small_y;    // circle-layer twiddle when L <= 2 (inverted for interpolate), doubled
   uint32_t scale;      // output multiplier (1 = none)
   uint32_t read_src;   // read from src (masked to 2^F) instead of dst
 };
@@ -45,10 +66,10 @@ __device__ __forceinline__ uint32_t fft_twiddle(const FftPass& p, uint32_t layer
     return __ldg(&p.tw[off + (idx0 >> (layer + 1))]);
   }
   uint32_t h = idx0 >> 1;
-  if (p.L <= 2) return (h & 1) ? m31_neg(p.small_y) : p.small_y;
+  if (p.L <= 2) return (h & 1) ? neg_tw2(p.small_y) : p.small_y;
   uint32_t off = p.tw_size - (1u << (p.L - 1));
   uint32_t t = __ldg(&p.tw[off + ((h >> 1) ^ 1)]);
-  return ((h ^ (h >> 1)) & 1) ? m31_neg(t) : t;
+  return ((h ^ (h >> 1)) & 1) ? neg_tw2(t) : t;
 }
 
 // Global index of tile element e: its low c bits are global bits [0, c), the next nl bits are
@@ -92,8 +113,8 @@ __device__ __forceinline__ void fft_round(const FftPass& p, uint32_t* sm, uint32
         const uint32_t t = fft_twiddle(p, layer, g0);
 #pragma unroll
         for (int kl = 0; kl < (1 << j); kl++) {
-          if (INV) ibfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
-          else bfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+          if (INV) ibfly2(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+          else bfly2(v[k0 | kl], v[k0 | kl | (1 << j)], t);
         }
       }
     }
@@ -191,11 +212,11 @@ __device__ __forceinline__ void fft_round_ct(const FftPass& p, uint32_t* sm, uin
           // compile-time; otherwise they come from the full index.
           if (RB - 1 - j >= 2) {
             uint32_t raw = __ldg(twp + ((kh >> 1) ^ 1));
-            t = ((kh ^ (kh >> 1)) & 1) ? m31_neg(raw) : raw;
+            t = ((kh ^ (kh >> 1)) & 1) ? neg_tw2(raw) : raw;
           } else {
             const uint32_t h = hb + kh;
             uint32_t raw = __ldg(p.tw + (p.tw_size - (llo >> 1)) + ((h >> 1) ^ 1));
-            t = ((h ^ (h >> 1)) & 1) ? m31_neg(raw) : raw;
+            t = ((h ^ (h >> 1)) & 1) ? neg_tw2(raw) : raw;
           }
         } else {
           t = __ldg(twp + kh);
@@ -203,8 +224,8 @@ __device__ __forceinline__ void fft_round_ct(const FftPass& p, uint32_t* sm, uin
         const int k0 = kh << (j + 1);
 #pragma unroll
         for (int kl = 0; kl < (1 << j); kl++) {
-          if (INV) ibfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
-          else bfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+          if (INV) ibfly2(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+          else bfly2(v[k0 | kl], v[k0 | kl | (1 << j)], t);
         }
       }
     }
@@ -306,8 +327,8 @@ __global__ void __launch_bounds__(256) k_fft_reg(FftPass p, ConstColPtrs src, Co
       const int k0 = kh << (j + 1);
 #pragma unroll
       for (int kl = 0; kl < (1 << j); kl++) {
-        if (INV) ibfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
-        else bfly(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+        if (INV) ibfly2(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+        else bfly2(v[k0 | kl], v[k0 | kl | (1 << j)], t);
       }
     }
   }
@@ -381,13 +402,13 @@ static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, c
   FftPass base{};
   base.L = L;
   base.F = F;
-  base.tw = inverse ? tree->d_itw : tree->d_tw;
+  base.tw = inverse ? tree->d_itw2 : tree->d_tw2;
   base.tw_size = (uint32_t)tree->size;
   base.scale = 1u;
   base.small_y = 0;
   if (L <= 2) {
     uint32_t y = h_index_to_point(half.initial_index).y;
-    base.small_y = inverse ? h_inv(y) : y;
+    base.small_y = 2u * (inverse ? h_inv(y) : y);  // doubled, as every twiddle here
   }
 
   std::vector<PassPlan> plan = plan_passes(F);

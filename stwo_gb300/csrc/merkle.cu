@@ -19,7 +19,7 @@ struct MerkleCols { const uint32_t* p[MERKLE_MAX_COLS]; };
 __global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const uint32_t* __restrict__ prev,
                                                       MerkleCols cols, uint32_t n_cols, uint32_t* __restrict__ out,
                                                       uint32_t* __restrict__ state, uint32_t first, uint32_t last,
-                                                      uint32_t total_bytes) {
+                                                      uint32_t one) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_nodes) return;
   uint32_t h[8];
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const ui
 #pragma unroll
     for (int q = 0; q < 16; q++) m[q] = (uint32_t)q < k ? __ldg(cols.p[c + q] + i) : 0u;
     t += 4 * k;
-    b2s_compress(h, m, t, fin);
+    b2s_compress_fma(h, m, t, fin, one);
     c += k;
   }
   if (last) {
@@ -69,7 +69,6 @@ __global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const ui
     for (int q = 0; q < 8; q++) state[(size_t)9 * i + q] = h[q];
     state[(size_t)9 * i + 8] = t;
   }
-  (void)total_bytes;
 }
 
 int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols, uint32_t n_cols,
@@ -94,7 +93,7 @@ int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint3
     uint32_t nc = n_cols - c0 < per_launch ? n_cols - c0 : per_launch;
     MerkleCols mc;
     for (uint32_t q = 0; q < nc; q++) mc.p[q] = cols[c0 + q];
-    k_merkle_layer<<<blocks, threads, 0, s>>>(n, prev, mc, nc, out, state, l == 0, l + 1 == n_launch, 0); note_launch();
+    k_merkle_layer<<<blocks, threads, 0, s>>>(n, prev, mc, nc, out, state, l == 0, l + 1 == n_launch, 1u); note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       scratch_free(state, s);

@@ -11,7 +11,7 @@
 
 namespace stwo {
 
-constexpr uint32_t EP_LOW = 8, EP_MID = 6;
+constexpr uint32_t EP_LOW = 8, EP_MID = 8;
 
 struct EvalJob {
   const uint32_t* coeffs;
@@ -40,8 +40,11 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
   __shared__ qm31 s_map[32];
   __shared__ qm31 s_mid[1 << EP_MID];
   __shared__ qm31 s_part[8];
+  __shared__ EvalJob s_job;
   const uint32_t e = blockIdx.y;
-  const EvalJob job = jobs[poly_of[e]];
+  if (threadIdx.x == 0) s_job = jobs[poly_of[e]];  // one read of the (possibly host-mapped) tables
+  __syncthreads();
+  const EvalJob job = s_job;
   const uint32_t L = job.log_size;
   const uint32_t lo_bits = L < EP_LOW ? L : EP_LOW;
   const uint32_t mid_bits = L - lo_bits < EP_MID ? L - lo_bits : EP_MID;
@@ -62,21 +65,36 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
   if (t < (1u << lo_bits)) {
     const uint32_t* c = job.coeffs + ((size_t)blockIdx.x << chunk_bits);
     unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    uint32_t cnt = 0;
-    for (uint32_t m = 0; m < (1u << mid_bits); m++) {
-      uint32_t v = __ldg(c + (m << lo_bits) + t);
-      qm31 w = s_mid[m];
-      a0 += (unsigned long long)w.a.a * v;
-      a1 += (unsigned long long)w.a.b * v;
-      a2 += (unsigned long long)w.b.a * v;
-      a3 += (unsigned long long)w.b.b * v;
-      if (++cnt == 3) {
-        a0 = (a0 & P) + (a0 >> 31);
-        a1 = (a1 & P) + (a1 >> 31);
-        a2 = (a2 & P) + (a2 >> 31);
-        a3 = (a3 & P) + (a3 >> 31);
-        cnt = 0;
+    // Products are < 2^62; folding after every second one keeps the sums below 2^64. Eight
+    // coefficient loads are issued before they are used.
+    const uint32_t n_mid = 1u << mid_bits;
+    uint32_t m = 0;
+    for (; m + 8 <= n_mid; m += 8) {
+      uint32_t v[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) v[k] = __ldg(c + ((m + k) << lo_bits) + t);
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const qm31 w = s_mid[m + k];
+        a0 += (unsigned long long)w.a.a * v[k];
+        a1 += (unsigned long long)w.a.b * v[k];
+        a2 += (unsigned long long)w.b.a * v[k];
+        a3 += (unsigned long long)w.b.b * v[k];
+        if (k & 1) {
+          a0 = (a0 & P) + (a0 >> 31);
+          a1 = (a1 & P) + (a1 >> 31);
+          a2 = (a2 & P) + (a2 >> 31);
+          a3 = (a3 & P) + (a3 >> 31);
+        }
       }
+    }
+    for (; m < n_mid; m++) {
+      const uint32_t v = __ldg(c + (m << lo_bits) + t);
+      const qm31 w = s_mid[m];
+      a0 = (a0 & P) + (a0 >> 31) + (unsigned long long)w.a.a * v;
+      a1 = (a1 & P) + (a1 >> 31) + (unsigned long long)w.a.b * v;
+      a2 = (a2 & P) + (a2 >> 31) + (unsigned long long)w.b.a * v;
+      a3 = (a3 & P) + (a3 >> 31) + (unsigned long long)w.b.b * v;
     }
     auto red = [](unsigned long long x) {
       x = (x & P) + (x >> 31);
@@ -139,40 +157,42 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
     max_chunks = std::max(max_chunks, 1u << (L - cb));
   }
   STWO_REQUIRE(n_evals <= 65535, "too many evaluations in one call");
-  size_t off_jobs = 0;
-  size_t off_polyof = off_jobs + ((jobs.size() * sizeof(EvalJob) + 255) / 256) * 256;
-  size_t off_pts = off_polyof + (((size_t)n_evals * 4 + 255) / 256) * 256;
-  size_t off_acc = off_pts + (((size_t)n_evals * sizeof(stwo_qm31_point) + 255) / 256) * 256;
-  size_t off_out = off_acc + (size_t)n_evals * 4 * 8;
-  size_t total = off_out + (size_t)n_evals * 16;
-  char* buf = nullptr;
-  int32_t st = scratch_alloc((void**)&buf, total, s);
+  // The job tables go to the kernel through mapped host memory (read once per block) and the
+  // results come back the same way: no staging copies around the launch.
+  const size_t w_jobs = (jobs.size() * sizeof(EvalJob) + 15) / 16 * 4;
+  const size_t w_polyof = ((size_t)n_evals + 3) / 4 * 4;
+  const size_t w_pts = (size_t)n_evals * sizeof(stwo_qm31_point) / 4;
+  const size_t w_out = (size_t)n_evals * 4;
+  Mapped mp;
+  int32_t st = mapped_words(w_jobs + w_polyof + w_pts + w_out, mp);
   if (st) return st;
-  cudaError_t err = cudaSuccess;
-  if (!jobs.empty()) err = cudaMemcpyAsync(buf + off_jobs, jobs.data(), jobs.size() * sizeof(EvalJob), cudaMemcpyHostToDevice, s);
-  if (!err) err = cudaMemcpyAsync(buf + off_polyof, poly_of, (size_t)n_evals * 4, cudaMemcpyHostToDevice, s);
-  if (!err) err = cudaMemcpyAsync(buf + off_pts, points, (size_t)n_evals * sizeof(stwo_qm31_point), cudaMemcpyHostToDevice, s);
-  if (!err) err = cudaMemsetAsync(buf + off_acc, 0, (size_t)n_evals * 32, s);
+  std::memcpy(mp.host, jobs.data(), jobs.size() * sizeof(EvalJob));
+  std::memcpy(mp.host + w_jobs, poly_of, (size_t)n_evals * 4);
+  std::memcpy(mp.host + w_jobs + w_polyof, points, (size_t)n_evals * sizeof(stwo_qm31_point));
+  unsigned long long* acc = nullptr;
+  st = scratch_alloc((void**)&acc, (size_t)n_evals * 32, s);
+  if (st) return st;
+  cudaError_t err = cudaMemsetAsync(acc, 0, (size_t)n_evals * 32, s);
   if (!err) {
     dim3 grid(max_chunks, n_evals);
-    k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<EvalJob*>(buf + off_jobs),
-                                         reinterpret_cast<uint32_t*>(buf + off_polyof),
-                                         reinterpret_cast<stwo_qm31_point*>(buf + off_pts),
-                                         reinterpret_cast<unsigned long long*>(buf + off_acc)); note_launch();
+    k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<const EvalJob*>(mp.dev),
+                                         mp.dev + w_jobs,
+                                         reinterpret_cast<const stwo_qm31_point*>(mp.dev + w_jobs + w_polyof), acc);
+    note_launch();
     err = cudaGetLastError();
   }
   if (!err) {
-    k_reduce_acc<<<(n_evals * 4 + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned long long*>(buf + off_acc),
-                                                            n_evals * 4, reinterpret_cast<uint32_t*>(buf + off_out)); note_launch();
+    k_reduce_acc<<<(n_evals * 4 + 255) / 256, 256, 0, s>>>(acc, n_evals * 4, mp.dev + w_jobs + w_polyof + w_pts);
+    note_launch();
     err = cudaGetLastError();
   }
-  if (!err) err = cudaMemcpyAsync(out, buf + off_out, (size_t)n_evals * 16, cudaMemcpyDeviceToHost, s);
-  scratch_free(buf, s);
+  scratch_free(acc, s);
   if (!err) err = cudaStreamSynchronize(s);
   if (err) {
     set_error("eval_at_points: %s", cudaGetErrorString(err));
     return STWO_ERR_CUDA;
   }
+  std::memcpy(out, mp.host + w_jobs + w_polyof + w_pts, (size_t)n_evals * 16);
   return STWO_OK;
 }
 

@@ -117,12 +117,14 @@ hpoint h_index_to_point(uint32_t idx) {
 // lies at offset 2^R - 2^(R-k); it is the x-coordinate of the coset point with index
 // bitrev_{R-k-1}(pos - offset). The final entry is the padding value 1.
 __global__ void k_twiddle_tree(uint32_t init, uint32_t step, uint32_t R, uint32_t* tw, uint32_t* itw,
-                               uint32_t* zero_flag) {
+                               uint32_t* tw2, uint32_t* itw2, uint32_t* zero_flag) {
   uint32_t n = 1u << R;
   for (uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x; pos < n; pos += gridDim.x * blockDim.x) {
     if (pos == n - 1) {
       tw[pos] = 1u;
       itw[pos] = 1u;
+      tw2[pos] = 2u;
+      itw2[pos] = 2u;
       continue;
     }
     uint32_t q = n - 1 - pos;              // = 2^(R-k) - 1 - j, in [2^(R-k-1), 2^(R-k) - 1]
@@ -135,8 +137,11 @@ __global__ void k_twiddle_tree(uint32_t init, uint32_t step, uint32_t R, uint32_
     uint32_t idx = (uint32_t)(((uint64_t)ik + (uint64_t)sk * brev(j, lvl_log - 1)) & IDX_MASK);
     uint32_t x = index_to_point(idx).x;
     if (x == 0) atomicOr(zero_flag, 1u);  // "0 has no inverse" (fields/m31.rs:66)
+    const uint32_t ix = m31_inv(x);
     tw[pos] = x;
-    itw[pos] = m31_inv(x);
+    itw[pos] = ix;
+    tw2[pos] = 2u * x;
+    itw2[pos] = 2u * ix;
   }
 }
 
@@ -146,6 +151,8 @@ int32_t build_tree(stwo_coset root, cudaStream_t stream, TwiddleTree* t) {
   t->size = (size_t)1 << root.log_size;
   STWO_CHECK_CUDA(cudaMalloc(&t->d_tw, t->size * 4 + 4));
   STWO_CHECK_CUDA(cudaMalloc(&t->d_itw, t->size * 4));
+  STWO_CHECK_CUDA(cudaMalloc(&t->d_tw2, t->size * 8));
+  t->d_itw2 = t->d_tw2 + t->size;
   // One word past the twiddles flags an x-coordinate equal to 0: such a coset has no inverse
   // twiddles and is rejected, as the reference panics on it.
   uint32_t* flag = t->d_tw + t->size;
@@ -154,7 +161,8 @@ int32_t build_tree(stwo_coset root, cudaStream_t stream, TwiddleTree* t) {
   uint32_t blocks = (uint32_t)((t->size + threads - 1) / threads);
   if (blocks > 65535u) blocks = 65535u;
   k_twiddle_tree<<<blocks, threads, 0, stream>>>(root.initial_index, root.step_size, root.log_size, t->d_tw,
-                                                 t->d_itw, flag); note_launch();
+                                                 t->d_itw, t->d_tw2, t->d_itw2, flag);
+  note_launch();
   STWO_LAUNCH_CHECK();
   uint32_t h_flag = 0;
   STWO_CHECK_CUDA(cudaMemcpyAsync(&h_flag, flag, 4, cudaMemcpyDeviceToHost, stream));
@@ -162,6 +170,8 @@ int32_t build_tree(stwo_coset root, cudaStream_t stream, TwiddleTree* t) {
   if (h_flag) {
     cudaFree(t->d_tw);
     cudaFree(t->d_itw);
+    cudaFree(t->d_tw2);
+    t->d_tw2 = t->d_itw2 = nullptr;
     t->d_tw = t->d_itw = nullptr;
     set_error("coset has a point with x = 0: 0 has no inverse");
     return STWO_ERR_INVALID_ARG;
@@ -306,6 +316,7 @@ stwo_status stwo_twiddles_free(stwo_twiddle_tree tree) {
   if (!tree) return STWO_OK;
   cudaFree(tree->t.d_tw);
   cudaFree(tree->t.d_itw);
+  cudaFree(tree->t.d_tw2);
   delete tree;
   return STWO_OK;
 }
