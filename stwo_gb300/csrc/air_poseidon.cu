@@ -278,7 +278,7 @@ __device__ __forceinline__ uint32_t prev_row_index(uint32_t r, uint32_t trace_lo
 // Trace (1264) and interaction (32) columns are contiguous blocks with a stride of 2^eval_log
 // words, so a mask value is one load at base + (col << eval_log) + row. Each round's masks are
 // loaded before its arithmetic so that their latency hides behind the matrix and S-box work.
-__global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* __restrict__ trace,
+__global__ void __launch_bounds__(128, 8) k_poseidon_composition(const uint32_t* __restrict__ trace,
                                                               const uint32_t* __restrict__ inter, uint32_t n_rows,
                                                               PoseidonParams pp, const uint32_t* __restrict__ coeffs,
                                                               const uint32_t* __restrict__ dinv, uint32_t* o0,
@@ -310,6 +310,7 @@ __global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* __
   qm31 logup = qm31_zero();
   qm31 prev_col = qm31_zero();
   uint32_t rp = prev_row_index(r, pp.trace_log, pp.eval_log);
+#pragma unroll 1
   for (int rep = 0; rep < PS_REPS; rep++) {
     const uint32_t c0 = rep * PS_COLS_PER_REP;
     uint32_t s[PS_ST], init[PS_ST];
@@ -333,20 +334,20 @@ __global__ void __launch_bounds__(128) k_poseidon_composition(const uint32_t* __
         s[i] = m[i];
       }
     };
+    // The rounds stay loops: fully unrolled, the kernel outgrew the instruction cache and stalled
+    // on instruction fetch.
+#pragma unroll 1
     for (int round = 0; round < PS_HALF; round++) full_round();
-    {
-      uint32_t m[PS_PARTIAL];
-#pragma unroll
-      for (int i = 0; i < PS_PARTIAL; i++) m[i] = col(trace, mc + i, r);
-      mc += PS_PARTIAL;
-#pragma unroll
-      for (int round = 0; round < PS_PARTIAL; round++) {
-        s[0] = m31_add(s[0], PS_RC);
-        internal_matrix(s);
-        acc(m31_sub(pow5(s[0]), m[round]));
-        s[0] = m[round];
-      }
+#pragma unroll 1
+    for (int round = 0; round < PS_PARTIAL; round++) {
+      const uint32_t m = col(trace, mc + round, r);
+      s[0] = m31_add(s[0], PS_RC);
+      internal_matrix(s);
+      acc(m31_sub(pow5(s[0]), m));
+      s[0] = m;
     }
+    mc += PS_PARTIAL;
+#pragma unroll 1
     for (int round = 0; round < PS_HALF; round++) full_round();
     // LogUp batch `rep`: fraction (1/d0 - 1/d1) = (d1 - d0) / (d0 d1).
     qm31 d0 = combine16(pp.lc, init), d1 = combine16(pp.lc, s);

@@ -163,13 +163,13 @@ __device__ __forceinline__ void publish_flag(uint32_t* flag, uint32_t seq) {
   *reinterpret_cast<volatile uint32_t*>(flag) = seq;
 }
 
-// (f(0), f(2)) of sum_x eq((0, x), y) P(t, x) over the current layer (cpu/lookups/gkr.rs:38-212).
+// Terms i = first, first + stride, ... of one round (cpu/lookups/gkr.rs:38-212), accumulated into
+// (e0, e2): with FIX the previous challenge is folded in on the fly (see gate()).
 template <uint32_t KIND, bool FIX>
-__global__ void __launch_bounds__(256) k_gkr_round(Cols src, ColsM dst, qm31 c, uint32_t cur, Sec eq, qm31 lambda,
-                                                   RoundOut ro) {
+__device__ __forceinline__ void round_terms(const Cols& src, const ColsM& dst, qm31 c, uint32_t cur, const Sec& eq,
+                                            qm31 lambda, uint32_t first, uint32_t stride, qm31& e0, qm31& e2) {
   const uint32_t nt = cur / 4;
-  qm31 e0 = qm31_zero(), e2 = qm31_zero();
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+  for (uint32_t i = first; i < nt; i += stride) {
     qm31 n00, n01, n10, n11, d00, d01, d10, d11;
     gate<KIND, FIX>(src, dst, c, cur, 2 * (size_t)i, n00, d00);
     gate<KIND, FIX>(src, dst, c, cur, 2 * (size_t)i + 1, n01, d01);
@@ -195,7 +195,11 @@ __global__ void __launch_bounds__(256) k_gkr_round(Cols src, ColsM dst, qm31 c, 
     e0 = qm31_add(e0, qm31_mul(w, qm31_add(num0, qm31_mul(lambda, qm31_mul(d00, d01)))));
     e2 = qm31_add(e2, qm31_mul(w, qm31_add(num2, qm31_mul(lambda, qm31_mul(d20, d21)))));
   }
-  // Block reduction, then the last block to arrive reduces the per-block partials.
+}
+
+// Block reduction of (e0, e2), then the last block to arrive reduces the per-block partials into
+// ro.result (and publishes ro.flag).
+__device__ __forceinline__ void block_reduce_and_finish(qm31 e0, qm31 e2, const RoundOut& ro) {
   __shared__ qm31 s0[8], s2[8];
   __shared__ bool last;
   for (int off = 16; off; off >>= 1) {
@@ -253,6 +257,17 @@ __global__ void __launch_bounds__(256) k_gkr_round(Cols src, ColsM dst, qm31 c, 
   }
 }
 
+// (f(0), f(2)) of sum_x eq((0, x), y) P(t, x) over the current layer (cpu/lookups/gkr.rs:38-212).
+template <uint32_t KIND, bool FIX>
+__global__ void __launch_bounds__(256) k_gkr_round(Cols src, ColsM dst, qm31 c, uint32_t cur, Sec eq, qm31 lambda,
+                                                   RoundOut ro) {
+  qm31 e0 = qm31_zero(), e2 = qm31_zero();
+  round_terms<KIND, FIX>(src, dst, c, cur, eq, lambda, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x,
+                         e0, e2);
+  block_reduce_and_finish(e0, e2, ro);
+}
+
+
 // The gates at positions 0..cur-1 (cur <= 2) into `out`: numerators at words 4j, denominators at
 // 8 + 4j. Used for output layer values and for the masks of constant oracles.
 template <uint32_t KIND, bool FIX>
@@ -268,6 +283,153 @@ __global__ void k_gkr_gates(Cols src, ColsM dst, qm31 c, uint32_t cur, uint32_t*
   }
   __syncthreads();
   if (j == 0 && flag) publish_flag(flag, seq);
+}
+
+// ------------------------------------------------------------------------------ small-layer tail
+// The last rounds of a GKR layer, once every layer left has at most TAIL_MAX_GATES gates, run in
+// one single-block kernel that stays resident and trades each round with the host through mapped
+// memory: it publishes the round's sums, waits for the challenge the host draws (the transcript
+// stays on the host, as in the reference), folds it in and goes on. A round then costs two
+// mapped-memory hand-offs instead of a kernel launch plus a host wait. The wait is bounded: with
+// no challenge after about two seconds the kernel records an error and returns.
+constexpr uint32_t TAIL_MAXI = 8;
+constexpr uint32_t TAIL_MAX_GATES = 4096;
+constexpr uint32_t TAIL_THREADS = 512;
+constexpr long long TAIL_WAIT_CYCLES = 4000000000ll;
+constexpr uint32_t TAIL_ABORT = 0xFFFFFFFFu;
+
+struct TailInst {
+  uint32_t kind, vars, cur, pending;
+  Cols src;
+  ColsM work;
+  uint32_t* out;  // mapped: 24 words (round sums, then mask gates)
+};
+struct TailParams {
+  uint32_t n_inst, sc_vars, r0;
+  TailInst inst[TAIL_MAXI];
+  Sec eq;
+  qm31 lambda, chal0;
+  uint32_t* to_host;          // mapped: [seq, error]
+  const uint32_t* from_host;  // mapped: [seq, challenge (4 words)]
+  uint32_t seq0;
+};
+
+template <uint32_t KIND>
+__device__ void tail_sums(const TailInst& t, qm31 c, const Sec& eq, qm31 lambda, uint32_t* out) {
+  __shared__ qm31 r0[TAIL_THREADS / 32], r2[TAIL_THREADS / 32];
+  qm31 e0 = qm31_zero(), e2 = qm31_zero();
+  if (t.pending) round_terms<KIND, true>(t.src, t.work, c, t.cur, eq, lambda, threadIdx.x, blockDim.x, e0, e2);
+  else round_terms<KIND, false>(t.src, t.work, c, t.cur, eq, lambda, threadIdx.x, blockDim.x, e0, e2);
+  for (int off = 16; off; off >>= 1) {
+    e0 = qm31_add(e0, shfl_q(e0, off));
+    e2 = qm31_add(e2, shfl_q(e2, off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r0[threadIdx.x >> 5] = e0;
+    r2[threadIdx.x >> 5] = e2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    qm31 a = r0[0], b = r2[0];
+    for (uint32_t w = 1; w < blockDim.x / 32; w++) {
+      a = qm31_add(a, r0[w]);
+      b = qm31_add(b, r2[w]);
+    }
+    out[0] = a.a.a; out[1] = a.a.b; out[2] = a.b.a; out[3] = a.b.b;
+    out[4] = b.a.a; out[5] = b.a.b; out[6] = b.b.a; out[7] = b.b.b;
+  }
+  __syncthreads();
+}
+
+template <uint32_t KIND>
+__device__ void tail_gates(const TailInst& t, qm31 c, uint32_t* out) {
+  const uint32_t j = threadIdx.x;
+  if (j < 2) {
+    qm31 n, d = qm31_zero();
+    if (t.pending) gate<KIND, true>(t.src, t.work, c, 2, j, n, d);
+    else gate<KIND, false>(t.src, t.work, c, 2, j, n, d);
+    uint32_t* o = out + 4 * j;
+    o[0] = n.a.a; o[1] = n.a.b; o[2] = n.b.a; o[3] = n.b.b;
+    o[8] = d.a.a; o[9] = d.a.b; o[10] = d.b.a; o[11] = d.b.b;
+  }
+}
+
+__global__ void __launch_bounds__(TAIL_THREADS) k_gkr_tail(TailParams p) {
+  __shared__ TailInst st[TAIL_MAXI];
+  __shared__ qm31 s_chal;
+  __shared__ uint32_t s_abort;
+  if (threadIdx.x < p.n_inst) st[threadIdx.x] = p.inst[threadIdx.x];
+  if (threadIdx.x == 0) {
+    s_chal = p.chal0;
+    s_abort = 0;
+  }
+  __syncthreads();
+  uint32_t seq = p.seq0;
+  for (uint32_t r = p.r0; r < p.sc_vars; r++) {
+    const uint32_t rem = p.sc_vars - r;
+    const qm31 c = s_chal;
+    for (uint32_t i = 0; i < p.n_inst; i++) {
+      if (st[i].vars != rem) continue;
+      switch (st[i].kind) {
+        case K_GP: tail_sums<K_GP>(st[i], c, p.eq, p.lambda, st[i].out); break;
+        case K_GENERIC: tail_sums<K_GENERIC>(st[i], c, p.eq, p.lambda, st[i].out); break;
+        case K_MULT: tail_sums<K_MULT>(st[i], c, p.eq, p.lambda, st[i].out); break;
+        default: tail_sums<K_SINGLES>(st[i], c, p.eq, p.lambda, st[i].out); break;
+      }
+    }
+    if (threadIdx.x == 0) {
+      // The live layers now hold their folded values in `work`; their first variable is next.
+      for (uint32_t i = 0; i < p.n_inst; i++) {
+        if (st[i].vars != rem) continue;
+        if (st[i].pending) {
+          for (int k = 0; k < 4; k++) {
+            st[i].src.num.c[k] = st[i].work.num.c[k];
+            st[i].src.den.c[k] = st[i].work.den.c[k];
+          }
+          if (st[i].kind == K_MULT) st[i].kind = K_GENERIC;
+        }
+        st[i].pending = 1;
+        st[i].cur >>= 1;
+        st[i].vars--;
+      }
+      ++seq;
+      publish_flag(p.to_host, seq);
+      const volatile uint32_t* fh = p.from_host;
+      const long long t0 = clock64();
+      bool ok = false;
+      while (clock64() - t0 < TAIL_WAIT_CYCLES) {
+        const uint32_t v = fh[0];
+        if (v == seq) {
+          ok = true;
+          break;
+        }
+        if (v == TAIL_ABORT) break;  // the host gave up on this proof
+        __nanosleep(128);
+      }
+      if (ok) {
+        __threadfence_system();
+        s_chal = qm31_from_u32(fh[1], fh[2], fh[3], fh[4]);
+      } else {
+        s_abort = 1;
+        reinterpret_cast<volatile uint32_t*>(p.to_host)[1] = 1u;
+      }
+    }
+    __syncthreads();
+    if (s_abort) return;
+  }
+  // Masks of the constant oracles, folded with the last challenge.
+  const qm31 c = s_chal;
+  for (uint32_t i = 0; i < p.n_inst; i++) {
+    switch (st[i].kind) {
+      case K_GP: tail_gates<K_GP>(st[i], c, st[i].out); break;
+      case K_GENERIC: tail_gates<K_GENERIC>(st[i], c, st[i].out); break;
+      case K_MULT: tail_gates<K_MULT>(st[i], c, st[i].out); break;
+      default: tail_gates<K_SINGLES>(st[i], c, st[i].out); break;
+    }
+  }
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0) publish_flag(p.to_host, seq + 1);
 }
 
 // ------------------------------------------------------------------------------ MleOps
@@ -552,12 +714,15 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
   STWO_CHECK_CUDA(cudaMemsetAsync(ro.ticket, 0, 4, s));
 
   Mapped mp;
-  st = mapped_words((size_t)n_inst * 24 + 1, mp);
+  st = mapped_words((size_t)n_inst * 24 + 8, mp);
   if (st) return st;
-  // Completion flag of the round and mask kernels, polled by the host (wait_flag).
+  // Completion flag (and error word) of the round and mask kernels, polled by the host
+  // (wait_flag), and the host-to-device challenge mailbox of the tail kernel.
   uint32_t* const flag_dev = mp.dev + (size_t)n_inst * 24;
   const uint32_t* const flag_host = mp.host + (size_t)n_inst * 24;
-  mp.host[(size_t)n_inst * 24] = 0;
+  uint32_t* const mailbox_host = mp.host + (size_t)n_inst * 24 + 2;
+  const uint32_t* const mailbox_dev = mp.dev + (size_t)n_inst * 24 + 2;
+  for (int k = 0; k < 8; k++) mp.host[(size_t)n_inst * 24 + k] = 0;
   uint32_t seq = 0;
 
   // Circuit layers (gen_layers, gkr_prover.rs:508-516): layers[n] is the caller's input.
@@ -651,14 +816,58 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
       I.claim = hq_mul(I.claim, hq_make((uint32_t)((1ull << (sc_vars - I.oracle_vars)) % P), 0, 0, 0));
     }
     std::vector<hq> assignment;
+    bool tail_on = false;
+    // On a failure while the tail kernel waits for a challenge, release it and let it end.
+    auto abort_tail = [&](int32_t code) {
+      if (tail_on) {
+        *reinterpret_cast<volatile uint32_t*>(mailbox_host) = TAIL_ABORT;
+        cudaStreamSynchronize(s);
+      }
+      return code;
+    };
     for (uint32_t r = 0; r < sc_vars; r++) {
       const uint32_t rem = sc_vars - r;
       size_t last_live = act.size();
       for (size_t a = 0; a < act.size(); a++)
         if (inst[act[a]].oracle_vars == rem) last_live = a;
       const bool any = last_live < act.size();
+      if (!tail_on && act.size() <= TAIL_MAXI && sc_vars - r >= 2) {
+        uint32_t biggest = 0;
+        for (uint32_t i : act) biggest = std::max(biggest, inst[i].cur);
+        if (biggest <= TAIL_MAX_GATES) {
+          // The remaining rounds and the masks of this layer run in the resident tail kernel.
+          TailParams tp{};
+          tp.n_inst = (uint32_t)act.size();
+          tp.sc_vars = sc_vars;
+          tp.r0 = r;
+          for (size_t a = 0; a < act.size(); a++) {
+            const Instance& I = inst[act[a]];
+            tp.inst[a] = TailInst{I.kind, I.oracle_vars, I.cur, I.fix_pending ? 1u : 0u, I.src,
+                                  ColsM{I.work_num, I.work_den}, mp.dev + 24 * act[a]};
+            if (I.fix_pending) tp.chal0 = to_q(I.pending);
+          }
+          tp.eq = as_const(eq);
+          tp.lambda = to_q(lambda);
+          tp.to_host = flag_dev;
+          tp.from_host = mailbox_dev;
+          tp.seq0 = seq;
+          mailbox_host[0] = 0;
+          std::atomic_thread_fence(std::memory_order_release);
+          k_gkr_tail<<<1, TAIL_THREADS, 0, s>>>(tp);
+          note_launch();
+          STWO_LAUNCH_CHECK();
+          tail_on = true;
+        }
+      }
       if (any) seq++;
-      for (size_t a = 0; a < act.size(); a++) {
+      for (size_t a = 0; a < act.size() && tail_on; a++) {
+        // Mirror of the tail kernel's bookkeeping: a live pending layer is folded this round.
+        Instance& I = inst[act[a]];
+        if (I.oracle_vars != rem || !I.fix_pending) continue;
+        if (I.kind == K_MULT) I.kind = K_GENERIC;
+        I.fix_pending = false;
+      }
+      for (size_t a = 0; a < act.size() && !tail_on; a++) {
         Instance& I = inst[act[a]];
         if (I.oracle_vars != rem) continue;
         RoundOut o = ro;
@@ -680,7 +889,7 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
       if (any) {
         STWO_LAUNCH_CHECK();
         st = wait_flag(flag_host, seq, s);
-        if (st) return st;
+        if (st) return abort_tail(st);
       }
       std::vector<HPoly> polys;
       for (size_t a = 0; a < act.size(); a++) {
@@ -690,13 +899,13 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
           const uint32_t* w = mp.host + 24 * act[a];
           hq f0 = hq_mul(hq_of_words(w), I.correction), f2 = hq_mul(hq_of_words(w + 4), I.correction);
           st = correct_sum(f0, f2, I.claim, y, I.oracle_vars, p);
-          if (st) return st;
+          if (st) return abort_tail(st);
         } else {
           p = hp_new({hq_mul(I.claim, half_inv)});
         }
         if (!hq_eq(hq_add(hp_eval(p, HQ_ZERO), hp_eval(p, HQ_ONE)), I.claim) || p.size() > 4) {
           set_error("prove_batch: round polynomial inconsistent with its claim (instance %u, round %u)", act[a], r);
-          return STWO_ERR_CUDA;
+          return abort_tail(STWO_ERR_CUDA);
         }
         polys.push_back(std::move(p));
       }
@@ -704,6 +913,11 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
       for (size_t k = polys.size(); k-- > 0;) comb = hp_add(hp_scale(comb, alpha), polys[k]);
       ch.mix_felts(comb);
       const hq chal = ch.draw_felt();
+      if (tail_on) {
+        for (int k = 0; k < 4; k++) mailbox_host[1 + k] = chal.v[k];
+        std::atomic_thread_fence(std::memory_order_release);
+        *reinterpret_cast<volatile uint32_t*>(mailbox_host) = seq;
+      }
       for (size_t a = 0; a < act.size(); a++) {
         Instance& I = inst[act[a]];
         I.claim = hp_eval(polys[a], chal);
@@ -722,7 +936,11 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
     rounds_per_layer.push_back(sc_vars);
     // Masks of the now constant oracles (gkr_prover.rs:320-346).
     seq++;
-    for (size_t a = 0; a < act.size(); a++) {
+    for (size_t a = 0; a < act.size() && tail_on; a++) {
+      Instance& I = inst[act[a]];
+      if (I.fix_pending && I.kind == K_MULT) I.kind = K_GENERIC;
+    }
+    for (size_t a = 0; a < act.size() && !tail_on; a++) {
       Instance& I = inst[act[a]];
       ColsM dst{I.work_num, I.work_den};
       uint32_t* f = a + 1 == act.size() ? flag_dev : nullptr;
@@ -732,7 +950,7 @@ int32_t prove_batch(uint32_t n_inst, const uint32_t* kinds, const uint32_t* logs
     }
     STWO_LAUNCH_CHECK();
     st = wait_flag(flag_host, seq, s);
-    if (st) return st;
+    if (st) return abort_tail(st);
     for (size_t a = 0; a < act.size(); a++) {
       Instance& I = inst[act[a]];
       const uint32_t* w = mp.host + 24 * act[a];
