@@ -180,10 +180,13 @@ __device__ __forceinline__ uint32_t coset_to_storage(uint32_t k, uint32_t log_n)
 }
 
 // tmp[k] = col[storage(k)] - shift  (four coordinate columns, blockIdx.y)
-__global__ void k_coset_gather(uint32_t* cols, uint32_t log_n, uint4 shift, uint32_t* tmp) {
+// `sums` holds the column's claimed sum as 64-bit coordinate sums (k_column_sums); the shift
+// claimed_sum / 2^log_n is taken on the device, so the host needs no read-back here.
+__global__ void k_coset_gather(uint32_t* cols, uint32_t log_n, const unsigned long long* sums, uint32_t inv_n,
+                               uint32_t* tmp) {
   uint32_t k = blockIdx.y;
   uint32_t n = 1u << log_n;
-  uint32_t sh = k == 0 ? shift.x : k == 1 ? shift.y : k == 2 ? shift.z : shift.w;
+  const uint32_t sh = m31_mul(fold64_p(sums[k]), inv_n);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     tmp[(size_t)k * n + i] = m31_sub(cols[(size_t)k * n + coset_to_storage(i, log_n)], sh);
 }
@@ -377,6 +380,16 @@ __global__ void __launch_bounds__(128, 8) k_poseidon_composition(const uint32_t*
 }
 
 // ------------------------------------------------------------------------------------ host side
+// Pinned landing words for the claimed-sum read-back (one per host thread).
+static unsigned long long* claimed_pinned() {
+  thread_local unsigned long long* p = [] {
+    void* q = nullptr;
+    if (cudaHostAlloc(&q, 64, cudaHostAllocDefault) != cudaSuccess) q = nullptr;
+    return static_cast<unsigned long long*>(q);
+  }();
+  return p;
+}
+
 static hq hq_m(hq x, uint32_t m) {
   for (int i = 0; i < 4; i++) x.v[i] = h_mul(x.v[i], m);
   return x;
@@ -587,22 +600,19 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
       unsigned long long* d_sums = reinterpret_cast<unsigned long long*>(pv.arena.alloc(8));
       uint32_t* tmp = pv.arena.alloc(4 * n);
       if (!d_sums || !tmp) st = STWO_ERR_OOM;
-      unsigned long long h_sums[4] = {0, 0, 0, 0};
       if (!st && cudaMemsetAsync(d_sums, 0, 32, s) != cudaSuccess) st = STWO_ERR_CUDA;
       if (!st) {
         k_column_sums<<<dim3(std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024), 4), 256, 0, s>>>(last, (uint32_t)n, d_sums);
         note_launch();
-        if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(h_sums, d_sums, 32, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-            cudaStreamSynchronize(s) != cudaSuccess)
+        // The sums reach the host with the next synchronisation (the interaction commitment's).
+        if (!claimed_pinned()) st = STWO_ERR_OOM;
+        else if (cudaGetLastError() != cudaSuccess ||
+                 cudaMemcpyAsync(claimed_pinned(), d_sums, 32, cudaMemcpyDeviceToHost, s) != cudaSuccess)
           st = STWO_ERR_CUDA;
       }
       if (!st) {
-        claimed = hq_make((uint32_t)(h_sums[0] % P), (uint32_t)(h_sums[1] % P), (uint32_t)(h_sums[2] % P),
-                          (uint32_t)(h_sums[3] % P));
-        hq sh = hq_m(claimed, h_inv((uint32_t)(n % P)));
-        uint4 shv = make_uint4(sh.v[0], sh.v[1], sh.v[2], sh.v[3]);
         uint32_t g = std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024);
-        k_coset_gather<<<dim3(g, 4), 256, 0, s>>>(last, log_n_rows, shv, tmp);
+        k_coset_gather<<<dim3(g, 4), 256, 0, s>>>(last, log_n_rows, d_sums, h_inv((uint32_t)(n % P)), tmp);
         note_launch();
         st = cudaGetLastError() ? STWO_ERR_CUDA : STWO_OK;
         if (!st) st = scan_rows(tmp, (uint32_t)n, 4, pv.arena, s);
@@ -617,6 +627,11 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
       std::vector<uint32_t*> cols(PS_INTERACTION_COLS);
       for (int c = 0; c < PS_INTERACTION_COLS; c++) cols[c] = inter + (size_t)c * n;
       st = pv.commit_evals(cols, log_n_rows);
+    }
+    if (!st) {
+      STWO_CHECK_CUDA(cudaStreamSynchronize(s));  // already idle: the commitment read its root
+      const unsigned long long* hs = claimed_pinned();
+      claimed = hq_make((uint32_t)(hs[0] % P), (uint32_t)(hs[1] % P), (uint32_t)(hs[2] % P), (uint32_t)(hs[3] % P));
     }
     if (!st) {
       PoseidonGpuAir air(log_n_rows, le, claimed);

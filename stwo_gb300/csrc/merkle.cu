@@ -7,6 +7,7 @@
 // compression, so a leaf costs ceil(k/16) compressions on the INT pipes.
 #include "common.cuh"
 #include "blake2s.cuh"
+#include "dchannel.cuh"
 
 namespace stwo {
 
@@ -126,8 +127,11 @@ __device__ __forceinline__ void hash_children(const uint32_t* l, const uint32_t*
   b2s_compress(h, m, 64, true);
 }
 
+// With `ch` set (on the launch that produces the root), thread 0 then runs one FRI transcript
+// step on the device channel: mix the root, draw the folding alpha into alpha_out (alpha, alpha^2).
 __global__ void __launch_bounds__(256) k_merkle_subtrees(const uint32_t* __restrict__ prev, uint32_t first_log,
-                                                         uint32_t levels, LayerPtrs outs) {
+                                                         uint32_t levels, LayerPtrs outs, DevChannel* ch,
+                                                         uint32_t* alpha_out) {
   __shared__ uint32_t sm[256 * 8];
   const uint32_t t = threadIdx.x;
   const uint32_t node = blockIdx.x * blockDim.x + t;  // node of layer first_log
@@ -169,12 +173,20 @@ __global__ void __launch_bounds__(256) k_merkle_subtrees(const uint32_t* __restr
     }
     __syncthreads();
   }
+  if (ch && t == 0) {
+    // This block's last level is the one-node root layer, written above by this thread.
+    d_ch_mix_root(ch, outs.p[levels - 1]);
+    const qm31 a = d_ch_draw_felt(ch);
+    const qm31 a2 = qm31_mul(a, a);
+    alpha_out[0] = a.a.a; alpha_out[1] = a.a.b; alpha_out[2] = a.b.a; alpha_out[3] = a.b.b;
+    alpha_out[4] = a2.a.a; alpha_out[5] = a2.a.b; alpha_out[6] = a2.b.a; alpha_out[7] = a2.b.b;
+  }
 }
 
 // Hashes the pure node layers first_log, first_log - 1, ..., first_log - n_levels + 1 from `prev`
 // (layer first_log + 1). out[i] receives layer first_log - i.
 int32_t merkle_node_layers(const uint32_t* prev, uint32_t first_log, uint32_t n_levels, uint32_t* const* out,
-                           cudaStream_t s) {
+                           cudaStream_t s, DevChannel* ch, uint32_t* alpha_out) {
   uint32_t done = 0;
   while (done < n_levels) {
     uint32_t lg = first_log - done;
@@ -184,7 +196,10 @@ int32_t merkle_node_layers(const uint32_t* prev, uint32_t first_log, uint32_t n_
     for (uint32_t i = 0; i < lv; i++) lp.p[i] = out[done + i];
     uint32_t threads = 1u << block_log;
     uint32_t blocks = 1u << (lg - block_log);
-    k_merkle_subtrees<<<blocks, threads, 0, s>>>(prev, lg, lv, lp);
+    // The channel step rides on the launch that ends at the root (one block, last level 0).
+    const bool root_launch = blocks == 1 && lg + 1 == lv;
+    k_merkle_subtrees<<<blocks, threads, 0, s>>>(prev, lg, lv, lp, root_launch ? ch : nullptr,
+                                                 root_launch ? alpha_out : nullptr);
     note_launch();
     STWO_LAUNCH_CHECK();
     prev = out[done + lv - 1];

@@ -26,7 +26,7 @@ int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* c
 int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols, uint32_t n_cols,
                             uint32_t* out, cudaStream_t s);
 int32_t merkle_node_layers(const uint32_t* prev, uint32_t first_log, uint32_t n_levels, uint32_t* const* out,
-                           cudaStream_t s);
+                           cudaStream_t s, DevChannel* ch = nullptr, uint32_t* alpha_out = nullptr);
 int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, stwo_qm31 rc_in,
                              const stwo_sample_batch* batches, uint32_t n_batches, uint32_t log_blowup,
                              uint32_t* const out[4], cudaStream_t s);
@@ -119,7 +119,9 @@ static uint32_t ilog2u(size_t n) {
   return l;
 }
 
-int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root) {
+int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root,
+                          DevChannel* ch, uint32_t* alpha_out) {
+  channel_fused = false;
   sorted = columns;
   std::stable_sort(sorted.begin(), sorted.end(), [](const ColRef& a, const ColRef& b) { return a.log > b.log; });
   uint32_t max_log = sorted.empty() ? 0 : sorted[0].log;
@@ -145,8 +147,11 @@ int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cuda
     while (stop - 1 >= 0 && !(ci < sorted.size() && sorted[ci].log == (uint32_t)(stop - 1))) stop--;
     std::vector<uint32_t*> outs;
     for (int l = lg; l >= stop; l--) outs.push_back(layers[l]);
-    int32_t st = merkle_node_layers(prev, (uint32_t)lg, (uint32_t)outs.size(), outs.data(), s);
+    // The run that ends at the root can carry the FRI transcript step in its last launch.
+    DevChannel* c = stop == 0 ? ch : nullptr;
+    int32_t st = merkle_node_layers(prev, (uint32_t)lg, (uint32_t)outs.size(), outs.data(), s, c, alpha_out);
     if (st) return st;
+    if (c) channel_fused = true;
     lg = stop - 1;
   }
   if (!read_root) return STWO_OK;
@@ -457,15 +462,20 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   auto mask = air.mask_offsets();
   std::vector<std::vector<std::vector<HPointQ>>> pts(trees.size());
   uint32_t step = 1u << (31 - air.log_size());
+  // Columns share a handful of offsets: each shifted point is computed once.
+  std::map<int, HPointQ> shifted;
+  auto point_at = [&](int off) -> const HPointQ& {
+    auto it = shifted.find(off);
+    if (it != shifted.end()) return it->second;
+    uint32_t idx = idx_reduce((uint64_t)step * (uint64_t)(off >= 0 ? off : -off));
+    if (off < 0) idx = idx_reduce((1ull << 31) - idx);
+    return shifted.emplace(off, hpq_add_m31(oods, h_index_to_point(idx))).first->second;
+  };
   for (size_t t = 0; t + 1 < trees.size(); t++) {
     pts[t].resize(trees[t].polys.size());
     if (t == 0 || t >= mask.size()) continue;
     for (size_t c = 0; c < mask[t].size(); c++)
-      for (int off : mask[t][c]) {
-        uint32_t idx = idx_reduce((uint64_t)step * (uint64_t)(off >= 0 ? off : -off));
-        if (off < 0) idx = idx_reduce((1ull << 31) - idx);
-        pts[t][c].push_back(hpq_add_m31(oods, h_index_to_point(idx)));
-      }
+      for (int off : mask[t][c]) pts[t][c].push_back(point_at(off));
   }
   pts.back().assign(4, {oods});
 
@@ -604,10 +614,10 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     if (st) return st;
   }
   DevMerkle first_tree;
-  st = first_tree.commit(first_cols, arena, s, false);
-  if (st) return st;
   size_t fstep = 0;
-  st = fri_channel_step(dch, first_tree.layers[0], alphas + 8 * fstep, s);
+  st = first_tree.commit(first_cols, arena, s, false, dch, alphas + 8 * fstep);
+  if (st) return st;
+  if (!first_tree.channel_fused) st = fri_channel_step(dch, first_tree.layers[0], alphas + 8 * fstep, s);
   if (st) return st;
   struct Layer { SecureCols eval; stwo_coset dom; DevMerkle merkle; };
   std::vector<Layer> layers;
@@ -631,10 +641,10 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     L.dom = dom;
     std::vector<ColRef> lc;
     for (int k = 0; k < 4; k++) lc.push_back({cur.c[k], dom.log_size});
-    st = L.merkle.commit(lc, arena, s, false);
-    if (st) return st;
     STWO_REQUIRE(++fstep < FRI_MAX_STEPS, "too many FRI layers");
-    st = fri_channel_step(dch, L.merkle.layers[0], alphas + 8 * fstep, s);
+    st = L.merkle.commit(lc, arena, s, false, dch, alphas + 8 * fstep);
+    if (st) return st;
+    if (!L.merkle.channel_fused) st = fri_channel_step(dch, L.merkle.layers[0], alphas + 8 * fstep, s);
     if (st) return st;
     SecureCols nxt;
     for (int k = 0; k < 4; k++) {

@@ -5,6 +5,7 @@
 #include <vector>
 #include "common.cuh"
 #include "host_channel.h"
+#include "dchannel.cuh"
 
 namespace stwo {
 
@@ -51,8 +52,12 @@ struct DevMerkle {
   std::vector<uint32_t*> layers;  // layers[l]: 2^l hashes of 8 words
   std::vector<ColRef> sorted;     // columns, stable-sorted by descending log size
   Digest root;
-  // With read_root false the root stays on the device (layers[0]) and `root` is left unset.
-  int32_t commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root = true);
+  // With read_root false the root stays on the device (layers[0]) and `root` is left unset. With
+  // `ch` set, the launch that writes the root also mixes it into that device channel and draws
+  // the next alpha into alpha_out, when the root comes from a node-only run (channel_fused).
+  int32_t commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root = true,
+                 DevChannel* ch = nullptr, uint32_t* alpha_out = nullptr);
+  bool channel_fused = false;
   void decommit(const std::map<uint32_t, std::vector<size_t>>& queries, Gather& g, DecommitRecipe& out) const;
 };
 

@@ -239,20 +239,44 @@ stwo_status stwo_set_stage_timing(int enable) {
 }
 
 uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap) {
-  std::vector<std::pair<const char*, float>> agg;
-  for (auto& r : g_stages) {
+  // Stage durations (summed by name), then the stream time between consecutive stages, summed as
+  // "gap before <stage>": device idle or unlabelled work while the host prepared the next stage.
+  thread_local std::vector<std::string> gap_names;
+  gap_names.clear();
+  gap_names.reserve(g_stages.size());
+  std::vector<std::pair<const char*, float>> agg, gaps;
+  auto add = [](std::vector<std::pair<const char*, float>>& v, const char* name, float t) {
+    for (auto& a : v)
+      if (strcmp(a.first, name) == 0) {
+        a.second += t;
+        return;
+      }
+    v.push_back({name, t});
+  };
+  for (size_t i = 0; i < g_stages.size(); i++) {
+    const StageRec& r = g_stages[i];
     float t = 0;
     if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&t, r.a, r.b) != cudaSuccess) t = -1;
-    bool found = false;
-    for (auto& a : agg)
-      if (strcmp(a.first, r.name) == 0) {
-        a.second += t;
-        found = true;
+    add(agg, r.name, t);
+    if (i > 0) {
+      float g = 0;
+      if (cudaEventElapsedTime(&g, g_stages[i - 1].b, r.a) != cudaSuccess) g = -1;
+      std::string gn = std::string("gap before ") + r.name;
+      const char* key = nullptr;
+      for (auto& n : gap_names)
+        if (n == gn) key = n.c_str();
+      if (!key) {
+        gap_names.push_back(gn);
+        key = gap_names.back().c_str();
       }
-    if (!found) agg.push_back({r.name, t});
+      add(gaps, key, g);
+    }
+  }
+  for (auto& r : g_stages) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
   }
+  for (auto& g : gaps) agg.push_back(g);
   g_stages.clear();
   g_stage_open = -1;
   uint32_t n = 0;
