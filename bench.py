@@ -606,17 +606,15 @@ def run_gb300(args):
     _lib.call("stwo_device_init", local)
     lib = _lib.load()
 
+    from stwo_gb300 import replicas
+
+    ranks = replicas.Ranks(world, rank, local)
+
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
+        replicas.barrier(ranks)
 
     def max_over_ranks(v):
-        if world > 1:
-            t = torch.tensor([v], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return v
+        return replicas.max_over_ranks(v, ranks)
 
     if args.workload == "kernels":
         return run_kernels(args, world, rank, local, lib, barrier, max_over_ranks)
