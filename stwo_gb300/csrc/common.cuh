@@ -104,14 +104,30 @@ inline void h_cmul(uint32_t x0, uint32_t x1, uint32_t y0, uint32_t y1, uint32_t*
   *r0 = a;
   *r1 = b;
 }
+// (a + bu)(c + du) = ac + (2+i) bd + (ad + bc) u over CM31, with a = x0 + x1 i, b = x2 + x3 i,
+// c = y0 + y1 i, d = y2 + y3 i. Each product is folded once to below 2^32; the signed
+// combinations are offset by a multiple of P and reduced once per coordinate.
+inline uint64_t h_fold(uint64_t p) { return (p & P) + (p >> 31); }  // < 2^32, congruent mod P
+inline uint32_t h_reduce64(uint64_t x) {
+  x = (x & P) + (x >> 31);
+  x = (x & P) + (x >> 31);
+  uint32_t r = (uint32_t)x;
+  return r >= P ? r - P : r;
+}
 inline hq hq_mul(hq x, hq y) {
-  uint32_t ac0, ac1, bd0, bd1, ad0, ad1, bc0, bc1;
-  h_cmul(x.v[0], x.v[1], y.v[0], y.v[1], &ac0, &ac1);
-  h_cmul(x.v[2], x.v[3], y.v[2], y.v[3], &bd0, &bd1);
-  h_cmul(x.v[0], x.v[1], y.v[2], y.v[3], &ad0, &ad1);
-  h_cmul(x.v[2], x.v[3], y.v[0], y.v[1], &bc0, &bc1);
-  uint32_t rb0 = h_sub(h_add(bd0, bd0), bd1), rb1 = h_add(bd0, h_add(bd1, bd1));  // (2+i) bd
-  return hq{{h_add(ac0, rb0), h_add(ac1, rb1), h_add(ad0, bc0), h_add(ad1, bc1)}};
+  const uint64_t a0 = x.v[0], a1 = x.v[1], b0 = x.v[2], b1 = x.v[3];
+  const uint64_t c0 = y.v[0], c1 = y.v[1], d0 = y.v[2], d1 = y.v[3];
+  const uint64_t a0c0 = h_fold(a0 * c0), a1c1 = h_fold(a1 * c1), a0c1 = h_fold(a0 * c1), a1c0 = h_fold(a1 * c0);
+  const uint64_t b0d0 = h_fold(b0 * d0), b1d1 = h_fold(b1 * d1), b0d1 = h_fold(b0 * d1), b1d0 = h_fold(b1 * d0);
+  const uint64_t a0d0 = h_fold(a0 * d0), a1d1 = h_fold(a1 * d1), a0d1 = h_fold(a0 * d1), a1d0 = h_fold(a1 * d0);
+  const uint64_t b0c0 = h_fold(b0 * c0), b1c1 = h_fold(b1 * c1), b0c1 = h_fold(b0 * c1), b1c0 = h_fold(b1 * c0);
+  // Every folded term is < 2^32 < 3P, so 16P covers the largest negative part (5 terms).
+  constexpr uint64_t K = 16ull * P;
+  const uint64_t r0 = a0c0 + 2 * b0d0 + K - (a1c1 + 2 * b1d1 + b0d1 + b1d0);
+  const uint64_t r1 = a0c1 + a1c0 + b0d0 + 2 * b0d1 + 2 * b1d0 + K - b1d1;
+  const uint64_t r2 = a0d0 + b0c0 + K - (a1d1 + b1c1);
+  const uint64_t r3 = a0d1 + a1d0 + b0c1 + b1c0;
+  return hq{{h_reduce64(r0), h_reduce64(r1), h_reduce64(r2), h_reduce64(r3)}};
 }
 inline hq hq_conj(hq x) { return hq{{x.v[0], x.v[1], h_sub(0, x.v[2]), h_sub(0, x.v[3])}}; }
 inline hq hq_pow(hq b, uint64_t e) { hq r = hq_make(1, 0, 0, 0); while (e) { if (e & 1) r = hq_mul(r, b); b = hq_mul(b, b); e >>= 1; } return r; }

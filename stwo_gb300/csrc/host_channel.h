@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 #include "common.cuh"
+#include "blake2s_rounds.cuh"
 
 namespace stwo {
 
@@ -27,12 +28,6 @@ inline uint32_t h_rotr(uint32_t x, int n) { return (x >> n) | (x << (32 - n)); }
 inline void h_b2s_compress(uint32_t h[8], const uint32_t m[16], uint64_t t, bool last, bool raw_iv = true) {
   static const uint32_t IV[8] = {0x6A09E667u, 0xBB67AE85u, 0x3C6EF372u, 0xA54FF53Au,
                                  0x510E527Fu, 0x9B05688Cu, 0x1F83D9ABu, 0x5BE0CD19u};
-  static const uint8_t S[10][16] = {
-      {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15}, {14, 10, 4, 8, 9, 15, 13, 6, 1, 12, 0, 2, 11, 7, 5, 3},
-      {11, 8, 12, 0, 5, 2, 15, 13, 10, 14, 3, 6, 7, 1, 9, 4}, {7, 9, 3, 1, 13, 12, 11, 14, 2, 6, 5, 10, 4, 0, 15, 8},
-      {9, 0, 5, 7, 2, 4, 10, 15, 14, 1, 11, 12, 6, 8, 3, 13}, {2, 12, 6, 10, 0, 11, 8, 3, 4, 13, 7, 5, 15, 14, 1, 9},
-      {12, 5, 1, 15, 14, 13, 4, 10, 0, 7, 6, 3, 9, 2, 8, 11}, {13, 11, 7, 14, 12, 1, 3, 9, 5, 0, 15, 4, 8, 6, 2, 10},
-      {6, 15, 14, 9, 11, 3, 0, 8, 12, 2, 13, 7, 1, 4, 10, 5}, {10, 2, 8, 4, 7, 6, 1, 5, 15, 11, 9, 14, 3, 12, 13, 0}};
   (void)raw_iv;
   uint32_t v[16];
   for (int i = 0; i < 8; i++) {
@@ -42,27 +37,24 @@ inline void h_b2s_compress(uint32_t h[8], const uint32_t m[16], uint64_t t, bool
   v[12] ^= (uint32_t)t;
   v[13] ^= (uint32_t)(t >> 32);
   if (last) v[14] = ~v[14];
-  auto G = [&](int a, int b, int c, int d, uint32_t x, uint32_t y) {
-    v[a] = v[a] + v[b] + x;
-    v[d] = h_rotr(v[d] ^ v[a], 16);
-    v[c] = v[c] + v[d];
-    v[b] = h_rotr(v[b] ^ v[c], 12);
-    v[a] = v[a] + v[b] + y;
-    v[d] = h_rotr(v[d] ^ v[a], 8);
-    v[c] = v[c] + v[d];
-    v[b] = h_rotr(v[b] ^ v[c], 7);
-  };
-  for (int r = 0; r < 10; r++) {
-    const uint8_t* s = S[r];
-    G(0, 4, 8, 12, m[s[0]], m[s[1]]);
-    G(1, 5, 9, 13, m[s[2]], m[s[3]]);
-    G(2, 6, 10, 14, m[s[4]], m[s[5]]);
-    G(3, 7, 11, 15, m[s[6]], m[s[7]]);
-    G(0, 5, 10, 15, m[s[8]], m[s[9]]);
-    G(1, 6, 11, 12, m[s[10]], m[s[11]]);
-    G(2, 7, 8, 13, m[s[12]], m[s[13]]);
-    G(3, 4, 9, 14, m[s[14]], m[s[15]]);
-  }
+  // The ten rounds unrolled with the schedule of blake2s_rounds.cuh (constant message indices).
+#define H_B2S_G(a, b, c, d, x, y) \
+  do {                            \
+    a = a + b + (x);              \
+    d = h_rotr(d ^ a, 16);        \
+    c = c + d;                    \
+    b = h_rotr(b ^ c, 12);        \
+    a = a + b + (y);              \
+    d = h_rotr(d ^ a, 8);         \
+    c = c + d;                    \
+    b = h_rotr(b ^ c, 7);         \
+  } while (0)
+#pragma push_macro("B2S_G")
+#undef B2S_G
+#define B2S_G(a, b, c, d, x, y) H_B2S_G(a, b, c, d, x, y)
+  B2S_ROUNDS(v, m)
+#pragma pop_macro("B2S_G")
+#undef H_B2S_G
   for (int i = 0; i < 8; i++) h[i] ^= v[i] ^ v[i + 8];
 }
 
