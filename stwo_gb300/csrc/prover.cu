@@ -60,55 +60,79 @@ Arena::~Arena() {
   for (void* p : ptrs) cudaFreeAsync(p, s);
 }
 uint32_t* Arena::alloc(size_t words) {
-  void* p = nullptr;
-  if (scratch_alloc(&p, std::max<size_t>(words, 1) * 4, s) != STWO_OK) {
-    failed = true;
-    return nullptr;
+  const size_t bytes = (std::max<size_t>(words, 1) * 4 + 255) / 256 * 256;
+  if (bytes > CHUNK / 4) {
+    void* p = nullptr;
+    if (scratch_alloc(&p, bytes, s) != STWO_OK) {
+      failed = true;
+      return nullptr;
+    }
+    ptrs.push_back(p);
+    return reinterpret_cast<uint32_t*>(p);
   }
-  ptrs.push_back(p);
-  return reinterpret_cast<uint32_t*>(p);
+  if (!chunk || chunk_used + bytes > CHUNK) {
+    void* p = nullptr;
+    if (scratch_alloc(&p, CHUNK, s) != STWO_OK) {
+      failed = true;
+      return nullptr;
+    }
+    ptrs.push_back(p);
+    chunk = reinterpret_cast<char*>(p);
+    chunk_used = 0;
+  }
+  uint32_t* r = reinterpret_cast<uint32_t*>(chunk + chunk_used);
+  chunk_used += bytes;
+  return r;
 }
 
 // ------------------------------------------------------------------------------------------------
 // Gather of words from HBM: each request is (device pointer, element index), 1 or 8 words.
-__global__ void k_gather(const unsigned long long* ptr, const unsigned long long* idx, uint32_t n, uint32_t words,
-                         uint32_t* out) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t* p = reinterpret_cast<const uint32_t*>(ptr[i]) + idx[i] * words;
-  for (uint32_t w = 0; w < words; w++) out[(size_t)i * words + w] = p[w];
+// Every requested word (values) and 8-word hash, in one launch: request i < nv reads one word,
+// the others one hash. Requests and results live in mapped host memory.
+__global__ void k_gather(const unsigned long long* req, uint32_t nv, uint32_t nh, uint32_t* vout, uint32_t* hout) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nv) {
+    vout[i] = reinterpret_cast<const uint32_t*>(req[2 * i])[req[2 * i + 1]];
+  } else if (i < nv + nh) {
+    const uint32_t j = i - nv;
+    const uint4* p = reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(req[2 * i]) + req[2 * i + 1] * 8);
+    uint4 a = p[0], b = p[1];
+    uint32_t* o = hout + (size_t)j * 8;
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+  }
 }
 
 int32_t Gather::run(cudaStream_t s) {
-  for (int kind = 0; kind < 2; kind++) {
-    auto& ptr = kind ? hptr : vptr;
-    auto& idx = kind ? hidx : vidx;
-    auto& res = kind ? hres : vres;
-    uint32_t words = kind ? 8 : 1;
-    size_t n = ptr.size();
-    res.assign(n * words, 0);
-    if (!n) continue;
-    char* buf = nullptr;
-    int32_t st = scratch_alloc((void**)&buf, n * 16 + n * words * 4, s);
-    if (st) return st;
-    unsigned long long* dptr = reinterpret_cast<unsigned long long*>(buf);
-    unsigned long long* didx = dptr + n;
-    uint32_t* dout = reinterpret_cast<uint32_t*>(didx + n);
-    cudaError_t e = cudaMemcpyAsync(dptr, ptr.data(), n * 8, cudaMemcpyHostToDevice, s);
-    if (!e) e = cudaMemcpyAsync(didx, idx.data(), n * 8, cudaMemcpyHostToDevice, s);
-    if (!e) {
-      k_gather<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>(dptr, didx, (uint32_t)n, words, dout);
-      note_launch();
-      e = cudaGetLastError();
-    }
-    if (!e) e = cudaMemcpyAsync(res.data(), dout, n * words * 4, cudaMemcpyDeviceToHost, s);
-    if (!e) e = cudaStreamSynchronize(s);
-    scratch_free(buf, s);
-    if (e) {
-      set_error("gather: %s", cudaGetErrorString(e));
-      return STWO_ERR_CUDA;
-    }
+  const size_t nv = vptr.size(), nh = hptr.size();
+  vres.assign(nv, 0);
+  hres.assign(nh * 8, 0);
+  if (nv + nh == 0) return STWO_OK;
+  Mapped mp;
+  int32_t st = mapped_words(4 * (nv + nh) + nv + 8 * nh, mp);
+  if (st) return st;
+  unsigned long long* req = reinterpret_cast<unsigned long long*>(mp.host);
+  for (size_t i = 0; i < nv; i++) {
+    req[2 * i] = vptr[i];
+    req[2 * i + 1] = vidx[i];
   }
+  for (size_t i = 0; i < nh; i++) {
+    req[2 * (nv + i)] = hptr[i];
+    req[2 * (nv + i) + 1] = hidx[i];
+  }
+  uint32_t* dres = mp.dev + 4 * (nv + nh);
+  k_gather<<<(uint32_t)((nv + nh + 127) / 128), 128, 0, s>>>(reinterpret_cast<const unsigned long long*>(mp.dev),
+                                                             (uint32_t)nv, (uint32_t)nh, dres, dres + nv);
+  note_launch();
+  cudaError_t e = cudaGetLastError();
+  if (!e) e = cudaStreamSynchronize(s);
+  if (e) {
+    set_error("gather: %s", cudaGetErrorString(e));
+    return STWO_ERR_CUDA;
+  }
+  const uint32_t* hres_p = mp.host + 4 * (nv + nh);
+  std::memcpy(vres.data(), hres_p, nv * 4);
+  std::memcpy(hres.data(), hres_p + nv, nh * 32);
   return STWO_OK;
 }
 

@@ -10,9 +10,15 @@
 namespace stwo {
 
 // Stream-ordered device allocations released together (one proof's working set).
+// Device memory of one proof, released together at its end. Small requests are carved from
+// 32 MiB chunks (256-byte aligned) so that a proof makes a few dozen pool allocations rather
+// than hundreds; large ones get their own.
 struct Arena {
+  static constexpr size_t CHUNK = 32u << 20;
   cudaStream_t s;
   std::vector<void*> ptrs;
+  char* chunk = nullptr;
+  size_t chunk_used = 0;
   bool failed = false;
   explicit Arena(cudaStream_t st) : s(st) {}
   ~Arena();

@@ -48,6 +48,72 @@ struct QStage {
   uint32_t c[4];
 };
 
+// Per-sample input of the line-coefficient kernel: column index and sampled value.
+struct QSample {
+  uint32_t col;
+  uint32_t v[4];
+};
+
+__device__ __forceinline__ qm31 q_conj(qm31 x) { return {x.a, cm31_sub({0u, 0u}, x.b)}; }
+__device__ __forceinline__ qm31 q_pow(qm31 b, uint32_t e) {
+  qm31 r = qm31_from_u32(1u, 0u, 0u, 0u);
+  while (e) {
+    if (e & 1u) r = qm31_mul(r, b);
+    b = qm31_mul(b, b);
+    e >>= 1;
+  }
+  return r;
+}
+
+// Line coefficients of one sample batch per block (cpu/quotients.rs:78-125, constraints.rs:98):
+// for the batch's j-th column with value v at point p, alpha_j = rc^(j+1), a_j = conj(v) - v,
+// c = conj(p.y) - p.y, b_j = v c - a_j p.y; the entry keeps alpha_j c, the batch the sums of
+// alpha_j a_j and alpha_j b_j and rc^n. Field sums are exact, so the reduction order is free.
+__global__ void __launch_bounds__(256) k_quotient_coeffs(const QSample* __restrict__ samples, QBatch* batches,
+                                                         QEntry* entries, qm31 rc) {
+  __shared__ qm31 s_a[8], s_b[8];
+  QBatch& B = batches[blockIdx.x];
+  const uint32_t e0 = B.e0, e1 = B.e1;
+  const qm31 py = qm31_from_u32(B.pry[0], B.pry[1], B.piy[0], B.piy[1]);
+  const qm31 c = qm31_sub(q_conj(py), py);
+  qm31 sa = qm31_zero(), sb = qm31_zero();
+  for (uint32_t j = threadIdx.x; j < e1 - e0; j += blockDim.x) {
+    const QSample sm = samples[e0 + j];
+    const qm31 v = qm31_from_u32(sm.v[0], sm.v[1], sm.v[2], sm.v[3]);
+    const qm31 alpha = q_pow(rc, j + 1);
+    const qm31 a = qm31_sub(q_conj(v), v);
+    const qm31 b = qm31_sub(qm31_mul(v, c), qm31_mul(a, py));
+    sa = qm31_add(sa, qm31_mul(alpha, a));
+    sb = qm31_add(sb, qm31_mul(alpha, b));
+    const qm31 ca = qm31_mul(alpha, c);
+    QEntry e;
+    e.col = sm.col;
+    e.c[0] = ca.a.a; e.c[1] = ca.a.b; e.c[2] = ca.b.a; e.c[3] = ca.b.b;
+    entries[e0 + j] = e;
+  }
+  for (int off = 16; off; off >>= 1) {
+    sa = qm31_from_u32(m31_add(sa.a.a, __shfl_xor_sync(~0u, sa.a.a, off)), m31_add(sa.a.b, __shfl_xor_sync(~0u, sa.a.b, off)),
+                       m31_add(sa.b.a, __shfl_xor_sync(~0u, sa.b.a, off)), m31_add(sa.b.b, __shfl_xor_sync(~0u, sa.b.b, off)));
+    sb = qm31_from_u32(m31_add(sb.a.a, __shfl_xor_sync(~0u, sb.a.a, off)), m31_add(sb.a.b, __shfl_xor_sync(~0u, sb.a.b, off)),
+                       m31_add(sb.b.a, __shfl_xor_sync(~0u, sb.b.a, off)), m31_add(sb.b.b, __shfl_xor_sync(~0u, sb.b.b, off)));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_a[threadIdx.x >> 5] = sa;
+    s_b[threadIdx.x >> 5] = sb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (uint32_t w = 1; w < blockDim.x / 32; w++) {
+      s_a[0] = qm31_add(s_a[0], s_a[w]);
+      s_b[0] = qm31_add(s_b[0], s_b[w]);
+    }
+    const qm31 bc = q_pow(rc, e1 - e0);
+    B.sum_a[0] = s_a[0].a.a; B.sum_a[1] = s_a[0].a.b; B.sum_a[2] = s_a[0].b.a; B.sum_a[3] = s_a[0].b.b;
+    B.sum_b[0] = s_b[0].a.a; B.sum_b[1] = s_b[0].a.b; B.sum_b[2] = s_b[0].b.a; B.sum_b[3] = s_b[0].b.b;
+    B.coeff[0] = bc.a.a; B.coeff[1] = bc.a.b; B.coeff[2] = bc.b.a; B.coeff[3] = bc.b.b;
+  }
+}
+
 constexpr int Q_ROWS = 32;    // rows per block (one warp-width of consecutive rows)
 constexpr int Q_SLICES = 8;   // column slices per row; 256 threads
 constexpr int Q_STAGE = 512;  // entries staged in shared memory at a time
@@ -170,54 +236,41 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
   STWO_REQUIRE(n_batches == 0 || batches, "null batches");
   hq rc = hq_from(rc_in);
 
-  // Host constants: O(#samples) (cpu/quotients.rs:78-125).
+  // Batch headers on the host (points, entry ranges); the line coefficients on the device.
   std::vector<QBatch> hb(n_batches);
-  std::vector<QEntry> he;
+  std::vector<QSample> hs;
   for (uint32_t b = 0; b < n_batches; b++) {
     const stwo_sample_batch& sb = batches[b];
     hq px = hq_from(sb.point.x), py = hq_from(sb.point.y);
     STWO_REQUIRE(!(py.v[2] == 0 && py.v[3] == 0), "Cannot evaluate a line with a single point");
     QBatch& B = hb[b];
+    std::memset(&B, 0, sizeof(B));
     B.prx[0] = px.v[0]; B.prx[1] = px.v[1]; B.pix[0] = px.v[2]; B.pix[1] = px.v[3];
     B.pry[0] = py.v[0]; B.pry[1] = py.v[1]; B.piy[0] = py.v[2]; B.piy[1] = py.v[3];
-    hq alpha = hq_make(1, 0, 0, 0), sa = hq_make(0, 0, 0, 0), sbb = hq_make(0, 0, 0, 0);
-    B.e0 = (uint32_t)he.size();
+    B.e0 = (uint32_t)hs.size();
     for (uint32_t j = 0; j < sb.n_columns; j++) {
       STWO_REQUIRE(sb.h_column_indices[j] < n_cols, "sample column index out of range");
-      alpha = hq_mul(alpha, rc);
-      hq value = hq_from(sb.h_values[j]);
-      hq a = hq_sub(hq_conj(value), value);
-      hq c = hq_sub(hq_conj(py), py);
-      hq bcoef = hq_sub(hq_mul(value, c), hq_mul(a, py));
-      sa = hq_add(sa, hq_mul(alpha, a));
-      sbb = hq_add(sbb, hq_mul(alpha, bcoef));
-      hq ca = hq_mul(alpha, c);
-      QEntry e;
-      e.col = sb.h_column_indices[j];
-      for (int q = 0; q < 4; q++) e.c[q] = ca.v[q];
-      he.push_back(e);
+      QSample q;
+      q.col = sb.h_column_indices[j];
+      for (int k = 0; k < 4; k++) q.v[k] = sb.h_values[j].v[k];
+      hs.push_back(q);
     }
-    B.e1 = (uint32_t)he.size();
-    hq bc = hq_pow(rc, sb.n_columns);
-    for (int q = 0; q < 4; q++) {
-      B.sum_a[q] = sa.v[q];
-      B.sum_b[q] = sbb.v[q];
-      B.coeff[q] = bc.v[q];
-    }
+    B.e1 = (uint32_t)hs.size();
   }
-
+  std::vector<QEntry> he(hs.size());
   stwo_coset dom_half = canonic_half_coset(log_n);
   uint32_t sub_log = log_n - log_blowup;
   bool direct = sub_log < 6;
   uint32_t rows = 1u << (direct ? log_n : sub_log);
 
-  size_t tbl_bytes = hb.size() * sizeof(QBatch) + he.size() * sizeof(QEntry);
+  size_t tbl_bytes = hb.size() * sizeof(QBatch) + he.size() * sizeof(QEntry) + hs.size() * sizeof(QSample);
   size_t sub_bytes = direct ? 0 : (size_t)4 * rows * 4;
   char* scratch = nullptr;
   int32_t st = scratch_alloc((void**)&scratch, tbl_bytes + sub_bytes + 256, s);
   if (st) return st;
   QBatch* d_b = reinterpret_cast<QBatch*>(scratch);
   QEntry* d_e = reinterpret_cast<QEntry*>(scratch + hb.size() * sizeof(QBatch));
+  QSample* d_s = reinterpret_cast<QSample*>(scratch + hb.size() * sizeof(QBatch) + he.size() * sizeof(QEntry));
   uint32_t* d_sub = reinterpret_cast<uint32_t*>(scratch + ((tbl_bytes + 255) / 256) * 256);
   auto fail = [&](int32_t code) {
     scratch_free(scratch, s);
@@ -225,8 +278,13 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
   };
   if (!hb.empty() && cudaMemcpyAsync(d_b, hb.data(), hb.size() * sizeof(QBatch), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return fail(STWO_ERR_CUDA);
-  if (!he.empty() && cudaMemcpyAsync(d_e, he.data(), he.size() * sizeof(QEntry), cudaMemcpyHostToDevice, s) != cudaSuccess)
+  if (!hs.empty() && cudaMemcpyAsync(d_s, hs.data(), hs.size() * sizeof(QSample), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return fail(STWO_ERR_CUDA);
+  if (n_batches) {
+    k_quotient_coeffs<<<n_batches, 256, 0, s>>>(d_s, d_b, d_e, qm31{{rc.v[0], rc.v[1]}, {rc.v[2], rc.v[3]}});
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
+  }
 
   QCols qc;
   for (uint32_t c = 0; c < n_cols; c++) qc.p[c] = cols[c];

@@ -2,6 +2,7 @@
 #include "common.cuh"
 #include <cstdarg>
 #include <atomic>
+#include <chrono>
 
 namespace stwo {
 
@@ -20,6 +21,7 @@ void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 struct StageRec {
   const char* name;
   cudaEvent_t a, b;
+  std::chrono::steady_clock::time_point ha, hb;  // host clock at the stage's begin and end calls
 };
 static thread_local bool g_stage_on = false;
 static thread_local std::vector<StageRec> g_stages;
@@ -28,7 +30,7 @@ static thread_local int g_stage_open = -1;
 void stage_begin(const char* name, cudaStream_t s) {
   if (!g_stage_on) return;
   if (g_stage_open >= 0) stage_end(s);
-  StageRec r{name, nullptr, nullptr};
+  StageRec r{name, nullptr, nullptr, std::chrono::steady_clock::now(), {}};
   if (cudaEventCreate(&r.a) != cudaSuccess || cudaEventCreate(&r.b) != cudaSuccess) return;
   cudaEventRecord(r.a, s);
   g_stages.push_back(r);
@@ -37,6 +39,7 @@ void stage_begin(const char* name, cudaStream_t s) {
 void stage_end(cudaStream_t s) {
   if (!g_stage_on || g_stage_open < 0) return;
   cudaEventRecord(g_stages[g_stage_open].b, s);
+  g_stages[g_stage_open].hb = std::chrono::steady_clock::now();
   g_stage_open = -1;
 }
 
@@ -243,7 +246,7 @@ uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap) {
   // "gap before <stage>": device idle or unlabelled work while the host prepared the next stage.
   thread_local std::vector<std::string> gap_names;
   gap_names.clear();
-  gap_names.reserve(g_stages.size());
+  gap_names.reserve(2 * g_stages.size());
   std::vector<std::pair<const char*, float>> agg, gaps;
   auto add = [](std::vector<std::pair<const char*, float>>& v, const char* name, float t) {
     for (auto& a : v)
@@ -272,11 +275,26 @@ uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap) {
       add(gaps, key, g);
     }
   }
+  // Host time spent issuing each stage ("host: <stage>"): when it approaches the device time,
+  // the stage is bound by host work or launch issue rather than by its kernels.
+  std::vector<std::pair<const char*, float>> host;
+  for (auto& r : g_stages) {
+    std::string hn = std::string("host: ") + r.name;
+    const char* key = nullptr;
+    for (auto& n : gap_names)
+      if (n == hn) key = n.c_str();
+    if (!key) {
+      gap_names.push_back(hn);
+      key = gap_names.back().c_str();
+    }
+    add(host, key, std::chrono::duration<float, std::milli>(r.hb - r.ha).count());
+  }
   for (auto& r : g_stages) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
   }
   for (auto& g : gaps) agg.push_back(g);
+  for (auto& h : host) agg.push_back(h);
   g_stages.clear();
   g_stage_open = -1;
   uint32_t n = 0;
