@@ -75,7 +75,7 @@ def test_interpolate(cuda, oracle, log):
 
 
 @pytest.mark.parametrize("coeff_log,log", [(1, 1), (1, 3), (2, 2), (3, 5), (5, 5), (4, 9), (10, 11), (12, 14),
-                                           (13, 13), (14, 16), (16, 17), (17, 19), (18, 20), (16, 20)])
+                                           (13, 13), (14, 16), (16, 17), (17, 19), (18, 20), (16, 20), (20, 22)])
 def test_evaluate(cuda, oracle, coeff_log, log):
     from stwo_gb300 import _lib
     from stwo_gb300.backend import TwiddleTree
@@ -104,7 +104,7 @@ def test_interpolate_non_canonic_domain(cuda, oracle):
     assert np.array_equal(host(c), oracle.interpolate(half, half, v))
 
 
-@pytest.mark.parametrize("log", [0, 1, 3, 8, 9, 13, 15])
+@pytest.mark.parametrize("log", [0, 1, 3, 8, 9, 13, 15, 16, 17, 18, 20])
 def test_eval_at_points(cuda, oracle, log):
     rng = np.random.default_rng(300 + log)
     polys = [F.rand_m31(rng, 1 << log) for _ in range(3)]
@@ -116,7 +116,8 @@ def test_eval_at_points(cuda, oracle, log):
 
 @pytest.mark.parametrize("log,ncols,prev", [(0, 0, False), (0, 0, True), (3, 1, False), (4, 15, True),
                                             (5, 16, False), (5, 17, True), (7, 100, False), (10, 0, True),
-                                            (9, 256, True), (2, 33, False), (6, 1300, False), (12, 4, True)])
+                                            (9, 256, True), (2, 33, False), (6, 1300, False), (12, 4, True),
+                                            (3, 3100, True), (2, 6200, False)])
 def test_merkle_layer(cuda, oracle, log, ncols, prev):
     import torch
 

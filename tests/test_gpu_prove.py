@@ -60,3 +60,19 @@ def test_poseidon_proof_bytes_match_oracle(cuda, oracle, log_n, seeded, cfg):
     assert got == want
     ok, why = oracle.verify_poseidon(log_n, cs, got)
     assert ok, why
+
+
+def test_poseidon_headline_size_matches_oracle(cuda, oracle):
+    # The benchmarked proof itself: 2^16 rows, seeded states, pow_bits 10 (the same generator as
+    # bench.py's workload), byte-identical to the oracle's and accepted by its verifier.
+    from stwo_gb300.prover import prove_poseidon
+    from tests.golden.cases import words
+
+    log_n, cfg = 16, (10, 1, 0, 3)
+    init = words(3, (1 << log_n) * 8 * 16)
+    want, want_cs = oracle.prove_poseidon(log_n, init, cfg)
+    got, cs = prove_poseidon(log_n, dev(init), cfg)
+    assert cs == want_cs
+    assert got == want
+    ok, why = oracle.verify_poseidon(log_n, cs, got)
+    assert ok, why
