@@ -10,6 +10,8 @@
 // g = f -+ lambda.
 // Each kernel is one streaming pass over four coordinate columns: HBM-bound.
 #include "common.cuh"
+#include <array>
+#include "blake2s.cuh"
 #include "dchannel.cuh"
 
 namespace stwo {
@@ -240,6 +242,112 @@ int32_t fri_decompose(const uint32_t* const src[4], uint32_t log_size, uint32_t*
     set_error("decompose: %s", cudaGetErrorString(e));
     return STWO_ERR_CUDA;
   }
+  return STWO_OK;
+}
+
+// ---------------------------------------------------------------- small-layer tail
+// The FRI layers of at most 2^FRI_TAIL_MAX_LOG points, in one single-block launch. Per layer:
+// Blake2s leaves of its four coordinate columns, the node levels up to the root (halving in the
+// block), the transcript step (mix the root, draw alpha) on the device channel, and the line
+// fold into the next layer. The results are the ones of the per-kernel path (the same Merkle
+// layout as DevMerkle, the same fold as k_fold_line); only the number of launches changes.
+constexpr uint32_t FRI_TAIL_MAX_LAYERS = 16;
+struct FriTailParams {
+  uint32_t n_layers;
+  uint32_t log[FRI_TAIL_MAX_LAYERS];           // layer j has 2^log[j] points
+  const uint32_t* eval[FRI_TAIL_MAX_LAYERS + 1][4];  // eval[j + 1] receives the fold of layer j
+  uint32_t* tree[FRI_TAIL_MAX_LAYERS];         // all Merkle layers of layer j (root at offset 0)
+  const uint32_t* itw[FRI_TAIL_MAX_LAYERS];    // inverse twiddles of layer j's line domain level
+  DevChannel* ch;
+  uint32_t* alphas;                            // 8 words per layer: alpha, alpha^2
+};
+
+__global__ void __launch_bounds__(1024) k_fri_tail(FriTailParams p) {
+  __shared__ qm31 s_alpha;
+  for (uint32_t j = 0; j < p.n_layers; j++) {
+    const uint32_t k = p.log[j], n = 1u << k;
+    const uint32_t* const* c = p.eval[j];
+    uint32_t* tree = p.tree[j];
+    uint32_t* leaves = tree + (size_t)8 * (n - 1);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      uint32_t h[8], m[16];
+      b2s_init(h);
+#pragma unroll
+      for (int q = 0; q < 16; q++) m[q] = 0u;
+      m[0] = c[0][i];
+      m[1] = c[1][i];
+      m[2] = c[2][i];
+      m[3] = c[3][i];
+      b2s_compress(h, m, 16, true);
+#pragma unroll
+      for (int q = 0; q < 8; q++) leaves[(size_t)8 * i + q] = h[q];
+    }
+    __syncthreads();
+    for (int lg = (int)k - 1; lg >= 0; lg--) {
+      const uint32_t w = 1u << lg;
+      const uint32_t* child = tree + (size_t)8 * (2 * w - 1);
+      uint32_t* out = tree + (size_t)8 * (w - 1);
+      for (uint32_t i = threadIdx.x; i < w; i += blockDim.x) {
+        uint32_t h[8], m[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) m[q] = child[(size_t)16 * i + q];
+        b2s_init(h);
+        b2s_compress(h, m, 64, true);
+#pragma unroll
+        for (int q = 0; q < 8; q++) out[(size_t)8 * i + q] = h[q];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      d_ch_mix_root(p.ch, tree);
+      const qm31 a = d_ch_draw_felt(p.ch);
+      const qm31 a2 = qm31_mul(a, a);
+      uint32_t* o = p.alphas + 8 * j;
+      o[0] = a.a.a; o[1] = a.a.b; o[2] = a.b.a; o[3] = a.b.b;
+      o[4] = a2.a.a; o[5] = a2.a.b; o[6] = a2.b.a; o[7] = a2.b.b;
+      s_alpha = a;
+    }
+    __syncthreads();
+    const qm31 alpha = s_alpha;
+    uint32_t* const* nxt = const_cast<uint32_t* const*>(p.eval[j + 1]);
+    for (uint32_t i = threadIdx.x; i < n / 2; i += blockDim.x) {
+      qm31 f0 = qm31_from_u32(c[0][2 * i], c[1][2 * i], c[2][2 * i], c[3][2 * i]);
+      qm31 f1 = qm31_from_u32(c[0][2 * i + 1], c[1][2 * i + 1], c[2][2 * i + 1], c[3][2 * i + 1]);
+      ibfly_q(f0, f1, p.itw[j][i]);
+      const qm31 r = qm31_add(f0, qm31_mul(alpha, f1));
+      nxt[0][i] = r.a.a;
+      nxt[1][i] = r.a.b;
+      nxt[2][i] = r.b.a;
+      nxt[3][i] = r.b.b;
+    }
+    __syncthreads();
+  }
+}
+
+// Launches the tail over layers whose line domains are `doms` (each the doubling of the last);
+// eval[0] holds the first layer, eval[j + 1] receives each fold.
+int32_t fri_tail(const TwiddleTree* tree, const std::vector<stwo_coset>& doms,
+                 const std::vector<std::array<uint32_t*, 4>>& evals, const std::vector<uint32_t*>& trees,
+                 DevChannel* ch, uint32_t* alphas, cudaStream_t s) {
+  STWO_REQUIRE(!doms.empty() && doms.size() <= FRI_TAIL_MAX_LAYERS, "FRI tail of %zu layers", doms.size());
+  STWO_REQUIRE(evals.size() == doms.size() + 1 && trees.size() == doms.size(), "FRI tail buffers");
+  FriTailParams p{};
+  p.n_layers = (uint32_t)doms.size();
+  for (size_t j = 0; j < doms.size(); j++) {
+    STWO_REQUIRE(doms[j].log_size >= 1, "Evaluation too small");
+    size_t off;
+    STWO_REQUIRE(level_offset(tree, doms[j], &off), "line domain is not a doubling of the twiddle root");
+    p.log[j] = doms[j].log_size;
+    p.itw[j] = tree->d_itw + off;
+    p.tree[j] = trees[j];
+  }
+  for (size_t j = 0; j < evals.size(); j++)
+    for (int k = 0; k < 4; k++) p.eval[j][k] = evals[j][k];
+  p.ch = ch;
+  p.alphas = alphas;
+  k_fri_tail<<<1, 1024, 0, s>>>(p);
+  note_launch();
+  STWO_LAUNCH_CHECK();
   return STWO_OK;
 }
 

@@ -15,6 +15,7 @@
 #include "host_channel.h"
 #include "prover.cuh"
 #include "dchannel.cuh"
+#include <array>
 #include <future>
 #include <set>
 
@@ -35,6 +36,11 @@ int32_t fri_fold_line(const TwiddleTree* tree, stwo_coset line_domain, const uin
 int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* const dst[4], const uint32_t* const src[4],
                         qm31 alpha, cudaStream_t s, const uint32_t* alpha_dev);
 int32_t fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_t* alpha_out, cudaStream_t s);
+int32_t fri_tail(const TwiddleTree* tree, const std::vector<stwo_coset>& doms,
+                 const std::vector<std::array<uint32_t*, 4>>& evals, const std::vector<uint32_t*>& trees,
+                 DevChannel* ch, uint32_t* alphas, cudaStream_t s);
+// FRI layers of at most 2^FRI_TAIL_LOG points run in the single-launch tail (fri_tail).
+constexpr uint32_t FRI_TAIL_LOG = 12;
 int32_t channel_set(DevChannel* ch, const uint32_t digest[8], uint64_t n_sent, cudaStream_t s);
 
 // Copies segments of device words into one destination (mapped host memory) in one launch.
@@ -226,8 +232,15 @@ void DevMerkle::decommit(const std::map<uint32_t, std::vector<size_t>>& queries,
 // Canonical proof bytes (same layout as the oracle's serialiser).
 struct ByteWriter {
   std::vector<uint8_t> b;
-  void u32(uint32_t v) { for (int i = 0; i < 4; i++) b.push_back((uint8_t)(v >> (8 * i))); }
-  void u64(uint64_t v) { for (int i = 0; i < 8; i++) b.push_back((uint8_t)(v >> (8 * i))); }
+  ByteWriter() { b.reserve(1 << 17); }
+  template <class T>
+  void le(T v) {  // little-endian bytes of an unsigned integer
+    uint8_t t[sizeof(T)];
+    for (size_t i = 0; i < sizeof(T); i++) t[i] = (uint8_t)(v >> (8 * i));
+    b.insert(b.end(), t, t + sizeof(T));
+  }
+  void u32(uint32_t v) { le(v); }
+  void u64(uint64_t v) { le(v); }
   void digest(const Digest& d) { b.insert(b.end(), d.b, d.b + 32); }
   void q(const hq& x) { for (int i = 0; i < 4; i++) u32(x.v[i]); }
   void hashes(const std::vector<size_t>& idx, const Gather& g) {
@@ -660,6 +673,36 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   next = 1;
   size_t last_size = (size_t)1 << (cfg.log_last_layer_degree_bound + cfg.log_blowup_factor);
   while (((size_t)1 << dom.log_size) > last_size) {
+    if (dom.log_size <= FRI_TAIL_LOG && next == quotients.size()) {
+      // The remaining small layers: buffers laid out as the per-kernel path would, one launch.
+      std::vector<stwo_coset> doms;
+      std::vector<std::array<uint32_t*, 4>> evals{{cur.c[0], cur.c[1], cur.c[2], cur.c[3]}};
+      std::vector<uint32_t*> trees;
+      const size_t first_step = fstep + 1;
+      while (((size_t)1 << dom.log_size) > last_size) {
+        STWO_REQUIRE(++fstep < FRI_MAX_STEPS, "too many FRI layers");
+        const uint32_t k = dom.log_size;
+        Layer L;
+        L.eval = cur;
+        L.dom = dom;
+        uint32_t* tbuf = arena.alloc((size_t)8 * ((2ull << k) - 1));
+        SecureCols nxt;
+        for (int c = 0; c < 4; c++) nxt.c[c] = arena.alloc((size_t)1 << (k - 1));
+        if (!tbuf || !nxt.c[0] || !nxt.c[1] || !nxt.c[2] || !nxt.c[3]) return STWO_ERR_OOM;
+        L.merkle.layers.assign(k + 1, nullptr);
+        for (uint32_t lg = 0; lg <= k; lg++) L.merkle.layers[lg] = tbuf + (size_t)8 * ((1ull << lg) - 1);
+        for (int c = 0; c < 4; c++) L.merkle.sorted.push_back({cur.c[c], k});
+        doms.push_back(dom);
+        trees.push_back(tbuf);
+        evals.push_back({nxt.c[0], nxt.c[1], nxt.c[2], nxt.c[3]});
+        layers.push_back(L);
+        cur = nxt;
+        dom = coset_double(dom);
+      }
+      st = fri_tail(tree, doms, evals, trees, dch, alphas + 8 * first_step, s);
+      if (st) return st;
+      break;
+    }
     Layer L;
     L.eval = cur;
     L.dom = dom;
