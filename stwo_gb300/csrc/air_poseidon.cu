@@ -380,16 +380,6 @@ __global__ void __launch_bounds__(128, 8) k_poseidon_composition(const uint32_t*
 }
 
 // ------------------------------------------------------------------------------------ host side
-// Pinned landing words for the claimed-sum read-back (one per host thread).
-static unsigned long long* claimed_pinned() {
-  thread_local unsigned long long* p = [] {
-    void* q = nullptr;
-    if (cudaHostAlloc(&q, 64, cudaHostAllocDefault) != cudaSuccess) q = nullptr;
-    return static_cast<unsigned long long*>(q);
-  }();
-  return p;
-}
-
 static hq hq_m(hq x, uint32_t m) {
   for (int i = 0; i < 4; i++) x.v[i] = h_mul(x.v[i], m);
   return x;
@@ -605,9 +595,9 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
         k_column_sums<<<dim3(std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024), 4), 256, 0, s>>>(last, (uint32_t)n, d_sums);
         note_launch();
         // The sums reach the host with the next synchronisation (the interaction commitment's).
-        if (!claimed_pinned()) st = STWO_ERR_OOM;
+        if (!small_pinned()) st = STWO_ERR_OOM;
         else if (cudaGetLastError() != cudaSuccess ||
-                 cudaMemcpyAsync(claimed_pinned(), d_sums, 32, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                 cudaMemcpyAsync(small_pinned(), d_sums, 32, cudaMemcpyDeviceToHost, s) != cudaSuccess)
           st = STWO_ERR_CUDA;
       }
       if (!st) {
@@ -630,7 +620,7 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
     }
     if (!st) {
       STWO_CHECK_CUDA(cudaStreamSynchronize(s));  // already idle: the commitment read its root
-      const unsigned long long* hs = claimed_pinned();
+      const unsigned long long* hs = small_pinned();
       claimed = hq_make((uint32_t)(hs[0] % P), (uint32_t)(hs[1] % P), (uint32_t)(hs[2] % P), (uint32_t)(hs[3] % P));
     }
     if (!st) {

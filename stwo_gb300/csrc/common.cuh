@@ -207,5 +207,7 @@ struct Mapped {
   size_t words = 0;
 };
 int32_t mapped_words(size_t words, Mapped& m);
+// 64 pinned bytes of the calling host thread, separate from mapped_words (nullptr on failure).
+unsigned long long* small_pinned();
 
 }  // namespace stwo

@@ -84,8 +84,52 @@ void scratch_free(void* p, cudaStream_t s) {
   if (p) cudaFreeAsync(p, s);
 }
 
+// Pinned staging of one host thread. Buffers outlive their thread: a worker that exits hands
+// them to a process-wide free list and the next new thread takes them over, so servers that
+// start fresh workers do not call cudaHostAlloc (slow, and it can wait for running work) for
+// every thread. A thread only exits between jobs, when nothing in flight still uses them.
+namespace {
+struct HostStaging {
+  Mapped mapped;
+  unsigned long long* small = nullptr;
+};
+std::mutex g_staging_mu;
+std::vector<HostStaging*> g_staging_free;
+struct StagingHolder {
+  HostStaging* s = nullptr;
+  ~StagingHolder() {
+    if (!s) return;
+    std::lock_guard<std::mutex> g(g_staging_mu);
+    g_staging_free.push_back(s);
+  }
+};
+HostStaging& staging() {
+  thread_local StagingHolder h;
+  if (!h.s) {
+    std::lock_guard<std::mutex> g(g_staging_mu);
+    if (!g_staging_free.empty()) {
+      h.s = g_staging_free.back();
+      g_staging_free.pop_back();
+    } else {
+      h.s = new HostStaging();
+    }
+  }
+  return *h.s;
+}
+}  // namespace
+
+unsigned long long* small_pinned() {
+  HostStaging& st = staging();
+  if (!st.small) {
+    void* q = nullptr;
+    if (cudaHostAlloc(&q, 64, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    st.small = static_cast<unsigned long long*>(q);
+  }
+  return st.small;
+}
+
 int32_t mapped_words(size_t words, Mapped& m) {
-  thread_local Mapped tl;
+  Mapped& tl = staging().mapped;
   if (tl.words < words) {
     if (tl.host) cudaFreeHost(tl.host);
     tl = Mapped{};
