@@ -301,7 +301,8 @@ stwo_status stwo_server_wait(stwo_server server, uint64_t ticket, stwo_proof_res
 stwo_status stwo_server_destroy(stwo_server server);
 /* The admission estimate of a job, in bytes. */
 size_t stwo_job_hbm_bytes(const stwo_proof_job* job);
-/* All n_jobs on a temporary server; results[i] belongs to jobs[i]. Returns the first failure. */
+/* All n_jobs on a temporary server, submitted largest first (by stwo_job_hbm_bytes); results[i]
+ * belongs to jobs[i]. Returns the first failure. */
 stwo_status stwo_prove_batch(const stwo_proof_job* jobs, uint32_t n_jobs, uint32_t n_workers,
                              size_t hbm_budget_bytes, stwo_proof_result* results);
 

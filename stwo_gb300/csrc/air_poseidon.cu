@@ -66,41 +66,44 @@ __device__ __forceinline__ void internal_matrix(uint32_t* s) {
 
 // ------------------------------------------------------------------------------------------ trace
 // init: ((row * 8 + rep) * 16 + i) or NULL for the reference inputs (row + i + rep).
-__global__ void __launch_bounds__(128) k_poseidon_trace(uint32_t n_rows, const uint32_t* __restrict__ init,
-                                                        uint32_t* __restrict__ trace, uint32_t* __restrict__ lookups) {
-  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+// Warp w of a block computes permutation w of 32 consecutive rows (the layout of
+// k_poseidon_composition): its 158 columns are written with coalesced 128-byte stores, and a
+// small trace takes the latency of one permutation rather than eight.
+__global__ void __launch_bounds__(32 * PS_REPS) k_poseidon_trace(uint32_t n_rows, const uint32_t* __restrict__ init,
+                                                                 uint32_t* __restrict__ trace,
+                                                                 uint32_t* __restrict__ lookups) {
+  const uint32_t rep = threadIdx.x >> 5;
+  const uint32_t r = blockIdx.x * 32 + (threadIdx.x & 31);
   if (r >= n_rows) return;
-  size_t n = n_rows;
-  int col = 0;
-  for (int rep = 0; rep < PS_REPS; rep++) {
-    uint32_t s[PS_ST];
+  const size_t n = n_rows;
+  uint32_t col = rep * PS_COLS_PER_REP;
+  uint32_t s[PS_ST];
 #pragma unroll
-    for (int i = 0; i < PS_ST; i++) {
-      s[i] = init ? init[((size_t)r * PS_REPS + rep) * PS_ST + i] : (r + i + rep);
-      trace[(size_t)col++ * n + r] = s[i];
-      lookups[((size_t)rep * 32 + i) * n + r] = s[i];
-    }
-    for (int round = 0; round < 2 * PS_HALF + PS_PARTIAL; round++) {
-      bool full = round < PS_HALF || round >= PS_HALF + PS_PARTIAL;
-      if (full) {
-#pragma unroll
-        for (int i = 0; i < PS_ST; i++) s[i] = m31_add(s[i], PS_RC);
-        external_matrix(s);
-#pragma unroll
-        for (int i = 0; i < PS_ST; i++) {
-          s[i] = pow5(s[i]);
-          trace[(size_t)col++ * n + r] = s[i];
-        }
-      } else {
-        s[0] = m31_add(s[0], PS_RC);
-        internal_matrix(s);
-        s[0] = pow5(s[0]);
-        trace[(size_t)col++ * n + r] = s[0];
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < PS_ST; i++) lookups[((size_t)rep * 32 + 16 + i) * n + r] = s[i];
+  for (int i = 0; i < PS_ST; i++) {
+    s[i] = init ? init[((size_t)r * PS_REPS + rep) * PS_ST + i] : (r + i + rep);
+    trace[(size_t)col++ * n + r] = s[i];
+    lookups[((size_t)rep * 32 + i) * n + r] = s[i];
   }
+  for (int round = 0; round < 2 * PS_HALF + PS_PARTIAL; round++) {
+    bool full = round < PS_HALF || round >= PS_HALF + PS_PARTIAL;
+    if (full) {
+#pragma unroll
+      for (int i = 0; i < PS_ST; i++) s[i] = m31_add(s[i], PS_RC);
+      external_matrix(s);
+#pragma unroll
+      for (int i = 0; i < PS_ST; i++) {
+        s[i] = pow5(s[i]);
+        trace[(size_t)col++ * n + r] = s[i];
+      }
+    } else {
+      s[0] = m31_add(s[0], PS_RC);
+      internal_matrix(s);
+      s[0] = pow5(s[0]);
+      trace[(size_t)col++ * n + r] = s[0];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < PS_ST; i++) lookups[((size_t)rep * 32 + 16 + i) * n + r] = s[i];
 }
 
 // ------------------------------------------------------------------------------------ interaction
@@ -279,50 +282,60 @@ __device__ __forceinline__ uint32_t prev_row_index(uint32_t r, uint32_t trace_lo
 }
 
 // Trace (1264) and interaction (32) columns are contiguous blocks with a stride of 2^eval_log
-// words, so a mask value is one load at base + (col << eval_log) + row. Each round's masks are
-// loaded before its arithmetic so that their latency hides behind the matrix and S-box work.
-__global__ void __launch_bounds__(128, 8) k_poseidon_composition(const uint32_t* __restrict__ trace,
-                                                              const uint32_t* __restrict__ inter, uint32_t n_rows,
-                                                              PoseidonParams pp, const uint32_t* __restrict__ coeffs,
-                                                              const uint32_t* __restrict__ dinv, uint32_t* o0,
-                                                              uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+// words, so a mask value is one load at base + (col << eval_log) + row.
+//
+// A block takes tiles of 32 rows; warp w evaluates permutation w of every row of the tile (its
+// 142 round constraints and LogUp batch w), so each warp reads the columns of one permutation
+// with one coalesced 128-byte load per column, and a row's eight partial sums meet in shared
+// memory. The random-coefficient sum is exact in the field, so splitting it by permutation gives
+// the same words as accumulating the constraints in order. Eight warps per row keep the latency
+// of a small evaluation domain at one permutation, and the grid, a few tiles per resident block,
+// loads the coefficient table once per block.
+constexpr uint32_t PC_ROWS = 32;
+constexpr uint32_t PC_THREADS = 32 * PS_REPS;
+constexpr uint32_t PC_BLOCKS_PER_SM = 4;
+
+__global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
+    k_poseidon_composition(const uint32_t* __restrict__ trace, const uint32_t* __restrict__ inter, uint32_t n_rows,
+                           PoseidonParams pp, const uint32_t* __restrict__ coeffs, const uint32_t* __restrict__ dinv,
+                           uint32_t* o0, uint32_t* o1, uint32_t* o2, uint32_t* o3) {
   __shared__ uint32_t s_coeffs[4 * PS_N_CONSTRAINTS];
+  __shared__ uint32_t s_part[PS_REPS][4][PC_ROWS];
   for (uint32_t i = threadIdx.x; i < 4 * PS_N_CONSTRAINTS; i += blockDim.x) s_coeffs[i] = coeffs[i];
   __syncthreads();
-  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_rows) return;
+  const uint32_t lane = threadIdx.x & 31, rep = threadIdx.x >> 5;
   const uint32_t el = pp.eval_log;
+  const uint32_t n_tiles = (n_rows + PC_ROWS - 1) / PC_ROWS;
   auto col = [&](const uint32_t* base, uint32_t c, uint32_t row) { return __ldg(base + ((size_t)c << el) + row); };
-  unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-  uint32_t cnt = 0;
-  int ci = 0;
-  auto acc = [&](uint32_t cons) {
-    const uint32_t* k = s_coeffs + 4 * ci++;
-    a0 += (unsigned long long)k[0] * cons;
-    a1 += (unsigned long long)k[1] * cons;
-    a2 += (unsigned long long)k[2] * cons;
-    a3 += (unsigned long long)k[3] * cons;
-    if (++cnt == 3) {
-      a0 = (a0 & P) + (a0 >> 31);
-      a1 = (a1 & P) + (a1 >> 31);
-      a2 = (a2 & P) + (a2 >> 31);
-      a3 = (a3 & P) + (a3 >> 31);
-      cnt = 0;
-    }
-  };
-  qm31 logup = qm31_zero();
-  qm31 prev_col = qm31_zero();
-  uint32_t rp = prev_row_index(r, pp.trace_log, pp.eval_log);
-#pragma unroll 1
-  for (int rep = 0; rep < PS_REPS; rep++) {
+  for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const uint32_t r_out = tile * PC_ROWS + lane;
+    const uint32_t r = min(r_out, n_rows - 1);  // lanes past the end compute a copy and write nothing
+    unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    uint32_t cnt = 0;
+    int ci = rep * (PS_COLS_PER_REP - PS_ST);  // 142 round constraints per permutation
+    auto acc = [&](uint32_t cons) {
+      const uint32_t* k = s_coeffs + 4 * ci++;
+      a0 += (unsigned long long)k[0] * cons;
+      a1 += (unsigned long long)k[1] * cons;
+      a2 += (unsigned long long)k[2] * cons;
+      a3 += (unsigned long long)k[3] * cons;
+      if (++cnt == 3) {
+        a0 = (a0 & P) + (a0 >> 31);
+        a1 = (a1 & P) + (a1 >> 31);
+        a2 = (a2 & P) + (a2 >> 31);
+        a3 = (a3 & P) + (a3 >> 31);
+        cnt = 0;
+      }
+    };
     const uint32_t c0 = rep * PS_COLS_PER_REP;
-    uint32_t s[PS_ST], init[PS_ST];
+    uint32_t s[PS_ST];
 #pragma unroll
-    for (int i = 0; i < PS_ST; i++) {
-      s[i] = col(trace, c0 + i, r);
-      init[i] = s[i];
-    }
+    for (int i = 0; i < PS_ST; i++) s[i] = col(trace, c0 + i, r);
+    // The lookup value of the initial state, taken now so that the state need not be kept.
+    const qm31 d0 = combine16(pp.lc, s);
     uint32_t mc = c0 + PS_ST;
+    // Each round's masks are loaded before its arithmetic so that their latency hides behind the
+    // matrix and S-box work.
     auto full_round = [&]() {
       uint32_t m[PS_ST];
 #pragma unroll
@@ -352,31 +365,43 @@ __global__ void __launch_bounds__(128, 8) k_poseidon_composition(const uint32_t*
     mc += PS_PARTIAL;
 #pragma unroll 1
     for (int round = 0; round < PS_HALF; round++) full_round();
-    // LogUp batch `rep`: fraction (1/d0 - 1/d1) = (d1 - d0) / (d0 d1).
-    qm31 d0 = combine16(pp.lc, init), d1 = combine16(pp.lc, s);
+    // LogUp batch `rep`: fraction (1/d0 - 1/d1) = (d1 - d0) / (d0 d1), against the cumulative
+    // column of this batch minus that of the previous one (for the last batch: minus its value at
+    // the previous trace row and plus claimed_sum / 2^trace_log).
+    const qm31 d1 = combine16(pp.lc, s);
     qm31 num = qm31_sub(d1, d0), den = qm31_mul(d0, d1);
     const uint32_t ic = 4 * rep;
-    qm31 cur = qm31_from_u32(col(inter, ic, r), col(inter, ic + 1, r), col(inter, ic + 2, r), col(inter, ic + 3, r));
-    qm31 diff;
-    if (rep + 1 < PS_REPS) {
-      diff = qm31_sub(cur, prev_col);
-      prev_col = cur;
-    } else {
+    qm31 diff = qm31_from_u32(col(inter, ic, r), col(inter, ic + 1, r), col(inter, ic + 2, r), col(inter, ic + 3, r));
+    if (rep > 0)
+      diff = qm31_sub(diff, qm31_from_u32(col(inter, ic - 4, r), col(inter, ic - 3, r), col(inter, ic - 2, r),
+                                          col(inter, ic - 1, r)));
+    if (rep + 1 == PS_REPS) {
+      const uint32_t rp = prev_row_index(r, pp.trace_log, pp.eval_log);
       qm31 prev = qm31_from_u32(col(inter, ic, rp), col(inter, ic + 1, rp), col(inter, ic + 2, rp),
                                 col(inter, ic + 3, rp));
-      diff = qm31_add(qm31_sub(qm31_sub(cur, prev), prev_col),
-                      qm31_from_u32(pp.shift[0], pp.shift[1], pp.shift[2], pp.shift[3]));
+      diff = qm31_add(qm31_sub(diff, prev), qm31_from_u32(pp.shift[0], pp.shift[1], pp.shift[2], pp.shift[3]));
     }
     qm31 cons = qm31_sub(qm31_mul(diff, den), num);
     const uint32_t* k = s_coeffs + 4 * (PS_N_CONSTRAINTS - PS_REPS + rep);
-    logup = qm31_add(logup, qm31_mul(qm31_from_u32(k[0], k[1], k[2], k[3]), cons));
+    qm31 res = qm31_add(qm31_from_u32(fold64_p(a0), fold64_p(a1), fold64_p(a2), fold64_p(a3)),
+                        qm31_mul(qm31_from_u32(k[0], k[1], k[2], k[3]), cons));
+    s_part[rep][0][lane] = res.a.a;
+    s_part[rep][1][lane] = res.a.b;
+    s_part[rep][2][lane] = res.b.a;
+    s_part[rep][3][lane] = res.b.b;
+    __syncthreads();
+    // Warps 0..3 each finish one coordinate of the tile's 32 rows.
+    if (rep < 4) {
+      uint32_t v = s_part[0][rep][lane];
+#pragma unroll
+      for (int w = 1; w < PS_REPS; w++) v = m31_add(v, s_part[w][rep][lane]);
+      if (r_out < n_rows) {
+        uint32_t* o = rep == 0 ? o0 : rep == 1 ? o1 : rep == 2 ? o2 : o3;
+        o[r_out] = m31_mul(v, __ldg(dinv + (r_out >> pp.trace_log)));
+      }
+    }
+    __syncthreads();
   }
-  qm31 res = qm31_add(qm31_from_u32(fold64_p(a0), fold64_p(a1), fold64_p(a2), fold64_p(a3)), logup);
-  uint32_t d = __ldg(dinv + (r >> pp.trace_log));
-  o0[r] = m31_mul(res.a.a, d);
-  o1[r] = m31_mul(res.a.b, d);
-  o2[r] = m31_mul(res.b.a, d);
-  o3[r] = m31_mul(res.b.b, d);
 }
 
 // ------------------------------------------------------------------------------------ host side
@@ -433,8 +458,10 @@ struct PoseidonGpuAir : GpuAir {
     for (int j = 0; j < PS_ST; j++)
       for (int i = 0; i < 4; i++) pp.lc.alpha_pow[j][i] = le.alpha_pow[j].v[i];
     uint32_t n_rows = 1u << pp.eval_log;
-    k_poseidon_composition<<<(n_rows + 127) / 128, 128, 0, s>>>(cols[1][0], cols[2][0], n_rows, pp, coeffs, dinv,
-                                                                acc[0], acc[1], acc[2], acc[3]);
+    const uint32_t n_tiles = (n_rows + PC_ROWS - 1) / PC_ROWS;
+    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)sm_count() * PC_BLOCKS_PER_SM);
+    k_poseidon_composition<<<grid, PC_THREADS, 0, s>>>(cols[1][0], cols[2][0], n_rows, pp, coeffs, dinv, acc[0],
+                                                       acc[1], acc[2], acc[3]);
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e) {
@@ -555,7 +582,7 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
     }
     if (!st) {
       StageScope stage("Generation", s);
-      k_poseidon_trace<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_init, trace, lookups);
+      k_poseidon_trace<<<(uint32_t)((n + 31) / 32), 32 * PS_REPS, 0, s>>>((uint32_t)n, d_init, trace, lookups);
       note_launch();
       if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
     }

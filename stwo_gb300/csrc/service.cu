@@ -15,6 +15,7 @@
 #include <condition_variable>
 #include <deque>
 #include <thread>
+#include <algorithm>
 #include <unordered_map>
 
 namespace stwo {
@@ -216,8 +217,17 @@ stwo_status stwo_prove_batch(const stwo_proof_job* jobs, uint32_t n_jobs, uint32
   stwo_server srv = nullptr;
   stwo_status st = stwo_server_create(n_workers, hbm_budget_bytes, dev, &srv);
   if (st) return st;
+  // Largest jobs first (by their device-byte estimate, which grows with the work): a large proof
+  // submitted last would otherwise run alone at the end of the batch. Results stay in job order.
+  std::vector<uint32_t> order(n_jobs);
+  for (uint32_t i = 0; i < n_jobs; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t a, uint32_t b) { return job_hbm_bytes(jobs[a]) > job_hbm_bytes(jobs[b]); });
   std::vector<uint64_t> tickets(n_jobs);
-  for (uint32_t i = 0; i < n_jobs && st == STWO_OK; i++) st = stwo_server_submit(srv, &jobs[i], &tickets[i]);
+  for (uint32_t k = 0; k < n_jobs && st == STWO_OK; k++) {
+    const uint32_t i = order[k];
+    st = stwo_server_submit(srv, &jobs[i], &tickets[i]);
+  }
   for (uint32_t i = 0; i < n_jobs && st == STWO_OK; i++) st = stwo_server_wait(srv, tickets[i], &results[i]);
   stwo_server_destroy(srv);
   if (st) return st;
