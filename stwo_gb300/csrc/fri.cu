@@ -247,11 +247,19 @@ int32_t fri_decompose(const uint32_t* const src[4], uint32_t log_size, uint32_t*
 
 // ---------------------------------------------------------------- small-layer tail
 // The FRI layers of at most 2^FRI_TAIL_MAX_LOG points, in one single-block launch. Per layer:
-// Blake2s leaves of its four coordinate columns, the node levels up to the root (halving in the
-// block), the transcript step (mix the root, draw alpha) on the device channel, and the line
-// fold into the next layer. The results are the ones of the per-kernel path (the same Merkle
-// layout as DevMerkle, the same fold as k_fold_line); only the number of launches changes.
+// Blake2s leaves of its four coordinate columns, the node levels up to the root, the transcript
+// step (mix the root, draw alpha) on the device channel, and the line fold into the next layer.
+// The results are the ones of the per-kernel path (the same Merkle layout as DevMerkle, the same
+// fold as k_fold_line, the same channel as dchannel.cuh); only the schedule differs:
+//   - node levels read their children from shared memory (ping-pong buffers) and write each
+//     level to the tree in HBM for the decommitment; levels of at most 32 nodes run in warp 0
+//     with warp barriers only;
+//   - the fold of layer j hashes, in the same thread, the leaf of layer j + 1 it produced;
+//   - the transcript step uses the unrolled compression.
 constexpr uint32_t FRI_TAIL_MAX_LAYERS = 16;
+constexpr uint32_t FRI_TAIL_MAX_LOG = 10;
+constexpr uint32_t FRI_TAIL_THREADS = 1024;
+constexpr size_t FRI_TAIL_SMEM = (size_t)8 * 4 * ((1u << FRI_TAIL_MAX_LOG) + (1u << (FRI_TAIL_MAX_LOG - 1)));
 struct FriTailParams {
   uint32_t n_layers;
   uint32_t log[FRI_TAIL_MAX_LAYERS];           // layer j has 2^log[j] points
@@ -262,55 +270,142 @@ struct FriTailParams {
   uint32_t* alphas;                            // 8 words per layer: alpha, alpha^2
 };
 
-__global__ void __launch_bounds__(1024) k_fri_tail(FriTailParams p) {
+// Blake2s-256 of a message of `bytes` <= 64 bytes given as 16 words (zero padded): one final
+// compression. Out of line, so that the single thread or warp that runs the upper levels and the
+// transcript step executes one copy of the unrolled rounds and keeps it in the instruction cache.
+static __device__ __noinline__ void tail_hash(const uint32_t* w, uint32_t bytes, uint32_t* out) {
+  uint32_t h[8], m[16];
+#pragma unroll
+  for (int q = 0; q < 16; q++) m[q] = w[q];
+  b2s_init(h);
+  b2s_compress_lat(h, m, bytes, true);
+#pragma unroll
+  for (int q = 0; q < 8; q++) out[q] = h[q];
+}
+__device__ __forceinline__ void tail_hash64(const uint32_t w[16], uint32_t out[8]) { tail_hash(w, 64, out); }
+
+// Leaf hash of one point: its four coordinates as a 16-byte message.
+__device__ __forceinline__ void tail_leaf(const qm31& v, uint32_t* tree_leaf, uint32_t* s_leaf) {
+  uint32_t h[8], m[16];
+#pragma unroll
+  for (int q = 0; q < 16; q++) m[q] = 0u;
+  m[0] = v.a.a;
+  m[1] = v.a.b;
+  m[2] = v.b.a;
+  m[3] = v.b.b;
+  tail_hash(m, 16, h);
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    tree_leaf[q] = h[q];
+    s_leaf[q] = h[q];
+  }
+}
+
+// One node of level `out` from its children in shared memory `src`.
+__device__ __forceinline__ void tail_node(const uint32_t* src, uint32_t i, uint32_t* dst, uint32_t* tree_level) {
+  uint32_t m[16], h[8];
+#pragma unroll
+  for (int q = 0; q < 16; q++) m[q] = src[16 * i + q];
+  tail_hash64(m, h);
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    dst[8 * i + q] = h[q];
+    tree_level[8 * i + q] = h[q];
+  }
+}
+
+// mix_root then draw_felt of dchannel.cuh (d_ch_mix_root, d_ch_draw_base8), unrolled.
+__device__ qm31 tail_channel_step(DevChannel* c, const uint32_t* root) {
+  uint32_t w[16], d[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    w[i] = c->digest[i];
+    w[8 + i] = root[i];
+  }
+  tail_hash64(w, d);
+  uint32_t nlo = 0, nhi = 0;
+  uint32_t f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  bool ok = false;
+  for (int attempt = 0; attempt < 64 && !ok; attempt++) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) w[i] = d[i];
+    w[8] = nlo;
+    w[9] = nhi;
+#pragma unroll
+    for (int i = 10; i < 16; i++) w[i] = 0u;
+    if (++nlo == 0) nhi++;
+    uint32_t h[8];
+    tail_hash64(w, h);
+    ok = true;
+#pragma unroll
+    for (int i = 0; i < 8; i++) ok = ok && h[i] < 2u * P;
+    if (ok) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) f[i] = h[i] >= P ? h[i] - P : h[i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; i++) c->digest[i] = d[i];
+  c->n_sent_lo = nlo;
+  c->n_sent_hi = nhi;
+  if (!ok) c->error = 1u;
+  return qm31_from_u32(f[0], f[1], f[2], f[3]);
+}
+
+__global__ void __launch_bounds__(FRI_TAIL_THREADS) k_fri_tail(FriTailParams p) {
+  extern __shared__ uint32_t s_nodes[];
+  uint32_t* const s_a = s_nodes;                                    // levels k, k - 2, ...
+  uint32_t* const s_b = s_nodes + 8 * (1u << FRI_TAIL_MAX_LOG);     // levels k - 1, k - 3, ...
   __shared__ qm31 s_alpha;
+  const uint32_t tid = threadIdx.x;
+  // Leaves of the first layer, from its evaluation in HBM.
+  {
+    const uint32_t n = 1u << p.log[0];
+    const uint32_t* const* c = p.eval[0];
+    uint32_t* leaves = p.tree[0] + (size_t)8 * (n - 1);
+    for (uint32_t i = tid; i < n; i += blockDim.x)
+      tail_leaf(qm31_from_u32(c[0][i], c[1][i], c[2][i], c[3][i]), leaves + 8 * i, s_a + 8 * i);
+  }
+  __syncthreads();
   for (uint32_t j = 0; j < p.n_layers; j++) {
     const uint32_t k = p.log[j], n = 1u << k;
-    const uint32_t* const* c = p.eval[j];
     uint32_t* tree = p.tree[j];
-    uint32_t* leaves = tree + (size_t)8 * (n - 1);
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-      uint32_t h[8], m[16];
-      b2s_init(h);
-#pragma unroll
-      for (int q = 0; q < 16; q++) m[q] = 0u;
-      m[0] = c[0][i];
-      m[1] = c[1][i];
-      m[2] = c[2][i];
-      m[3] = c[3][i];
-      b2s_compress(h, m, 16, true);
-#pragma unroll
-      for (int q = 0; q < 8; q++) leaves[(size_t)8 * i + q] = h[q];
-    }
-    __syncthreads();
-    for (int lg = (int)k - 1; lg >= 0; lg--) {
+    uint32_t* src = s_a;
+    uint32_t* dst = s_b;
+    int lg = (int)k - 1;
+    for (; lg >= 5; lg--) {
       const uint32_t w = 1u << lg;
-      const uint32_t* child = tree + (size_t)8 * (2 * w - 1);
-      uint32_t* out = tree + (size_t)8 * (w - 1);
-      for (uint32_t i = threadIdx.x; i < w; i += blockDim.x) {
-        uint32_t h[8], m[16];
-#pragma unroll
-        for (int q = 0; q < 16; q++) m[q] = child[(size_t)16 * i + q];
-        b2s_init(h);
-        b2s_compress(h, m, 64, true);
-#pragma unroll
-        for (int q = 0; q < 8; q++) out[(size_t)8 * i + q] = h[q];
-      }
+      for (uint32_t i = tid; i < w; i += blockDim.x) tail_node(src, i, dst, tree + (size_t)8 * (w - 1));
       __syncthreads();
+      uint32_t* t = src;
+      src = dst;
+      dst = t;
     }
-    if (threadIdx.x == 0) {
-      d_ch_mix_root(p.ch, tree);
-      const qm31 a = d_ch_draw_felt(p.ch);
-      const qm31 a2 = qm31_mul(a, a);
-      uint32_t* o = p.alphas + 8 * j;
-      o[0] = a.a.a; o[1] = a.a.b; o[2] = a.b.a; o[3] = a.b.b;
-      o[4] = a2.a.a; o[5] = a2.a.b; o[6] = a2.b.a; o[7] = a2.b.b;
-      s_alpha = a;
+    if (tid < 32) {
+      for (; lg >= 0; lg--) {
+        const uint32_t w = 1u << lg;
+        if (tid < w) tail_node(src, tid, dst, tree + (size_t)8 * (w - 1));
+        __syncwarp();
+        uint32_t* t = src;
+        src = dst;
+        dst = t;
+      }
+      if (tid == 0) {
+        const qm31 a = tail_channel_step(p.ch, src);
+        const qm31 a2 = qm31_mul(a, a);
+        uint32_t* o = p.alphas + 8 * j;
+        o[0] = a.a.a; o[1] = a.a.b; o[2] = a.b.a; o[3] = a.b.b;
+        o[4] = a2.a.a; o[5] = a2.a.b; o[6] = a2.b.a; o[7] = a2.b.b;
+        s_alpha = a;
+      }
     }
     __syncthreads();
     const qm31 alpha = s_alpha;
+    const uint32_t* const* c = p.eval[j];
     uint32_t* const* nxt = const_cast<uint32_t* const*>(p.eval[j + 1]);
-    for (uint32_t i = threadIdx.x; i < n / 2; i += blockDim.x) {
+    const bool next_in_tail = j + 1 < p.n_layers;
+    uint32_t* next_leaves = next_in_tail ? p.tree[j + 1] + (size_t)8 * (n / 2 - 1) : nullptr;
+    for (uint32_t i = tid; i < n / 2; i += blockDim.x) {
       qm31 f0 = qm31_from_u32(c[0][2 * i], c[1][2 * i], c[2][2 * i], c[3][2 * i]);
       qm31 f1 = qm31_from_u32(c[0][2 * i + 1], c[1][2 * i + 1], c[2][2 * i + 1], c[3][2 * i + 1]);
       ibfly_q(f0, f1, p.itw[j][i]);
@@ -319,6 +414,7 @@ __global__ void __launch_bounds__(1024) k_fri_tail(FriTailParams p) {
       nxt[1][i] = r.a.b;
       nxt[2][i] = r.b.a;
       nxt[3][i] = r.b.b;
+      if (next_in_tail) tail_leaf(r, next_leaves + 8 * i, s_a + 8 * i);
     }
     __syncthreads();
   }
@@ -335,6 +431,8 @@ int32_t fri_tail(const TwiddleTree* tree, const std::vector<stwo_coset>& doms,
   p.n_layers = (uint32_t)doms.size();
   for (size_t j = 0; j < doms.size(); j++) {
     STWO_REQUIRE(doms[j].log_size >= 1, "Evaluation too small");
+    STWO_REQUIRE(doms[j].log_size <= FRI_TAIL_MAX_LOG, "FRI tail layer of 2^%u points", doms[j].log_size);
+    STWO_REQUIRE(j == 0 || doms[j].log_size + 1 == doms[j - 1].log_size, "FRI tail layers must halve");
     size_t off;
     STWO_REQUIRE(level_offset(tree, doms[j], &off), "line domain is not a doubling of the twiddle root");
     p.log[j] = doms[j].log_size;
@@ -345,7 +443,10 @@ int32_t fri_tail(const TwiddleTree* tree, const std::vector<stwo_coset>& doms,
     for (int k = 0; k < 4; k++) p.eval[j][k] = evals[j][k];
   p.ch = ch;
   p.alphas = alphas;
-  k_fri_tail<<<1, 1024, 0, s>>>(p);
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(k_fri_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FRI_TAIL_SMEM);
+  STWO_CHECK_CUDA(attr);
+  k_fri_tail<<<1, FRI_TAIL_THREADS, FRI_TAIL_SMEM, s>>>(p);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;

@@ -40,7 +40,7 @@ int32_t fri_tail(const TwiddleTree* tree, const std::vector<stwo_coset>& doms,
                  const std::vector<std::array<uint32_t*, 4>>& evals, const std::vector<uint32_t*>& trees,
                  DevChannel* ch, uint32_t* alphas, cudaStream_t s);
 // FRI layers of at most 2^FRI_TAIL_LOG points run in the single-launch tail (fri_tail).
-constexpr uint32_t FRI_TAIL_LOG = 12;
+constexpr uint32_t FRI_TAIL_LOG = 10;
 int32_t channel_set(DevChannel* ch, const uint32_t digest[8], uint64_t n_sent, cudaStream_t s);
 
 // Copies segments of device words into one destination (mapped host memory) in one launch.

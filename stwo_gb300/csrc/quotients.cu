@@ -158,19 +158,19 @@ __global__ void __launch_bounds__(256) k_quotient_rows(uint32_t rows, uint32_t l
       if (live) {
         uint32_t cnt = 0;
         uint32_t i = slice;
-        // Four independent column loads in flight per iteration.
-        for (; i + 3 * Q_SLICES < ne; i += 4 * Q_SLICES) {
-          uint32_t v[4];
+        // Eight independent column loads in flight per iteration.
+        for (; i + 7 * Q_SLICES < ne; i += 8 * Q_SLICES) {
+          uint32_t v[8];
 #pragma unroll
-          for (int u = 0; u < 4; u++) v[u] = __ldg(st[i + u * Q_SLICES].col + r);
+          for (int u = 0; u < 8; u++) v[u] = __ldg(st[i + u * Q_SLICES].col + r);
 #pragma unroll
-          for (int u = 0; u < 4; u++) {
+          for (int u = 0; u < 8; u++) {
             const QStage& q = st[i + u * Q_SLICES];
             s0 += (unsigned long long)q.c[0] * v[u];
             s1 += (unsigned long long)q.c[1] * v[u];
             s2 += (unsigned long long)q.c[2] * v[u];
             s3 += (unsigned long long)q.c[3] * v[u];
-            if (u == 1 || u == 3) {
+            if (u & 1) {
               s0 = fold64(s0);
               s1 = fold64(s1);
               s2 = fold64(s2);
