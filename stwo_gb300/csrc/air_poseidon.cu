@@ -472,8 +472,10 @@ struct PoseidonGpuAir : GpuAir {
   }
   // The same constraints over QM31 at the OODS point (PointEvaluator).
   hq eval_at_point(const std::vector<std::vector<std::vector<hq>>>& mask, hq rc, hq denom_inv) const override {
+    // The PointEvaluator accumulation acc <- acc * rc + denom_inv * c, with denom_inv factored out
+    // of the sum (one product per constraint fewer, the same field element).
     hq acc = hq_make(0, 0, 0, 0);
-    auto add = [&](hq c) { acc = hq_add(hq_mul(acc, rc), hq_mul(denom_inv, c)); };
+    auto add = [&](hq c) { acc = hq_add(hq_mul(acc, rc), c); };
     auto m4 = [](hq* x) {
       hq t0 = hq_add(x[0], x[1]), t02 = hq_add(t0, t0), t1 = hq_add(x[2], x[3]), t12 = hq_add(t1, t1);
       hq t2 = hq_add(hq_add(x[1], x[1]), t1), t3 = hq_add(hq_add(x[3], x[3]), t0);
@@ -547,7 +549,7 @@ struct PoseidonGpuAir : GpuAir {
       }
       add(hq_sub(hq_mul(diff, fr[b].second), fr[b].first));
     }
-    return acc;
+    return hq_mul(acc, denom_inv);
   }
 };
 

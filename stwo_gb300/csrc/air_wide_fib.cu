@@ -100,11 +100,11 @@ struct WideFibGpuAir : GpuAir {
     for (uint32_t i = 2; i < n_cols; i++) {
       hq c = t[i][0];
       hq cons = hq_sub(c, hq_add(hq_mul(a, a), hq_mul(b, b)));
-      acc = hq_add(hq_mul(acc, rc), hq_mul(denom_inv, cons));
+      acc = hq_add(hq_mul(acc, rc), cons);  // denom_inv factored out of the sum
       a = b;
       b = c;
     }
-    return acc;
+    return hq_mul(acc, denom_inv);
   }
 };
 

@@ -16,7 +16,10 @@ struct MerkleCols { const uint32_t* p[MERKLE_MAX_COLS]; };
 
 // Hashes nodes [0, n_nodes) of a layer. When `n_cols` spans several launches the running
 // chaining value and byte count persist in `state` (8 words + 1 per node); `first`/`last`
-// mark the launch that starts / finishes the message.
+// mark the launch that starts / finishes the message. LAT: a layer too small to fill the GPU,
+// whose threads each run their chain of compressions with little else to overlap, uses the
+// latency-oriented compression (every addition on the FMA pipe).
+template <bool LAT>
 __global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const uint32_t* __restrict__ prev,
                                                       MerkleCols cols, uint32_t n_cols, uint32_t* __restrict__ out,
                                                       uint32_t* __restrict__ state, uint32_t first, uint32_t last,
@@ -58,7 +61,8 @@ __global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const ui
 #pragma unroll
     for (int q = 0; q < 16; q++) m[q] = (uint32_t)q < k ? __ldg(cols.p[c + q] + i) : 0u;
     t += 4 * k;
-    b2s_compress_fma(h, m, t, fin, one);
+    if (LAT) b2s_compress_lat(h, m, t, fin);
+    else b2s_compress_fma(h, m, t, fin, one);
     c += k;
   }
   if (last) {
@@ -71,6 +75,9 @@ __global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const ui
     state[(size_t)9 * i + 8] = t;
   }
 }
+
+// Layers of at most this many nodes (under two warps per SM) take the latency-oriented kernel.
+constexpr uint32_t MERKLE_LAT_NODES = 8192;
 
 int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols, uint32_t n_cols,
                             uint32_t* out, cudaStream_t s) {
@@ -94,7 +101,11 @@ int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint3
     uint32_t nc = n_cols - c0 < per_launch ? n_cols - c0 : per_launch;
     MerkleCols mc;
     for (uint32_t q = 0; q < nc; q++) mc.p[q] = cols[c0 + q];
-    k_merkle_layer<<<blocks, threads, 0, s>>>(n, prev, mc, nc, out, state, l == 0, l + 1 == n_launch, 1u); note_launch();
+    if (n <= MERKLE_LAT_NODES)
+      k_merkle_layer<true><<<blocks, threads, 0, s>>>(n, prev, mc, nc, out, state, l == 0, l + 1 == n_launch, 1u);
+    else
+      k_merkle_layer<false><<<blocks, threads, 0, s>>>(n, prev, mc, nc, out, state, l == 0, l + 1 == n_launch, 1u);
+    note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       scratch_free(state, s);

@@ -390,6 +390,7 @@ int32_t Prover::commit_evals(const std::vector<uint32_t*>& cols, uint32_t log_si
 }
 
 Prover::Prover(const stwo_pcs_config& c, uint32_t max_log, cudaStream_t st) : cfg(c), s(st), arena(st) {
+  StageScope stage("Setup", s);
   init_status = get_tree(canonic_half_coset(max_log), s, &tree);
 }
 Prover::~Prover() = default;
@@ -829,6 +830,7 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   if (st) return st;
 
   // Canonical bytes: config, commitments, sampled values, decommitments, queried values, pow, FRI.
+  StageScope stage_out("Proof assembly", s);
   ByteWriter w;
   write_config(w, cfg);
   w.u64(trees.size());
