@@ -55,15 +55,35 @@ __global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const ui
     t = state[(size_t)9 * i + 8];
   }
   uint32_t c = 0;
-  while (c < n_cols) {
-    uint32_t k = n_cols - c < 16 ? n_cols - c : 16;
-    bool fin = last && (c + k == n_cols);
+  if (LAT) {
+    // Few threads: the next 16 column words are fetched while the current block compresses.
+    uint32_t nx[16];
+    auto fetch = [&](uint32_t c0) {
+      const uint32_t kk = n_cols - c0 < 16 ? n_cols - c0 : 16;
 #pragma unroll
-    for (int q = 0; q < 16; q++) m[q] = (uint32_t)q < k ? __ldg(cols.p[c + q] + i) : 0u;
-    t += 4 * k;
-    if (LAT) b2s_compress_lat(h, m, t, fin);
-    else b2s_compress_fma(h, m, t, fin, one);
-    c += k;
+      for (int q = 0; q < 16; q++) nx[q] = (uint32_t)q < kk ? __ldg(cols.p[c0 + q] + i) : 0u;
+    };
+    if (n_cols) fetch(0);
+    while (c < n_cols) {
+      const uint32_t k = n_cols - c < 16 ? n_cols - c : 16;
+      const bool fin = last && (c + k == n_cols);
+#pragma unroll
+      for (int q = 0; q < 16; q++) m[q] = nx[q];
+      if (c + k < n_cols) fetch(c + k);
+      t += 4 * k;
+      b2s_compress_lat(h, m, t, fin);
+      c += k;
+    }
+  } else {
+    while (c < n_cols) {
+      uint32_t k = n_cols - c < 16 ? n_cols - c : 16;
+      bool fin = last && (c + k == n_cols);
+#pragma unroll
+      for (int q = 0; q < 16; q++) m[q] = (uint32_t)q < k ? __ldg(cols.p[c + q] + i) : 0u;
+      t += 4 * k;
+      b2s_compress_fma(h, m, t, fin, one);
+      c += k;
+    }
   }
   if (last) {
     uint4* po = reinterpret_cast<uint4*>(out + (size_t)8 * i);
@@ -94,8 +114,10 @@ int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint3
     int32_t st = scratch_alloc((void**)&state, (size_t)n * 9 * 4, s);
     if (st) return st;
   }
-  uint32_t threads = 256;
-  uint32_t blocks = (n + threads - 1) / threads;
+  // A small layer goes out as one-warp blocks, so that its few warps land on different SMs
+  // instead of sharing the issue slots of one.
+  const uint32_t threads = n <= MERKLE_LAT_NODES ? 32 : 256;
+  const uint32_t blocks = (n + threads - 1) / threads;
   for (uint32_t l = 0; l < n_launch; l++) {
     uint32_t c0 = l * per_launch;
     uint32_t nc = n_cols - c0 < per_launch ? n_cols - c0 : per_launch;

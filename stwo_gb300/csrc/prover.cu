@@ -16,7 +16,6 @@
 #include "prover.cuh"
 #include "dchannel.cuh"
 #include <array>
-#include <future>
 #include <set>
 
 namespace stwo {
@@ -143,11 +142,6 @@ int32_t Gather::run(cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------------------------------------
-static uint32_t ilog2u(size_t n) {
-  uint32_t l = 0;
-  while (((size_t)1 << (l + 1)) <= n) l++;
-  return l;
-}
 
 int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root,
                           DevChannel* ch, uint32_t* alpha_out) {
@@ -311,7 +305,6 @@ static void fri_positions_and_witness(const SecureCols& col, const std::vector<s
   }
 }
 
-static qm31 to_dq(hq x) { return {{x.v[0], x.v[1]}, {x.v[2], x.v[3]}}; }
 static stwo_qm31 to_sq(hq x) { stwo_qm31 r; for (int i = 0; i < 4; i++) r.v[i] = x.v[i]; return r; }
 static hq from_sq(const stwo_qm31& x) { return hq_make(x.v[0], x.v[1], x.v[2], x.v[3]); }
 
@@ -540,21 +533,26 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   ch.mix_felts(flat);
 
   // Sanity check of the composition at the OODS point (prover/mod.rs:70-76). It is host
-  // arithmetic only, so it runs on another host thread while the stream computes the quotients
-  // and the FRI layers; its verdict is collected before the proof is written.
-  std::future<bool> sanity;
+  // arithmetic only, so it runs once every quotient and FRI kernel has been enqueued, just before
+  // the host waits for the FRI results: the stream works meanwhile. Its verdict is checked before
+  // the proof is written (the reference returns the same error earlier, with no proof either).
+  struct OodsCheck {
+    std::vector<std::vector<std::vector<hq>>> mv;
+    hq dinv, lhs;
+    bool done = false, ok = true;
+  } check;
   {
-    std::vector<std::vector<std::vector<hq>>> mv(trees.size() - 1);
+    check.mv.resize(trees.size() - 1);
     size_t k = 0;
     for (size_t t = 0; t + 1 < trees.size(); t++) {
-      mv[t].resize(pts[t].size());
+      check.mv[t].resize(pts[t].size());
       for (size_t c = 0; c < pts[t].size(); c++)
-        for (size_t j = 0; j < pts[t][c].size(); j++) mv[t][c].push_back(flat[k++]);
+        check.mv[t][c].assign(flat.begin() + k, flat.begin() + k + pts[t][c].size()), k += pts[t][c].size();
     }
     hq comp[4];
     for (int i = 0; i < 4; i++) comp[i] = flat[k++];
-    hq lhs = hq_add(hq_add(comp[0], hq_mul(comp[1], hq_make(0, 1, 0, 0))),
-                    hq_add(hq_mul(comp[2], hq_make(0, 0, 1, 0)), hq_mul(comp[3], hq_make(0, 0, 0, 1))));
+    check.lhs = hq_add(hq_add(comp[0], hq_mul(comp[1], hq_make(0, 1, 0, 0))),
+                       hq_add(hq_mul(comp[2], hq_make(0, 0, 1, 0)), hq_mul(comp[3], hq_make(0, 0, 0, 1))));
     // denom inverse 1 / coset_vanishing(CanonicCoset(log).coset, oods)
     stwo_coset tc = coset_new(1u << (31 - (air.log_size() + 1)), air.log_size());
     hpoint init = h_index_to_point(tc.initial_index);
@@ -563,19 +561,14 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     HPointQ q = hpq_add_m31(oods, shift);
     hq x = q.x;
     for (uint32_t i = 1; i < air.log_size(); i++) x = hq_sub(hq_add(hq_mul(x, x), hq_mul(x, x)), hq_make(1, 0, 0, 0));
-    hq dinv = hq_inv(x);
-    sanity = std::async(std::launch::async, [&air, mv = std::move(mv), rc, dinv, lhs]() {
-      hq rhs = air.eval_at_point(mv, rc, dinv);
-      return std::memcmp(lhs.v, rhs.v, sizeof(lhs.v)) == 0;
-    });
+    check.dinv = hq_inv(x);
   }
-  // Every return below first waits for the check (it reads `air`).
-  struct JoinCheck {
-    std::future<bool>& f;
-    ~JoinCheck() {
-      if (f.valid()) f.wait();
-    }
-  } join_check{sanity};
+  auto run_check = [&]() {
+    if (check.done) return;
+    const hq rhs = air.eval_at_point(check.mv, rc, check.dinv);
+    check.ok = std::memcmp(check.lhs.v, rhs.v, sizeof(rhs.v)) == 0;
+    check.done = true;
+  };
 
   // FRI quotients per log size, descending (pcs/quotients.rs:76-101).
   struct ColS { const uint32_t* p; uint32_t log; std::vector<std::pair<HPointQ, hq>> samples; };
@@ -753,6 +746,7 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     k_collect<<<1, 256, 0, s>>>(cl, mp.dev);
     note_launch();
     STWO_LAUNCH_CHECK();
+    run_check();
     STWO_CHECK_CUDA(cudaStreamSynchronize(s));
     const uint32_t* w = mp.host;
     first_tree.root = Digest::from_words(w);
@@ -866,7 +860,8 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   }
   w.u64(coeffs.size());
   for (auto& c : coeffs) w.q(c);
-  if (!sanity.get()) {
+  run_check();
+  if (!check.ok) {
     set_error("ConstraintsNotSatisfied");
     return STWO_ERR_INVALID_ARG;
   }
