@@ -293,7 +293,7 @@ __device__ __forceinline__ uint32_t prev_row_index(uint32_t r, uint32_t trace_lo
 // loads the coefficient table once per block.
 constexpr uint32_t PC_ROWS = 32;
 constexpr uint32_t PC_THREADS = 32 * PS_REPS;
-constexpr uint32_t PC_BLOCKS_PER_SM = 4;
+constexpr uint32_t PC_BLOCKS_PER_SM = 3;  // 85 registers: the rounds run without spills
 
 __global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
     k_poseidon_composition(const uint32_t* __restrict__ trace, const uint32_t* __restrict__ inter, uint32_t n_rows,
@@ -354,9 +354,13 @@ __global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
     // on instruction fetch.
 #pragma unroll 1
     for (int round = 0; round < PS_HALF; round++) full_round();
+    // A partial round has little arithmetic to hide its one load behind: the mask of the next
+    // round is fetched one round ahead.
+    uint32_t m_next = col(trace, mc, r);
 #pragma unroll 1
     for (int round = 0; round < PS_PARTIAL; round++) {
-      const uint32_t m = col(trace, mc + round, r);
+      const uint32_t m = m_next;
+      if (round + 1 < PS_PARTIAL) m_next = col(trace, mc + round + 1, r);
       s[0] = m31_add(s[0], PS_RC);
       internal_matrix(s);
       acc(m31_sub(pow5(s[0]), m));
