@@ -229,6 +229,14 @@ class PoseidonWorkload:
         self.proof, self.claimed_sum = prove_poseidon(self.LOG, src, self.CFG)
         return self.proof
 
+    # DRAM bytes (read + write) of the composition extension's kernels in one proof of 2^14 rows,
+    # from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); traffic grows with the rows.
+    COMPOSITION_EXT_TRAFFIC_2E14 = 836.6e6
+
+    def stage_traffic(self):
+        """Measured DRAM traffic of the stages that have an ncu capture, scaled to 2^LOG rows."""
+        return {"Composition extension": self.COMPOSITION_EXT_TRAFFIC_2E14 * (1 << self.LOG) / (1 << 14)}
+
     def stage_bytes(self):
         """Algorithmic HBM bytes of the HBM-bound stages (reads + writes of the column data)."""
         n = 1 << self.LOG
@@ -676,7 +684,10 @@ def run_gb300(args):
     if dom:
         ach = sbytes[dom] / (hbm_stages[dom] / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": sbytes[dom],
+                "peak_kind": peak_kind, "traffic": wl.stage_traffic().get(dom),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels at "
+                                  "2^14 rows, scaled by the rows (2-pass FFT: intermediate written and re-read)",
+                "algorithmic_bytes_per_launch": sbytes[dom],
                 "stage_ms": hbm_stages[dom]}
     line = {
         "metric": "proof s & trace cells/s (Poseidon2 2^16 rows)",
