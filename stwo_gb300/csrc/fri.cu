@@ -11,6 +11,7 @@
 // Each kernel is one streaming pass over four coordinate columns: HBM-bound.
 #include "common.cuh"
 #include <array>
+#include <mutex>
 #include "blake2s.cuh"
 #include "dchannel.cuh"
 
@@ -52,14 +53,35 @@ __device__ __forceinline__ void load_alpha(const uint32_t* alpha_dev, qm31& alph
   if (alpha_sq) *alpha_sq = qm31_from_u32(__ldg(alpha_dev + 4), __ldg(alpha_dev + 5), __ldg(alpha_dev + 6), __ldg(alpha_dev + 7));
 }
 
+// Merkle leaf of one folded point for the next FRI layer's tree: BLAKE2s-256 of its four
+// coordinates (16 bytes), the node k_merkle_layer computes for a layer of four columns and no
+// children. `leaves` may be null (the next layer is hashed elsewhere).
+__device__ __forceinline__ void fold_leaf(uint32_t* leaves, uint32_t i, const qm31& v) {
+  if (!leaves) return;
+  uint32_t h[8], m[16];
+#pragma unroll
+  for (int q = 0; q < 16; q++) m[q] = 0u;
+  m[0] = v.a.a;
+  m[1] = v.a.b;
+  m[2] = v.b.a;
+  m[3] = v.b.b;
+  b2s_init(h);
+  b2s_compress(h, m, 16, true);
+  uint4* po = reinterpret_cast<uint4*>(leaves + (size_t)8 * i);
+  po[0] = make_uint4(h[0], h[1], h[2], h[3]);
+  po[1] = make_uint4(h[4], h[5], h[6], h[7]);
+}
+
 __global__ void k_fold_line(Secure4 src, Secure4M dst, uint32_t n_out, const uint32_t* __restrict__ itw_level,
-                            qm31 alpha, const uint32_t* alpha_dev) {
+                            qm31 alpha, const uint32_t* alpha_dev, uint32_t* leaves) {
   load_alpha(alpha_dev, alpha, nullptr);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
     qm31 f0, f1;
     load_pair(src, i, f0, f1);
     ibfly_q(f0, f1, __ldg(itw_level + i));
-    store_q(dst, i, qm31_add(f0, qm31_mul(alpha, f1)));
+    const qm31 r = qm31_add(f0, qm31_mul(alpha, f1));
+    store_q(dst, i, r);
+    fold_leaf(leaves, i, r);
   }
 }
 
@@ -67,7 +89,7 @@ __global__ void k_fold_line(Secure4 src, Secure4M dst, uint32_t n_out, const uin
 // n >= 3. For n <= 2 the y-coordinates come from the domain points directly.
 __global__ void k_fold_circle(Secure4 src, Secure4M dst, uint32_t n_out, const uint32_t* __restrict__ itw_level,
                               uint32_t log_src, uint32_t half_init, uint32_t half_step, qm31 alpha, qm31 alpha_sq,
-                              const uint32_t* alpha_dev) {
+                              const uint32_t* alpha_dev, uint32_t* leaves) {
   load_alpha(alpha_dev, alpha, &alpha_sq);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
     uint32_t yinv;
@@ -86,7 +108,9 @@ __global__ void k_fold_circle(Secure4 src, Secure4M dst, uint32_t n_out, const u
     ibfly_q(f0, f1, yinv);
     qm31 fp = qm31_add(qm31_mul(alpha, f1), f0);
     qm31 d = qm31_from_u32(dst.p[0][i], dst.p[1][i], dst.p[2][i], dst.p[3][i]);
-    store_q(dst, i, qm31_add(qm31_mul(d, alpha_sq), fp));
+    const qm31 r = qm31_add(qm31_mul(d, alpha_sq), fp);
+    store_q(dst, i, r);
+    fold_leaf(leaves, i, r);
   }
 }
 
@@ -176,21 +200,23 @@ static bool level_offset(const TwiddleTree* t, stwo_coset c, size_t* off) {
 }
 
 int32_t fri_fold_line(const TwiddleTree* tree, stwo_coset line_domain, const uint32_t* const src[4],
-                      qm31 alpha, uint32_t* const out[4], cudaStream_t s, const uint32_t* alpha_dev) {
+                      qm31 alpha, uint32_t* const out[4], cudaStream_t s, const uint32_t* alpha_dev,
+                      uint32_t* leaves) {
   STWO_REQUIRE(line_domain.log_size >= 1, "Evaluation too small");
   size_t off;
   STWO_REQUIRE(level_offset(tree, line_domain, &off), "line domain is not a doubling of the twiddle root");
   uint32_t n_out = 1u << (line_domain.log_size - 1);
   Secure4 sp{{src[0], src[1], src[2], src[3]}};
   Secure4M dp{{out[0], out[1], out[2], out[3]}};
-  k_fold_line<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, tree->d_itw + off, alpha, alpha_dev);
+  k_fold_line<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, tree->d_itw + off, alpha, alpha_dev, leaves);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
 }
 
 int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* const dst[4],
-                        const uint32_t* const src[4], qm31 alpha, cudaStream_t s, const uint32_t* alpha_dev) {
+                        const uint32_t* const src[4], qm31 alpha, cudaStream_t s, const uint32_t* alpha_dev,
+                        uint32_t* leaves) {
   uint32_t log_src = half.log_size + 1;
   size_t off = 0;
   const uint32_t* lvl = nullptr;
@@ -215,7 +241,7 @@ int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* cons
   uint32_t rb0 = h_sub(h_add(bb0, bb0), bb1), rb1 = h_add(bb0, h_add(bb1, bb1));
   qm31 a2 = {{h_add(aa0, rb0), h_add(aa1, rb1)}, {h_add(ab0, ab0), h_add(ab1, ab1)}};
   k_fold_circle<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, lvl, log_src, half.initial_index,
-                                                     half.step_size, alpha, a2, alpha_dev);
+                                                     half.step_size, alpha, a2, alpha_dev, leaves);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
@@ -443,9 +469,20 @@ int32_t fri_tail(const TwiddleTree* tree, const std::vector<stwo_coset>& doms,
     for (int k = 0; k < 4; k++) p.eval[j][k] = evals[j][k];
   p.ch = ch;
   p.alphas = alphas;
-  static const cudaError_t attr =
-      cudaFuncSetAttribute(k_fri_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FRI_TAIL_SMEM);
-  STWO_CHECK_CUDA(attr);
+  // The 48 KB of dynamic shared memory needs the opt-in attribute, once per device.
+  {
+    static std::mutex mu;
+    static bool done[256] = {};
+    int dev = 0;
+    STWO_CHECK_CUDA(cudaGetDevice(&dev));
+    STWO_REQUIRE(dev >= 0 && dev < 256, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> g(mu);
+    if (!done[dev]) {
+      STWO_CHECK_CUDA(
+          cudaFuncSetAttribute(k_fri_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FRI_TAIL_SMEM));
+      done[dev] = true;
+    }
+  }
   k_fri_tail<<<1, FRI_TAIL_THREADS, FRI_TAIL_SMEM, s>>>(p);
   note_launch();
   STWO_LAUNCH_CHECK();
@@ -476,13 +513,14 @@ extern "C" {
 
 stwo_status stwo_fri_fold_line(stwo_twiddle_tree tree, stwo_coset line_domain, const uint32_t* const d_eval[4],
                                stwo_qm31 alpha, uint32_t* const d_out[4], void* stream) {
-  return fri_fold_line(tree_of(tree), line_domain, d_eval, to_q(alpha), d_out, as_stream(stream), nullptr);
+  return fri_fold_line(tree_of(tree), line_domain, d_eval, to_q(alpha), d_out, as_stream(stream), nullptr, nullptr);
 }
 
 stwo_status stwo_fri_fold_circle_into_line(stwo_twiddle_tree tree, stwo_coset src_half_coset,
                                            uint32_t* const d_dst[4], const uint32_t* const d_src[4],
                                            stwo_qm31 alpha, void* stream) {
-  return fri_fold_circle(tree_of(tree), src_half_coset, d_dst, d_src, to_q(alpha), as_stream(stream), nullptr);
+  return fri_fold_circle(tree_of(tree), src_half_coset, d_dst, d_src, to_q(alpha), as_stream(stream), nullptr,
+                         nullptr);
 }
 
 stwo_status stwo_fri_decompose(const uint32_t* const d_eval[4], uint32_t log_size, uint32_t* const d_g[4],

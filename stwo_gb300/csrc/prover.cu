@@ -30,10 +30,12 @@ int32_t merkle_node_layers(const uint32_t* prev, uint32_t first_log, uint32_t n_
 int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, stwo_qm31 rc_in,
                              const stwo_sample_batch* batches, uint32_t n_batches, uint32_t log_blowup,
                              uint32_t* const out[4], cudaStream_t s);
+// With `leaves` set, the fold also writes the Merkle leaves of the next FRI layer (8 words per
+// folded point), so that layer's tree starts at its first node level.
 int32_t fri_fold_line(const TwiddleTree* tree, stwo_coset line_domain, const uint32_t* const src[4], qm31 alpha,
-                      uint32_t* const out[4], cudaStream_t s, const uint32_t* alpha_dev);
+                      uint32_t* const out[4], cudaStream_t s, const uint32_t* alpha_dev, uint32_t* leaves);
 int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* const dst[4], const uint32_t* const src[4],
-                        qm31 alpha, cudaStream_t s, const uint32_t* alpha_dev);
+                        qm31 alpha, cudaStream_t s, const uint32_t* alpha_dev, uint32_t* leaves);
 int32_t fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_t* alpha_out, cudaStream_t s);
 int32_t fri_tail(const TwiddleTree* tree, const std::vector<stwo_coset>& doms,
                  const std::vector<std::array<uint32_t*, 4>>& evals, const std::vector<uint32_t*>& trees,
@@ -185,6 +187,25 @@ int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cuda
   STWO_CHECK_CUDA(cudaMemcpyAsync(mp.host, layers[0], 32, cudaMemcpyDeviceToHost, s));
   STWO_CHECK_CUDA(cudaStreamSynchronize(s));
   root = Digest::from_words(mp.host);
+  return STWO_OK;
+}
+
+// The tree of columns whose leaf hashes are already in `all` (the layout of commit: layer lg at
+// offset 8 (2^lg - 1)): only the node levels run, the last launch also taking the transcript step.
+int32_t DevMerkle::commit_from_leaves(const std::vector<ColRef>& columns, uint32_t* all, cudaStream_t s,
+                                      DevChannel* ch, uint32_t* alpha_out) {
+  STWO_REQUIRE(!columns.empty() && all, "commit_from_leaves: no columns");
+  const uint32_t k = columns[0].log;
+  for (const ColRef& c : columns) STWO_REQUIRE(c.log == k, "commit_from_leaves: mixed column sizes");
+  STWO_REQUIRE(k >= 1, "commit_from_leaves: a tree of one leaf");
+  sorted = columns;
+  layers.assign(k + 1, nullptr);
+  for (uint32_t lg = 0; lg <= k; lg++) layers[lg] = all + (size_t)8 * ((1ull << lg) - 1);
+  std::vector<uint32_t*> outs;
+  for (int lg = (int)k - 1; lg >= 0; lg--) outs.push_back(layers[lg]);
+  int32_t st = merkle_node_layers(layers[k], k - 1, k, outs.data(), s, ch, alpha_out);
+  if (st) return st;
+  channel_fused = ch != nullptr;
   return STWO_OK;
 }
 
@@ -660,12 +681,25 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     STWO_CHECK_CUDA(cudaMemsetAsync(cur.c[k], 0, ((size_t)4) << dom.log_size, s));
   }
   const qm31 unused_alpha = {{0u, 0u}, {0u, 0u}};
+  size_t last_size = (size_t)1 << (cfg.log_last_layer_degree_bound + cfg.log_blowup_factor);
+  // A layer of 2^k points committed by the multi-block kernels (not the last layer, not in the
+  // tail) gets its tree buffer before the fold that completes it, and that fold writes its leaves.
+  auto tree_for = [&](uint32_t k, size_t next_after, uint32_t** out) -> int32_t {
+    *out = nullptr;
+    if (((size_t)1 << k) <= last_size) return STWO_OK;
+    if (k <= FRI_TAIL_LOG && next_after == quotients.size()) return STWO_OK;
+    *out = arena.alloc((size_t)8 * ((2ull << k) - 1));
+    return *out ? STWO_OK : STWO_ERR_OOM;
+  };
+  auto leaves_of = [](uint32_t* tbuf, uint32_t k) { return tbuf ? tbuf + (size_t)8 * ((1ull << k) - 1) : nullptr; };
   size_t next = 0;
+  uint32_t* pending_tree = nullptr;
+  st = tree_for(dom.log_size, 1, &pending_tree);
+  if (st) return st;
   st = fri_fold_circle(tree, canonic_half_coset(qlogs[0]), cur.c, const_cast<const uint32_t* const*>(quotients[0].c),
-                       unused_alpha, s, alphas + 8 * fstep);
+                       unused_alpha, s, alphas + 8 * fstep, leaves_of(pending_tree, dom.log_size));
   if (st) return st;
   next = 1;
-  size_t last_size = (size_t)1 << (cfg.log_last_layer_degree_bound + cfg.log_blowup_factor);
   while (((size_t)1 << dom.log_size) > last_size) {
     if (dom.log_size <= FRI_TAIL_LOG && next == quotients.size()) {
       // The remaining small layers: buffers laid out as the per-kernel path would, one launch.
@@ -703,7 +737,12 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     std::vector<ColRef> lc;
     for (int k = 0; k < 4; k++) lc.push_back({cur.c[k], dom.log_size});
     STWO_REQUIRE(++fstep < FRI_MAX_STEPS, "too many FRI layers");
-    st = L.merkle.commit(lc, arena, s, false, dch, alphas + 8 * fstep);
+    if (pending_tree) {
+      st = L.merkle.commit_from_leaves(lc, pending_tree, s, dch, alphas + 8 * fstep);
+      pending_tree = nullptr;
+    } else {
+      st = L.merkle.commit(lc, arena, s, false, dch, alphas + 8 * fstep);
+    }
     if (st) return st;
     if (!L.merkle.channel_fused) st = fri_channel_step(dch, L.merkle.layers[0], alphas + 8 * fstep, s);
     if (st) return st;
@@ -712,16 +751,24 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
       nxt.c[k] = arena.alloc((size_t)1 << (dom.log_size - 1));
       if (!nxt.c[k]) return STWO_ERR_OOM;
     }
+    const uint32_t next_log = dom.log_size - 1;
+    const bool inject = next < quotients.size() && qlogs[next] - 1 == next_log;
+    uint32_t* next_tree = nullptr;
+    st = tree_for(next_log, next + (inject ? 1 : 0), &next_tree);
+    if (st) return st;
+    uint32_t* next_leaves = leaves_of(next_tree, next_log);
     st = fri_fold_line(tree, dom, const_cast<const uint32_t* const*>(cur.c), unused_alpha, nxt.c, s,
-                       alphas + 8 * fstep);
+                       alphas + 8 * fstep, inject ? nullptr : next_leaves);
     if (st) return st;
     dom = coset_double(dom);
-    if (next < quotients.size() && qlogs[next] - 1 == dom.log_size) {
+    if (inject) {
       st = fri_fold_circle(tree, canonic_half_coset(qlogs[next]), nxt.c,
-                           const_cast<const uint32_t* const*>(quotients[next].c), unused_alpha, s, alphas + 8 * fstep);
+                           const_cast<const uint32_t* const*>(quotients[next].c), unused_alpha, s, alphas + 8 * fstep,
+                           next_leaves);
       if (st) return st;
       next++;
     }
+    pending_tree = next_tree;
     layers.push_back(L);
     cur = nxt;
   }

@@ -63,6 +63,10 @@ struct DevMerkle {
   // the next alpha into alpha_out, when the root comes from a node-only run (channel_fused).
   int32_t commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root = true,
                  DevChannel* ch = nullptr, uint32_t* alpha_out = nullptr);
+  // A tree of equal-size columns whose leaf level is already in `all` (written by the FRI fold
+  // that produced the columns); `all` holds every layer, as commit lays them out.
+  int32_t commit_from_leaves(const std::vector<ColRef>& columns, uint32_t* all, cudaStream_t s,
+                             DevChannel* ch = nullptr, uint32_t* alpha_out = nullptr);
   bool channel_fused = false;
   void decommit(const std::map<uint32_t, std::vector<size_t>>& queries, Gather& g, DecommitRecipe& out) const;
 };

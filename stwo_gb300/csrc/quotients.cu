@@ -115,13 +115,13 @@ __global__ void __launch_bounds__(256) k_quotient_coeffs(const QSample* __restri
 }
 
 constexpr int Q_ROWS = 32;    // rows per block (one warp-width of consecutive rows)
-constexpr int Q_SLICES = 8;   // column slices per row; 256 threads
+constexpr int Q_SLICES = 8;   // column slices per row; one warp each
 constexpr int Q_STAGE = 512;  // entries staged in shared memory at a time
 
 // One block = 32 consecutive rows x 8 column slices: a warp reads 32 consecutive words of one
 // column, the 8 warps stream disjoint columns of the same rows, and the 8 partial sums of a
 // batch meet in shared memory. Slice 0 then finishes the batch (line term, denominator).
-__global__ void __launch_bounds__(256) k_quotient_rows(uint32_t rows, uint32_t log_n, uint32_t half_init,
+__global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows(uint32_t rows, uint32_t log_n, uint32_t half_init,
                                                        uint32_t half_step, QCols cols,
                                                        const QBatch* __restrict__ batches, uint32_t n_batches,
                                                        const QEntry* __restrict__ entries, uint32_t* o0, uint32_t* o1,
@@ -290,7 +290,7 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
   for (uint32_t c = 0; c < n_cols; c++) qc.p[c] = cols[c];
   uint32_t* o[4];
   for (int q = 0; q < 4; q++) o[q] = direct ? out[q] : d_sub + (size_t)q * rows;
-  k_quotient_rows<<<(rows + Q_ROWS - 1) / Q_ROWS, 256, 0, s>>>(rows, log_n, dom_half.initial_index, dom_half.step_size, qc,
+  k_quotient_rows<<<(rows + Q_ROWS - 1) / Q_ROWS, Q_SLICES * 32, 0, s>>>(rows, log_n, dom_half.initial_index, dom_half.step_size, qc,
                                                      d_b, n_batches, d_e, o[0], o[1], o[2], o[3]); note_launch();
   if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
 
