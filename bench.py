@@ -382,7 +382,7 @@ def run_gkr(args, world, rank, local, lib, barrier, max_over_ranks):
         "wall_s": wall,
         "clocks": clk.summary(),
     }
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:  # the CPU baseline is timed at N=1 only
         line["cpu_baseline"] = cpu_baseline_gkr(args.cpu_threads)
     print(json.dumps(line), flush=True)
 
@@ -717,7 +717,7 @@ def run_gb300(args):
         "wall_s": wall,
         "clocks": clk.summary(),
     }
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:  # the CPU baseline is timed at N=1 only
         line["cpu_baseline"] = cpu_baseline_poseidon(args.cpu_threads, log=15)
     print(json.dumps(line), flush=True)
 
@@ -830,7 +830,7 @@ def run_kernels(args, world, rank, local, lib, barrier, max_over_ranks):
         "wall_s": wall,
         "clocks": clk.summary(),
     }
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:  # the CPU baseline is timed at N=1 only
         line["cpu_baseline"] = cpu_baseline_kernels(args.cpu_threads)
     print(json.dumps(line), flush=True)
 
