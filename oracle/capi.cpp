@@ -449,3 +449,76 @@ void oracle_channel_draw_felts(size_t n, uint32_t* out) {
 }
 
 }  // extern "C"
+
+#include "air_blake_round.h"
+
+extern "C" {
+
+// Proves the Blake2s round AIR (2^log_n rows, one BLAKE2s round per row): empty preprocessed
+// tree, the log size mixed into the channel, the trace, the relation elements, the claimed sum
+// mixed, the LogUp interaction trace, then prove(). `inputs` holds per row the 16 state words and
+// the 16 message words (row * 32 + i), or is NULL for the reference test's inputs.
+size_t oracle_prove_blake_round(uint32_t log_n, const uint32_t* inputs, const uint32_t cfg[4], uint8_t* out,
+                                size_t cap, uint32_t claimed_sum[4], char* err, size_t err_cap) {
+  try {
+    PcsConfig config{cfg[0], cfg[1], cfg[2], cfg[3]};
+    std::vector<uint32_t> ref;
+    if (!inputs) {
+      ref = blake_round_reference_inputs(log_n);
+      inputs = ref.data();
+    }
+    TwiddleTree tw = precompute_twiddles(canonic_domain(log_n + 1 + config.log_blowup).half_coset);
+    Channel ch;
+    CommitmentSchemeProver pcs;
+    pcs.config = config;
+    pcs.twiddles = &tw;
+    pcs.commit({}, ch);
+    ch.mix_u64(log_n);
+    std::vector<BrXorLookup> xl;
+    std::vector<std::vector<M31>> round;
+    pcs.commit_evals(blake_round_trace(log_n, inputs, xl, round), log_n, ch);
+    BlakeRoundElements el = BlakeRoundElements::draw(ch);
+    QM31 cs;
+    std::vector<Column> inter = blake_round_interaction_trace(log_n, xl, round, el, cs);
+    ch.mix_felts({cs});
+    pcs.commit_evals(inter, log_n, ch);
+    BlakeRoundAir air(log_n, el, cs);
+    StarkProof proof = prove(air, ch, pcs);
+    std::vector<uint8_t> bytes = serialize(proof);
+    if (bytes.size() > cap) throw std::runtime_error("output buffer too small");
+    std::memcpy(out, bytes.data(), bytes.size());
+    q_to(cs, claimed_sum);
+    return bytes.size();
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+int oracle_verify_blake_round(uint32_t log_n, const uint32_t claimed_sum[4], const uint8_t* proof, size_t len,
+                              char* err, size_t err_cap) {
+  try {
+    StarkProof p;
+    if (!deserialize(proof, len, p)) throw std::runtime_error("malformed proof bytes");
+    Channel ch;
+    BlakeRoundAir air(log_n, BlakeRoundElements{}, q_of(claimed_sum));
+    auto hook = [&](size_t t, Channel& c) {
+      if (t == 0) c.mix_u64(log_n);
+      if (t == 1) {
+        air.el = BlakeRoundElements::draw(c);
+        c.mix_felts({air.claimed_sum});
+      }
+    };
+    std::string r = verify(air, ch, p,
+                           {{}, std::vector<uint32_t>(BR_TRACE_COLS, log_n),
+                            std::vector<uint32_t>(4 * BR_INTERACTION_SECURE, log_n)},
+                           hook);
+    if (!r.empty()) throw std::runtime_error(r);
+    return 1;
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+}  // extern "C"

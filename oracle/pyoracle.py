@@ -230,6 +230,31 @@ def verify_poseidon(log_n, claimed_sum, proof: bytes):
     return bool(ok), err.value.decode()
 
 
+def prove_blake_round(log_n, inputs=None, config=(5, 1, 0, 3)):
+    """(proof bytes, claimed_sum) of the Blake2s round AIR; inputs (per row 16 state + 16 message
+    words) = None for the reference test's inputs."""
+    cap = 256 << 20
+    out = np.zeros(cap, np.uint8)
+    cs = np.zeros(4, np.uint32)
+    err = C.create_string_buffer(512)
+    f = lib().oracle_prove_blake_round
+    f.restype = C.c_size_t
+    keep = _u32(inputs).reshape(-1) if inputs is not None else None
+    ip = _p(keep) if keep is not None else None
+    n = f(C.c_uint32(log_n), ip, _p(_u32(config)), _p(out), C.c_size_t(cap), _p(cs), err, C.c_size_t(512))
+    if n == 0:
+        raise RuntimeError("oracle prove failed: " + err.value.decode())
+    return bytes(out[:n]), tuple(int(x) for x in cs)
+
+
+def verify_blake_round(log_n, claimed_sum, proof: bytes):
+    buf = np.frombuffer(proof, dtype=np.uint8).copy()
+    err = C.create_string_buffer(512)
+    ok = lib().oracle_verify_blake_round(C.c_uint32(log_n), _p(_u32(claimed_sum)), _p(buf), C.c_size_t(len(proof)),
+                                         err, C.c_size_t(512))
+    return bool(ok), err.value.decode()
+
+
 # ---------------------------------------------------------------- GKR / MLE
 GRAND_PRODUCT, LOGUP_GENERIC, LOGUP_MULTIPLICITIES, LOGUP_SINGLES = 0, 1, 2, 3
 

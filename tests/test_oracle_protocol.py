@@ -52,3 +52,30 @@ def test_poseidon_seeded_inputs(oracle):
     init = rng.integers(0, (1 << 31) - 1, size=(1 << 5) * 8 * 16, dtype=np.int64).astype(np.uint32)
     proof, cs = oracle.prove_poseidon(5, init)
     assert oracle.verify_poseidon(5, cs, proof)[0]
+
+
+@pytest.mark.parametrize("log_n", [4, 5, 7, 10])
+def test_blake_round_prove_verify(oracle, log_n):
+    # The reference round test's inputs (crates/prover/src/examples/blake/round/mod.rs:60-110: v_i = i,
+    # m_i = i + 1 on every row); prove() itself checks the constraints at the OODS point.
+    proof, cs = oracle.prove_blake_round(log_n)
+    ok, why = oracle.verify_blake_round(log_n, cs, proof)
+    assert ok, why
+
+
+def test_blake_round_seeded_inputs_and_tampering(oracle):
+    rng = np.random.default_rng(3)
+    inputs = rng.integers(0, 2**32, (1 << 6) * 32, dtype=np.uint64).astype(np.uint32)
+    proof, cs = oracle.prove_blake_round(6, inputs, (3, 2, 1, 5))
+    assert oracle.verify_blake_round(6, cs, proof)[0]
+    # A different claimed sum changes the transcript (it is mixed before the interaction tree).
+    wrong = (cs[0] ^ 1,) + tuple(cs[1:])
+    assert not oracle.verify_blake_round(6, wrong, proof)[0]
+    for pos in rng.integers(0, len(proof), size=8):
+        bad = bytearray(proof)
+        bad[int(pos)] ^= 0x10
+        assert not oracle.verify_blake_round(6, cs, bytes(bad))[0], int(pos)
+    # Other inputs give another claimed sum.
+    other = inputs.copy()
+    other[5] ^= 1
+    assert oracle.prove_blake_round(6, other, (3, 2, 1, 5))[1] != cs
