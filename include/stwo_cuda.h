@@ -260,22 +260,36 @@ stwo_status stwo_prove_wide_fib(uint32_t log_n_rows, uint32_t n_cols, uint32_t* 
 stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* d_init, stwo_pcs_config cfg, uint8_t* h_proof,
                                 size_t capacity, size_t* h_len, stwo_qm31* h_claimed_sum, void* stream);
 
+/* The Blake2s round AIR: BlakeRoundComponent (crates/prover/src/examples/blake/round/) proved on
+ * its own, one BLAKE2s round per row over 2^log_n_rows rows (log_n_rows >= 4). d_inputs holds per
+ * row the 16 state words then the 16 message words (word row * 32 + i), or is NULL for the
+ * reference test's inputs (v_i = i, m_i = i + 1, round/mod.rs:60-110). The transcript follows the
+ * Blake example's statements (blake/air.rs:83-183): an empty preprocessed tree, the log size
+ * mixed, the trace committed, RoundElements then the five XOR relations drawn, the claimed LogUp
+ * sum mixed, the interaction trace committed, then prove(). The claimed sum is returned in
+ * *h_claimed_sum. */
+stwo_status stwo_prove_blake_round(uint32_t log_n_rows, const uint32_t* d_inputs, stwo_pcs_config cfg,
+                                   uint8_t* h_proof, size_t capacity, size_t* h_len, stwo_qm31* h_claimed_sum,
+                                   void* stream);
+
 /* ------------------------------------------------------------------ batched and served proving */
 /* No counterpart in the reference, which proves one statement per call (prover/mod.rs:27-79).
  * A server owns a pool of host workers, each with its own CUDA stream, that run whole-proof jobs
- * (stwo_prove_wide_fib / stwo_prove_poseidon) concurrently. A job starts when its estimated
+ * (stwo_prove_wide_fib / stwo_prove_poseidon / stwo_prove_blake_round) concurrently. A job starts when its estimated
  * device bytes (stwo_job_hbm_bytes) fit in the HBM budget beside the running jobs; among queued
  * jobs the first in submission order that fits starts next. Proof bytes equal those of the
  * single-call entry points. */
 #define STWO_AIR_WIDE_FIB 0u
 #define STWO_AIR_POSEIDON 1u
+#define STWO_AIR_BLAKE_ROUND 2u
 typedef struct {
   uint32_t air;
   uint32_t log_n_rows;
   uint32_t n_cols;        /* wide-Fibonacci columns */
   const uint32_t* d_a;    /* wide-Fibonacci: per-row first two values (device, 2^log_n_rows each) */
   const uint32_t* d_b;
-  const uint32_t* d_init; /* Poseidon2 initial states (device) or NULL for the reference inputs */
+  const uint32_t* d_init; /* Poseidon2 initial states or Blake2s round inputs (device), or NULL for
+                             the reference inputs */
   stwo_pcs_config cfg;
   uint8_t* h_proof;       /* host buffer for the proof bytes */
   size_t capacity;

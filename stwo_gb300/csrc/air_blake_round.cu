@@ -1,0 +1,737 @@
+// Blake2s round AIR on the device: the reference's BlakeRoundComponent
+// (crates/prover/src/examples/blake/round/{constraints,gen}.rs) proved on its own, with the
+// statement mixing of the Blake example (blake/air.rs:83-183): the log size before the trace
+// commitment, the round's claimed LogUp sum before the interaction commitment. Relation elements
+// are drawn in AllElements order without the scheduler's: RoundElements (96 values), then the
+// five 3-value XOR relations (blake/mod.rs:55-121).
+//
+// Kernels (one thread per row):
+//   k_br_trace        the 384 trace columns of one BLAKE2s round (gen.rs:75-204)
+//   k_br_interaction  64 cumulative columns of paired XOR lookups and one of the Round relation
+//                     (gen.rs:237-280); the row's round is recomputed from its inputs, so no
+//                     lookup columns are stored
+//   k_br_composition  the 64 carry constraints and 65 LogUp constraints (constraints.rs:22-206,
+//                     finalize_logup_in_pairs) with random-coefficient accumulation, times 1/Z
+#include "common.cuh"
+#include "prover.cuh"
+
+namespace stwo {
+
+constexpr int BR_ST = 16;
+constexpr int BR_COLS = 384;            // 2 * (16 + 16) + 8 G-functions * 40
+constexpr int BR_ROUND_FELTS = 96;      // (input state, output state, message) as (low, high) halves
+constexpr int BR_XOR_PAIRS = 64;        // 128 xor lookups per row, in pairs
+constexpr int BR_INTER_SECURE = BR_XOR_PAIRS + 1;
+constexpr int BR_N_CONSTRAINTS = 64 + BR_INTER_SECURE;  // 129
+
+// Relation elements: z and alpha powers per relation (XOR widths 12, 9, 8, 7, 4, then Round).
+struct BrElements {
+  uint32_t xz[5][4];
+  uint32_t xa[5][3][4];
+  uint32_t rz[4];
+  uint32_t ra[BR_ROUND_FELTS][4];
+};
+
+__device__ __forceinline__ int br_xor_index(uint32_t w) { return w == 12 ? 0 : w == 9 ? 1 : w == 8 ? 2 : w == 7 ? 3 : 4; }
+// Four words of the relation elements in global memory (read-only loads: never a parameter's address).
+__device__ __forceinline__ qm31 br_q(const uint32_t* v) { return qm31_from_u32(__ldg(v), __ldg(v + 1), __ldg(v + 2), __ldg(v + 3)); }
+
+// LookupElements::combine for one XOR lookup: a + alpha b + alpha^2 c - z (logup.rs:95-113).
+// The elements live in device memory (read through the read-only cache, the same words for
+// every thread): a kernel parameter of this size, addressed by index, would be copied to each
+// thread's stack.
+__device__ __forceinline__ qm31 br_xor_combine(const BrElements* e, uint32_t w, uint32_t a, uint32_t b, uint32_t c) {
+  const int k = br_xor_index(w);
+  qm31 acc = qm31_add(qm31_add(qm31_mul_m31(br_q(e->xa[k][0]), a), qm31_mul_m31(br_q(e->xa[k][1]), b)),
+                      qm31_mul_m31(br_q(e->xa[k][2]), c));
+  return qm31_sub(acc, br_q(e->xz[k]));
+}
+
+__device__ __forceinline__ void br_inputs(const uint32_t* in, uint32_t r, uint32_t v[BR_ST], uint32_t m[BR_ST]) {
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    v[i] = in ? __ldg(in + (size_t)r * 32 + i) : (uint32_t)i;
+    m[i] = in ? __ldg(in + (size_t)r * 32 + 16 + i) : (uint32_t)(i + 1);
+  }
+}
+
+// ------------------------------------------------------------------------------------------ trace
+// One row of TraceGeneratorRow::generate. The visitor gets every trace felt in column order and
+// every XOR lookup (w, a, b, a ^ b) in lookup order.
+template <class V>
+__device__ __forceinline__ void br_round(uint32_t v[BR_ST], const uint32_t m[BR_ST], V& vis) {
+  auto u32 = [&](uint32_t x) {
+    vis.felt(x & 0xffffu);
+    vis.felt(x >> 16);
+  };
+  auto split = [&](uint32_t a, uint32_t rr, uint32_t& l, uint32_t& h) {
+    h = a >> rr;
+    l = a & ((1u << rr) - 1);
+    vis.felt(h);
+  };
+  auto xor1 = [&](uint32_t w, uint32_t a, uint32_t b) {
+    const uint32_t c = a ^ b;
+    vis.felt(c);
+    vis.lookup(w, a, b, c);
+  };
+  auto xor_rotr = [&](uint32_t a, uint32_t b, uint32_t rr) {
+    const uint32_t c = a ^ b;
+    uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
+    split(a & 0xffffu, rr, all, alh);
+    split(a >> 16, rr, ahl, ahh);
+    split(b & 0xffffu, rr, bll, blh);
+    split(b >> 16, rr, bhl, bhh);
+    xor1(rr, all, bll);
+    xor1(rr, ahl, bhl);
+    xor1(16 - rr, alh, blh);
+    xor1(16 - rr, ahh, bhh);
+    return (c >> rr) | (c << (32 - rr));
+  };
+  // xor_rotr16_u32: both halves split at 8, all four lookups of width 8.
+  auto xor_rotr16 = [&](uint32_t a, uint32_t b) {
+    const uint32_t c = a ^ b;
+    uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
+    split(a & 0xffffu, 8, all, alh);
+    split(a >> 16, 8, ahl, ahh);
+    split(b & 0xffffu, 8, bll, blh);
+    split(b >> 16, 8, bhl, bhh);
+    xor1(8, all, bll);
+    xor1(8, ahl, bhl);
+    xor1(8, alh, blh);
+    xor1(8, ahh, bhh);
+    return (c >> 16) | (c << 16);
+  };
+  auto g = [&](int ia, int ib, int ic, int id, uint32_t m0, uint32_t m1) {
+    uint32_t a = v[ia], b = v[ib], c = v[ic], d = v[id];
+    a = a + b + m0;
+    u32(a);
+    d = xor_rotr16(a, d);
+    c = c + d;
+    u32(c);
+    b = xor_rotr(b, c, 12);
+    a = a + b + m1;
+    u32(a);
+    d = xor_rotr(a, d, 8);
+    c = c + d;
+    u32(c);
+    b = xor_rotr(b, c, 7);
+    v[ia] = a;
+    v[ib] = b;
+    v[ic] = c;
+    v[id] = d;
+  };
+  g(0, 4, 8, 12, m[0], m[1]);
+  g(1, 5, 9, 13, m[2], m[3]);
+  g(2, 6, 10, 14, m[4], m[5]);
+  g(3, 7, 11, 15, m[6], m[7]);
+  g(0, 5, 10, 15, m[8], m[9]);
+  g(1, 6, 11, 12, m[10], m[11]);
+  g(2, 7, 8, 13, m[12], m[13]);
+  g(3, 4, 9, 14, m[14], m[15]);
+}
+
+struct BrTraceWriter {
+  uint32_t* trace;
+  size_t n;
+  uint32_t r;
+  uint32_t col = 0;
+  __device__ void felt(uint32_t x) { trace[(size_t)col++ * n + r] = x; }
+  __device__ void lookup(uint32_t, uint32_t, uint32_t, uint32_t) {}
+};
+
+// inputs: per row 16 state words then 16 message words, or NULL for the reference test's inputs
+// (v_i = i, m_i = i + 1).
+__global__ void __launch_bounds__(128) k_br_trace(uint32_t n_rows, const uint32_t* __restrict__ inputs,
+                                                  uint32_t* __restrict__ trace) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  uint32_t v[BR_ST], m[BR_ST];
+  br_inputs(inputs, r, v, m);
+  BrTraceWriter w{trace, n_rows, r};
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    w.felt(v[i] & 0xffffu);
+    w.felt(v[i] >> 16);
+  }
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    w.felt(m[i] & 0xffffu);
+    w.felt(m[i] >> 16);
+  }
+  br_round(v, m, w);
+}
+
+// ------------------------------------------------------------------------------------ interaction
+// Accumulates the paired XOR fractions into cumulative secure columns as the lookups appear.
+struct BrInteractionWriter {
+  const BrElements* e;
+  uint32_t* out;
+  size_t n;
+  uint32_t r;
+  qm31 cum = qm31_zero();
+  qm31 pending;
+  bool have = false;
+  uint32_t col = 0;
+  __device__ void felt(uint32_t) {}
+  __device__ void lookup(uint32_t w, uint32_t a, uint32_t b, uint32_t c) {
+    const qm31 p = br_xor_combine(e, w, a, b, c);
+    if (!have) {
+      pending = p;
+      have = true;
+      return;
+    }
+    have = false;
+    // 1/p0 + 1/p1 = (p0 + p1) / (p0 p1)
+    cum = qm31_add(cum, qm31_mul(qm31_add(pending, p), qm31_inv(qm31_mul(pending, p))));
+    write(cum);
+  }
+  __device__ void write(const qm31& x) {
+    out[((size_t)4 * col + 0) * n + r] = x.a.a;
+    out[((size_t)4 * col + 1) * n + r] = x.a.b;
+    out[((size_t)4 * col + 2) * n + r] = x.b.a;
+    out[((size_t)4 * col + 3) * n + r] = x.b.b;
+    col++;
+  }
+};
+
+__global__ void __launch_bounds__(128) k_br_interaction(uint32_t n_rows, const uint32_t* __restrict__ inputs,
+                                                        const BrElements* __restrict__ e, uint32_t* __restrict__ out) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  uint32_t v[BR_ST], m[BR_ST];
+  br_inputs(inputs, r, v, m);
+  // The Round relation's denominator: sum_k alpha^k x_k - z over (input, output, message) halves.
+  qm31 p = qm31_zero();
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i]), v[i] & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i + 1]), v[i] >> 16));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), m[i] & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), m[i] >> 16));
+  }
+  BrInteractionWriter w{e, out, n_rows, r};
+  br_round(v, m, w);
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i]), v[i] & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i + 1]), v[i] >> 16));
+  }
+  p = qm31_sub(p, br_q(e->rz));
+  // -1 / p
+  w.write(qm31_add(w.cum, qm31_sub(qm31_zero(), qm31_inv(p))));
+}
+
+// ------------------------------------------------------------------------------------ composition
+struct BrParams {
+  uint32_t trace_log, eval_log;
+  uint32_t shift[4];  // claimed_sum / 2^trace_log
+};
+
+__device__ __forceinline__ uint32_t br_prev_row(uint32_t r, uint32_t trace_log, uint32_t eval_log) {
+  // offset_bit_reversed_circle_domain_index(r, trace_log, eval_log, -1) (core/utils.rs:74-90)
+  uint32_t prev = brev(r, eval_log);
+  const uint32_t half = 1u << (eval_log - 1);
+  const uint32_t step = 1u << (eval_log - trace_log - 1);
+  if (prev < half) prev = (prev + half - step) & (half - 1);
+  else prev = ((prev - half + step) & (half - 1)) + half;
+  return brev(prev, eval_log);
+}
+
+// The constraint evaluator at one row of the evaluation domain (F = M31). Trace masks are read in
+// the evaluator's column order; each XOR pair's LogUp constraint is accumulated as soon as its two
+// lookups are known, with its own coefficient (the random-coefficient sum is exact in the field,
+// so the order of accumulation does not change it).
+struct BrRowEval {
+  const uint32_t* trace;
+  const uint32_t* inter;
+  uint32_t el, r;
+  const uint32_t* coeffs;  // 4 words per constraint, in constraint order
+  uint32_t col = 0;
+  uint32_t ci = 0;  // round (carry) constraint index
+  uint32_t batch = 0;
+  unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  uint32_t cnt = 0;
+  qm31 logup = qm31_zero();
+  qm31 prev_col = qm31_zero();
+
+  __device__ uint32_t mask() { return __ldg(trace + ((size_t)col++ << el) + r); }
+  __device__ void carry_constraint(uint32_t c) {
+    const uint32_t* k = coeffs + 4 * ci++;
+    a0 += (unsigned long long)k[0] * c;
+    a1 += (unsigned long long)k[1] * c;
+    a2 += (unsigned long long)k[2] * c;
+    a3 += (unsigned long long)k[3] * c;
+    if (++cnt == 3) {
+      a0 = (a0 & P) + (a0 >> 31);
+      a1 = (a1 & P) + (a1 >> 31);
+      a2 = (a2 & P) + (a2 >> 31);
+      a3 = (a3 & P) + (a3 >> 31);
+      cnt = 0;
+    }
+  }
+  __device__ void logup_constraint(const qm31& c) {
+    const uint32_t* k = coeffs + 4 * (64 + batch++);
+    logup = qm31_add(logup, qm31_mul(qm31_from_u32(k[0], k[1], k[2], k[3]), c));
+  }
+  __device__ qm31 inter_at(uint32_t b, uint32_t row) const {
+    const uint32_t* base = inter + (((size_t)4 * b) << el) + row;
+    return qm31_from_u32(__ldg(base), __ldg(base + ((size_t)1 << el)), __ldg(base + ((size_t)2 << el)),
+                         __ldg(base + ((size_t)3 << el)));
+  }
+};
+
+__device__ __forceinline__ uint32_t br_inv16(uint32_t x) { return m31_mul(x, 1u << 15); }
+// A 64-bit sum of M31 products, reduced to [0, P).
+__device__ __forceinline__ uint32_t br_fold64(unsigned long long x) {
+  x = (x & P) + (x >> 31);
+  x = (x & P) + (x >> 31);
+  const uint32_t r = (uint32_t)x;
+  return r >= P ? r - P : r;
+}
+
+__global__ void __launch_bounds__(128) k_br_composition(const uint32_t* __restrict__ trace,
+                                                        const uint32_t* __restrict__ inter, uint32_t n_rows,
+                                                        BrParams pp, const BrElements* __restrict__ e,
+                                                        const uint32_t* __restrict__ coeffs,
+                                                        const uint32_t* __restrict__ dinv, uint32_t* o0,
+                                                        uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+  __shared__ uint32_t s_coeffs[4 * BR_N_CONSTRAINTS];
+  for (uint32_t i = threadIdx.x; i < 4 * BR_N_CONSTRAINTS; i += blockDim.x) s_coeffs[i] = coeffs[i];
+  __syncthreads();
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  BrRowEval ev{trace, inter, pp.eval_log, r, s_coeffs};
+  struct U {
+    uint32_t l, h;
+  };
+  U v[BR_ST];
+  qm31 round_p = qm31_zero();
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    v[i].l = ev.mask();
+    v[i].h = ev.mask();
+    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[2 * i]), v[i].l));
+    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[2 * i + 1]), v[i].h));
+  }
+  // The message masks follow the state's; each message word is used by exactly one G, in order.
+  const uint32_t m_col = 2 * BR_ST;
+  ev.col = 4 * BR_ST;
+  auto msg = [&](int i) {
+    U x;
+    x.l = __ldg(trace + ((size_t)(m_col + 2 * i) << pp.eval_log) + r);
+    x.h = __ldg(trace + ((size_t)(m_col + 2 * i + 1) << pp.eval_log) + r);
+    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), x.l));
+    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), x.h));
+    return x;
+  };
+  auto add2 = [&](U a, U b) {
+    U s;
+    s.l = ev.mask();
+    s.h = ev.mask();
+    const uint32_t cl = br_inv16(m31_sub(m31_add(a.l, b.l), s.l));
+    ev.carry_constraint(m31_sub(m31_mul(cl, cl), cl));
+    const uint32_t ch = br_inv16(m31_sub(m31_add(m31_add(a.h, b.h), cl), s.h));
+    ev.carry_constraint(m31_sub(m31_mul(ch, ch), ch));
+    return s;
+  };
+  auto add3 = [&](U a, U b, U c) {
+    U s;
+    s.l = ev.mask();
+    s.h = ev.mask();
+    const uint32_t cl = br_inv16(m31_sub(m31_add(m31_add(a.l, b.l), c.l), s.l));
+    ev.carry_constraint(m31_mul(m31_mul(cl, m31_sub(cl, 1u)), m31_sub(cl, 2u)));
+    const uint32_t ch = br_inv16(m31_sub(m31_add(m31_add(m31_add(a.h, b.h), c.h), cl), s.h));
+    ev.carry_constraint(m31_mul(m31_mul(ch, m31_sub(ch, 1u)), m31_sub(ch, 2u)));
+    return s;
+  };
+  auto split = [&](uint32_t a, uint32_t rr, uint32_t& l, uint32_t& h) {
+    h = ev.mask();
+    l = m31_sub(a, m31_mul(h, 1u << rr));
+  };
+  // Two XOR lookups (one LogUp batch): constraint (cur - prev) * p0 p1 - (p0 + p1).
+  auto xor2 = [&](uint32_t w, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1, uint32_t& c0, uint32_t& c1) {
+    c0 = ev.mask();
+    c1 = ev.mask();
+    const qm31 p0 = br_xor_combine(e, w, a0, b0, c0);
+    const qm31 p1 = br_xor_combine(e, w, a1, b1, c1);
+    const qm31 cur = ev.inter_at(ev.batch, r);
+    const qm31 diff = qm31_sub(cur, ev.prev_col);
+    ev.prev_col = cur;
+    ev.logup_constraint(qm31_sub(qm31_mul(diff, qm31_mul(p0, p1)), qm31_add(p0, p1)));
+  };
+  auto xor_rotr = [&](U a, U b, uint32_t rr) {
+    uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
+    split(a.l, rr, all, alh);
+    split(a.h, rr, ahl, ahh);
+    split(b.l, rr, bll, blh);
+    split(b.h, rr, bhl, bhh);
+    uint32_t xll, xhl, xlh, xhh;
+    xor2(rr, all, ahl, bll, bhl, xll, xhl);
+    xor2(16 - rr, alh, ahh, blh, bhh, xlh, xhh);
+    U o;
+    o.l = m31_add(m31_mul(xhl, 1u << (16 - rr)), xlh);
+    o.h = m31_add(m31_mul(xll, 1u << (16 - rr)), xhh);
+    return o;
+  };
+  auto xor_rotr16 = [&](U a, U b) {
+    uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
+    split(a.l, 8, all, alh);
+    split(a.h, 8, ahl, ahh);
+    split(b.l, 8, bll, blh);
+    split(b.h, 8, bhl, bhh);
+    uint32_t xll, xhl, xlh, xhh;
+    xor2(8, all, ahl, bll, bhl, xll, xhl);
+    xor2(8, alh, ahh, blh, bhh, xlh, xhh);
+    U o;
+    o.l = m31_add(m31_mul(xhh, 1u << 8), xhl);
+    o.h = m31_add(m31_mul(xlh, 1u << 8), xll);
+    return o;
+  };
+  auto g = [&](int ia, int ib, int ic, int id, int mi) {
+    U a = v[ia], b = v[ib], c = v[ic], d = v[id];
+    a = add3(a, b, msg(mi));
+    d = xor_rotr16(a, d);
+    c = add2(c, d);
+    b = xor_rotr(b, c, 12);
+    a = add3(a, b, msg(mi + 1));
+    d = xor_rotr(a, d, 8);
+    c = add2(c, d);
+    b = xor_rotr(b, c, 7);
+    v[ia] = a;
+    v[ib] = b;
+    v[ic] = c;
+    v[id] = d;
+  };
+  g(0, 4, 8, 12, 0);
+  g(1, 5, 9, 13, 2);
+  g(2, 6, 10, 14, 4);
+  g(3, 7, 11, 15, 6);
+  g(0, 5, 10, 15, 8);
+  g(1, 6, 11, 12, 10);
+  g(2, 7, 8, 13, 12);
+  g(3, 4, 9, 14, 14);
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[32 + 2 * i]), v[i].l));
+    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[32 + 2 * i + 1]), v[i].h));
+  }
+  round_p = qm31_sub(round_p, br_q(e->rz));
+  // Last batch: the Round entry alone (multiplicity -1), against the last cumulative column at
+  // the previous and current trace rows plus the cumsum shift.
+  {
+    const uint32_t rp = br_prev_row(r, pp.trace_log, pp.eval_log);
+    const qm31 prev_row = ev.inter_at(BR_XOR_PAIRS, rp);
+    const qm31 cur = ev.inter_at(BR_XOR_PAIRS, r);
+    const qm31 shift = qm31_from_u32(pp.shift[0], pp.shift[1], pp.shift[2], pp.shift[3]);  // a kernel parameter
+    const qm31 fixed = qm31_add(qm31_sub(qm31_sub(cur, prev_row), ev.prev_col), shift);
+    // fixed * p - (-1)
+    ev.logup_constraint(qm31_add(qm31_mul(fixed, round_p), qm31_from_u32(1, 0, 0, 0)));
+  }
+  const qm31 res = qm31_add(qm31_from_u32(br_fold64(ev.a0), br_fold64(ev.a1), br_fold64(ev.a2), br_fold64(ev.a3)),
+                            ev.logup);
+  const uint32_t d = __ldg(dinv + (r >> pp.trace_log));
+  o0[r] = m31_mul(res.a.a, d);
+  o1[r] = m31_mul(res.a.b, d);
+  o2[r] = m31_mul(res.b.a, d);
+  o3[r] = m31_mul(res.b.b, d);
+}
+
+// ------------------------------------------------------------------------------------ host side
+struct HRel {
+  hq z;
+  std::vector<hq> alpha_pow;
+  // LookupElements::draw: draw_felts(2) (logup.rs:80-94).
+  void draw(HostChannel& ch, size_t n) {
+    auto f = ch.draw_base_felts();
+    z = hq_make(f[0], f[1], f[2], f[3]);
+    const hq alpha = hq_make(f[4], f[5], f[6], f[7]);
+    hq cur = hq_make(1, 0, 0, 0);
+    alpha_pow.resize(n);
+    for (size_t i = 0; i < n; i++) {
+      alpha_pow[i] = cur;
+      cur = hq_mul(cur, alpha);
+    }
+  }
+  hq combine(const hq* v, size_t n) const {
+    hq acc = hq_make(0, 0, 0, 0);
+    for (size_t i = 0; i < n; i++) acc = hq_add(acc, hq_mul(alpha_pow[i], v[i]));
+    return hq_sub(acc, z);
+  }
+};
+
+struct HBrElements {
+  HRel round, xr[5];  // XOR widths 12, 9, 8, 7, 4
+  static int xi(uint32_t w) { return w == 12 ? 0 : w == 9 ? 1 : w == 8 ? 2 : w == 7 ? 3 : 4; }
+  void to_device(BrElements& d) const {
+    for (int k = 0; k < 5; k++) {
+      for (int i = 0; i < 4; i++) d.xz[k][i] = xr[k].z.v[i];
+      for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 4; i++) d.xa[k][j][i] = xr[k].alpha_pow[j].v[i];
+    }
+    for (int i = 0; i < 4; i++) d.rz[i] = round.z.v[i];
+    for (int j = 0; j < BR_ROUND_FELTS; j++)
+      for (int i = 0; i < 4; i++) d.ra[j][i] = round.alpha_pow[j].v[i];
+  }
+};
+
+static hq hq_sc(hq x, uint32_t k) {
+  for (int i = 0; i < 4; i++) x.v[i] = h_mul(x.v[i], k);
+  return x;
+}
+
+struct BlakeRoundGpuAir : GpuAir {
+  uint32_t log_n;
+  HBrElements el;
+  hq claimed_sum;
+  BlakeRoundGpuAir(uint32_t l, const HBrElements& e, hq cs) : log_n(l), el(e), claimed_sum(cs) {}
+  uint32_t log_size() const override { return log_n; }
+  uint32_t max_constraint_log_degree_bound() const override { return log_n + 1; }
+  size_t n_constraints() const override { return BR_N_CONSTRAINTS; }
+  std::vector<std::vector<std::vector<int>>> mask_offsets() const override {
+    std::vector<std::vector<std::vector<int>>> m(3);
+    m[1].assign(BR_COLS, {0});
+    for (int b = 0; b + 1 < BR_INTER_SECURE; b++)
+      for (int k = 0; k < 4; k++) m[2].push_back({0});
+    for (int k = 0; k < 4; k++) m[2].push_back({-1, 0});
+    return m;
+  }
+  hq shift() const { return hq_sc(claimed_sum, h_inv((uint32_t)((1ull << log_n) % P))); }
+  int32_t eval_composition(const std::vector<std::vector<const uint32_t*>>& cols, const uint32_t* coeffs,
+                           const uint32_t* dinv, uint32_t* const acc[4], cudaStream_t s) const override {
+    STWO_REQUIRE(cols.size() >= 3 && cols[1].size() == BR_COLS && cols[2].size() == 4 * BR_INTER_SECURE,
+                 "trace trees mismatch");
+    const uint32_t el_log = log_n + 1;
+    for (int c = 0; c < BR_COLS; c++)
+      STWO_REQUIRE(cols[1][c] == cols[1][0] + ((size_t)c << el_log), "trace columns are not one contiguous block");
+    for (int c = 0; c < 4 * BR_INTER_SECURE; c++)
+      STWO_REQUIRE(cols[2][c] == cols[2][0] + ((size_t)c << el_log),
+                   "interaction columns are not one contiguous block");
+    BrParams pp;
+    pp.trace_log = log_n;
+    pp.eval_log = el_log;
+    const hq sh = shift();
+    for (int i = 0; i < 4; i++) pp.shift[i] = sh.v[i];
+    BrElements he;
+    el.to_device(he);
+    BrElements* de = nullptr;
+    int32_t st = scratch_alloc((void**)&de, sizeof(BrElements), s);
+    if (st) return st;
+    cudaError_t e = cudaMemcpyAsync(de, &he, sizeof(BrElements), cudaMemcpyHostToDevice, s);
+    const uint32_t n_rows = 1u << el_log;
+    if (!e) {
+      k_br_composition<<<(n_rows + 127) / 128, 128, 0, s>>>(cols[1][0], cols[2][0], n_rows, pp, de, coeffs, dinv,
+                                                            acc[0], acc[1], acc[2], acc[3]);
+      note_launch();
+      e = cudaGetLastError();
+    }
+    scratch_free(de, s);
+    if (e) {
+      set_error("blake round composition: %s", cudaGetErrorString(e));
+      return STWO_ERR_CUDA;
+    }
+    return STWO_OK;
+  }
+  // The same constraints over QM31 at the OODS point, the PointEvaluator accumulation with the
+  // vanishing inverse factored out of the sum.
+  hq eval_at_point(const std::vector<std::vector<std::vector<hq>>>& mask, hq rc, hq denom_inv) const override {
+    const auto& t = mask[1];
+    const auto& it = mask[2];
+    size_t mc = 0;
+    hq acc = hq_make(0, 0, 0, 0);
+    auto add = [&](hq c) { acc = hq_add(hq_mul(acc, rc), c); };
+    auto next = [&]() { return t[mc++][0]; };
+    const hq one = hq_make(1, 0, 0, 0), two = hq_make(2, 0, 0, 0);
+    const uint32_t inv16 = 1u << 15;
+    struct U {
+      hq l, h;
+    };
+    std::vector<std::pair<hq, hq>> fr;  // (numerator, denominator) of every relation entry
+    auto add2 = [&](U a, U b) {
+      U s{next(), next()};
+      hq cl = hq_sc(hq_sub(hq_add(a.l, b.l), s.l), inv16);
+      add(hq_sub(hq_mul(cl, cl), cl));
+      hq ch = hq_sc(hq_sub(hq_add(hq_add(a.h, b.h), cl), s.h), inv16);
+      add(hq_sub(hq_mul(ch, ch), ch));
+      return s;
+    };
+    auto add3 = [&](U a, U b, U c) {
+      U s{next(), next()};
+      hq cl = hq_sc(hq_sub(hq_add(hq_add(a.l, b.l), c.l), s.l), inv16);
+      add(hq_mul(hq_mul(cl, hq_sub(cl, one)), hq_sub(cl, two)));
+      hq ch = hq_sc(hq_sub(hq_add(hq_add(hq_add(a.h, b.h), c.h), cl), s.h), inv16);
+      add(hq_mul(hq_mul(ch, hq_sub(ch, one)), hq_sub(ch, two)));
+      return s;
+    };
+    auto split = [&](hq a, uint32_t rr, hq& l, hq& h) {
+      h = next();
+      l = hq_sub(a, hq_sc(h, 1u << rr));
+    };
+    auto xor2 = [&](uint32_t w, hq a0, hq a1, hq b0, hq b1, hq& c0, hq& c1) {
+      c0 = next();
+      c1 = next();
+      const HRel& rel = el.xr[HBrElements::xi(w)];
+      hq v0[3] = {a0, b0, c0}, v1[3] = {a1, b1, c1};
+      fr.push_back({one, rel.combine(v0, 3)});
+      fr.push_back({one, rel.combine(v1, 3)});
+    };
+    auto xor_rotr = [&](U a, U b, uint32_t rr) {
+      hq all, alh, ahl, ahh, bll, blh, bhl, bhh, xll, xhl, xlh, xhh;
+      split(a.l, rr, all, alh);
+      split(a.h, rr, ahl, ahh);
+      split(b.l, rr, bll, blh);
+      split(b.h, rr, bhl, bhh);
+      xor2(rr, all, ahl, bll, bhl, xll, xhl);
+      xor2(16 - rr, alh, ahh, blh, bhh, xlh, xhh);
+      return U{hq_add(hq_sc(xhl, 1u << (16 - rr)), xlh), hq_add(hq_sc(xll, 1u << (16 - rr)), xhh)};
+    };
+    auto xor_rotr16 = [&](U a, U b) {
+      hq all, alh, ahl, ahh, bll, blh, bhl, bhh, xll, xhl, xlh, xhh;
+      split(a.l, 8, all, alh);
+      split(a.h, 8, ahl, ahh);
+      split(b.l, 8, bll, blh);
+      split(b.h, 8, bhl, bhh);
+      xor2(8, all, ahl, bll, bhl, xll, xhl);
+      xor2(8, alh, ahh, blh, bhh, xlh, xhh);
+      return U{hq_add(hq_sc(xhh, 1u << 8), xhl), hq_add(hq_sc(xlh, 1u << 8), xll)};
+    };
+    U v[BR_ST], m[BR_ST], in[BR_ST];
+    for (int i = 0; i < BR_ST; i++) v[i] = U{next(), next()};
+    for (int i = 0; i < BR_ST; i++) in[i] = v[i];
+    for (int i = 0; i < BR_ST; i++) m[i] = U{next(), next()};
+    auto g = [&](int ia, int ib, int ic, int id, int mi) {
+      U a = v[ia], b = v[ib], c = v[ic], d = v[id];
+      a = add3(a, b, m[mi]);
+      d = xor_rotr16(a, d);
+      c = add2(c, d);
+      b = xor_rotr(b, c, 12);
+      a = add3(a, b, m[mi + 1]);
+      d = xor_rotr(a, d, 8);
+      c = add2(c, d);
+      b = xor_rotr(b, c, 7);
+      v[ia] = a;
+      v[ib] = b;
+      v[ic] = c;
+      v[id] = d;
+    };
+    g(0, 4, 8, 12, 0);
+    g(1, 5, 9, 13, 2);
+    g(2, 6, 10, 14, 4);
+    g(3, 7, 11, 15, 6);
+    g(0, 5, 10, 15, 8);
+    g(1, 6, 11, 12, 10);
+    g(2, 7, 8, 13, 12);
+    g(3, 4, 9, 14, 14);
+    std::vector<hq> vals;
+    for (int i = 0; i < BR_ST; i++) vals.push_back(in[i].l), vals.push_back(in[i].h);
+    for (int i = 0; i < BR_ST; i++) vals.push_back(v[i].l), vals.push_back(v[i].h);
+    for (int i = 0; i < BR_ST; i++) vals.push_back(m[i].l), vals.push_back(m[i].h);
+    fr.push_back({hq_sub(hq_make(0, 0, 0, 0), one), el.round.combine(vals.data(), vals.size())});
+    // finalize_logup_in_pairs (constraint_framework/mod.rs:180-243).
+    auto comb = [&](size_t col, size_t j) {
+      return hq_add(hq_add(it[4 * col][j], hq_mul(it[4 * col + 1][j], hq_make(0, 1, 0, 0))),
+                    hq_add(hq_mul(it[4 * col + 2][j], hq_make(0, 0, 1, 0)), hq_mul(it[4 * col + 3][j], hq_make(0, 0, 0, 1))));
+    };
+    const size_t n_batches = (fr.size() + 1) / 2;
+    auto batch = [&](size_t b) {
+      std::pair<hq, hq> f = fr[2 * b];
+      if (2 * b + 1 < fr.size()) {
+        const auto& g2 = fr[2 * b + 1];
+        f = {hq_add(hq_mul(g2.second, f.first), hq_mul(f.second, g2.first)), hq_mul(f.second, g2.second)};
+      }
+      return f;
+    };
+    hq prev_col = hq_make(0, 0, 0, 0);
+    for (size_t b = 0; b + 1 < n_batches; b++) {
+      auto f = batch(b);
+      const hq cur = comb(b, 0);
+      const hq diff = hq_sub(cur, prev_col);
+      prev_col = cur;
+      add(hq_sub(hq_mul(diff, f.second), f.first));
+    }
+    auto f = batch(n_batches - 1);
+    const hq pr = comb(n_batches - 1, 0), cur = comb(n_batches - 1, 1);
+    const hq fixed = hq_add(hq_sub(hq_sub(cur, pr), prev_col), shift());
+    add(hq_sub(hq_mul(fixed, f.second), f.first));
+    return hq_mul(acc, denom_inv);
+  }
+};
+
+}  // namespace stwo
+
+using namespace stwo;
+
+extern "C" stwo_status stwo_prove_blake_round(uint32_t log_n_rows, const uint32_t* d_inputs, stwo_pcs_config cfg,
+                                              uint8_t* h_proof, size_t capacity, size_t* h_len,
+                                              stwo_qm31* h_claimed_sum, void* stream) {
+  STWO_REQUIRE(log_n_rows >= 4 && log_n_rows + 1 + cfg.log_blowup_factor <= 28, "bad log_n_rows");
+  STWO_REQUIRE(cfg.log_blowup_factor >= 1 && cfg.log_blowup_factor <= 16, "log_blowup_factor out of [1, 16]");
+  STWO_REQUIRE(cfg.log_last_layer_degree_bound <= 10, "log_last_layer_degree_bound > 10");
+  STWO_REQUIRE(h_len, "null length");
+  cudaStream_t s = as_stream(stream);
+  std::vector<uint8_t> bytes;
+  hq claimed = hq_make(0, 0, 0, 0);
+  int32_t st;
+  {
+    Prover pv(cfg, log_n_rows + 1 + cfg.log_blowup_factor, s);
+    if (pv.init_status) return pv.init_status;
+    const size_t n = (size_t)1 << log_n_rows;
+    st = pv.commit_polys({}, {});
+    // BlakeStatement0::mix_into (blake/air.rs:126-128).
+    if (!st) pv.ch.mix_u64(log_n_rows);
+    uint32_t* trace = nullptr;
+    uint32_t* inter = nullptr;
+    if (!st) {
+      trace = pv.arena.alloc(n * BR_COLS);
+      inter = pv.arena.alloc(n * 4 * BR_INTER_SECURE);
+      if (!trace || !inter) st = STWO_ERR_OOM;
+    }
+    if (!st) {
+      StageScope stage("Generation", s);
+      k_br_trace<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_inputs, trace);
+      note_launch();
+      if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
+    }
+    if (!st) {
+      std::vector<uint32_t*> cols(BR_COLS);
+      for (int c = 0; c < BR_COLS; c++) cols[c] = trace + (size_t)c * n;
+      st = pv.commit_evals(cols, log_n_rows);
+    }
+    HBrElements el;
+    if (!st) {
+      el.round.draw(pv.ch, BR_ROUND_FELTS);
+      for (int k = 0; k < 5; k++) el.xr[k].draw(pv.ch, 3);
+      StageScope stage("Interaction", s);
+      BrElements he;
+      el.to_device(he);
+      BrElements* de = reinterpret_cast<BrElements*>(pv.arena.alloc((sizeof(BrElements) + 3) / 4));
+      if (!de) st = STWO_ERR_OOM;
+      if (!st && cudaMemcpyAsync(de, &he, sizeof(BrElements), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        st = STWO_ERR_CUDA;
+      if (!st) {
+        k_br_interaction<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_inputs, de, inter);
+        note_launch();
+        if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
+      }
+    }
+    // The claimed sum is mixed before the interaction commitment (BlakeStatement1::mix_into).
+    if (!st) st = logup_finalize_last(inter + (size_t)4 * (BR_INTER_SECURE - 1) * n, log_n_rows, pv.arena, s, &claimed);
+    if (!st) {
+      pv.ch.mix_felts({claimed});
+      std::vector<uint32_t*> cols(4 * BR_INTER_SECURE);
+      for (int c = 0; c < 4 * BR_INTER_SECURE; c++) cols[c] = inter + (size_t)c * n;
+      st = pv.commit_evals(cols, log_n_rows);
+    }
+    if (!st) {
+      BlakeRoundGpuAir air(log_n_rows, el, claimed);
+      st = pv.prove(air, bytes);
+    }
+    cudaStreamSynchronize(s);
+  }
+  if (st) return st;
+  if (h_claimed_sum)
+    for (int i = 0; i < 4; i++) h_claimed_sum->v[i] = claimed.v[i];
+  *h_len = bytes.size();
+  STWO_REQUIRE(bytes.size() <= capacity, "proof buffer too small (%zu bytes needed)", bytes.size());
+  if (h_proof) memcpy(h_proof, bytes.data(), bytes.size());
+  return STWO_OK;
+}

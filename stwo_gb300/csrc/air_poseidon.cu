@@ -264,6 +264,39 @@ static int32_t scan_rows(uint32_t* data, uint32_t len, uint32_t rows, Arena& are
   return STWO_OK;
 }
 
+// LogupTraceGenerator::finalize_last (logup.rs:150-190) on the device for the last secure column
+// (four contiguous coordinate columns of 2^log_n words): its coordinate sums (the claimed sum),
+// the column minus claimed_sum / 2^log_n, and the inclusive prefix sum in coset order. The sums
+// land in small_pinned(); with `claimed` set the stream is synchronised and the claimed sum
+// returned, otherwise the caller reads small_pinned() after its next synchronisation.
+int32_t logup_finalize_last(uint32_t* last, uint32_t log_n, Arena& arena, cudaStream_t s, hq* claimed) {
+  const size_t n = (size_t)1 << log_n;
+  unsigned long long* d_sums = reinterpret_cast<unsigned long long*>(arena.alloc(8));
+  uint32_t* tmp = arena.alloc(4 * n);
+  if (!d_sums || !tmp) return STWO_ERR_OOM;
+  STWO_CHECK_CUDA(cudaMemsetAsync(d_sums, 0, 32, s));
+  const uint32_t g = std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024);
+  k_column_sums<<<dim3(g, 4), 256, 0, s>>>(last, (uint32_t)n, d_sums);
+  note_launch();
+  STWO_LAUNCH_CHECK();
+  unsigned long long* hs = small_pinned();
+  if (!hs) return STWO_ERR_OOM;
+  STWO_CHECK_CUDA(cudaMemcpyAsync(hs, d_sums, 32, cudaMemcpyDeviceToHost, s));
+  k_coset_gather<<<dim3(g, 4), 256, 0, s>>>(last, log_n, d_sums, h_inv((uint32_t)(n % P)), tmp);
+  note_launch();
+  STWO_LAUNCH_CHECK();
+  int32_t st = scan_rows(tmp, (uint32_t)n, 4, arena, s);
+  if (st) return st;
+  k_coset_scatter<<<dim3(g, 4), 256, 0, s>>>(last, log_n, tmp);
+  note_launch();
+  STWO_LAUNCH_CHECK();
+  if (claimed) {
+    STWO_CHECK_CUDA(cudaStreamSynchronize(s));
+    *claimed = hq_make((uint32_t)(hs[0] % P), (uint32_t)(hs[1] % P), (uint32_t)(hs[2] % P), (uint32_t)(hs[3] % P));
+  }
+  return STWO_OK;
+}
+
 // ------------------------------------------------------------------------------------ composition
 struct PoseidonParams {
   uint32_t trace_log, eval_log;
@@ -619,32 +652,8 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
     }
     if (!st) {
       // Claimed sum of the last column, its shift, and the coset-order prefix sum (logup.rs:155-195).
-      uint32_t* last = inter + (size_t)(PS_INTERACTION_COLS - 4) * n;
-      unsigned long long* d_sums = reinterpret_cast<unsigned long long*>(pv.arena.alloc(8));
-      uint32_t* tmp = pv.arena.alloc(4 * n);
-      if (!d_sums || !tmp) st = STWO_ERR_OOM;
-      if (!st && cudaMemsetAsync(d_sums, 0, 32, s) != cudaSuccess) st = STWO_ERR_CUDA;
-      if (!st) {
-        k_column_sums<<<dim3(std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024), 4), 256, 0, s>>>(last, (uint32_t)n, d_sums);
-        note_launch();
-        // The sums reach the host with the next synchronisation (the interaction commitment's).
-        if (!small_pinned()) st = STWO_ERR_OOM;
-        else if (cudaGetLastError() != cudaSuccess ||
-                 cudaMemcpyAsync(small_pinned(), d_sums, 32, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-          st = STWO_ERR_CUDA;
-      }
-      if (!st) {
-        uint32_t g = std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024);
-        k_coset_gather<<<dim3(g, 4), 256, 0, s>>>(last, log_n_rows, d_sums, h_inv((uint32_t)(n % P)), tmp);
-        note_launch();
-        st = cudaGetLastError() ? STWO_ERR_CUDA : STWO_OK;
-        if (!st) st = scan_rows(tmp, (uint32_t)n, 4, pv.arena, s);
-        if (!st) {
-          k_coset_scatter<<<dim3(g, 4), 256, 0, s>>>(last, log_n_rows, tmp);
-          note_launch();
-          st = cudaGetLastError() ? STWO_ERR_CUDA : STWO_OK;
-        }
-      }
+      // The claimed sum reaches the host with the next synchronisation (the interaction commitment's).
+      st = logup_finalize_last(inter + (size_t)(PS_INTERACTION_COLS - 4) * n, log_n_rows, pv.arena, s, nullptr);
     }
     if (!st) {
       std::vector<uint32_t*> cols(PS_INTERACTION_COLS);

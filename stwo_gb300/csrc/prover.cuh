@@ -114,6 +114,10 @@ struct Prover {
 
 std::vector<hq> line_interpolate_host(stwo_coset dom, std::vector<hq> v);
 
+// LogupTraceGenerator::finalize_last on the device (air_poseidon.cu): claimed sum, shift and
+// coset-order prefix sum of the last secure column (four contiguous coordinate columns).
+int32_t logup_finalize_last(uint32_t* last, uint32_t log_n, Arena& arena, cudaStream_t s, hq* claimed);
+
 template <class T>
 inline void bit_reverse_host(std::vector<T>& v) {
   size_t n = v.size();

@@ -8,8 +8,8 @@
 // queued jobs the first one, in submission order, that fits is started next.
 //
 // The reference proves one statement per call (crates/prover/src/core/prover/mod.rs:27-79) and
-// has no scheduler; this runtime only multiplexes calls of stwo_prove_wide_fib and
-// stwo_prove_poseidon, whose results are unchanged by it.
+// has no scheduler; this runtime only multiplexes calls of stwo_prove_wide_fib,
+// stwo_prove_poseidon and stwo_prove_blake_round, whose results are unchanged by it.
 #include "common.cuh"
 #include <chrono>
 #include <condition_variable>
@@ -48,6 +48,10 @@ size_t job_hbm_bytes(const stwo_proof_job& j) {
     const size_t cols = 1264 + 32 + 8;
     return cols * n * 4 * (1 + blow + 4) + 64 * n * blow + (64u << 20);
   }
+  if (j.air == STWO_AIR_BLAKE_ROUND) {
+    const size_t cols = 384 + 260 + 8;
+    return cols * n * 4 * (1 + blow + 2) + 64 * n * blow + (64u << 20);
+  }
   const size_t cols = j.n_cols + 4;
   return cols * n * 4 * (2 + blow + 2) + 64 * n * blow + (64u << 20);
 }
@@ -56,6 +60,9 @@ int32_t run_job(const stwo_proof_job& j, cudaStream_t s, stwo_proof_result& r) {
   r.len = 0;
   if (j.air == STWO_AIR_POSEIDON) {
     return stwo_prove_poseidon(j.log_n_rows, j.d_init, j.cfg, j.h_proof, j.capacity, &r.len, &r.claimed_sum, s);
+  }
+  if (j.air == STWO_AIR_BLAKE_ROUND) {
+    return stwo_prove_blake_round(j.log_n_rows, j.d_init, j.cfg, j.h_proof, j.capacity, &r.len, &r.claimed_sum, s);
   }
   STWO_REQUIRE(j.air == STWO_AIR_WIDE_FIB, "unknown AIR %u", j.air);
   STWO_REQUIRE(j.d_a && j.d_b, "wide-Fibonacci job without its first two columns");

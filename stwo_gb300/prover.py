@@ -61,13 +61,28 @@ def prove_poseidon(log_n_rows: int, init=None, cfg=DEFAULT_CONFIG):
     return C.string_at(buf, n.value), tuple(cs.v)
 
 
+def prove_blake_round(log_n_rows: int, inputs=None, cfg=DEFAULT_CONFIG):
+    """Proves the Blake2s round AIR; `inputs` is None (the reference test's inputs) or a device
+    int32 tensor of 32 words per row (16 state words, then 16 message words). Returns (proof
+    bytes, claimed LogUp sum)."""
+    from ._lib import QM31
+
+    buf = _out()
+    n = C.c_size_t()
+    cs = QM31()
+    call("stwo_prove_blake_round", log_n_rows, inputs.data_ptr() if inputs is not None else None, pcs_config(cfg),
+         buf, _OUT_CAP, C.byref(n), C.byref(cs), _stream())
+    return C.string_at(buf, n.value), tuple(cs.v)
+
+
 # ------------------------------------------------------------------ batched and served proving
-AIR_WIDE_FIB, AIR_POSEIDON = 0, 1
+AIR_WIDE_FIB, AIR_POSEIDON, AIR_BLAKE_ROUND = 0, 1, 2
 
 
 class Job:
-    """One whole-proof job: wide-Fibonacci (a, b device tensors of 2^log_n_rows words) or
-    Poseidon2 (init device tensor, or None for the reference inputs)."""
+    """One whole-proof job: wide-Fibonacci (a, b device tensors of 2^log_n_rows words), Poseidon2
+    or the Blake2s round AIR (init: a device tensor of initial states / round inputs, or None for
+    the reference inputs)."""
 
     def __init__(self, air: int, log_n_rows: int, cfg=DEFAULT_CONFIG, n_cols: int = 0, a=None, b=None, init=None,
                  capacity: int = 1 << 22):
