@@ -410,19 +410,21 @@ class BatchWorkload:
     """Mixed batch of whole proofs: n jobs, half wide-Fibonacci (100 columns, 2^log rows) and half
     Poseidon2 (2^log instances = 2^(log-3) rows), log sizes uniform in [lo, hi] from `seed`, each
     with its seeded inputs resident in HBM. Wide-Fibonacci uses PcsConfig::default(); Poseidon2
-    pow_bits 10."""
+    pow_bits 10. With arrivals (the served workload) the AIR of each request is uniform over
+    wide-Fibonacci, Poseidon2 and the Blake2s round AIR (2^log rows of one BLAKE2s round each,
+    uniform 32-bit state and message words, PcsConfig::default())."""
 
     def __init__(self, n=64, lo=10, hi=18, seed=4, arrivals=None):
         import numpy as np
         import torch
 
-        from stwo_gb300.prover import AIR_POSEIDON, AIR_WIDE_FIB
+        from stwo_gb300.prover import AIR_BLAKE_ROUND, AIR_POSEIDON, AIR_WIDE_FIB
 
         rng = np.random.default_rng(seed)
         if arrivals is None:
             airs = rng.permutation([AIR_WIDE_FIB] * (n // 2) + [AIR_POSEIDON] * (n - n // 2))
         else:
-            airs = rng.integers(0, 2, n)
+            airs = rng.integers(0, 3, n)
         logs = rng.integers(lo, hi + 1, n)
         self.arrivals = arrivals
         self.specs = []
@@ -432,6 +434,11 @@ class BatchWorkload:
                 rows = int(log)
                 words = gen_words(40 + seed, i, 2 << rows)
                 cfg, cols = (5, 1, 0, 3), 100
+            elif air == AIR_BLAKE_ROUND:
+                rows = int(log)
+                words = np.random.default_rng((seed, i)).integers(0, 2**32, (1 << rows) * 32, dtype=np.uint64)
+                words = words.astype(np.uint32)
+                cfg, cols = (5, 1, 0, 3), 0
             else:
                 rows = int(log) - 3
                 words = gen_words(40 + seed, i, (1 << rows) * 128)
@@ -441,7 +448,8 @@ class BatchWorkload:
             self.host.append(h)
             self.specs.append((int(air), rows, cols, cfg))
         self.dev = [h.cuda() for h in self.host]
-        self.cells = sum((1 << r) * (c if a == AIR_WIDE_FIB else 1296) for a, r, c, _ in self.specs)
+        cells_per_row = {AIR_WIDE_FIB: None, AIR_POSEIDON: 1296, AIR_BLAKE_ROUND: 384 + 260}
+        self.cells = sum((1 << r) * (c if a == AIR_WIDE_FIB else cells_per_row[a]) for a, r, c, _ in self.specs)
 
     def jobs(self, from_host=False):
         from stwo_gb300.prover import AIR_WIDE_FIB, Job
@@ -467,7 +475,7 @@ def run_batch(args, world, rank, local, lib, barrier, max_over_ranks):
     from stwo_gb300.prover import prove_batch
 
     wl = BatchWorkload()
-    workers = args.workers or 16  # 4: 1,085 proofs/s, 8: 1,063, 16: 1,129, 32: 758 on GB300
+    workers = args.workers or 16  # on GB300: 8 workers 38.7 ms per batch, 12: 37.7, 16: 38.0, 24: 40.9
 
     def run(n_workers, from_host=False):
         jobs = wl.jobs(from_host)
@@ -519,9 +527,80 @@ def run_batch(args, world, rank, local, lib, barrier, max_over_ranks):
     print(json.dumps(line), flush=True)
 
 
+def run_blake_round(args, world, rank, local, lib, barrier, max_over_ranks):
+    """One proof of the Blake2s round AIR (BlakeRoundComponent alone): 2^log rows (default 16) of
+    one BLAKE2s round each, uniform 32-bit state and message words, PcsConfig::default()."""
+    import numpy as np
+    import torch
+
+    from stwo_gb300 import _lib
+    from stwo_gb300.prover import prove_blake_round
+
+    log = args.log_rows or 16
+    cfg = (5, 1, 0, 3)
+    n = (1 << log) * 32
+    host = torch.empty(n, dtype=torch.int32).pin_memory()
+    host.numpy().view(np.uint32)[:] = np.random.default_rng(11).integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    inp = host.cuda()
+    cells = (1 << log) * (384 + 260)
+    for _ in range(args.warmup):
+        prove_blake_round(log, inp, cfg)
+    barrier()
+    launches0 = lib.stwo_kernel_launches()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            proof, _ = prove_blake_round(log, inp, cfg)
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    launches = lib.stwo_kernel_launches() - launches0
+    step_ms = max_over_ranks(float(np.mean(times)))
+    work = torch.empty_like(inp)
+    et = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        work.copy_(host, non_blocking=True)
+        prove_blake_round(log, work, cfg)
+        torch.cuda.synchronize()
+        et.append((time.perf_counter() - t1) * 1e3)
+    e2e_ms = max_over_ranks(float(np.mean(et)))
+    _lib.call("stwo_set_stage_timing", 1)
+    prove_blake_round(log, inp, cfg)
+    names = (C.c_char_p * 64)()
+    ms = (C.c_float * 64)()
+    k = lib.stwo_stage_times(names, ms, 64)
+    _lib.call("stwo_set_stage_timing", 0)
+    stages = {names[i].decode(): float(ms[i]) for i in range(min(k, 64)) if not names[i].decode().startswith("host")}
+    if rank != 0:
+        return
+    line = {
+        "metric": f"Blake2s round AIR proof s & trace cells/s (2^{log} rows)",
+        "value": cells * world / (step_ms / 1e3), "unit": "trace cells/s", "proof_s": step_ms / 1e3,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
+        "data": "synthetic: uniform 32-bit state and message words (seed 11)",
+        "config": {"workload": f"Blake2s round AIR (BlakeRoundComponent alone), 2^{log} rows, 384 trace + 260 "
+                               "interaction columns", "log_n_rows": log, "trace_cells": cells,
+                   "pcs_config": list(cfg), "l2": "working set larger than L2; no flush",
+                   "parallelism": f"replicas x{world}"},
+        "proof_bytes": len(proof),
+        "stages_ms": stages,
+        "e2e": {"value": cells * world / (e2e_ms / 1e3), "unit": "trace cells/s", "proof_s": e2e_ms / 1e3,
+                "h2d_bytes_per_step": n * 4, "d2h_bytes_per_step": len(proof)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args, world, rank, local, lib, barrier, max_over_ranks):
-    """Served proving: Poisson arrivals (rate 200/s, seed 5), wide-Fibonacci or Poseidon2 uniform,
-    log sizes 12..20, HBM budget 150 GB; latency percentiles beside a plain one-at-a-time server."""
+    """Served proving: Poisson arrivals (rate 200/s, seed 5), AIR uniform over wide-Fibonacci,
+    Poseidon2 and the Blake2s round AIR, log sizes 12..20, HBM budget 150 GB; latency percentiles
+    beside a plain one-at-a-time server."""
     import numpy as np
     import torch
 
@@ -567,15 +646,18 @@ def run_serve(args, world, rank, local, lib, barrier, max_over_ranks):
     p50 = float(np.median([pct(r, 0.50) for r, _ in runs]))
     same = all(a.proof == b.proof for a, b in zip(runs[-1][0], plain))
     line = {
-        "metric": "served p99 latency vs plain (Poisson 200/s, wide-Fibonacci / Poseidon2, log 12..20)",
+        "metric": "served p99 latency vs plain (Poisson 200/s, wide-Fibonacci / Poseidon2 / Blake2s round, "
+                  "log 12..20)",
         "value": p99, "unit": "ms (p99 latency)",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": float(np.mean([w for _, w in runs])) * 1e3,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
         "data": "synthetic: Poisson arrivals and sizes from seed 5, seeded inputs (splitmix64 mod P)",
         "config": {"workload": f"{n_req} requests, Poisson rate 200/s, AIR uniform in {{wide-Fibonacci (100 cols), "
-                               f"Poseidon2}}, log size uniform 12..20, HBM budget 150 GB", "workers": workers,
-                   "blake_round_air": "not built (constraint kernel for the Blake round AIR is a next step)",
+                               f"Poseidon2, Blake2s round (BlakeRoundComponent alone)}}, log size uniform 12..20, "
+                               f"HBM budget 150 GB", "workers": workers,
+                   "air_mix": {name: int(sum(1 for a, _, _, _ in wl.specs if a == k))
+                               for k, name in ((0, "wide_fib"), (1, "poseidon2"), (2, "blake2s_round"))},
                    "l2": "working set larger than L2; no flush", "parallelism": f"replicas x{world}"},
         "p50_ms": p50,
         "plain": {"p99_ms": pct(plain, 0.99), "p50_ms": pct(plain, 0.50), "wall_s": plain_wall,
@@ -632,6 +714,8 @@ def run_gb300(args):
         return run_batch(args, world, rank, local, lib, barrier, max_over_ranks)
     if args.workload == "serve":
         return run_serve(args, world, rank, local, lib, barrier, max_over_ranks)
+    if args.workload == "blake_round":
+        return run_blake_round(args, world, rank, local, lib, barrier, max_over_ranks)
 
     wl = PoseidonWorkload(log=args.log_rows)
     for _ in range(args.warmup):
@@ -909,10 +993,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="poseidon", choices=["poseidon", "kernels", "gkr", "batch", "serve"],
+    ap.add_argument("--workload", default="poseidon", choices=["poseidon", "kernels", "gkr", "batch", "serve",
+                                                                "blake_round"],
                     help="poseidon: the headline Poseidon2 2^16-row proof; kernels: the kernel microbench; "
                          "gkr: GKR batch proof of 2^20 LogUp leaves; batch: 64 mixed proofs on a worker pool; "
-                         "serve: Poisson-arrival serving with latency percentiles")
+                         "serve: Poisson-arrival serving with latency percentiles; blake_round: one proof of the "
+                         "Blake2s round AIR")
     ap.add_argument("--workers", type=int, default=0, help="worker streams of the batch (16) / serve (8) workloads")
     ap.add_argument("--requests", type=int, default=0, help="requests of the serve workload (200)")
     ap.add_argument("--cpu-threads", type=int, default=0)
