@@ -33,13 +33,20 @@ struct BrElements {
 };
 
 __device__ __forceinline__ int br_xor_index(uint32_t w) { return w == 12 ? 0 : w == 9 ? 1 : w == 8 ? 2 : w == 7 ? 3 : 4; }
-// Four words of the relation elements in global memory (read-only loads: never a parameter's address).
-__device__ __forceinline__ qm31 br_q(const uint32_t* v) { return qm31_from_u32(__ldg(v), __ldg(v + 1), __ldg(v + 2), __ldg(v + 3)); }
+// Four words of the relation elements (a block's shared-memory copy; plain loads, valid for any
+// address space).
+__device__ __forceinline__ qm31 br_q(const uint32_t* v) { return qm31_from_u32(v[0], v[1], v[2], v[3]); }
+
+// The block's copy of the relation elements (1,856 bytes), read by every row's combines.
+__device__ __forceinline__ void br_stage_elements(const BrElements* __restrict__ e, BrElements* s) {
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(e);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(s);
+  for (uint32_t i = threadIdx.x; i < sizeof(BrElements) / 4; i += blockDim.x) dst[i] = __ldg(src + i);
+}
 
 // LookupElements::combine for one XOR lookup: a + alpha b + alpha^2 c - z (logup.rs:95-113).
-// The elements live in device memory (read through the read-only cache, the same words for
-// every thread): a kernel parameter of this size, addressed by index, would be copied to each
-// thread's stack.
+// The elements reach the kernels through device memory, staged into shared memory per block: a
+// kernel parameter of this size, addressed by index, would be copied to each thread's stack.
 __device__ __forceinline__ qm31 br_xor_combine(const BrElements* e, uint32_t w, uint32_t a, uint32_t b, uint32_t c) {
   const int k = br_xor_index(w);
   qm31 acc = qm31_add(qm31_add(qm31_mul_m31(br_q(e->xa[k][0]), a), qm31_mul_m31(br_q(e->xa[k][1]), b)),
@@ -47,19 +54,56 @@ __device__ __forceinline__ qm31 br_xor_combine(const BrElements* e, uint32_t w, 
   return qm31_sub(acc, br_q(e->xz[k]));
 }
 
-__device__ __forceinline__ void br_inputs(const uint32_t* in, uint32_t r, uint32_t v[BR_ST], uint32_t m[BR_ST]) {
+// Word i of row r's round inputs: the 16 state words then the 16 message words, or the
+// reference test's inputs (v_i = i, m_i = i + 1) when `in` is NULL.
+__device__ __forceinline__ uint32_t br_input(const uint32_t* in, uint32_t r, uint32_t i) {
+  return in ? __ldg(in + (size_t)r * 32 + i) : (i < BR_ST ? i : i - BR_ST + 1);
+}
+
+// The state is kept as four rows of four words (v[0..3] the a's, v[4..7] the b's, v[8..11] the
+// c's, v[12..15] the d's), and every G works on column 0: after each G all rows rotate left by
+// one, and between the column and the diagonal half the rows are diagonalised (row k rotated
+// left by k). The eight G-functions then run as one loop body with fixed register operands; the
+// order of G calls, and so of trace columns and lookups, is the reference's
+// (round/constraints.rs:25-64).
+template <class T>
+__device__ __forceinline__ void br_rotate_rows(T v[BR_ST]) {
 #pragma unroll
-  for (int i = 0; i < BR_ST; i++) {
-    v[i] = in ? __ldg(in + (size_t)r * 32 + i) : (uint32_t)i;
-    m[i] = in ? __ldg(in + (size_t)r * 32 + 16 + i) : (uint32_t)(i + 1);
+  for (int k = 0; k < 4; k++) {
+    const T t = v[4 * k];
+    v[4 * k] = v[4 * k + 1];
+    v[4 * k + 1] = v[4 * k + 2];
+    v[4 * k + 2] = v[4 * k + 3];
+    v[4 * k + 3] = t;
   }
+}
+template <class T>
+__device__ __forceinline__ void br_rotate_row(T v[BR_ST], int k, int by) {
+  T t[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) t[j] = v[4 * k + ((j + by) & 3)];
+#pragma unroll
+  for (int j = 0; j < 4; j++) v[4 * k + j] = t[j];
+}
+template <class T>
+__device__ __forceinline__ void br_diagonalize(T v[BR_ST]) {
+  br_rotate_row(v, 1, 1);
+  br_rotate_row(v, 2, 2);
+  br_rotate_row(v, 3, 3);
+}
+template <class T>
+__device__ __forceinline__ void br_undiagonalize(T v[BR_ST]) {
+  br_rotate_row(v, 1, 3);
+  br_rotate_row(v, 2, 2);
+  br_rotate_row(v, 3, 1);
 }
 
 // ------------------------------------------------------------------------------------------ trace
-// One row of TraceGeneratorRow::generate. The visitor gets every trace felt in column order and
-// every XOR lookup (w, a, b, a ^ b) in lookup order.
-template <class V>
-__device__ __forceinline__ void br_round(uint32_t v[BR_ST], const uint32_t m[BR_ST], V& vis) {
+// One row of TraceGeneratorRow::generate from the G-functions on: the visitor gets every trace
+// felt in column order and every XOR lookup (w, a, b, a ^ b) in lookup order; msg(i) is message
+// word i.
+template <class V, class M>
+__device__ __forceinline__ void br_round(uint32_t v[BR_ST], M msg, V& vis) {
   auto u32 = [&](uint32_t x) {
     vis.felt(x & 0xffffu);
     vis.felt(x >> 16);
@@ -74,60 +118,44 @@ __device__ __forceinline__ void br_round(uint32_t v[BR_ST], const uint32_t m[BR_
     vis.felt(c);
     vis.lookup(w, a, b, c);
   };
+  // xor_rotr_u32 (rr < 16) and xor_rotr16_u32 (both halves split at 8, all four lookups of width 8).
   auto xor_rotr = [&](uint32_t a, uint32_t b, uint32_t rr) {
     const uint32_t c = a ^ b;
+    const uint32_t sp = rr == 16 ? 8 : rr;
     uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
-    split(a & 0xffffu, rr, all, alh);
-    split(a >> 16, rr, ahl, ahh);
-    split(b & 0xffffu, rr, bll, blh);
-    split(b >> 16, rr, bhl, bhh);
-    xor1(rr, all, bll);
-    xor1(rr, ahl, bhl);
-    xor1(16 - rr, alh, blh);
-    xor1(16 - rr, ahh, bhh);
+    split(a & 0xffffu, sp, all, alh);
+    split(a >> 16, sp, ahl, ahh);
+    split(b & 0xffffu, sp, bll, blh);
+    split(b >> 16, sp, bhl, bhh);
+    xor1(sp, all, bll);
+    xor1(sp, ahl, bhl);
+    xor1(16 - sp, alh, blh);
+    xor1(16 - sp, ahh, bhh);
     return (c >> rr) | (c << (32 - rr));
   };
-  // xor_rotr16_u32: both halves split at 8, all four lookups of width 8.
-  auto xor_rotr16 = [&](uint32_t a, uint32_t b) {
-    const uint32_t c = a ^ b;
-    uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
-    split(a & 0xffffu, 8, all, alh);
-    split(a >> 16, 8, ahl, ahh);
-    split(b & 0xffffu, 8, bll, blh);
-    split(b >> 16, 8, bhl, bhh);
-    xor1(8, all, bll);
-    xor1(8, ahl, bhl);
-    xor1(8, alh, blh);
-    xor1(8, ahh, bhh);
-    return (c >> 16) | (c << 16);
-  };
-  auto g = [&](int ia, int ib, int ic, int id, uint32_t m0, uint32_t m1) {
-    uint32_t a = v[ia], b = v[ib], c = v[ic], d = v[id];
-    a = a + b + m0;
+#pragma unroll 1
+  for (int it = 0; it < 8; it++) {
+    if (it == 4) br_diagonalize(v);
+    uint32_t a = v[0], b = v[4], c = v[8], d = v[12];
+    a = a + b + msg(2 * it);
     u32(a);
-    d = xor_rotr16(a, d);
+    d = xor_rotr(a, d, 16);
     c = c + d;
     u32(c);
     b = xor_rotr(b, c, 12);
-    a = a + b + m1;
+    a = a + b + msg(2 * it + 1);
     u32(a);
     d = xor_rotr(a, d, 8);
     c = c + d;
     u32(c);
     b = xor_rotr(b, c, 7);
-    v[ia] = a;
-    v[ib] = b;
-    v[ic] = c;
-    v[id] = d;
-  };
-  g(0, 4, 8, 12, m[0], m[1]);
-  g(1, 5, 9, 13, m[2], m[3]);
-  g(2, 6, 10, 14, m[4], m[5]);
-  g(3, 7, 11, 15, m[6], m[7]);
-  g(0, 5, 10, 15, m[8], m[9]);
-  g(1, 6, 11, 12, m[10], m[11]);
-  g(2, 7, 8, 13, m[12], m[13]);
-  g(3, 4, 9, 14, m[14], m[15]);
+    v[0] = a;
+    v[4] = b;
+    v[8] = c;
+    v[12] = d;
+    br_rotate_rows(v);
+  }
+  br_undiagonalize(v);
 }
 
 struct BrTraceWriter {
@@ -139,26 +167,26 @@ struct BrTraceWriter {
   __device__ void lookup(uint32_t, uint32_t, uint32_t, uint32_t) {}
 };
 
-// inputs: per row 16 state words then 16 message words, or NULL for the reference test's inputs
-// (v_i = i, m_i = i + 1).
+// inputs: per row 16 state words then 16 message words, or NULL for the reference test's inputs.
 __global__ void __launch_bounds__(128) k_br_trace(uint32_t n_rows, const uint32_t* __restrict__ inputs,
                                                   uint32_t* __restrict__ trace) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
-  uint32_t v[BR_ST], m[BR_ST];
-  br_inputs(inputs, r, v, m);
+  uint32_t v[BR_ST];
   BrTraceWriter w{trace, n_rows, r};
 #pragma unroll
   for (int i = 0; i < BR_ST; i++) {
+    v[i] = br_input(inputs, r, i);
     w.felt(v[i] & 0xffffu);
     w.felt(v[i] >> 16);
   }
 #pragma unroll
   for (int i = 0; i < BR_ST; i++) {
-    w.felt(m[i] & 0xffffu);
-    w.felt(m[i] >> 16);
+    const uint32_t m = br_input(inputs, r, BR_ST + i);
+    w.felt(m & 0xffffu);
+    w.felt(m >> 16);
   }
-  br_round(v, m, w);
+  br_round(v, [&](int i) { return br_input(inputs, r, BR_ST + i); }, w);
 }
 
 // ------------------------------------------------------------------------------------ interaction
@@ -195,22 +223,27 @@ struct BrInteractionWriter {
 };
 
 __global__ void __launch_bounds__(128) k_br_interaction(uint32_t n_rows, const uint32_t* __restrict__ inputs,
-                                                        const BrElements* __restrict__ e, uint32_t* __restrict__ out) {
+                                                        const BrElements* __restrict__ e_dev, uint32_t* __restrict__ out) {
+  __shared__ BrElements s_e;
+  br_stage_elements(e_dev, &s_e);
+  __syncthreads();
+  const BrElements* e = &s_e;
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
-  uint32_t v[BR_ST], m[BR_ST];
-  br_inputs(inputs, r, v, m);
   // The Round relation's denominator: sum_k alpha^k x_k - z over (input, output, message) halves.
   qm31 p = qm31_zero();
+  uint32_t v[BR_ST];
 #pragma unroll
   for (int i = 0; i < BR_ST; i++) {
+    v[i] = br_input(inputs, r, i);
+    const uint32_t m = br_input(inputs, r, BR_ST + i);
     p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i]), v[i] & 0xffffu));
     p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i + 1]), v[i] >> 16));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), m[i] & 0xffffu));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), m[i] >> 16));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), m & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), m >> 16));
   }
   BrInteractionWriter w{e, out, n_rows, r};
-  br_round(v, m, w);
+  br_round(v, [&](int i) { return br_input(inputs, r, BR_ST + i); }, w);
 #pragma unroll
   for (int i = 0; i < BR_ST; i++) {
     p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i]), v[i] & 0xffffu));
@@ -237,6 +270,19 @@ __device__ __forceinline__ uint32_t br_prev_row(uint32_t r, uint32_t trace_log, 
   return brev(prev, eval_log);
 }
 
+__device__ __forceinline__ uint32_t br_inv16(uint32_t x) { return m31_mul(x, 1u << 15); }
+// A 64-bit sum of M31 products, reduced to [0, P).
+__device__ __forceinline__ uint32_t br_fold64(unsigned long long x) {
+  x = (x & P) + (x >> 31);
+  x = (x & P) + (x >> 31);
+  const uint32_t r = (uint32_t)x;
+  return r >= P ? r - P : r;
+}
+
+struct BrU {
+  uint32_t l, h;
+};
+
 // The constraint evaluator at one row of the evaluation domain (F = M31). Trace masks are read in
 // the evaluator's column order; each XOR pair's LogUp constraint is accumulated as soon as its two
 // lookups are known, with its own coefficient (the random-coefficient sum is exact in the field,
@@ -244,18 +290,21 @@ __device__ __forceinline__ uint32_t br_prev_row(uint32_t r, uint32_t trace_log, 
 struct BrRowEval {
   const uint32_t* trace;
   const uint32_t* inter;
+  const BrElements* e;
+  const uint32_t* coeffs;  // 4 words per constraint, in constraint order (shared memory)
   uint32_t el, r;
-  const uint32_t* coeffs;  // 4 words per constraint, in constraint order
-  uint32_t col = 0;
-  uint32_t ci = 0;  // round (carry) constraint index
-  uint32_t batch = 0;
+  uint32_t col;
+  uint32_t ci = 0;     // carry constraint index
+  uint32_t batch = 0;  // LogUp batch index
   unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
   uint32_t cnt = 0;
   qm31 logup = qm31_zero();
   qm31 prev_col = qm31_zero();
+  qm31 round_p = qm31_zero();
 
-  __device__ uint32_t mask() { return __ldg(trace + ((size_t)col++ << el) + r); }
-  __device__ void carry_constraint(uint32_t c) {
+  __device__ __forceinline__ uint32_t load(uint32_t c) const { return __ldg(trace + ((size_t)c << el) + r); }
+  __device__ __forceinline__ uint32_t mask() { return load(col++); }
+  __device__ __forceinline__ void carry_constraint(uint32_t c) {
     const uint32_t* k = coeffs + 4 * ci++;
     a0 += (unsigned long long)k[0] * c;
     a1 += (unsigned long long)k[1] * c;
@@ -269,153 +318,121 @@ struct BrRowEval {
       cnt = 0;
     }
   }
-  __device__ void logup_constraint(const qm31& c) {
+  __device__ __forceinline__ void logup_constraint(const qm31& c) {
     const uint32_t* k = coeffs + 4 * (64 + batch++);
     logup = qm31_add(logup, qm31_mul(qm31_from_u32(k[0], k[1], k[2], k[3]), c));
   }
-  __device__ qm31 inter_at(uint32_t b, uint32_t row) const {
+  __device__ __forceinline__ qm31 inter_at(uint32_t b, uint32_t row) const {
     const uint32_t* base = inter + (((size_t)4 * b) << el) + row;
     return qm31_from_u32(__ldg(base), __ldg(base + ((size_t)1 << el)), __ldg(base + ((size_t)2 << el)),
                          __ldg(base + ((size_t)3 << el)));
   }
+  // Round relation contribution of one (low, high) pair at position k of the 96 values.
+  __device__ __forceinline__ void round_felts(uint32_t k, const BrU& x) {
+    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[k]), x.l));
+    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[k + 1]), x.h));
+  }
+  // Message word i (columns 32 + 2i, 33 + 2i), used once, by its G.
+  __device__ __forceinline__ BrU msg(uint32_t i) {
+    BrU x{load(2 * BR_ST + 2 * i), load(2 * BR_ST + 2 * i + 1)};
+    round_felts(64 + 2 * i, x);
+    return x;
+  }
+  __device__ __forceinline__ BrU add2(BrU a, BrU b) {
+    BrU s{mask(), mask()};
+    const uint32_t cl = br_inv16(m31_sub(m31_add(a.l, b.l), s.l));
+    carry_constraint(m31_sub(m31_mul(cl, cl), cl));
+    const uint32_t ch = br_inv16(m31_sub(m31_add(m31_add(a.h, b.h), cl), s.h));
+    carry_constraint(m31_sub(m31_mul(ch, ch), ch));
+    return s;
+  }
+  __device__ __forceinline__ BrU add3(BrU a, BrU b, BrU c) {
+    BrU s{mask(), mask()};
+    const uint32_t cl = br_inv16(m31_sub(m31_add(m31_add(a.l, b.l), c.l), s.l));
+    carry_constraint(m31_mul(m31_mul(cl, m31_sub(cl, 1u)), m31_sub(cl, 2u)));
+    const uint32_t ch = br_inv16(m31_sub(m31_add(m31_add(m31_add(a.h, b.h), c.h), cl), s.h));
+    carry_constraint(m31_mul(m31_mul(ch, m31_sub(ch, 1u)), m31_sub(ch, 2u)));
+    return s;
+  }
+  // split_unchecked: (a - h 2^rr, h) with h from the trace.
+  __device__ __forceinline__ void split(uint32_t a, uint32_t rr, uint32_t& l, uint32_t& h) {
+    h = mask();
+    l = m31_sub(a, m31_mul(h, 1u << rr));
+  }
+  // Two XOR lookups (one LogUp batch): constraint (cur - prev) * p0 p1 - (p0 + p1).
+  __device__ __forceinline__ void xor2(uint32_t w, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1, uint32_t& c0,
+                                       uint32_t& c1) {
+    c0 = mask();
+    c1 = mask();
+    const qm31 p0 = br_xor_combine(e, w, a0, b0, c0);
+    const qm31 p1 = br_xor_combine(e, w, a1, b1, c1);
+    const qm31 cur = inter_at(batch, r);
+    const qm31 diff = qm31_sub(cur, prev_col);
+    prev_col = cur;
+    logup_constraint(qm31_sub(qm31_mul(diff, qm31_mul(p0, p1)), qm31_add(p0, p1)));
+  }
+  // xor_rotr_u32 (rr < 16) or xor_rotr16_u32 (rr == 16: halves split at 8).
+  __device__ __forceinline__ BrU xor_rotr(BrU a, BrU b, uint32_t rr) {
+    const uint32_t sp = rr == 16 ? 8 : rr;
+    uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
+    split(a.l, sp, all, alh);
+    split(a.h, sp, ahl, ahh);
+    split(b.l, sp, bll, blh);
+    split(b.h, sp, bhl, bhh);
+    uint32_t xll, xhl, xlh, xhh;
+    xor2(sp, all, ahl, bll, bhl, xll, xhl);
+    xor2(16 - sp, alh, ahh, blh, bhh, xlh, xhh);
+    if (rr == 16) return BrU{m31_add(m31_mul(xhh, 1u << 8), xhl), m31_add(m31_mul(xlh, 1u << 8), xll)};
+    return BrU{m31_add(m31_mul(xhl, 1u << (16 - rr)), xlh), m31_add(m31_mul(xll, 1u << (16 - rr)), xhh)};
+  }
 };
 
-__device__ __forceinline__ uint32_t br_inv16(uint32_t x) { return m31_mul(x, 1u << 15); }
-// A 64-bit sum of M31 products, reduced to [0, P).
-__device__ __forceinline__ uint32_t br_fold64(unsigned long long x) {
-  x = (x & P) + (x >> 31);
-  x = (x & P) + (x >> 31);
-  const uint32_t r = (uint32_t)x;
-  return r >= P ? r - P : r;
-}
-
-__global__ void __launch_bounds__(128) k_br_composition(const uint32_t* __restrict__ trace,
+__global__ void __launch_bounds__(128, 4) k_br_composition(const uint32_t* __restrict__ trace,
                                                         const uint32_t* __restrict__ inter, uint32_t n_rows,
-                                                        BrParams pp, const BrElements* __restrict__ e,
+                                                        BrParams pp, const BrElements* __restrict__ e_dev,
                                                         const uint32_t* __restrict__ coeffs,
                                                         const uint32_t* __restrict__ dinv, uint32_t* o0,
                                                         uint32_t* o1, uint32_t* o2, uint32_t* o3) {
   __shared__ uint32_t s_coeffs[4 * BR_N_CONSTRAINTS];
+  __shared__ BrElements s_e;
   for (uint32_t i = threadIdx.x; i < 4 * BR_N_CONSTRAINTS; i += blockDim.x) s_coeffs[i] = coeffs[i];
+  br_stage_elements(e_dev, &s_e);
   __syncthreads();
+  const BrElements* e = &s_e;
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
-  BrRowEval ev{trace, inter, pp.eval_log, r, s_coeffs};
-  struct U {
-    uint32_t l, h;
-  };
-  U v[BR_ST];
-  qm31 round_p = qm31_zero();
+  BrRowEval ev{trace, inter, e, s_coeffs, pp.eval_log, r, 0};
+  BrU v[BR_ST];
 #pragma unroll
   for (int i = 0; i < BR_ST; i++) {
     v[i].l = ev.mask();
     v[i].h = ev.mask();
-    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[2 * i]), v[i].l));
-    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[2 * i + 1]), v[i].h));
+    ev.round_felts(2 * i, v[i]);
   }
-  // The message masks follow the state's; each message word is used by exactly one G, in order.
-  const uint32_t m_col = 2 * BR_ST;
+  // The message masks (columns 32..63) are read by their G; the G masks follow them.
   ev.col = 4 * BR_ST;
-  auto msg = [&](int i) {
-    U x;
-    x.l = __ldg(trace + ((size_t)(m_col + 2 * i) << pp.eval_log) + r);
-    x.h = __ldg(trace + ((size_t)(m_col + 2 * i + 1) << pp.eval_log) + r);
-    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), x.l));
-    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), x.h));
-    return x;
-  };
-  auto add2 = [&](U a, U b) {
-    U s;
-    s.l = ev.mask();
-    s.h = ev.mask();
-    const uint32_t cl = br_inv16(m31_sub(m31_add(a.l, b.l), s.l));
-    ev.carry_constraint(m31_sub(m31_mul(cl, cl), cl));
-    const uint32_t ch = br_inv16(m31_sub(m31_add(m31_add(a.h, b.h), cl), s.h));
-    ev.carry_constraint(m31_sub(m31_mul(ch, ch), ch));
-    return s;
-  };
-  auto add3 = [&](U a, U b, U c) {
-    U s;
-    s.l = ev.mask();
-    s.h = ev.mask();
-    const uint32_t cl = br_inv16(m31_sub(m31_add(m31_add(a.l, b.l), c.l), s.l));
-    ev.carry_constraint(m31_mul(m31_mul(cl, m31_sub(cl, 1u)), m31_sub(cl, 2u)));
-    const uint32_t ch = br_inv16(m31_sub(m31_add(m31_add(m31_add(a.h, b.h), c.h), cl), s.h));
-    ev.carry_constraint(m31_mul(m31_mul(ch, m31_sub(ch, 1u)), m31_sub(ch, 2u)));
-    return s;
-  };
-  auto split = [&](uint32_t a, uint32_t rr, uint32_t& l, uint32_t& h) {
-    h = ev.mask();
-    l = m31_sub(a, m31_mul(h, 1u << rr));
-  };
-  // Two XOR lookups (one LogUp batch): constraint (cur - prev) * p0 p1 - (p0 + p1).
-  auto xor2 = [&](uint32_t w, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1, uint32_t& c0, uint32_t& c1) {
-    c0 = ev.mask();
-    c1 = ev.mask();
-    const qm31 p0 = br_xor_combine(e, w, a0, b0, c0);
-    const qm31 p1 = br_xor_combine(e, w, a1, b1, c1);
-    const qm31 cur = ev.inter_at(ev.batch, r);
-    const qm31 diff = qm31_sub(cur, ev.prev_col);
-    ev.prev_col = cur;
-    ev.logup_constraint(qm31_sub(qm31_mul(diff, qm31_mul(p0, p1)), qm31_add(p0, p1)));
-  };
-  auto xor_rotr = [&](U a, U b, uint32_t rr) {
-    uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
-    split(a.l, rr, all, alh);
-    split(a.h, rr, ahl, ahh);
-    split(b.l, rr, bll, blh);
-    split(b.h, rr, bhl, bhh);
-    uint32_t xll, xhl, xlh, xhh;
-    xor2(rr, all, ahl, bll, bhl, xll, xhl);
-    xor2(16 - rr, alh, ahh, blh, bhh, xlh, xhh);
-    U o;
-    o.l = m31_add(m31_mul(xhl, 1u << (16 - rr)), xlh);
-    o.h = m31_add(m31_mul(xll, 1u << (16 - rr)), xhh);
-    return o;
-  };
-  auto xor_rotr16 = [&](U a, U b) {
-    uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
-    split(a.l, 8, all, alh);
-    split(a.h, 8, ahl, ahh);
-    split(b.l, 8, bll, blh);
-    split(b.h, 8, bhl, bhh);
-    uint32_t xll, xhl, xlh, xhh;
-    xor2(8, all, ahl, bll, bhl, xll, xhl);
-    xor2(8, alh, ahh, blh, bhh, xlh, xhh);
-    U o;
-    o.l = m31_add(m31_mul(xhh, 1u << 8), xhl);
-    o.h = m31_add(m31_mul(xlh, 1u << 8), xll);
-    return o;
-  };
-  auto g = [&](int ia, int ib, int ic, int id, int mi) {
-    U a = v[ia], b = v[ib], c = v[ic], d = v[id];
-    a = add3(a, b, msg(mi));
-    d = xor_rotr16(a, d);
-    c = add2(c, d);
-    b = xor_rotr(b, c, 12);
-    a = add3(a, b, msg(mi + 1));
-    d = xor_rotr(a, d, 8);
-    c = add2(c, d);
-    b = xor_rotr(b, c, 7);
-    v[ia] = a;
-    v[ib] = b;
-    v[ic] = c;
-    v[id] = d;
-  };
-  g(0, 4, 8, 12, 0);
-  g(1, 5, 9, 13, 2);
-  g(2, 6, 10, 14, 4);
-  g(3, 7, 11, 15, 6);
-  g(0, 5, 10, 15, 8);
-  g(1, 6, 11, 12, 10);
-  g(2, 7, 8, 13, 12);
-  g(3, 4, 9, 14, 14);
-#pragma unroll
-  for (int i = 0; i < BR_ST; i++) {
-    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[32 + 2 * i]), v[i].l));
-    round_p = qm31_add(round_p, qm31_mul_m31(br_q(e->ra[32 + 2 * i + 1]), v[i].h));
+#pragma unroll 1
+  for (int it = 0; it < 8; it++) {
+    if (it == 4) br_diagonalize(v);
+    BrU a = v[0], b = v[4], c = v[8], d = v[12];
+    a = ev.add3(a, b, ev.msg(2 * it));
+    d = ev.xor_rotr(a, d, 16);
+    c = ev.add2(c, d);
+    b = ev.xor_rotr(b, c, 12);
+    a = ev.add3(a, b, ev.msg(2 * it + 1));
+    d = ev.xor_rotr(a, d, 8);
+    c = ev.add2(c, d);
+    b = ev.xor_rotr(b, c, 7);
+    v[0] = a;
+    v[4] = b;
+    v[8] = c;
+    v[12] = d;
+    br_rotate_rows(v);
   }
-  round_p = qm31_sub(round_p, br_q(e->rz));
+  br_undiagonalize(v);
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) ev.round_felts(32 + 2 * i, v[i]);
+  const qm31 round_p = qm31_sub(ev.round_p, br_q(e->rz));
   // Last batch: the Round entry alone (multiplicity -1), against the last cumulative column at
   // the previous and current trace rows plus the cumsum shift.
   {
@@ -429,11 +446,11 @@ __global__ void __launch_bounds__(128) k_br_composition(const uint32_t* __restri
   }
   const qm31 res = qm31_add(qm31_from_u32(br_fold64(ev.a0), br_fold64(ev.a1), br_fold64(ev.a2), br_fold64(ev.a3)),
                             ev.logup);
-  const uint32_t d = __ldg(dinv + (r >> pp.trace_log));
-  o0[r] = m31_mul(res.a.a, d);
-  o1[r] = m31_mul(res.a.b, d);
-  o2[r] = m31_mul(res.b.a, d);
-  o3[r] = m31_mul(res.b.b, d);
+  const uint32_t dv = __ldg(dinv + (r >> pp.trace_log));
+  o0[r] = m31_mul(res.a.a, dv);
+  o1[r] = m31_mul(res.a.b, dv);
+  o2[r] = m31_mul(res.b.a, dv);
+  o3[r] = m31_mul(res.b.b, dv);
 }
 
 // ------------------------------------------------------------------------------------ host side

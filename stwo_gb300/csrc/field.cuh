@@ -37,8 +37,25 @@ __device__ __forceinline__ uint32_t m31_pow(uint32_t b, uint32_t e) {
   }
   return r;
 }
-// Fermat inverse: a^(P-2). The caller guarantees a != 0.
-__device__ __forceinline__ uint32_t m31_inv(uint32_t a) { return m31_pow(a, P - 2); }
+__device__ __forceinline__ uint32_t m31_sqn(uint32_t x, int n) {
+#pragma unroll 1
+  for (int i = 0; i < n; i++) x = m31_sqr(x);
+  return x;
+}
+// Fermat inverse a^(P-2) with P - 2 = 4 (2^29 - 1) + 1, through the powers a^(2^k - 1) for
+// k = 1, 2, 3, 6, 12, 24, 27, 29: 30 squarings and 8 products instead of 30 and 29. The caller
+// guarantees a != 0.
+__device__ __forceinline__ uint32_t m31_inv(uint32_t a) {
+  const uint32_t e1 = a;
+  const uint32_t e2 = m31_mul(m31_sqr(e1), e1);
+  const uint32_t e3 = m31_mul(m31_sqr(e2), e1);
+  const uint32_t e6 = m31_mul(m31_sqn(e3, 3), e3);
+  const uint32_t e12 = m31_mul(m31_sqn(e6, 6), e6);
+  const uint32_t e24 = m31_mul(m31_sqn(e12, 12), e12);
+  const uint32_t e27 = m31_mul(m31_sqn(e24, 3), e3);
+  const uint32_t e29 = m31_mul(m31_sqn(e27, 2), e2);
+  return m31_mul(m31_sqn(e29, 2), a);
+}
 
 struct cm31 { uint32_t a, b; };
 struct qm31 { cm31 a, b; };
