@@ -77,6 +77,15 @@ __device__ __forceinline__ cm31 cm31_mul_r(cm31 x) {
 
 __device__ __forceinline__ qm31 qm31_add(qm31 x, qm31 y) { return {cm31_add(x.a, y.a), cm31_add(x.b, y.b)}; }
 __device__ __forceinline__ qm31 qm31_sub(qm31 x, qm31 y) { return {cm31_sub(x.a, y.a), cm31_sub(x.b, y.b)}; }
+// Reductions of 64-bit sums of M31 products. fold: x < 2^64 -> < 2^34, same residue.
+__host__ __device__ __forceinline__ unsigned long long m31_fold64(unsigned long long x) { return (x & P) + (x >> 31); }
+// x < 2^64 -> the canonical residue.
+__host__ __device__ __forceinline__ uint32_t m31_reduce64(unsigned long long x) {
+  x = m31_fold64(m31_fold64(x));  // < 2^31 + 2^3
+  const uint32_t r = (uint32_t)x;
+  return r >= P ? r - P : r;
+}
+
 __device__ __forceinline__ qm31 qm31_mul(qm31 x, qm31 y) {
   // (a + bu)(c + du) = (ac + (2+i) bd) + (ad + bc) u
   cm31 ac = cm31_mul(x.a, y.a), bd = cm31_mul(x.b, y.b);

@@ -160,13 +160,6 @@ __global__ void k_decompose_sum(Secure4 src, uint32_t n, unsigned long long* acc
   }
 }
 
-__device__ __forceinline__ uint32_t m31_reduce64(unsigned long long x) {
-  x = (x & P) + (x >> 31);
-  x = (x & P) + (x >> 31);
-  uint32_t r = (uint32_t)x;
-  return r >= P ? r - P : r;
-}
-
 __global__ void k_decompose_apply(Secure4 src, Secure4M dst, uint32_t n, const unsigned long long* acc,
                                   uint32_t inv_n, uint32_t* lambda_out) {
   qm31 lambda = qm31_mul_m31(qm31_from_u32(m31_reduce64(acc[0]), m31_reduce64(acc[1]), m31_reduce64(acc[2]),
