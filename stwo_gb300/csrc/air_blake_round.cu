@@ -371,7 +371,8 @@ struct BrRowEval {
     prev_col = cur;
     logup_constraint(qm31_sub(qm31_mul(diff, qm31_mul(p0, p1)), qm31_add(p0, p1)));
   }
-  // xor_rotr_u32 (rr < 16) or xor_rotr16_u32 (rr == 16: halves split at 8).
+  // xor_rotr_u32 (rr < 16) or xor_rotr16_u32 (rr == 16: halves split at 8); rr may be a run-time
+  // value, the same for every thread.
   __device__ __forceinline__ BrU xor_rotr(BrU a, BrU b, uint32_t rr) {
     const uint32_t sp = rr == 16 ? 8 : rr;
     uint32_t all, alh, ahl, ahh, bll, blh, bhl, bhh;
@@ -409,25 +410,25 @@ __global__ void __launch_bounds__(128, 4) k_br_composition(const uint32_t* __res
     v[i].h = ev.mask();
     ev.round_felts(2 * i, v[i]);
   }
-  // The message masks (columns 32..63) are read by their G; the G masks follow them.
+  // The message masks (columns 32..63) are read by their G; the G masks follow them. Each G is
+  // two iterations with the same operand roles (a += b + m, d = (a ^ d) >>> r1, c += d,
+  // b = (b ^ c) >>> r2), rotations (16, 12) then (8, 7): half the loop body, which keeps the
+  // kernel's instruction footprint small.
   ev.col = 4 * BR_ST;
 #pragma unroll 1
-  for (int it = 0; it < 8; it++) {
-    if (it == 4) br_diagonalize(v);
+  for (int it = 0; it < 16; it++) {
+    const int half = it & 1;
+    if (it == 8) br_diagonalize(v);
     BrU a = v[0], b = v[4], c = v[8], d = v[12];
-    a = ev.add3(a, b, ev.msg(2 * it));
-    d = ev.xor_rotr(a, d, 16);
+    a = ev.add3(a, b, ev.msg(it));
+    d = ev.xor_rotr(a, d, half ? 8u : 16u);
     c = ev.add2(c, d);
-    b = ev.xor_rotr(b, c, 12);
-    a = ev.add3(a, b, ev.msg(2 * it + 1));
-    d = ev.xor_rotr(a, d, 8);
-    c = ev.add2(c, d);
-    b = ev.xor_rotr(b, c, 7);
+    b = ev.xor_rotr(b, c, half ? 7u : 12u);
     v[0] = a;
     v[4] = b;
     v[8] = c;
     v[12] = d;
-    br_rotate_rows(v);
+    if (half) br_rotate_rows(v);
   }
   br_undiagonalize(v);
 #pragma unroll
