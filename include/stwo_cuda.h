@@ -305,7 +305,11 @@ typedef struct {
 } stwo_proof_result;
 typedef struct stwo_server_s* stwo_server;
 
-/* n_workers streams on `device`; hbm_budget_bytes = 0 takes 90% of the free device memory. */
+/* n_workers workers on `device`; hbm_budget_bytes = 0 takes 90% of the free device memory. Each
+ * worker owns one stream per priority level: jobs under 256 MB of estimated device bytes run at
+ * the highest priority, jobs under 2 GB at the next, and larger jobs below those, each below the
+ * large jobs already running, so that small proofs are not queued behind the blocks of large
+ * ones and overlapping large proofs finish in arrival order. */
 stwo_status stwo_server_create(uint32_t n_workers, size_t hbm_budget_bytes, int device, stwo_server* out);
 /* Queues a job (its buffers must stay valid until its wait returns); returns at once. */
 stwo_status stwo_server_submit(stwo_server server, const stwo_proof_job* job, uint64_t* ticket);
@@ -315,8 +319,8 @@ stwo_status stwo_server_wait(stwo_server server, uint64_t ticket, stwo_proof_res
 stwo_status stwo_server_destroy(stwo_server server);
 /* The admission estimate of a job, in bytes. */
 size_t stwo_job_hbm_bytes(const stwo_proof_job* job);
-/* All n_jobs on a temporary server, submitted largest first (by stwo_job_hbm_bytes); results[i]
- * belongs to jobs[i]. Returns the first failure. */
+/* All n_jobs on a temporary server without stream priorities, submitted largest first (by
+ * stwo_job_hbm_bytes); results[i] belongs to jobs[i]. Returns the first failure. */
 stwo_status stwo_prove_batch(const stwo_proof_job* jobs, uint32_t n_jobs, uint32_t n_workers,
                              size_t hbm_budget_bytes, stwo_proof_result* results);
 

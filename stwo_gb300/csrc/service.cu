@@ -7,6 +7,16 @@
 // next to the jobs already running (a job larger than the whole budget runs alone). Among the
 // queued jobs the first one, in submission order, that fits is started next.
 //
+// Stream priorities: a small proof is a chain of about a hundred short launches, and behind the
+// wide kernels of a large proof each of them waits for whole waves of blocks, so that a 1 ms
+// proof took 50 ms next to two 2^20-row proofs. Each worker therefore owns one stream per
+// priority level and starts a job on the level of its size: jobs under 256 MB of device bytes on
+// the highest, jobs under 2 GB on the next, and larger jobs on the levels below in the order they
+// start (each below every large job still running), so that large proofs that overlap finish one
+// after another instead of all late. Priorities only order the dispatch of waiting blocks; a
+// lower-priority proof still takes every SM the others leave idle. A batch (stwo_prove_batch)
+// is judged by its total time, not by the latency of each proof, and runs without priorities.
+//
 // The reference proves one statement per call (crates/prover/src/core/prover/mod.rs:27-79) and
 // has no scheduler; this runtime only multiplexes calls of stwo_prove_wide_fib,
 // stwo_prove_poseidon and stwo_prove_blake_round, whose results are unchanged by it.
@@ -36,6 +46,10 @@ struct Pending {
 struct Done {
   stwo_proof_result r;
 };
+
+constexpr uint32_t PRIO_LEVELS = 6;
+constexpr size_t SMALL_JOB_BYTES = (size_t)256 << 20;
+constexpr size_t LARGE_JOB_BYTES = (size_t)2 << 30;
 
 }  // namespace
 
@@ -96,7 +110,19 @@ struct stwo_server_s {
   uint64_t next_ticket = 1;
   bool stop = false;
   std::vector<std::thread> workers;
-  std::vector<cudaStream_t> streams;
+  std::vector<cudaStream_t> streams;  // `levels` per worker, highest priority first
+  uint32_t levels = 1;                 // PRIO_LEVELS, or 1 without priorities
+  uint32_t level_use[PRIO_LEVELS] = {};
+
+  // Priority level of a job that starts now (called with mu held).
+  uint32_t level_for(size_t bytes) const {
+    if (levels == 1 || bytes < SMALL_JOB_BYTES) return 0;
+    if (bytes < LARGE_JOB_BYTES) return 1;
+    uint32_t lv = 2;
+    for (uint32_t k = 2; k < PRIO_LEVELS; k++)
+      if (level_use[k]) lv = k + 1;
+    return std::min(lv, PRIO_LEVELS - 1);
+  }
 
   // The first queued job that fits next to the running ones (any job when nothing runs).
   bool pick(Pending& out) {
@@ -110,11 +136,12 @@ struct stwo_server_s {
     return false;
   }
 
-  void work(cudaStream_t s) {
+  void work(const cudaStream_t* level_streams) {
     cudaSetDevice(device);
     for (;;) {
       Pending p{};
       bool got = false;
+      uint32_t level = 0;
       {
         // After stop the queue is drained before the workers leave.
         std::unique_lock<std::mutex> g(mu);
@@ -125,10 +152,12 @@ struct stwo_server_s {
         if (!got) break;
         running++;
         in_flight_bytes += p.bytes;
+        level = level_for(p.bytes);
+        level_use[level]++;
       }
       stwo_proof_result r{};
       const Clock::time_point t0 = Clock::now();
-      r.status = run_job(p.job, s, r);
+      r.status = run_job(p.job, level_streams[level], r);
       if (r.status != STWO_OK) {
         std::snprintf(r.error, sizeof(r.error), "%s", stwo_last_error());
       }
@@ -140,6 +169,7 @@ struct stwo_server_s {
         std::lock_guard<std::mutex> g(mu);
         running--;
         in_flight_bytes -= p.bytes;
+        level_use[level]--;
         done[p.ticket] = Done{r};
       }
       cv_done.notify_all();
@@ -148,11 +178,10 @@ struct stwo_server_s {
   }
 };
 
-extern "C" {
+namespace {
 
-size_t stwo_job_hbm_bytes(const stwo_proof_job* job) { return job ? job_hbm_bytes(*job) : 0; }
-
-stwo_status stwo_server_create(uint32_t n_workers, size_t hbm_budget_bytes, int device, stwo_server* out) {
+stwo_status server_create(uint32_t n_workers, size_t hbm_budget_bytes, int device, bool priorities,
+                          stwo_server* out) {
   STWO_REQUIRE(out && n_workers >= 1 && n_workers <= 256, "server: 1..256 workers");
   STWO_CHECK_CUDA(cudaSetDevice(device));
   STWO_CHECK_CUDA(cudaFree(nullptr));
@@ -161,12 +190,16 @@ stwo_status stwo_server_create(uint32_t n_workers, size_t hbm_budget_bytes, int 
     STWO_CHECK_CUDA(cudaMemGetInfo(&free_b, &total));
     hbm_budget_bytes = free_b / 10 * 9;
   }
+  int least = 0, greatest = 0;
+  STWO_CHECK_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
   auto* srv = new stwo_server_s();
   srv->device = device;
   srv->budget = hbm_budget_bytes;
-  for (uint32_t i = 0; i < n_workers; i++) {
+  srv->levels = priorities ? PRIO_LEVELS : 1;
+  for (uint32_t i = 0; i < n_workers * srv->levels; i++) {
     cudaStream_t s = nullptr;
-    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    const int prio = std::min(least, greatest + (int)(i % srv->levels));
+    cudaError_t e = cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio);
     if (e != cudaSuccess) {
       for (cudaStream_t t : srv->streams) cudaStreamDestroy(t);
       delete srv;
@@ -175,9 +208,22 @@ stwo_status stwo_server_create(uint32_t n_workers, size_t hbm_budget_bytes, int 
     }
     srv->streams.push_back(s);
   }
-  for (cudaStream_t s : srv->streams) srv->workers.emplace_back([srv, s] { srv->work(s); });
+  for (uint32_t i = 0; i < n_workers; i++) {
+    const cudaStream_t* level_streams = srv->streams.data() + (size_t)i * srv->levels;
+    srv->workers.emplace_back([srv, level_streams] { srv->work(level_streams); });
+  }
   *out = srv;
   return STWO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t stwo_job_hbm_bytes(const stwo_proof_job* job) { return job ? job_hbm_bytes(*job) : 0; }
+
+stwo_status stwo_server_create(uint32_t n_workers, size_t hbm_budget_bytes, int device, stwo_server* out) {
+  return server_create(n_workers, hbm_budget_bytes, device, true, out);
 }
 
 stwo_status stwo_server_submit(stwo_server srv, const stwo_proof_job* job, uint64_t* ticket) {
@@ -222,7 +268,7 @@ stwo_status stwo_prove_batch(const stwo_proof_job* jobs, uint32_t n_jobs, uint32
   int dev = 0;
   STWO_CHECK_CUDA(cudaGetDevice(&dev));
   stwo_server srv = nullptr;
-  stwo_status st = stwo_server_create(n_workers, hbm_budget_bytes, dev, &srv);
+  stwo_status st = server_create(n_workers, hbm_budget_bytes, dev, false, &srv);
   if (st) return st;
   // Largest jobs first (by their device-byte estimate, which grows with the work): a large proof
   // submitted last would otherwise run alone at the end of the batch. Results stay in job order.
