@@ -180,7 +180,10 @@ int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cuda
     if (c) channel_fused = true;
     lg = stop - 1;
   }
-  if (!read_root) return STWO_OK;
+  return read_root ? this->read_root(s) : STWO_OK;
+}
+
+int32_t DevMerkle::read_root(cudaStream_t s) {
   Mapped mp;
   int32_t st = mapped_words(8, mp);
   if (st) return st;
@@ -387,7 +390,15 @@ int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t>
   }
   for (size_t i = 0; i < t.evals.size(); i++) refs.push_back({t.evals[i], t.eval_logs[i]});
   StageScope stage_merkle("Merkle", s);
-  int32_t st = t.merkle.commit(refs, arena, s);
+  int32_t st = t.merkle.commit(refs, arena, s, false);
+  if (st) return st;
+  if (before_root_wait) {
+    // Host work that needs nothing from this commitment runs while the device computes it.
+    std::function<void()> f = std::move(before_root_wait);
+    before_root_wait = nullptr;
+    f();
+  }
+  st = t.merkle.read_root(s);
   if (st) return st;
   ch.mix_root(t.merkle.root);
   return STWO_OK;
@@ -503,54 +514,103 @@ static void write_config(ByteWriter& w, const stwo_pcs_config& c) {
   w.u64(c.n_queries);
 }
 
-int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
-  // Composition polynomial and OODS point (prover/mod.rs:41-61).
-  hq rc = ch.draw_felt();
-  int32_t st = commit_composition(air, rc);
-  if (st) return st;
-  HPointQ oods = random_point(ch);
+// Which columns are sampled at which mask offsets. It does not depend on the OODS point, so
+// prove() builds it while the device computes the composition commitment. Columns are listed
+// tree by tree, the composition tree's four columns last, each sampled at the OODS point (offset
+// 0) as the reference samples them (prover/mod.rs:63-68).
+struct SampleLayout {
+  std::vector<int> offsets;          // distinct mask offsets, in order of first use
+  std::vector<uint32_t> tree_first;  // first column of each tree; one entry per tree, plus the end
+  std::vector<uint32_t> col_first;   // first sample of each column; one entry per column, plus the end
+  std::vector<uint32_t> sample_off;  // the offset (index into `offsets`) of each sample
+};
 
-  // Sample points: mask offsets of the AIR, then four times the OODS point for the composition.
-  auto mask = air.mask_offsets();
-  std::vector<std::vector<std::vector<HPointQ>>> pts(trees.size());
-  uint32_t step = 1u << (31 - air.log_size());
-  // Columns share a handful of offsets: each shifted point is computed once.
-  std::map<int, HPointQ> shifted;
-  auto point_at = [&](int off) -> const HPointQ& {
-    auto it = shifted.find(off);
-    if (it != shifted.end()) return it->second;
-    uint32_t idx = idx_reduce((uint64_t)step * (uint64_t)(off >= 0 ? off : -off));
-    if (off < 0) idx = idx_reduce((1ull << 31) - idx);
-    return shifted.emplace(off, hpq_add_m31(oods, h_index_to_point(idx))).first->second;
+static SampleLayout sample_layout(const GpuAir& air, const std::vector<Tree>& trees) {
+  SampleLayout L;
+  const auto mask = air.mask_offsets();
+  auto offset_id = [&](int off) -> uint32_t {
+    for (size_t i = 0; i < L.offsets.size(); i++)
+      if (L.offsets[i] == off) return (uint32_t)i;
+    L.offsets.push_back(off);
+    return (uint32_t)L.offsets.size() - 1;
   };
-  for (size_t t = 0; t + 1 < trees.size(); t++) {
-    pts[t].resize(trees[t].polys.size());
-    if (t == 0 || t >= mask.size()) continue;
-    for (size_t c = 0; c < mask[t].size(); c++)
-      for (int off : mask[t][c]) pts[t][c].push_back(point_at(off));
-  }
-  pts.back().assign(4, {oods});
-
-  // Batched OODS evaluation of every sampled polynomial (pcs/prover.rs:89-101).
-  std::vector<const uint32_t*> polys;
-  std::vector<uint32_t> plogs, poly_of;
-  std::vector<stwo_qm31_point> qpts;
-  for (size_t t = 0; t < trees.size(); t++)
-    for (size_t c = 0; c < pts[t].size(); c++) {
-      polys.push_back(trees[t].polys[c]);
-      plogs.push_back(trees[t].poly_logs[c]);
-      for (auto& p : pts[t][c]) {
-        poly_of.push_back((uint32_t)polys.size() - 1);
-        qpts.push_back({to_sq(p.x), to_sq(p.y)});
+  for (size_t t = 0; t < trees.size(); t++) {
+    L.tree_first.push_back((uint32_t)L.col_first.size());
+    const bool comp = t + 1 == trees.size();
+    for (size_t c = 0; c < trees[t].polys.size(); c++) {
+      L.col_first.push_back((uint32_t)L.sample_off.size());
+      if (comp) {
+        L.sample_off.push_back(offset_id(0));
+      } else if (t != 0 && t < mask.size()) {
+        for (int off : mask[t][c]) L.sample_off.push_back(offset_id(off));
       }
     }
-  std::vector<stwo_qm31> svals(qpts.size());
-  StageScope stage_oods("Evaluate columns out of domain", s);
-  st = eval_at_points(polys.data(), plogs.data(), (uint32_t)polys.size(), poly_of.data(), qpts.data(),
-                      (uint32_t)qpts.size(), svals.data(), s);
+  }
+  L.tree_first.push_back((uint32_t)L.col_first.size());
+  L.col_first.push_back((uint32_t)L.sample_off.size());
+  return L;
+}
+
+int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
+  // Composition polynomial and OODS point (prover/mod.rs:41-61). The sample layout is built
+  // while the device commits the composition polynomial.
+  SampleLayout lay;
+  bool have_layout = false;
+  before_root_wait = [&] {
+    lay = sample_layout(air, trees);
+    have_layout = true;
+  };
+  hq rc = ch.draw_felt();
+  int32_t st = commit_composition(air, rc);
+  before_root_wait = nullptr;
   if (st) return st;
-  std::vector<hq> flat;
-  for (auto& v : svals) flat.push_back(from_sq(v));
+  STWO_REQUIRE(have_layout && lay.tree_first.size() == trees.size() + 1, "sample layout not built");
+  HPointQ oods = random_point(ch);
+
+  // The point of each distinct mask offset; offsets that land on the same point share its id,
+  // as the reference groups samples by point value (ColumnSampleBatch::new_vec).
+  const uint32_t step = 1u << (31 - air.log_size());
+  std::vector<HPointQ> upts;
+  std::vector<uint32_t> pid(lay.offsets.size());
+  for (size_t i = 0; i < lay.offsets.size(); i++) {
+    const int off = lay.offsets[i];
+    uint32_t idx = idx_reduce((uint64_t)step * (uint64_t)(off >= 0 ? off : -off));
+    if (off < 0) idx = idx_reduce((1ull << 31) - idx);
+    const HPointQ q = hpq_add_m31(oods, h_index_to_point(idx));
+    uint32_t k = 0;
+    while (k < upts.size() && !hpq_eq(upts[k], q)) k++;
+    if (k == upts.size()) upts.push_back(q);
+    pid[i] = k;
+  }
+  const size_t n_cols = lay.col_first.size() - 1;
+  const size_t n_samples = lay.sample_off.size();
+
+  // Batched OODS evaluation of every sampled polynomial (pcs/prover.rs:89-101).
+  std::vector<const uint32_t*> polys(n_cols);
+  std::vector<uint32_t> plogs(n_cols), poly_of(n_samples);
+  std::vector<const uint32_t*> ceval(n_cols);
+  std::vector<uint32_t> clog(n_cols);
+  std::vector<stwo_qm31_point> qpts(n_samples);
+  for (size_t t = 0; t < trees.size(); t++)
+    for (uint32_t c = lay.tree_first[t]; c < lay.tree_first[t + 1]; c++) {
+      const uint32_t lc = c - lay.tree_first[t];
+      polys[c] = trees[t].polys[lc];
+      plogs[c] = trees[t].poly_logs[lc];
+      ceval[c] = trees[t].evals[lc];
+      clog[c] = trees[t].eval_logs[lc];
+      for (uint32_t e = lay.col_first[c]; e < lay.col_first[c + 1]; e++) {
+        poly_of[e] = c;
+        const HPointQ& q = upts[pid[lay.sample_off[e]]];
+        qpts[e] = {to_sq(q.x), to_sq(q.y)};
+      }
+    }
+  std::vector<stwo_qm31> svals(n_samples);
+  StageScope stage_oods("Evaluate columns out of domain", s);
+  st = eval_at_points(polys.data(), plogs.data(), (uint32_t)n_cols, poly_of.data(), qpts.data(),
+                      (uint32_t)n_samples, svals.data(), s);
+  if (st) return st;
+  std::vector<hq> flat(n_samples);
+  for (size_t e = 0; e < n_samples; e++) flat[e] = from_sq(svals[e]);
   ch.mix_felts(flat);
 
   // Sanity check of the composition at the OODS point (prover/mod.rs:70-76). It is host
@@ -558,22 +618,19 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   // the host waits for the FRI results: the stream works meanwhile. Its verdict is checked before
   // the proof is written (the reference returns the same error earlier, with no proof either).
   struct OodsCheck {
-    std::vector<std::vector<std::vector<hq>>> mv;
-    hq dinv, lhs;
     bool done = false, ok = true;
   } check;
-  {
-    check.mv.resize(trees.size() - 1);
-    size_t k = 0;
+  auto run_check = [&]() {
+    if (check.done) return;
+    std::vector<std::vector<std::vector<hq>>> mv(trees.size() - 1);
     for (size_t t = 0; t + 1 < trees.size(); t++) {
-      check.mv[t].resize(pts[t].size());
-      for (size_t c = 0; c < pts[t].size(); c++)
-        check.mv[t][c].assign(flat.begin() + k, flat.begin() + k + pts[t][c].size()), k += pts[t][c].size();
+      mv[t].resize(lay.tree_first[t + 1] - lay.tree_first[t]);
+      for (uint32_t c = lay.tree_first[t]; c < lay.tree_first[t + 1]; c++)
+        mv[t][c - lay.tree_first[t]].assign(flat.begin() + lay.col_first[c], flat.begin() + lay.col_first[c + 1]);
     }
-    hq comp[4];
-    for (int i = 0; i < 4; i++) comp[i] = flat[k++];
-    check.lhs = hq_add(hq_add(comp[0], hq_mul(comp[1], hq_make(0, 1, 0, 0))),
-                       hq_add(hq_mul(comp[2], hq_make(0, 0, 1, 0)), hq_mul(comp[3], hq_make(0, 0, 0, 1))));
+    const hq* comp = flat.data() + lay.col_first[lay.tree_first[trees.size() - 1]];
+    const hq lhs = hq_add(hq_add(comp[0], hq_mul(comp[1], hq_make(0, 1, 0, 0))),
+                          hq_add(hq_mul(comp[2], hq_make(0, 0, 1, 0)), hq_mul(comp[3], hq_make(0, 0, 0, 1))));
     // denom inverse 1 / coset_vanishing(CanonicCoset(log).coset, oods)
     stwo_coset tc = coset_new(1u << (31 - (air.log_size() + 1)), air.log_size());
     hpoint init = h_index_to_point(tc.initial_index);
@@ -582,68 +639,56 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     HPointQ q = hpq_add_m31(oods, shift);
     hq x = q.x;
     for (uint32_t i = 1; i < air.log_size(); i++) x = hq_sub(hq_add(hq_mul(x, x), hq_mul(x, x)), hq_make(1, 0, 0, 0));
-    check.dinv = hq_inv(x);
-  }
-  auto run_check = [&]() {
-    if (check.done) return;
-    const hq rhs = air.eval_at_point(check.mv, rc, check.dinv);
-    check.ok = std::memcmp(check.lhs.v, rhs.v, sizeof(rhs.v)) == 0;
+    const hq rhs = air.eval_at_point(mv, rc, hq_inv(x));
+    check.ok = std::memcmp(lhs.v, rhs.v, sizeof(rhs.v)) == 0;
     check.done = true;
   };
 
-  // FRI quotients per log size, descending (pcs/quotients.rs:76-101).
-  struct ColS { const uint32_t* p; uint32_t log; std::vector<std::pair<HPointQ, hq>> samples; };
-  std::vector<ColS> cols;
-  {
-    size_t k = 0;
-    for (size_t t = 0; t < trees.size(); t++)
-      for (size_t c = 0; c < trees[t].evals.size(); c++) {
-        ColS cs{trees[t].evals[c], trees[t].eval_logs[c], {}};
-        for (auto& p : pts[t][c]) cs.samples.push_back({p, flat[k++]});
-        cols.push_back(cs);
-      }
-  }
-  std::stable_sort(cols.begin(), cols.end(), [](const ColS& a, const ColS& b) { return a.log > b.log; });
+  // FRI quotients per log size, descending (pcs/quotients.rs:76-101); columns of one log size
+  // keep their tree order.
+  std::vector<uint32_t> order(n_cols);
+  for (uint32_t c = 0; c < n_cols; c++) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return clog[a] > clog[b]; });
   hq qrc = ch.draw_felt();
   StageScope stage_q("Compute FRI quotients", s);
   std::vector<SecureCols> quotients;
   std::vector<uint32_t> qlogs;
-  for (size_t i = 0; i < cols.size();) {
+  for (size_t i = 0; i < n_cols;) {
     size_t j = i;
-    while (j < cols.size() && cols[j].log == cols[i].log) j++;
+    while (j < n_cols && clog[order[j]] == clog[order[i]]) j++;
     // ColumnSampleBatch::new_vec: group by point in CirclePoint<QM31> order.
-    std::vector<HPointQ> points;
-    for (size_t c = i; c < j; c++)
-      for (auto& sp : cols[c].samples) {
-        bool found = false;
-        for (auto& q : points) found = found || hpq_eq(q, sp.first);
-        if (!found) points.push_back(sp.first);
+    std::vector<uint32_t> points;
+    for (size_t k = i; k < j; k++)
+      for (uint32_t e = lay.col_first[order[k]]; e < lay.col_first[order[k] + 1]; e++) {
+        const uint32_t p = pid[lay.sample_off[e]];
+        if (std::find(points.begin(), points.end(), p) == points.end()) points.push_back(p);
       }
-    std::sort(points.begin(), points.end(), hpq_less);
+    std::sort(points.begin(), points.end(), [&](uint32_t a, uint32_t b) { return hpq_less(upts[a], upts[b]); });
     std::vector<std::vector<uint32_t>> bidx(points.size());
     std::vector<std::vector<stwo_qm31>> bval(points.size());
-    for (size_t c = i; c < j; c++)
-      for (auto& sp : cols[c].samples)
-        for (size_t b = 0; b < points.size(); b++)
-          if (hpq_eq(points[b], sp.first)) {
-            bidx[b].push_back((uint32_t)(c - i));
-            bval[b].push_back(to_sq(sp.second));
-          }
+    for (size_t k = i; k < j; k++)
+      for (uint32_t e = lay.col_first[order[k]]; e < lay.col_first[order[k] + 1]; e++) {
+        const size_t b = std::find(points.begin(), points.end(), pid[lay.sample_off[e]]) - points.begin();
+        bidx[b].push_back((uint32_t)(k - i));
+        bval[b].push_back(svals[e]);
+      }
     std::vector<stwo_sample_batch> batches(points.size());
     for (size_t b = 0; b < points.size(); b++)
-      batches[b] = {{to_sq(points[b].x), to_sq(points[b].y)}, (uint32_t)bidx[b].size(), bidx[b].data(), bval[b].data()};
-    std::vector<const uint32_t*> gc;
-    for (size_t c = i; c < j; c++) gc.push_back(cols[c].p);
+      batches[b] = {{to_sq(upts[points[b]].x), to_sq(upts[points[b]].y)}, (uint32_t)bidx[b].size(), bidx[b].data(),
+                    bval[b].data()};
+    std::vector<const uint32_t*> gc(j - i);
+    for (size_t k = i; k < j; k++) gc[k - i] = ceval[order[k]];
+    const uint32_t glog = clog[order[i]];
     SecureCols q;
     for (int k = 0; k < 4; k++) {
-      q.c[k] = arena.alloc((size_t)1 << cols[i].log);
+      q.c[k] = arena.alloc((size_t)1 << glog);
       if (!q.c[k]) return STWO_ERR_OOM;
     }
-    st = accumulate_quotients(cols[i].log, gc.data(), (uint32_t)gc.size(), to_sq(qrc), batches.data(),
+    st = accumulate_quotients(glog, gc.data(), (uint32_t)gc.size(), to_sq(qrc), batches.data(),
                               (uint32_t)batches.size(), cfg.log_blowup_factor, q.c, s);
     if (st) return st;
     quotients.push_back(q);
-    qlogs.push_back(cols[i].log);
+    qlogs.push_back(glog);
     i = j;
   }
 
@@ -878,12 +923,11 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   for (auto& t : trees) w.digest(t.merkle.root);
   w.u64(trees.size());
   {
-    size_t k = 0;
     for (size_t t = 0; t < trees.size(); t++) {
-      w.u64(pts[t].size());
-      for (auto& c : pts[t]) {
-        w.u64(c.size());
-        for (size_t j = 0; j < c.size(); j++) w.q(flat[k++]);
+      w.u64(lay.tree_first[t + 1] - lay.tree_first[t]);
+      for (uint32_t c = lay.tree_first[t]; c < lay.tree_first[t + 1]; c++) {
+        w.u64(lay.col_first[c + 1] - lay.col_first[c]);
+        for (uint32_t e = lay.col_first[c]; e < lay.col_first[c + 1]; e++) w.q(flat[e]);
       }
     }
   }

@@ -1,6 +1,7 @@
 // Declarations of the GPU prover host (prover.cu) and of the AIR interface its constraint
 // kernels implement.
 #pragma once
+#include <functional>
 #include <map>
 #include <vector>
 #include "common.cuh"
@@ -63,6 +64,8 @@ struct DevMerkle {
   // the next alpha into alpha_out, when the root comes from a node-only run (channel_fused).
   int32_t commit(const std::vector<ColRef>& columns, Arena& arena, cudaStream_t s, bool read_root = true,
                  DevChannel* ch = nullptr, uint32_t* alpha_out = nullptr);
+  // Waits for the stream and copies the root (layers[0]) into `root`.
+  int32_t read_root(cudaStream_t s);
   // A tree of equal-size columns whose leaf level is already in `all` (written by the FRI fold
   // that produced the columns); `all` holds every layer, as commit lays them out.
   int32_t commit_from_leaves(const std::vector<ColRef>& columns, uint32_t* all, cudaStream_t s,
@@ -103,6 +106,8 @@ struct Prover {
   int32_t init_status = 0;
   HostChannel ch;
   std::vector<Tree> trees;
+  // Run once by the next commit_polys, after its launches and before it waits for the root.
+  std::function<void()> before_root_wait;
 
   Prover(const stwo_pcs_config& c, uint32_t max_log, cudaStream_t st);
   ~Prover();
