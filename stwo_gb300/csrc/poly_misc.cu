@@ -5,13 +5,19 @@
 // t_i = y^{i_0} x^{i_1} pi(x)^{i_2} ... pi^{L-2}(x)^{i_{L-1}}, pi(x) = 2x^2 - 1. The index is split
 // as (top | mid 6 bits | low 8 bits): thread t of a block owns low = t, accumulates
 // sum_mid coeff * Mid[mid] (4 IMAD per coefficient), multiplies once by Low[t]; the block sum is
-// scaled by Top[block] and folded into 64-bit accumulators. One pass over the coefficients,
-// coalesced; HBM-bound for large polynomials.
+// scaled by Top[block] and folded into 64-bit accumulators. The mappings and the Low and Mid
+// products are computed once per distinct point (k_point_tables). One pass over the
+// coefficients, coalesced; HBM-bound for large polynomials.
 #include "common.cuh"
+#include <array>
+#include <map>
 
 namespace stwo {
 
 constexpr uint32_t EP_LOW = 8, EP_MID = 8;
+// Chunks of 2^(8 + 6) coefficients when the point tables are precomputed: a block then starts
+// loading at once, and a 2^16-coefficient polynomial is four blocks, which balances the waves.
+constexpr uint32_t EP_MID_TABLES = 6;
 
 struct EvalJob {
   const uint32_t* coeffs;
@@ -34,30 +40,68 @@ __device__ __forceinline__ void point_mappings(const stwo_qm31_point& pt, uint32
   }
 }
 
+// Per distinct point, in global memory: its EP_MAPS mappings, then the products Low[t] over the
+// set bits of t of mappings [0, EP_LOW), then Mid[m] over those of [EP_LOW, EP_LOW + EP_MID).
+// They depend on the point only, not on the polynomial's size (for L < EP_LOW only Low[t < 2^L]
+// is read, which uses mappings below L).
+constexpr uint32_t EP_MAPS = 30;
+constexpr uint32_t EP_TABLE = EP_MAPS + (1u << EP_LOW) + (1u << EP_MID);
+
+__global__ void __launch_bounds__(256) k_point_tables(const stwo_qm31_point* __restrict__ points, qm31* __restrict__ tables) {
+  __shared__ qm31 s_map[EP_MAPS];
+  if (threadIdx.x == 0) point_mappings(points[blockIdx.x], EP_MAPS, s_map);
+  __syncthreads();
+  qm31* T = tables + (size_t)blockIdx.x * EP_TABLE;
+  const uint32_t t = threadIdx.x;
+  if (t < EP_MAPS) T[t] = s_map[t];
+  qm31 lo = qm31_from_u32(1, 0, 0, 0), mid = lo;
+  for (uint32_t b = 0; b < EP_LOW; b++)
+    if ((t >> b) & 1) lo = qm31_mul(lo, s_map[b]);
+  for (uint32_t b = 0; b < EP_MID; b++)
+    if ((t >> b) & 1) mid = qm31_mul(mid, s_map[EP_LOW + b]);
+  T[EP_MAPS + t] = lo;
+  T[EP_MAPS + (1u << EP_LOW) + t] = mid;
+}
+
+// One block per (chunk of 2^(EP_LOW + mid_max) coefficients, evaluation). With `tables` the
+// point's mappings and products come from k_point_tables (table_of[e] names the evaluation's
+// entry); without, the block derives them from points[e].
 __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict__ jobs, const uint32_t* __restrict__ poly_of,
                                                        const stwo_qm31_point* __restrict__ points,
+                                                       const qm31* __restrict__ tables,
+                                                       const uint32_t* __restrict__ table_of, uint32_t mid_max,
                                                        unsigned long long* __restrict__ acc) {
   __shared__ qm31 s_map[32];
   __shared__ qm31 s_mid[1 << EP_MID];
   __shared__ qm31 s_part[8];
   __shared__ EvalJob s_job;
+  __shared__ uint32_t s_table;
   const uint32_t e = blockIdx.y;
-  if (threadIdx.x == 0) s_job = jobs[poly_of[e]];  // one read of the (possibly host-mapped) tables
+  if (threadIdx.x == 0) {
+    s_job = jobs[poly_of[e]];  // one read of the (possibly host-mapped) tables
+    if (tables) s_table = table_of[e];
+  }
   __syncthreads();
   const EvalJob job = s_job;
   const uint32_t L = job.log_size;
   const uint32_t lo_bits = L < EP_LOW ? L : EP_LOW;
-  const uint32_t mid_bits = L - lo_bits < EP_MID ? L - lo_bits : EP_MID;
+  const uint32_t mid_bits = L - lo_bits < mid_max ? L - lo_bits : mid_max;
   const uint32_t chunk_bits = lo_bits + mid_bits;
   const uint32_t n_chunks = 1u << (L - chunk_bits);
   if (blockIdx.x >= n_chunks) return;
-  if (threadIdx.x == 0) point_mappings(points[e], L, s_map);
-  __syncthreads();
-  if (threadIdx.x < (1u << mid_bits)) {
-    qm31 t = qm31_from_u32(1, 0, 0, 0);
-    for (uint32_t b = 0; b < mid_bits; b++)
-      if ((threadIdx.x >> b) & 1) t = qm31_mul(t, s_map[lo_bits + b]);
-    s_mid[threadIdx.x] = t;
+  const qm31* T = tables ? tables + (size_t)s_table * EP_TABLE : nullptr;
+  if (T) {
+    if (threadIdx.x < EP_MAPS) s_map[threadIdx.x] = T[threadIdx.x];
+    if (threadIdx.x < (1u << mid_bits)) s_mid[threadIdx.x] = T[EP_MAPS + (1u << EP_LOW) + threadIdx.x];
+  } else {
+    if (threadIdx.x == 0) point_mappings(points[e], L, s_map);
+    __syncthreads();
+    if (threadIdx.x < (1u << mid_bits)) {
+      qm31 t = qm31_from_u32(1, 0, 0, 0);
+      for (uint32_t b = 0; b < mid_bits; b++)
+        if ((threadIdx.x >> b) & 1) t = qm31_mul(t, s_map[lo_bits + b]);
+      s_mid[threadIdx.x] = t;
+    }
   }
   __syncthreads();
   qm31 res = qm31_zero();
@@ -65,8 +109,9 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
   if (t < (1u << lo_bits)) {
     const uint32_t* c = job.coeffs + ((size_t)blockIdx.x << chunk_bits);
     unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    // Products are < 2^62; folding after every second one keeps the sums below 2^64. Eight
-    // coefficient loads are issued before they are used.
+    // Products are at most (P - 1)^2 < 2^62 - 2^33 + 4, and a folded sum is below 2^33 + 2^31:
+    // folding after every fourth product keeps the sums below 2^64. Eight coefficient loads are
+    // issued before they are used.
     const uint32_t n_mid = 1u << mid_bits;
     uint32_t m = 0;
     for (; m + 8 <= n_mid; m += 8) {
@@ -80,7 +125,7 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
         a1 += (unsigned long long)w.a.b * v[k];
         a2 += (unsigned long long)w.b.a * v[k];
         a3 += (unsigned long long)w.b.b * v[k];
-        if (k & 1) {
+        if ((k & 3) == 3) {
           a0 = (a0 & P) + (a0 >> 31);
           a1 = (a1 & P) + (a1 >> 31);
           a2 = (a2 & P) + (a2 >> 31);
@@ -103,9 +148,14 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
       return r >= P ? r - P : r;
     };
     res = qm31_from_u32(red(a0), red(a1), red(a2), red(a3));
-    qm31 low = qm31_from_u32(1, 0, 0, 0);
-    for (uint32_t b = 0; b < lo_bits; b++)
-      if ((t >> b) & 1) low = qm31_mul(low, s_map[b]);
+    qm31 low;
+    if (T) {
+      low = T[EP_MAPS + t];
+    } else {
+      low = qm31_from_u32(1, 0, 0, 0);
+      for (uint32_t b = 0; b < lo_bits; b++)
+        if ((t >> b) & 1) low = qm31_mul(low, s_map[b]);
+    }
     res = qm31_mul(res, low);
   }
   // Block reduction of the QM31 partials.
@@ -153,46 +203,74 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
   for (uint32_t e = 0; e < n_evals; e++) {
     STWO_REQUIRE(poly_of[e] < n_polys, "poly index out of range");
     uint32_t L = log_sizes[poly_of[e]];
-    uint32_t cb = std::min(L, EP_LOW) + std::min(L - std::min(L, EP_LOW), EP_MID);
+    uint32_t cb = std::min(L, EP_LOW) + std::min(L - std::min(L, EP_LOW), EP_MID_TABLES);
     max_chunks = std::max(max_chunks, 1u << (L - cb));
   }
   STWO_REQUIRE(n_evals <= 65535, "too many evaluations in one call");
-  // The job tables go to the kernel through mapped host memory (read once per block) and the
-  // results come back the same way: no staging copies around the launch.
+  // Evaluations share a handful of points (the mask offsets of one OODS point): the point tables
+  // are built once per distinct point.
+  std::map<std::array<uint32_t, 8>, uint32_t> uniq;
+  std::vector<stwo_qm31_point> upts;
+  std::vector<uint32_t> table_of(n_evals);
+  for (uint32_t e = 0; e < n_evals; e++) {
+    std::array<uint32_t, 8> key;
+    std::memcpy(key.data(), &points[e], sizeof(key));
+    auto it = uniq.emplace(key, (uint32_t)upts.size());
+    if (it.second) upts.push_back(points[e]);
+    table_of[e] = it.first->second;
+  }
+  const uint32_t n_pts = (uint32_t)upts.size();
+  // The job tables go to the kernels through mapped host memory (read once per block) and the
+  // results come back the same way: no staging copies around the launches.
   const size_t w_jobs = (jobs.size() * sizeof(EvalJob) + 15) / 16 * 4;
   const size_t w_polyof = ((size_t)n_evals + 3) / 4 * 4;
-  const size_t w_pts = (size_t)n_evals * sizeof(stwo_qm31_point) / 4;
+  const size_t w_tabof = w_polyof;
+  const size_t w_pts = (size_t)n_pts * sizeof(stwo_qm31_point) / 4;
   const size_t w_out = (size_t)n_evals * 4;
   Mapped mp;
-  int32_t st = mapped_words(w_jobs + w_polyof + w_pts + w_out, mp);
+  int32_t st = mapped_words(w_jobs + w_polyof + w_tabof + w_pts + w_out, mp);
   if (st) return st;
+  uint32_t* h_polyof = mp.host + w_jobs;
+  uint32_t* h_tabof = h_polyof + w_polyof;
+  uint32_t* h_pts = h_tabof + w_tabof;
+  uint32_t* h_out = h_pts + w_pts;
   std::memcpy(mp.host, jobs.data(), jobs.size() * sizeof(EvalJob));
-  std::memcpy(mp.host + w_jobs, poly_of, (size_t)n_evals * 4);
-  std::memcpy(mp.host + w_jobs + w_polyof, points, (size_t)n_evals * sizeof(stwo_qm31_point));
-  unsigned long long* acc = nullptr;
-  st = scratch_alloc((void**)&acc, (size_t)n_evals * 32, s);
+  std::memcpy(h_polyof, poly_of, (size_t)n_evals * 4);
+  std::memcpy(h_tabof, table_of.data(), (size_t)n_evals * 4);
+  std::memcpy(h_pts, upts.data(), (size_t)n_pts * sizeof(stwo_qm31_point));
+  auto dev = [&](const uint32_t* h) { return mp.dev + (h - mp.host); };
+  // One stream-ordered block: the 64-bit accumulators, then the point tables.
+  const size_t acc_bytes = (size_t)n_evals * 32;
+  unsigned char* scratch = nullptr;
+  st = scratch_alloc((void**)&scratch, acc_bytes + (size_t)n_pts * EP_TABLE * sizeof(qm31), s);
   if (st) return st;
-  cudaError_t err = cudaMemsetAsync(acc, 0, (size_t)n_evals * 32, s);
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(scratch);
+  qm31* tables = reinterpret_cast<qm31*>(scratch + acc_bytes);
+  cudaError_t err = cudaMemsetAsync(acc, 0, acc_bytes, s);
+  if (!err) {
+    k_point_tables<<<n_pts, 1u << EP_LOW, 0, s>>>(reinterpret_cast<const stwo_qm31_point*>(dev(h_pts)), tables);
+    note_launch();
+    err = cudaGetLastError();
+  }
   if (!err) {
     dim3 grid(max_chunks, n_evals);
-    k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<const EvalJob*>(mp.dev),
-                                         mp.dev + w_jobs,
-                                         reinterpret_cast<const stwo_qm31_point*>(mp.dev + w_jobs + w_polyof), acc);
+    k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<const EvalJob*>(mp.dev), dev(h_polyof), nullptr, tables,
+                                         dev(h_tabof), EP_MID_TABLES, acc);
     note_launch();
     err = cudaGetLastError();
   }
   if (!err) {
-    k_reduce_acc<<<(n_evals * 4 + 255) / 256, 256, 0, s>>>(acc, n_evals * 4, mp.dev + w_jobs + w_polyof + w_pts);
+    k_reduce_acc<<<(n_evals * 4 + 255) / 256, 256, 0, s>>>(acc, n_evals * 4, dev(h_out));
     note_launch();
     err = cudaGetLastError();
   }
-  scratch_free(acc, s);
+  scratch_free(scratch, s);
   if (!err) err = cudaStreamSynchronize(s);
   if (err) {
     set_error("eval_at_points: %s", cudaGetErrorString(err));
     return STWO_ERR_CUDA;
   }
-  std::memcpy(out, mp.host + w_jobs + w_polyof + w_pts, (size_t)n_evals * 16);
+  std::memcpy(out, h_out, (size_t)n_evals * 16);
   return STWO_OK;
 }
 
@@ -271,8 +349,8 @@ int32_t eval_at_points_noalloc(const uint32_t* const* coeffs, const uint32_t* lo
     dim3 grid(max_chunks, n_evals);
     k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<EvalJob*>(buf + NA_OFF_JOBS),
                                          reinterpret_cast<uint32_t*>(buf + NA_OFF_POLYOF),
-                                         reinterpret_cast<stwo_qm31_point*>(buf + NA_OFF_PTS),
-                                         reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC));
+                                         reinterpret_cast<stwo_qm31_point*>(buf + NA_OFF_PTS), nullptr, nullptr,
+                                         EP_MID, reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC));
     note_launch();
     err = cudaGetLastError();
   }

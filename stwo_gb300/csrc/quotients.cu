@@ -158,7 +158,9 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows(uint32_t rows, 
       if (live) {
         uint32_t cnt = 0;
         uint32_t i = slice;
-        // Eight independent column loads in flight per iteration.
+        // Eight independent column loads in flight per iteration. Products are at most
+        // (P - 1)^2 < 2^62 - 2^33 + 4 and a folded sum is below 2^33 + 2^31, so a sum takes four
+        // products between folds without passing 2^64.
         for (; i + 7 * Q_SLICES < ne; i += 8 * Q_SLICES) {
           uint32_t v[8];
 #pragma unroll
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows(uint32_t rows, 
             s1 += (unsigned long long)q.c[1] * v[u];
             s2 += (unsigned long long)q.c[2] * v[u];
             s3 += (unsigned long long)q.c[3] * v[u];
-            if (u & 1) {
+            if ((u & 3) == 3) {
               s0 = fold64(s0);
               s1 = fold64(s1);
               s2 = fold64(s2);
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows(uint32_t rows, 
           s1 += (unsigned long long)st[i].c[1] * v;
           s2 += (unsigned long long)st[i].c[2] * v;
           s3 += (unsigned long long)st[i].c[3] * v;
-          if (++cnt == 2) {
+          if (++cnt == 4) {
             s0 = fold64(s0);
             s1 = fold64(s1);
             s2 = fold64(s2);
@@ -192,6 +194,11 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows(uint32_t rows, 
             cnt = 0;
           }
         }
+        // The next staged group starts from a folded sum.
+        s0 = fold64(s0);
+        s1 = fold64(s1);
+        s2 = fold64(s2);
+        s3 = fold64(s3);
       }
     }
     part[slice][lane][0] = red64(s0);
