@@ -7,9 +7,10 @@
 //
 // Kernels (one thread per row):
 //   k_br_trace        the 384 trace columns of one BLAKE2s round (gen.rs:75-204)
-//   k_br_interaction  64 cumulative columns of paired XOR lookups and one of the Round relation
-//                     (gen.rs:237-280); the row's round is recomputed from its inputs, so no
-//                     lookup columns are stored
+//   k_br_interaction_rows / _warps
+//                     64 cumulative columns of paired XOR lookups and one of the Round relation
+//                     (gen.rs:237-280), one thread per row or one warp per G-function; the row's
+//                     round is recomputed from its inputs, so no lookup columns are stored
 //   k_br_composition  the 64 carry constraints and 65 LogUp constraints (constraints.rs:22-206,
 //                     finalize_logup_in_pairs) with random-coefficient accumulation, times 1/Z
 #include "common.cuh"
@@ -190,7 +191,13 @@ __global__ void __launch_bounds__(128) k_br_trace(uint32_t n_rows, const uint32_
 }
 
 // ------------------------------------------------------------------------------------ interaction
-// Accumulates the paired XOR fractions into cumulative secure columns as the lookups appear.
+// Two schedules give the same columns. With many rows, one thread per row (k_br_interaction_rows)
+// fills the GPU and does the least work. With few rows, each thread's 64 dependent inversions
+// would set the kernel's time, and one warp per G-function (k_br_interaction_warps) divides that
+// chain by eight.
+//
+// One thread per row: accumulates the paired XOR fractions into cumulative secure columns as the
+// lookups appear.
 struct BrInteractionWriter {
   const BrElements* e;
   uint32_t* out;
@@ -222,7 +229,7 @@ struct BrInteractionWriter {
   }
 };
 
-__global__ void __launch_bounds__(128) k_br_interaction(uint32_t n_rows, const uint32_t* __restrict__ inputs,
+__global__ void __launch_bounds__(128) k_br_interaction_rows(uint32_t n_rows, const uint32_t* __restrict__ inputs,
                                                         const BrElements* __restrict__ e_dev, uint32_t* __restrict__ out) {
   __shared__ BrElements s_e;
   br_stage_elements(e_dev, &s_e);
@@ -252,6 +259,130 @@ __global__ void __launch_bounds__(128) k_br_interaction(uint32_t n_rows, const u
   p = qm31_sub(p, br_q(e->rz));
   // -1 / p
   w.write(qm31_add(w.cum, qm31_sub(qm31_zero(), qm31_inv(p))));
+}
+
+// Each XOR pair contributes 1/p0 + 1/p1 = (p0 + p1) / (p0 p1) to the next cumulative column; the
+// pairs come in the evaluator's lookup order, eight per G-function (two per xor_rotr call), so
+// G-function g owns columns 8g .. 8g + 7.
+//
+// One warp per G-function: warp g of a block takes 32 consecutive rows, replays the integer state
+// of G-functions 0 .. g-1 (cheap next to the QM31 inversions), then computes its own eight pair
+// fractions. The eight warps' fraction sums meet in shared memory, and each warp writes its
+// columns as prefix sums from the sum of the warps before it. A row's 64 inversions are thus
+// spread over eight threads, which shortens the dependent chain of a thread eightfold, and every
+// column store of a warp is one 128-byte line.
+constexpr uint32_t BI_ROWS = 32;
+constexpr uint32_t BI_WARPS_MAX_LOG = 15;  // k_br_interaction_warps up to 2^15 rows
+
+// The two pair fractions of one xor_rotr_u32 (RR < 16) or xor_rotr16_u32 (RR == 16, halves split
+// at 8): lookups (ll, hl) and (lh, hh), into f[K] and f[K + 1]. Returns the rotated xor.
+template <int K, uint32_t RR>
+__device__ __forceinline__ uint32_t br_xr_fracs(const BrElements* e, uint32_t a, uint32_t b, qm31 f[8]) {
+  constexpr uint32_t SP = RR == 16 ? 8 : RR;
+  constexpr uint32_t M = (1u << SP) - 1;
+  const uint32_t al = a & 0xffffu, ah = a >> 16, bl = b & 0xffffu, bh = b >> 16;
+  const uint32_t all = al & M, alh = al >> SP, ahl = ah & M, ahh = ah >> SP;
+  const uint32_t bll = bl & M, blh = bl >> SP, bhl = bh & M, bhh = bh >> SP;
+  const qm31 p0 = br_xor_combine(e, SP, all, bll, all ^ bll);
+  const qm31 p1 = br_xor_combine(e, SP, ahl, bhl, ahl ^ bhl);
+  f[K] = qm31_mul(qm31_add(p0, p1), qm31_inv(qm31_mul(p0, p1)));
+  const qm31 p2 = br_xor_combine(e, 16 - SP, alh, blh, alh ^ blh);
+  const qm31 p3 = br_xor_combine(e, 16 - SP, ahh, bhh, ahh ^ bhh);
+  f[K + 1] = qm31_mul(qm31_add(p2, p3), qm31_inv(qm31_mul(p2, p3)));
+  const uint32_t c = a ^ b;
+  return (c >> RR) | (c << (32 - RR));
+}
+
+__device__ __forceinline__ uint32_t br_rotr(uint32_t x, uint32_t r) { return (x >> r) | (x << (32 - r)); }
+
+__device__ __forceinline__ void br_write_q(uint32_t* out, size_t n, uint32_t r, uint32_t col, const qm31& x) {
+  out[((size_t)4 * col + 0) * n + r] = x.a.a;
+  out[((size_t)4 * col + 1) * n + r] = x.a.b;
+  out[((size_t)4 * col + 2) * n + r] = x.b.a;
+  out[((size_t)4 * col + 3) * n + r] = x.b.b;
+}
+
+__global__ void __launch_bounds__(256) k_br_interaction_warps(uint32_t n_rows, const uint32_t* __restrict__ inputs,
+                                                        const BrElements* __restrict__ e_dev, uint32_t* __restrict__ out) {
+  __shared__ BrElements s_e;
+  __shared__ qm31 s_tot[8][BI_ROWS];
+  br_stage_elements(e_dev, &s_e);
+  __syncthreads();
+  const BrElements* e = &s_e;
+  const uint32_t lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const uint32_t r = blockIdx.x * BI_ROWS + lane;
+  const bool live = r < n_rows;
+  const uint32_t rr = live ? r : n_rows - 1;  // lanes past the end replay a real row, write nothing
+  uint32_t v[BR_ST];
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) v[i] = br_input(inputs, rr, i);
+  // The integer state before G-function g, in br_round's rotating-state order.
+#pragma unroll 1
+  for (uint32_t it = 0; it < g; it++) {
+    if (it == 4) br_diagonalize(v);
+    uint32_t a = v[0], b = v[4], c = v[8], d = v[12];
+    a = a + b + br_input(inputs, rr, BR_ST + 2 * it);
+    d = br_rotr(a ^ d, 16);
+    c = c + d;
+    b = br_rotr(b ^ c, 12);
+    a = a + b + br_input(inputs, rr, BR_ST + 2 * it + 1);
+    d = br_rotr(a ^ d, 8);
+    c = c + d;
+    b = br_rotr(b ^ c, 7);
+    v[0] = a;
+    v[4] = b;
+    v[8] = c;
+    v[12] = d;
+    br_rotate_rows(v);
+  }
+  if (g == 4) br_diagonalize(v);
+  qm31 f[8];
+  {
+    uint32_t a = v[0], b = v[4], c = v[8], d = v[12];
+    a = a + b + br_input(inputs, rr, BR_ST + 2 * g);
+    d = br_xr_fracs<0, 16>(e, a, d, f);
+    c = c + d;
+    b = br_xr_fracs<2, 12>(e, b, c, f);
+    a = a + b + br_input(inputs, rr, BR_ST + 2 * g + 1);
+    d = br_xr_fracs<4, 8>(e, a, d, f);
+    c = c + d;
+    b = br_xr_fracs<6, 7>(e, b, c, f);
+    v[0] = a;
+    v[4] = b;
+    v[8] = c;
+    v[12] = d;
+  }
+  qm31 tot = f[0];
+#pragma unroll
+  for (int k = 1; k < 8; k++) tot = qm31_add(tot, f[k]);
+  s_tot[g][lane] = tot;
+  __syncthreads();
+  qm31 cum = qm31_zero();
+  for (uint32_t h = 0; h < g; h++) cum = qm31_add(cum, s_tot[h][lane]);
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    cum = qm31_add(cum, f[k]);
+    if (live) br_write_q(out, n_rows, r, 8 * g + k, cum);
+  }
+  if (g != 7) return;
+  // The Round relation, last column: sum_k alpha^k x_k - z over the (input, output, message)
+  // halves, its fraction -1/p added to the sum of all 64 pairs.
+  br_rotate_rows(v);
+  br_undiagonalize(v);
+  qm31 p = qm31_zero();
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    const uint32_t x = br_input(inputs, rr, i);
+    const uint32_t m = br_input(inputs, rr, BR_ST + i);
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i]), x & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i + 1]), x >> 16));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i]), v[i] & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i + 1]), v[i] >> 16));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), m & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), m >> 16));
+  }
+  p = qm31_sub(p, br_q(e->rz));
+  if (live) br_write_q(out, n_rows, r, BR_XOR_PAIRS, qm31_add(cum, qm31_sub(qm31_zero(), qm31_inv(p))));
 }
 
 // ------------------------------------------------------------------------------------ composition
@@ -726,7 +857,11 @@ extern "C" stwo_status stwo_prove_blake_round(uint32_t log_n_rows, const uint32_
       if (!st && cudaMemcpyAsync(de, &he, sizeof(BrElements), cudaMemcpyHostToDevice, s) != cudaSuccess)
         st = STWO_ERR_CUDA;
       if (!st) {
-        k_br_interaction<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_inputs, de, inter);
+        if (log_n_rows <= BI_WARPS_MAX_LOG)
+          k_br_interaction_warps<<<(uint32_t)((n + BI_ROWS - 1) / BI_ROWS), 8 * 32, 0, s>>>((uint32_t)n, d_inputs, de,
+                                                                                          inter);
+        else
+          k_br_interaction_rows<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_inputs, de, inter);
         note_launch();
         if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
       }

@@ -13,9 +13,11 @@ def dev(x):
     return torch.from_numpy(np.ascontiguousarray(np.asarray(x, np.uint32)).view(np.int32)).cuda()
 
 
+# Up to 2^15 rows the interaction trace runs one warp per G-function, above it one thread per row:
+# 2^16 covers the second schedule.
 @pytest.mark.parametrize("log_n,seeded,cfg", [(4, False, (5, 1, 0, 3)), (5, True, (5, 1, 0, 3)),
                                               (7, True, (3, 2, 1, 5)), (10, False, (10, 1, 0, 3)),
-                                              (12, True, (10, 1, 0, 3))])
+                                              (12, True, (10, 1, 0, 3)), (16, True, (5, 1, 0, 3))])
 def test_blake_round_proof_bytes_match_oracle(cuda, oracle, log_n, seeded, cfg):
     from stwo_gb300.prover import prove_blake_round
 
