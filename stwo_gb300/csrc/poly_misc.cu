@@ -215,9 +215,12 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
   for (uint32_t e = 0; e < n_evals; e++) {
     std::array<uint32_t, 8> key;
     std::memcpy(key.data(), &points[e], sizeof(key));
-    auto it = uniq.emplace(key, (uint32_t)upts.size());
-    if (it.second) upts.push_back(points[e]);
-    table_of[e] = it.first->second;
+    auto it = uniq.find(key);
+    if (it == uniq.end()) {
+      it = uniq.emplace(key, (uint32_t)upts.size()).first;
+      upts.push_back(points[e]);
+    }
+    table_of[e] = it->second;
   }
   const uint32_t n_pts = (uint32_t)upts.size();
   // The job tables go to the kernels through mapped host memory (read once per block) and the
