@@ -243,6 +243,71 @@ __global__ void k_scan_add(uint32_t* data, uint32_t len, const uint32_t* tile_of
 }
 
 // Inclusive scan of `rows` arrays of `len` words (len <= 4096^2), in place.
+// finalize_last for columns of at most 2^FIN_ONE_BLOCK_LOG rows in one launch: block k owns
+// coordinate column k. It sums the column (the claimed sum's coordinate, also written to
+// sums[k]), then scans the shifted values in coset order: each thread takes a run of consecutive
+// coset positions, the run totals are scanned across the block, and a second pass writes the
+// prefix sums back. The column stays in L2 between the passes. One block per column is bound by
+// the latency of its scattered coset-order accesses, so above 2^14 rows the multi-launch path
+// below is faster (2^16 rows: 0.12 ms against 0.045 ms); below it, one launch beats seven.
+constexpr uint32_t FIN_ONE_BLOCK_LOG = 14;
+constexpr uint32_t FIN_THREADS = 1024;
+
+__global__ void __launch_bounds__(FIN_THREADS) k_logup_finalize_small(uint32_t* cols, uint32_t log_n, uint32_t inv_n,
+                                                                      unsigned long long* sums) {
+  __shared__ unsigned long long s_sum[FIN_THREADS / 32];
+  __shared__ uint32_t s_scan[FIN_THREADS / 32];
+  __shared__ uint32_t s_shift;
+  const uint32_t k = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const uint32_t n = 1u << log_n;
+  uint32_t* c = cols + (size_t)k * n;
+  unsigned long long sum = 0;
+  for (uint32_t r = t; r < n; r += FIN_THREADS) sum += c[r];
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) s_sum[w] = sum;
+  __syncthreads();
+  if (t == 0) {
+    unsigned long long tot = 0;
+    for (uint32_t i = 0; i < FIN_THREADS / 32; i++) tot += s_sum[i];
+    sums[k] = tot;
+    s_shift = m31_mul(fold64_p(tot), inv_n);
+  }
+  __syncthreads();
+  const uint32_t sh = s_shift;
+  // Coset positions [t * run, (t + 1) * run) belong to thread t.
+  const uint32_t run = n >= FIN_THREADS ? n / FIN_THREADS : 1u;
+  const uint32_t k0 = t * run;
+  const bool own = k0 < n;
+  uint32_t tot = 0;
+  if (own)
+    for (uint32_t i = 0; i < run; i++) tot = m31_add(tot, m31_sub(c[coset_to_storage(k0 + i, log_n)], sh));
+  // Exclusive scan of the run totals across the block.
+  uint32_t inc = tot;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o) inc = m31_add(inc, y);
+  }
+  if (lane == 31) s_scan[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t x = s_scan[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= (uint32_t)o) x = m31_add(x, y);
+    }
+    s_scan[lane] = x;  // inclusive over warps
+  }
+  __syncthreads();
+  uint32_t acc = m31_sub(inc, tot);  // exclusive within the warp
+  if (w > 0) acc = m31_add(acc, s_scan[w - 1]);
+  if (own)
+    for (uint32_t i = 0; i < run; i++) {
+      const uint32_t st = coset_to_storage(k0 + i, log_n);
+      acc = m31_add(acc, m31_sub(c[st], sh));
+      c[st] = acc;
+    }
+}
+
 static int32_t scan_rows(uint32_t* data, uint32_t len, uint32_t rows, Arena& arena, cudaStream_t s) {
   uint32_t n_tiles = (len + 4095) / 4096;
   STWO_REQUIRE(n_tiles <= 4096, "scan length too large");
@@ -272,8 +337,22 @@ static int32_t scan_rows(uint32_t* data, uint32_t len, uint32_t rows, Arena& are
 int32_t logup_finalize_last(uint32_t* last, uint32_t log_n, Arena& arena, cudaStream_t s, hq* claimed) {
   const size_t n = (size_t)1 << log_n;
   unsigned long long* d_sums = reinterpret_cast<unsigned long long*>(arena.alloc(8));
+  if (!d_sums) return STWO_ERR_OOM;
+  if (log_n <= FIN_ONE_BLOCK_LOG) {
+    k_logup_finalize_small<<<4, FIN_THREADS, 0, s>>>(last, log_n, h_inv((uint32_t)(n % P)), d_sums);
+    note_launch();
+    STWO_LAUNCH_CHECK();
+    unsigned long long* hs = small_pinned();
+    if (!hs) return STWO_ERR_OOM;
+    STWO_CHECK_CUDA(cudaMemcpyAsync(hs, d_sums, 32, cudaMemcpyDeviceToHost, s));
+    if (claimed) {
+      STWO_CHECK_CUDA(cudaStreamSynchronize(s));
+      *claimed = hq_make((uint32_t)(hs[0] % P), (uint32_t)(hs[1] % P), (uint32_t)(hs[2] % P), (uint32_t)(hs[3] % P));
+    }
+    return STWO_OK;
+  }
   uint32_t* tmp = arena.alloc(4 * n);
-  if (!d_sums || !tmp) return STWO_ERR_OOM;
+  if (!tmp) return STWO_ERR_OOM;
   STWO_CHECK_CUDA(cudaMemsetAsync(d_sums, 0, 32, s));
   const uint32_t g = std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024);
   k_column_sums<<<dim3(g, 4), 256, 0, s>>>(last, (uint32_t)n, d_sums);
