@@ -396,7 +396,9 @@ __global__ void k_secure_accumulate(uint32_t* a0, uint32_t* a1, uint32_t* a2, ui
   }
 }
 
-__global__ void k_secure_powers(qm31 felt, uint32_t n, uint32_t* out) {
+// out[j] = felt^i with j = i, or j = n - 1 - i when `reversed` (highest power first, the order of
+// the composition's random coefficients).
+__global__ void k_secure_powers(qm31 felt, uint32_t n, uint32_t reversed, uint32_t* out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   qm31 r = qm31_from_u32(1, 0, 0, 0), b = felt;
@@ -406,10 +408,20 @@ __global__ void k_secure_powers(qm31 felt, uint32_t n, uint32_t* out) {
     b = qm31_mul(b, b);
     e >>= 1;
   }
-  out[4 * i] = r.a.a;
-  out[4 * i + 1] = r.a.b;
-  out[4 * i + 2] = r.b.a;
-  out[4 * i + 3] = r.b.b;
+  const uint32_t j = reversed ? n - 1 - i : i;
+  out[4 * j] = r.a.a;
+  out[4 * j + 1] = r.a.b;
+  out[4 * j + 2] = r.b.a;
+  out[4 * j + 3] = r.b.b;
+}
+
+int32_t secure_powers_reversed(const uint32_t felt[4], uint32_t n, uint32_t* out, cudaStream_t s) {
+  if (n == 0) return STWO_OK;
+  const qm31 f = {{felt[0], felt[1]}, {felt[2], felt[3]}};
+  k_secure_powers<<<(n + 255) / 256, 256, 0, s>>>(f, n, 1u, out);
+  note_launch();
+  STWO_LAUNCH_CHECK();
+  return STWO_OK;
 }
 
 __global__ void k_gather(const uint32_t* col, const unsigned long long* idx, size_t n, uint32_t* out) {
@@ -477,7 +489,7 @@ stwo_status stwo_generate_secure_powers(stwo_qm31 felt, uint32_t n_powers, stwo_
   int32_t st = scratch_alloc((void**)&d, (size_t)n_powers * 16, s);
   if (st) return st;
   qm31 f = {{felt.v[0], felt.v[1]}, {felt.v[2], felt.v[3]}};
-  k_secure_powers<<<(n_powers + 255) / 256, 256, 0, s>>>(f, n_powers, d); note_launch();
+  k_secure_powers<<<(n_powers + 255) / 256, 256, 0, s>>>(f, n_powers, 0u, d); note_launch();
   cudaError_t e = cudaGetLastError();
   if (!e) e = cudaMemcpyAsync(h_out, d, (size_t)n_powers * 16, cudaMemcpyDeviceToHost, s);
   scratch_free(d, s);

@@ -58,6 +58,9 @@ __global__ void k_collect(CollectList l, uint32_t* out) {
     base += l.n[k];
   }
 }
+// rc^(n-1), ..., rc, 1 as 4-word QM31 values into out (AccumulationOps::generate_secure_powers,
+// reversed).
+int32_t secure_powers_reversed(const uint32_t felt[4], uint32_t n, uint32_t* out, cudaStream_t s);
 int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
                        const uint32_t* poly_of, const stwo_qm31_point* points, uint32_t n_evals, stwo_qm31* out,
                        cudaStream_t s);
@@ -427,13 +430,6 @@ int32_t Prover::commit_composition(const GpuAir& air, hq rc) {
   uint32_t eval_log = air.max_constraint_log_degree_bound();
   uint32_t trace_log = air.log_size();
   size_t n = air.n_constraints();
-  // Random coefficient powers, highest first: constraint k gets rc^(n-1-k).
-  std::vector<uint32_t> coeffs(4 * n);
-  hq p = hq_make(1, 0, 0, 0);
-  for (size_t k = 0; k < n; k++) {
-    for (int i = 0; i < 4; i++) coeffs[4 * (n - 1 - k) + i] = p.v[i];
-    p = hq_mul(p, rc);
-  }
   // Denominator inverses: 1 / coset_vanishing(trace coset, eval_domain.at(i)), bit-reversed.
   uint32_t expand = eval_log - trace_log;
   std::vector<uint32_t> dinv((size_t)1 << expand);
@@ -460,10 +456,12 @@ int32_t Prover::commit_composition(const GpuAir& air, hq rc) {
     }
     dinv.swap(tmp);
   }
-  uint32_t* d_coeffs = arena.alloc(coeffs.size() + dinv.size());
+  uint32_t* d_coeffs = arena.alloc(4 * n + dinv.size());
   if (!d_coeffs) return STWO_ERR_OOM;
-  uint32_t* d_dinv = d_coeffs + coeffs.size();
-  STWO_CHECK_CUDA(cudaMemcpyAsync(d_coeffs, coeffs.data(), coeffs.size() * 4, cudaMemcpyHostToDevice, s));
+  uint32_t* d_dinv = d_coeffs + 4 * n;
+  // Random coefficient powers, highest first: constraint k gets rc^(n-1-k), computed on the device.
+  int32_t pst = secure_powers_reversed(rc.v, (uint32_t)n, d_coeffs, s);
+  if (pst) return pst;
   STWO_CHECK_CUDA(cudaMemcpyAsync(d_dinv, dinv.data(), dinv.size() * 4, cudaMemcpyHostToDevice, s));
   StageScope stage_cext("Composition extension", s);
   // Trace columns on the evaluation domain, per tree (extension when the committed domain differs).
