@@ -191,109 +191,70 @@ __global__ void __launch_bounds__(128) k_br_trace(uint32_t n_rows, const uint32_
 }
 
 // ------------------------------------------------------------------------------------ interaction
-// Two schedules give the same columns. With many rows, one thread per row (k_br_interaction_rows)
-// fills the GPU and does the least work. With few rows, each thread's 64 dependent inversions
-// would set the kernel's time, and one warp per G-function (k_br_interaction_warps) divides that
-// chain by eight.
-//
-// One thread per row: accumulates the paired XOR fractions into cumulative secure columns as the
-// lookups appear.
-struct BrInteractionWriter {
-  const BrElements* e;
-  uint32_t* out;
-  size_t n;
-  uint32_t r;
-  qm31 cum = qm31_zero();
-  qm31 pending;
-  bool have = false;
-  uint32_t col = 0;
-  __device__ void felt(uint32_t) {}
-  __device__ void lookup(uint32_t w, uint32_t a, uint32_t b, uint32_t c) {
-    const qm31 p = br_xor_combine(e, w, a, b, c);
-    if (!have) {
-      pending = p;
-      have = true;
-      return;
-    }
-    have = false;
-    // 1/p0 + 1/p1 = (p0 + p1) / (p0 p1)
-    cum = qm31_add(cum, qm31_mul(qm31_add(pending, p), qm31_inv(qm31_mul(pending, p))));
-    write(cum);
-  }
-  __device__ void write(const qm31& x) {
-    out[((size_t)4 * col + 0) * n + r] = x.a.a;
-    out[((size_t)4 * col + 1) * n + r] = x.a.b;
-    out[((size_t)4 * col + 2) * n + r] = x.b.a;
-    out[((size_t)4 * col + 3) * n + r] = x.b.b;
-    col++;
-  }
-};
-
-__global__ void __launch_bounds__(128) k_br_interaction_rows(uint32_t n_rows, const uint32_t* __restrict__ inputs,
-                                                        const BrElements* __restrict__ e_dev, uint32_t* __restrict__ out) {
-  __shared__ BrElements s_e;
-  br_stage_elements(e_dev, &s_e);
-  __syncthreads();
-  const BrElements* e = &s_e;
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_rows) return;
-  // The Round relation's denominator: sum_k alpha^k x_k - z over (input, output, message) halves.
-  qm31 p = qm31_zero();
-  uint32_t v[BR_ST];
-#pragma unroll
-  for (int i = 0; i < BR_ST; i++) {
-    v[i] = br_input(inputs, r, i);
-    const uint32_t m = br_input(inputs, r, BR_ST + i);
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i]), v[i] & 0xffffu));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i + 1]), v[i] >> 16));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), m & 0xffffu));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), m >> 16));
-  }
-  BrInteractionWriter w{e, out, n_rows, r};
-  br_round(v, [&](int i) { return br_input(inputs, r, BR_ST + i); }, w);
-#pragma unroll
-  for (int i = 0; i < BR_ST; i++) {
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i]), v[i] & 0xffffu));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i + 1]), v[i] >> 16));
-  }
-  p = qm31_sub(p, br_q(e->rz));
-  // -1 / p
-  w.write(qm31_add(w.cum, qm31_sub(qm31_zero(), qm31_inv(p))));
-}
-
 // Each XOR pair contributes 1/p0 + 1/p1 = (p0 + p1) / (p0 p1) to the next cumulative column; the
 // pairs come in the evaluator's lookup order, eight per G-function (two per xor_rotr call), so
 // G-function g owns columns 8g .. 8g + 7.
 //
-// One warp per G-function: warp g of a block takes 32 consecutive rows, replays the integer state
-// of G-functions 0 .. g-1 (cheap next to the QM31 inversions), then computes its own eight pair
-// fractions. The eight warps' fraction sums meet in shared memory, and each warp writes its
-// columns as prefix sums from the sum of the warps before it. A row's 64 inversions are thus
-// spread over eight threads, which shortens the dependent chain of a thread eightfold, and every
-// column store of a warp is one 128-byte line.
+// A fraction is taken in cofactor form: g = (p0 + p1) * cof and the M31 norm n of p0 p1, with
+// (p0 p1) * cof = n (qm31_inv_parts), so it equals g / n. The four pairs of half a G-function
+// share one M31 inversion of their norms' product (Montgomery's batch trick in the base field),
+// which removes three of every four M31 inversions, the bulk of the kernel's instructions. The
+// denominators are z minus a random combination and nonzero except with negligible probability,
+// as the reference's batch inversion of the same columns (constraint_framework/logup.rs:224) also
+// assumes.
+//
+// Two schedules give the same columns. With many rows, one thread per row (k_br_interaction_rows)
+// fills the GPU and does the least work. With few rows, each thread's chain of dependent
+// inversions would set the kernel's time, and one warp per G-function (k_br_interaction_warps)
+// divides that chain by eight.
 constexpr uint32_t BI_ROWS = 32;
 constexpr uint32_t BI_WARPS_MAX_LOG = 15;  // k_br_interaction_warps up to 2^15 rows
 
-// The two pair fractions of one xor_rotr_u32 (RR < 16) or xor_rotr16_u32 (RR == 16, halves split
-// at 8): lookups (ll, hl) and (lh, hh), into f[K] and f[K + 1]. Returns the rotated xor.
+__device__ __forceinline__ void br_pair_parts(const qm31& p0, const qm31& p1, qm31& g, uint32_t& n) {
+  qm31 cof;
+  qm31_inv_parts(qm31_mul(p0, p1), cof, n);
+  g = qm31_mul(qm31_add(p0, p1), cof);
+}
+
+// The two pairs of one xor_rotr_u32 (RR < 16) or xor_rotr16_u32 (RR == 16, halves split at 8):
+// lookups (ll, hl) and (lh, hh), into slots K and K + 1. Returns the rotated xor.
 template <int K, uint32_t RR>
-__device__ __forceinline__ uint32_t br_xr_fracs(const BrElements* e, uint32_t a, uint32_t b, qm31 f[8]) {
+__device__ __forceinline__ uint32_t br_xr_parts(const BrElements* e, uint32_t a, uint32_t b, qm31 g[4], uint32_t n[4]) {
   constexpr uint32_t SP = RR == 16 ? 8 : RR;
   constexpr uint32_t M = (1u << SP) - 1;
   const uint32_t al = a & 0xffffu, ah = a >> 16, bl = b & 0xffffu, bh = b >> 16;
   const uint32_t all = al & M, alh = al >> SP, ahl = ah & M, ahh = ah >> SP;
   const uint32_t bll = bl & M, blh = bl >> SP, bhl = bh & M, bhh = bh >> SP;
-  const qm31 p0 = br_xor_combine(e, SP, all, bll, all ^ bll);
-  const qm31 p1 = br_xor_combine(e, SP, ahl, bhl, ahl ^ bhl);
-  f[K] = qm31_mul(qm31_add(p0, p1), qm31_inv(qm31_mul(p0, p1)));
-  const qm31 p2 = br_xor_combine(e, 16 - SP, alh, blh, alh ^ blh);
-  const qm31 p3 = br_xor_combine(e, 16 - SP, ahh, bhh, ahh ^ bhh);
-  f[K + 1] = qm31_mul(qm31_add(p2, p3), qm31_inv(qm31_mul(p2, p3)));
+  br_pair_parts(br_xor_combine(e, SP, all, bll, all ^ bll), br_xor_combine(e, SP, ahl, bhl, ahl ^ bhl), g[K], n[K]);
+  br_pair_parts(br_xor_combine(e, 16 - SP, alh, blh, alh ^ blh), br_xor_combine(e, 16 - SP, ahh, bhh, ahh ^ bhh),
+                g[K + 1], n[K + 1]);
   const uint32_t c = a ^ b;
   return (c >> RR) | (c << (32 - RR));
 }
 
-__device__ __forceinline__ uint32_t br_rotr(uint32_t x, uint32_t r) { return (x >> r) | (x << (32 - r)); }
+// Half a G-function (a += b + m, then the xor_rotr calls with rotations R1 and R2) and its four
+// pair fractions, in lookup order.
+template <uint32_t R1, uint32_t R2>
+__device__ __forceinline__ void br_half_g(const BrElements* e, uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d,
+                                          uint32_t m, qm31 f[4]) {
+  qm31 g[4];
+  uint32_t n[4];
+  a = a + b + m;
+  d = br_xr_parts<0, R1>(e, a, d, g, n);
+  c = c + d;
+  b = br_xr_parts<2, R2>(e, b, c, g, n);
+  const uint32_t n01 = m31_mul(n[0], n[1]);
+  const uint32_t n012 = m31_mul(n01, n[2]);
+  uint32_t inv = m31_inv(m31_mul(n012, n[3]));  // 1 / (n0 n1 n2 n3)
+  const uint32_t i3 = m31_mul(inv, n012);
+  inv = m31_mul(inv, n[3]);  // 1 / (n0 n1 n2)
+  const uint32_t i2 = m31_mul(inv, n01);
+  inv = m31_mul(inv, n[2]);  // 1 / (n0 n1)
+  f[0] = qm31_mul_m31(g[0], m31_mul(inv, n[1]));
+  f[1] = qm31_mul_m31(g[1], m31_mul(inv, n[0]));
+  f[2] = qm31_mul_m31(g[2], i2);
+  f[3] = qm31_mul_m31(g[3], i3);
+}
 
 __device__ __forceinline__ void br_write_q(uint32_t* out, size_t n, uint32_t r, uint32_t col, const qm31& x) {
   out[((size_t)4 * col + 0) * n + r] = x.a.a;
@@ -302,8 +263,79 @@ __device__ __forceinline__ void br_write_q(uint32_t* out, size_t n, uint32_t r, 
   out[((size_t)4 * col + 3) * n + r] = x.b.b;
 }
 
+// The Round relation's denominator: sum_k alpha^k x_k - z over the (input, output, message)
+// halves; `vo` is the state after the round.
+__device__ __forceinline__ qm31 br_round_denominator(const BrElements* e, const uint32_t* inputs, uint32_t r,
+                                                     const uint32_t vo[BR_ST]) {
+  qm31 p = qm31_zero();
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    const uint32_t x = br_input(inputs, r, i);
+    const uint32_t m = br_input(inputs, r, BR_ST + i);
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i]), x & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i + 1]), x >> 16));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i]), vo[i] & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i + 1]), vo[i] >> 16));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), m & 0xffffu));
+    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), m >> 16));
+  }
+  return qm31_sub(p, br_q(e->rz));
+}
+
+// One thread per row, the G-functions in br_round's rotating-state order.
+__global__ void __launch_bounds__(128) k_br_interaction_rows(uint32_t n_rows, const uint32_t* __restrict__ inputs,
+                                                             const BrElements* __restrict__ e_dev,
+                                                             uint32_t* __restrict__ out) {
+  __shared__ BrElements s_e;
+  br_stage_elements(e_dev, &s_e);
+  __syncthreads();
+  const BrElements* e = &s_e;
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  uint32_t v[BR_ST];
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) v[i] = br_input(inputs, r, i);
+  qm31 cum = qm31_zero();
+  uint32_t col = 0;
+#pragma unroll 1
+  for (uint32_t it = 0; it < 8; it++) {
+    if (it == 4) br_diagonalize(v);
+    uint32_t a = v[0], b = v[4], c = v[8], d = v[12];
+    qm31 f[4];
+    br_half_g<16, 12>(e, a, b, c, d, br_input(inputs, r, BR_ST + 2 * it), f);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      cum = qm31_add(cum, f[k]);
+      br_write_q(out, n_rows, r, col++, cum);
+    }
+    br_half_g<8, 7>(e, a, b, c, d, br_input(inputs, r, BR_ST + 2 * it + 1), f);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      cum = qm31_add(cum, f[k]);
+      br_write_q(out, n_rows, r, col++, cum);
+    }
+    v[0] = a;
+    v[4] = b;
+    v[8] = c;
+    v[12] = d;
+    br_rotate_rows(v);
+  }
+  br_undiagonalize(v);
+  // -1 / p of the Round relation, added to the sum of all 64 pairs.
+  const qm31 p = br_round_denominator(e, inputs, r, v);
+  br_write_q(out, n_rows, r, BR_XOR_PAIRS, qm31_add(cum, qm31_sub(qm31_zero(), qm31_inv(p))));
+}
+
+__device__ __forceinline__ uint32_t br_rotr(uint32_t x, uint32_t r) { return (x >> r) | (x << (32 - r)); }
+
+// One warp per G-function: warp g of a block takes 32 consecutive rows, replays the integer state
+// of G-functions 0 .. g-1 (cheap next to the fractions), then computes its own eight pair
+// fractions. The eight warps' fraction sums meet in shared memory, and each warp writes its
+// columns as prefix sums from the sum of the warps before it. Every column store of a warp is one
+// 128-byte line.
 __global__ void __launch_bounds__(256) k_br_interaction_warps(uint32_t n_rows, const uint32_t* __restrict__ inputs,
-                                                        const BrElements* __restrict__ e_dev, uint32_t* __restrict__ out) {
+                                                              const BrElements* __restrict__ e_dev,
+                                                              uint32_t* __restrict__ out) {
   __shared__ BrElements s_e;
   __shared__ qm31 s_tot[8][BI_ROWS];
   br_stage_elements(e_dev, &s_e);
@@ -339,14 +371,8 @@ __global__ void __launch_bounds__(256) k_br_interaction_warps(uint32_t n_rows, c
   qm31 f[8];
   {
     uint32_t a = v[0], b = v[4], c = v[8], d = v[12];
-    a = a + b + br_input(inputs, rr, BR_ST + 2 * g);
-    d = br_xr_fracs<0, 16>(e, a, d, f);
-    c = c + d;
-    b = br_xr_fracs<2, 12>(e, b, c, f);
-    a = a + b + br_input(inputs, rr, BR_ST + 2 * g + 1);
-    d = br_xr_fracs<4, 8>(e, a, d, f);
-    c = c + d;
-    b = br_xr_fracs<6, 7>(e, b, c, f);
+    br_half_g<16, 12>(e, a, b, c, d, br_input(inputs, rr, BR_ST + 2 * g), f);
+    br_half_g<8, 7>(e, a, b, c, d, br_input(inputs, rr, BR_ST + 2 * g + 1), f + 4);
     v[0] = a;
     v[4] = b;
     v[8] = c;
@@ -365,23 +391,10 @@ __global__ void __launch_bounds__(256) k_br_interaction_warps(uint32_t n_rows, c
     if (live) br_write_q(out, n_rows, r, 8 * g + k, cum);
   }
   if (g != 7) return;
-  // The Round relation, last column: sum_k alpha^k x_k - z over the (input, output, message)
-  // halves, its fraction -1/p added to the sum of all 64 pairs.
+  // The Round relation, last column: -1 / p added to the sum of all 64 pairs.
   br_rotate_rows(v);
   br_undiagonalize(v);
-  qm31 p = qm31_zero();
-#pragma unroll
-  for (int i = 0; i < BR_ST; i++) {
-    const uint32_t x = br_input(inputs, rr, i);
-    const uint32_t m = br_input(inputs, rr, BR_ST + i);
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i]), x & 0xffffu));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[2 * i + 1]), x >> 16));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i]), v[i] & 0xffffu));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[32 + 2 * i + 1]), v[i] >> 16));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i]), m & 0xffffu));
-    p = qm31_add(p, qm31_mul_m31(br_q(e->ra[64 + 2 * i + 1]), m >> 16));
-  }
-  p = qm31_sub(p, br_q(e->rz));
+  const qm31 p = br_round_denominator(e, inputs, rr, v);
   if (live) br_write_q(out, n_rows, r, BR_XOR_PAIRS, qm31_add(cum, qm31_sub(qm31_zero(), qm31_inv(p))));
 }
 

@@ -96,6 +96,16 @@ __device__ __forceinline__ qm31 qm31_mul_m31(qm31 x, uint32_t y) { return {cm31_
 __device__ __forceinline__ qm31 qm31_mul_cm31(qm31 x, cm31 y) { return {cm31_mul(x.a, y), cm31_mul(x.b, y)}; }
 __device__ __forceinline__ qm31 qm31_from_u32(uint32_t a, uint32_t b, uint32_t c, uint32_t d) { return {{a, b}, {c, d}}; }
 __device__ __forceinline__ qm31 qm31_zero() { return {{0u, 0u}, {0u, 0u}}; }
+// x^-1 = cof / norm with norm in M31: cof = (a - bu) * conj(a^2 - (2+i) b^2) and norm = |a^2 -
+// (2+i) b^2|^2, so x * cof = norm. Callers with several inverses to take share one M31 inversion
+// of the norms' product.
+__device__ __forceinline__ void qm31_inv_parts(qm31 x, qm31& cof, uint32_t& norm) {
+  const cm31 b2 = cm31_mul(x.b, x.b);
+  const cm31 den = cm31_sub(cm31_mul(x.a, x.a), cm31_mul_r(b2));
+  const cm31 cd = {den.a, m31_neg(den.b)};
+  norm = m31_add(m31_sqr(den.a), m31_sqr(den.b));
+  cof = {cm31_mul(x.a, cd), cm31_mul(cm31_sub({0u, 0u}, x.b), cd)};
+}
 __device__ __forceinline__ qm31 qm31_inv(qm31 x) {
   // (a + bu)^-1 = (a - bu) / (a^2 - (2+i) b^2)  (fields/qm31.rs:121-129)
   cm31 b2 = cm31_mul(x.b, x.b);
