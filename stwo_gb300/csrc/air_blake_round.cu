@@ -454,7 +454,9 @@ struct BrRowEval {
     a1 += (unsigned long long)k[1] * c;
     a2 += (unsigned long long)k[2] * c;
     a3 += (unsigned long long)k[3] * c;
-    if (++cnt == 3) {
+    // Products are at most (P - 1)^2 and a folded sum is below 2^33 + 2^31: four products fit
+    // between folds without passing 2^64.
+    if (++cnt == 4) {
       a0 = (a0 & P) + (a0 >> 31);
       a1 = (a1 & P) + (a1 >> 31);
       a2 = (a2 & P) + (a2 >> 31);

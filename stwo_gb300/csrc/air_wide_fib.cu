@@ -36,7 +36,9 @@ __global__ void __launch_bounds__(256) k_wide_fib_composition(ConstColPtrs cols,
     acc1 += (unsigned long long)k[1] * cons;
     acc2 += (unsigned long long)k[2] * cons;
     acc3 += (unsigned long long)k[3] * cons;
-    if (++cnt == 3) {
+    // Products are at most (P - 1)^2 and a folded sum is below 2^33 + 2^31: four products fit
+    // between folds without passing 2^64.
+    if (++cnt == 4) {
       acc0 = (acc0 & P) + (acc0 >> 31);
       acc1 = (acc1 & P) + (acc1 >> 31);
       acc2 = (acc2 & P) + (acc2 >> 31);
