@@ -69,9 +69,12 @@ __device__ __forceinline__ qm31 q_pow(qm31 b, uint32_t e) {
 // for the batch's j-th column with value v at point p, alpha_j = rc^(j+1), a_j = conj(v) - v,
 // c = conj(p.y) - p.y, b_j = v c - a_j p.y; the entry keeps alpha_j c, the batch the sums of
 // alpha_j a_j and alpha_j b_j and rc^n. Field sums are exact, so the reduction order is free.
-__global__ void __launch_bounds__(256) k_quotient_coeffs(const QSample* __restrict__ samples, QBatch* batches,
+// A batch can hold every column of a group (1,296 for Poseidon2), each needing rc^(j+1) by a
+// chain of QM31 products: 1024 threads per batch keep that to about one entry per thread.
+constexpr uint32_t QC_THREADS = 1024;
+__global__ void __launch_bounds__(QC_THREADS) k_quotient_coeffs(const QSample* __restrict__ samples, QBatch* batches,
                                                          QEntry* entries, qm31 rc) {
-  __shared__ qm31 s_a[8], s_b[8];
+  __shared__ qm31 s_a[QC_THREADS / 32], s_b[QC_THREADS / 32];
   QBatch& B = batches[blockIdx.x];
   const uint32_t e0 = B.e0, e1 = B.e1;
   const qm31 py = qm31_from_u32(B.pry[0], B.pry[1], B.piy[0], B.piy[1]);
@@ -158,15 +161,15 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows(uint32_t rows, 
       if (live) {
         uint32_t cnt = 0;
         uint32_t i = slice;
-        // Eight independent column loads in flight per iteration. Products are at most
+        // Sixteen independent column loads in flight per iteration. Products are at most
         // (P - 1)^2 < 2^62 - 2^33 + 4 and a folded sum is below 2^33 + 2^31, so a sum takes four
         // products between folds without passing 2^64.
-        for (; i + 7 * Q_SLICES < ne; i += 8 * Q_SLICES) {
-          uint32_t v[8];
+        for (; i + 15 * Q_SLICES < ne; i += 16 * Q_SLICES) {
+          uint32_t v[16];
 #pragma unroll
-          for (int u = 0; u < 8; u++) v[u] = __ldg(st[i + u * Q_SLICES].col + r);
+          for (int u = 0; u < 16; u++) v[u] = __ldg(st[i + u * Q_SLICES].col + r);
 #pragma unroll
-          for (int u = 0; u < 8; u++) {
+          for (int u = 0; u < 16; u++) {
             const QStage& q = st[i + u * Q_SLICES];
             s0 += (unsigned long long)q.c[0] * v[u];
             s1 += (unsigned long long)q.c[1] * v[u];
@@ -288,7 +291,7 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
   if (!hs.empty() && cudaMemcpyAsync(d_s, hs.data(), hs.size() * sizeof(QSample), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return fail(STWO_ERR_CUDA);
   if (n_batches) {
-    k_quotient_coeffs<<<n_batches, 256, 0, s>>>(d_s, d_b, d_e, qm31{{rc.v[0], rc.v[1]}, {rc.v[2], rc.v[3]}});
+    k_quotient_coeffs<<<n_batches, QC_THREADS, 0, s>>>(d_s, d_b, d_e, qm31{{rc.v[0], rc.v[1]}, {rc.v[2], rc.v[3]}});
     note_launch();
     if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
   }
