@@ -94,3 +94,23 @@ def test_admission_estimate_grows_with_size(cuda):
     small, big = Job(AIR_POSEIDON, 8), Job(AIR_POSEIDON, 16)
     assert 0 < small.hbm_bytes() < big.hbm_bytes()
     assert big.hbm_bytes() > 2 << 30  # a 2^16-row Poseidon2 proof holds ~3 GB
+
+
+def test_server_priority_levels_keep_results(cuda):
+    """Jobs of every stream-priority class at once (under 256 MB, under 2 GB, and two large ones
+    that overlap) give the same proofs as single calls."""
+    from stwo_gb300.prover import AIR_POSEIDON, AIR_WIDE_FIB, Job, Server
+
+    jobs = [Job(AIR_POSEIDON, 16, (10, 1, 0, 3), init=_dev(cases.words(31, (1 << 16) * 128))),
+            Job(AIR_POSEIDON, 6, (5, 1, 0, 3), init=_dev(cases.words(32, (1 << 6) * 128))),
+            Job(AIR_POSEIDON, 13, (10, 1, 0, 3), init=_dev(cases.words(33, (1 << 13) * 128))),
+            Job(AIR_POSEIDON, 16, (10, 1, 0, 3), init=_dev(cases.words(34, (1 << 16) * 128))),
+            Job(AIR_WIDE_FIB, 8, (5, 1, 0, 3), n_cols=100, a=_dev(cases.words(35, 256)), b=_dev(cases.words(36, 256)))]
+    sizes = [j.hbm_bytes() for j in jobs]
+    assert sizes[1] < 256 << 20 and sizes[4] < 256 << 20
+    assert 256 << 20 <= sizes[2] < 2 << 30
+    assert sizes[0] >= 2 << 30 and sizes[3] >= 2 << 30
+    want = [_single(j) for j in jobs]
+    with Server(n_workers=5) as srv:
+        rs = [srv.wait(t) for t in [srv.submit(j) for j in jobs]]
+    assert [r.proof for r in rs] == want
