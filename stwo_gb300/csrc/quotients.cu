@@ -9,9 +9,10 @@
 // the full domain through an interpolation and an evaluation; below a sub-domain of 2^6 points
 // every row is computed directly (the CPU fallback at simd/quotients.rs:41-58).
 //
-// GB300 mapping: one thread per row, columns streamed with coalesced 128-byte warp loads;
-// sum_j c_j * f_j is accumulated in 64-bit lanes (3 products per partial reduction) and the
-// linear terms are hoisted per batch (sum_j a_j, sum_j b_j), which leaves ~4 IMAD.WIDE + 4 IADD
+// GB300 mapping: four consecutive rows per lane with one 16-byte load per column, so a warp
+// reads 512 contiguous bytes of each column (one row per lane, 128 bytes, for unaligned
+// columns); sum_j c_j * f_j is accumulated in 64-bit lanes (4 products per partial reduction)
+// and the linear terms are hoisted per batch (sum_j a_j, sum_j b_j), which leaves ~4 IMAD.WIDE
 // per (column, row). The batch tables travel in a small device buffer.
 #include "common.cuh"
 
