@@ -243,3 +243,20 @@ def test_invalid_arguments_return_status(cuda):
     assert e.value.status == 1
     with pytest.raises(_lib.StwoError):
         cuda.grind([0] * 8, 33)
+
+
+def test_accumulate_quotients_unaligned_columns(cuda, oracle):
+    """Columns that start 4 bytes past a 16-byte boundary take the one-row-per-lane kernel; the
+    result is the same."""
+    rng = np.random.default_rng(811)
+    log_n, blowup, ncols = 12, 1, 9
+    cols = [F.rand_m31(rng, 1 << log_n) for _ in range(ncols)]
+    pts = sorted(rand_point(oracle, rng) for _ in range(2))
+    batches = [(pts[0], [(c, rq(rng)) for c in range(ncols)]), (pts[1], [(c, rq(rng)) for c in range(0, ncols, 3)])]
+    rc = rq(rng)
+    shifted = [dev(np.concatenate([np.zeros(1, np.uint32), c]))[1:] for c in cols]
+    assert all(t.data_ptr() % 16 == 4 for t in shifted)
+    out = cuda.accumulate_quotients(log_n, shifted, rc, batches, blowup)
+    want = oracle.accumulate_quotients(log_n, cols, rc, batches, blowup)
+    for k in range(4):
+        assert np.array_equal(host(out.cols[k]), want[k])
