@@ -20,7 +20,9 @@ timed region starts; `e2e` is the same metric through the public C ABI with the 
 from pinned host memory and the Merkle root + last FRI layer read back inside the timed region.
 
 `--impl reference` times the oracle (C++ restatement of the reference CPU backend; the reference
-Rust crate cannot be built without a Rust toolchain) on all host cores over a bounded sample.
+Rust crate cannot be built without a Rust toolchain) on all host cores: for the Poseidon2
+workload each step is one whole proof of the same 2^16-row configuration; the kernel workload
+takes a bounded sample of its columns.
 Multi-GPU (torchrun): independent replicas per rank, no collective on the data path.
 """
 from __future__ import annotations
@@ -56,10 +58,12 @@ def gen_words(k: int, c: int, n: int):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled every `period_ms` (25 ms) during the timed
+    region (a read-only query)."""
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, period_ms: int = 25):
         self.index = index
+        self.period_ms = period_ms
         self.rows = []
         self.proc = None
 
@@ -69,7 +73,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -104,7 +108,7 @@ class ClockSampler:
                 continue
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "period_ms": self.period_ms}
 
 
 def measured_peaks():
@@ -790,10 +794,7 @@ def run_gb300(args):
         "vs_baseline": None,
         "dtype": "u32 (M31 field words)",
         "data": "synthetic: seeded uniform M31 initial states (splitmix64 mod P)",
-        "config": {"workload": "Poseidon2 AIR proof, 2^16 rows x 8 permutations, LogUp interaction trace",
-                   "log_n_rows": wl.LOG, "trace_cells": wl.cells, "pow_bits": wl.CFG[0], "log_blowup": wl.CFG[1],
-                   "log_last_layer": wl.CFG[2], "n_queries": wl.CFG[3],
-                   "l2": "working set (~3 GB) far larger than L2; no flush", "parallelism": f"replicas x{world}"},
+        "config": poseidon_config(wl.LOG, world),
         "proof_bytes": len(wl.proof),
         "ms_per_step_spread": step_spread,
         "stages_ms": stages,
@@ -805,11 +806,21 @@ def run_gb300(args):
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline and world == 1:  # the CPU baseline is timed at N=1 only
-        line["cpu_baseline"] = cpu_baseline_poseidon(args.cpu_threads, log=15)
+        line["cpu_baseline"] = cpu_baseline_poseidon(args.cpu_threads, log=wl.LOG)
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline_poseidon(threads=0, log=15):
+def poseidon_config(log, world):
+    """The `config` of the Poseidon2 proof workload, shared by both arms."""
+    cfg = PoseidonWorkload.CFG
+    return {"workload": f"Poseidon2 AIR proof, 2^{log} rows x 8 permutations, LogUp interaction trace",
+            "log_n_rows": log, "trace_cells": (1 << log) * PoseidonWorkload.TRACE_COLS, "pow_bits": cfg[0],
+            "log_blowup": cfg[1], "log_last_layer": cfg[2], "n_queries": cfg[3],
+            "l2": "working set (~3 GB at 2^16 rows) far larger than L2; no flush",
+            "parallelism": f"replicas x{world}"}
+
+
+def cpu_baseline_poseidon(threads=0, log=16):
     """The oracle's Poseidon2 proof on all host cores (OpenMP), a bounded sample of 2^log rows."""
     import oracle.pyoracle as O
 
@@ -822,8 +833,9 @@ def cpu_baseline_poseidon(threads=0, log=15):
     secs = time.perf_counter() - t0
     cells = (1 << log) * PoseidonWorkload.TRACE_COLS
     return {"value": cells / secs, "unit": "trace cells/s", "cores": nthreads, "kind": "port",
-            "proof_s": secs, "sample": f"one full Poseidon2 proof of 2^{log} rows (the same AIR, config and "
-                                        f"input generator; 1/{1 << (16 - log)} of the rows): {secs:.2f} s"}
+            "proof_s": secs, "sample": f"one whole Poseidon2 proof of 2^{log} rows, the benchmarked "
+                                        f"configuration itself (same AIR, PcsConfig and input generator): "
+                                        f"{secs:.2f} s"}
 
 
 def run_kernels(args, world, rank, local, lib, barrier, max_over_ranks):
@@ -967,14 +979,15 @@ def run_reference(args):
         config = {"workload": "GKR batch proof, one LogUp-generic layer of 2^20 leaves (Poseidon2 relation shape "
                               "at 2^16 rows)", "log_leaves": 20}
     else:
-        log = 14
+        # Each step is one whole proof of the benchmarked configuration (2^16 rows: ~2-3 s on 16
+        # cores), so both arms time the same work.
+        log = args.log_rows or PoseidonWorkload.LOG
         for _ in range(min(args.warmup, 1)):
             cpu_baseline_poseidon(args.cpu_threads, log=log)
         vals = [cpu_baseline_poseidon(args.cpu_threads, log=log) for _ in range(args.steps)]
         metric = "proof s & trace cells/s (Poseidon2 2^16 rows)"
         unit = "trace cells/s"
-        config = {"workload": "Poseidon2 AIR proof, 2^16 rows x 8 permutations, LogUp interaction trace",
-                  "sample_rows_per_step": 1 << log}
+        config = poseidon_config(log, int(os.environ.get("WORLD_SIZE", "1")))
     v = sorted(x["value"] for x in vals)[len(vals) // 2]
     cb = dict(vals[0])
     cb["value"] = v

@@ -118,10 +118,12 @@ stwo_status stwo_eval_at_points(const uint32_t* const* d_coeffs, const uint32_t*
  * calls no cudaMalloc/cudaFree or allocating library routine: its scratch is a fixed
  * 256-byte-aligned static device array of about 200 KB, held by every GPU that loads this library
  * until the process exits. Limits: n_evals <= STWO_NOALLOC_MAX_EVALS and
- * n_polys <= STWO_NOALLOC_MAX_POLYS, else STWO_ERR_INVALID_ARG. The first call on a device looks
- * up the array's device address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture. All calls share the one array: calls that overlap on the GPU
- * (other streams, other host threads) race and must be serialised by the caller. */
+ * n_polys <= STWO_NOALLOC_MAX_POLYS, else STWO_ERR_INVALID_ARG. Every call looks up the array's
+ * device address (cudaGetSymbolAddress, which allocates nothing) in the current device's context,
+ * so the first call on a device also loads the module there; make that first call before any
+ * stream capture. All calls share the one array and it keeps the last call's contents (the call
+ * clears its accumulators itself): calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. */
 #define STWO_NOALLOC_MAX_EVALS 2048
 #define STWO_NOALLOC_MAX_POLYS 2048
 stwo_status stwo_eval_at_points_noalloc(const uint32_t* const* d_coeffs, const uint32_t* h_log_sizes,

@@ -32,13 +32,18 @@ void oracle_gen_words(uint64_t k, uint64_t c, uint64_t n, uint32_t* out) {
   for (uint64_t i = 0; i < n; i++) out[i] = gen_word(k, c, i);
 }
 
+}  // extern "C"
+
+namespace {
+
 // Kernel-microbench sample: `n_cols` columns of 2^log words (workload k = 1) interpolated on the
 // canonic domain, evaluated at log + blowup, committed in a Blake2s Merkle tree; plus one FRI
 // fold chain of a 2^fri_log QM31 circle evaluation (columns 1000..1003) down to 2^4 with seeded
 // alphas. Returns compute seconds (input generation and twiddles excluded); writes the Merkle
-// root (8 words) and the last FRI layer (4 x 16 words).
-double oracle_bench_cfg2(uint32_t n_cols, uint32_t log, uint32_t blowup, uint32_t fri_log, int threads,
-                         uint32_t* root_out, uint32_t* fri_out) {
+// root (8 words) and the last FRI layer (4 x 16 words). With `fri_layers_out` set, every folded
+// FRI layer is written there too (4 coordinate columns per layer, largest layer first).
+double cfg2_pass(uint32_t n_cols, uint32_t log, uint32_t blowup, uint32_t fri_log, int threads, uint32_t* root_out,
+                 uint32_t* fri_out, uint32_t* fri_layers_out) {
   if (threads > 0) omp_set_num_threads(threads);
   const uint32_t L = log + blowup;
   size_t n = (size_t)1 << log, N = (size_t)1 << L;
@@ -91,16 +96,39 @@ double oracle_bench_cfg2(uint32_t n_cols, uint32_t log, uint32_t blowup, uint32_
   // FRI fold chain.
   SecureColumn line((size_t)1 << (fri_log - 1));
   fold_circle_into_line(line, fsrc, fdom, alphas[0]);
+  auto keep = [&](const SecureColumn& l) {
+    if (!fri_layers_out) return;
+    for (int k = 0; k < 4; k++)
+      for (size_t i = 0; i < l.size(); i++) *fri_layers_out++ = l.c[k][i].v;
+  };
+  keep(line);
   Coset ld = fdom.half_coset;
   for (uint32_t j = 1; line.size() > 16; j++) {
     line = fold_line(line, ld, alphas[j]);
     ld = ld.dbl();
+    keep(line);
   }
   double t1 = now();
   layers.back()[0].words(root_out);
   for (int k = 0; k < 4; k++)
     for (size_t i = 0; i < line.size() && i < 16; i++) fri_out[16 * k + i] = line.c[k][i].v;
   return t1 - t0;
+}
+
+}  // namespace
+
+extern "C" {
+
+double oracle_bench_cfg2(uint32_t n_cols, uint32_t log, uint32_t blowup, uint32_t fri_log, int threads,
+                         uint32_t* root_out, uint32_t* fri_out) {
+  return cfg2_pass(n_cols, log, blowup, fri_log, threads, root_out, fri_out, nullptr);
+}
+
+// The same pass with every folded FRI layer written to `fri_layers_out`: 4 x 2^(fri_log-1) words
+// for the circle fold, then 4 x 2^(k-1) for each line fold down to 2^4 points.
+double oracle_cfg2_outputs(uint32_t n_cols, uint32_t log, uint32_t blowup, uint32_t fri_log, int threads,
+                           uint32_t* root_out, uint32_t* fri_out, uint32_t* fri_layers_out) {
+  return cfg2_pass(n_cols, log, blowup, fri_log, threads, root_out, fri_out, fri_layers_out);
 }
 
 }  // extern "C"

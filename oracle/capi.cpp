@@ -220,6 +220,27 @@ int oracle_verify_wide_fib(uint32_t log_n, uint32_t n_cols, const uint8_t* proof
 
 extern "C" {
 
+// The Poseidon2 linear layers of the example (poseidon/mod.rs apply_m4, apply_internal_round_matrix,
+// apply_external_round_matrix), in place on canonical words.
+void oracle_poseidon_apply_m4(uint32_t x[4]) {
+  M31 v[4];
+  for (int i = 0; i < 4; i++) v[i] = M31(x[i]);
+  apply_m4(v);
+  for (int i = 0; i < 4; i++) x[i] = v[i].v;
+}
+void oracle_poseidon_apply_internal(uint32_t x[16]) {
+  M31 v[16];
+  for (int i = 0; i < 16; i++) v[i] = M31(x[i]);
+  apply_internal_round_matrix(v);
+  for (int i = 0; i < 16; i++) x[i] = v[i].v;
+}
+void oracle_poseidon_apply_external(uint32_t x[16]) {
+  M31 v[16];
+  for (int i = 0; i < 16; i++) v[i] = M31(x[i]);
+  apply_external_round_matrix(v);
+  for (int i = 0; i < 16; i++) x[i] = v[i].v;
+}
+
 // Proves the Poseidon2 AIR (2^log_n rows, 8 permutations per row) as prove_poseidon does
 // (poseidon/mod.rs:327-389). `init` holds the initial states ((row * 8 + rep) * 16 + i), or is NULL
 // for the reference's deterministic inputs. Writes the proof bytes; claimed_sum (4 words) out.

@@ -342,3 +342,37 @@ def channel_draw_felts(n):
     out = np.zeros((n, 4), np.uint32)
     lib().oracle_channel_draw_felts(C.c_size_t(n), _p(out))
     return out
+
+
+def gen_words(k, c, n):
+    """The benchmark input generator (word i of column c of workload k)."""
+    out = np.zeros(n, np.uint32)
+    lib().oracle_gen_words(C.c_uint64(k), C.c_uint64(c), C.c_uint64(n), _p(out))
+    return out
+
+
+def cfg2_outputs(n_cols, log, blowup, fri_log, threads=0):
+    """The kernel-microbench pass on the oracle: (Merkle root words, [FRI layers as 4 columns each])."""
+    root = np.zeros(8, np.uint32)
+    last = np.zeros(64, np.uint32)
+    sizes = [1 << (fri_log - 1)]
+    while sizes[-1] > 16:
+        sizes.append(sizes[-1] // 2)
+    layers = np.zeros(4 * sum(sizes), np.uint32)
+    f = lib().oracle_cfg2_outputs
+    f.restype = C.c_double
+    f(C.c_uint32(n_cols), C.c_uint32(log), C.c_uint32(blowup), C.c_uint32(fri_log), C.c_int(threads), _p(root),
+      _p(last), _p(layers))
+    out, off = [], 0
+    for n in sizes:
+        out.append(layers[off:off + 4 * n].reshape(4, n))
+        off += 4 * n
+    return root, out
+
+
+def poseidon_linear(kind, state):
+    """The Poseidon2 example's linear layers on a state: kind "m4" (4 words), "internal" or
+    "external" (16 words)."""
+    x = _u32(state).copy()
+    getattr(lib(), f"oracle_poseidon_apply_{kind}")(_p(x))
+    return [int(v) for v in x]

@@ -295,26 +295,18 @@ static_assert(NA_OFF_POLYOF % 8 == 0 && NA_OFF_PTS % 8 == 0 && NA_OFF_ACC % 8 ==
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
-// Device address of g_noalloc_scratch, looked up once per device with that device current (the
-// host-side symbol is only a stand-in and must never reach a kernel).
-static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[256] = {};
-
+// Device address of g_noalloc_scratch in the current device's context. It is looked up on every
+// call (cudaGetSymbolAddress allocates nothing): a cached address would go stale after a device
+// reset or when the caller makes a context current that is not the device's primary one. The
+// host-side symbol is only a stand-in and must never reach a kernel.
 static int32_t noalloc_scratch(unsigned char** out) {
-  int dev = 0;
-  STWO_CHECK_CUDA(cudaGetDevice(&dev));
-  STWO_REQUIRE(dev >= 0 && dev < 256, "device ordinal %d out of range", dev);
-  std::lock_guard<std::mutex> g(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      set_error("cudaGetSymbolAddress of the no-alloc scratch: %s", cudaGetErrorString(e));
-      return STWO_ERR_CUDA;
-    }
-    g_noalloc_addr[dev] = p;
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    set_error("cudaGetSymbolAddress of the no-alloc scratch: %s", cudaGetErrorString(e));
+    return STWO_ERR_CUDA;
   }
-  *out = reinterpret_cast<unsigned char*>(g_noalloc_addr[dev]);
+  *out = reinterpret_cast<unsigned char*>(p);
   return STWO_OK;
 }
 

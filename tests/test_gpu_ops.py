@@ -131,7 +131,7 @@ def test_merkle_layer(cuda, oracle, log, ncols, prev):
     assert np.array_equal(host(got).reshape(-1, 8), want)
 
 
-@pytest.mark.parametrize("log", [1, 2, 3, 4, 5, 10, 15])
+@pytest.mark.parametrize("log", [1, 2, 3, 4, 5, 10, 15, 21, 22])
 def test_fold_line(cuda, oracle, log):
     from stwo_gb300 import _lib
     from stwo_gb300.backend import SecureColumn, TwiddleTree
@@ -148,7 +148,7 @@ def test_fold_line(cuda, oracle, log):
         assert np.array_equal(host(out.cols[k]), want[k])
 
 
-@pytest.mark.parametrize("log", [1, 2, 3, 4, 6, 12, 16])
+@pytest.mark.parametrize("log", [1, 2, 3, 4, 6, 12, 16, 21, 22])
 def test_fold_circle_into_line(cuda, oracle, log):
     from stwo_gb300 import _lib
     from stwo_gb300.backend import SecureColumn, TwiddleTree

@@ -10,6 +10,7 @@ Each test restates a reference test or a published vector:
   FRI:      crates/prover/src/core/fri.rs:1224-1253 (fold_line_works).
   Twiddles: crates/prover/src/core/poly/utils.rs:104-113 (test_domain_line_twiddles_works).
   Quotients: crates/prover/src/core/backend/simd/quotients.rs:296-344 (SIMD == CPU on low-degree input).
+  Poseidon2: crates/prover/src/examples/poseidon/mod.rs:427-461 (test_apply_m4, test_apply_internal).
 """
 import numpy as np
 import pytest
@@ -170,3 +171,35 @@ def test_grind_minimum_nonce(oracle):
     for k in range(n):
         assert oracle.raw_compress(digest, [k & 0xFFFFFFFF, k >> 32] + [0] * 14)[0] % 64 != 0
     assert oracle.raw_compress(digest, [n, 0] + [0] * 14)[0] % 64 == 0
+
+
+def _matmul(rows, state):
+    return [sum(r * s for r, s in zip(row, state)) % F.P for row in rows]
+
+
+def test_poseidon_apply_m4(oracle):
+    """test_apply_m4 (crates/prover/src/examples/poseidon/mod.rs:427-440): apply_m4 equals the
+    row-major matrix [5 7 1 3; 4 6 1 1; 1 3 5 7; 1 1 4 6] on the state (0, 1, 2, 3)."""
+    m4 = [[5, 7, 1, 3], [4, 6, 1, 1], [1, 3, 5, 7], [1, 1, 4, 6]]
+    state = [0, 1, 2, 3]
+    assert oracle.poseidon_linear("m4", state) == _matmul(m4, state)
+    # The same matrix on a state of large words (wrap-around of the additions).
+    big = [F.P - 1, F.P - 2, 12345, F.P - 7]
+    assert oracle.poseidon_linear("m4", big) == _matmul(m4, big)
+
+
+def test_poseidon_apply_internal(oracle):
+    """test_apply_internal (poseidon/mod.rs:442-461): the internal round matrix is the all-ones
+    matrix plus diag(2^(i+1)), on the state (3i + 187)."""
+    state = [3 * i + 187 for i in range(16)]
+    mat = [[1 + ((1 << (i + 1)) if i == j else 0) for j in range(16)] for i in range(16)]
+    assert oracle.poseidon_linear("internal", state) == _matmul(mat, state)
+
+
+def test_poseidon_apply_external(oracle):
+    """The external round matrix (poseidon/mod.rs apply_external_round_matrix): circ(2 M4, M4, M4,
+    M4) as blocks, i.e. M4 on each quarter followed by adding the column sums of the quarters."""
+    m4 = [[5, 7, 1, 3], [4, 6, 1, 1], [1, 3, 5, 7], [1, 1, 4, 6]]
+    mat = [[m4[i % 4][j % 4] * (2 if i // 4 == j // 4 else 1) for j in range(16)] for i in range(16)]
+    state = [(i * 0x1234567 + 99) % F.P for i in range(16)]
+    assert oracle.poseidon_linear("external", state) == _matmul(mat, state)

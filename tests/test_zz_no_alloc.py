@@ -56,6 +56,22 @@ def test_noalloc_matches_allocating_entry_point_twice(cuda):
         assert got == want
 
 
+def test_noalloc_matches_oracle_on_multi_block_polynomials(cuda, oracle):
+    """Polynomials of 2^20 and 2^18 coefficients span several blocks of the table-less split, so
+    each block's partial sum is scaled by the point's top-bit factors before the accumulation;
+    several evaluations per polynomial share its coefficients. Two calls in a row, each checked
+    against the oracle's eval_at_point."""
+    rng = np.random.default_rng(2025)
+    for log, n_polys, n_evals in ((20, 2, 6), (18, 3, 7)):
+        host_polys = [F.rand_m31(rng, 1 << log) for _ in range(n_polys)]
+        polys = [_dev(p) for p in host_polys]
+        queries = [(i % n_polys, (_rq(rng), _rq(rng))) for i in range(n_evals)]
+        st, got = _call("stwo_eval_at_points_noalloc", polys, queries)
+        assert st == 0
+        for (pi, pt), g in zip(queries, got):
+            assert g == oracle.eval_at_point(host_polys[pi], pt)
+
+
 def test_noalloc_rejects_sizes_beyond_its_maximum(cuda):
     from stwo_gb300 import _lib
 
