@@ -326,6 +326,47 @@ size_t stwo_job_hbm_bytes(const stwo_proof_job* job);
 stwo_status stwo_prove_batch(const stwo_proof_job* jobs, uint32_t n_jobs, uint32_t n_workers,
                              size_t hbm_budget_bytes, stwo_proof_result* results);
 
+/* ------------------------------------------------------------------ components */
+/* One component of a configured AIR: the FrameworkComponent<E> of the wide-Fibonacci, Poseidon2 or
+ * Blake2s-round example (crates/prover/src/constraint_framework/component.rs:126-200). Relation
+ * elements are given as the channel drew them (LookupElements::draw, logup.rs:74-88): Poseidon2
+ * takes 2 (z, alpha); the Blake2s round takes 12: (z, alpha) of the round relation, then of the XOR
+ * relations of widths 12, 9, 8, 7 and 4. claimed_sum is the LogUp claimed sum (unused by
+ * wide-Fibonacci). */
+typedef struct {
+  uint32_t air;                /* STWO_AIR_WIDE_FIB, STWO_AIR_POSEIDON or STWO_AIR_BLAKE_ROUND */
+  uint32_t log_n_rows;         /* trace log size */
+  uint32_t n_cols;             /* wide-Fibonacci columns */
+  stwo_qm31 claimed_sum;
+  const stwo_qm31* h_elements;
+  uint32_t n_elements;
+} stwo_component;
+
+/* Component::n_constraints, max_constraint_log_degree_bound and trace_log_degree_bounds
+ * (crates/prover/src/core/air/mod.rs:17-40): the constraint count, the log size of the evaluation
+ * domain CanonicCoset(eval_log_size).circle_domain(), and how many columns the component reads from
+ * each tree (tree 0 preprocessed, 1 trace, 2 interaction; *h_n_trees of them). */
+stwo_status stwo_component_info(const stwo_component* component, uint32_t* h_n_constraints, uint32_t* h_eval_log_size,
+                                uint32_t* h_n_trees, uint32_t h_tree_n_cols[3]);
+
+/* ComponentProver::evaluate_constraint_quotients_on_domain (crates/prover/src/core/air/mod.rs:59-62;
+ * SimdBackend implementation crates/prover/src/constraint_framework/component.rs:278-416), after its
+ * extension step:
+ *   d_cols          the component's columns on the evaluation domain (bit-reversed evaluations),
+ *                   tree by tree in stwo_component_info's counts; the caller extends the committed
+ *                   polynomials with stwo_evaluate_columns where the domains differ. Poseidon2 and
+ *                   Blake2s-round columns must form one contiguous block per tree (column c at the
+ *                   tree's first column + c * 2^eval_log_size words).
+ *   h_coeff_powers  the n_constraints random-coefficient powers that
+ *                   DomainEvaluationAccumulator::columns hands the component
+ *                   (crates/prover/src/core/air/accumulation.rs:71-93), in that order.
+ *   d_accum         the accumulation column of the evaluation domain's log size: every row adds
+ *                   row_res / coset_vanishing(trace coset, row point).
+ * Stream ordered. */
+stwo_status stwo_eval_constraints(const stwo_component* component, const uint32_t* const* d_cols, uint32_t n_cols,
+                                  const stwo_qm31* h_coeff_powers, uint32_t n_coeff_powers,
+                                  uint32_t* const d_accum[4], void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -3,6 +3,7 @@
 // Nothing in the product links this library.
 #include "ops.h"
 #include <cstring>
+#include <memory>
 
 using namespace oracle;
 
@@ -539,6 +540,89 @@ int oracle_verify_blake_round(uint32_t log_n, const uint32_t claimed_sum[4], con
   } catch (const std::exception& e) {
     snprintf(err, err_cap, "%s", e.what());
     return 0;
+  }
+}
+
+// ComponentProver::evaluate_constraint_quotients_on_domain after the extension step
+// (constraint_framework/component.rs:322-416): acc[r] += row_res(r) / coset_vanishing(trace coset,
+// point r) on CanonicCoset(eval log).circle_domain(). `cols` lists the component's columns on that
+// domain tree by tree (trace, then interaction); `coeffs` are the accumulator's powers in the order
+// it hands them (reversed here, as the component does). air: 0 wide-Fibonacci, 1 Poseidon2,
+// 2 Blake2s round; `elements` as drawn (z, alpha pairs). Returns 0, or 1 on bad input.
+int oracle_eval_constraints(uint32_t air_id, uint32_t log_n, uint32_t n_cols, const uint32_t claimed_sum[4],
+                            const uint32_t* elements, uint32_t n_elements, const uint32_t* const* cols,
+                            uint32_t n_cols_total, const uint32_t* coeffs, uint32_t n_coeffs, uint32_t* const acc[4]) {
+  try {
+    auto rel_powers = [](QM31 alpha, QM31* out, size_t n) {
+      QM31 cur(M31(1));
+      for (size_t i = 0; i < n; i++) {
+        out[i] = cur;
+        cur = cur * alpha;
+      }
+    };
+    std::unique_ptr<Air> air;
+    std::vector<size_t> tree_cols;
+    if (air_id == 0) {
+      air.reset(new WideFibAir(log_n, n_cols));
+      tree_cols = {0, n_cols};
+    } else if (air_id == 1) {
+      if (n_elements != 2) return 1;
+      LookupElements le;
+      le.z = q_of(elements);
+      le.alpha = q_of(elements + 4);
+      rel_powers(le.alpha, le.alpha_powers, PS_STATE);
+      air.reset(new PoseidonAir(log_n, le, q_of(claimed_sum)));
+      tree_cols = {0, PS_COLUMNS, 4 * PS_INSTANCES_PER_ROW};
+    } else if (air_id == 2) {
+      if (n_elements != 12) return 1;
+      BlakeRoundElements el;
+      auto set = [&](auto& r, int k, size_t n) {
+        r.z = q_of(elements + 8 * k);
+        r.alpha = q_of(elements + 8 * k + 4);
+        rel_powers(r.alpha, r.alpha_powers, n);
+      };
+      set(el.round, 0, BR_ROUND_FELTS);
+      set(el.xor_.xor12, 1, 3);
+      set(el.xor_.xor9, 2, 3);
+      set(el.xor_.xor8, 3, 3);
+      set(el.xor_.xor7, 4, 3);
+      set(el.xor_.xor4, 5, 3);
+      air.reset(new BlakeRoundAir(log_n, el, q_of(claimed_sum)));
+      tree_cols = {0, BR_TRACE_COLS, 4 * BR_INTERACTION_SECURE};
+    } else {
+      return 1;
+    }
+    size_t total = 0;
+    for (size_t t : tree_cols) total += t;
+    if (total != n_cols_total || n_coeffs != air->n_constraints()) return 1;
+    const uint32_t trace_log = air->log_size(), eval_log = air->max_constraint_log_degree_bound();
+    const size_t N = (size_t)1 << eval_log;
+    std::vector<std::vector<Column>> own(tree_cols.size());
+    std::vector<std::vector<const Column*>> tr(tree_cols.size());
+    size_t k = 0;
+    for (size_t t = 0; t < tree_cols.size(); t++) {
+      for (size_t c = 0; c < tree_cols[t]; c++) own[t].push_back(col_of(cols[k++], N));
+      for (auto& c : own[t]) tr[t].push_back(&c);
+    }
+    std::vector<QM31> rc;
+    for (size_t i = n_coeffs; i-- > 0;) rc.push_back(q_of(coeffs + 4 * i));
+    CircleDomain ed = canonic_domain(eval_log);
+    Coset tc = canonic_coset(trace_log);
+    std::vector<M31> dinv;
+    for (size_t i = 0; i < ((size_t)1 << (eval_log - trace_log)); i++) dinv.push_back(inv(coset_vanishing(tc, ed.at(i))));
+    bit_reverse(dinv);
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < (long)N; r++) {
+      DomainEvaluator e(&tr, r, trace_log, eval_log, rc.data());
+      QM31 v = air->eval_row(e) * dinv[r >> trace_log];
+      QM31 a = QM31::from_u32(acc[0][r], acc[1][r], acc[2][r], acc[3][r]) + v;
+      uint32_t w[4];
+      q_to(a, w);
+      for (int j = 0; j < 4; j++) acc[j][r] = w[j];
+    }
+    return 0;
+  } catch (...) {
+    return 1;
   }
 }
 

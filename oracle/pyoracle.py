@@ -376,3 +376,21 @@ def poseidon_linear(kind, state):
     x = _u32(state).copy()
     getattr(lib(), f"oracle_poseidon_apply_{kind}")(_p(x))
     return [int(v) for v in x]
+
+
+def eval_constraints(air, log_n, n_cols, claimed_sum, elements, cols, coeffs, acc):
+    """The oracle's per-component constraint accumulation: returns acc (4 columns) after adding
+    row_res / Z(row) on the evaluation domain. `cols` are the component's columns on that domain,
+    tree by tree; `coeffs` the accumulator's powers in the order it hands them."""
+    cs = _u32(claimed_sum)
+    el = _u32(np.asarray(elements, np.uint32).reshape(-1)) if len(elements) else np.zeros(4, np.uint32)
+    cl = [_u32(c) for c in cols]
+    tbl = (C.c_void_p * max(1, len(cl)))(*[c.ctypes.data for c in cl])
+    co = _u32(np.asarray(coeffs, np.uint32).reshape(-1))
+    out = [_u32(a).copy() for a in acc]
+    st = lib().oracle_eval_constraints(C.c_uint32(air), C.c_uint32(log_n), C.c_uint32(n_cols), _p(cs), _p(el),
+                                       C.c_uint32(len(elements)), tbl, C.c_uint32(len(cl)), _p(co),
+                                       C.c_uint32(len(coeffs)), _arr4(out))
+    if st != 0:
+        raise ValueError("oracle_eval_constraints: bad input")
+    return out

@@ -58,6 +58,11 @@ class ProofJob(C.Structure):
                 ("capacity", C.c_size_t)]
 
 
+class Component(C.Structure):
+    _fields_ = [("air", C.c_uint32), ("log_n_rows", C.c_uint32), ("n_cols", C.c_uint32), ("claimed_sum", QM31),
+                ("h_elements", C.POINTER(QM31)), ("n_elements", C.c_uint32)]
+
+
 class ProofResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("len", C.c_size_t), ("claimed_sum", QM31), ("queue_ms", C.c_double),
                 ("run_ms", C.c_double), ("latency_ms", C.c_double), ("error", C.c_char * 256)]
@@ -116,6 +121,9 @@ SIGNATURES = {
     "stwo_server_destroy": (C.c_int32, [VP]),
     "stwo_job_hbm_bytes": (C.c_size_t, [C.POINTER(ProofJob)]),
     "stwo_prove_batch": (C.c_int32, [C.POINTER(ProofJob), U32, U32, C.c_size_t, C.POINTER(ProofResult)]),
+    "stwo_component_info": (C.c_int32, [C.POINTER(Component), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                        C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "stwo_eval_constraints": (C.c_int32, [C.POINTER(Component), PVP, U32, C.POINTER(QM31), U32, PVP, VP]),
 }
 
 _lib = None

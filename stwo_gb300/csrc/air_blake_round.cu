@@ -401,6 +401,7 @@ __global__ void __launch_bounds__(256) k_br_interaction_warps(uint32_t n_rows, c
 // ------------------------------------------------------------------------------------ composition
 struct BrParams {
   uint32_t trace_log, eval_log;
+  uint32_t accumulate;  // add row_res * denom_inv to the output columns instead of writing it
   uint32_t shift[4];  // claimed_sum / 2^trace_log
 };
 
@@ -594,10 +595,17 @@ __global__ void __launch_bounds__(128, 4) k_br_composition(const uint32_t* __res
   const qm31 res = qm31_add(qm31_from_u32(br_fold64(ev.a0), br_fold64(ev.a1), br_fold64(ev.a2), br_fold64(ev.a3)),
                             ev.logup);
   const uint32_t dv = __ldg(dinv + (r >> pp.trace_log));
-  o0[r] = m31_mul(res.a.a, dv);
-  o1[r] = m31_mul(res.a.b, dv);
-  o2[r] = m31_mul(res.b.a, dv);
-  o3[r] = m31_mul(res.b.b, dv);
+  uint32_t v0 = m31_mul(res.a.a, dv), v1 = m31_mul(res.a.b, dv), v2 = m31_mul(res.b.a, dv), v3 = m31_mul(res.b.b, dv);
+  if (pp.accumulate) {
+    v0 = m31_add(o0[r], v0);
+    v1 = m31_add(o1[r], v1);
+    v2 = m31_add(o2[r], v2);
+    v3 = m31_add(o3[r], v3);
+  }
+  o0[r] = v0;
+  o1[r] = v1;
+  o2[r] = v2;
+  o3[r] = v3;
 }
 
 // ------------------------------------------------------------------------------------ host side
@@ -661,7 +669,8 @@ struct BlakeRoundGpuAir : GpuAir {
   }
   hq shift() const { return hq_sc(claimed_sum, h_inv((uint32_t)((1ull << log_n) % P))); }
   int32_t eval_composition(const std::vector<std::vector<const uint32_t*>>& cols, const uint32_t* coeffs,
-                           const uint32_t* dinv, uint32_t* const acc[4], cudaStream_t s) const override {
+                           const uint32_t* dinv, uint32_t* const acc[4], bool accumulate,
+                           cudaStream_t s) const override {
     STWO_REQUIRE(cols.size() >= 3 && cols[1].size() == BR_COLS && cols[2].size() == 4 * BR_INTER_SECURE,
                  "trace trees mismatch");
     const uint32_t el_log = log_n + 1;
@@ -673,6 +682,7 @@ struct BlakeRoundGpuAir : GpuAir {
     BrParams pp;
     pp.trace_log = log_n;
     pp.eval_log = el_log;
+    pp.accumulate = accumulate ? 1u : 0u;
     const hq sh = shift();
     for (int i = 0; i < 4; i++) pp.shift[i] = sh.v[i];
     BrElements he;
@@ -819,6 +829,22 @@ struct BlakeRoundGpuAir : GpuAir {
     return hq_mul(acc, denom_inv);
   }
 };
+
+GpuAir* new_blake_round_air(uint32_t log_n, const hq* z_alpha, const hq& claimed_sum) {
+  auto rel = [](HRel& r, hq z, hq alpha, size_t n) {
+    r.z = z;
+    hq cur = hq_make(1, 0, 0, 0);
+    r.alpha_pow.resize(n);
+    for (size_t i = 0; i < n; i++) {
+      r.alpha_pow[i] = cur;
+      cur = hq_mul(cur, alpha);
+    }
+  };
+  HBrElements el;
+  rel(el.round, z_alpha[0], z_alpha[1], BR_ROUND_FELTS);
+  for (int k = 0; k < 5; k++) rel(el.xr[k], z_alpha[2 + 2 * k], z_alpha[3 + 2 * k], 3);
+  return new BlakeRoundGpuAir(log_n, el, claimed_sum);
+}
 
 }  // namespace stwo
 

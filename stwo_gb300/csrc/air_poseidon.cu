@@ -379,6 +379,7 @@ int32_t logup_finalize_last(uint32_t* last, uint32_t log_n, Arena& arena, cudaSt
 // ------------------------------------------------------------------------------------ composition
 struct PoseidonParams {
   uint32_t trace_log, eval_log;
+  uint32_t accumulate;  // add row_res * denom_inv to the output columns instead of writing it
   uint32_t shift[4];  // claimed_sum / 2^trace_log
   LookupConsts lc;
 };
@@ -515,7 +516,9 @@ __global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
       for (int w = 1; w < PS_REPS; w++) v = m31_add(v, s_part[w][rep][lane]);
       if (r_out < n_rows) {
         uint32_t* o = rep == 0 ? o0 : rep == 1 ? o1 : rep == 2 ? o2 : o3;
-        o[r_out] = m31_mul(v, __ldg(dinv + (r_out >> pp.trace_log)));
+        v = m31_mul(v, __ldg(dinv + (r_out >> pp.trace_log)));
+        if (pp.accumulate) v = m31_add(o[r_out], v);
+        o[r_out] = v;
       }
     }
     __syncthreads();
@@ -558,7 +561,8 @@ struct PoseidonGpuAir : GpuAir {
   }
   hq shift() const { return hq_m(claimed_sum, h_inv((uint32_t)((1ull << log_n) % P))); }
   int32_t eval_composition(const std::vector<std::vector<const uint32_t*>>& cols, const uint32_t* coeffs,
-                           const uint32_t* dinv, uint32_t* const acc[4], cudaStream_t s) const override {
+                           const uint32_t* dinv, uint32_t* const acc[4], bool accumulate,
+                           cudaStream_t s) const override {
     STWO_REQUIRE(cols.size() >= 3 && cols[1].size() == PS_COLS && cols[2].size() == PS_INTERACTION_COLS,
                  "trace trees mismatch");
     // The prover hands each tree's columns on the evaluation domain as one contiguous block.
@@ -570,6 +574,7 @@ struct PoseidonGpuAir : GpuAir {
     PoseidonParams pp;
     pp.trace_log = log_n;
     pp.eval_log = log_n + PS_LOG_EXPAND;
+    pp.accumulate = accumulate ? 1u : 0u;
     hq sh = shift();
     for (int i = 0; i < 4; i++) pp.shift[i] = sh.v[i];
     for (int i = 0; i < 4; i++) pp.lc.z[i] = le.z.v[i];
@@ -670,6 +675,17 @@ struct PoseidonGpuAir : GpuAir {
     return hq_mul(acc, denom_inv);
   }
 };
+
+GpuAir* new_poseidon_air(uint32_t log_n, const hq& z, const hq& alpha, const hq& claimed_sum) {
+  HLookup le;
+  le.z = z;
+  hq cur = hq_make(1, 0, 0, 0);
+  for (int i = 0; i < PS_ST; i++) {
+    le.alpha_pow[i] = cur;
+    cur = hq_mul(cur, alpha);
+  }
+  return new PoseidonGpuAir(log_n, le, claimed_sum);
+}
 
 }  // namespace stwo
 

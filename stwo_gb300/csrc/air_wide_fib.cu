@@ -3,7 +3,7 @@
 //
 // Composition kernel: one thread per row of the evaluation domain streams the N columns
 // (coalesced), accumulates sum_k coeff_k * C_k in four 64-bit lanes (partial reduction every
-// three terms) and writes row_res * denom_inv as four coordinate columns.
+// three terms) and writes row_res * denom_inv as four coordinate columns (or adds it to them).
 #include "common.cuh"
 #include "prover.cuh"
 
@@ -18,8 +18,8 @@ __device__ __forceinline__ uint32_t fold64_(unsigned long long x) {
 
 __global__ void __launch_bounds__(256) k_wide_fib_composition(ConstColPtrs cols, uint32_t n_cols, uint32_t n_rows,
                                                               uint32_t trace_log, const uint32_t* __restrict__ coeffs,
-                                                              const uint32_t* __restrict__ dinv, uint32_t* o0,
-                                                              uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+                                                              const uint32_t* __restrict__ dinv, uint32_t accumulate,
+                                                              uint32_t* o0, uint32_t* o1, uint32_t* o2, uint32_t* o3) {
   extern __shared__ uint32_t s_coeffs[];
   for (uint32_t i = threadIdx.x; i < 4 * (n_cols - 2); i += blockDim.x) s_coeffs[i] = coeffs[i];
   __syncthreads();
@@ -49,10 +49,18 @@ __global__ void __launch_bounds__(256) k_wide_fib_composition(ConstColPtrs cols,
     b = c;
   }
   uint32_t d = __ldg(dinv + (r >> trace_log));
-  o0[r] = m31_mul(fold64_(acc0), d);
-  o1[r] = m31_mul(fold64_(acc1), d);
-  o2[r] = m31_mul(fold64_(acc2), d);
-  o3[r] = m31_mul(fold64_(acc3), d);
+  uint32_t v0 = m31_mul(fold64_(acc0), d), v1 = m31_mul(fold64_(acc1), d);
+  uint32_t v2 = m31_mul(fold64_(acc2), d), v3 = m31_mul(fold64_(acc3), d);
+  if (accumulate) {
+    v0 = m31_add(o0[r], v0);
+    v1 = m31_add(o1[r], v1);
+    v2 = m31_add(o2[r], v2);
+    v3 = m31_add(o3[r], v3);
+  }
+  o0[r] = v0;
+  o1[r] = v1;
+  o2[r] = v2;
+  o3[r] = v3;
 }
 
 // Trace of generate_trace (wide_fibonacci/mod.rs:46-68): row r starts from (a[r], b[r]).
@@ -83,14 +91,16 @@ struct WideFibGpuAir : GpuAir {
     return m;
   }
   int32_t eval_composition(const std::vector<std::vector<const uint32_t*>>& cols, const uint32_t* coeffs,
-                           const uint32_t* dinv, uint32_t* const acc[4], cudaStream_t s) const override {
+                           const uint32_t* dinv, uint32_t* const acc[4], bool accumulate,
+                           cudaStream_t s) const override {
     STWO_REQUIRE(cols.size() >= 2 && cols[1].size() == n_cols, "trace tree mismatch");
     ConstColPtrs cp;
     for (uint32_t i = 0; i < n_cols; i++) cp.p[i] = cols[1][i];
     uint32_t n_rows = 1u << (log_n + 1);
     size_t smem = (size_t)4 * (n_cols - 2) * 4;
-    k_wide_fib_composition<<<(n_rows + 255) / 256, 256, smem, s>>>(cp, n_cols, n_rows, log_n, coeffs, dinv, acc[0],
-                                                                   acc[1], acc[2], acc[3]);
+    k_wide_fib_composition<<<(n_rows + 255) / 256, 256, smem, s>>>(cp, n_cols, n_rows, log_n, coeffs, dinv,
+                                                                   accumulate ? 1u : 0u, acc[0], acc[1], acc[2],
+                                                                   acc[3]);
     note_launch();
     STWO_LAUNCH_CHECK();
     return STWO_OK;
@@ -109,6 +119,8 @@ struct WideFibGpuAir : GpuAir {
     return hq_mul(acc, denom_inv);
   }
 };
+
+GpuAir* new_wide_fib_air(uint32_t log_n, uint32_t n_cols) { return new WideFibGpuAir(log_n, n_cols); }
 
 }  // namespace stwo
 

@@ -426,36 +426,36 @@ Prover::~Prover() = default;
 // Composition polynomial (air/accumulation.rs:49-149 for one component): the AIR kernel
 // accumulates row_res * denom_inv on the evaluation domain; the four coordinate columns are then
 // interpolated and committed as a tree.
+std::vector<uint32_t> composition_denom_inv(uint32_t trace_log, uint32_t eval_log) {
+  // Denominator inverses: 1 / coset_vanishing(trace coset, eval_domain.at(i)), bit-reversed.
+  const uint32_t expand = eval_log - trace_log;
+  std::vector<uint32_t> dinv((size_t)1 << expand);
+  stwo_coset tc = coset_new(1u << (31 - (trace_log + 1)), trace_log);  // Coset::odds(trace_log)
+  hpoint init = h_index_to_point(tc.initial_index);
+  hpoint half = h_index_to_point(tc.step_size >> 1);
+  hpoint shift = h_padd({init.x, h_sub(0, init.y)}, half);
+  stwo_coset eh = canonic_half_coset(eval_log);
+  for (size_t i = 0; i < dinv.size(); i++) {
+    uint32_t idx = idx_reduce((uint64_t)eh.initial_index + (uint64_t)eh.step_size * i);  // i < half size
+    hpoint pt = h_padd(h_index_to_point(idx), shift);
+    uint32_t x = pt.x;
+    for (uint32_t k = 1; k < trace_log; k++) x = h_sub(h_add(h_mul(x, x), h_mul(x, x)), 1);
+    dinv[i] = h_inv(x);
+  }
+  std::vector<uint32_t> tmp(dinv.size());
+  for (size_t i = 0; i < dinv.size(); i++) {
+    size_t r = 0;
+    for (uint32_t b = 0; b < expand; b++) r |= ((i >> b) & 1) << (expand - 1 - b);
+    tmp[r] = dinv[i];
+  }
+  return tmp;
+}
+
 int32_t Prover::commit_composition(const GpuAir& air, hq rc) {
   uint32_t eval_log = air.max_constraint_log_degree_bound();
   uint32_t trace_log = air.log_size();
   size_t n = air.n_constraints();
-  // Denominator inverses: 1 / coset_vanishing(trace coset, eval_domain.at(i)), bit-reversed.
-  uint32_t expand = eval_log - trace_log;
-  std::vector<uint32_t> dinv((size_t)1 << expand);
-  {
-    stwo_coset tc = coset_new(1u << (31 - (trace_log + 1)), trace_log);  // Coset::odds(trace_log)
-    hpoint init = h_index_to_point(tc.initial_index);
-    hpoint half = h_index_to_point(tc.step_size >> 1);
-    hpoint shift = h_padd({init.x, h_sub(0, init.y)}, half);
-    stwo_coset eh = canonic_half_coset(eval_log);
-    for (size_t i = 0; i < dinv.size(); i++) {
-      uint32_t idx = idx_reduce((uint64_t)eh.initial_index + (uint64_t)eh.step_size * i);  // i < half size
-      hpoint pt = h_padd(h_index_to_point(idx), shift);
-      uint32_t x = pt.x;
-      for (uint32_t k = 1; k < trace_log; k++) x = h_sub(h_add(h_mul(x, x), h_mul(x, x)), 1);
-      dinv[i] = h_inv(x);
-    }
-    // bit-reverse
-    uint32_t lb = expand;
-    std::vector<uint32_t> tmp(dinv.size());
-    for (size_t i = 0; i < dinv.size(); i++) {
-      size_t r = 0;
-      for (uint32_t b = 0; b < lb; b++) r |= ((i >> b) & 1) << (lb - 1 - b);
-      tmp[r] = dinv[i];
-    }
-    dinv.swap(tmp);
-  }
+  const std::vector<uint32_t> dinv = composition_denom_inv(trace_log, eval_log);
   uint32_t* d_coeffs = arena.alloc(4 * n + dinv.size());
   if (!d_coeffs) return STWO_ERR_OOM;
   uint32_t* d_dinv = d_coeffs + 4 * n;
@@ -497,7 +497,7 @@ int32_t Prover::commit_composition(const GpuAir& air, hq rc) {
     if (!acc[k]) return STWO_ERR_OOM;
   }
   StageScope stage_cons("Constraint point-wise eval", s);
-  int32_t st = air.eval_composition(tcols, d_coeffs, d_dinv, acc, s);
+  int32_t st = air.eval_composition(tcols, d_coeffs, d_dinv, acc, false, s);
   if (st) return st;
   StageScope stage_ci("Constraints interpolation", s);
   st = fft_interpolate(tree, canonic_half_coset(eval_log), acc, 4, s);

@@ -87,13 +87,26 @@ struct GpuAir {
   // [tree][column] -> mask offsets (tree 0 = preprocessed, 1 = trace, 2 = interaction).
   virtual std::vector<std::vector<std::vector<int>>> mask_offsets() const = 0;
   // Writes row_res * denom_inv for every row of the evaluation domain into acc (4 coordinate
-  // columns); `cols[tree][col]` are the trace columns on that domain, `coeffs` the reversed powers
-  // of the random coefficient (4 words each), `dinv` the bit-reversed denominator inverses.
+  // columns), or adds it to acc's words when `accumulate` is set; `cols[tree][col]` are the trace
+  // columns on that domain, `coeffs` the reversed powers of the random coefficient (4 words each,
+  // device), `dinv` the bit-reversed denominator inverses (device).
   virtual int32_t eval_composition(const std::vector<std::vector<const uint32_t*>>& cols, const uint32_t* coeffs,
-                                   const uint32_t* dinv, uint32_t* const acc[4], cudaStream_t s) const = 0;
+                                   const uint32_t* dinv, uint32_t* const acc[4], bool accumulate,
+                                   cudaStream_t s) const = 0;
   // The constraint quotient sum at a point from the sampled mask values (PointEvaluator).
   virtual hq eval_at_point(const std::vector<std::vector<std::vector<hq>>>& mask, hq rc, hq denom_inv) const = 0;
 };
+
+// The configured AIRs, for callers outside their translation units. Relation elements are given
+// as drawn: Poseidon2 (z, alpha); the Blake2s round (z, alpha) of the round relation, then of the
+// XOR relations of widths 12, 9, 8, 7, 4.
+GpuAir* new_wide_fib_air(uint32_t log_n, uint32_t n_cols);
+GpuAir* new_poseidon_air(uint32_t log_n, const hq& z, const hq& alpha, const hq& claimed_sum);
+GpuAir* new_blake_round_air(uint32_t log_n, const hq* z_alpha, const hq& claimed_sum);
+
+// 1 / coset_vanishing(trace coset, eval_domain.at(i)) for the 2^(eval_log - trace_log) cosets,
+// bit-reversed (constraint_framework/component.rs:323-328).
+std::vector<uint32_t> composition_denom_inv(uint32_t trace_log, uint32_t eval_log);
 
 struct Tree;
 
