@@ -254,8 +254,12 @@ __device__ __forceinline__ void fft_rounds_inv(const FftPass& p, uint32_t* sm, u
   }
 }
 
+// At least 5 resident blocks per SM: the 2^12-word tiles of 256 threads otherwise take 63-80
+// registers and 4 blocks, and the kernel is bound by issue latency with too few warps (0.64
+// instructions issued per cycle per scheduler). Capping at 48 registers (a 12-byte spill) gives
+// 40 warps per SM and 6-7% shorter FFT passes on 1,296 columns of 2^16-2^18 words.
 template <bool INV, int C, int NL>
-__global__ void __launch_bounds__(1 << (C + NL - 4)) k_fft_tile(FftPass p, ConstColPtrs src, ColPtrs dst) {
+__global__ void __launch_bounds__(1 << (C + NL - 4), 5) k_fft_tile(FftPass p, ConstColPtrs src, ColPtrs dst) {
   constexpr int T = C + NL;
   constexpr int THREADS = 1 << (T - 4);
   constexpr int PADW = THREADS + THREADS / 32;  // padded stride of consecutive thread rows
