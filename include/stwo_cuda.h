@@ -141,6 +141,15 @@ stwo_status stwo_merkle_commit_layer(uint32_t log_size, const uint32_t* d_prev_l
                                      const uint32_t* const* d_cols, uint32_t n_cols, uint32_t* d_out,
                                      void* stream);
 
+/* MerkleOps<Poseidon252MerkleHasher>::commit_on_layer (crates/prover/src/core/vcs/ops.rs:41-45; hasher
+ * crates/prover/src/core/vcs/poseidon252_merkle.rs:17-45, CPU backend backend/cpu/poseidon252.rs:9-25),
+ * the Merkle half of BackendForChannel<Poseidon252MerkleChannel> (backend/simd/mod.rs:34-35). Hashes
+ * are FieldElement252 values, each 8 little-endian u32 limbs of the canonical integer below
+ * p = 2^251 + 17 * 2^192 + 1. `d_prev_layer` is NULL for the leaf layer, else 2^(log_size+1) hashes. */
+stwo_status stwo_merkle_commit_layer_poseidon252(uint32_t log_size, const uint32_t* d_prev_layer,
+                                                 const uint32_t* const* d_cols, uint32_t n_cols, uint32_t* d_out,
+                                                 void* stream);
+
 /* ------------------------------------------------------------------ FriOps */
 /* FriOps::fold_line (crates/prover/src/core/fri.rs:103-107): evaluation on the line domain
  * `line_domain` (2^log_size values) folded into 2^(log_size-1) values. */
@@ -230,6 +239,12 @@ stwo_status stwo_gkr_prove_batch(uint32_t n_instances, const uint32_t* h_kinds, 
  * backend/simd/grind.rs:21-63): the smallest nonce whose raw Blake2s compression of
  * (digest, [nonce_lo, nonce_hi, 0...]) has >= pow_bits trailing zeros in word 0. */
 stwo_status stwo_grind_blake2s(const uint32_t h_digest[8], uint32_t pow_bits, uint64_t* h_nonce, void* stream);
+
+/* GrindOps<Poseidon252Channel>::grind (crates/prover/src/core/backend/simd/grind.rs:65-79): the smallest
+ * nonce for which poseidon_hash(digest, nonce) has >= pow_bits trailing zeros as
+ * Poseidon252Channel::trailing_zeros counts them (channel/poseidon252.rs:59-62). h_digest is the channel
+ * digest as 8 little-endian u32 limbs; pow_bits <= 32. */
+stwo_status stwo_grind_poseidon252(const uint32_t h_digest[8], uint32_t pow_bits, uint64_t* h_nonce, void* stream);
 
 /* ------------------------------------------------------------------ proving */
 /* PcsConfig { pow_bits, fri_config: FriConfig { log_last_layer_degree_bound, log_blowup_factor,

@@ -627,3 +627,69 @@ int oracle_eval_constraints(uint32_t air_id, uint32_t log_n, uint32_t n_cols, co
 }
 
 }  // extern "C"
+
+#include "poseidon252.h"
+
+extern "C" {
+
+// Poseidon252: felts cross this interface as 8 little-endian u32 limbs of the canonical integer.
+void oracle_p252_hash(const uint32_t x[8], const uint32_t y[8], uint32_t out[8]) {
+  f252_to_words(poseidon_hash(f252_from_words(x), f252_from_words(y)), out);
+}
+void oracle_p252_hash_many(const uint32_t* v, size_t n, uint32_t out[8]) {
+  std::vector<F252> in;
+  for (size_t i = 0; i < n; i++) in.push_back(f252_from_words(v + 8 * i));
+  f252_to_words(poseidon_hash_many(in), out);
+}
+void oracle_p252_hash_node(const uint32_t* left, const uint32_t* right, const uint32_t* vals, size_t n,
+                           uint32_t out[8]) {
+  F252 l, r;
+  if (left) {
+    l = f252_from_words(left);
+    r = f252_from_words(right);
+  }
+  f252_to_words(p252_hash_node(left ? &l : nullptr, left ? &r : nullptr, vals, n), out);
+}
+// MerkleOps<Poseidon252MerkleHasher>::commit_on_layer (backend/cpu/poseidon252.rs:9-25).
+void oracle_p252_commit_on_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols,
+                                 uint32_t n_cols, uint32_t* out) {
+  const size_t n = (size_t)1 << log_size;
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)n; i++) {
+    std::vector<uint32_t> vals(n_cols);
+    for (uint32_t c = 0; c < n_cols; c++) vals[c] = cols[c][i];
+    F252 l, r;
+    if (prev) {
+      l = f252_from_words(prev + 16 * i);
+      r = f252_from_words(prev + 16 * i + 8);
+    }
+    f252_to_words(p252_hash_node(prev ? &l : nullptr, prev ? &r : nullptr, vals.data(), n_cols), out + 8 * i);
+  }
+}
+uint64_t oracle_p252_grind(const uint32_t digest[8], uint32_t pow_bits) {
+  Poseidon252Channel ch;
+  ch.digest = f252_from_words(digest);
+  return p252_grind(ch, pow_bits);
+}
+uint32_t oracle_p252_trailing_zeros(const uint32_t digest[8]) {
+  Poseidon252Channel ch;
+  ch.digest = f252_from_words(digest);
+  return ch.trailing_zeros();
+}
+// A channel script: from `digest`, mix `n_felts` QM31 values (if any), then draw `n_draw` felts;
+// writes the draws and the final digest.
+void oracle_p252_channel(const uint32_t digest[8], const uint32_t* felts, size_t n_felts, size_t n_draw,
+                         uint32_t* draws, uint32_t digest_out[8]) {
+  Poseidon252Channel ch;
+  ch.digest = f252_from_words(digest);
+  if (n_felts) {
+    std::vector<QM31> f;
+    for (size_t i = 0; i < n_felts; i++) f.push_back(q_of(felts + 4 * i));
+    ch.mix_felts(f);
+  }
+  auto d = ch.draw_felts(n_draw);
+  for (size_t i = 0; i < d.size(); i++) q_to(d[i], draws + 4 * i);
+  f252_to_words(ch.digest, digest_out);
+}
+
+}  // extern "C"

@@ -394,3 +394,65 @@ def eval_constraints(air, log_n, n_cols, claimed_sum, elements, cols, coeffs, ac
     if st != 0:
         raise ValueError("oracle_eval_constraints: bad input")
     return out
+
+
+# ---------------------------------------------------------------- Poseidon252
+def _w8(x: int):
+    return np.array([(x >> (32 * i)) & 0xFFFFFFFF for i in range(8)], np.uint32)
+
+
+def _int8(w) -> int:
+    return sum(int(v) << (32 * i) for i, v in enumerate(w))
+
+
+def p252_hash(x: int, y: int) -> int:
+    out = np.zeros(8, np.uint32)
+    lib().oracle_p252_hash(_p(_w8(x)), _p(_w8(y)), _p(out))
+    return _int8(out)
+
+
+def p252_hash_many(vals) -> int:
+    v = np.concatenate([_w8(x) for x in vals]) if len(vals) else np.zeros(8, np.uint32)
+    out = np.zeros(8, np.uint32)
+    lib().oracle_p252_hash_many(_p(v), C.c_size_t(len(vals)), _p(out))
+    return _int8(out)
+
+
+def p252_hash_node(children, vals) -> int:
+    out = np.zeros(8, np.uint32)
+    v = _u32(vals) if len(vals) else np.zeros(1, np.uint32)
+    if children:
+        l, r = _w8(children[0]), _w8(children[1])
+        lib().oracle_p252_hash_node(_p(l), _p(r), _p(v), C.c_size_t(len(vals)), _p(out))
+    else:
+        lib().oracle_p252_hash_node(None, None, _p(v), C.c_size_t(len(vals)), _p(out))
+    return _int8(out)
+
+
+def p252_commit_on_layer(log_size, prev, cols):
+    """prev: None or 2^(log+1) x 8 words; returns 2^log x 8 words."""
+    cols = [_u32(c) for c in cols]
+    out = np.zeros((1 << log_size) * 8, np.uint32)
+    pv = _u32(prev).reshape(-1) if prev is not None else None
+    lib().oracle_p252_commit_on_layer(C.c_uint32(log_size), _p(pv) if pv is not None else None, _ptr_table(cols),
+                                      C.c_uint32(len(cols)), _p(out))
+    return out.reshape(-1, 8)
+
+
+def p252_grind(digest: int, pow_bits: int) -> int:
+    f = lib().oracle_p252_grind
+    f.restype = C.c_uint64
+    return int(f(_p(_w8(digest)), C.c_uint32(pow_bits)))
+
+
+def p252_trailing_zeros(digest: int) -> int:
+    return int(lib().oracle_p252_trailing_zeros(_p(_w8(digest))))
+
+
+def p252_channel(digest: int, felts, n_draw):
+    """Mixes `felts` (QM31 tuples) into a channel at `digest`, then draws n_draw felts."""
+    f = _u32(np.asarray(felts, np.uint32).reshape(-1)) if len(felts) else np.zeros(4, np.uint32)
+    draws = np.zeros(max(1, n_draw) * 4, np.uint32)
+    out = np.zeros(8, np.uint32)
+    lib().oracle_p252_channel(_p(_w8(digest)), _p(f), C.c_size_t(len(felts)), C.c_size_t(n_draw), _p(draws), _p(out))
+    return [tuple(int(x) for x in draws[4 * i:4 * i + 4]) for i in range(n_draw)], _int8(out)

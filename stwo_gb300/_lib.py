@@ -121,6 +121,8 @@ SIGNATURES = {
     "stwo_server_destroy": (C.c_int32, [VP]),
     "stwo_job_hbm_bytes": (C.c_size_t, [C.POINTER(ProofJob)]),
     "stwo_prove_batch": (C.c_int32, [C.POINTER(ProofJob), U32, U32, C.c_size_t, C.POINTER(ProofResult)]),
+    "stwo_merkle_commit_layer_poseidon252": (C.c_int32, [U32, VP, PVP, U32, VP, VP]),
+    "stwo_grind_poseidon252": (C.c_int32, [C.POINTER(C.c_uint32), U32, C.POINTER(C.c_uint64), VP]),
     "stwo_component_info": (C.c_int32, [C.POINTER(Component), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                         C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "stwo_eval_constraints": (C.c_int32, [C.POINTER(Component), PVP, U32, C.POINTER(QM31), U32, PVP, VP]),

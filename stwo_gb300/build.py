@@ -47,6 +47,9 @@ def _run(cmd):
 def build_backend(force: bool = False, verbose: bool = False) -> str:
     """Compile and link libstwo_gb300.so; returns its path."""
     os.makedirs(BUILD, exist_ok=True)
+    # The Poseidon252 round-constant table is generated from the hash's published constant
+    # derivation (rewritten only when it differs).
+    _run([sys.executable, os.path.join(CSRC, "gen_poseidon252_constants.py")])
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
     nvcc = _nvcc()
