@@ -5,7 +5,9 @@
 // a hash are raw u32 words (backend/simd/blake2s.rs:124-138), so every routine here returns
 // the canonical representative: 0 is never stored as P.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cstdint>
+#endif
 
 namespace stwo {
 
