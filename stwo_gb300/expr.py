@@ -84,6 +84,10 @@ def q_inv(a: Q) -> Q:
 
 # ------------------------------------------------------------------ nodes
 _INTERN: Dict[tuple, "Expr"] = {}
+# Nodes are immutable and interned, so simplification is memoised by node: expressions with
+# heavy sharing (a Poseidon2 partial round reuses the running sum in every lane) are DAGs whose
+# trees are exponentially large.
+_SIMPLIFIED: Dict[int, "Expr"] = {}
 
 
 class Expr:
@@ -214,6 +218,12 @@ class BaseExpr(Expr):
 
     # ---- simplify (simplify.rs:86-102)
     def simplify(self) -> "BaseExpr":
+        done = _SIMPLIFIED.get(self.uid)
+        if done is None:
+            done = _SIMPLIFIED[self.uid] = self._simplify()
+        return done
+
+    def _simplify(self) -> "BaseExpr":
         s = _simplify_arith(self)
         if s.kind == "inv":
             a = s.args[0].simplify()
@@ -251,8 +261,14 @@ class BaseExpr(Expr):
             return f"1 / ({a[0].format_expr()})"
         raise AssertionError(k)
 
-    # ---- degree (degree.rs:38-84)
+    # ---- degree (degree.rs:38-84), memoised per NamedExprs
     def degree_bound(self, named: "NamedExprs") -> int:
+        d = named.memo.get(self.uid)
+        if d is None:
+            d = named.memo[self.uid] = self._degree(named)
+        return d
+
+    def _degree(self, named: "NamedExprs") -> int:
         k = self.kind
         if k == "col":
             return 1
@@ -335,6 +351,12 @@ class ExtExpr(Expr):
 
     # ---- simplify (simplify.rs:104-140)
     def simplify(self) -> "ExtExpr":
+        done = _SIMPLIFIED.get(self.uid)
+        if done is None:
+            done = _SIMPLIFIED[self.uid] = self._simplify()
+        return done
+
+    def _simplify(self) -> "ExtExpr":
         s = _simplify_arith(self)
         if s.kind == "secure_col":
             parts = [p.simplify() for p in s.args]
@@ -372,8 +394,14 @@ class ExtExpr(Expr):
             return f"-({a[0].format_expr()})"
         raise AssertionError(k)
 
-    # ---- degree (degree.rs:86-104)
+    # ---- degree (degree.rs:86-104), memoised per NamedExprs
     def degree_bound(self, named: "NamedExprs") -> int:
+        d = named.memo.get(self.uid)
+        if d is None:
+            d = named.memo[self.uid] = self._degree(named)
+        return d
+
+    def _degree(self, named: "NamedExprs") -> int:
         k = self.kind
         if k == "secure_col":
             return max(p.degree_bound(named) for p in self.args)
@@ -492,8 +520,16 @@ class NamedExprs:
 
     def __init__(self, exprs: Dict[str, BaseExpr], ext_exprs: Dict[str, ExtExpr]):
         self.exprs, self.ext_exprs = exprs, ext_exprs
+        self.memo: Dict[int, int] = {}
+        self.name_memo: Dict[str, int] = {}
 
     def degree_bound(self, name: str) -> int:
+        d = self.name_memo.get(name)
+        if d is None:
+            d = self.name_memo[name] = self._named_degree(name)
+        return d
+
+    def _named_degree(self, name: str) -> int:
         if name in self.exprs:
             return self.exprs[name].degree_bound(self)
         if name in self.ext_exprs:
