@@ -382,6 +382,45 @@ stwo_status stwo_eval_constraints(const stwo_component* component, const uint32_
                                   const stwo_qm31* h_coeff_powers, uint32_t n_coeff_powers,
                                   uint32_t* const d_accum[4], void* stream);
 
+/* ---- Generated constraint kernels (constraint framework's expr module,
+ * crates/prover/src/constraint_framework/expr/evaluator.rs:54-227, evaluated on the domain as
+ * SimdDomainEvaluator does, constraint_framework/simd_domain.rs:24-114). A component written
+ * against the framework is recorded as expressions and emitted as CUDA source defining
+ * `extern "C" __global__ void stwo_generated_constraints(stwo::GenArgs)` (the argument block of
+ * stwo_gb300/csrc/codegen_rt.cuh, which the source may include together with field.cuh). */
+typedef struct stwo_codegen_component_s* stwo_codegen_component;
+
+/* Compiles kernel_source with NVRTC for sm_103a (no device needed) and, when load_now is set,
+ * loads it on the current device (otherwise the first evaluation loads it). n_cols, n_params and
+ * n_constraints are the component's column count (all interactions), parameter count and
+ * constraint count, checked on every call. A source that does not compile returns
+ * STWO_ERR_INVALID_ARG with the compiler log in stwo_last_error(). */
+stwo_status stwo_codegen_compile(const char* kernel_source, uint32_t n_cols, uint32_t n_params,
+                                 uint32_t n_constraints, int load_now, stwo_codegen_component* out);
+/* Size of the compiled cubin (diagnostic). */
+stwo_status stwo_codegen_cubin_size(stwo_codegen_component component, size_t* h_size);
+stwo_status stwo_codegen_destroy(stwo_codegen_component component);
+
+/* ComponentProver::evaluate_constraint_quotients_on_domain (crates/prover/src/core/air/mod.rs:59-62;
+ * SimdBackend implementation crates/prover/src/constraint_framework/component.rs:278-416) for a
+ * generated component, after its extension step:
+ *   d_cols          the columns on the evaluation domain (bit-reversed), interaction 0 (preprocessed,
+ *                   in the order the component requests them), then the trace, then the interaction
+ *                   trace, each in mask order;
+ *   h_params        the values of the component's formal parameters, in the generator's order
+ *                   (relation elements, claimed_sum, column_size = 2^trace_log_size, ...), 4 words
+ *                   each (a base-field parameter in word 0);
+ *   h_coeff_powers  the n_constraints powers DomainEvaluationAccumulator::columns hands the
+ *                   component (crates/prover/src/core/air/accumulation.rs:71-93), in that order;
+ *   d_accum         the accumulation column of size 2^eval_log_size: every row adds
+ *                   row_res / coset_vanishing(trace coset, row point).
+ * Stream ordered. */
+stwo_status stwo_eval_constraints_codegen(stwo_codegen_component component, uint32_t trace_log_size,
+                                          uint32_t eval_log_size, const uint32_t* const* d_cols, uint32_t n_cols,
+                                          const stwo_qm31* h_params, uint32_t n_params,
+                                          const stwo_qm31* h_coeff_powers, uint32_t n_coeff_powers,
+                                          uint32_t* const d_accum[4], void* stream);
+
 #ifdef __cplusplus
 }
 #endif

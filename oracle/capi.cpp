@@ -473,6 +473,7 @@ void oracle_channel_draw_felts(size_t n, uint32_t* out) {
 }  // extern "C"
 
 #include "air_blake_round.h"
+#include "air_examples.h"
 
 extern "C" {
 
@@ -548,7 +549,8 @@ int oracle_verify_blake_round(uint32_t log_n, const uint32_t claimed_sum[4], con
 // point r) on CanonicCoset(eval log).circle_domain(). `cols` lists the component's columns on that
 // domain tree by tree (trace, then interaction); `coeffs` are the accumulator's powers in the order
 // it hands them (reversed here, as the component does). air: 0 wide-Fibonacci, 1 Poseidon2,
-// 2 Blake2s round; `elements` as drawn (z, alpha pairs). Returns 0, or 1 on bad input.
+// 2 Blake2s round, 3 Plonk, 4 / 5 state-machine transition of coordinate 0 / 1; `elements` as
+// drawn (z, alpha pairs). Returns 0, or 1 on bad input.
 int oracle_eval_constraints(uint32_t air_id, uint32_t log_n, uint32_t n_cols, const uint32_t claimed_sum[4],
                             const uint32_t* elements, uint32_t n_elements, const uint32_t* const* cols,
                             uint32_t n_cols_total, const uint32_t* coeffs, uint32_t n_coeffs, uint32_t* const acc[4]) {
@@ -589,6 +591,19 @@ int oracle_eval_constraints(uint32_t air_id, uint32_t log_n, uint32_t n_cols, co
       set(el.xor_.xor4, 5, 3);
       air.reset(new BlakeRoundAir(log_n, el, q_of(claimed_sum)));
       tree_cols = {0, BR_TRACE_COLS, 4 * BR_INTERACTION_SECURE};
+    } else if (air_id == 3 || air_id == 4 || air_id == 5) {
+      if (n_elements != 2) return 1;
+      Relation<2> r;
+      r.z = q_of(elements);
+      r.alpha = q_of(elements + 4);
+      rel_powers(r.alpha, r.alpha_powers, 2);
+      if (air_id == 3) {
+        air.reset(new PlonkAir(log_n, r, q_of(claimed_sum)));
+        tree_cols = {4, 4, 8};
+      } else {
+        air.reset(new StateTransitionAir(air_id - 4, log_n, r, q_of(claimed_sum)));
+        tree_cols = {0, 2, 4};
+      }
     } else {
       return 1;
     }

@@ -44,12 +44,30 @@ def _run(cmd):
     return r
 
 
+def _write_codegen_headers() -> None:
+    """The two headers that generated constraint kernels compile against (NVRTC has no file
+    system view of the package), as C++ raw strings in _build/codegen_headers.inc; rewritten only
+    when they change."""
+    out = os.path.join(BUILD, "codegen_headers.inc")
+    parts = []
+    for var, name in (("kFieldCuh", "field.cuh"), ("kCodegenRtCuh", "codegen_rt.cuh")):
+        with open(os.path.join(CSRC, name)) as f:
+            text = f.read()
+        assert ")STWORT" not in text
+        parts.append(f'static const char {var}[] = R"STWORT({text})STWORT";\n')
+    body = "// Generated by stwo_gb300/build.py from csrc/field.cuh and csrc/codegen_rt.cuh.\n" + "".join(parts)
+    if not os.path.exists(out) or open(out).read() != body:
+        with open(out, "w") as f:
+            f.write(body)
+
+
 def build_backend(force: bool = False, verbose: bool = False) -> str:
     """Compile and link libstwo_gb300.so; returns its path."""
     os.makedirs(BUILD, exist_ok=True)
     # The Poseidon252 round-constant table is generated from the hash's published constant
     # derivation (rewritten only when it differs).
     _run([sys.executable, os.path.join(CSRC, "gen_poseidon252_constants.py")])
+    _write_codegen_headers()
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
     nvcc = _nvcc()
@@ -60,7 +78,7 @@ def build_backend(force: bool = False, verbose: bool = False) -> str:
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if force or not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr_time):
-            jobs.append([nvcc, *NVCC_FLAGS, "-c", src, "-o", obj])
+            jobs.append([nvcc, *NVCC_FLAGS, "-I", BUILD, "-c", src, "-o", obj])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for r in ex.map(_run, jobs):
@@ -68,7 +86,7 @@ def build_backend(force: bool = False, verbose: bool = False) -> str:
                     sys.stderr.write(r.stdout + r.stderr)
     if force or jobs or not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
         tmp = LIB + ".tmp"
-        _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+        _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lnvrtc"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -1,0 +1,439 @@
+"""CUDA code generation for constraint evaluation on the domain.
+
+An AIR written against the constraint framework (a FrameworkEval: `evaluate(eval)` over the
+EvalAtRow surface) is recorded once with `expr.ExprEvaluator`, then emitted as one CUDA kernel
+that evaluates every constraint at every row of the evaluation domain and adds
+row_res * denom_inv to the accumulation column — what the reference does per row with
+SimdDomainEvaluator inside FrameworkComponent::evaluate_constraint_quotients_on_domain
+(crates/prover/src/constraint_framework/component.rs:278-416, simd_domain.rs:24-114). The
+library compiles the source with NVRTC (stwo_codegen_compile) and launches it through
+stwo_eval_constraints_codegen.
+
+Kernel shape (one thread per row, a grid-stride loop):
+  * The column table and the random-coefficient powers are staged in shared memory.
+  * Every distinct subexpression is one SSA value (nodes are interned, so sharing is exact);
+    values that depend on no column (parameters, their inverses and products) are computed once
+    per thread before the row loop.
+  * Extension values that are embedded base values stay 32-bit words: `ext * base` is four M31
+    products, not a QM31 product.
+  * Base-field constraints accumulate p_i * c_i into four 64-bit lanes, folded every third
+    product; extension constraints take a QM31 product.
+  * Mask offsets other than 0 read the row given by offset_bit_reversed_circle_domain_index
+    (core/utils.rs:74-90), computed once per offset.
+Any order of these exact field operations gives the same words, so the column equals the
+reference's row by row.
+
+`GeneratedComponent.eval_at_point` evaluates the same expressions at an out-of-domain point on
+the host (PointEvaluator, constraint_framework/point.rs:15-70).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+from typing import Dict, List, Sequence, Tuple
+
+from . import expr as X
+from .expr import BaseExpr, Expr, ExprEvaluator
+
+SMEM_BUDGET = 40 * 1024  # shared memory for the column table and the powers, bytes
+
+
+class _Gen:
+    def __init__(self, ev: ExprEvaluator):
+        self.ev = ev
+        self.col_base = [0]
+        for m in ev.mask[:-1]:
+            self.col_base.append(self.col_base[-1] + len(m))
+        self.n_cols = sum(len(m) for m in ev.mask)
+        self.params: List[Tuple[str, bool]] = []  # external parameters: (name, is_ext)
+        self.param_index: Dict[str, int] = {}
+        self.pre: List[str] = []
+        self.tables: List[str] = []
+        self.offsets: Dict[int, str] = {0: "row"}
+        self.uniform_memo: Dict[int, Tuple[str, str, bool]] = {}
+        self.resolved: Dict[int, Expr] = {}
+
+    # ---- intermediates and preprocessed columns substituted: a DAG over columns, constants and
+    # external parameters only.
+    def resolve(self, root: Expr) -> Expr:
+        ev = self.ev
+        stack = [root]
+        while stack:
+            n = stack[-1]
+            if n.uid in self.resolved:
+                stack.pop()
+                continue
+            if n.kind == "param":
+                name = n.val
+                if name in ev.intermediates or name in ev.ext_intermediates:
+                    target = ev.intermediate(name).simplify()
+                elif name in ev.preprocessed:
+                    target = BaseExpr.col(0, -1, 0, ev.preprocessed.index(name))
+                else:
+                    target = n
+                if target is n:
+                    self.resolved[n.uid] = n
+                    stack.pop()
+                elif target.uid in self.resolved:
+                    self.resolved[n.uid] = self.resolved[target.uid]
+                    stack.pop()
+                else:
+                    stack.append(target)
+                continue
+            pending = [a for a in n.args if a.uid not in self.resolved]
+            if pending:
+                stack.extend(pending)
+                continue
+            stack.pop()
+            args = tuple(self.resolved[a.uid] for a in n.args)
+            self.resolved[n.uid] = n if all(x is y for x, y in zip(args, n.args)) else type(n)(n.kind, args, n.val)
+        return self.resolved[root.uid]
+
+    @staticmethod
+    def _topo(roots: Sequence[Expr]) -> List[Expr]:
+        """Every node reachable from roots, children before parents, roots in order."""
+        seen, out = set(), []
+        for r in roots:
+            stack = [(r, False)]
+            while stack:
+                n, done = stack.pop()
+                if done:
+                    out.append(n)
+                    continue
+                if n.uid in seen:
+                    continue
+                seen.add(n.uid)
+                stack.append((n, True))
+                for a in reversed(n.args):
+                    if a.uid not in seen:
+                        stack.append((a, False))
+        return out
+
+    # ---- grouping: constraints that share a computed (non-uniform) node belong to one group;
+    # groups with the same shape up to column renaming form a class, emitted once as a loop.
+    def _groups(self, roots: List[Expr]) -> List[List[int]]:
+        nodes = self._topo(roots)
+        self.uniform = {}
+        for n in nodes:
+            if n.kind == "col":
+                self.uniform[n.uid] = False
+            elif n.kind in ("const", "param"):
+                self.uniform[n.uid] = True
+            else:
+                self.uniform[n.uid] = all(self.uniform[a.uid] for a in n.args)
+        parent: Dict[int, int] = {}
+
+        def find(x):
+            while parent.get(x, x) != x:
+                parent[x] = parent.get(parent[x], parent[x])
+                x = parent[x]
+            return x
+
+        for n in nodes:
+            if n.args and not self.uniform[n.uid]:
+                for a in n.args:
+                    if a.args and not self.uniform[a.uid]:
+                        ra, rb = find(a.uid), find(n.uid)
+                        if ra != rb:
+                            parent[ra] = rb
+        by: Dict[int, List[int]] = {}
+        for i, r in enumerate(roots):
+            by.setdefault(find(r.uid), []).append(i)
+        return sorted(by.values(), key=lambda g: g[0])
+
+    def _signature(self, roots: List[Expr], idx: List[int]):
+        """Canonical shape of a group: nodes in emission order with columns numbered by first
+        use; returns (signature, column table indices in slot order)."""
+        canon: Dict[int, int] = {}
+        slots: Dict[int, int] = {}
+        toks = []
+        for n in self._topo([roots[i] for i in idx]):
+            if self.uniform[n.uid] and n.args:
+                tok = ("u", n.uid)
+            elif n.kind == "col":
+                c = n.val
+                t = self.col_base[c.interaction] + c.local
+                tok = ("c", slots.setdefault(t, len(slots)), c.offset)
+            elif n.kind in ("const", "param"):
+                tok = (n.kind, n.is_ext, n.val)
+            else:
+                tok = (n.kind, n.is_ext) + tuple(canon[a.uid] for a in n.args)
+            canon[n.uid] = len(toks)
+            toks.append(tok)
+        sig = (tuple(toks), tuple(canon[roots[i].uid] for i in idx))
+        return sig, list(slots)
+
+    # ---- emission
+    def _param(self, name: str, is_ext: bool) -> Tuple[str, str, bool]:
+        k = self.param_index.get(name)
+        if k is None:
+            k = self.param_index[name] = len(self.params)
+            self.params.append((name, is_ext))
+            if is_ext:
+                self.pre.append(f"const qm31 p{k} = gen_param_q(a.params, {k});")
+            else:
+                self.pre.append(f"const uint32_t p{k} = __ldg(a.params + {4 * k});")
+        return (f"p{k}", "q" if is_ext else "b", True)
+
+    def _offset(self, off: int) -> str:
+        rv = self.offsets.get(off)
+        if rv is None:
+            rv = self.offsets[off] = f"r_{'m' if off < 0 else 'p'}{abs(off)}"
+        return rv
+
+    def _value(self, root: Expr, memo: Dict[int, Tuple[str, str, bool]], out: List[str], col_ref) -> Tuple[str, str, bool]:
+        for n in self._topo([root]):
+            if n.uid in memo or n.uid in self.uniform_memo:
+                continue
+            uni = self.uniform[n.uid] if n.uid in self.uniform else False
+            m = self.uniform_memo if uni else memo
+            m[n.uid] = self._emit(n, lambda u: self.uniform_memo.get(u) or memo[u], out, col_ref)
+        return self.uniform_memo.get(root.uid) or memo[root.uid]
+
+    def _stmt(self, uniform: bool, ty: str, code: str, uid: int, out: List[str]) -> Tuple[str, str, bool]:
+        name = f"t{uid}"
+        decl = "uint32_t" if ty == "b" else "qm31"
+        (self.pre if uniform else out).append(f"const {decl} {name} = {code};")
+        return (name, ty, uniform)
+
+    def _emit(self, n: Expr, get, out: List[str], col_ref) -> Tuple[str, str, bool]:
+        k = n.kind
+        if k == "col":
+            c = n.val
+            name = f"c{n.uid}"
+            out.append(f"const uint32_t {name} = __ldg({col_ref(self.col_base[c.interaction] + c.local)} + "
+                       f"{self._offset(c.offset)});")
+            return (name, "b", False)
+        if k == "const":
+            if not n.is_ext:
+                return (f"{n.val}u", "b", True)
+            v = n.val
+            if v[1] == v[2] == v[3] == 0:
+                return (f"{v[0]}u", "b", True)
+            return self._stmt(True, "q", f"qm31_from_u32({v[0]}u, {v[1]}u, {v[2]}u, {v[3]}u)", n.uid, out)
+        if k == "param":
+            return self._param(n.val, n.is_ext)
+        args = [get(a.uid) for a in n.args]
+        uni = all(a[2] for a in args)
+        if k == "secure_col":
+            zero = BaseExpr.zero()
+            if all(a is zero for a in n.args[1:]):
+                return args[0]
+            return self._stmt(uni, "q", "qm31_from_u32({}, {}, {}, {})".format(*(a[0] for a in args)), n.uid, out)
+        if k == "neg":
+            (x, t, _), = args
+            return self._stmt(uni, t, f"m31_neg({x})" if t == "b" else f"gen_q_neg({x})", n.uid, out)
+        if k == "inv":
+            (x, t, _), = args
+            return self._stmt(uni, "b", f"m31_inv({x})", n.uid, out)
+        (x, tx, _), (y, ty, _) = args
+        if k == "add":
+            if tx == ty == "b":
+                return self._stmt(uni, "b", f"m31_add({x}, {y})", n.uid, out)
+            if tx == "q" and ty == "q":
+                return self._stmt(uni, "q", f"qm31_add({x}, {y})", n.uid, out)
+            q, b = (x, y) if tx == "q" else (y, x)
+            return self._stmt(uni, "q", f"gen_q_add_m31({q}, {b})", n.uid, out)
+        if k == "sub":
+            if tx == ty == "b":
+                return self._stmt(uni, "b", f"m31_sub({x}, {y})", n.uid, out)
+            if tx == "q" and ty == "q":
+                return self._stmt(uni, "q", f"qm31_sub({x}, {y})", n.uid, out)
+            if tx == "q":
+                return self._stmt(uni, "q", f"gen_q_sub_m31({x}, {y})", n.uid, out)
+            return self._stmt(uni, "q", f"gen_m31_sub_q({x}, {y})", n.uid, out)
+        if k == "mul":
+            if tx == ty == "b":
+                return self._stmt(uni, "b", f"m31_mul({x}, {y})", n.uid, out)
+            if tx == "q" and ty == "q":
+                return self._stmt(uni, "q", f"qm31_mul({x}, {y})", n.uid, out)
+            q, b = (x, y) if tx == "q" else (y, x)
+            return self._stmt(uni, "q", f"qm31_mul_m31({q}, {b})", n.uid, out)
+        raise AssertionError(k)
+
+    def _accumulate(self, roots, idx, memo, out, col_ref, pw_ref) -> None:
+        n_base = 0
+        for j, i in enumerate(idx):
+            code, ty, _ = self._value(roots[i], memo, out, col_ref)
+            if ty == "b":
+                out.append(f"gen_acc_base(acc, {pw_ref(j, i)}, {code});")
+                n_base += 1
+                if n_base % 3 == 0:
+                    out.append("gen_fold(acc);")
+            else:
+                out.append(f"qacc = qm31_add(qacc, qm31_mul(gen_q_of_u4({pw_ref(j, i)}), {code}));")
+        if n_base % 3:
+            out.append("gen_fold(acc);")
+
+    # ---- the kernel
+    def source(self) -> str:
+        ev = self.ev
+        roots = [self.resolve(c.simplify()) for c in ev.constraints]
+        n_cons = len(roots)
+        smem_pw = n_cons * 16 + self.n_cols * 8 <= SMEM_BUDGET
+        pw_at = (lambda e: f"s_pw[{e}]") if smem_pw else (lambda e: f"gen_ldg_u4(a.powers, {e})")
+        classes: Dict[tuple, List[Tuple[List[int], List[int]]]] = {}
+        order = []
+        for g in self._groups(roots):
+            sig, slots = self._signature(roots, g)
+            if sig not in classes:
+                classes[sig] = []
+                order.append(sig)
+            classes[sig].append((g, slots))
+        body: List[str] = []
+        outer: Dict[int, Tuple[str, str, bool]] = {}  # values in the row loop's own scope
+        for ci, sig in enumerate(order):
+            members = classes[sig]
+            if len(members) == 1:
+                g, slots = members[0]
+                self._accumulate(roots, g, outer, body, lambda t: f"s_cols[{t}]", lambda j, i: pw_at(i))
+                continue
+            # One loop over the members: column slots and constraint indices from tables.
+            m, ns, nc = len(members), len(members[0][1]), len(members[0][0])
+            cmap = ", ".join(str(t) for g, slots in members for t in slots)
+            pmap = ", ".join(str(i) for g, slots in members for i in g)
+            ctype = "uint16_t" if self.n_cols < 65536 else "uint32_t"
+            ptype = "uint16_t" if n_cons < 65536 else "uint32_t"
+            self.tables.append(f"__constant__ {ctype} g_cmap{ci}[{m * ns}] = {{{cmap}}};")
+            self.tables.append(f"__constant__ {ptype} g_pmap{ci}[{m * nc}] = {{{pmap}}};")
+            g0, slots0 = members[0]
+            slot_of = {t: s for s, t in enumerate(slots0)}
+            inner: List[str] = []
+            self._accumulate(roots, g0, {}, inner, lambda t: f"s_cols[g_cmap{ci}[g * {ns} + {slot_of[t]}]]",
+                             lambda j, i: pw_at(f"g_pmap{ci}[g * {nc} + {j}]"))
+            body.append("#pragma unroll 1")
+            body.append(f"for (int g = 0; g < {m}; g++) {{")
+            body += ["  " + x for x in inner]
+            body.append("}")
+        nc = max(self.n_cols, 1)
+        lines = [
+            "// Generated from a constraint-framework component by stwo_gb300/codegen.py.",
+            '#include "codegen_rt.cuh"',
+            "using namespace stwo;",
+            "typedef unsigned short uint16_t;",
+            "__device__ __forceinline__ uint4 gen_ldg_u4(const uint32_t* p, int i) {",
+            "  return __ldg(reinterpret_cast<const uint4*>(p) + i);",
+            "}",
+        ] + self.tables + [
+            'extern "C" __global__ void __launch_bounds__(128) stwo_generated_constraints(const GenArgs a) {',
+            f"  __shared__ const uint32_t* s_cols[{nc}];",
+            f"  for (int i = threadIdx.x; i < {self.n_cols}; i += blockDim.x) s_cols[i] = a.cols[i];",
+        ]
+        if smem_pw:
+            lines += [f"  __shared__ uint4 s_pw[{max(n_cons, 1)}];",
+                      f"  for (int i = threadIdx.x; i < {n_cons}; i += blockDim.x) s_pw[i] = gen_ldg_u4(a.powers, i);"]
+        lines += ["  __syncthreads();"]
+        lines += ["  " + x for x in self.pre]
+        lines += [
+            "  const uint32_t n_rows = 1u << a.eval_log;",
+            "  for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < n_rows; row += gridDim.x * blockDim.x) {",
+            "    uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};",
+            "    qm31 qacc = qm31_zero();",
+        ]
+        lines += [f"    const uint32_t {rv} = gen_offset_row(row, a.trace_log, a.eval_log, {off});"
+                  for off, rv in self.offsets.items() if off != 0]
+        lines += ["    " + x for x in body]
+        lines += [
+            "    qm31 rr = qm31_add(qm31_from_u32(m31_reduce64(acc[0]), m31_reduce64(acc[1]), m31_reduce64(acc[2]),",
+            "                                     m31_reduce64(acc[3])), qacc);",
+            "    rr = qm31_mul_m31(rr, __ldg(a.dinv + (row >> a.trace_log)));",
+            "    a.acc0[row] = m31_add(a.acc0[row], rr.a.a);",
+            "    a.acc1[row] = m31_add(a.acc1[row], rr.a.b);",
+            "    a.acc2[row] = m31_add(a.acc2[row], rr.b.a);",
+            "    a.acc3[row] = m31_add(a.acc3[row], rr.b.b);",
+            "  }",
+            "}",
+        ]
+        return "\n".join(lines) + "\n"
+
+
+def generate(ev: ExprEvaluator) -> Tuple[str, List[Tuple[str, bool]]]:
+    """CUDA source of the constraint kernel of a recorded component, and its external parameters
+    (name, is_extension) in the order the kernel reads them."""
+    g = _Gen(ev)
+    src = g.source()
+    return src, g.params
+
+
+_CACHE: Dict[str, int] = {}  # source digest -> compiled component handle (process lifetime)
+
+
+class GeneratedComponent:
+    """A FrameworkEval-like object (`log_size`, `max_constraint_log_degree_bound`, `evaluate`,
+    `params`) with its generated constraint kernel."""
+
+    def __init__(self, air, load: bool = True):
+        from . import _lib
+
+        self.air = air
+        self.ev = air.evaluate(ExprEvaluator())
+        self.source, self.param_names = generate(self.ev)
+        self.n_cols = sum(len(m) for m in self.ev.mask)
+        self.n_constraints = len(self.ev.constraints)
+        key = hashlib.sha256(self.source.encode()).hexdigest()
+        h = _CACHE.get(key)
+        if h is None:
+            out = C.c_void_p()
+            _lib.call("stwo_codegen_compile", self.source.encode(), self.n_cols, len(self.param_names),
+                      self.n_constraints, 1 if load else 0, C.byref(out))
+            h = _CACHE[key] = out.value
+        self.handle = h
+
+    def log_size(self) -> int:
+        return self.air.log_size()
+
+    def max_constraint_log_degree_bound(self) -> int:
+        return self.air.max_constraint_log_degree_bound()
+
+    def mask(self) -> List[List[List[int]]]:
+        return self.ev.mask
+
+    def param_values(self, params: Dict[str, object] = None):
+        from ._lib import QM31
+
+        vals = dict(self.air.params())
+        if params:
+            vals.update(params)
+        arr = (QM31 * max(len(self.param_names), 1))()
+        for i, (name, _) in enumerate(self.param_names):
+            v = vals[name]
+            arr[i] = QM31(tuple(v) if not isinstance(v, int) else (v % X.P, 0, 0, 0))
+        return arr
+
+    def eval_constraints(self, cols: Sequence[int], coeff_powers, accum4: Sequence[int], stream=None,
+                         params: Dict[str, object] = None) -> None:
+        """stwo_eval_constraints_codegen: `cols` are device addresses of the columns on the
+        evaluation domain (interaction 0, 1, 2 in mask order), `coeff_powers` the accumulator's
+        QM31 slice, `accum4` the four coordinate columns."""
+        from . import _lib
+
+        n = len(cols)
+        tab = (C.c_void_p * max(n, 1))(*cols)
+        acc = (C.c_void_p * 4)(*accum4)
+        _lib.call("stwo_eval_constraints_codegen", self.handle, self.log_size(),
+                  self.max_constraint_log_degree_bound(), tab, n, self.param_values(params),
+                  len(self.param_names), coeff_powers, self.n_constraints, acc, stream)
+
+    def eval_at_point(self, mask_values: Sequence[Sequence[Sequence[X.Q]]], rc: X.Q, denom_inv: X.Q,
+                      params: Dict[str, object] = None, acc: X.Q = (0, 0, 0, 0)) -> X.Q:
+        """PointEvaluator (constraint_framework/point.rs:15-70): acc = acc * rc + denom_inv * c
+        for every constraint in order. `mask_values[interaction][local column][offset index]` are
+        the sampled values; preprocessed columns are interaction 0 in request order."""
+        vals = dict(self.air.params())
+        if params:
+            vals.update(params)
+        ev = self.ev
+
+        def col(c):
+            offs = ev.mask[c.interaction][c.local]
+            return tuple(mask_values[c.interaction][c.local][offs.index(c.offset)])
+
+        for k, name in enumerate(ev.preprocessed):
+            vals.setdefault(name, tuple(mask_values[0][ev.preprocessed.index(name)][0]))
+        vals = {k: ((v % X.P, 0, 0, 0) if isinstance(v, int) else tuple(v)) for k, v in vals.items()}
+        vals = X.with_intermediates(ev, col, vals)
+        memo: dict = {}
+        for c in ev.constraints:
+            v = X.eval_expr(c, col, vals, memo)
+            acc = X.q_add(X.q_mul(acc, rc), X.q_mul(denom_inv, v))
+        return acc

@@ -1,0 +1,186 @@
+// Generated constraint kernels: run-time compilation (NVRTC, sm_103a) and the per-component
+// constraint entry point that launches them.
+//
+// The reference writes each AIR once, as a FrameworkEval over an EvalAtRow, and evaluates it on
+// the domain with SimdDomainEvaluator (crates/prover/src/constraint_framework/simd_domain.rs);
+// its expr module records the same AIR as expression trees (constraint_framework/expr/
+// evaluator.rs). Here the recorded expressions become CUDA source (stwo_gb300/codegen.py, or any
+// caller that emits the same kernel interface), which this file compiles and loads, so that every
+// AIR written against the framework runs on the device without a hand-written kernel.
+//
+// The generated kernel is `extern "C" __global__ void stwo_generated_constraints(stwo::GenArgs)`
+// (codegen_rt.cuh). stwo_eval_constraints_codegen does the rest of ComponentProver::
+// evaluate_constraint_quotients_on_domain (component.rs:278-416) as stwo_eval_constraints does:
+// it reverses the accumulator's slice of random-coefficient powers, computes the bit-reversed
+// vanishing inverses and launches the kernel, which adds row_res * denom_inv to the column.
+#include "common.cuh"
+#include "prover.cuh"
+#include "codegen_rt.cuh"
+#include <nvrtc.h>
+#include <memory>
+#include <string>
+
+#include "codegen_headers.inc"  // kFieldCuh, kCodegenRtCuh: the two headers, as text
+
+namespace stwo {
+
+struct CodegenComponent {
+  std::string cubin;
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t kernel = nullptr;
+  uint32_t n_cols = 0, n_params = 0, n_constraints = 0;
+};
+
+static int32_t nvrtc_compile(const char* src, std::string& cubin) {
+  nvrtcProgram prog;
+  const char* headers[] = {kFieldCuh, kCodegenRtCuh};
+  const char* names[] = {"field.cuh", "codegen_rt.cuh"};
+  nvrtcResult r = nvrtcCreateProgram(&prog, src, "stwo_generated.cu", 2, headers, names);
+  if (r != NVRTC_SUCCESS) {
+    set_error("nvrtcCreateProgram: %s", nvrtcGetErrorString(r));
+    return STWO_ERR_CUDA;
+  }
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
+  r = nvrtcCompileProgram(prog, 3, opts);
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    if (n) nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    set_error("generated kernel does not compile: %s\n%.4000s", nvrtcGetErrorString(r), log.c_str());
+    return STWO_ERR_INVALID_ARG;
+  }
+  size_t n = 0;
+  r = nvrtcGetCUBINSize(prog, &n);
+  if (r == NVRTC_SUCCESS) {
+    cubin.assign(n, '\0');
+    r = nvrtcGetCUBIN(prog, &cubin[0]);
+  }
+  nvrtcDestroyProgram(&prog);
+  if (r != NVRTC_SUCCESS) {
+    set_error("nvrtcGetCUBIN: %s", nvrtcGetErrorString(r));
+    return STWO_ERR_CUDA;
+  }
+  return STWO_OK;
+}
+
+static int32_t load(CodegenComponent* c) {
+  if (c->kernel) return STWO_OK;
+  STWO_CHECK_CUDA(cudaLibraryLoadData(&c->lib, c->cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+  cudaError_t e = cudaLibraryGetKernel(&c->kernel, c->lib, "stwo_generated_constraints");
+  if (e != cudaSuccess) {
+    cudaLibraryUnload(c->lib);
+    c->lib = nullptr;
+    set_error("generated module has no stwo_generated_constraints kernel: %s", cudaGetErrorString(e));
+    return STWO_ERR_INVALID_ARG;
+  }
+  return STWO_OK;
+}
+
+}  // namespace stwo
+
+using namespace stwo;
+
+extern "C" {
+
+stwo_status stwo_codegen_compile(const char* kernel_source, uint32_t n_cols, uint32_t n_params,
+                                 uint32_t n_constraints, int load_now, stwo_codegen_component* out) {
+  STWO_REQUIRE(kernel_source && out, "null argument");
+  *out = nullptr;
+  std::unique_ptr<CodegenComponent> c(new CodegenComponent());
+  c->n_cols = n_cols;
+  c->n_params = n_params;
+  c->n_constraints = n_constraints;
+  int32_t st = nvrtc_compile(kernel_source, c->cubin);
+  if (st) return st;
+  if (load_now) {
+    st = load(c.get());
+    if (st) return st;
+  }
+  *out = reinterpret_cast<stwo_codegen_component>(c.release());
+  return STWO_OK;
+}
+
+stwo_status stwo_codegen_cubin_size(stwo_codegen_component comp, size_t* h_size) {
+  STWO_REQUIRE(comp && h_size, "null argument");
+  *h_size = reinterpret_cast<CodegenComponent*>(comp)->cubin.size();
+  return STWO_OK;
+}
+
+stwo_status stwo_codegen_destroy(stwo_codegen_component comp) {
+  auto* c = reinterpret_cast<CodegenComponent*>(comp);
+  if (!c) return STWO_OK;
+  if (c->lib) cudaLibraryUnload(c->lib);
+  delete c;
+  return STWO_OK;
+}
+
+stwo_status stwo_eval_constraints_codegen(stwo_codegen_component comp, uint32_t trace_log_size,
+                                          uint32_t eval_log_size, const uint32_t* const* d_cols, uint32_t n_cols,
+                                          const stwo_qm31* h_params, uint32_t n_params,
+                                          const stwo_qm31* h_coeff_powers, uint32_t n_coeff_powers,
+                                          uint32_t* const d_accum[4], void* stream) {
+  auto* c = reinterpret_cast<CodegenComponent*>(comp);
+  STWO_REQUIRE(c, "null component");
+  STWO_REQUIRE(n_cols == c->n_cols, "the component reads %u columns, %u given", c->n_cols, n_cols);
+  STWO_REQUIRE(n_params == c->n_params, "the component names %u parameters, %u given", c->n_params, n_params);
+  STWO_REQUIRE(n_coeff_powers == c->n_constraints, "the component has %u constraints, %u coefficient powers given",
+               c->n_constraints, n_coeff_powers);
+  STWO_REQUIRE(trace_log_size >= 1 && eval_log_size > trace_log_size && eval_log_size <= 28,
+               "need 1 <= trace_log_size < eval_log_size <= 28 (got %u, %u)", trace_log_size, eval_log_size);
+  STWO_REQUIRE(d_cols || n_cols == 0, "null column table");
+  STWO_REQUIRE(n_params == 0 || h_params, "null parameters");
+  STWO_REQUIRE(h_coeff_powers || n_coeff_powers == 0, "null coefficient powers");
+  STWO_REQUIRE(d_accum && d_accum[0] && d_accum[1] && d_accum[2] && d_accum[3], "null accumulator");
+  for (uint32_t i = 0; i < n_cols; i++) STWO_REQUIRE(d_cols[i], "null column %u", i);
+  if (c->n_constraints == 0) return STWO_OK;
+  int32_t st = load(c);
+  if (st) return st;
+
+  cudaStream_t s = as_stream(stream);
+  const size_t n = c->n_constraints;
+  const std::vector<uint32_t> dinv = composition_denom_inv(trace_log_size, eval_log_size);
+  // One upload: the column table (2 words per pointer, padded to 16 bytes), the parameters, the
+  // powers (the accumulator's slice reversed, component.rs:331; 16-byte aligned for vector loads)
+  // and the denominators.
+  const size_t w_cols = (2 * (size_t)n_cols + 3) & ~(size_t)3, w_par = 4 * (size_t)n_params, w_pow = 4 * n;
+  std::vector<uint32_t> host(w_cols + w_par + w_pow + dinv.size());
+  std::memcpy(host.data(), d_cols, n_cols * sizeof(void*));
+  for (size_t i = 0; i < n_params; i++)
+    for (int j = 0; j < 4; j++) host[w_cols + 4 * i + j] = h_params[i].v[j];
+  for (size_t i = 0; i < n; i++)
+    for (int j = 0; j < 4; j++) host[w_cols + w_par + 4 * i + j] = h_coeff_powers[n - 1 - i].v[j];
+  std::copy(dinv.begin(), dinv.end(), host.begin() + w_cols + w_par + w_pow);
+  uint32_t* d = nullptr;
+  st = scratch_alloc((void**)&d, host.size() * 4, s);
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(d, host.data(), host.size() * 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    GenArgs a;
+    a.cols = reinterpret_cast<const uint32_t* const*>(d);
+    a.params = d + w_cols;
+    a.powers = d + w_cols + w_par;
+    a.dinv = d + w_cols + w_par + w_pow;
+    a.acc0 = d_accum[0];
+    a.acc1 = d_accum[1];
+    a.acc2 = d_accum[2];
+    a.acc3 = d_accum[3];
+    a.trace_log = trace_log_size;
+    a.eval_log = eval_log_size;
+    const uint32_t rows = 1u << eval_log_size;
+    const uint32_t threads = 128;
+    const uint32_t blocks = std::min<uint32_t>((rows + threads - 1) / threads, (uint32_t)sm_count() * 16);
+    void* args[] = {&a};
+    e = cudaLaunchKernel((const void*)c->kernel, dim3(blocks), dim3(threads), args, 0, s);
+    note_launch();
+  }
+  scratch_free(d, s);
+  if (e != cudaSuccess) {
+    set_error("eval_constraints_codegen: %s", cudaGetErrorString(e));
+    return STWO_ERR_CUDA;
+  }
+  return STWO_OK;
+}
+
+}  // extern "C"
