@@ -681,6 +681,101 @@ def run_serve(args, world, rank, local, lib, barrier, max_over_ranks):
     print(json.dumps(line), flush=True)
 
 
+def run_constraints(args, world, rank, local, lib, barrier, max_over_ranks):
+    """Constraint point-wise evaluation (ComponentProver::evaluate_constraint_quotients_on_domain
+    after its extension step) of one component per AIR, on seeded uniform column words resident
+    in HBM: Poseidon2 at 2^16 rows (1,296 columns on 2^18 points) and, generated only, Plonk and
+    the wide-Fibonacci AIR at 2^20 rows. One step = one call per AIR. The generated kernels
+    (stwo_eval_constraints_codegen, compiled once with NVRTC before timing) are timed beside the
+    hand-written ones (stwo_eval_constraints) where those exist; `value` is the generated
+    Poseidon2 kernel's evaluation-domain rows/s."""
+    import numpy as np
+    import torch
+
+    from stwo_gb300 import _lib, airs, codegen
+
+    def rq(rng):
+        return tuple(int(v) for v in rng.integers(0, P, 4))
+
+    specs = [("poseidon", 16, 1), ("plonk", 20, None), ("wide_fib", 20, 0)]
+    out = {}
+    peak, peak_kind = measured_peaks()
+    for name, log, hand_id in specs:
+        rng = np.random.default_rng(5)
+        el, cs = (rq(rng), rq(rng)), rq(rng)
+        air = {"poseidon": lambda: airs.PoseidonEval(log, el, cs), "plonk": lambda: airs.PlonkEval(log, el, cs),
+               "wide_fib": lambda: airs.WideFibonacciEval(log, 100)}[name]()
+        t_c = time.perf_counter()
+        gc = codegen.GeneratedComponent(air)
+        compile_s = time.perf_counter() - t_c
+        N = 1 << air.max_constraint_log_degree_bound()
+        n_cols = gc.n_cols
+        block = torch.randint(0, P, (n_cols, N), dtype=torch.int64, device="cuda").to(torch.int32)
+        ptrs = [block[i].data_ptr() for i in range(n_cols)]
+        acc = [torch.zeros(N, dtype=torch.int32, device="cuda") for _ in range(4)]
+        accp = [a.data_ptr() for a in acc]
+        pw = (_lib.QM31 * gc.n_constraints)(*[_lib.QM31(rq(rng)) for _ in range(gc.n_constraints)])
+        stream = torch.cuda.current_stream().cuda_stream
+
+        def gen():
+            gc.eval_constraints(ptrs, pw, accp, stream)
+
+        def timed(fn):
+            for _ in range(args.warmup):
+                fn()
+            barrier()
+            ts = []
+            for _ in range(args.steps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                fn()
+                e1.record()
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            return max_over_ranks(float(np.median(ts)))
+
+        ms = timed(gen)
+        algo = 4 * n_cols * N + 32 * N  # column words read, accumulation column read and written
+        rec = {"rows": N, "columns": n_cols, "constraints": gc.n_constraints, "generated_ms": ms,
+               "generated_gbs": algo / ms / 1e6, "generated_frac_hbm": algo / ms / 1e6 / peak,
+               "nvrtc_compile_s": compile_s}
+        if hand_id is not None:
+            els = (_lib.QM31 * 2)(_lib.QM31(el[0]), _lib.QM31(el[1]))
+            comp = _lib.Component(hand_id, log, 100 if hand_id == 0 else 0, _lib.QM31(cs),
+                                  els if hand_id == 1 else None, 2 if hand_id == 1 else 0)
+            tab = (C.c_void_p * n_cols)(*ptrs)
+            a4 = (C.c_void_p * 4)(*accp)
+
+            def hand():
+                _lib.call("stwo_eval_constraints", C.byref(comp), tab, n_cols, pw, gc.n_constraints, a4, stream)
+
+            hms = timed(hand)
+            rec.update({"hand_written_ms": hms, "hand_written_gbs": algo / hms / 1e6})
+        out[f"{name}_2e{log}"] = rec
+        del block, acc
+        torch.cuda.empty_cache()
+    if rank != 0:
+        return
+    pos = out["poseidon_2e16"]
+    line = {
+        "metric": "constraint evaluation rows/s (Poseidon2 2^16 rows on the 2^18-point evaluation domain, "
+                  "generated kernel)",
+        "value": pos["rows"] * world / (pos["generated_ms"] / 1e3), "unit": "rows/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": pos["generated_ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
+        "data": "synthetic: uniform column words (seed 5)",
+        "config": {"workload": "constraint point-wise eval: Poseidon2 2^16, Plonk 2^20, wide-Fibonacci 2^20 x 100",
+                   "l2": "columns (1.36 GB for Poseidon2) larger than L2; no flush",
+                   "parallelism": f"replicas x{world}"},
+        "airs": out,
+        "roofline": {"bound": "hbm", "kernel": "generated Poseidon2 constraint kernel",
+                     "achieved": pos["generated_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": pos["generated_frac_hbm"], "peak_kind": peak_kind, "traffic": None},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -723,6 +818,8 @@ def run_gb300(args):
         return run_serve(args, world, rank, local, lib, barrier, max_over_ranks)
     if args.workload == "blake_round":
         return run_blake_round(args, world, rank, local, lib, barrier, max_over_ranks)
+    if args.workload == "constraints":
+        return run_constraints(args, world, rank, local, lib, barrier, max_over_ranks)
 
     wl = PoseidonWorkload(log=args.log_rows)
     for _ in range(args.warmup):
@@ -1010,11 +1107,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="poseidon", choices=["poseidon", "kernels", "gkr", "batch", "serve",
-                                                                "blake_round"],
+                                                                "blake_round", "constraints"],
                     help="poseidon: the headline Poseidon2 2^16-row proof; kernels: the kernel microbench; "
                          "gkr: GKR batch proof of 2^20 LogUp leaves; batch: 64 mixed proofs on a worker pool; "
                          "serve: Poisson-arrival serving with latency percentiles; blake_round: one proof of the "
-                         "Blake2s round AIR")
+                         "Blake2s round AIR; constraints: generated vs hand-written constraint kernels")
     ap.add_argument("--workers", type=int, default=0, help="worker streams of the batch (16) / serve (8) workloads")
     ap.add_argument("--requests", type=int, default=0, help="requests of the serve workload (200)")
     ap.add_argument("--cpu-threads", type=int, default=0)

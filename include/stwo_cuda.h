@@ -397,8 +397,13 @@ typedef struct stwo_codegen_component_s* stwo_codegen_component;
  * STWO_ERR_INVALID_ARG with the compiler log in stwo_last_error(). */
 stwo_status stwo_codegen_compile(const char* kernel_source, uint32_t n_cols, uint32_t n_params,
                                  uint32_t n_constraints, int load_now, stwo_codegen_component* out);
-/* Size of the compiled cubin (diagnostic). */
-stwo_status stwo_codegen_cubin_size(stwo_codegen_component component, size_t* h_size);
+/* The compiled cubin: its size in *h_size, and a copy in h_dst when h_dst is given (capacity must
+ * cover it). With stwo_codegen_from_cubin, a caller can cache compiled components across
+ * processes (NVRTC takes tens of seconds for a component of a thousand constraints). */
+stwo_status stwo_codegen_cubin(stwo_codegen_component component, void* h_dst, size_t capacity, size_t* h_size);
+/* A component from a cubin that stwo_codegen_cubin returned for the same source and sizes. */
+stwo_status stwo_codegen_from_cubin(const void* h_cubin, size_t size, uint32_t n_cols, uint32_t n_params,
+                                    uint32_t n_constraints, int load_now, stwo_codegen_component* out);
 stwo_status stwo_codegen_destroy(stwo_codegen_component component);
 
 /* ComponentProver::evaluate_constraint_quotients_on_domain (crates/prover/src/core/air/mod.rs:59-62;

@@ -127,7 +127,8 @@ SIGNATURES = {
                                         C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "stwo_eval_constraints": (C.c_int32, [C.POINTER(Component), PVP, U32, C.POINTER(QM31), U32, PVP, VP]),
     "stwo_codegen_compile": (C.c_int32, [C.c_char_p, U32, U32, U32, C.c_int, PVP]),
-    "stwo_codegen_cubin_size": (C.c_int32, [VP, C.POINTER(C.c_size_t)]),
+    "stwo_codegen_cubin": (C.c_int32, [VP, VP, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "stwo_codegen_from_cubin": (C.c_int32, [VP, C.c_size_t, U32, U32, U32, C.c_int, PVP]),
     "stwo_codegen_destroy": (C.c_int32, [VP]),
     "stwo_eval_constraints_codegen": (C.c_int32, [VP, U32, U32, PVP, U32, C.POINTER(QM31), U32, C.POINTER(QM31), U32,
                                                   PVP, VP]),

@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import ctypes as C
 import hashlib
+import os
 from typing import Dict, List, Sequence, Tuple
 
 from . import expr as X
@@ -163,6 +164,30 @@ class _Gen:
         sig = (tuple(toks), tuple(canon[roots[i].uid] for i in idx))
         return sig, list(slots)
 
+    def _units(self, roots: List[Expr]) -> List[List[int]]:
+        """The emission units: the groups, except that a periodic run of repeated groups (an AIR
+        that evaluates N identical instances per row, each a sequence of groups) becomes one unit
+        per period, so that one loop body covers a whole instance and loads each of its columns
+        once."""
+        units = self._groups(roots)
+        sigs = [self._signature(roots, u)[0] for u in units]
+        count: Dict[tuple, int] = {}
+        for sg in sigs:
+            count[sg] = count.get(sg, 0) + 1
+        rep = [i for i, sg in enumerate(sigs) if count[sg] > 1]
+        seq = [sigs[i] for i in rep]
+        for p in range(2, len(seq) // 2 + 1):
+            if len(seq) % p or any(seq[k] != seq[k % p] for k in range(len(seq))):
+                continue
+            supers = [sorted(i for j in range(p) for i in units[rep[k * p + j]]) for k in range(len(seq) // p)]
+            first = self._signature(roots, supers[0])[0]
+            if all(self._signature(roots, sp)[0] == first for sp in supers[1:]):
+                taken = set(rep)
+                units = [u for i, u in enumerate(units) if i not in taken] + supers
+                units.sort(key=lambda u: u[0])
+            break
+        return units
+
     # ---- emission
     def _param(self, name: str, is_ext: bool) -> Tuple[str, str, bool]:
         k = self.param_index.get(name)
@@ -244,6 +269,13 @@ class _Gen:
             return self._stmt(uni, "q", f"gen_m31_sub_q({x}, {y})", n.uid, out)
         if k == "mul":
             if tx == ty == "b":
+                # A power-of-two constant factor 2^j is a 31-bit rotation (2^31 = 1 mod P).
+                for (a_, b_) in ((n.args[0], y), (n.args[1], x)):
+                    if a_.kind == "const" and not a_.is_ext and a_.val and a_.val & (a_.val - 1) == 0:
+                        return self._stmt(uni, "b", f"gen_mul_pow2({b_}, {a_.val.bit_length() - 1})", n.uid, out)
+                    if (a_.kind == "const" and a_.is_ext and a_.val[1:] == (0, 0, 0) and a_.val[0]
+                            and a_.val[0] & (a_.val[0] - 1) == 0):
+                        return self._stmt(uni, "b", f"gen_mul_pow2({b_}, {a_.val[0].bit_length() - 1})", n.uid, out)
                 return self._stmt(uni, "b", f"m31_mul({x}, {y})", n.uid, out)
             if tx == "q" and ty == "q":
                 return self._stmt(uni, "q", f"qm31_mul({x}, {y})", n.uid, out)
@@ -274,7 +306,7 @@ class _Gen:
         pw_at = (lambda e: f"s_pw[{e}]") if smem_pw else (lambda e: f"gen_ldg_u4(a.powers, {e})")
         classes: Dict[tuple, List[Tuple[List[int], List[int]]]] = {}
         order = []
-        for g in self._groups(roots):
+        for g in self._units(roots):
             sig, slots = self._signature(roots, g)
             if sig not in classes:
                 classes[sig] = []
@@ -356,6 +388,29 @@ def generate(ev: ExprEvaluator) -> Tuple[str, List[Tuple[str, bool]]]:
 
 
 _CACHE: Dict[str, int] = {}  # source digest -> compiled component handle (process lifetime)
+# Compiled kernels persist across processes here (the package's build directory), keyed by the
+# digest of the source and the component's sizes.
+CUBIN_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "codegen_cache")
+
+
+def _runtime_headers() -> bytes:
+    """The text the library compiles generated kernels against (part of the cache key)."""
+    csrc = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
+    return b"".join(open(os.path.join(csrc, n), "rb").read() for n in ("field.cuh", "codegen_rt.cuh"))
+
+
+def _store_cubin(handle: int, path: str) -> None:
+    from . import _lib
+
+    size = C.c_size_t()
+    _lib.call("stwo_codegen_cubin", handle, None, 0, C.byref(size))
+    buf = C.create_string_buffer(size.value)
+    _lib.call("stwo_codegen_cubin", handle, buf, size.value, C.byref(size))
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + f".{os.getpid()}.tmp"
+    with open(tmp, "wb") as f:
+        f.write(buf.raw)
+    os.replace(tmp, path)
 
 
 class GeneratedComponent:
@@ -370,12 +425,18 @@ class GeneratedComponent:
         self.source, self.param_names = generate(self.ev)
         self.n_cols = sum(len(m) for m in self.ev.mask)
         self.n_constraints = len(self.ev.constraints)
-        key = hashlib.sha256(self.source.encode()).hexdigest()
+        sizes = (self.n_cols, len(self.param_names), self.n_constraints)
+        key = hashlib.sha256(self.source.encode() + repr(sizes).encode() + _runtime_headers()).hexdigest()
         h = _CACHE.get(key)
         if h is None:
             out = C.c_void_p()
-            _lib.call("stwo_codegen_compile", self.source.encode(), self.n_cols, len(self.param_names),
-                      self.n_constraints, 1 if load else 0, C.byref(out))
+            path = os.path.join(CUBIN_CACHE, key + ".cubin")
+            if os.path.exists(path):
+                blob = open(path, "rb").read()
+                _lib.call("stwo_codegen_from_cubin", blob, len(blob), *sizes, 1 if load else 0, C.byref(out))
+            else:
+                _lib.call("stwo_codegen_compile", self.source.encode(), *sizes, 1 if load else 0, C.byref(out))
+                _store_cubin(out.value, path)
             h = _CACHE[key] = out.value
         self.handle = h
 

@@ -102,9 +102,31 @@ stwo_status stwo_codegen_compile(const char* kernel_source, uint32_t n_cols, uin
   return STWO_OK;
 }
 
-stwo_status stwo_codegen_cubin_size(stwo_codegen_component comp, size_t* h_size) {
+stwo_status stwo_codegen_cubin(stwo_codegen_component comp, void* h_dst, size_t capacity, size_t* h_size) {
   STWO_REQUIRE(comp && h_size, "null argument");
-  *h_size = reinterpret_cast<CodegenComponent*>(comp)->cubin.size();
+  const std::string& cubin = reinterpret_cast<CodegenComponent*>(comp)->cubin;
+  *h_size = cubin.size();
+  if (h_dst) {
+    STWO_REQUIRE(capacity >= cubin.size(), "capacity %zu below the cubin's %zu bytes", capacity, cubin.size());
+    std::memcpy(h_dst, cubin.data(), cubin.size());
+  }
+  return STWO_OK;
+}
+
+stwo_status stwo_codegen_from_cubin(const void* h_cubin, size_t size, uint32_t n_cols, uint32_t n_params,
+                                    uint32_t n_constraints, int load_now, stwo_codegen_component* out) {
+  STWO_REQUIRE(h_cubin && size && out, "null argument");
+  *out = nullptr;
+  std::unique_ptr<CodegenComponent> c(new CodegenComponent());
+  c->n_cols = n_cols;
+  c->n_params = n_params;
+  c->n_constraints = n_constraints;
+  c->cubin.assign(static_cast<const char*>(h_cubin), size);
+  if (load_now) {
+    int32_t st = load(c.get());
+    if (st) return st;
+  }
+  *out = reinterpret_cast<stwo_codegen_component>(c.release());
   return STWO_OK;
 }
 

@@ -43,6 +43,11 @@ __device__ __forceinline__ uint32_t gen_offset_row(uint32_t i, uint32_t trace_lo
   return brev(prev, eval_log);
 }
 
+// x * 2^k mod P for canonical x and 0 <= k < 31: a rotation of the 31-bit word (2^31 = 1 mod P).
+// The result is canonical: only x = P would rotate to P, and canonical x is below P.
+__device__ __forceinline__ uint32_t gen_mul_pow2(uint32_t x, int k) {
+  return k ? (((x << k) | (x >> (31 - k))) & P) : x;
+}
 __device__ __forceinline__ qm31 gen_param_q(const uint32_t* p, int k) {
   return qm31_from_u32(__ldg(p + 4 * k), __ldg(p + 4 * k + 1), __ldg(p + 4 * k + 2), __ldg(p + 4 * k + 3));
 }

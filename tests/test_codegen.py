@@ -61,17 +61,17 @@ def test_generated_kernel_compiles(name):
     _, air, *_ = make_case(name)
     gc = codegen.GeneratedComponent(air, load=False)
     size = C.c_size_t()
-    _lib.call("stwo_codegen_cubin_size", gc.handle, C.byref(size))
+    _lib.call("stwo_codegen_cubin", gc.handle, None, 0, C.byref(size))
     assert size.value > 1000
     assert gc.n_constraints == air.evaluate(X.ExprEvaluator()).n_constraints()
 
 
-def test_poseidon_rounds_share_loop_bodies():
-    """Constraint groups of one shape are emitted once, as a loop over column tables: the 56 full
-    rounds that read a round's fresh masks, and the 8 (full round + partial rounds) blocks."""
+def test_poseidon_instances_share_one_loop_body():
+    """The eight Poseidon2 instances of a row (each a run of constraint groups) are one unit
+    class: one loop body over column tables, which loads each column of an instance once."""
     src, params = codegen.generate(airs.PoseidonEval(4).evaluate(X.ExprEvaluator()))
-    assert re.findall(r"for \(int g = 0; g < (\d+); g\+\+\)", src) == ["56", "8"]
-    assert len(src.splitlines()) < 3000
+    assert re.findall(r"for \(int g = 0; g < (\d+); g\+\+\)", src) == ["8"]
+    assert len(src.splitlines()) < 4000
     assert {n for n, _ in params} >= {"PoseidonElements_z", "claimed_sum", "column_size"}
 
 
