@@ -597,10 +597,13 @@ def _wide_fib_oods(log_n: int, n_cols: int, mask: List[Q], rc: Q, px: Q, py: Q) 
     return acc
 
 
-def prove_wide_fib(log_n: int, n_cols: int, d_a: int, d_b: int, cfg=(5, 1, 0, 3)) -> bytes:
+def prove_wide_fib(log_n: int, n_cols: int, d_a: int, d_b: int, cfg=(5, 1, 0, 3), generated: bool = False) -> bytes:
     """test_wide_fib_prove_with_blake (wide_fibonacci/mod.rs:174-227) over the per-operation ABI:
     the trace of 2^log_n rows is generated on the device from the per-row pairs at device
-    addresses d_a, d_b; returns the canonical proof bytes."""
+    addresses d_a, d_b; returns the canonical proof bytes. With `generated`, the component's
+    constraints come from its recorded expressions instead of the hand-written kernel: the domain
+    evaluation is the generated kernel (stwo_eval_constraints_codegen) and the out-of-domain check
+    evaluates the same expressions at the point (PointEvaluator)."""
     pow_bits, log_blowup, log_last, n_queries = cfg
     pcs = CommitmentSchemeProver(cfg, log_n + 1 + log_blowup)
     ch = Blake2sChannel()
@@ -627,7 +630,15 @@ def prove_wide_fib(log_n: int, n_cols: int, d_a: int, d_b: int, cfg=(5, 1, 0, 3)
         cols = [Buf(1 << eval_log) for _ in t.polys]
         call("stwo_evaluate_columns", pcs.tw, canonic_half_coset(eval_log), _ptrs(t.polys), log_n, _ptrs(cols),
              len(cols), None)
-    call("stwo_eval_constraints", C.byref(comp), _ptrs(cols), len(cols), powers, n_cons, _ptr4(acc.cols), None)
+    gen = None
+    if generated:
+        from .airs import WideFibonacciEval
+        from .codegen import GeneratedComponent
+
+        gen = GeneratedComponent(WideFibonacciEval(log_n, n_cols))
+        gen.eval_constraints([c.ptr for c in cols], powers, [c.ptr for c in acc.cols])
+    else:
+        call("stwo_eval_constraints", C.byref(comp), _ptrs(cols), len(cols), powers, n_cons, _ptr4(acc.cols), None)
     call("stwo_interpolate_columns", pcs.tw, canonic_half_coset(eval_log), _ptr4(acc.cols), 4, None)
     pcs.commit_polys(acc.cols, ch)
 
@@ -659,7 +670,14 @@ def prove_wide_fib(log_n: int, n_cols: int, d_a: int, d_b: int, cfg=(5, 1, 0, 3)
     comp_vals = [cv[0] for cv in sampled[2]]
     comp_at = q_add(q_add(comp_vals[0], q_mul(comp_vals[1], (0, 1, 0, 0))),
                     q_add(q_mul(comp_vals[2], (0, 0, 1, 0)), q_mul(comp_vals[3], (0, 0, 0, 1))))
-    if comp_at != _wide_fib_oods(log_n, n_cols, [cv[0] for cv in sampled[1]], rc, px, py):
+    if gen is not None:
+        from .circle import coset, subgroup_gen
+
+        dinv = q_inv(_coset_vanishing(coset(subgroup_gen(log_n + 1), log_n), px, py))
+        want_at = gen.eval_at_point([[], sampled[1], []], rc, dinv)
+    else:
+        want_at = _wide_fib_oods(log_n, n_cols, [cv[0] for cv in sampled[1]], rc, px, py)
+    if comp_at != want_at:
         raise RuntimeError("ConstraintsNotSatisfied")
 
     # FRI quotients, stable-sorted by descending log size.
