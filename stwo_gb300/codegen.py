@@ -37,6 +37,7 @@ from . import expr as X
 from .expr import BaseExpr, Expr, ExprEvaluator
 
 SMEM_BUDGET = 40 * 1024  # shared memory for the column table and the powers, bytes
+MAX_WARPS = 8  # warps per block when repeated instances are spread over warps
 
 
 class _Gen:
@@ -52,6 +53,7 @@ class _Gen:
         self.tables: List[str] = []
         self.offsets: Dict[int, str] = {0: "row"}
         self.uniform_memo: Dict[int, Tuple[str, str, bool]] = {}
+        self.pre_params: Dict[str, bool] = {}
         self.resolved: Dict[int, Expr] = {}
 
     # ---- intermediates and preprocessed columns substituted: a DAG over columns, constants and
@@ -189,16 +191,25 @@ class _Gen:
         return units
 
     # ---- emission
-    def _param(self, name: str, is_ext: bool) -> Tuple[str, str, bool]:
+    def _param(self, name: str, is_ext: bool, out, memo) -> Tuple[str, str, bool]:
+        """An external parameter, read where it is used: in the code before the row loop when a
+        column-independent value needs it (out is None), else in the unit's own scope, so that a
+        warp keeps in registers only the parameters of the units it evaluates."""
         k = self.param_index.get(name)
         if k is None:
             k = self.param_index[name] = len(self.params)
             self.params.append((name, is_ext))
+        if out is None:
+            code, dest, key, seen = f"p{k}", self.pre, name, self.pre_params
+        else:
+            code, dest, key, seen = f"q{k}_{id(memo) % 100003}", out, ("param", name), memo
+        if key not in seen:
+            seen[key] = True
             if is_ext:
-                self.pre.append(f"const qm31 p{k} = gen_param_q(a.params, {k});")
+                dest.append(f"const qm31 {code} = gen_param_q(a.params, {k});")
             else:
-                self.pre.append(f"const uint32_t p{k} = __ldg(a.params + {4 * k});")
-        return (f"p{k}", "q" if is_ext else "b", True)
+                dest.append(f"const uint32_t {code} = __ldg(a.params + {4 * k});")
+        return (code, "q" if is_ext else "b", out is None)
 
     def _offset(self, off: int) -> str:
         rv = self.offsets.get(off)
@@ -206,14 +217,26 @@ class _Gen:
             rv = self.offsets[off] = f"r_{'m' if off < 0 else 'p'}{abs(off)}"
         return rv
 
-    def _value(self, root: Expr, memo: Dict[int, Tuple[str, str, bool]], out: List[str], col_ref) -> Tuple[str, str, bool]:
+    def _value(self, root: Expr, memo: Dict, out: List[str], col_ref) -> Tuple[str, str, bool]:
         for n in self._topo([root]):
-            if n.uid in memo or n.uid in self.uniform_memo:
+            if n.kind in ("param", "const") or n.uid in memo or n.uid in self.uniform_memo:
                 continue
             uni = self.uniform[n.uid] if n.uid in self.uniform else False
-            m = self.uniform_memo if uni else memo
-            m[n.uid] = self._emit(n, lambda u: self.uniform_memo.get(u) or memo[u], out, col_ref)
-        return self.uniform_memo.get(root.uid) or memo[root.uid]
+            (self.uniform_memo if uni else memo)[n.uid] = self._emit(n, memo, out, col_ref)
+        return self._ref(root, memo, out, False)
+
+    def _ref(self, n: Expr, memo: Dict, out: List[str], parent_uniform: bool) -> Tuple[str, str, bool]:
+        """The code of a node for a parent: constants inline, parameters where the parent is."""
+        if n.kind == "const":
+            if not n.is_ext:
+                return (f"{n.val}u", "b", True)
+            v = n.val
+            if v[1] == v[2] == v[3] == 0:
+                return (f"{v[0]}u", "b", True)
+            return (f"qm31_from_u32({v[0]}u, {v[1]}u, {v[2]}u, {v[3]}u)", "q", True)
+        if n.kind == "param":
+            return self._param(n.val, n.is_ext, None if parent_uniform else out, None if parent_uniform else memo)
+        return self.uniform_memo.get(n.uid) or memo[n.uid]
 
     def _stmt(self, uniform: bool, ty: str, code: str, uid: int, out: List[str]) -> Tuple[str, str, bool]:
         name = f"t{uid}"
@@ -221,7 +244,7 @@ class _Gen:
         (self.pre if uniform else out).append(f"const {decl} {name} = {code};")
         return (name, ty, uniform)
 
-    def _emit(self, n: Expr, get, out: List[str], col_ref) -> Tuple[str, str, bool]:
+    def _emit(self, n: Expr, memo: Dict, out: List[str], col_ref) -> Tuple[str, str, bool]:
         k = n.kind
         if k == "col":
             c = n.val
@@ -229,17 +252,8 @@ class _Gen:
             out.append(f"const uint32_t {name} = __ldg({col_ref(self.col_base[c.interaction] + c.local)} + "
                        f"{self._offset(c.offset)});")
             return (name, "b", False)
-        if k == "const":
-            if not n.is_ext:
-                return (f"{n.val}u", "b", True)
-            v = n.val
-            if v[1] == v[2] == v[3] == 0:
-                return (f"{v[0]}u", "b", True)
-            return self._stmt(True, "q", f"qm31_from_u32({v[0]}u, {v[1]}u, {v[2]}u, {v[3]}u)", n.uid, out)
-        if k == "param":
-            return self._param(n.val, n.is_ext)
-        args = [get(a.uid) for a in n.args]
-        uni = all(a[2] for a in args)
+        uni = self.uniform.get(n.uid, False)
+        args = [self._ref(a, memo, out, uni) for a in n.args]
         if k == "secure_col":
             zero = BaseExpr.zero()
             if all(a is zero for a in n.args[1:]):
@@ -312,13 +326,25 @@ class _Gen:
                 classes[sig] = []
                 order.append(sig)
             classes[sig].append((g, slots))
+        loops = [ci for ci, sig in enumerate(order) if len(classes[sig]) > 1]
+        warps = min(max(len(classes[order[ci]]) for ci in loops), MAX_WARPS) if loops else 0
         body: List[str] = []
         outer: Dict[int, Tuple[str, str, bool]] = {}  # values in the row loop's own scope
+        n_inline = 0
         for ci, sig in enumerate(order):
             members = classes[sig]
             if len(members) == 1:
                 g, slots = members[0]
-                self._accumulate(roots, g, outer, body, lambda t: f"s_cols[{t}]", lambda j, i: pw_at(i))
+                if warps >= 2:
+                    # Warp layout: each inline unit is evaluated by one warp, in turn.
+                    inner: List[str] = []
+                    self._accumulate(roots, g, {}, inner, lambda t: f"s_cols[{t}]", lambda j, i: pw_at(i))
+                    body.append(f"if (warp == {n_inline % warps}) {{")
+                    body += ["  " + x for x in inner]
+                    body.append("}")
+                    n_inline += 1
+                else:
+                    self._accumulate(roots, g, outer, body, lambda t: f"s_cols[{t}]", lambda j, i: pw_at(i))
                 continue
             # One loop over the members: column slots and constraint indices from tables.
             m, ns, nc = len(members), len(members[0][1]), len(members[0][0])
@@ -330,14 +356,19 @@ class _Gen:
             self.tables.append(f"__constant__ {ptype} g_pmap{ci}[{m * nc}] = {{{pmap}}};")
             g0, slots0 = members[0]
             slot_of = {t: s for s, t in enumerate(slots0)}
-            inner: List[str] = []
+            inner = []
             self._accumulate(roots, g0, {}, inner, lambda t: f"s_cols[g_cmap{ci}[g * {ns} + {slot_of[t]}]]",
                              lambda j, i: pw_at(f"g_pmap{ci}[g * {nc} + {j}]"))
             body.append("#pragma unroll 1")
-            body.append(f"for (int g = 0; g < {m}; g++) {{")
+            if warps >= 2:
+                body.append(f"for (int g = warp; g < {m}; g += {warps}) {{")
+            else:
+                body.append(f"for (int g = 0; g < {m}; g++) {{")
             body += ["  " + x for x in inner]
             body.append("}")
         nc = max(self.n_cols, 1)
+        threads = 32 * warps if warps >= 2 else 128
+        rows_per_iter = 32 if warps >= 2 else 128
         lines = [
             "// Generated from a constraint-framework component by stwo_gb300/codegen.py.",
             '#include "codegen_rt.cuh"',
@@ -346,36 +377,69 @@ class _Gen:
             "__device__ __forceinline__ uint4 gen_ldg_u4(const uint32_t* p, int i) {",
             "  return __ldg(reinterpret_cast<const uint4*>(p) + i);",
             "}",
+            "// Launch shape read by the library: threads per block, rows per block and iteration.",
+            f'extern "C" __constant__ uint32_t stwo_generated_layout[2] = {{{threads}, {rows_per_iter}}};',
         ] + self.tables + [
-            'extern "C" __global__ void __launch_bounds__(128) stwo_generated_constraints(const GenArgs a) {',
+            f'extern "C" __global__ void __launch_bounds__({threads}) stwo_generated_constraints(const GenArgs a) {{',
             f"  __shared__ const uint32_t* s_cols[{nc}];",
             f"  for (int i = threadIdx.x; i < {self.n_cols}; i += blockDim.x) s_cols[i] = a.cols[i];",
         ]
         if smem_pw:
             lines += [f"  __shared__ uint4 s_pw[{max(n_cons, 1)}];",
                       f"  for (int i = threadIdx.x; i < {n_cons}; i += blockDim.x) s_pw[i] = gen_ldg_u4(a.powers, i);"]
+        if warps >= 2:
+            lines += [f"  __shared__ uint4 s_part[{warps}][32];"]
         lines += ["  __syncthreads();"]
         lines += ["  " + x for x in self.pre]
-        lines += [
-            "  const uint32_t n_rows = 1u << a.eval_log;",
-            "  for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < n_rows; row += gridDim.x * blockDim.x) {",
-            "    uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};",
-            "    qm31 qacc = qm31_zero();",
+        offs = [f"const uint32_t {rv} = gen_offset_row(row, a.trace_log, a.eval_log, {off});"
+                for off, rv in self.offsets.items() if off != 0]
+        finish_row = [
+            "rr = qm31_mul_m31(rr, __ldg(a.dinv + (row >> a.trace_log)));",
+            "a.acc0[row] = m31_add(a.acc0[row], rr.a.a);",
+            "a.acc1[row] = m31_add(a.acc1[row], rr.a.b);",
+            "a.acc2[row] = m31_add(a.acc2[row], rr.b.a);",
+            "a.acc3[row] = m31_add(a.acc3[row], rr.b.b);",
         ]
-        lines += [f"    const uint32_t {rv} = gen_offset_row(row, a.trace_log, a.eval_log, {off});"
-                  for off, rv in self.offsets.items() if off != 0]
-        lines += ["    " + x for x in body]
-        lines += [
-            "    qm31 rr = qm31_add(qm31_from_u32(m31_reduce64(acc[0]), m31_reduce64(acc[1]), m31_reduce64(acc[2]),",
-            "                                     m31_reduce64(acc[3])), qacc);",
-            "    rr = qm31_mul_m31(rr, __ldg(a.dinv + (row >> a.trace_log)));",
-            "    a.acc0[row] = m31_add(a.acc0[row], rr.a.a);",
-            "    a.acc1[row] = m31_add(a.acc1[row], rr.a.b);",
-            "    a.acc2[row] = m31_add(a.acc2[row], rr.b.a);",
-            "    a.acc3[row] = m31_add(a.acc3[row], rr.b.b);",
-            "  }",
-            "}",
+        reduce_acc = [
+            "qm31 rr = qm31_add(qm31_from_u32(m31_reduce64(acc[0]), m31_reduce64(acc[1]), m31_reduce64(acc[2]),",
+            "                                 m31_reduce64(acc[3])), qacc);",
         ]
+        lines += ["  const uint32_t n_rows = 1u << a.eval_log;"]
+        if warps >= 2:
+            # Tiles of 32 rows: warp w takes members w, w + W, ... of each instance loop and every
+            # W-th inline unit for the tile's rows; the warps' partial sums meet in shared memory.
+            lines += [
+                "  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;",
+                "  for (uint32_t tile = blockIdx.x; tile * 32 < n_rows; tile += gridDim.x) {",
+                "    const uint32_t row = min(tile * 32 + lane, n_rows - 1);",
+                "    uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};",
+                "    qm31 qacc = qm31_zero();",
+            ]
+            lines += ["    " + x for x in offs]
+            lines += ["    " + x for x in body]
+            lines += ["    " + x for x in reduce_acc]
+            lines += [
+                "    s_part[warp][lane] = make_uint4(rr.a.a, rr.a.b, rr.b.a, rr.b.b);",
+                "    __syncthreads();",
+                f"    if (warp == 0 && tile * 32 + lane < n_rows) {{",
+                "      for (int w = 1; w < %d; w++) {" % warps,
+                "        const uint4 o = s_part[w][lane];",
+                "        rr = qm31_add(rr, qm31_from_u32(o.x, o.y, o.z, o.w));",
+                "      }",
+            ]
+            lines += ["      " + x for x in finish_row]
+            lines += ["    }", "    __syncthreads();", "  }", "}"]
+        else:
+            lines += [
+                "  for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < n_rows; row += gridDim.x * blockDim.x) {",
+                "    uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};",
+                "    qm31 qacc = qm31_zero();",
+            ]
+            lines += ["    " + x for x in offs]
+            lines += ["    " + x for x in body]
+            lines += ["    " + x for x in reduce_acc]
+            lines += ["    " + x for x in finish_row]
+            lines += ["  }", "}"]
         return "\n".join(lines) + "\n"
 
 

@@ -29,6 +29,9 @@ struct CodegenComponent {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t kernel = nullptr;
   uint32_t n_cols = 0, n_params = 0, n_constraints = 0;
+  // Launch shape the generated source declares (stwo_generated_layout): threads per block and
+  // rows a block covers per iteration of its row loop.
+  uint32_t threads = 128, rows_per_block = 128;
 };
 
 static int32_t nvrtc_compile(const char* src, std::string& cubin) {
@@ -74,6 +77,18 @@ static int32_t load(CodegenComponent* c) {
     c->lib = nullptr;
     set_error("generated module has no stwo_generated_constraints kernel: %s", cudaGetErrorString(e));
     return STWO_ERR_INVALID_ARG;
+  }
+  void* d_layout = nullptr;
+  size_t bytes = 0;
+  if (cudaLibraryGetGlobal(&d_layout, &bytes, c->lib, "stwo_generated_layout") == cudaSuccess && bytes == 8) {
+    uint32_t layout[2];
+    STWO_CHECK_CUDA(cudaMemcpy(layout, d_layout, 8, cudaMemcpyDeviceToHost));
+    STWO_REQUIRE(layout[0] >= 32 && layout[0] <= 1024 && layout[0] % 32 == 0 && layout[1] >= 1,
+                 "generated module declares an invalid launch shape (%u, %u)", layout[0], layout[1]);
+    c->threads = layout[0];
+    c->rows_per_block = layout[1];
+  } else {
+    cudaGetLastError();  // a source without the declaration takes the default shape
   }
   return STWO_OK;
 }
@@ -191,8 +206,9 @@ stwo_status stwo_eval_constraints_codegen(stwo_codegen_component comp, uint32_t 
     a.trace_log = trace_log_size;
     a.eval_log = eval_log_size;
     const uint32_t rows = 1u << eval_log_size;
-    const uint32_t threads = 128;
-    const uint32_t blocks = std::min<uint32_t>((rows + threads - 1) / threads, (uint32_t)sm_count() * 16);
+    const uint32_t threads = c->threads;
+    const uint32_t blocks =
+        std::min<uint32_t>((rows + c->rows_per_block - 1) / c->rows_per_block, (uint32_t)sm_count() * (2048 / threads));
     void* args[] = {&a};
     e = cudaLaunchKernel((const void*)c->kernel, dim3(blocks), dim3(threads), args, 0, s);
     note_launch();
