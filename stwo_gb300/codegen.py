@@ -331,18 +331,20 @@ class _Gen:
         body: List[str] = []
         outer: Dict[int, Tuple[str, str, bool]] = {}  # values in the row loop's own scope
         n_inline = 0
+        inline_by_warp: Dict[int, List[str]] = {}
         for ci, sig in enumerate(order):
             members = classes[sig]
             if len(members) == 1:
                 g, slots = members[0]
                 if warps >= 2:
-                    # Warp layout: each inline unit is evaluated by one warp, in turn.
-                    inner: List[str] = []
-                    self._accumulate(roots, g, {}, inner, lambda t: f"s_cols[{t}]", lambda j, i: pw_at(i))
-                    body.append(f"if (warp == {n_inline % warps}) {{")
-                    body += ["  " + x for x in inner]
-                    body.append("}")
-                    n_inline += 1
+                    # Warp layout: the constraints of the units outside the instance loops go to
+                    # the warps in turn, one constraint at a time (a LogUp batch per warp), each
+                    # warp recomputing whatever its constraints share with another warp's.
+                    for i in g:
+                        inner: List[str] = []
+                        self._accumulate(roots, [i], {}, inner, lambda t: f"s_cols[{t}]", lambda j, i_: pw_at(i_))
+                        inline_by_warp.setdefault(n_inline % warps, []).extend(inner)
+                        n_inline += 1
                 else:
                     self._accumulate(roots, g, outer, body, lambda t: f"s_cols[{t}]", lambda j, i: pw_at(i))
                 continue
@@ -365,6 +367,10 @@ class _Gen:
             else:
                 body.append(f"for (int g = 0; g < {m}; g++) {{")
             body += ["  " + x for x in inner]
+            body.append("}")
+        for w in sorted(inline_by_warp):
+            body.append(f"if (warp == {w}) {{")
+            body += ["  " + x for x in inline_by_warp[w]]
             body.append("}")
         nc = max(self.n_cols, 1)
         threads = 32 * warps if warps >= 2 else 128
