@@ -54,6 +54,7 @@ class _Gen:
         self.offsets: Dict[int, str] = {0: "row"}
         self.uniform_memo: Dict[int, Tuple[str, str, bool]] = {}
         self.pre_params: Dict[str, bool] = {}
+        self.n_scopes = 0
         self.resolved: Dict[int, Expr] = {}
 
     # ---- intermediates and preprocessed columns substituted: a DAG over columns, constants and
@@ -202,7 +203,10 @@ class _Gen:
         if out is None:
             code, dest, key, seen = f"p{k}", self.pre, name, self.pre_params
         else:
-            code, dest, key, seen = f"q{k}_{id(memo) % 100003}", out, ("param", name), memo
+            if "scope" not in memo:
+                self.n_scopes += 1
+                memo["scope"] = self.n_scopes
+            code, dest, key, seen = f"q{k}_{memo['scope']}", out, ("param", name), memo
         if key not in seen:
             seen[key] = True
             if is_ext:
