@@ -37,7 +37,6 @@ from . import expr as X
 from .expr import BaseExpr, Expr, ExprEvaluator
 
 SMEM_BUDGET = 40 * 1024  # shared memory for the column table and the powers, bytes
-MAX_WARPS = 8  # warps per block when repeated instances are spread over warps
 
 
 class _Gen:
@@ -194,8 +193,8 @@ class _Gen:
     # ---- emission
     def _param(self, name: str, is_ext: bool, out, memo) -> Tuple[str, str, bool]:
         """An external parameter, read where it is used: in the code before the row loop when a
-        column-independent value needs it (out is None), else in the unit's own scope, so that a
-        warp keeps in registers only the parameters of the units it evaluates."""
+        column-independent value needs it (out is None), else in the scope of the unit that uses
+        it, so that the relation elements of a LogUp unit are not live across the whole row."""
         k = self.param_index.get(name)
         if k is None:
             k = self.param_index[name] = len(self.params)
@@ -330,27 +329,13 @@ class _Gen:
                 classes[sig] = []
                 order.append(sig)
             classes[sig].append((g, slots))
-        loops = [ci for ci, sig in enumerate(order) if len(classes[sig]) > 1]
-        warps = min(max(len(classes[order[ci]]) for ci in loops), MAX_WARPS) if loops else 0
         body: List[str] = []
         outer: Dict[int, Tuple[str, str, bool]] = {}  # values in the row loop's own scope
-        n_inline = 0
-        inline_by_warp: Dict[int, List[str]] = {}
         for ci, sig in enumerate(order):
             members = classes[sig]
             if len(members) == 1:
                 g, slots = members[0]
-                if warps >= 2:
-                    # Warp layout: the constraints of the units outside the instance loops go to
-                    # the warps in turn, one constraint at a time (a LogUp batch per warp), each
-                    # warp recomputing whatever its constraints share with another warp's.
-                    for i in g:
-                        inner: List[str] = []
-                        self._accumulate(roots, [i], {}, inner, lambda t: f"s_cols[{t}]", lambda j, i_: pw_at(i_))
-                        inline_by_warp.setdefault(n_inline % warps, []).extend(inner)
-                        n_inline += 1
-                else:
-                    self._accumulate(roots, g, outer, body, lambda t: f"s_cols[{t}]", lambda j, i: pw_at(i))
+                self._accumulate(roots, g, outer, body, lambda t: f"s_cols[{t}]", lambda j, i: pw_at(i))
                 continue
             # One loop over the members: column slots and constraint indices from tables.
             m, ns, nc = len(members), len(members[0][1]), len(members[0][0])
@@ -366,19 +351,11 @@ class _Gen:
             self._accumulate(roots, g0, {}, inner, lambda t: f"s_cols[g_cmap{ci}[g * {ns} + {slot_of[t]}]]",
                              lambda j, i: pw_at(f"g_pmap{ci}[g * {nc} + {j}]"))
             body.append("#pragma unroll 1")
-            if warps >= 2:
-                body.append(f"for (int g = warp; g < {m}; g += {warps}) {{")
-            else:
-                body.append(f"for (int g = 0; g < {m}; g++) {{")
+            body.append(f"for (int g = 0; g < {m}; g++) {{")
             body += ["  " + x for x in inner]
             body.append("}")
-        for w in sorted(inline_by_warp):
-            body.append(f"if (warp == {w}) {{")
-            body += ["  " + x for x in inline_by_warp[w]]
-            body.append("}")
         nc = max(self.n_cols, 1)
-        threads = 32 * warps if warps >= 2 else 128
-        rows_per_iter = 32 if warps >= 2 else 128
+        threads = rows_per_iter = 128
         lines = [
             "// Generated from a constraint-framework component by stwo_gb300/codegen.py.",
             '#include "codegen_rt.cuh"',
@@ -397,8 +374,6 @@ class _Gen:
         if smem_pw:
             lines += [f"  __shared__ uint4 s_pw[{max(n_cons, 1)}];",
                       f"  for (int i = threadIdx.x; i < {n_cons}; i += blockDim.x) s_pw[i] = gen_ldg_u4(a.powers, i);"]
-        if warps >= 2:
-            lines += [f"  __shared__ uint4 s_part[{warps}][32];"]
         lines += ["  __syncthreads();"]
         lines += ["  " + x for x in self.pre]
         offs = [f"const uint32_t {rv} = gen_offset_row(row, a.trace_log, a.eval_log, {off});"
@@ -415,41 +390,16 @@ class _Gen:
             "                                 m31_reduce64(acc[3])), qacc);",
         ]
         lines += ["  const uint32_t n_rows = 1u << a.eval_log;"]
-        if warps >= 2:
-            # Tiles of 32 rows: warp w takes members w, w + W, ... of each instance loop and every
-            # W-th inline unit for the tile's rows; the warps' partial sums meet in shared memory.
-            lines += [
-                "  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;",
-                "  for (uint32_t tile = blockIdx.x; tile * 32 < n_rows; tile += gridDim.x) {",
-                "    const uint32_t row = min(tile * 32 + lane, n_rows - 1);",
-                "    uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};",
-                "    qm31 qacc = qm31_zero();",
-            ]
-            lines += ["    " + x for x in offs]
-            lines += ["    " + x for x in body]
-            lines += ["    " + x for x in reduce_acc]
-            lines += [
-                "    s_part[warp][lane] = make_uint4(rr.a.a, rr.a.b, rr.b.a, rr.b.b);",
-                "    __syncthreads();",
-                f"    if (warp == 0 && tile * 32 + lane < n_rows) {{",
-                "      for (int w = 1; w < %d; w++) {" % warps,
-                "        const uint4 o = s_part[w][lane];",
-                "        rr = qm31_add(rr, qm31_from_u32(o.x, o.y, o.z, o.w));",
-                "      }",
-            ]
-            lines += ["      " + x for x in finish_row]
-            lines += ["    }", "    __syncthreads();", "  }", "}"]
-        else:
-            lines += [
-                "  for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < n_rows; row += gridDim.x * blockDim.x) {",
-                "    uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};",
-                "    qm31 qacc = qm31_zero();",
-            ]
-            lines += ["    " + x for x in offs]
-            lines += ["    " + x for x in body]
-            lines += ["    " + x for x in reduce_acc]
-            lines += ["    " + x for x in finish_row]
-            lines += ["  }", "}"]
+        lines += [
+            "  for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < n_rows; row += gridDim.x * blockDim.x) {",
+            "    uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};",
+            "    qm31 qacc = qm31_zero();",
+        ]
+        lines += ["    " + x for x in offs]
+        lines += ["    " + x for x in body]
+        lines += ["    " + x for x in reduce_acc]
+        lines += ["    " + x for x in finish_row]
+        lines += ["  }", "}"]
         return "\n".join(lines) + "\n"
 
 

@@ -71,7 +71,6 @@ def test_poseidon_instances_share_one_loop_body():
     class: one loop body over column tables, which loads each column of an instance once."""
     src, params = codegen.generate(airs.PoseidonEval(4).evaluate(X.ExprEvaluator()))
     assert re.findall(r"for \(int g = \w+; g < (\d+);", src) == ["8"]
-    assert "__launch_bounds__(256)" in src  # one warp per instance
     assert len(src.splitlines()) < 4000
     assert {n for n, _ in params} >= {"PoseidonElements_z", "claimed_sum", "column_size"}
 
