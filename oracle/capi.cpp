@@ -474,6 +474,7 @@ void oracle_channel_draw_felts(size_t n, uint32_t* out) {
 
 #include "air_blake_round.h"
 #include "air_examples.h"
+#include "components.h"
 
 extern "C" {
 
@@ -638,6 +639,39 @@ int oracle_eval_constraints(uint32_t air_id, uint32_t log_n, uint32_t n_cols, co
     return 0;
   } catch (...) {
     return 1;
+  }
+}
+
+// prove_fibonacci_plonk (plonk/mod.rs:153-266) with the canonical proof bytes; returns the length
+// (0 on error).
+size_t oracle_prove_plonk(uint32_t log_n, const uint32_t cfg[4], uint8_t* out, size_t cap, char* err, size_t err_cap) {
+  try {
+    std::vector<uint8_t> bytes = serialize(prove_plonk(log_n, PcsConfig{cfg[0], cfg[1], cfg[2], cfg[3]}));
+    if (bytes.size() > cap) throw std::runtime_error("output buffer too small");
+    std::memcpy(out, bytes.data(), bytes.size());
+    return bytes.size();
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+// prove_state_machine (state_machine/mod.rs:26-135): the stark proof's canonical bytes and the two
+// components' claimed sums.
+size_t oracle_prove_state_machine(uint32_t log_n, const uint32_t initial[2], const uint32_t cfg[4], uint8_t* out,
+                                  size_t cap, uint32_t claimed[8], char* err, size_t err_cap) {
+  try {
+    QM31 cs[2];
+    std::vector<uint8_t> bytes =
+        serialize(prove_state_machine(log_n, initial, PcsConfig{cfg[0], cfg[1], cfg[2], cfg[3]}, cs));
+    if (bytes.size() > cap) throw std::runtime_error("output buffer too small");
+    std::memcpy(out, bytes.data(), bytes.size());
+    q_to(cs[0], claimed);
+    q_to(cs[1], claimed + 4);
+    return bytes.size();
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
   }
 }
 

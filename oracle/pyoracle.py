@@ -222,6 +222,36 @@ def prove_poseidon(log_n, init=None, config=(5, 1, 0, 3)):
     return bytes(out[:n]), tuple(int(x) for x in cs)
 
 
+def prove_plonk(log_n, config=(5, 1, 0, 3)):
+    """Proof bytes of prove_fibonacci_plonk (plonk/mod.rs:153-266) with 2^log_n gates."""
+    cap = 64 << 20
+    out = np.zeros(cap, np.uint8)
+    err = C.create_string_buffer(512)
+    f = lib().oracle_prove_plonk
+    f.restype = C.c_size_t
+    cfg = _u32(config)
+    n = f(C.c_uint32(log_n), _p(cfg), _p(out), C.c_size_t(cap), err, C.c_size_t(512))
+    if n == 0:
+        raise RuntimeError("oracle prove failed: " + err.value.decode())
+    return bytes(out[:n])
+
+
+def prove_state_machine(log_n, initial=(0, 0), config=(5, 1, 0, 3)):
+    """(stark proof bytes, (claimed sum x, claimed sum y)) of prove_state_machine
+    (state_machine/mod.rs:26-135)."""
+    cap = 64 << 20
+    out = np.zeros(cap, np.uint8)
+    cs = np.zeros(8, np.uint32)
+    err = C.create_string_buffer(512)
+    f = lib().oracle_prove_state_machine
+    f.restype = C.c_size_t
+    init, cfg = _u32(initial), _u32(config)
+    n = f(C.c_uint32(log_n), _p(init), _p(cfg), _p(out), C.c_size_t(cap), _p(cs), err, C.c_size_t(512))
+    if n == 0:
+        raise RuntimeError("oracle prove failed: " + err.value.decode())
+    return bytes(out[:n]), (tuple(int(x) for x in cs[:4]), tuple(int(x) for x in cs[4:]))
+
+
 def verify_poseidon(log_n, claimed_sum, proof: bytes):
     buf = np.frombuffer(proof, dtype=np.uint8).copy()
     err = C.create_string_buffer(512)

@@ -130,6 +130,7 @@ SIGNATURES = {
     "stwo_codegen_cubin": (C.c_int32, [VP, VP, C.c_size_t, C.POINTER(C.c_size_t)]),
     "stwo_codegen_from_cubin": (C.c_int32, [VP, C.c_size_t, U32, U32, U32, C.c_int, PVP]),
     "stwo_codegen_destroy": (C.c_int32, [VP]),
+    "stwo_logup_interaction_codegen": (C.c_int32, [VP, U32, PVP, U32, C.POINTER(QM31), U32, VP, C.POINTER(QM31), VP]),
     "stwo_eval_constraints_codegen": (C.c_int32, [VP, U32, U32, PVP, U32, C.POINTER(QM31), U32, C.POINTER(QM31), U32,
                                                   PVP, VP]),
 }

@@ -403,6 +403,69 @@ class _Gen:
         return "\n".join(lines) + "\n"
 
 
+class _FracGen(_Gen):
+    """The interaction trace of a component's LogUp relations (LogupTraceGenerator,
+    crates/prover/src/constraint_framework/logup.rs:123-260): per row of the trace domain, the
+    value num_b / den_b of each batch fraction that finalize_logup_batched formed, accumulated
+    across the batches, written as four coordinate columns per batch. The library then finalises
+    the last column (claimed sum, shift, prefix sum in coset order)."""
+
+    def source(self) -> str:
+        ev = self.ev
+        assert ev.logup_batches, "the component has no LogUp relation"
+        self.n_cols = len(ev.mask[0]) + len(ev.mask[1])
+        roots = []
+        for f in ev.logup_batches:
+            roots += [self.resolve(X._as_ext(f.numerator).simplify()), self.resolve(X._as_ext(f.denominator).simplify())]
+        nodes = self._topo(roots)
+        self.uniform = {}
+        for n in nodes:
+            if n.kind == "col":
+                assert n.val.interaction in (0, 1) and n.val.offset == 0, \
+                    "relation entries read trace columns of the current row only"
+                self.uniform[n.uid] = False
+            elif n.kind in ("const", "param"):
+                self.uniform[n.uid] = True
+            else:
+                self.uniform[n.uid] = all(self.uniform[a.uid] for a in n.args)
+        body: List[str] = []
+        memo: Dict = {}
+        col = lambda t: f"s_cols[{t}]"  # noqa: E731
+        body.append("qm31 prev = qm31_zero();")
+        for b in range(len(ev.logup_batches)):
+            num, den = (self._value(r, memo, body, col) for r in roots[2 * b:2 * b + 2])
+            lift = lambda v: v[0] if v[1] == "q" else f"qm31_from_u32({v[0]}, 0u, 0u, 0u)"  # noqa: E731
+            body.append(f"prev = qm31_add(prev, qm31_mul({lift(num)}, qm31_inv({lift(den)})));")
+            for j, c in enumerate(("prev.a.a", "prev.a.b", "prev.b.a", "prev.b.b")):
+                body.append(f"a.acc0[(size_t){4 * b + j} * n_rows + row] = {c};")
+        nc = max(self.n_cols, 1)
+        lines = [
+            "// Generated from a constraint-framework component by stwo_gb300/codegen.py.",
+            '#include "codegen_rt.cuh"',
+            "using namespace stwo;",
+            'extern "C" __constant__ uint32_t stwo_generated_layout[2] = {128, 128};',
+            'extern "C" __global__ void __launch_bounds__(128) stwo_generated_fractions(const GenArgs a) {',
+            f"  __shared__ const uint32_t* s_cols[{nc}];",
+            f"  for (int i = threadIdx.x; i < {self.n_cols}; i += blockDim.x) s_cols[i] = a.cols[i];",
+            "  __syncthreads();",
+        ]
+        lines += ["  " + x for x in self.pre]
+        lines += [
+            "  const uint32_t n_rows = 1u << a.eval_log;",
+            "  for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < n_rows; row += gridDim.x * blockDim.x) {",
+        ]
+        lines += ["    " + x for x in body]
+        lines += ["  }", "}"]
+        return "\n".join(lines) + "\n"
+
+
+def generate_fractions(ev: ExprEvaluator) -> Tuple[str, List[Tuple[str, bool]]]:
+    """CUDA source of the interaction-trace kernel of a recorded component and its parameters."""
+    g = _FracGen(ev)
+    src = g.source()
+    return src, g.params
+
+
 def generate(ev: ExprEvaluator) -> Tuple[str, List[Tuple[str, bool]]]:
     """CUDA source of the constraint kernel of a recorded component, and its external parameters
     (name, is_extension) in the order the kernel reads them."""
@@ -415,6 +478,26 @@ _CACHE: Dict[str, int] = {}  # source digest -> compiled component handle (proce
 # Compiled kernels persist across processes here (the package's build directory), keyed by the
 # digest of the source and the component's sizes.
 CUBIN_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "codegen_cache")
+
+
+def _compiled(source: str, sizes: Tuple[int, int, int], load: bool = True) -> int:
+    """A compiled component handle for `source`: from this process's cache, the cubin cache on
+    disk, or NVRTC."""
+    from . import _lib
+
+    key = hashlib.sha256(source.encode() + repr(sizes).encode() + _runtime_headers()).hexdigest()
+    h = _CACHE.get(key)
+    if h is None:
+        out = C.c_void_p()
+        path = os.path.join(CUBIN_CACHE, key + ".cubin")
+        if os.path.exists(path):
+            blob = open(path, "rb").read()
+            _lib.call("stwo_codegen_from_cubin", blob, len(blob), *sizes, 1 if load else 0, C.byref(out))
+        else:
+            _lib.call("stwo_codegen_compile", source.encode(), *sizes, 1 if load else 0, C.byref(out))
+            _store_cubin(out.value, path)
+        h = _CACHE[key] = out.value
+    return h
 
 
 def _runtime_headers() -> bytes:
@@ -449,20 +532,8 @@ class GeneratedComponent:
         self.source, self.param_names = generate(self.ev)
         self.n_cols = sum(len(m) for m in self.ev.mask)
         self.n_constraints = len(self.ev.constraints)
-        sizes = (self.n_cols, len(self.param_names), self.n_constraints)
-        key = hashlib.sha256(self.source.encode() + repr(sizes).encode() + _runtime_headers()).hexdigest()
-        h = _CACHE.get(key)
-        if h is None:
-            out = C.c_void_p()
-            path = os.path.join(CUBIN_CACHE, key + ".cubin")
-            if os.path.exists(path):
-                blob = open(path, "rb").read()
-                _lib.call("stwo_codegen_from_cubin", blob, len(blob), *sizes, 1 if load else 0, C.byref(out))
-            else:
-                _lib.call("stwo_codegen_compile", self.source.encode(), *sizes, 1 if load else 0, C.byref(out))
-                _store_cubin(out.value, path)
-            h = _CACHE[key] = out.value
-        self.handle = h
+        self.handle = _compiled(self.source, (self.n_cols, len(self.param_names), self.n_constraints), load)
+        self._frac = None
 
     def log_size(self) -> int:
         return self.air.log_size()
@@ -473,14 +544,15 @@ class GeneratedComponent:
     def mask(self) -> List[List[List[int]]]:
         return self.ev.mask
 
-    def param_values(self, params: Dict[str, object] = None):
+    def param_values(self, params: Dict[str, object] = None, names=None):
         from ._lib import QM31
 
+        names = self.param_names if names is None else names
         vals = dict(self.air.params())
         if params:
             vals.update(params)
-        arr = (QM31 * max(len(self.param_names), 1))()
-        for i, (name, _) in enumerate(self.param_names):
+        arr = (QM31 * max(len(names), 1))()
+        for i, (name, _) in enumerate(names):
             v = vals[name]
             arr[i] = QM31(tuple(v) if not isinstance(v, int) else (v % X.P, 0, 0, 0))
         return arr
@@ -498,6 +570,30 @@ class GeneratedComponent:
         _lib.call("stwo_eval_constraints_codegen", self.handle, self.log_size(),
                   self.max_constraint_log_degree_bound(), tab, n, self.param_values(params),
                   len(self.param_names), coeff_powers, self.n_constraints, acc, stream)
+
+    def n_interaction_columns(self) -> int:
+        return 4 * len(self.ev.logup_batches)
+
+    def interaction(self, cols: Sequence[int], out: int, stream=None, params: Dict[str, object] = None) -> X.Q:
+        """The LogUp interaction trace (stwo_logup_interaction_codegen): `cols` are device
+        addresses of the preprocessed then trace columns on the trace domain, `out` a device block
+        of n_interaction_columns() columns of 2^log_size words. Returns the claimed sum; the
+        relation elements come from the AIR's params (its claimed sum is not read)."""
+        from . import _lib
+        from ._lib import QM31
+
+        if self._frac is None:
+            src, names = generate_fractions(self.ev)
+            n_in = len(self.ev.mask[0]) + len(self.ev.mask[1])
+            self._frac = (_compiled(src, (n_in, len(names), len(self.ev.logup_batches))), names, n_in)
+        h, names, n_in = self._frac
+        vals = dict(params or {})
+        vals.setdefault("claimed_sum", (0, 0, 0, 0))
+        tab = (C.c_void_p * max(len(cols), 1))(*cols)
+        cs = QM31()
+        _lib.call("stwo_logup_interaction_codegen", h, self.log_size(), tab, len(cols),
+                  self.param_values(vals, names), len(names), out, C.byref(cs), stream)
+        return tuple(cs.v)
 
     def eval_at_point(self, mask_values: Sequence[Sequence[Sequence[X.Q]]], rc: X.Q, denom_inv: X.Q,
                       params: Dict[str, object] = None, acc: X.Q = (0, 0, 0, 0)) -> X.Q:

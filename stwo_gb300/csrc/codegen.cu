@@ -32,6 +32,7 @@ struct CodegenComponent {
   // Launch shape the generated source declares (stwo_generated_layout): threads per block and
   // rows a block covers per iteration of its row loop.
   uint32_t threads = 128, rows_per_block = 128;
+  bool fractions = false;  // the module holds stwo_generated_fractions (LogUp interaction trace)
 };
 
 static int32_t nvrtc_compile(const char* src, std::string& cubin) {
@@ -73,9 +74,17 @@ static int32_t load(CodegenComponent* c) {
   STWO_CHECK_CUDA(cudaLibraryLoadData(&c->lib, c->cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
   cudaError_t e = cudaLibraryGetKernel(&c->kernel, c->lib, "stwo_generated_constraints");
   if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaLibraryGetKernel(&c->kernel, c->lib, "stwo_generated_fractions");
+    c->fractions = e == cudaSuccess;
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
     cudaLibraryUnload(c->lib);
     c->lib = nullptr;
-    set_error("generated module has no stwo_generated_constraints kernel: %s", cudaGetErrorString(e));
+    c->kernel = nullptr;
+    set_error("generated module has neither stwo_generated_constraints nor stwo_generated_fractions: %s",
+              cudaGetErrorString(e));
     return STWO_ERR_INVALID_ARG;
   }
   void* d_layout = nullptr;
@@ -174,6 +183,7 @@ stwo_status stwo_eval_constraints_codegen(stwo_codegen_component comp, uint32_t 
   if (c->n_constraints == 0) return STWO_OK;
   int32_t st = load(c);
   if (st) return st;
+  STWO_REQUIRE(!c->fractions, "this module is an interaction-trace kernel, not a constraint kernel");
 
   cudaStream_t s = as_stream(stream);
   const size_t n = c->n_constraints;
@@ -218,6 +228,53 @@ stwo_status stwo_eval_constraints_codegen(stwo_codegen_component comp, uint32_t 
     set_error("eval_constraints_codegen: %s", cudaGetErrorString(e));
     return STWO_ERR_CUDA;
   }
+  return STWO_OK;
+}
+
+stwo_status stwo_logup_interaction_codegen(stwo_codegen_component comp, uint32_t log_size,
+                                          const uint32_t* const* d_cols, uint32_t n_cols, const stwo_qm31* h_params,
+                                          uint32_t n_params, uint32_t* d_out, stwo_qm31* h_claimed_sum,
+                                          void* stream) {
+  auto* c = reinterpret_cast<CodegenComponent*>(comp);
+  STWO_REQUIRE(c && d_out, "null argument");
+  STWO_REQUIRE(n_cols == c->n_cols, "the interaction kernel reads %u columns, %u given", c->n_cols, n_cols);
+  STWO_REQUIRE(n_params == c->n_params, "the interaction kernel names %u parameters, %u given", c->n_params,
+               n_params);
+  STWO_REQUIRE(c->n_constraints >= 1, "no LogUp batch");
+  STWO_REQUIRE(log_size >= 1 && log_size <= 28, "log_size out of range");
+  STWO_REQUIRE(d_cols || n_cols == 0, "null column table");
+  STWO_REQUIRE(n_params == 0 || h_params, "null parameters");
+  for (uint32_t i = 0; i < n_cols; i++) STWO_REQUIRE(d_cols[i], "null column %u", i);
+  int32_t st = load(c);
+  if (st) return st;
+  STWO_REQUIRE(c->fractions, "this module is a constraint kernel, not an interaction-trace kernel");
+  cudaStream_t s = as_stream(stream);
+  const size_t w_cols = (2 * (size_t)n_cols + 3) & ~(size_t)3, w_par = 4 * (size_t)n_params;
+  std::vector<uint32_t> host(w_cols + w_par + 4);
+  std::memcpy(host.data(), d_cols, n_cols * sizeof(void*));
+  for (size_t i = 0; i < n_params; i++)
+    for (int j = 0; j < 4; j++) host[w_cols + 4 * i + j] = h_params[i].v[j];
+  Arena arena(s);
+  uint32_t* d = arena.alloc(host.size());
+  if (!d) return STWO_ERR_OOM;
+  STWO_CHECK_CUDA(cudaMemcpyAsync(d, host.data(), host.size() * 4, cudaMemcpyHostToDevice, s));
+  GenArgs a{};
+  a.cols = reinterpret_cast<const uint32_t* const*>(d);
+  a.params = d + w_cols;
+  a.acc0 = d_out;
+  a.trace_log = a.eval_log = log_size;
+  const uint32_t rows = 1u << log_size;
+  const uint32_t blocks =
+      std::min<uint32_t>((rows + c->rows_per_block - 1) / c->rows_per_block, (uint32_t)sm_count() * (2048 / c->threads));
+  void* args[] = {&a};
+  STWO_CHECK_CUDA(cudaLaunchKernel((const void*)c->kernel, dim3(blocks), dim3(c->threads), args, 0, s));
+  note_launch();
+  // LogupTraceGenerator::finalize_last on the last batch's column (logup.rs:150-190).
+  hq claimed;
+  st = logup_finalize_last(d_out + (size_t)4 * (c->n_constraints - 1) * rows, log_size, arena, s, &claimed);
+  if (st) return st;
+  if (h_claimed_sum)
+    for (int j = 0; j < 4; j++) h_claimed_sum->v[j] = claimed.v[j];
   return STWO_OK;
 }
 

@@ -603,6 +603,7 @@ class ExprEvaluator:
         self.mask: List[List[List[int]]] = [[], [], []]
         # LogUp state (FormalLogupAtRow, evaluator.rs:13-31).
         self.logup_fracs: List[Fraction] = []
+        self.logup_batches: List[Fraction] = []
         self.logup_finalized = True
         self.cumsum_shift = ExtExpr.param("claimed_sum") * BaseExpr.param("column_size").inverse()
 
@@ -675,6 +676,9 @@ class ExprEvaluator:
             by_batch.setdefault(b, []).append(f)
         assert set(by_batch) == set(range(last + 1)), "Batching must contain all consecutive batches"
         prev_col = ExtExpr.zero()
+        # The batch fractions, in column order: what the interaction trace's columns accumulate
+        # (LogupColGenerator::write_frac, logup.rs:222-238).
+        self.logup_batches = [_sum_fracs(by_batch[b]) for b in range(last + 1)]
         for b in range(last):
             frac = _sum_fracs(by_batch[b])
             cur, = self.next_extension_interaction_mask(INTERACTION_TRACE_IDX, [0])

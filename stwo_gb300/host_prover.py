@@ -219,7 +219,17 @@ class Buf:
         if zero:
             call("stwo_buf_zero", self.ptr, n_words * 4, None)
 
+    @classmethod
+    def view(cls, owner: "Buf", word_offset: int, n_words: int) -> "Buf":
+        """Words [word_offset, word_offset + n_words) of `owner`, which stays allocated while the
+        view lives (the view frees nothing)."""
+        v = cls.__new__(cls)
+        v.n, v.ptr, v.owner = n_words, owner.ptr + 4 * word_offset, owner
+        return v
+
     def __del__(self):
+        if getattr(self, "owner", None) is not None:
+            return
         try:
             _lib.load().stwo_buf_free(self.ptr, None)
         except Exception:
@@ -680,6 +690,13 @@ def prove_wide_fib(log_n: int, n_cols: int, d_a: int, d_b: int, cfg=(5, 1, 0, 3)
     if comp_at != want_at:
         raise RuntimeError("ConstraintsNotSatisfied")
 
+    return _finish_proof(pcs, ch, points, sampled, cfg)
+
+
+def _finish_proof(pcs: "CommitmentSchemeProver", ch: Blake2sChannel, points, sampled, cfg) -> bytes:
+    """prove_values after the sampled values are mixed (pcs/prover.rs:104-148): FRI quotients,
+    the FRI commitment, proof of work, decommitment, and the canonical proof bytes."""
+    pow_bits, log_blowup, log_last, n_queries = cfg
     # FRI quotients, stable-sorted by descending log size.
     cols = []
     for ti, tr in enumerate(pcs.trees):
