@@ -234,9 +234,39 @@ inline bool rebuild_evals(const std::vector<size_t>& queries, const std::vector<
 // Full verification (prover/mod.rs:81-127 with pcs/verifier.rs and the FRI verifier).
 // `trace_log_sizes[t]` are the committed trees' column log sizes before blowup (trees before
 // the composition tree). Returns "" on success, else the failure reason.
+// The component-specific parts of verify(): the composition's log size, the mask points of every
+// committed tree at the out-of-domain point, and the composition value those samples imply.
+struct VerifyAir {
+  uint32_t composition_log;
+  std::function<std::vector<std::vector<std::vector<CirclePointQM31>>>(CirclePointQM31)> mask_points;
+  std::function<QM31(CirclePointQM31, const MaskValues&, QM31)> composition_at;
+};
+
+inline std::string verify_with(const VerifyAir& va, Channel& ch, const StarkProof& proof,
+                               const std::vector<std::vector<uint32_t>>& trace_log_sizes,
+                               const std::function<void(size_t, Channel&)>& after_tree);
+
 inline std::string verify(const Air& air, Channel& ch, const StarkProof& proof,
                           const std::vector<std::vector<uint32_t>>& trace_log_sizes,
                           const std::function<void(size_t, Channel&)>& after_tree = nullptr) {
+  VerifyAir va;
+  va.composition_log = air.max_constraint_log_degree_bound();
+  const size_t n_trees = trace_log_sizes.size(), n_pre = trace_log_sizes[0].size();
+  va.mask_points = [&air, n_trees, n_pre](CirclePointQM31 oods) {
+    auto pts = mask_points(air, oods);
+    while (pts.size() < n_trees) pts.emplace_back();
+    pts[0].assign(n_pre, {});
+    return pts;
+  };
+  va.composition_at = [&air](CirclePointQM31 oods, const MaskValues& mv, QM31 rc) {
+    return eval_composition_at_point(air, oods, mv, rc);
+  };
+  return verify_with(va, ch, proof, trace_log_sizes, after_tree);
+}
+
+inline std::string verify_with(const VerifyAir& va, Channel& ch, const StarkProof& proof,
+                               const std::vector<std::vector<uint32_t>>& trace_log_sizes,
+                               const std::function<void(size_t, Channel&)>& after_tree) {
   const PcsConfig& cfg = proof.config;
   size_t n_trees = trace_log_sizes.size();
   if (proof.commitments.size() != n_trees + 1) return "commitments";
@@ -250,11 +280,9 @@ inline std::string verify(const Air& air, Channel& ch, const StarkProof& proof,
   }
   QM31 rc = ch.draw_felt();
   ch.mix_root(proof.commitments[n_trees]);
-  tree_logs.push_back(std::vector<uint32_t>(4, air.max_constraint_log_degree_bound() + cfg.log_blowup));
+  tree_logs.push_back(std::vector<uint32_t>(4, va.composition_log + cfg.log_blowup));
   CirclePointQM31 oods = random_point(ch);
-  auto pts = mask_points(air, oods);
-  while (pts.size() < n_trees) pts.emplace_back();
-  pts[0].assign(trace_log_sizes[0].size(), {});
+  auto pts = va.mask_points(oods);
   pts.push_back(std::vector<std::vector<CirclePointQM31>>(4, {oods}));
   if (proof.sampled_values.size() != pts.size()) return "sampled structure";
   for (size_t t = 0; t < pts.size(); t++) {
@@ -265,7 +293,7 @@ inline std::string verify(const Air& air, Channel& ch, const StarkProof& proof,
   MaskValues mv(proof.sampled_values.begin(), proof.sampled_values.end() - 1);
   const auto& comp = proof.sampled_values.back();
   QM31 parts[4] = {comp[0][0], comp[1][0], comp[2][0], comp[3][0]};
-  if (PointEvaluator::combine_ef(parts) != eval_composition_at_point(air, oods, mv, rc)) return "OodsNotMatching";
+  if (PointEvaluator::combine_ef(parts) != va.composition_at(oods, mv, rc)) return "OodsNotMatching";
 
   // verify_values
   std::vector<QM31> flat;

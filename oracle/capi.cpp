@@ -644,12 +644,71 @@ int oracle_eval_constraints(uint32_t air_id, uint32_t log_n, uint32_t n_cols, co
 
 // prove_fibonacci_plonk (plonk/mod.rs:153-266) with the canonical proof bytes; returns the length
 // (0 on error).
-size_t oracle_prove_plonk(uint32_t log_n, const uint32_t cfg[4], uint8_t* out, size_t cap, char* err, size_t err_cap) {
+size_t oracle_prove_plonk(uint32_t log_n, const uint32_t cfg[4], uint8_t* out, size_t cap, uint32_t claimed[4],
+                          char* err, size_t err_cap) {
   try {
-    std::vector<uint8_t> bytes = serialize(prove_plonk(log_n, PcsConfig{cfg[0], cfg[1], cfg[2], cfg[3]}));
+    QM31 cs;
+    std::vector<uint8_t> bytes = serialize(prove_plonk(log_n, PcsConfig{cfg[0], cfg[1], cfg[2], cfg[3]}, &cs));
+    q_to(cs, claimed);
     if (bytes.size() > cap) throw std::runtime_error("output buffer too small");
     std::memcpy(out, bytes.data(), bytes.size());
     return bytes.size();
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+// Verification of a prove_fibonacci_plonk proof (prover/mod.rs:81-127) given the claimed sum.
+int oracle_verify_plonk(uint32_t log_n, const uint32_t claimed_sum[4], const uint8_t* proof, size_t len, char* err,
+                        size_t err_cap) {
+  try {
+    StarkProof p;
+    if (!deserialize(proof, len, p)) throw std::runtime_error("malformed proof bytes");
+    Channel ch;
+    PlonkAir air(log_n, Relation<2>{}, q_of(claimed_sum));
+    auto hook = [&](size_t t, Channel& c) {
+      if (t == 1) air.rel = Relation<2>::draw(c);
+    };
+    std::vector<uint32_t> four(4, log_n);
+    std::string r = verify_components(place({&air}, {{0, 1, 2, 3}}), ch, p, {four, four, std::vector<uint32_t>(8, log_n)},
+                                      hook);
+    if (!r.empty()) throw std::runtime_error(r);
+    return 1;
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+// Verification of a prove_state_machine stark proof given the two claimed sums: the statements are
+// mixed where the prover mixed them (the log sizes after the empty preprocessed root, the claimed
+// sums after the relation elements are drawn).
+int oracle_verify_state_machine(uint32_t log_n, const uint32_t claimed[8], const uint8_t* proof, size_t len,
+                                char* err, size_t err_cap) {
+  try {
+    StarkProof p;
+    if (!deserialize(proof, len, p)) throw std::runtime_error("malformed proof bytes");
+    Channel ch;
+    mix_config(p.config, ch);
+    const uint32_t logs[2] = {log_n, log_n - 1};
+    QM31 cs[2] = {q_of(claimed), q_of(claimed + 4)};
+    StateTransitionAir a0(0, logs[0], Relation<2>{}, cs[0]), a1(1, logs[1], Relation<2>{}, cs[1]);
+    auto hook = [&](size_t t, Channel& c) {
+      if (t == 0) {
+        c.mix_u64(logs[0]);
+        c.mix_u64(logs[1]);
+      } else if (t == 1) {
+        a0.rel = a1.rel = Relation<2>::draw(c);
+        c.mix_felts({cs[0], cs[1]});
+      }
+    };
+    std::string r = verify_components(place({&a0, &a1}, {{}, {}}), ch, p,
+                                      {{}, {logs[0], logs[0], logs[1], logs[1]},
+                                       {logs[0], logs[0], logs[0], logs[0], logs[1], logs[1], logs[1], logs[1]}},
+                                      hook);
+    if (!r.empty()) throw std::runtime_error(r);
+    return 1;
   } catch (const std::exception& e) {
     snprintf(err, err_cap, "%s", e.what());
     return 0;

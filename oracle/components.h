@@ -147,6 +147,41 @@ inline StarkProof prove_components(const std::vector<Placed>& comps, Channel& ch
   return proof;
 }
 
+// verify() for placed components (prover/mod.rs:81-127 with Components' mask points and
+// composition at the point). `trace_log_sizes[t]` are the committed trees' column log sizes.
+inline std::string verify_components(const std::vector<Placed>& comps, Channel& ch, const StarkProof& proof,
+                                     const std::vector<std::vector<uint32_t>>& trace_log_sizes,
+                                     const std::function<void(size_t, Channel&)>& after_tree) {
+  VerifyAir va;
+  va.composition_log = 0;
+  for (auto& c : comps) va.composition_log = std::max(va.composition_log, c.air->max_constraint_log_degree_bound());
+  va.mask_points = [&](CirclePointQM31 oods) {
+    std::vector<std::vector<std::vector<CirclePointQM31>>> pts(trace_log_sizes.size());
+    pts[0].assign(trace_log_sizes[0].size(), {});
+    for (auto& c : comps) {
+      auto mp = mask_points(*c.air, oods);
+      for (size_t t = 1; t < mp.size(); t++)
+        for (auto& col : mp[t]) pts[t].push_back(col);
+      for (size_t idx : c.preprocessed) pts[0][idx] = {oods};
+    }
+    return pts;
+  };
+  va.composition_at = [&](CirclePointQM31 oods, const MaskValues& all, QM31 rc) {
+    QM31 acc;
+    for (auto& c : comps) {
+      MaskValues mv(c.air->mask_offsets().size());
+      for (size_t idx : c.preprocessed) mv[0].push_back(all[0][idx]);
+      for (size_t t = 1; t < mv.size(); t++)
+        for (size_t i = c.spans[t - 1].first; i < c.spans[t - 1].second; i++) mv[t].push_back(all[t][i]);
+      QM31 dinv = inv(coset_vanishing(canonic_coset(c.air->log_size()), oods));
+      PointEvaluator e(&mv, &acc, rc, dinv);
+      c.air->eval_point(e);
+    }
+    return acc;
+  };
+  return verify_with(va, ch, proof, trace_log_sizes, after_tree);
+}
+
 inline void commit_evals_mixed(CommitmentSchemeProver& pcs, const std::vector<Column>& evals, Channel& ch) {
   std::vector<Column> polys(evals.size());
 #pragma omp parallel for schedule(dynamic)
@@ -183,7 +218,7 @@ inline std::vector<Column> logup_trace(const std::vector<std::vector<Frac>>& bat
 }
 
 // prove_fibonacci_plonk (plonk/mod.rs:153-266): a Fibonacci circuit of 2^log_n gates.
-inline StarkProof prove_plonk(uint32_t log_n, const PcsConfig& config) {
+inline StarkProof prove_plonk(uint32_t log_n, const PcsConfig& config, QM31* claimed = nullptr) {
   size_t n = (size_t)1 << log_n;
   std::vector<M31> fib = {M31(1), M31(1)};
   for (size_t i = 0; i < n; i++) fib.push_back(fib[fib.size() - 1] + fib[fib.size() - 2]);
@@ -218,6 +253,7 @@ inline StarkProof prove_plonk(uint32_t log_n, const PcsConfig& config) {
   }
   QM31 cs;
   pcs.commit_evals(logup_trace(batches, n, cs), log_n, ch);
+  if (claimed) *claimed = cs;
   PlonkAir air(log_n, rel, cs);
   return prove_components(place({&air}, {{0, 1, 2, 3}}), ch, pcs);
 }

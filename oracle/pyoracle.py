@@ -223,17 +223,19 @@ def prove_poseidon(log_n, init=None, config=(5, 1, 0, 3)):
 
 
 def prove_plonk(log_n, config=(5, 1, 0, 3)):
-    """Proof bytes of prove_fibonacci_plonk (plonk/mod.rs:153-266) with 2^log_n gates."""
+    """(proof bytes, claimed sum) of prove_fibonacci_plonk (plonk/mod.rs:153-266) with 2^log_n
+    gates."""
     cap = 64 << 20
     out = np.zeros(cap, np.uint8)
+    cs = np.zeros(4, np.uint32)
     err = C.create_string_buffer(512)
     f = lib().oracle_prove_plonk
     f.restype = C.c_size_t
     cfg = _u32(config)
-    n = f(C.c_uint32(log_n), _p(cfg), _p(out), C.c_size_t(cap), err, C.c_size_t(512))
+    n = f(C.c_uint32(log_n), _p(cfg), _p(out), C.c_size_t(cap), _p(cs), err, C.c_size_t(512))
     if n == 0:
         raise RuntimeError("oracle prove failed: " + err.value.decode())
-    return bytes(out[:n])
+    return bytes(out[:n]), tuple(int(x) for x in cs)
 
 
 def prove_state_machine(log_n, initial=(0, 0), config=(5, 1, 0, 3)):
@@ -250,6 +252,23 @@ def prove_state_machine(log_n, initial=(0, 0), config=(5, 1, 0, 3)):
     if n == 0:
         raise RuntimeError("oracle prove failed: " + err.value.decode())
     return bytes(out[:n]), (tuple(int(x) for x in cs[:4]), tuple(int(x) for x in cs[4:]))
+
+
+def verify_plonk(log_n, claimed_sum, proof: bytes):
+    buf = np.frombuffer(proof, dtype=np.uint8).copy()
+    err = C.create_string_buffer(512)
+    ok = lib().oracle_verify_plonk(C.c_uint32(log_n), _p(_u32(claimed_sum)), _p(buf), C.c_size_t(len(proof)), err,
+                                   C.c_size_t(512))
+    return bool(ok), err.value.decode()
+
+
+def verify_state_machine(log_n, claimed_sums, proof: bytes):
+    buf = np.frombuffer(proof, dtype=np.uint8).copy()
+    err = C.create_string_buffer(512)
+    cs = _u32(list(claimed_sums[0]) + list(claimed_sums[1]))
+    ok = lib().oracle_verify_state_machine(C.c_uint32(log_n), _p(cs), _p(buf), C.c_size_t(len(proof)), err,
+                                           C.c_size_t(512))
+    return bool(ok), err.value.decode()
 
 
 def verify_poseidon(log_n, claimed_sum, proof: bytes):

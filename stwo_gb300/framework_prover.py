@@ -219,8 +219,9 @@ def plonk_circuit(log_n: int) -> Dict[str, np.ndarray]:
     return c
 
 
-def prove_plonk(log_n: int, cfg=(5, 1, 0, 3)) -> bytes:
-    """prove_fibonacci_plonk (plonk/mod.rs:153-266) on the device; the canonical proof bytes."""
+def prove_plonk(log_n: int, cfg=(5, 1, 0, 3)) -> Tuple[bytes, Q]:
+    """prove_fibonacci_plonk (plonk/mod.rs:153-266) on the device: the canonical proof bytes and
+    the component's claimed sum."""
     from .airs import PlonkEval
 
     circuit = plonk_circuit(log_n)
@@ -239,7 +240,7 @@ def prove_plonk(log_n: int, cfg=(5, 1, 0, 3)) -> bytes:
     _commit_evals(pcs, inter, ch)
     gc = GeneratedComponent(PlonkEval(log_n, (z, alpha), cs))
     alloc = TraceLocationAllocator()
-    return prove([alloc.place(gc)], pcs, ch, cfg)
+    return prove([alloc.place(gc)], pcs, ch, cfg), cs
 
 
 def _split(block: Buf, k: int, n: int) -> List[Buf]:

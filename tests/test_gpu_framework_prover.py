@@ -12,7 +12,12 @@ pytestmark = pytest.mark.gpu
 def test_plonk_proof_matches_oracle(cuda, oracle, log_n, cfg):
     from stwo_gb300 import framework_prover
 
-    assert framework_prover.prove_plonk(log_n, cfg) == oracle.prove_plonk(log_n, cfg)
+    got, cs = framework_prover.prove_plonk(log_n, cfg)
+    want, want_cs = oracle.prove_plonk(log_n, cfg)
+    assert cs == want_cs
+    assert got == want
+    ok, why = oracle.verify_plonk(log_n, cs, got)
+    assert ok, why
 
 
 @pytest.mark.parametrize("log_n,initial,cfg", [(5, (0, 0), (5, 1, 0, 3)), (7, (17, 12), (5, 1, 0, 3)),
@@ -24,3 +29,5 @@ def test_state_machine_proof_matches_oracle(cuda, oracle, log_n, initial, cfg):
     want, want_sums = oracle.prove_state_machine(log_n, initial, cfg)
     assert sums == want_sums
     assert got == want
+    ok, why = oracle.verify_state_machine(log_n, sums, got)
+    assert ok, why

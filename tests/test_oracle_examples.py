@@ -1,0 +1,23 @@
+"""The oracle's multi-component prove() and verify() on the reference's Plonk and state-machine
+examples (CPU): proofs verify, and a flipped byte or a wrong claimed sum is rejected."""
+import pytest
+
+
+@pytest.mark.parametrize("log_n,cfg", [(4, (5, 1, 0, 3)), (7, (8, 2, 1, 5))])
+def test_plonk_prove_verify(oracle, log_n, cfg):
+    proof, cs = oracle.prove_plonk(log_n, cfg)
+    assert oracle.verify_plonk(log_n, cs, proof) == (True, "")
+    bad = bytearray(proof)
+    bad[len(bad) // 2] ^= 1
+    assert not oracle.verify_plonk(log_n, cs, bytes(bad))[0]
+    assert not oracle.verify_plonk(log_n, (cs[0] ^ 1,) + cs[1:], proof)[0]
+
+
+@pytest.mark.parametrize("log_n,initial", [(5, (0, 0)), (8, (17, 12))])
+def test_state_machine_prove_verify(oracle, log_n, initial):
+    proof, sums = oracle.prove_state_machine(log_n, initial)
+    assert oracle.verify_state_machine(log_n, sums, proof) == (True, "")
+    bad = bytearray(proof)
+    bad[-40] ^= 1
+    assert not oracle.verify_state_machine(log_n, sums, bytes(bad))[0]
+    assert not oracle.verify_state_machine(log_n, (sums[1], sums[0]), proof)[0]
