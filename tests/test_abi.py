@@ -40,3 +40,18 @@ def test_status_strings_without_gpu():
     lib = _lib.load()
     assert lib.stwo_status_string(0) == b"ok"
     assert lib.stwo_status_string(1) == b"invalid argument"
+
+
+def test_rust_binding_matches_header():
+    """Every entry point the Rust CudaBackend crate declares exists in include/stwo_cuda.h with the
+    same number of parameters (the crate cannot be compiled here: no Rust toolchain)."""
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "stwo_cuda.h")).read(), flags=re.S)
+    header = {m.group(1): len([a for a in m.group(2).split(",") if a.strip() not in ("", "void")])
+              for m in re.finditer(r"\b(stwo_\w+)\s*\(([^;]*?)\)\s*;", text, flags=re.S)}
+    ffi = open(os.path.join(ROOT, "stwo_gb300", "rust", "stwo-cuda-backend", "src", "ffi.rs")).read()
+    decls = {m.group(1): len([a for a in m.group(2).split(",") if a.strip()])
+             for m in re.finditer(r"pub fn (stwo_\w+)\s*\(([^)]*)\)", ffi, flags=re.S)}
+    assert len(decls) >= 40
+    for name, n in decls.items():
+        assert name in header, name
+        assert header[name] == n, (name, header[name], n)
