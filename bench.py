@@ -698,6 +698,8 @@ def run_constraints(args, world, rank, local, lib, barrier, max_over_ranks):
         return tuple(int(v) for v in rng.integers(0, P, 4))
 
     specs = [("poseidon", 16, 1), ("plonk", 20, None), ("wide_fib", 20, 0)]
+    if args.log_rows:  # a smaller Poseidon2 case alone (profiling captures)
+        specs = [("poseidon", args.log_rows, 1)]
     out = {}
     peak, peak_kind = measured_peaks()
     for name, log, hand_id in specs:
@@ -757,10 +759,10 @@ def run_constraints(args, world, rank, local, lib, barrier, max_over_ranks):
         torch.cuda.empty_cache()
     if rank != 0:
         return
-    pos = out["poseidon_2e16"]
+    pos = out[f"poseidon_2e{specs[0][1]}"]
     line = {
-        "metric": "constraint evaluation rows/s (Poseidon2 2^16 rows on the 2^18-point evaluation domain, "
-                  "generated kernel)",
+        "metric": f"constraint evaluation rows/s (Poseidon2 2^{specs[0][1]} rows on the "
+                  f"2^{specs[0][1] + 2}-point evaluation domain, generated kernel)",
         "value": pos["rows"] * world / (pos["generated_ms"] / 1e3), "unit": "rows/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": pos["generated_ms"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 (M31 field words)",
@@ -877,6 +879,18 @@ def run_gb300(args):
                                   "2^14 rows, scaled by the rows (2-pass FFT: intermediate written and re-read)",
                 "algorithmic_bytes_per_launch": sbytes[dom],
                 "stage_ms": hbm_stages[dom]}
+        if dom == "Composition extension":
+            # What actually bounds the stage: the butterfly's integer datapath. The composition
+            # extension evaluates each column of 2^LOG coefficients on the 2^(LOG + 2)-point
+            # domain, four sub-domains of LOG layers of 2^(LOG - 1) butterflies each.
+            rate = C.c_double()
+            _lib.call("stwo_butterfly_rate", 512, C.byref(rate), None)
+            bfly = wl.TRACE_COLS * 4 * wl.LOG * (1 << (wl.LOG - 1))
+            got = bfly / (hbm_stages[dom] / 1e3)
+            roof["int_bound"] = {"unit": "butterflies/s", "achieved": got, "peak": rate.value,
+                                 "frac": got / rate.value, "butterflies_per_launch": bfly,
+                                 "peak_source": "stwo_butterfly_rate: the library's butterfly with every operand "
+                                                "in registers, one full wave of blocks"}
     line = {
         "metric": "proof s & trace cells/s (Poseidon2 2^16 rows)",
         "value": wl.cells * world / (step_ms / 1e3),

@@ -70,6 +70,11 @@ uint64_t stwo_kernel_launches(void);
  * calling thread, named after the reference's tracing spans ("Extension", "Merkle", ...).
  * stwo_set_stage_timing(1) enables recording (and clears earlier records); stwo_stage_times
  * returns the number of distinct stages and fills up to `cap` names / summed milliseconds. */
+/* Diagnostic without a reference counterpart: the device's rate for the circle-FFT butterfly of
+ * the library's FFT kernels with every operand in registers (one full wave of blocks, `rounds`
+ * rounds of 32 butterflies per thread, timed on `stream`), in butterflies per second. This is the
+ * integer-datapath bound that the FFT passes are measured against. */
+stwo_status stwo_butterfly_rate(uint32_t rounds, double* h_butterflies_per_s, void* stream);
 stwo_status stwo_set_stage_timing(int enable);
 uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap);
 
@@ -405,6 +410,19 @@ stwo_status stwo_codegen_cubin(stwo_codegen_component component, void* h_dst, si
 stwo_status stwo_codegen_from_cubin(const void* h_cubin, size_t size, uint32_t n_cols, uint32_t n_params,
                                     uint32_t n_constraints, int load_now, stwo_codegen_component* out);
 stwo_status stwo_codegen_destroy(stwo_codegen_component component);
+
+/* The LogUp interaction trace of a generated component (LogupTraceGenerator,
+ * crates/prover/src/constraint_framework/logup.rs:123-260): `component` was compiled from the source
+ * of its fraction kernel (stwo_gb300/codegen.py generate_fractions; n_constraints = the number of
+ * LogUp batches B), d_cols are its preprocessed then trace columns on the trace domain (2^log_size
+ * bit-reversed evaluations), d_out 4 B contiguous columns of 2^log_size words: batch b's column holds
+ * the running sum over batches 0..b of num/den, the last one finalised (claimed sum subtracted as
+ * claimed_sum / 2^log_size, inclusive prefix sum in coset order). The claimed sum is returned in
+ * h_claimed_sum (the call synchronises the stream). */
+stwo_status stwo_logup_interaction_codegen(stwo_codegen_component component, uint32_t log_size,
+                                          const uint32_t* const* d_cols, uint32_t n_cols, const stwo_qm31* h_params,
+                                          uint32_t n_params, uint32_t* d_out, stwo_qm31* h_claimed_sum,
+                                          void* stream);
 
 /* ComponentProver::evaluate_constraint_quotients_on_domain (crates/prover/src/core/air/mod.rs:59-62;
  * SimdBackend implementation crates/prover/src/constraint_framework/component.rs:278-416) for a

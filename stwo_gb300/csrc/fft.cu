@@ -482,11 +482,75 @@ int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* c
   return run_fft(tree, half, false, coeffs, coeff_log, out, n, s);
 }
 
+// Register-only throughput of the butterfly above: each thread keeps 16 words and 15 doubled
+// twiddles in registers and runs `rounds` rounds of 4 forward layers (the shape of one register
+// round of k_fft_tile), with no memory traffic in the loop. Its rate is the integer-datapath
+// bound of the circle FFT on this device.
+__global__ void __launch_bounds__(256) k_butterfly_probe(const uint32_t* in, uint32_t* out, uint32_t rounds) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
+  uint32_t v[16], t[15];
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = in[g + i * n];
+#pragma unroll
+  for (int i = 0; i < 15; i++) t[i] = 2u * (in[(g * 15 + i) % (16 * n)] % (P - 1));
+  for (uint32_t it = 0; it < rounds; it++) {
+    int ti = 0;
+#pragma unroll
+    for (int j = 3; j >= 0; j--)
+#pragma unroll
+      for (int kh = 0; kh < (1 << (3 - j)); kh++) {
+        const uint32_t tt = t[ti++];
+#pragma unroll
+        for (int kl = 0; kl < (1 << j); kl++) bfly2(v[(kh << (j + 1)) | kl], v[(kh << (j + 1)) | kl | (1 << j)], tt);
+      }
+  }
+#pragma unroll
+  for (int i = 0; i < 16; i++) out[g + i * n] = v[i];
+}
+
 }  // namespace stwo
 
 using namespace stwo;
 
 extern "C" {
+
+stwo_status stwo_butterfly_rate(uint32_t rounds, double* h_butterflies_per_s, void* stream) {
+  STWO_REQUIRE(h_butterflies_per_s && rounds >= 1 && rounds <= (1u << 16), "need 1 <= rounds <= 65536");
+  cudaStream_t s = as_stream(stream);
+  int per_sm = 0;
+  STWO_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_butterfly_probe, 256, 0));
+  // One full wave: every SM holds as many blocks as fit, so elapsed time equals active time.
+  const uint32_t blocks = (uint32_t)std::max(1, per_sm) * (uint32_t)sm_count();
+  const size_t words = (size_t)blocks * 256 * 16;
+  uint32_t* d = nullptr;
+  int32_t st = scratch_alloc((void**)&d, words * 8, s);
+  if (st) return st;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t err = cudaMemsetAsync(d, 0x5a, words * 4, s);
+  if (!err) err = cudaEventCreate(&e0);
+  if (!err) err = cudaEventCreate(&e1);
+  float ms = 0.f;
+  if (!err) {
+    k_butterfly_probe<<<blocks, 256, 0, s>>>(d, d + words, rounds);  // warm-up
+    cudaEventRecord(e0, s);
+    k_butterfly_probe<<<blocks, 256, 0, s>>>(d, d + words, rounds);
+    cudaEventRecord(e1, s);
+    note_launch();
+    note_launch();
+    err = cudaGetLastError();
+    if (!err) err = cudaEventSynchronize(e1);
+    if (!err) err = cudaEventElapsedTime(&ms, e0, e1);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  scratch_free(d, s);
+  if (err) {
+    set_error("butterfly_rate: %s", cudaGetErrorString(err));
+    return STWO_ERR_CUDA;
+  }
+  *h_butterflies_per_s = (double)blocks * 256.0 * rounds * 32.0 / (ms * 1e-3);
+  return STWO_OK;
+}
 
 stwo_status stwo_interpolate_columns(stwo_twiddle_tree tree, stwo_coset domain_half_coset, uint32_t* const* d_cols,
                                      uint32_t n_cols, void* stream) {
