@@ -485,8 +485,10 @@ int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* c
 // Register-only throughput of the butterfly above: each thread keeps 16 words and 15 doubled
 // twiddles in registers and runs `rounds` rounds of 4 forward layers (the shape of one register
 // round of k_fft_tile), with no memory traffic in the loop. Its rate is the integer-datapath
-// bound of the circle FFT on this device.
-__global__ void __launch_bounds__(256) k_butterfly_probe(const uint32_t* in, uint32_t* out, uint32_t rounds) {
+// bound of the circle FFT on this device. Compiled for 4 to 6 resident blocks per SM (the register
+// budget decides how many warps hide the butterflies' dependency chains); the best is reported.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_butterfly_probe(const uint32_t* in, uint32_t* out, uint32_t rounds) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
   uint32_t v[16], t[15];
 #pragma unroll
@@ -517,38 +519,44 @@ extern "C" {
 stwo_status stwo_butterfly_rate(uint32_t rounds, double* h_butterflies_per_s, void* stream) {
   STWO_REQUIRE(h_butterflies_per_s && rounds >= 1 && rounds <= (1u << 16), "need 1 <= rounds <= 65536");
   cudaStream_t s = as_stream(stream);
-  int per_sm = 0;
-  STWO_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_butterfly_probe, 256, 0));
-  // One full wave: every SM holds as many blocks as fit, so elapsed time equals active time.
-  const uint32_t blocks = (uint32_t)std::max(1, per_sm) * (uint32_t)sm_count();
-  const size_t words = (size_t)blocks * 256 * 16;
-  uint32_t* d = nullptr;
-  int32_t st = scratch_alloc((void**)&d, words * 8, s);
-  if (st) return st;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  cudaError_t err = cudaMemsetAsync(d, 0x5a, words * 4, s);
-  if (!err) err = cudaEventCreate(&e0);
-  if (!err) err = cudaEventCreate(&e1);
-  float ms = 0.f;
-  if (!err) {
-    k_butterfly_probe<<<blocks, 256, 0, s>>>(d, d + words, rounds);  // warm-up
-    cudaEventRecord(e0, s);
-    k_butterfly_probe<<<blocks, 256, 0, s>>>(d, d + words, rounds);
-    cudaEventRecord(e1, s);
-    note_launch();
-    note_launch();
-    err = cudaGetLastError();
-    if (!err) err = cudaEventSynchronize(e1);
-    if (!err) err = cudaEventElapsedTime(&ms, e0, e1);
+  double best = 0.0;
+  for (int variant = 0; variant < 3; variant++) {
+    void (*kern)(const uint32_t*, uint32_t*, uint32_t) =
+        variant == 0 ? k_butterfly_probe<4> : variant == 1 ? k_butterfly_probe<5> : k_butterfly_probe<6>;
+    int per_sm = 0;
+    STWO_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+    // One full wave: every SM holds as many blocks as fit, so elapsed time equals active time.
+    const uint32_t blocks = (uint32_t)std::max(1, per_sm) * (uint32_t)sm_count();
+    const size_t words = (size_t)blocks * 256 * 16;
+    uint32_t* d = nullptr;
+    int32_t st = scratch_alloc((void**)&d, words * 8, s);
+    if (st) return st;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaMemsetAsync(d, 0x5a, words * 4, s);
+    if (!err) err = cudaEventCreate(&e0);
+    if (!err) err = cudaEventCreate(&e1);
+    float ms = 0.f;
+    if (!err) {
+      kern<<<blocks, 256, 0, s>>>(d, d + words, rounds);  // warm-up
+      cudaEventRecord(e0, s);
+      kern<<<blocks, 256, 0, s>>>(d, d + words, rounds);
+      cudaEventRecord(e1, s);
+      note_launch();
+      note_launch();
+      err = cudaGetLastError();
+      if (!err) err = cudaEventSynchronize(e1);
+      if (!err) err = cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    scratch_free(d, s);
+    if (err) {
+      set_error("butterfly_rate: %s", cudaGetErrorString(err));
+      return STWO_ERR_CUDA;
+    }
+    best = std::max(best, (double)blocks * 256.0 * rounds * 32.0 / (ms * 1e-3));
   }
-  if (e0) cudaEventDestroy(e0);
-  if (e1) cudaEventDestroy(e1);
-  scratch_free(d, s);
-  if (err) {
-    set_error("butterfly_rate: %s", cudaGetErrorString(err));
-    return STWO_ERR_CUDA;
-  }
-  *h_butterflies_per_s = (double)blocks * 256.0 * rounds * 32.0 / (ms * 1e-3);
+  *h_butterflies_per_s = best;
   return STWO_OK;
 }
 

@@ -66,29 +66,36 @@ __global__ void __launch_bounds__(256) k_point_tables(const stwo_qm31_point* __r
 // One block per (chunk of 2^(EP_LOW + mid_max) coefficients, evaluation). With `tables` the
 // point's mappings and products come from k_point_tables (table_of[e] names the evaluation's
 // entry); without, the block derives them from points[e].
+// With `work`, block b evaluates chunk work[2b + 1] of evaluation work[2b] (a flat list of the
+// chunks that exist, so polynomials of different sizes launch no idle blocks); without, the grid is
+// (chunks of the largest polynomial, evaluations) and blocks past a polynomial's chunks return.
 __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict__ jobs, const uint32_t* __restrict__ poly_of,
                                                        const stwo_qm31_point* __restrict__ points,
                                                        const qm31* __restrict__ tables,
                                                        const uint32_t* __restrict__ table_of, uint32_t mid_max,
-                                                       unsigned long long* __restrict__ acc) {
+                                                       unsigned long long* __restrict__ acc,
+                                                       const uint32_t* __restrict__ work = nullptr) {
   __shared__ qm31 s_map[32];
   __shared__ qm31 s_mid[1 << EP_MID];
   __shared__ qm31 s_part[8];
   __shared__ EvalJob s_job;
-  __shared__ uint32_t s_table;
-  const uint32_t e = blockIdx.y;
+  __shared__ uint32_t s_table, s_e, s_chunk;
   if (threadIdx.x == 0) {
-    s_job = jobs[poly_of[e]];  // one read of the (possibly host-mapped) tables
-    if (tables) s_table = table_of[e];
+    const uint32_t e0 = work ? work[2 * blockIdx.x] : blockIdx.y;
+    s_e = e0;
+    s_chunk = work ? work[2 * blockIdx.x + 1] : blockIdx.x;
+    s_job = jobs[poly_of[e0]];  // one read of the (possibly host-mapped) tables
+    if (tables) s_table = table_of[e0];
   }
   __syncthreads();
+  const uint32_t e = s_e, chunk = s_chunk;
   const EvalJob job = s_job;
   const uint32_t L = job.log_size;
   const uint32_t lo_bits = L < EP_LOW ? L : EP_LOW;
   const uint32_t mid_bits = L - lo_bits < mid_max ? L - lo_bits : mid_max;
   const uint32_t chunk_bits = lo_bits + mid_bits;
   const uint32_t n_chunks = 1u << (L - chunk_bits);
-  if (blockIdx.x >= n_chunks) return;
+  if (chunk >= n_chunks) return;
   const qm31* T = tables ? tables + (size_t)s_table * EP_TABLE : nullptr;
   if (T) {
     if (threadIdx.x < EP_MAPS) s_map[threadIdx.x] = T[threadIdx.x];
@@ -107,7 +114,7 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
   qm31 res = qm31_zero();
   const uint32_t t = threadIdx.x;
   if (t < (1u << lo_bits)) {
-    const uint32_t* c = job.coeffs + ((size_t)blockIdx.x << chunk_bits);
+    const uint32_t* c = job.coeffs + ((size_t)chunk << chunk_bits);
     unsigned long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
     // Products are at most (P - 1)^2 < 2^62 - 2^33 + 4, and a folded sum is below 2^33 + 2^31:
     // folding after every fourth product keeps the sums below 2^64. Eight coefficient loads are
@@ -170,7 +177,7 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
     for (uint32_t i = 0; i < blockDim.x / 32; i++) sum = qm31_add(sum, s_part[i]);
     qm31 top = qm31_from_u32(1, 0, 0, 0);
     for (uint32_t b = chunk_bits; b < L; b++)
-      if ((blockIdx.x >> (b - chunk_bits)) & 1) top = qm31_mul(top, s_map[b]);
+      if ((chunk >> (b - chunk_bits)) & 1) top = qm31_mul(top, s_map[b]);
     sum = qm31_mul(sum, top);
     atomicAdd(acc + 4 * e + 0, (unsigned long long)sum.a.a);
     atomicAdd(acc + 4 * e + 1, (unsigned long long)sum.a.b);
@@ -195,17 +202,11 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
   if (n_evals == 0) return STWO_OK;
   STWO_REQUIRE(coeffs && log_sizes && poly_of && points && out, "null argument");
   std::vector<EvalJob> jobs(n_polys);
-  uint32_t max_chunks = 1;
   for (uint32_t i = 0; i < n_polys; i++) {
     STWO_REQUIRE(log_sizes[i] <= 30, "poly log size %u > 30", log_sizes[i]);
     jobs[i] = {coeffs[i], log_sizes[i], 0};
   }
-  for (uint32_t e = 0; e < n_evals; e++) {
-    STWO_REQUIRE(poly_of[e] < n_polys, "poly index out of range");
-    uint32_t L = log_sizes[poly_of[e]];
-    uint32_t cb = std::min(L, EP_LOW) + std::min(L - std::min(L, EP_LOW), EP_MID_TABLES);
-    max_chunks = std::max(max_chunks, 1u << (L - cb));
-  }
+  for (uint32_t e = 0; e < n_evals; e++) STWO_REQUIRE(poly_of[e] < n_polys, "poly index out of range");
   STWO_REQUIRE(n_evals <= 65535, "too many evaluations in one call");
   // Evaluations share a handful of points (the mask offsets of one OODS point): the point tables
   // are built once per distinct point.
@@ -230,13 +231,25 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
   const size_t w_tabof = w_polyof;
   const size_t w_pts = (size_t)n_pts * sizeof(stwo_qm31_point) / 4;
   const size_t w_out = (size_t)n_evals * 4;
+  std::vector<uint32_t> work;  // (evaluation, chunk) of every block
+  for (uint32_t e = 0; e < n_evals; e++) {
+    const uint32_t L = log_sizes[poly_of[e]];
+    const uint32_t cb = std::min(L, EP_LOW) + std::min(L - std::min(L, EP_LOW), EP_MID_TABLES);
+    for (uint32_t c = 0; c < (1u << (L - cb)); c++) {
+      work.push_back(e);
+      work.push_back(c);
+    }
+  }
+  STWO_REQUIRE(work.size() / 2 <= 0x7fffffffu, "too many chunks");
   Mapped mp;
-  int32_t st = mapped_words(w_jobs + w_polyof + w_tabof + w_pts + w_out, mp);
+  int32_t st = mapped_words(w_jobs + w_polyof + w_tabof + w_pts + w_out + work.size(), mp);
   if (st) return st;
   uint32_t* h_polyof = mp.host + w_jobs;
   uint32_t* h_tabof = h_polyof + w_polyof;
   uint32_t* h_pts = h_tabof + w_tabof;
   uint32_t* h_out = h_pts + w_pts;
+  uint32_t* h_work = h_out + w_out;
+  std::memcpy(h_work, work.data(), work.size() * 4);
   std::memcpy(mp.host, jobs.data(), jobs.size() * sizeof(EvalJob));
   std::memcpy(h_polyof, poly_of, (size_t)n_evals * 4);
   std::memcpy(h_tabof, table_of.data(), (size_t)n_evals * 4);
@@ -256,9 +269,9 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
     err = cudaGetLastError();
   }
   if (!err) {
-    dim3 grid(max_chunks, n_evals);
-    k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<const EvalJob*>(mp.dev), dev(h_polyof), nullptr, tables,
-                                         dev(h_tabof), EP_MID_TABLES, acc);
+    k_eval_at_point<<<(uint32_t)(work.size() / 2), 256, 0, s>>>(reinterpret_cast<const EvalJob*>(mp.dev),
+                                                                dev(h_polyof), nullptr, tables, dev(h_tabof),
+                                                                EP_MID_TABLES, acc, dev(h_work));
     note_launch();
     err = cudaGetLastError();
   }
