@@ -42,7 +42,6 @@ __device__ __forceinline__ void ibfly2(uint32_t& v0, uint32_t& v1, uint32_t it2)
 }
 
 constexpr uint32_t FFT_TMAX = 12;   // contiguous tile: 2^12 words = 16 KB (+ padding)
-constexpr uint32_t FFT_TMAX_STRIDED = 13;
 constexpr uint32_t FFT_R = 4;        // 2^4 words per thread, 4 layers per register round
 
 struct FftPass {
