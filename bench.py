@@ -111,6 +111,30 @@ class ClockSampler:
                 "samples": len(sm), "period_ms": self.period_ms}
 
 
+def int_bound(kind, achieved, clocks, local):
+    """Integer-datapath bound of a stage from the library's register-only probe of its inner
+    operation (`kind` "butterfly" or "blake2s"): the probe's issue cost in SM cycles per warp-wide
+    operation, times 4 schedulers x SMs x the SM clock sampled during the timed region."""
+    import torch
+
+    from stwo_gb300 import _lib
+
+    rate, cyc, pmhz = C.c_double(), C.c_double(), C.c_double()
+    fn, rounds = {"butterfly": ("stwo_butterfly_rate", 512), "blake2s": ("stwo_blake2s_rate", 256)}[kind]
+    _lib.call(fn, rounds, C.byref(rate), C.byref(cyc), C.byref(pmhz), None)
+    csum = clocks or {}
+    mhz = csum.get("sm_mhz") or csum.get("sm_max_mhz") or 2070.0
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    bound = 4 * n_sm * mhz * 1e6 * 32 / cyc.value
+    unit = {"butterfly": "butterflies/s", "blake2s": "compressions/s"}[kind]
+    return {"unit": unit, "achieved": achieved, "peak": bound, "frac": achieved / bound,
+            "cycles_per_warp_op": cyc.value, "sm_mhz": mhz, "sms": n_sm,
+            "probe_rate_event_timed": rate.value, "probe_sm_mhz": pmhz.value,
+            "peak_source": f"{fn}: the library's {kind} with every operand in registers, one full wave of "
+                           "blocks; its issue cost in SM cycles (clock64 per block) x 4 schedulers x SMs x "
+                           "the SM clock sampled during the timed region"}
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -522,6 +546,12 @@ def run_batch(args, world, rank, local, lib, barrier, max_over_ranks):
                   "runs_ms": [round(t * 1e3, 3) for t, _ in plains],
                   "note": "the same jobs one at a time (one worker)"},
         "speedup_vs_plain": plain_s / step_s,
+        # Where plain mode's time goes: the proofs whose solo run is long enough to fill the GPU,
+        # and the rest (latency-bound chains of short kernels that batching overlaps).
+        "plain_breakdown": {
+            "solo_ms_of_jobs_over_1ms": round(sum(r.run_ms for r in plain_res if r.run_ms >= 1.0), 3),
+            "jobs_over_1ms": sum(1 for r in plain_res if r.run_ms >= 1.0),
+            "solo_ms_of_other_jobs": round(sum(r.run_ms for r in plain_res if r.run_ms < 1.0), 3)},
         "proofs_identical_to_plain": same,
         "trace_cells_per_s": wl.cells * world / step_s,
         "latency_ms_in_batch": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
@@ -883,14 +913,9 @@ def run_gb300(args):
             # What actually bounds the stage: the butterfly's integer datapath. The composition
             # extension evaluates each column of 2^LOG coefficients on the 2^(LOG + 2)-point
             # domain, four sub-domains of LOG layers of 2^(LOG - 1) butterflies each.
-            rate = C.c_double()
-            _lib.call("stwo_butterfly_rate", 512, C.byref(rate), None)
             bfly = wl.TRACE_COLS * 4 * wl.LOG * (1 << (wl.LOG - 1))
-            got = bfly / (hbm_stages[dom] / 1e3)
-            roof["int_bound"] = {"unit": "butterflies/s", "achieved": got, "peak": rate.value,
-                                 "frac": got / rate.value, "butterflies_per_launch": bfly,
-                                 "peak_source": "stwo_butterfly_rate: the library's butterfly with every operand "
-                                                "in registers, one full wave of blocks"}
+            roof["int_bound"] = int_bound("butterfly", bfly / (hbm_stages[dom] / 1e3), clk.summary(), local)
+            roof["int_bound"]["butterflies_per_launch"] = bfly
     line = {
         "metric": "proof s & trace cells/s (Poseidon2 2^16 rows)",
         "value": wl.cells * world / (step_ms / 1e3),
@@ -1006,8 +1031,7 @@ def run_kernels(args, world, rank, local, lib, barrier, max_over_ranks):
     eval_s = stage_ms[1] / 1e3
     achieved = eval_bytes / eval_s / 1e9
     interp_gbs = wl.N_COLS * 8 * n / (stage_ms[0] / 1e3) / 1e9
-    comp = wl.N_COLS * N * (wl.N_COLS // 16) // wl.N_COLS  # leaf compressions = N * ceil(256/16)
-    comp = N * ((wl.N_COLS + 15) // 16)
+    comp = N * ((wl.N_COLS + 15) // 16)  # leaf compressions = N * ceil(columns / 16)
     line = {
         "metric": "trace cells/s (kernel microbench: interpolate+evaluate 256x2^20 @ blowup 4, "
                   "Blake2s Merkle 256x2^22, FRI fold 2^22->2^4)",
@@ -1033,6 +1057,13 @@ def run_kernels(args, world, rank, local, lib, barrier, max_over_ranks):
                      "algorithmic_bytes_per_call": eval_bytes},
         "interpolate_gbs": interp_gbs,
         "merkle_leaf_compressions_per_s": comp / (stage_ms[2] / 1e3),
+        # Both stages are bound by the integer datapath, not HBM: each against the library's
+        # register-only probe of its inner operation. The evaluation runs 2^b sub-domain FFTs of
+        # LOG layers of 2^(LOG-1) butterflies per column.
+        "int_bound": {
+            "evaluate": int_bound("butterfly", wl.N_COLS * (1 << wl.BLOWUP) * wl.LOG * (1 << (wl.LOG - 1))
+                                  / (stage_ms[1] / 1e3), clk.summary(), local),
+            "merkle_leaves": int_bound("blake2s", comp / (stage_ms[2] / 1e3), clk.summary(), local)},
         "e2e": {"value": wl.cells * world / (e2e_ms / 1e3), "unit": "cells/s",
                 "h2d_bytes_per_step": wl.cells * 4, "d2h_bytes_per_step": 32 + 4 * 4 * (1 << wl.FRI_LAST),
                 "ms_per_step": e2e_ms},

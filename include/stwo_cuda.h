@@ -70,13 +70,23 @@ uint64_t stwo_kernel_launches(void);
  * calling thread, named after the reference's tracing spans ("Extension", "Merkle", ...).
  * stwo_set_stage_timing(1) enables recording (and clears earlier records); stwo_stage_times
  * returns the number of distinct stages and fills up to `cap` names / summed milliseconds. */
-/* Diagnostic without a reference counterpart: the device's rate for the circle-FFT butterfly of
- * the library's FFT kernels with every operand in registers (one full wave of blocks, `rounds`
- * rounds of 32 butterflies per thread, timed on `stream`), in butterflies per second. This is the
- * integer-datapath bound that the FFT passes are measured against. */
-stwo_status stwo_butterfly_rate(uint32_t rounds, double* h_butterflies_per_s, void* stream);
 stwo_status stwo_set_stage_timing(int enable);
 uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap);
+/* Diagnostic without a reference counterpart: the circle-FFT butterfly of the library's FFT
+ * kernels with every operand in registers (one full wave of blocks, `rounds` rounds of 32
+ * butterflies per thread, on `stream`). `h_butterflies_per_s` is its rate from event timing;
+ * `h_cycles_per_warp_butterfly` (may be null) is its issue cost from the SM cycle counter: SM
+ * cycles per warp-wide butterfly on one of the SM's four schedulers, independent of the clock;
+ * `h_probe_sm_mhz` (may be null) is the SM clock the probe ran at (cycle counter over the global
+ * timer). The integer-datapath bound of an FFT pass at SM clock f is 4 x SMs x f x 32 / cost. */
+stwo_status stwo_butterfly_rate(uint32_t rounds, double* h_butterflies_per_s, double* h_cycles_per_warp_butterfly,
+                                double* h_probe_sm_mhz, void* stream);
+/* Diagnostic without a reference counterpart: the same for the BLAKE2s compression of the Merkle
+ * leaf kernels (each thread chains `rounds` compressions of a message held in registers): the
+ * event-timed rate in compressions per second, the issue cost in SM cycles per warp-wide
+ * compression on one scheduler, and the SM clock the probe ran at. */
+stwo_status stwo_blake2s_rate(uint32_t rounds, double* h_compressions_per_s, double* h_cycles_per_warp_compression,
+                              double* h_probe_sm_mhz, void* stream);
 
 /* Column storage: Column::zeros / uninitialized / to_cpu / at
  * (crates/prover/src/core/backend/mod.rs:46-65). */

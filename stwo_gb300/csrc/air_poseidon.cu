@@ -72,6 +72,7 @@ __device__ __forceinline__ void internal_matrix(uint32_t* s) {
 __global__ void __launch_bounds__(32 * PS_REPS) k_poseidon_trace(uint32_t n_rows, const uint32_t* __restrict__ init,
                                                                  uint32_t* __restrict__ trace,
                                                                  uint32_t* __restrict__ lookups) {
+  pdl_enter();
   const uint32_t rep = threadIdx.x >> 5;
   const uint32_t r = blockIdx.x * 32 + (threadIdx.x & 31);
   if (r >= n_rows) return;
@@ -142,6 +143,7 @@ __device__ __forceinline__ qm31 combine16(const LookupConsts& lc, const uint32_t
 
 __global__ void __launch_bounds__(128) k_poseidon_interaction(uint32_t n_rows, const uint32_t* __restrict__ lookups,
                                                               LookupConsts lc, uint32_t* __restrict__ out) {
+  pdl_enter();
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
   size_t n = n_rows;
@@ -166,6 +168,7 @@ __global__ void __launch_bounds__(128) k_poseidon_interaction(uint32_t n_rows, c
 
 // Per-coordinate column sums into 64-bit accumulators.
 __global__ void k_column_sums(const uint32_t* __restrict__ cols, uint32_t n_rows, unsigned long long* acc) {
+  pdl_enter();
   uint32_t k = blockIdx.y;
   const uint32_t* c = cols + (size_t)k * n_rows;
   unsigned long long s = 0;
@@ -187,6 +190,7 @@ __device__ __forceinline__ uint32_t coset_to_storage(uint32_t k, uint32_t log_n)
 // claimed_sum / 2^log_n is taken on the device, so the host needs no read-back here.
 __global__ void k_coset_gather(uint32_t* cols, uint32_t log_n, const unsigned long long* sums, uint32_t inv_n,
                                uint32_t* tmp) {
+  pdl_enter();
   uint32_t k = blockIdx.y;
   uint32_t n = 1u << log_n;
   const uint32_t sh = m31_mul(fold64_p(sums[k]), inv_n);
@@ -194,6 +198,7 @@ __global__ void k_coset_gather(uint32_t* cols, uint32_t log_n, const unsigned lo
     tmp[(size_t)k * n + i] = m31_sub(cols[(size_t)k * n + coset_to_storage(i, log_n)], sh);
 }
 __global__ void k_coset_scatter(uint32_t* cols, uint32_t log_n, const uint32_t* tmp) {
+  pdl_enter();
   uint32_t k = blockIdx.y;
   uint32_t n = 1u << log_n;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -203,6 +208,7 @@ __global__ void k_coset_scatter(uint32_t* cols, uint32_t log_n, const uint32_t* 
 // Inclusive M31 scan of `len` words per row (blockIdx.y) in tiles of 4096 (256 threads x 16).
 // Tile totals go to `sums` (exclusive offsets are applied by k_scan_add).
 __global__ void __launch_bounds__(256) k_scan_tiles(uint32_t* data, uint32_t len, uint32_t* sums, uint32_t n_tiles) {
+  pdl_enter();
   __shared__ uint32_t warp_tot[8];
   uint32_t* d = data + (size_t)blockIdx.y * len;
   uint32_t base = blockIdx.x * 4096 + threadIdx.x * 16;
@@ -232,6 +238,7 @@ __global__ void __launch_bounds__(256) k_scan_tiles(uint32_t* data, uint32_t len
   if (threadIdx.x == 255) sums[(size_t)blockIdx.y * n_tiles + blockIdx.x] = m31_add(excl, run);
 }
 __global__ void k_scan_add(uint32_t* data, uint32_t len, const uint32_t* tile_offsets, uint32_t n_tiles) {
+  pdl_enter();
   uint32_t* d = data + (size_t)blockIdx.y * len;
   uint32_t t = blockIdx.x;
   if (t == 0) return;
@@ -255,6 +262,7 @@ constexpr uint32_t FIN_THREADS = 1024;
 
 __global__ void __launch_bounds__(FIN_THREADS) k_logup_finalize_small(uint32_t* cols, uint32_t log_n, uint32_t inv_n,
                                                                       unsigned long long* sums) {
+  pdl_enter();
   __shared__ unsigned long long s_sum[FIN_THREADS / 32];
   __shared__ uint32_t s_scan[FIN_THREADS / 32];
   __shared__ uint32_t s_shift;
@@ -313,16 +321,16 @@ static int32_t scan_rows(uint32_t* data, uint32_t len, uint32_t rows, Arena& are
   STWO_REQUIRE(n_tiles <= 4096, "scan length too large");
   uint32_t* sums = arena.alloc((size_t)n_tiles * rows);
   if (!sums) return STWO_ERR_OOM;
-  k_scan_tiles<<<dim3(n_tiles, rows), 256, 0, s>>>(data, len, sums, n_tiles);
+  launch_pdl(k_scan_tiles, dim3(n_tiles, rows), dim3(256), 0, s, data, len, sums, n_tiles);
   note_launch();
   STWO_LAUNCH_CHECK();
   if (n_tiles > 1) {
     uint32_t* sums2 = arena.alloc(rows);
     if (!sums2) return STWO_ERR_OOM;
-    k_scan_tiles<<<dim3(1, rows), 256, 0, s>>>(sums, n_tiles, sums2, 1);
+    launch_pdl(k_scan_tiles, dim3(1, rows), dim3(256), 0, s, sums, n_tiles, sums2, 1);
     note_launch();
     STWO_LAUNCH_CHECK();
-    k_scan_add<<<dim3(n_tiles, rows), 256, 0, s>>>(data, len, sums, n_tiles);
+    launch_pdl(k_scan_add, dim3(n_tiles, rows), dim3(256), 0, s, data, len, sums, n_tiles);
     note_launch();
     STWO_LAUNCH_CHECK();
   }
@@ -339,7 +347,7 @@ int32_t logup_finalize_last(uint32_t* last, uint32_t log_n, Arena& arena, cudaSt
   unsigned long long* d_sums = reinterpret_cast<unsigned long long*>(arena.alloc(8));
   if (!d_sums) return STWO_ERR_OOM;
   if (log_n <= FIN_ONE_BLOCK_LOG) {
-    k_logup_finalize_small<<<4, FIN_THREADS, 0, s>>>(last, log_n, h_inv((uint32_t)(n % P)), d_sums);
+    launch_pdl(k_logup_finalize_small, dim3(4), dim3(FIN_THREADS), 0, s, last, log_n, h_inv((uint32_t)(n % P)), d_sums);
     note_launch();
     STWO_LAUNCH_CHECK();
     unsigned long long* hs = small_pinned();
@@ -355,18 +363,18 @@ int32_t logup_finalize_last(uint32_t* last, uint32_t log_n, Arena& arena, cudaSt
   if (!tmp) return STWO_ERR_OOM;
   STWO_CHECK_CUDA(cudaMemsetAsync(d_sums, 0, 32, s));
   const uint32_t g = std::min<uint32_t>((uint32_t)((n + 255) / 256), 1024);
-  k_column_sums<<<dim3(g, 4), 256, 0, s>>>(last, (uint32_t)n, d_sums);
+  launch_pdl(k_column_sums, dim3(g, 4), dim3(256), 0, s, last, (uint32_t)n, d_sums);
   note_launch();
   STWO_LAUNCH_CHECK();
   unsigned long long* hs = small_pinned();
   if (!hs) return STWO_ERR_OOM;
   STWO_CHECK_CUDA(cudaMemcpyAsync(hs, d_sums, 32, cudaMemcpyDeviceToHost, s));
-  k_coset_gather<<<dim3(g, 4), 256, 0, s>>>(last, log_n, d_sums, h_inv((uint32_t)(n % P)), tmp);
+  launch_pdl(k_coset_gather, dim3(g, 4), dim3(256), 0, s, last, log_n, d_sums, h_inv((uint32_t)(n % P)), tmp);
   note_launch();
   STWO_LAUNCH_CHECK();
   int32_t st = scan_rows(tmp, (uint32_t)n, 4, arena, s);
   if (st) return st;
-  k_coset_scatter<<<dim3(g, 4), 256, 0, s>>>(last, log_n, tmp);
+  launch_pdl(k_coset_scatter, dim3(g, 4), dim3(256), 0, s, last, log_n, tmp);
   note_launch();
   STWO_LAUNCH_CHECK();
   if (claimed) {
@@ -412,6 +420,7 @@ __global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
     k_poseidon_composition(const uint32_t* __restrict__ trace, const uint32_t* __restrict__ inter, uint32_t n_rows,
                            PoseidonParams pp, const uint32_t* __restrict__ coeffs, const uint32_t* __restrict__ dinv,
                            uint32_t* o0, uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+  pdl_enter();
   __shared__ uint32_t s_coeffs[4 * PS_N_CONSTRAINTS];
   __shared__ uint32_t s_part[PS_REPS][4][PC_ROWS];
   for (uint32_t i = threadIdx.x; i < 4 * PS_N_CONSTRAINTS; i += blockDim.x) s_coeffs[i] = coeffs[i];
@@ -583,8 +592,8 @@ struct PoseidonGpuAir : GpuAir {
     uint32_t n_rows = 1u << pp.eval_log;
     const uint32_t n_tiles = (n_rows + PC_ROWS - 1) / PC_ROWS;
     const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)sm_count() * PC_BLOCKS_PER_SM);
-    k_poseidon_composition<<<grid, PC_THREADS, 0, s>>>(cols[1][0], cols[2][0], n_rows, pp, coeffs, dinv, acc[0],
-                                                       acc[1], acc[2], acc[3]);
+    launch_pdl(k_poseidon_composition, dim3(grid), dim3(PC_THREADS), 0, s, cols[1][0], cols[2][0], n_rows, pp, coeffs,
+               dinv, acc[0], acc[1], acc[2], acc[3]);
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e) {
@@ -718,7 +727,8 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
     }
     if (!st) {
       StageScope stage("Generation", s);
-      k_poseidon_trace<<<(uint32_t)((n + 31) / 32), 32 * PS_REPS, 0, s>>>((uint32_t)n, d_init, trace, lookups);
+      launch_pdl(k_poseidon_trace, dim3((uint32_t)((n + 31) / 32)), dim3(32 * PS_REPS), 0, s, (uint32_t)n, d_init,
+                 trace, lookups);
       note_launch();
       if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
     }
@@ -743,7 +753,8 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
       for (int i = 0; i < 4; i++) lc.z[i] = le.z.v[i];
       for (int j = 0; j < PS_ST; j++)
         for (int i = 0; i < 4; i++) lc.alpha_pow[j][i] = le.alpha_pow[j].v[i];
-      k_poseidon_interaction<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, lookups, lc, inter);
+      launch_pdl(k_poseidon_interaction, dim3((uint32_t)((n + 127) / 128)), dim3(128), 0, s, (uint32_t)n, lookups, lc,
+                 inter);
       note_launch();
       if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
     }

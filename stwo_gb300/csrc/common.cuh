@@ -199,6 +199,65 @@ struct StageScope {
 // Number of SMs of the current device (152 on GB300).
 int sm_count();
 
+// Register-only throughput probes (diagnostics): a kernel of this signature runs `rounds` rounds of
+// one operation per thread on `words` input words per thread (word i of thread g at in[g + i * n],
+// n = threads), writes its result the same way to `out`, and has thread 0 of each block call
+// probe_record after the loop.
+using RateProbeKernel = void (*)(const uint32_t*, uint32_t*, unsigned long long*, uint32_t);
+struct RateProbe {
+  double ms = 0.0;            // event time of the timed launch
+  double sm_cycles = 0.0;     // median over SMs of the SM's busy cycles (first block start to last end)
+  double warps_per_sm = 0.0;  // warps that ran on that SM
+  double sm_mhz = 0.0;        // SM clock during the loops: block cycles over block nanoseconds
+  uint32_t blocks = 0;        // one full wave by the occupancy calculator: blocks per SM x SMs
+};
+// Launches `kern` twice (warm-up, then timed) with 256-thread blocks.
+int32_t run_rate_probe(RateProbeKernel kern, uint32_t words, uint32_t rounds, cudaStream_t s, RateProbe* r);
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Six words per block: SM id, loop start and end (SM cycle counter), start and end (global ns).
+__device__ __forceinline__ void probe_record(unsigned long long* span, long long c0, unsigned long long g0) {
+  uint32_t smid;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+  unsigned long long* o = span + 6 * blockIdx.x;
+  o[0] = smid;
+  o[1] = (unsigned long long)c0;
+  o[2] = (unsigned long long)clock64();
+  o[3] = g0;
+  o[4] = global_ns();
+  o[5] = 0;
+}
+
+// Programmatic dependent launch. A kernel started by launch_pdl may be scheduled while the kernel
+// before it on the stream is still running; it calls pdl_wait() before it touches memory (that
+// returns once the predecessor has completed and its writes are visible), then pdl_trigger(), which
+// lets its own successor be scheduled in the same way. Both are no-ops for a plain launch. What is
+// saved is the launch and ramp-up gap between dependent kernels of a proof.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_enter() {
+  pdl_wait();
+  pdl_trigger();
+}
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // Pinned host words mapped into the device address space, one growable buffer per host thread:
 // kernels write small results straight into host memory, read after a stream synchronisation.
 struct Mapped {

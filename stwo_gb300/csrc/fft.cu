@@ -137,6 +137,7 @@ __device__ __forceinline__ void fft_round_dispatch(const FftPass& p, uint32_t* s
 template <bool INV, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_fft_pass(FftPass p, ConstColPtrs src, ColPtrs dst) {
   extern __shared__ uint32_t sm[];
+  pdl_enter();
   const uint32_t col = blockIdx.y;
   const uint32_t n_tile = 1u << p.T;
   const uint32_t fixed = tile_fixed_bits(p, blockIdx.x);
@@ -263,6 +264,7 @@ __global__ void __launch_bounds__(1 << (C + NL - 4), 5) k_fft_tile(FftPass p, Co
   constexpr int THREADS = 1 << (T - 4);
   constexpr int PADW = THREADS + THREADS / 32;  // padded stride of consecutive thread rows
   __shared__ uint32_t sm[(1 << T) + (1 << T) / 32 + 1];
+  pdl_enter();
   const uint32_t col = blockIdx.y;
   const uint32_t fixed = tile_fixed_bits(p, blockIdx.x);
   const uint32_t fixed_hi = fixed >> (p.lo + NL);
@@ -309,6 +311,7 @@ __global__ void __launch_bounds__(1 << (C + NL - 4), 5) k_fft_tile(FftPass p, Co
 // and no barrier. Requires lo >= 5.
 template <bool INV, int RB>
 __global__ void __launch_bounds__(256) k_fft_reg(FftPass p, ConstColPtrs src, ColPtrs dst) {
+  pdl_enter();
   const uint32_t col = blockIdx.y;
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;  // < 2^(L - RB)
   // Insert RB zero bits at position lo.
@@ -348,7 +351,7 @@ template <bool INV>
 static bool launch_tile(const FftPass& p, dim3 grid, cudaStream_t s, const ConstColPtrs& sp, const ColPtrs& dp) {
 #define STWO_FFT_CASE(CC, NN)                                                          \
   if (p.c == CC && p.nl == NN) {                                                       \
-    k_fft_tile<INV, CC, NN><<<grid, 1 << (CC + NN - 4), 0, s>>>(p, sp, dp);          \
+    launch_pdl(k_fft_tile<INV, CC, NN>, grid, dim3(1 << (CC + NN - 4)), 0, s, p, sp, dp); \
     return true;                                                                       \
   }
   STWO_FFT_CASE(0, 4) STWO_FFT_CASE(0, 5) STWO_FFT_CASE(0, 6) STWO_FFT_CASE(0, 7) STWO_FFT_CASE(0, 8)
@@ -450,8 +453,8 @@ static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, c
         dim3 g2(1u << (L - p.nl - 8), nc);
 #define STWO_REG_CASE(RB)                                                       \
   if (p.nl == RB) {                                                             \
-    if (inverse) k_fft_reg<true, RB><<<g2, 256, 0, s>>>(p, sp, dp);             \
-    else k_fft_reg<false, RB><<<g2, 256, 0, s>>>(p, sp, dp);                    \
+    if (inverse) launch_pdl(k_fft_reg<true, RB>, g2, dim3(256), 0, s, p, sp, dp);  \
+    else launch_pdl(k_fft_reg<false, RB>, g2, dim3(256), 0, s, p, sp, dp);         \
   }
         STWO_REG_CASE(1) STWO_REG_CASE(2) STWO_REG_CASE(3) STWO_REG_CASE(4)
 #undef STWO_REG_CASE
@@ -460,11 +463,11 @@ static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, c
       if (!done && L >= 3 && p.T >= 4) done = inverse ? launch_tile<true>(p, grid, s, sp, dp) : launch_tile<false>(p, grid, s, sp, dp);
       if (done) {
       } else if (threads <= 256) {
-        if (inverse) k_fft_pass<true, 256><<<grid, threads, smem, s>>>(p, sp, dp);
-        else k_fft_pass<false, 256><<<grid, threads, smem, s>>>(p, sp, dp);
+        if (inverse) launch_pdl(k_fft_pass<true, 256>, grid, dim3(threads), smem, s, p, sp, dp);
+        else launch_pdl(k_fft_pass<false, 256>, grid, dim3(threads), smem, s, p, sp, dp);
       } else {
-        if (inverse) k_fft_pass<true, 512><<<grid, threads, smem, s>>>(p, sp, dp);
-        else k_fft_pass<false, 512><<<grid, threads, smem, s>>>(p, sp, dp);
+        if (inverse) launch_pdl(k_fft_pass<true, 512>, grid, dim3(threads), smem, s, p, sp, dp);
+        else launch_pdl(k_fft_pass<false, 512>, grid, dim3(threads), smem, s, p, sp, dp);
       }
       note_launch();
       STWO_LAUNCH_CHECK();
@@ -486,14 +489,20 @@ int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* c
 // round of k_fft_tile), with no memory traffic in the loop. Its rate is the integer-datapath
 // bound of the circle FFT on this device. Compiled for 4 to 6 resident blocks per SM (the register
 // budget decides how many warps hide the butterflies' dependency chains); the best is reported.
+// Thread 0 of each block records its SM and the cycle counter and global timer around the loop
+// (between two barriers).
 template <int MINB>
-__global__ void __launch_bounds__(256, MINB) k_butterfly_probe(const uint32_t* in, uint32_t* out, uint32_t rounds) {
+__global__ void __launch_bounds__(256, MINB)
+    k_butterfly_probe(const uint32_t* in, uint32_t* out, unsigned long long* span, uint32_t rounds) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
   uint32_t v[16], t[15];
 #pragma unroll
   for (int i = 0; i < 16; i++) v[i] = in[g + i * n];
 #pragma unroll
   for (int i = 0; i < 15; i++) t[i] = 2u * (in[(g * 15 + i) % (16 * n)] % (P - 1));
+  __syncthreads();
+  const unsigned long long g0 = global_ns();
+  const long long c0 = clock64();
   for (uint32_t it = 0; it < rounds; it++) {
     int ti = 0;
 #pragma unroll
@@ -507,6 +516,8 @@ __global__ void __launch_bounds__(256, MINB) k_butterfly_probe(const uint32_t* i
   }
 #pragma unroll
   for (int i = 0; i < 16; i++) out[g + i * n] = v[i];
+  __syncthreads();
+  if (threadIdx.x == 0) probe_record(span, c0, g0);
 }
 
 }  // namespace stwo
@@ -515,47 +526,27 @@ using namespace stwo;
 
 extern "C" {
 
-stwo_status stwo_butterfly_rate(uint32_t rounds, double* h_butterflies_per_s, void* stream) {
+stwo_status stwo_butterfly_rate(uint32_t rounds, double* h_butterflies_per_s, double* h_cycles_per_warp_butterfly,
+                                double* h_probe_sm_mhz, void* stream) {
   STWO_REQUIRE(h_butterflies_per_s && rounds >= 1 && rounds <= (1u << 16), "need 1 <= rounds <= 65536");
-  cudaStream_t s = as_stream(stream);
-  double best = 0.0;
+  double best = 0.0, best_cycles = 0.0, best_mhz = 0.0;
   for (int variant = 0; variant < 3; variant++) {
-    void (*kern)(const uint32_t*, uint32_t*, uint32_t) =
+    RateProbeKernel kern =
         variant == 0 ? k_butterfly_probe<4> : variant == 1 ? k_butterfly_probe<5> : k_butterfly_probe<6>;
-    int per_sm = 0;
-    STWO_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
-    // One full wave: every SM holds as many blocks as fit, so elapsed time equals active time.
-    const uint32_t blocks = (uint32_t)std::max(1, per_sm) * (uint32_t)sm_count();
-    const size_t words = (size_t)blocks * 256 * 16;
-    uint32_t* d = nullptr;
-    int32_t st = scratch_alloc((void**)&d, words * 8, s);
+    RateProbe r;
+    int32_t st = run_rate_probe(kern, 16, rounds, as_stream(stream), &r);
     if (st) return st;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    cudaError_t err = cudaMemsetAsync(d, 0x5a, words * 4, s);
-    if (!err) err = cudaEventCreate(&e0);
-    if (!err) err = cudaEventCreate(&e1);
-    float ms = 0.f;
-    if (!err) {
-      kern<<<blocks, 256, 0, s>>>(d, d + words, rounds);  // warm-up
-      cudaEventRecord(e0, s);
-      kern<<<blocks, 256, 0, s>>>(d, d + words, rounds);
-      cudaEventRecord(e1, s);
-      note_launch();
-      note_launch();
-      err = cudaGetLastError();
-      if (!err) err = cudaEventSynchronize(e1);
-      if (!err) err = cudaEventElapsedTime(&ms, e0, e1);
+    best = std::max(best, (double)r.blocks * 256.0 * rounds * 32.0 / (r.ms * 1e-3));
+    // The SM's four schedulers shared its warps of rounds * 32 butterflies each.
+    const double c = 4.0 * r.sm_cycles / (r.warps_per_sm * rounds * 32.0);
+    if (best_cycles == 0.0 || c < best_cycles) {
+      best_cycles = c;
+      best_mhz = r.sm_mhz;
     }
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
-    scratch_free(d, s);
-    if (err) {
-      set_error("butterfly_rate: %s", cudaGetErrorString(err));
-      return STWO_ERR_CUDA;
-    }
-    best = std::max(best, (double)blocks * 256.0 * rounds * 32.0 / (ms * 1e-3));
   }
   *h_butterflies_per_s = best;
+  if (h_cycles_per_warp_butterfly) *h_cycles_per_warp_butterfly = best_cycles;
+  if (h_probe_sm_mhz) *h_probe_sm_mhz = best_mhz;
   return STWO_OK;
 }
 

@@ -74,6 +74,7 @@ __device__ __forceinline__ void fold_leaf(uint32_t* leaves, uint32_t i, const qm
 
 __global__ void k_fold_line(Secure4 src, Secure4M dst, uint32_t n_out, const uint32_t* __restrict__ itw_level,
                             qm31 alpha, const uint32_t* alpha_dev, uint32_t* leaves) {
+  pdl_enter();
   load_alpha(alpha_dev, alpha, nullptr);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
     qm31 f0, f1;
@@ -90,6 +91,7 @@ __global__ void k_fold_line(Secure4 src, Secure4M dst, uint32_t n_out, const uin
 __global__ void k_fold_circle(Secure4 src, Secure4M dst, uint32_t n_out, const uint32_t* __restrict__ itw_level,
                               uint32_t log_src, uint32_t half_init, uint32_t half_step, qm31 alpha, qm31 alpha_sq,
                               const uint32_t* alpha_dev, uint32_t* leaves) {
+  pdl_enter();
   load_alpha(alpha_dev, alpha, &alpha_sq);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_out; i += gridDim.x * blockDim.x) {
     uint32_t yinv;
@@ -117,6 +119,7 @@ __global__ void k_fold_circle(Secure4 src, Secure4M dst, uint32_t n_out, const u
 // One FRI transcript step on the device (fri.rs:198-214): mix the layer's Merkle root, draw the
 // folding alpha; alpha and alpha^2 go to `alpha_out` (8 words).
 __global__ void k_fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_t* alpha_out) {
+  pdl_enter();
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   d_ch_mix_root(ch, root);
   qm31 a = d_ch_draw_felt(ch);
@@ -127,6 +130,7 @@ __global__ void k_fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_
 
 struct Digest8 { uint32_t w[8]; };
 __global__ void k_channel_set(DevChannel* ch, Digest8 d, uint64_t n_sent) {
+  pdl_enter();
   for (int i = 0; i < 8; i++) ch->digest[i] = d.w[i];
   ch->n_sent_lo = (uint32_t)n_sent;
   ch->n_sent_hi = (uint32_t)(n_sent >> 32);
@@ -201,7 +205,8 @@ int32_t fri_fold_line(const TwiddleTree* tree, stwo_coset line_domain, const uin
   uint32_t n_out = 1u << (line_domain.log_size - 1);
   Secure4 sp{{src[0], src[1], src[2], src[3]}};
   Secure4M dp{{out[0], out[1], out[2], out[3]}};
-  k_fold_line<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, tree->d_itw + off, alpha, alpha_dev, leaves);
+  launch_pdl(k_fold_line, dim3(grid_for(n_out, 256)), dim3(256), 0, s, sp, dp, n_out, tree->d_itw + off, alpha,
+             alpha_dev, leaves);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
@@ -233,8 +238,8 @@ int32_t fri_fold_circle(const TwiddleTree* tree, stwo_coset half, uint32_t* cons
   cmul(a[0], a[1], a[2], a[3], &ab0, &ab1);
   uint32_t rb0 = h_sub(h_add(bb0, bb0), bb1), rb1 = h_add(bb0, h_add(bb1, bb1));
   qm31 a2 = {{h_add(aa0, rb0), h_add(aa1, rb1)}, {h_add(ab0, ab0), h_add(ab1, ab1)}};
-  k_fold_circle<<<grid_for(n_out, 256), 256, 0, s>>>(sp, dp, n_out, lvl, log_src, half.initial_index,
-                                                     half.step_size, alpha, a2, alpha_dev, leaves);
+  launch_pdl(k_fold_circle, dim3(grid_for(n_out, 256)), dim3(256), 0, s, sp, dp, n_out, lvl, log_src,
+             half.initial_index, half.step_size, alpha, a2, alpha_dev, leaves);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
@@ -372,6 +377,7 @@ __device__ qm31 tail_channel_step(DevChannel* c, const uint32_t* root) {
 }
 
 __global__ void __launch_bounds__(FRI_TAIL_THREADS) k_fri_tail(FriTailParams p) {
+  pdl_enter();
   extern __shared__ uint32_t s_nodes[];
   uint32_t* const s_a = s_nodes;                                    // levels k, k - 2, ...
   uint32_t* const s_b = s_nodes + 8 * (1u << FRI_TAIL_MAX_LOG);     // levels k - 1, k - 3, ...
@@ -476,14 +482,14 @@ int32_t fri_tail(const TwiddleTree* tree, const std::vector<stwo_coset>& doms,
       done[dev] = true;
     }
   }
-  k_fri_tail<<<1, FRI_TAIL_THREADS, FRI_TAIL_SMEM, s>>>(p);
+  launch_pdl(k_fri_tail, dim3(1), dim3(FRI_TAIL_THREADS), FRI_TAIL_SMEM, s, p);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
 }
 
 int32_t fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_t* alpha_out, cudaStream_t s) {
-  k_fri_channel_step<<<1, 32, 0, s>>>(ch, root, alpha_out);
+  launch_pdl(k_fri_channel_step, dim3(1), dim3(32), 0, s, ch, root, alpha_out);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
@@ -492,7 +498,7 @@ int32_t fri_channel_step(DevChannel* ch, const uint32_t* root, uint32_t* alpha_o
 int32_t channel_set(DevChannel* ch, const uint32_t digest[8], uint64_t n_sent, cudaStream_t s) {
   Digest8 d;
   for (int i = 0; i < 8; i++) d.w[i] = digest[i];
-  k_channel_set<<<1, 1, 0, s>>>(ch, d, n_sent);
+  launch_pdl(k_channel_set, dim3(1), dim3(1), 0, s, ch, d, n_sent);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;

@@ -24,6 +24,7 @@ __global__ void __launch_bounds__(256) k_merkle_layer(uint32_t n_nodes, const ui
                                                       MerkleCols cols, uint32_t n_cols, uint32_t* __restrict__ out,
                                                       uint32_t* __restrict__ state, uint32_t first, uint32_t last,
                                                       uint32_t one) {
+  pdl_enter();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_nodes) return;
   uint32_t h[8];
@@ -124,9 +125,11 @@ int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint3
     MerkleCols mc;
     for (uint32_t q = 0; q < nc; q++) mc.p[q] = cols[c0 + q];
     if (n <= MERKLE_LAT_NODES)
-      k_merkle_layer<true><<<blocks, threads, 0, s>>>(n, prev, mc, nc, out, state, l == 0, l + 1 == n_launch, 1u);
+      launch_pdl(k_merkle_layer<true>, dim3(blocks), dim3(threads), 0, s, n, prev, mc, nc, out, state, l == 0,
+                 l + 1 == n_launch, 1u);
     else
-      k_merkle_layer<false><<<blocks, threads, 0, s>>>(n, prev, mc, nc, out, state, l == 0, l + 1 == n_launch, 1u);
+      launch_pdl(k_merkle_layer<false>, dim3(blocks), dim3(threads), 0, s, n, prev, mc, nc, out, state, l == 0,
+                 l + 1 == n_launch, 1u);
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -165,6 +168,7 @@ __device__ __forceinline__ void hash_children(const uint32_t* l, const uint32_t*
 __global__ void __launch_bounds__(256) k_merkle_subtrees(const uint32_t* __restrict__ prev, uint32_t first_log,
                                                          uint32_t levels, LayerPtrs outs, DevChannel* ch,
                                                          uint32_t* alpha_out) {
+  pdl_enter();
   __shared__ uint32_t sm[256 * 8];
   const uint32_t t = threadIdx.x;
   const uint32_t node = blockIdx.x * blockDim.x + t;  // node of layer first_log
@@ -231,8 +235,8 @@ int32_t merkle_node_layers(const uint32_t* prev, uint32_t first_log, uint32_t n_
     uint32_t blocks = 1u << (lg - block_log);
     // The channel step rides on the launch that ends at the root (one block, last level 0).
     const bool root_launch = blocks == 1 && lg + 1 == lv;
-    k_merkle_subtrees<<<blocks, threads, 0, s>>>(prev, lg, lv, lp, root_launch ? ch : nullptr,
-                                                 root_launch ? alpha_out : nullptr);
+    launch_pdl(k_merkle_subtrees, dim3(blocks), dim3(threads), 0, s, prev, lg, lv, lp, root_launch ? ch : nullptr,
+               root_launch ? alpha_out : nullptr);
     note_launch();
     STWO_LAUNCH_CHECK();
     prev = out[done + lv - 1];
@@ -261,11 +265,48 @@ __global__ void k_grind(uint32_t d0, uint32_t d1, uint32_t d2, uint32_t d3, uint
   if (tz >= pow_bits) atomicMin(best, (unsigned long long)nonce);
 }
 
+// Register-only throughput of the compression that k_merkle_layer's many-node path runs
+// (b2s_compress_fma): each thread chains `rounds` compressions of a 16-word message into its
+// 8-word state, with no memory traffic in the loop. Its rate is the integer-datapath bound of the
+// Merkle leaf layers on this device. Thread 0 of each block records its SM and the cycle counter
+// and global timer around the loop.
+__global__ void __launch_bounds__(256) k_blake2s_probe(const uint32_t* in, uint32_t* out, unsigned long long* span,
+                                                       uint32_t rounds) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
+  uint32_t h[8], m[16];
+#pragma unroll
+  for (int i = 0; i < 8; i++) h[i] = in[g + i * n];
+#pragma unroll
+  for (int i = 0; i < 16; i++) m[i] = in[g + (8 + i) * n];
+  const uint32_t one = g_b2s_one;
+  __syncthreads();
+  const unsigned long long g0 = global_ns();
+  const long long c0 = clock64();
+  for (uint32_t it = 0; it < rounds; it++) b2s_compress_fma(h, m, 64u * (it + 1), false, one);
+#pragma unroll
+  for (int i = 0; i < 8; i++) out[g + i * n] = h[i];
+  __syncthreads();
+  if (threadIdx.x == 0) probe_record(span, c0, g0);
+}
+
 }  // namespace stwo
 
 using namespace stwo;
 
 extern "C" {
+
+stwo_status stwo_blake2s_rate(uint32_t rounds, double* h_compressions_per_s, double* h_cycles_per_warp_compression,
+                              double* h_probe_sm_mhz, void* stream) {
+  STWO_REQUIRE(h_compressions_per_s && rounds >= 1 && rounds <= (1u << 16), "need 1 <= rounds <= 65536");
+  RateProbe r;
+  int32_t st = run_rate_probe(k_blake2s_probe, 24, rounds, as_stream(stream), &r);
+  if (st) return st;
+  *h_compressions_per_s = (double)r.blocks * 256.0 * rounds / (r.ms * 1e-3);
+  // The SM's four schedulers shared its warps of `rounds` compressions each.
+  if (h_cycles_per_warp_compression) *h_cycles_per_warp_compression = 4.0 * r.sm_cycles / (r.warps_per_sm * rounds);
+  if (h_probe_sm_mhz) *h_probe_sm_mhz = r.sm_mhz;
+  return STWO_OK;
+}
 
 stwo_status stwo_merkle_commit_layer(uint32_t log_size, const uint32_t* d_prev_layer, const uint32_t* const* d_cols,
                                      uint32_t n_cols, uint32_t* d_out, void* stream) {

@@ -48,6 +48,7 @@ constexpr uint32_t EP_MAPS = 30;
 constexpr uint32_t EP_TABLE = EP_MAPS + (1u << EP_LOW) + (1u << EP_MID);
 
 __global__ void __launch_bounds__(256) k_point_tables(const stwo_qm31_point* __restrict__ points, qm31* __restrict__ tables) {
+  pdl_enter();
   __shared__ qm31 s_map[EP_MAPS];
   if (threadIdx.x == 0) point_mappings(points[blockIdx.x], EP_MAPS, s_map);
   __syncthreads();
@@ -75,6 +76,7 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
                                                        const uint32_t* __restrict__ table_of, uint32_t mid_max,
                                                        unsigned long long* __restrict__ acc,
                                                        const uint32_t* __restrict__ work = nullptr) {
+  pdl_enter();
   __shared__ qm31 s_map[32];
   __shared__ qm31 s_mid[1 << EP_MID];
   __shared__ qm31 s_part[8];
@@ -187,6 +189,7 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
 }
 
 __global__ void k_reduce_acc(const unsigned long long* acc, uint32_t n, uint32_t* out) {
+  pdl_enter();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   unsigned long long x = acc[i];
@@ -264,19 +267,20 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
   qm31* tables = reinterpret_cast<qm31*>(scratch + acc_bytes);
   cudaError_t err = cudaMemsetAsync(acc, 0, acc_bytes, s);
   if (!err) {
-    k_point_tables<<<n_pts, 1u << EP_LOW, 0, s>>>(reinterpret_cast<const stwo_qm31_point*>(dev(h_pts)), tables);
+    launch_pdl(k_point_tables, dim3(n_pts), dim3(1u << EP_LOW), 0, s,
+               reinterpret_cast<const stwo_qm31_point*>(dev(h_pts)), tables);
     note_launch();
     err = cudaGetLastError();
   }
   if (!err) {
-    k_eval_at_point<<<(uint32_t)(work.size() / 2), 256, 0, s>>>(reinterpret_cast<const EvalJob*>(mp.dev),
-                                                                dev(h_polyof), nullptr, tables, dev(h_tabof),
-                                                                EP_MID_TABLES, acc, dev(h_work));
+    launch_pdl(k_eval_at_point, dim3((uint32_t)(work.size() / 2)), dim3(256), 0, s,
+               reinterpret_cast<const EvalJob*>(mp.dev), dev(h_polyof), nullptr, tables, dev(h_tabof), EP_MID_TABLES,
+               acc, dev(h_work));
     note_launch();
     err = cudaGetLastError();
   }
   if (!err) {
-    k_reduce_acc<<<(n_evals * 4 + 255) / 256, 256, 0, s>>>(acc, n_evals * 4, dev(h_out));
+    launch_pdl(k_reduce_acc, dim3((n_evals * 4 + 255) / 256), dim3(256), 0, s, acc, n_evals * 4, dev(h_out));
     note_launch();
     err = cudaGetLastError();
   }
@@ -355,16 +359,16 @@ int32_t eval_at_points_noalloc(const uint32_t* const* coeffs, const uint32_t* lo
   if (!err) err = cudaMemsetAsync(buf + NA_OFF_ACC, 0, (size_t)n_evals * 32, s);
   if (!err) {
     dim3 grid(max_chunks, n_evals);
-    k_eval_at_point<<<grid, 256, 0, s>>>(reinterpret_cast<EvalJob*>(buf + NA_OFF_JOBS),
-                                         reinterpret_cast<uint32_t*>(buf + NA_OFF_POLYOF),
-                                         reinterpret_cast<stwo_qm31_point*>(buf + NA_OFF_PTS), nullptr, nullptr,
-                                         EP_MID, reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC));
+    launch_pdl(k_eval_at_point, grid, dim3(256), 0, s, reinterpret_cast<EvalJob*>(buf + NA_OFF_JOBS),
+               reinterpret_cast<uint32_t*>(buf + NA_OFF_POLYOF), reinterpret_cast<stwo_qm31_point*>(buf + NA_OFF_PTS),
+               nullptr, nullptr, EP_MID, reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC), nullptr);
     note_launch();
     err = cudaGetLastError();
   }
   if (!err) {
-    k_reduce_acc<<<(n_evals * 4 + 255) / 256, 256, 0, s>>>(reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC),
-                                                            n_evals * 4, reinterpret_cast<uint32_t*>(buf + NA_OFF_OUT));
+    launch_pdl(k_reduce_acc, dim3((n_evals * 4 + 255) / 256), dim3(256), 0, s,
+               reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC), n_evals * 4,
+               reinterpret_cast<uint32_t*>(buf + NA_OFF_OUT));
     note_launch();
     err = cudaGetLastError();
   }
@@ -404,6 +408,7 @@ __global__ void k_secure_accumulate(uint32_t* a0, uint32_t* a1, uint32_t* a2, ui
 // out[j] = felt^i with j = i, or j = n - 1 - i when `reversed` (highest power first, the order of
 // the composition's random coefficients).
 __global__ void k_secure_powers(qm31 felt, uint32_t n, uint32_t reversed, uint32_t* out) {
+  pdl_enter();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   qm31 r = qm31_from_u32(1, 0, 0, 0), b = felt;
@@ -423,7 +428,7 @@ __global__ void k_secure_powers(qm31 felt, uint32_t n, uint32_t reversed, uint32
 int32_t secure_powers_reversed(const uint32_t felt[4], uint32_t n, uint32_t* out, cudaStream_t s) {
   if (n == 0) return STWO_OK;
   const qm31 f = {{felt[0], felt[1]}, {felt[2], felt[3]}};
-  k_secure_powers<<<(n + 255) / 256, 256, 0, s>>>(f, n, 1u, out);
+  launch_pdl(k_secure_powers, dim3((n + 255) / 256), dim3(256), 0, s, f, n, 1u, out);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;
@@ -494,7 +499,7 @@ stwo_status stwo_generate_secure_powers(stwo_qm31 felt, uint32_t n_powers, stwo_
   int32_t st = scratch_alloc((void**)&d, (size_t)n_powers * 16, s);
   if (st) return st;
   qm31 f = {{felt.v[0], felt.v[1]}, {felt.v[2], felt.v[3]}};
-  k_secure_powers<<<(n_powers + 255) / 256, 256, 0, s>>>(f, n_powers, 0u, d); note_launch();
+  launch_pdl(k_secure_powers, dim3((n_powers + 255) / 256), dim3(256), 0, s, f, n_powers, 0u, d); note_launch();
   cudaError_t e = cudaGetLastError();
   if (!e) e = cudaMemcpyAsync(h_out, d, (size_t)n_powers * 16, cudaMemcpyDeviceToHost, s);
   scratch_free(d, s);

@@ -52,6 +52,7 @@ struct CollectList {
   uint32_t count;
 };
 __global__ void k_collect(CollectList l, uint32_t* out) {
+  pdl_enter();
   uint32_t base = 0;
   for (uint32_t k = 0; k < l.count; k++) {
     for (uint32_t i = threadIdx.x; i < l.n[k]; i += blockDim.x) out[base + i] = l.src[k][i];
@@ -100,6 +101,7 @@ uint32_t* Arena::alloc(size_t words) {
 // Every requested word (values) and 8-word hash, in one launch: request i < nv reads one word,
 // the others one hash. Requests and results live in mapped host memory.
 __global__ void k_gather(const unsigned long long* req, uint32_t nv, uint32_t nh, uint32_t* vout, uint32_t* hout) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nv) {
     vout[i] = reinterpret_cast<const uint32_t*>(req[2 * i])[req[2 * i + 1]];
@@ -131,8 +133,8 @@ int32_t Gather::run(cudaStream_t s) {
     req[2 * (nv + i) + 1] = hidx[i];
   }
   uint32_t* dres = mp.dev + 4 * (nv + nh);
-  k_gather<<<(uint32_t)((nv + nh + 127) / 128), 128, 0, s>>>(reinterpret_cast<const unsigned long long*>(mp.dev),
-                                                             (uint32_t)nv, (uint32_t)nh, dres, dres + nv);
+  launch_pdl(k_gather, dim3((uint32_t)((nv + nh + 127) / 128)), dim3(128), 0, s,
+             reinterpret_cast<const unsigned long long*>(mp.dev), (uint32_t)nv, (uint32_t)nh, dres, dres + nv);
   note_launch();
   cudaError_t e = cudaGetLastError();
   if (!e) e = cudaStreamSynchronize(s);
@@ -833,7 +835,7 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     Mapped mp;
     st = mapped_words(total, mp);
     if (st) return st;
-    k_collect<<<1, 256, 0, s>>>(cl, mp.dev);
+    launch_pdl(k_collect, dim3(1), dim3(256), 0, s, cl, mp.dev);
     note_launch();
     STWO_LAUNCH_CHECK();
     run_check();

@@ -70,21 +70,31 @@ __device__ __forceinline__ qm31 q_pow(qm31 b, uint32_t e) {
 // for the batch's j-th column with value v at point p, alpha_j = rc^(j+1), a_j = conj(v) - v,
 // c = conj(p.y) - p.y, b_j = v c - a_j p.y; the entry keeps alpha_j c, the batch the sums of
 // alpha_j a_j and alpha_j b_j and rc^n. Field sums are exact, so the reduction order is free.
-// A batch can hold every column of a group (1,296 for Poseidon2), each needing rc^(j+1) by a
-// chain of QM31 products: 1024 threads per batch keep that to about one entry per thread.
+// A batch can hold every column of a group (1,296 for Poseidon2). The powers rc^(j+1) come from
+// three tables in shared memory, pw[l][i] = rc^(i * 32^l) for i < 32: two products per entry
+// (exponents of 2^15 and above take the square-and-multiply path).
 constexpr uint32_t QC_THREADS = 1024;
 __global__ void __launch_bounds__(QC_THREADS) k_quotient_coeffs(const QSample* __restrict__ samples, QBatch* batches,
                                                          QEntry* entries, qm31 rc) {
+  pdl_enter();
   __shared__ qm31 s_a[QC_THREADS / 32], s_b[QC_THREADS / 32];
+  __shared__ qm31 s_pw[3][32];
   QBatch& B = batches[blockIdx.x];
   const uint32_t e0 = B.e0, e1 = B.e1;
+  if (threadIdx.x < 96) {
+    const uint32_t l = threadIdx.x >> 5, i = threadIdx.x & 31;
+    s_pw[l][i] = q_pow(q_pow(rc, 1u << (5 * l)), i);
+  }
+  __syncthreads();
   const qm31 py = qm31_from_u32(B.pry[0], B.pry[1], B.piy[0], B.piy[1]);
   const qm31 c = qm31_sub(q_conj(py), py);
   qm31 sa = qm31_zero(), sb = qm31_zero();
   for (uint32_t j = threadIdx.x; j < e1 - e0; j += blockDim.x) {
     const QSample sm = samples[e0 + j];
     const qm31 v = qm31_from_u32(sm.v[0], sm.v[1], sm.v[2], sm.v[3]);
-    const qm31 alpha = q_pow(rc, j + 1);
+    const uint32_t k = j + 1;
+    const qm31 alpha =
+        k < (1u << 15) ? qm31_mul(qm31_mul(s_pw[0][k & 31], s_pw[1][(k >> 5) & 31]), s_pw[2][k >> 10]) : q_pow(rc, k);
     const qm31 a = qm31_sub(q_conj(v), v);
     const qm31 b = qm31_sub(qm31_mul(v, c), qm31_mul(a, py));
     sa = qm31_add(sa, qm31_mul(alpha, a));
@@ -130,6 +140,7 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows(uint32_t rows, 
                                                        const QBatch* __restrict__ batches, uint32_t n_batches,
                                                        const QEntry* __restrict__ entries, uint32_t* o0, uint32_t* o1,
                                                        uint32_t* o2, uint32_t* o3) {
+  pdl_enter();
   __shared__ QStage st[Q_STAGE];
   __shared__ uint32_t part[Q_SLICES][Q_ROWS][4];
   const uint32_t lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
@@ -249,6 +260,7 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows4(uint32_t rows,
                                                                   const QBatch* __restrict__ batches, uint32_t n_batches,
                                                                   const QEntry* __restrict__ entries, uint32_t* o0,
                                                                   uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+  pdl_enter();
   __shared__ QStage st[Q_STAGE];
   __shared__ uint32_t part[Q_SLICES][Q4_ROWS][4];
   const uint32_t lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
@@ -411,7 +423,8 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
   if (!hs.empty() && cudaMemcpyAsync(d_s, hs.data(), hs.size() * sizeof(QSample), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return fail(STWO_ERR_CUDA);
   if (n_batches) {
-    k_quotient_coeffs<<<n_batches, QC_THREADS, 0, s>>>(d_s, d_b, d_e, qm31{{rc.v[0], rc.v[1]}, {rc.v[2], rc.v[3]}});
+    launch_pdl(k_quotient_coeffs, dim3(n_batches), dim3(QC_THREADS), 0, s, d_s, d_b, d_e,
+               qm31{{rc.v[0], rc.v[1]}, {rc.v[2], rc.v[3]}});
     note_launch();
     if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
   }
@@ -423,12 +436,11 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
   bool aligned = rows % Q4_ROWS == 0;
   for (uint32_t c = 0; c < n_cols && aligned; c++) aligned = (reinterpret_cast<uintptr_t>(cols[c]) & 15) == 0;
   if (aligned)
-    k_quotient_rows4<<<rows / Q4_ROWS, Q_SLICES * 32, 0, s>>>(rows, log_n, dom_half.initial_index, dom_half.step_size, qc,
-                                                              d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
+    launch_pdl(k_quotient_rows4, dim3(rows / Q4_ROWS), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
+               dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
   else
-    k_quotient_rows<<<(rows + Q_ROWS - 1) / Q_ROWS, Q_SLICES * 32, 0, s>>>(rows, log_n, dom_half.initial_index,
-                                                                           dom_half.step_size, qc, d_b, n_batches, d_e,
-                                                                           o[0], o[1], o[2], o[3]);
+    launch_pdl(k_quotient_rows, dim3((rows + Q_ROWS - 1) / Q_ROWS), dim3(Q_SLICES * 32), 0, s, rows, log_n,
+               dom_half.initial_index, dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
   note_launch();
   if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
 

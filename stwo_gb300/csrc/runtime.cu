@@ -1,5 +1,6 @@
 // Runtime: errors, device context, stream-ordered buffers and twiddle trees.
 #include "common.cuh"
+#include <array>
 #include <cstdarg>
 #include <atomic>
 #include <chrono>
@@ -71,6 +72,66 @@ static void keep_pool_memory() {
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
   done_dev = dev;
+}
+
+int32_t run_rate_probe(RateProbeKernel kern, uint32_t words, uint32_t rounds, cudaStream_t s, RateProbe* r) {
+  int per_sm = 0;
+  STWO_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+  r->blocks = (uint32_t)std::max(1, per_sm) * (uint32_t)sm_count();
+  const size_t n = (size_t)r->blocks * 256 * words;
+  uint32_t* d = nullptr;
+  int32_t st = scratch_alloc((void**)&d, n * 8 + (size_t)r->blocks * 48, s);
+  if (st) return st;
+  unsigned long long* d_span = reinterpret_cast<unsigned long long*>(d + 2 * n);
+  std::vector<unsigned long long> h(6 * (size_t)r->blocks);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t err = cudaMemsetAsync(d, 0x5a, n * 4, s);
+  if (!err) err = cudaEventCreate(&e0);
+  if (!err) err = cudaEventCreate(&e1);
+  float ms = 0.f;
+  if (!err) {
+    kern<<<r->blocks, 256, 0, s>>>(d, d + n, d_span, rounds);  // warm-up
+    cudaEventRecord(e0, s);
+    kern<<<r->blocks, 256, 0, s>>>(d, d + n, d_span, rounds);
+    cudaEventRecord(e1, s);
+    note_launch();
+    note_launch();
+    err = cudaGetLastError();
+    if (!err) err = cudaMemcpyAsync(h.data(), d_span, h.size() * 8, cudaMemcpyDeviceToHost, s);
+    if (!err) err = cudaStreamSynchronize(s);
+    if (!err) err = cudaEventElapsedTime(&ms, e0, e1);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  scratch_free(d, s);
+  if (err) {
+    set_error("rate probe: %s", cudaGetErrorString(err));
+    return STWO_ERR_CUDA;
+  }
+  // Per SM: busy cycles from its first block's start to its last block's end (the counter is the
+  // SM's own), and the blocks it ran, whatever their residency; the median SM is reported.
+  std::map<unsigned long long, std::array<unsigned long long, 3>> sm;  // min start, max end, blocks
+  double sum_c = 0.0, sum_ns = 0.0;
+  for (uint32_t b = 0; b < r->blocks; b++) {
+    const unsigned long long* o = h.data() + 6 * (size_t)b;
+    auto it = sm.find(o[0]);
+    if (it == sm.end()) it = sm.emplace(o[0], std::array<unsigned long long, 3>{o[1], o[2], 0}).first;
+    it->second[0] = std::min(it->second[0], o[1]);
+    it->second[1] = std::max(it->second[1], o[2]);
+    it->second[2]++;
+    sum_c += (double)(o[2] - o[1]);
+    sum_ns += (double)(o[4] - o[3]);
+  }
+  std::vector<std::pair<double, double>> per;  // (busy cycles per block, blocks) of each SM
+  for (auto& kv : sm) per.push_back({(double)(kv.second[1] - kv.second[0]) / (double)kv.second[2],
+                                     (double)kv.second[2]});
+  std::sort(per.begin(), per.end());
+  const auto& med = per[per.size() / 2];
+  r->ms = ms;
+  r->warps_per_sm = med.second * 8.0;
+  r->sm_cycles = med.first * med.second;
+  r->sm_mhz = sum_ns > 0.0 ? 1e3 * sum_c / sum_ns : 0.0;
+  return STWO_OK;
 }
 
 int32_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {

@@ -260,3 +260,36 @@ def test_accumulate_quotients_unaligned_columns(cuda, oracle):
     want = oracle.accumulate_quotients(log_n, cols, rc, batches, blowup)
     for k in range(4):
         assert np.array_equal(host(out.cols[k]), want[k])
+
+
+def test_butterfly_rate_diagnostic(cuda):
+    """The butterfly probe reports a positive event-timed rate and an issue cost in SM cycles that
+    is consistent with it: the rate cannot exceed what every scheduler issuing one warp-butterfly
+    per that many cycles at the maximum SM clock allows."""
+    import ctypes as C
+
+    import torch
+    from stwo_gb300 import _lib
+
+    rate, cyc, mhz = C.c_double(), C.c_double(), C.c_double()
+    _lib.call("stwo_butterfly_rate", 64, C.byref(rate), C.byref(cyc), C.byref(mhz), None)
+    assert rate.value > 0 and 4.0 < cyc.value < 200.0 and 100.0 < mhz.value < 3000.0
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert rate.value <= 4 * sms * mhz.value * 1.05e6 * 32 / cyc.value
+    with pytest.raises(_lib.StwoError):
+        _lib.call("stwo_butterfly_rate", 0, C.byref(rate), None, None, None)
+
+
+def test_blake2s_rate_diagnostic(cuda):
+    """The BLAKE2s probe: a positive rate, an issue cost per warp-wide compression of at least its
+    ~1,100 integer operations spread over the scheduler's pipes, and a consistent clock."""
+    import ctypes as C
+
+    import torch
+    from stwo_gb300 import _lib
+
+    rate, cyc, mhz = C.c_double(), C.c_double(), C.c_double()
+    _lib.call("stwo_blake2s_rate", 16, C.byref(rate), C.byref(cyc), C.byref(mhz), None)
+    assert rate.value > 0 and 100.0 < cyc.value < 20000.0 and 100.0 < mhz.value < 3000.0
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert rate.value <= 4 * sms * mhz.value * 1.05e6 * 32 / cyc.value
