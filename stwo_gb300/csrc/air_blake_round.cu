@@ -171,6 +171,7 @@ struct BrTraceWriter {
 // inputs: per row 16 state words then 16 message words, or NULL for the reference test's inputs.
 __global__ void __launch_bounds__(128) k_br_trace(uint32_t n_rows, const uint32_t* __restrict__ inputs,
                                                   uint32_t* __restrict__ trace) {
+  pdl_enter();
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
   uint32_t v[BR_ST];
@@ -286,6 +287,7 @@ __device__ __forceinline__ qm31 br_round_denominator(const BrElements* e, const 
 __global__ void __launch_bounds__(128) k_br_interaction_rows(uint32_t n_rows, const uint32_t* __restrict__ inputs,
                                                              const BrElements* __restrict__ e_dev,
                                                              uint32_t* __restrict__ out) {
+  pdl_enter();
   __shared__ BrElements s_e;
   br_stage_elements(e_dev, &s_e);
   __syncthreads();
@@ -336,6 +338,7 @@ __device__ __forceinline__ uint32_t br_rotr(uint32_t x, uint32_t r) { return (x 
 __global__ void __launch_bounds__(256) k_br_interaction_warps(uint32_t n_rows, const uint32_t* __restrict__ inputs,
                                                               const BrElements* __restrict__ e_dev,
                                                               uint32_t* __restrict__ out) {
+  pdl_enter();
   __shared__ BrElements s_e;
   __shared__ qm31 s_tot[8][BI_ROWS];
   br_stage_elements(e_dev, &s_e);
@@ -541,6 +544,7 @@ __global__ void __launch_bounds__(128, 4) k_br_composition(const uint32_t* __res
                                                         const uint32_t* __restrict__ coeffs,
                                                         const uint32_t* __restrict__ dinv, uint32_t* o0,
                                                         uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+  pdl_enter();
   __shared__ uint32_t s_coeffs[4 * BR_N_CONSTRAINTS];
   __shared__ BrElements s_e;
   for (uint32_t i = threadIdx.x; i < 4 * BR_N_CONSTRAINTS; i += blockDim.x) s_coeffs[i] = coeffs[i];
@@ -693,8 +697,8 @@ struct BlakeRoundGpuAir : GpuAir {
     cudaError_t e = cudaMemcpyAsync(de, &he, sizeof(BrElements), cudaMemcpyHostToDevice, s);
     const uint32_t n_rows = 1u << el_log;
     if (!e) {
-      k_br_composition<<<(n_rows + 127) / 128, 128, 0, s>>>(cols[1][0], cols[2][0], n_rows, pp, de, coeffs, dinv,
-                                                            acc[0], acc[1], acc[2], acc[3]);
+      launch_pdl(k_br_composition, dim3((n_rows + 127) / 128), dim3(128), 0, s, cols[1][0], cols[2][0], n_rows, pp, de,
+                 coeffs, dinv, acc[0], acc[1], acc[2], acc[3]);
       note_launch();
       e = cudaGetLastError();
     }
@@ -877,7 +881,7 @@ extern "C" stwo_status stwo_prove_blake_round(uint32_t log_n_rows, const uint32_
     }
     if (!st) {
       StageScope stage("Generation", s);
-      k_br_trace<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_inputs, trace);
+      launch_pdl(k_br_trace, dim3((uint32_t)((n + 127) / 128)), dim3(128), 0, s, (uint32_t)n, d_inputs, trace);
       note_launch();
       if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
     }
@@ -899,10 +903,11 @@ extern "C" stwo_status stwo_prove_blake_round(uint32_t log_n_rows, const uint32_
         st = STWO_ERR_CUDA;
       if (!st) {
         if (log_n_rows <= BI_WARPS_MAX_LOG)
-          k_br_interaction_warps<<<(uint32_t)((n + BI_ROWS - 1) / BI_ROWS), 8 * 32, 0, s>>>((uint32_t)n, d_inputs, de,
-                                                                                          inter);
+          launch_pdl(k_br_interaction_warps, dim3((uint32_t)((n + BI_ROWS - 1) / BI_ROWS)), dim3(8 * 32), 0, s,
+                     (uint32_t)n, d_inputs, de, inter);
         else
-          k_br_interaction_rows<<<(uint32_t)((n + 127) / 128), 128, 0, s>>>((uint32_t)n, d_inputs, de, inter);
+          launch_pdl(k_br_interaction_rows, dim3((uint32_t)((n + 127) / 128)), dim3(128), 0, s, (uint32_t)n, d_inputs, de,
+                     inter);
         note_launch();
         if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;
       }

@@ -20,6 +20,7 @@ __global__ void __launch_bounds__(256) k_wide_fib_composition(ConstColPtrs cols,
                                                               uint32_t trace_log, const uint32_t* __restrict__ coeffs,
                                                               const uint32_t* __restrict__ dinv, uint32_t accumulate,
                                                               uint32_t* o0, uint32_t* o1, uint32_t* o2, uint32_t* o3) {
+  pdl_enter();
   extern __shared__ uint32_t s_coeffs[];
   for (uint32_t i = threadIdx.x; i < 4 * (n_cols - 2); i += blockDim.x) s_coeffs[i] = coeffs[i];
   __syncthreads();
@@ -66,6 +67,7 @@ __global__ void __launch_bounds__(256) k_wide_fib_composition(ConstColPtrs cols,
 // Trace of generate_trace (wide_fibonacci/mod.rs:46-68): row r starts from (a[r], b[r]).
 __global__ void k_wide_fib_trace(const uint32_t* a, const uint32_t* b, uint32_t n_rows, ColPtrs cols,
                                  uint32_t n_cols) {
+  pdl_enter();
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rows) return;
   uint32_t x = a[r], y = b[r];
@@ -98,9 +100,8 @@ struct WideFibGpuAir : GpuAir {
     for (uint32_t i = 0; i < n_cols; i++) cp.p[i] = cols[1][i];
     uint32_t n_rows = 1u << (log_n + 1);
     size_t smem = (size_t)4 * (n_cols - 2) * 4;
-    k_wide_fib_composition<<<(n_rows + 255) / 256, 256, smem, s>>>(cp, n_cols, n_rows, log_n, coeffs, dinv,
-                                                                   accumulate ? 1u : 0u, acc[0], acc[1], acc[2],
-                                                                   acc[3]);
+    launch_pdl(k_wide_fib_composition, dim3((n_rows + 255) / 256), dim3(256), smem, s, cp, n_cols, n_rows, log_n, coeffs,
+               dinv, accumulate ? 1u : 0u, acc[0], acc[1], acc[2], acc[3]);
     note_launch();
     STWO_LAUNCH_CHECK();
     return STWO_OK;
@@ -135,7 +136,7 @@ stwo_status stwo_gen_wide_fib_trace(uint32_t log_n_rows, uint32_t n_cols, const 
   ColPtrs cp;
   for (uint32_t i = 0; i < n_cols; i++) cp.p[i] = d_cols[i];
   uint32_t n = 1u << log_n_rows;
-  k_wide_fib_trace<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(d_a, d_b, n, cp, n_cols);
+  launch_pdl(k_wide_fib_trace, dim3((n + 255) / 256), dim3(256), 0, as_stream(stream), d_a, d_b, n, cp, n_cols);
   note_launch();
   STWO_LAUNCH_CHECK();
   return STWO_OK;

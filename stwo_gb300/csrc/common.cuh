@@ -178,8 +178,10 @@ int32_t scratch_alloc(void** p, size_t bytes, cudaStream_t s);
 void scratch_free(void* p, cudaStream_t s);
 
 // Kernel-parameter tables of column pointers. Kernel parameters may be up to 32 KB on
-// sm_70+, so batches of this many columns travel in the launch itself and need no copy.
-constexpr int MAX_PARAM_COLS = 1024;
+// sm_70+, so batches of this many columns travel in the launch itself and need no copy (two
+// tables of 1,536 pointers are 24 KB). 1,536 keeps the 1,264 trace columns of the Poseidon2 AIR
+// in one launch per FFT pass: one partial last wave instead of two.
+constexpr int MAX_PARAM_COLS = 1536;
 struct ColPtrs { uint32_t* p[MAX_PARAM_COLS]; };
 struct ConstColPtrs { const uint32_t* p[MAX_PARAM_COLS]; };
 

@@ -116,8 +116,10 @@ int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint3
     if (st) return st;
   }
   // A small layer goes out as one-warp blocks, so that its few warps land on different SMs
-  // instead of sharing the issue slots of one.
-  const uint32_t threads = n <= MERKLE_LAT_NODES ? 32 : 256;
+  // instead of sharing the issue slots of one. Larger layers use two-warp blocks: a layer of
+  // 2^17 nodes is then 2,048 blocks, 13-14 per SM, where 256-thread blocks (3 or 4 per SM) left
+  // the SMs with three blocks idle for a quarter of the launch.
+  const uint32_t threads = n <= MERKLE_LAT_NODES ? 32 : 64;
   const uint32_t blocks = (n + threads - 1) / threads;
   for (uint32_t l = 0; l < n_launch; l++) {
     uint32_t c0 = l * per_launch;

@@ -180,6 +180,7 @@ __device__ __forceinline__ f252 load_felt(const uint32_t* p) {
 __global__ void __launch_bounds__(128) k_p252_merkle_layer(uint32_t n_nodes, const uint32_t* __restrict__ prev,
                                                            const uint32_t* const* __restrict__ cols,
                                                            uint32_t n_cols, uint32_t* __restrict__ out) {
+  pdl_enter();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_nodes) return;
   const uint32_t n_children = prev ? 2u : 0u;
@@ -266,7 +267,7 @@ stwo_status stwo_merkle_commit_layer_poseidon252(uint32_t log_size, const uint32
       return STWO_ERR_CUDA;
     }
   }
-  k_p252_merkle_layer<<<(n + 127) / 128, 128, 0, s>>>(n, d_prev_layer, d_tab, n_cols, d_out);
+  launch_pdl(k_p252_merkle_layer, dim3((n + 127) / 128), dim3(128), 0, s, n, d_prev_layer, d_tab, n_cols, d_out);
   note_launch();
   cudaError_t e = cudaGetLastError();
   if (d_tab) scratch_free(d_tab, s);
