@@ -753,7 +753,9 @@ extern "C" stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* 
       for (int i = 0; i < 4; i++) lc.z[i] = le.z.v[i];
       for (int j = 0; j < PS_ST; j++)
         for (int i = 0; i < 4; i++) lc.alpha_pow[j][i] = le.alpha_pow[j].v[i];
-      launch_pdl(k_poseidon_interaction, dim3((uint32_t)((n + 127) / 128)), dim3(128), 0, s, (uint32_t)n, lookups, lc,
+      // Two-warp blocks: 2^16 rows make 1,024 blocks, 6-7 per SM (128-thread blocks left some SMs
+      // with three of four busy for the last quarter of the launch).
+      launch_pdl(k_poseidon_interaction, dim3((uint32_t)((n + 63) / 64)), dim3(64), 0, s, (uint32_t)n, lookups, lc,
                  inter);
       note_launch();
       if (cudaGetLastError() != cudaSuccess) st = STWO_ERR_CUDA;

@@ -249,24 +249,40 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows(uint32_t rows, 
   }
 }
 
-// The same sums with four consecutive rows per lane: one 16-byte load per column gives a warp
-// 512 contiguous bytes of that column (against 128 bytes with a row per lane), so the loads keep
-// longer runs within a DRAM page. Needs 16-byte aligned columns and a multiple of 128 rows.
-// Warps 0-3 finish the batches, one row per lane.
-constexpr int Q4_ROWS = 128;
+// The same sums with RPL (4 or 2) consecutive rows per lane: one 16-byte (8-byte) load per column
+// gives a warp 512 (256) contiguous bytes of that column, against 128 bytes with a row per lane,
+// so the loads keep longer runs within a DRAM page. A block covers 32 RPL rows; two rows per lane
+// give small domains twice the blocks (2^16 rows: 1,024 blocks, 6-7 per SM, where 512 blocks left
+// the SMs with three blocks idle for a quarter of the launch). Needs 4 RPL-byte aligned columns
+// and a multiple of 32 RPL rows. The first RPL warps finish the batches, one row per lane.
+template <int RPL>
+struct QVec;
+template <>
+struct QVec<4> {
+  using T = uint4;
+  static __device__ __forceinline__ void words(const T& v, uint32_t* x) { x[0] = v.x, x[1] = v.y, x[2] = v.z, x[3] = v.w; }
+};
+template <>
+struct QVec<2> {
+  using T = uint2;
+  static __device__ __forceinline__ void words(const T& v, uint32_t* x) { x[0] = v.x, x[1] = v.y; }
+};
 
+template <int RPL>
 __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows4(uint32_t rows, uint32_t log_n, uint32_t half_init,
                                                                   uint32_t half_step, QCols cols,
                                                                   const QBatch* __restrict__ batches, uint32_t n_batches,
                                                                   const QEntry* __restrict__ entries, uint32_t* o0,
                                                                   uint32_t* o1, uint32_t* o2, uint32_t* o3) {
   pdl_enter();
+  using V = typename QVec<RPL>::T;
+  constexpr int BR = 32 * RPL;  // rows per block
   __shared__ QStage st[Q_STAGE];
-  __shared__ uint32_t part[Q_SLICES][Q4_ROWS][4];
+  __shared__ uint32_t part[Q_SLICES][BR][4];
   const uint32_t lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
-  const uint32_t base = blockIdx.x * Q4_ROWS;
-  const uint32_t r0 = base + 4 * lane;  // rows r0 .. r0 + 3 (rows is a multiple of Q4_ROWS)
-  const bool fin = slice < Q4_ROWS / 32;
+  const uint32_t base = blockIdx.x * BR;
+  const uint32_t r0 = base + RPL * lane;  // rows r0 .. r0 + RPL - 1 (rows is a multiple of BR)
+  const bool fin = slice < RPL;
   const uint32_t rf = base + 32 * slice + lane;  // the row a finishing lane owns
   cpoint p = {0u, 0u};
   if (fin) {
@@ -279,21 +295,22 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows4(uint32_t rows,
   qm31 acc = qm31_zero();
   for (uint32_t b = 0; b < n_batches; b++) {
     const QBatch& B = batches[b];
-    unsigned long long s[4][4];
+    unsigned long long s[RPL][4];
 #pragma unroll
-    for (int j = 0; j < 4; j++)
+    for (int j = 0; j < RPL; j++)
 #pragma unroll
       for (int q = 0; q < 4; q++) s[j][q] = 0;
     auto fold_all = [&]() {
 #pragma unroll
-      for (int j = 0; j < 4; j++)
+      for (int j = 0; j < RPL; j++)
 #pragma unroll
         for (int q = 0; q < 4; q++) s[j][q] = fold64(s[j][q]);
     };
-    auto add = [&](const QStage& q, const uint4& v) {
-      const uint32_t x[4] = {v.x, v.y, v.z, v.w};
+    auto add = [&](const QStage& q, const V& v) {
+      uint32_t x[RPL];
+      QVec<RPL>::words(v, x);
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
+      for (int j = 0; j < RPL; j++) {
         s[j][0] += (unsigned long long)q.c[0] * x[j];
         s[j][1] += (unsigned long long)q.c[1] * x[j];
         s[j][2] += (unsigned long long)q.c[2] * x[j];
@@ -313,12 +330,12 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows4(uint32_t rows,
       }
       __syncthreads();
       uint32_t i = slice;
-      // Eight 16-byte loads in flight per iteration; as in k_quotient_rows, a sum takes four
+      // Eight vector loads in flight per iteration; as in k_quotient_rows, a sum takes four
       // products between folds.
       for (; i + 7 * Q_SLICES < ne; i += 8 * Q_SLICES) {
-        uint4 v[8];
+        V v[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) v[u] = __ldg(reinterpret_cast<const uint4*>(st[i + u * Q_SLICES].col + r0));
+        for (int u = 0; u < 8; u++) v[u] = __ldg(reinterpret_cast<const V*>(st[i + u * Q_SLICES].col + r0));
 #pragma unroll
         for (int u = 0; u < 8; u++) {
           add(st[i + u * Q_SLICES], v[u]);
@@ -327,7 +344,7 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows4(uint32_t rows,
       }
       uint32_t cnt = 0;
       for (; i < ne; i += Q_SLICES) {
-        add(st[i], __ldg(reinterpret_cast<const uint4*>(st[i].col + r0)));
+        add(st[i], __ldg(reinterpret_cast<const V*>(st[i].col + r0)));
         if (++cnt == 4) {
           fold_all();
           cnt = 0;
@@ -336,9 +353,9 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows4(uint32_t rows,
       fold_all();  // the next staged group starts from a folded sum
     }
 #pragma unroll
-    for (int j = 0; j < 4; j++)
+    for (int j = 0; j < RPL; j++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) part[slice][4 * lane + j][q] = red64(s[j][q]);
+      for (int q = 0; q < 4; q++) part[slice][RPL * lane + j][q] = red64(s[j][q]);
     __syncthreads();
     if (fin) {
       const uint32_t rl = 32 * slice + lane;
@@ -433,10 +450,16 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
   for (uint32_t c = 0; c < n_cols; c++) qc.p[c] = cols[c];
   uint32_t* o[4];
   for (int q = 0; q < 4; q++) o[q] = direct ? out[q] : d_sub + (size_t)q * rows;
-  bool aligned = rows % Q4_ROWS == 0;
-  for (uint32_t c = 0; c < n_cols && aligned; c++) aligned = (reinterpret_cast<uintptr_t>(cols[c]) & 15) == 0;
-  if (aligned)
-    launch_pdl(k_quotient_rows4, dim3(rows / Q4_ROWS), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
+  // Four rows per lane once the domain gives at least four 128-row blocks per SM, else two.
+  const int rpl = rows >= 4u * 128u * (uint32_t)sm_count() ? 4 : 2;
+  bool aligned = rows % (32 * rpl) == 0;
+  for (uint32_t c = 0; c < n_cols && aligned; c++)
+    aligned = (reinterpret_cast<uintptr_t>(cols[c]) & (4 * rpl - 1)) == 0;
+  if (aligned && rpl == 4)
+    launch_pdl(k_quotient_rows4<4>, dim3(rows / 128), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
+               dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
+  else if (aligned)
+    launch_pdl(k_quotient_rows4<2>, dim3(rows / 64), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
                dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
   else
     launch_pdl(k_quotient_rows, dim3((rows + Q_ROWS - 1) / Q_ROWS), dim3(Q_SLICES * 32), 0, s, rows, log_n,

@@ -114,10 +114,13 @@ def test_eval_at_points(cuda, oracle, log):
         assert g == oracle.eval_at_point(polys[pi], pt)
 
 
+# Layers of at most 2^13 nodes take the latency kernel, larger ones (log 14, 17, 19) the throughput
+# kernel.
 @pytest.mark.parametrize("log,ncols,prev", [(0, 0, False), (0, 0, True), (3, 1, False), (4, 15, True),
                                             (5, 16, False), (5, 17, True), (7, 100, False), (10, 0, True),
                                             (9, 256, True), (2, 33, False), (6, 1300, False), (12, 4, True),
-                                            (3, 3100, True), (2, 6200, False)])
+                                            (3, 3100, True), (2, 6200, False), (14, 37, True), (17, 20, False),
+                                            (19, 3, True)])
 def test_merkle_layer(cuda, oracle, log, ncols, prev):
     import torch
 
@@ -179,8 +182,9 @@ def test_decompose(cuda, oracle, log):
         assert np.array_equal(host(g.cols[k]), wg[k])
 
 
+# Sub-domains below 4 x 128 rows per SM take two rows per lane, larger ones four (log 18, blowup 1).
 @pytest.mark.parametrize("log_n,blowup,ncols,npts", [(3, 1, 2, 1), (6, 1, 3, 2), (7, 1, 5, 2), (8, 2, 4, 3),
-                                                      (10, 1, 40, 2), (12, 1, 7, 1), (13, 3, 9, 2)])
+                                                      (10, 1, 40, 2), (12, 1, 7, 1), (13, 3, 9, 2), (18, 1, 3, 2)])
 def test_accumulate_quotients(cuda, oracle, log_n, blowup, ncols, npts):
     rng = np.random.default_rng(800 + log_n * 13 + ncols)
     cols = [F.rand_m31(rng, 1 << log_n) for _ in range(ncols)]
@@ -245,17 +249,18 @@ def test_invalid_arguments_return_status(cuda):
         cuda.grind([0] * 8, 33)
 
 
-def test_accumulate_quotients_unaligned_columns(cuda, oracle):
-    """Columns that start 4 bytes past a 16-byte boundary take the one-row-per-lane kernel; the
-    result is the same."""
+@pytest.mark.parametrize("shift", [1, 2])
+def test_accumulate_quotients_unaligned_columns(cuda, oracle, shift):
+    """Columns that start 4 bytes past a 16-byte boundary take the one-row-per-lane kernel, and 8
+    bytes past it the two-rows-per-lane kernel; the result is the same."""
     rng = np.random.default_rng(811)
     log_n, blowup, ncols = 12, 1, 9
     cols = [F.rand_m31(rng, 1 << log_n) for _ in range(ncols)]
     pts = sorted(rand_point(oracle, rng) for _ in range(2))
     batches = [(pts[0], [(c, rq(rng)) for c in range(ncols)]), (pts[1], [(c, rq(rng)) for c in range(0, ncols, 3)])]
     rc = rq(rng)
-    shifted = [dev(np.concatenate([np.zeros(1, np.uint32), c]))[1:] for c in cols]
-    assert all(t.data_ptr() % 16 == 4 for t in shifted)
+    shifted = [dev(np.concatenate([np.zeros(shift, np.uint32), c]))[shift:] for c in cols]
+    assert all(t.data_ptr() % 16 == 4 * shift for t in shifted)
     out = cuda.accumulate_quotients(log_n, shifted, rc, batches, blowup)
     want = oracle.accumulate_quotients(log_n, cols, rc, batches, blowup)
     for k in range(4):
