@@ -414,7 +414,7 @@ __device__ __forceinline__ uint32_t prev_row_index(uint32_t r, uint32_t trace_lo
 // loads the coefficient table once per block.
 constexpr uint32_t PC_ROWS = 32;
 constexpr uint32_t PC_THREADS = 32 * PS_REPS;
-constexpr uint32_t PC_BLOCKS_PER_SM = 3;  // 85 registers: the rounds run without spills
+constexpr uint32_t PC_BLOCKS_PER_SM = 4;  // 64 registers: the rounds still run without spills
 
 __global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
     k_poseidon_composition(const uint32_t* __restrict__ trace, const uint32_t* __restrict__ inter, uint32_t n_rows,

@@ -387,9 +387,11 @@ static std::vector<PassPlan> plan_passes(uint32_t F) {
   return v;
 }
 
-// Runs the layers [0, F) of a 2^L-point circle FFT (F == L for interpolation).
+// Runs the layers [0, F) of a 2^L-point circle FFT (F == L for interpolation): the passes
+// [pass_begin, pass_end) of its plan, in execution order (all of them by default).
 static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, const uint32_t* const* src,
-                       uint32_t F, uint32_t* const* dst, uint32_t n_cols, cudaStream_t s) {
+                       uint32_t F, uint32_t* const* dst, uint32_t n_cols, cudaStream_t s, size_t pass_begin = 0,
+                       size_t pass_end = SIZE_MAX) {
   const uint32_t L = half.log_size + 1;
   STWO_REQUIRE(tree, "null twiddle tree");
   STWO_REQUIRE(L <= 30, "domain log size %u > 30", L);
@@ -433,7 +435,7 @@ static int32_t run_fft(const TwiddleTree* tree, stwo_coset half, bool inverse, c
       sp.p[i] = src ? src[c0 + i] : dst[c0 + i];
       dp.p[i] = dst[c0 + i];
     }
-    for (size_t pi = 0; pi < plan.size(); pi++) {
+    for (size_t pi = pass_begin; pi < std::min(pass_end, plan.size()); pi++) {
       FftPass p = base;
       p.lo = plan[pi].lo;
       p.nl = plan[pi].nl;
@@ -482,6 +484,133 @@ int32_t fft_interpolate(const TwiddleTree* tree, stwo_coset half, uint32_t* cons
 int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* const* coeffs, uint32_t coeff_log,
                      uint32_t* const* out, uint32_t n, cudaStream_t s) {
   return run_fft(tree, half, false, coeffs, coeff_log, out, n, s);
+}
+
+// The last interpolation pass and the first evaluation pass in one kernel, for 2^13..2^16-point
+// columns, where both are register passes over the same layers [12, F): a thread loads the 2^RB
+// evaluations g0 + k 2^12, applies the inverse layers and the 1/2^F scale, stores the 2^RB
+// coefficients in place, then for each sub-domain of the evaluation domain applies the forward
+// layers to them and stores that sub-domain's 2^RB words. The coefficients are read from HBM once
+// instead of twice (written by the interpolation, read back by the evaluation).
+template <int RB>
+__global__ void __launch_bounds__(256) k_fft_reg_ie(FftPass pi, FftPass pe, ColPtrs cols, ColPtrs out) {
+  pdl_enter();
+  const uint32_t col = blockIdx.y;
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;  // < 2^(F - RB)
+  const uint32_t lo = pi.lo;
+  const uint32_t g0 = (gid & ((1u << lo) - 1)) | ((gid >> lo) << (lo + RB));
+  uint32_t* c = cols.p[col];
+  uint32_t v[1 << RB];
+#pragma unroll
+  for (int k = 0; k < (1 << RB); k++) v[k] = c[g0 + ((uint32_t)k << lo)];
+#pragma unroll
+  for (int j = 0; j < RB; j++) {
+    const uint32_t layer = lo + j;
+    const uint32_t* twp = pi.tw + (pi.tw_size - (1u << (pi.L - layer))) + (g0 >> (layer + 1));
+#pragma unroll
+    for (int kh = 0; kh < (1 << (RB - 1 - j)); kh++) {
+      const uint32_t t = __ldg(twp + kh);
+      const int k0 = kh << (j + 1);
+#pragma unroll
+      for (int kl = 0; kl < (1 << j); kl++) ibfly2(v[k0 | kl], v[k0 | kl | (1 << j)], t);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < (1 << RB); k++) {
+    v[k] = m31_mul(v[k], pi.scale);
+    c[g0 + ((uint32_t)k << lo)] = v[k];
+  }
+  uint32_t* o = out.p[col];
+  for (uint32_t sub = 0; sub < (1u << (pe.L - pe.F)); sub++) {
+    const uint32_t gs = g0 | (sub << pe.F);
+    uint32_t w[1 << RB];
+#pragma unroll
+    for (int k = 0; k < (1 << RB); k++) w[k] = v[k];
+#pragma unroll
+    for (int jj = 0; jj < RB; jj++) {
+      const int j = RB - 1 - jj;
+      const uint32_t layer = lo + j;
+      const uint32_t* twp = pe.tw + (pe.tw_size - (1u << (pe.L - layer))) + (gs >> (layer + 1));
+#pragma unroll
+      for (int kh = 0; kh < (1 << (RB - 1 - j)); kh++) {
+        const uint32_t t = __ldg(twp + kh);
+        const int k0 = kh << (j + 1);
+#pragma unroll
+        for (int kl = 0; kl < (1 << j); kl++) bfly2(w[k0 | kl], w[k0 | kl | (1 << j)], t);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < (1 << RB); k++) o[gs + ((uint32_t)k << lo)] = w[k];
+  }
+}
+
+// Interpolates n columns of 2^F evaluations on the domain of `src_half` in place (coefficients
+// left in `cols`) and evaluates them on the larger domain of `dst_half` into `out`: the same words
+// as fft_interpolate followed by fft_evaluate. For F in [13, 16] the pass both transforms share
+// runs fused (k_fft_reg_ie). In two steps, so that a caller can time them apart: the first runs
+// the interpolation (up to and including the fused pass, where there is one; `*fused` says which),
+// the second the rest of the evaluation.
+int32_t fft_interpolate_extend_begin(const TwiddleTree* tree_src, stwo_coset src_half, uint32_t* const* cols,
+                                     uint32_t n, const TwiddleTree* tree_dst, stwo_coset dst_half,
+                                     uint32_t* const* out, cudaStream_t s, bool* fused) {
+  const uint32_t F = src_half.log_size + 1, L = dst_half.log_size + 1;
+  STWO_REQUIRE(tree_src && tree_dst && fused, "null argument");
+  STWO_REQUIRE(L >= F && L <= 30, "evaluation domain 2^%u smaller than 2^%u", L, F);
+  *fused = n > 0 && F >= 13 && F <= 16 && coset_is_doubling_of(src_half, tree_src->root) &&
+           coset_is_doubling_of(dst_half, tree_dst->root);
+  if (!*fused) return run_fft(tree_src, src_half, true, nullptr, F, cols, n, s);
+  // Interpolation plan: [0, 12) then [12, F); evaluation plan: [12, F) then [0, 12).
+  int32_t st = run_fft(tree_src, src_half, true, nullptr, F, cols, n, s, 0, 1);
+  if (st) return st;
+  const uint32_t RB = F - 12;
+  FftPass pi{}, pe{};
+  pi.L = F;
+  pi.F = F;
+  pi.lo = 12;
+  pi.nl = RB;
+  pi.tw = tree_src->d_itw2;
+  pi.tw_size = (uint32_t)tree_src->size;
+  pi.scale = h_inv((uint32_t)((1ull << F) % P));
+  pe.L = L;
+  pe.F = F;
+  pe.lo = 12;
+  pe.nl = RB;
+  pe.tw = tree_dst->d_tw2;
+  pe.tw_size = (uint32_t)tree_dst->size;
+  pe.scale = 1u;
+  for (uint32_t c0 = 0; c0 < n; c0 += MAX_PARAM_COLS) {
+    const uint32_t nc = std::min<uint32_t>(MAX_PARAM_COLS, n - c0);
+    ColPtrs cp, op;
+    for (uint32_t i = 0; i < nc; i++) {
+      cp.p[i] = cols[c0 + i];
+      op.p[i] = out[c0 + i];
+    }
+    const dim3 grid(1u << (F - RB - 8), nc);  // one thread per 2^RB-word group: 2^12 per column
+    switch (RB) {
+      case 1: launch_pdl(k_fft_reg_ie<1>, grid, dim3(256), 0, s, pi, pe, cp, op); break;
+      case 2: launch_pdl(k_fft_reg_ie<2>, grid, dim3(256), 0, s, pi, pe, cp, op); break;
+      case 3: launch_pdl(k_fft_reg_ie<3>, grid, dim3(256), 0, s, pi, pe, cp, op); break;
+      default: launch_pdl(k_fft_reg_ie<4>, grid, dim3(256), 0, s, pi, pe, cp, op); break;
+    }
+    note_launch();
+    STWO_LAUNCH_CHECK();
+  }
+  return STWO_OK;
+}
+int32_t fft_interpolate_extend_end(const TwiddleTree* tree_dst, stwo_coset dst_half, uint32_t coeff_log,
+                                   uint32_t* const* cols, uint32_t n, uint32_t* const* out, bool fused,
+                                   cudaStream_t s) {
+  if (fused) return run_fft(tree_dst, dst_half, false, nullptr, coeff_log, out, n, s, 1);
+  std::vector<const uint32_t*> co(cols, cols + n);
+  return run_fft(tree_dst, dst_half, false, co.data(), coeff_log, out, n, s);
+}
+int32_t fft_interpolate_evaluate(const TwiddleTree* tree_src, stwo_coset src_half, uint32_t* const* cols, uint32_t n,
+                                 const TwiddleTree* tree_dst, stwo_coset dst_half, uint32_t* const* out,
+                                 cudaStream_t s) {
+  bool fused = false;
+  int32_t st = fft_interpolate_extend_begin(tree_src, src_half, cols, n, tree_dst, dst_half, out, s, &fused);
+  if (st) return st;
+  return fft_interpolate_extend_end(tree_dst, dst_half, src_half.log_size + 1, cols, n, out, fused, s);
 }
 
 // Register-only throughput of the butterfly above: each thread keeps 16 words and 15 doubled

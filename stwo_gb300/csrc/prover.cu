@@ -23,6 +23,12 @@ namespace stwo {
 int32_t fft_interpolate(const TwiddleTree* tree, stwo_coset half, uint32_t* const* cols, uint32_t n, cudaStream_t s);
 int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* const* coeffs, uint32_t coeff_log,
                      uint32_t* const* out, uint32_t n, cudaStream_t s);
+int32_t fft_interpolate_extend_begin(const TwiddleTree* tree_src, stwo_coset src_half, uint32_t* const* cols,
+                                     uint32_t n, const TwiddleTree* tree_dst, stwo_coset dst_half,
+                                     uint32_t* const* out, cudaStream_t s, bool* fused);
+int32_t fft_interpolate_extend_end(const TwiddleTree* tree_dst, stwo_coset dst_half, uint32_t coeff_log,
+                                   uint32_t* const* cols, uint32_t n, uint32_t* const* out, bool fused,
+                                   cudaStream_t s);
 int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint32_t* const* cols, uint32_t n_cols,
                             uint32_t* out, cudaStream_t s);
 int32_t merkle_node_layers(const uint32_t* prev, uint32_t first_log, uint32_t n_levels, uint32_t* const* out,
@@ -366,32 +372,39 @@ struct Tree {
   DevMerkle merkle;
 };
 
-int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t> logs) {
+int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t> logs,
+                             const std::vector<uint32_t*>* evals) {
   trees.emplace_back();
   Tree& t = trees.back();
   t.polys = std::move(polys);
   t.poly_logs = std::move(logs);
   std::vector<ColRef> refs;
-  // Evaluate all polynomials of the same log size in one batched call.
+  // Evaluate all polynomials of the same log size in one batched call (unless the caller has).
   std::map<uint32_t, std::vector<size_t>> by_log;
   for (size_t i = 0; i < t.polys.size(); i++) by_log[t.poly_logs[i]].push_back(i);
   t.evals.assign(t.polys.size(), nullptr);
   t.eval_logs.assign(t.polys.size(), 0);
-  StageScope stage_ext("Extension", s);
-  for (auto& kv : by_log) {
-    uint32_t el = kv.first + cfg.log_blowup_factor;
-    std::vector<const uint32_t*> src;
-    std::vector<uint32_t*> dst;
-    uint32_t* block = arena.alloc(kv.second.size() << el);
-    if (!block) return STWO_ERR_OOM;
-    for (size_t i : kv.second) {
-      t.evals[i] = block + (dst.size() << el);
-      t.eval_logs[i] = el;
-      src.push_back(t.polys[i]);
-      dst.push_back(t.evals[i]);
+  if (evals) {
+    t.evals = *evals;
+    for (size_t i = 0; i < t.polys.size(); i++) t.eval_logs[i] = t.poly_logs[i] + cfg.log_blowup_factor;
+  } else {
+    StageScope stage_ext("Extension", s);
+    for (auto& kv : by_log) {
+      uint32_t el = kv.first + cfg.log_blowup_factor;
+      std::vector<const uint32_t*> src;
+      std::vector<uint32_t*> dst;
+      uint32_t* block = arena.alloc(kv.second.size() << el);
+      if (!block) return STWO_ERR_OOM;
+      for (size_t i : kv.second) {
+        t.evals[i] = block + (dst.size() << el);
+        t.eval_logs[i] = el;
+        src.push_back(t.polys[i]);
+        dst.push_back(t.evals[i]);
+      }
+      int32_t st =
+          fft_evaluate(tree, canonic_half_coset(el), src.data(), kv.first, dst.data(), (uint32_t)src.size(), s);
+      if (st) return st;
     }
-    int32_t st = fft_evaluate(tree, canonic_half_coset(el), src.data(), kv.first, dst.data(), (uint32_t)src.size(), s);
-    if (st) return st;
   }
   for (size_t i = 0; i < t.evals.size(); i++) refs.push_back({t.evals[i], t.eval_logs[i]});
   StageScope stage_merkle("Merkle", s);
@@ -410,13 +423,30 @@ int32_t Prover::commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t>
 }
 
 int32_t Prover::commit_evals(const std::vector<uint32_t*>& cols, uint32_t log_size) {
-  // Interpolate in place (the evaluation is consumed, as PolyOps::interpolate takes it by value).
-  if (!cols.empty()) {
+  // Interpolate in place (the evaluation is consumed, as PolyOps::interpolate takes it by value),
+  // then evaluate on the blown-up domain; the pass the two transforms share runs fused where it
+  // can (fft_interpolate_extend_begin), so the coefficients are read back from HBM once less.
+  if (cols.empty()) return commit_polys(cols, {});
+  const uint32_t el = log_size + cfg.log_blowup_factor;
+  uint32_t* block = arena.alloc(cols.size() << el);
+  if (!block) return STWO_ERR_OOM;
+  std::vector<uint32_t*> evals(cols.size());
+  for (size_t i = 0; i < cols.size(); i++) evals[i] = block + (i << el);
+  const uint32_t n = (uint32_t)cols.size();
+  bool fused = false;
+  {
     StageScope stage("Interpolation for commitment", s);
-    int32_t st = fft_interpolate(tree, canonic_half_coset(log_size), cols.data(), (uint32_t)cols.size(), s);
+    int32_t st = fft_interpolate_extend_begin(tree, canonic_half_coset(log_size), cols.data(), n, tree,
+                                              canonic_half_coset(el), evals.data(), s, &fused);
     if (st) return st;
   }
-  return commit_polys(cols, std::vector<uint32_t>(cols.size(), log_size));
+  {
+    StageScope stage("Extension", s);
+    int32_t st = fft_interpolate_extend_end(tree, canonic_half_coset(el), log_size, cols.data(), n, evals.data(),
+                                            fused, s);
+    if (st) return st;
+  }
+  return commit_polys(cols, std::vector<uint32_t>(cols.size(), log_size), &evals);
 }
 
 Prover::Prover(const stwo_pcs_config& c, uint32_t max_log, cudaStream_t st) : cfg(c), s(st), arena(st) {

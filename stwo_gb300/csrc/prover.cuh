@@ -124,7 +124,9 @@ struct Prover {
 
   Prover(const stwo_pcs_config& c, uint32_t max_log, cudaStream_t st);
   ~Prover();
-  int32_t commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t> logs);
+  // `evals`, when given, are the polynomials' evaluations on the blown-up domains already.
+  int32_t commit_polys(std::vector<uint32_t*> polys, std::vector<uint32_t> logs,
+                       const std::vector<uint32_t*>* evals = nullptr);
   int32_t commit_evals(const std::vector<uint32_t*>& cols, uint32_t log_size);
   int32_t commit_composition(const GpuAir& air, hq rc);
   int32_t prove(const GpuAir& air, std::vector<uint8_t>& out);

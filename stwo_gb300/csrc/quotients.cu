@@ -18,9 +18,9 @@
 
 namespace stwo {
 
-int32_t fft_interpolate(const TwiddleTree* tree, stwo_coset half, uint32_t* const* cols, uint32_t n, cudaStream_t s);
-int32_t fft_evaluate(const TwiddleTree* tree, stwo_coset half, const uint32_t* const* coeffs, uint32_t coeff_log,
-                     uint32_t* const* out, uint32_t n, cudaStream_t s);
+int32_t fft_interpolate_evaluate(const TwiddleTree* tree_src, stwo_coset src_half, uint32_t* const* cols, uint32_t n,
+                                 const TwiddleTree* tree_dst, stwo_coset dst_half, uint32_t* const* out,
+                                 cudaStream_t s);
 
 struct QBatch {
   uint32_t prx[2], pix[2], pry[2], piy[2];  // CM31 parts of the sample point
@@ -474,11 +474,7 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
     TwiddleTree* t_dom = nullptr;
     st = get_tree(sub_half, s, &t_sub);
     if (!st) st = get_tree(dom_half, s, &t_dom);
-    if (!st) st = fft_interpolate(t_sub, sub_half, o, 4, s);
-    if (!st) {
-      const uint32_t* co[4] = {o[0], o[1], o[2], o[3]};
-      st = fft_evaluate(t_dom, dom_half, co, sub_log, out, 4, s);
-    }
+    if (!st) st = fft_interpolate_evaluate(t_sub, sub_half, o, 4, t_dom, dom_half, out, s);
     if (st) return fail(st);
   }
   scratch_free(scratch, s);

@@ -182,9 +182,11 @@ def test_decompose(cuda, oracle, log):
         assert np.array_equal(host(g.cols[k]), wg[k])
 
 
-# Sub-domains below 4 x 128 rows per SM take two rows per lane, larger ones four (log 18, blowup 1).
+# Sub-domains below 4 x 128 rows per SM take two rows per lane, larger ones four (log 18, blowup 1);
+# sub-domains of 2^13..2^16 rows interpolate and extend with the shared pass fused (log 15).
 @pytest.mark.parametrize("log_n,blowup,ncols,npts", [(3, 1, 2, 1), (6, 1, 3, 2), (7, 1, 5, 2), (8, 2, 4, 3),
-                                                      (10, 1, 40, 2), (12, 1, 7, 1), (13, 3, 9, 2), (18, 1, 3, 2)])
+                                                      (10, 1, 40, 2), (12, 1, 7, 1), (13, 3, 9, 2), (15, 1, 3, 2),
+                                                      (18, 1, 3, 2)])
 def test_accumulate_quotients(cuda, oracle, log_n, blowup, ncols, npts):
     rng = np.random.default_rng(800 + log_n * 13 + ncols)
     cols = [F.rand_m31(rng, 1 << log_n) for _ in range(ncols)]

@@ -13,11 +13,14 @@ def dev(x):
     return torch.from_numpy(np.ascontiguousarray(np.asarray(x, np.uint32)).view(np.int32)).cuda()
 
 
+# Traces of 2^13..2^16 rows interpolate and extend with the shared pass fused (one to four
+# layers in it: 13, 14 with blowup 2, 15); smaller ones run the two transforms apart.
 @pytest.mark.parametrize("log_n,n_cols,cfg", [(2, 100, (5, 1, 0, 3)), (3, 100, (5, 1, 0, 3)),
                                               (5, 100, (5, 1, 0, 3)), (6, 100, (5, 1, 0, 3)),
                                               (8, 100, (5, 1, 0, 3)), (10, 32, (10, 1, 0, 3)),
                                               (7, 20, (3, 2, 1, 5)), (9, 50, (0, 1, 2, 8)),
-                                              (12, 100, (5, 1, 0, 3))])
+                                              (12, 100, (5, 1, 0, 3)), (13, 20, (5, 1, 0, 3)),
+                                              (14, 8, (3, 2, 1, 5)), (15, 4, (5, 1, 0, 3))])
 def test_wide_fib_proof_bytes_match_oracle(cuda, oracle, log_n, n_cols, cfg):
     from stwo_gb300.prover import prove_wide_fib, wide_fib_trace
 
