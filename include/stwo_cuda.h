@@ -286,7 +286,9 @@ stwo_status stwo_prove_wide_fib(uint32_t log_n_rows, uint32_t n_cols, uint32_t* 
 
 /* prove_poseidon (crates/prover/src/examples/poseidon/mod.rs:327-389): 2^log_n_rows rows of 8
  * Poseidon2 permutations. d_init holds the initial states (word ((row * 8 + rep) * 16 + i)), or is
- * NULL for the reference's deterministic inputs (row + i + rep). Trace, lookup elements, LogUp
+ * NULL for the reference's deterministic inputs (row + i + rep). It may be device memory or pinned
+ * host memory (cudaHostAlloc / cudaHostRegister), which the trace kernel reads once, coalesced,
+ * across the host link. Trace, lookup elements, LogUp
  * interaction trace and proof are produced on the device; the claimed LogUp sum (part of the
  * statement the verifier needs) is returned in *h_claimed_sum. */
 stwo_status stwo_prove_poseidon(uint32_t log_n_rows, const uint32_t* d_init, stwo_pcs_config cfg, uint8_t* h_proof,

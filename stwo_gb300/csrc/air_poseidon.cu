@@ -68,20 +68,30 @@ __device__ __forceinline__ void internal_matrix(uint32_t* s) {
 // init: ((row * 8 + rep) * 16 + i) or NULL for the reference inputs (row + i + rep).
 // Warp w of a block computes permutation w of 32 consecutive rows (the layout of
 // k_poseidon_composition): its 158 columns are written with coalesced 128-byte stores, and a
-// small trace takes the latency of one permutation rather than eight.
+// small trace takes the latency of one permutation rather than eight. The block's initial states
+// are one contiguous run of 32 x 8 x 16 words: the block reads it with coalesced loads into shared
+// memory (word w at w + w / 128, so that the lanes' reads of one state word hit distinct banks).
+// `init` may be pinned host memory: the states then cross the host link inside this kernel.
 __global__ void __launch_bounds__(32 * PS_REPS) k_poseidon_trace(uint32_t n_rows, const uint32_t* __restrict__ init,
                                                                  uint32_t* __restrict__ trace,
                                                                  uint32_t* __restrict__ lookups) {
   pdl_enter();
-  const uint32_t rep = threadIdx.x >> 5;
-  const uint32_t r = blockIdx.x * 32 + (threadIdx.x & 31);
+  __shared__ uint32_t s_init[32 * PS_REPS * PS_ST + 32];
+  const uint32_t lane = threadIdx.x & 31, rep = threadIdx.x >> 5;
+  const uint32_t r = blockIdx.x * 32 + lane;
+  if (init) {
+    const uint32_t valid = min(32u, n_rows - blockIdx.x * 32) * PS_REPS * PS_ST;
+    const uint32_t* src = init + (size_t)blockIdx.x * 32 * PS_REPS * PS_ST;
+    for (uint32_t w = threadIdx.x; w < valid; w += blockDim.x) s_init[w + (w >> 7)] = src[w];
+    __syncthreads();
+  }
   if (r >= n_rows) return;
   const size_t n = n_rows;
   uint32_t col = rep * PS_COLS_PER_REP;
   uint32_t s[PS_ST];
 #pragma unroll
   for (int i = 0; i < PS_ST; i++) {
-    s[i] = init ? init[((size_t)r * PS_REPS + rep) * PS_ST + i] : (r + i + rep);
+    s[i] = init ? s_init[(lane * PS_REPS + rep) * PS_ST + i + lane] : (r + i + rep);
     trace[(size_t)col++ * n + r] = s[i];
     lookups[((size_t)rep * 32 + i) * n + r] = s[i];
   }

@@ -49,8 +49,9 @@ def prove_wide_fib(log_n_rows: int, trace: Sequence[torch.Tensor], cfg=DEFAULT_C
 
 
 def prove_poseidon(log_n_rows: int, init=None, cfg=DEFAULT_CONFIG):
-    """Proves the Poseidon2 AIR; `init` is None (reference inputs) or a device int32 tensor of
-    initial states. Returns (proof bytes, claimed LogUp sum)."""
+    """Proves the Poseidon2 AIR; `init` is None (reference inputs) or an int32 tensor of initial
+    states, on the device or in pinned host memory (read by the trace kernel across the host
+    link). Returns (proof bytes, claimed LogUp sum)."""
     from ._lib import QM31
 
     buf = _out()

@@ -65,6 +65,24 @@ def test_poseidon_proof_bytes_match_oracle(cuda, oracle, log_n, seeded, cfg):
     assert ok, why
 
 
+@pytest.mark.parametrize("log_n", [4, 9])
+def test_poseidon_initial_states_from_pinned_host_memory(cuda, oracle, log_n):
+    # The trace kernel reads the initial states straight from pinned host memory (16 rows: half a
+    # block of 32); the proof equals the one from device memory and the oracle's.
+    import torch
+    from stwo_gb300.prover import prove_poseidon
+
+    rng = np.random.default_rng(70 + log_n)
+    init = F.rand_m31(rng, (1 << log_n) * 8 * 16)
+    host = torch.from_numpy(init.view(np.int32)).pin_memory()
+    cfg = (5, 1, 0, 3)
+    want, want_cs = oracle.prove_poseidon(log_n, init, cfg)
+    got_host, cs_host = prove_poseidon(log_n, host, cfg)
+    got_dev, cs_dev = prove_poseidon(log_n, dev(init), cfg)
+    assert cs_host == cs_dev == want_cs
+    assert got_host == got_dev == want
+
+
 def test_poseidon_headline_size_matches_oracle(cuda, oracle):
     # The benchmarked proof itself: 2^16 rows, seeded states, pow_bits 10 (the same generator as
     # bench.py's workload), byte-identical to the oracle's and accepted by its verifier.
