@@ -260,6 +260,21 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
+// A batch of out-of-domain evaluations whose polynomials, and which of a few points each
+// evaluation takes, are known before the points are: eval_plan_build lays out and uploads the job
+// tables (stream-ordered, while the device still works on earlier stages), eval_plan_run takes the
+// points and evaluates, eval_plan_free releases the device block.
+struct EvalPlan {
+  uint32_t n_evals = 0, n_points = 0, n_blocks = 0;
+  unsigned char* d = nullptr;
+  size_t off_polyof = 0, off_pointof = 0, off_work = 0, off_acc = 0, off_tables = 0;
+};
+int32_t eval_plan_build(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
+                        const uint32_t* poly_of, const uint32_t* point_of, uint32_t n_evals, uint32_t n_points,
+                        cudaStream_t s, EvalPlan* plan);
+int32_t eval_plan_run(const EvalPlan& plan, const stwo_qm31_point* points, stwo_qm31* out, cudaStream_t s);
+void eval_plan_free(EvalPlan& plan, cudaStream_t s);
+
 // Pinned host words mapped into the device address space, one growable buffer per host thread:
 // kernels write small results straight into host memory, read after a stream synchronisation.
 struct Mapped {

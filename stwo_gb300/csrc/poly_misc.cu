@@ -47,10 +47,9 @@ __device__ __forceinline__ void point_mappings(const stwo_qm31_point& pt, uint32
 constexpr uint32_t EP_MAPS = 30;
 constexpr uint32_t EP_TABLE = EP_MAPS + (1u << EP_LOW) + (1u << EP_MID);
 
-__global__ void __launch_bounds__(256) k_point_tables(const stwo_qm31_point* __restrict__ points, qm31* __restrict__ tables) {
-  pdl_enter();
+__device__ __forceinline__ void point_tables_block(const stwo_qm31_point& pt, qm31* __restrict__ tables) {
   __shared__ qm31 s_map[EP_MAPS];
-  if (threadIdx.x == 0) point_mappings(points[blockIdx.x], EP_MAPS, s_map);
+  if (threadIdx.x == 0) point_mappings(pt, EP_MAPS, s_map);
   __syncthreads();
   qm31* T = tables + (size_t)blockIdx.x * EP_TABLE;
   const uint32_t t = threadIdx.x;
@@ -62,6 +61,19 @@ __global__ void __launch_bounds__(256) k_point_tables(const stwo_qm31_point* __r
     if ((t >> b) & 1) mid = qm31_mul(mid, s_map[EP_LOW + b]);
   T[EP_MAPS + t] = lo;
   T[EP_MAPS + (1u << EP_LOW) + t] = mid;
+}
+__global__ void __launch_bounds__(256) k_point_tables(const stwo_qm31_point* __restrict__ points, qm31* __restrict__ tables) {
+  pdl_enter();
+  point_tables_block(points[blockIdx.x], tables);
+}
+// The same with the points in the launch parameters (at most EP_PARAM_POINTS).
+constexpr uint32_t EP_PARAM_POINTS = 8;
+struct EvalPoints {
+  stwo_qm31_point p[EP_PARAM_POINTS];
+};
+__global__ void __launch_bounds__(256) k_point_tables_param(EvalPoints pts, qm31* __restrict__ tables) {
+  pdl_enter();
+  point_tables_block(pts.p[blockIdx.x], tables);
 }
 
 // One block per (chunk of 2^(EP_LOW + mid_max) coefficients, evaluation). With `tables` the
@@ -292,6 +304,101 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
   }
   std::memcpy(out, h_out, (size_t)n_evals * 16);
   return STWO_OK;
+}
+
+// ---------------------------------------------------------------- planned evaluation (the prover's OODS)
+int32_t eval_plan_build(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
+                        const uint32_t* poly_of, const uint32_t* point_of, uint32_t n_evals, uint32_t n_points,
+                        cudaStream_t s, EvalPlan* plan) {
+  STWO_REQUIRE(plan && coeffs && log_sizes && poly_of && point_of, "null argument");
+  STWO_REQUIRE(n_evals >= 1, "no evaluations");
+  STWO_REQUIRE(n_points >= 1 && n_points <= EP_PARAM_POINTS, "%u points (at most %u)", n_points, EP_PARAM_POINTS);
+  std::vector<EvalJob> jobs(n_polys);
+  for (uint32_t i = 0; i < n_polys; i++) {
+    STWO_REQUIRE(log_sizes[i] <= 30, "poly log size %u > 30", log_sizes[i]);
+    jobs[i] = {coeffs[i], log_sizes[i], 0};
+  }
+  std::vector<uint32_t> work;  // (evaluation, chunk) of every block
+  for (uint32_t e = 0; e < n_evals; e++) {
+    STWO_REQUIRE(poly_of[e] < n_polys && point_of[e] < n_points, "evaluation %u: index out of range", e);
+    const uint32_t L = log_sizes[poly_of[e]];
+    const uint32_t cb = std::min(L, EP_LOW) + std::min(L - std::min(L, EP_LOW), EP_MID_TABLES);
+    for (uint32_t c = 0; c < (1u << (L - cb)); c++) {
+      work.push_back(e);
+      work.push_back(c);
+    }
+  }
+  STWO_REQUIRE(work.size() / 2 <= 0x7fffffffu, "too many chunks");
+  // One device block: jobs, poly_of, point_of, work (uploaded now), then the 64-bit accumulators
+  // and the point tables (written at run time). Every part starts on a 16-byte boundary.
+  auto up16 = [](size_t b) { return (b + 15) / 16 * 16; };
+  EvalPlan p;
+  p.n_evals = n_evals;
+  p.n_points = n_points;
+  p.n_blocks = (uint32_t)(work.size() / 2);
+  p.off_polyof = up16(jobs.size() * sizeof(EvalJob));
+  p.off_pointof = p.off_polyof + up16((size_t)n_evals * 4);
+  p.off_work = p.off_pointof + up16((size_t)n_evals * 4);
+  p.off_acc = p.off_work + up16(work.size() * 4);
+  p.off_tables = p.off_acc + (size_t)n_evals * 32;
+  const size_t bytes = p.off_tables + (size_t)n_points * EP_TABLE * sizeof(qm31);
+  std::vector<unsigned char> host(p.off_acc, 0);
+  std::memcpy(host.data(), jobs.data(), jobs.size() * sizeof(EvalJob));
+  std::memcpy(host.data() + p.off_polyof, poly_of, (size_t)n_evals * 4);
+  std::memcpy(host.data() + p.off_pointof, point_of, (size_t)n_evals * 4);
+  std::memcpy(host.data() + p.off_work, work.data(), work.size() * 4);
+  int32_t st = scratch_alloc((void**)&p.d, bytes, s);
+  if (st) return st;
+  cudaError_t err = cudaMemcpyAsync(p.d, host.data(), host.size(), cudaMemcpyHostToDevice, s);
+  if (err) {
+    scratch_free(p.d, s);
+    set_error("eval_plan_build: %s", cudaGetErrorString(err));
+    return STWO_ERR_CUDA;
+  }
+  *plan = p;
+  return STWO_OK;
+}
+
+int32_t eval_plan_run(const EvalPlan& p, const stwo_qm31_point* points, stwo_qm31* out, cudaStream_t s) {
+  STWO_REQUIRE(p.d && points && out, "null argument");
+  EvalPoints ep{};
+  for (uint32_t i = 0; i < p.n_points; i++) ep.p[i] = points[i];
+  Mapped mp;
+  int32_t st = mapped_words((size_t)p.n_evals * 4, mp);
+  if (st) return st;
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(p.d + p.off_acc);
+  qm31* tables = reinterpret_cast<qm31*>(p.d + p.off_tables);
+  cudaError_t err = cudaMemsetAsync(acc, 0, (size_t)p.n_evals * 32, s);
+  if (!err) {
+    launch_pdl(k_point_tables_param, dim3(p.n_points), dim3(1u << EP_LOW), 0, s, ep, tables);
+    note_launch();
+    err = cudaGetLastError();
+  }
+  if (!err) {
+    launch_pdl(k_eval_at_point, dim3(p.n_blocks), dim3(256), 0, s, reinterpret_cast<const EvalJob*>(p.d),
+               reinterpret_cast<const uint32_t*>(p.d + p.off_polyof), nullptr, tables,
+               reinterpret_cast<const uint32_t*>(p.d + p.off_pointof), EP_MID_TABLES, acc,
+               reinterpret_cast<const uint32_t*>(p.d + p.off_work));
+    note_launch();
+    err = cudaGetLastError();
+  }
+  if (!err) {
+    launch_pdl(k_reduce_acc, dim3((p.n_evals * 4 + 255) / 256), dim3(256), 0, s, acc, p.n_evals * 4, mp.dev);
+    note_launch();
+    err = cudaGetLastError();
+  }
+  if (!err) err = cudaStreamSynchronize(s);
+  if (err) {
+    set_error("eval_plan_run: %s", cudaGetErrorString(err));
+    return STWO_ERR_CUDA;
+  }
+  std::memcpy(out, mp.host, (size_t)p.n_evals * 16);
+  return STWO_OK;
+}
+
+void eval_plan_free(EvalPlan& p, cudaStream_t s) {
+  if (p.d) scratch_free(p.d, s);
+  p.d = nullptr;
 }
 
 // ---------------------------------------------------------------- eval_at_points without allocation

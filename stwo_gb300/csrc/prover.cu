@@ -68,9 +68,6 @@ __global__ void k_collect(CollectList l, uint32_t* out) {
 // rc^(n-1), ..., rc, 1 as 4-word QM31 values into out (AccumulationOps::generate_secure_powers,
 // reversed).
 int32_t secure_powers_reversed(const uint32_t felt[4], uint32_t n, uint32_t* out, cudaStream_t s);
-int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
-                       const uint32_t* poly_of, const stwo_qm31_point* points, uint32_t n_evals, stwo_qm31* out,
-                       cudaStream_t s);
 
 // ------------------------------------------------------------------------------------------------
 Arena::~Arena() {
@@ -586,9 +583,39 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   // while the device commits the composition polynomial.
   SampleLayout lay;
   bool have_layout = false;
+  // Per column (tree order): coefficients and evaluations with their log sizes; per sample: its
+  // column. With the layout they fix the OODS evaluation's job tables (plan), which upload while
+  // the device still computes the composition commitment.
+  std::vector<const uint32_t*> polys, ceval;
+  std::vector<uint32_t> plogs, clog, poly_of;
+  EvalPlan plan;
+  struct PlanRelease {
+    EvalPlan& p;
+    cudaStream_t s;
+    ~PlanRelease() { eval_plan_free(p, s); }
+  } plan_release{plan, s};
+  int32_t plan_st = STWO_OK;
   before_root_wait = [&] {
     lay = sample_layout(air, trees);
     have_layout = true;
+    const size_t n_cols = lay.col_first.size() - 1;
+    polys.assign(n_cols, nullptr);
+    ceval.assign(n_cols, nullptr);
+    plogs.assign(n_cols, 0);
+    clog.assign(n_cols, 0);
+    poly_of.assign(lay.sample_off.size(), 0);
+    for (size_t t = 0; t < trees.size() && t + 1 < lay.tree_first.size(); t++)
+      for (uint32_t c = lay.tree_first[t]; c < lay.tree_first[t + 1]; c++) {
+        const uint32_t lc = c - lay.tree_first[t];
+        polys[c] = trees[t].polys[lc];
+        plogs[c] = trees[t].poly_logs[lc];
+        ceval[c] = trees[t].evals[lc];
+        clog[c] = trees[t].eval_logs[lc];
+        for (uint32_t e = lay.col_first[c]; e < lay.col_first[c + 1]; e++) poly_of[e] = c;
+      }
+    if (!lay.sample_off.empty())
+      plan_st = eval_plan_build(polys.data(), plogs.data(), (uint32_t)n_cols, poly_of.data(), lay.sample_off.data(),
+                                (uint32_t)lay.sample_off.size(), (uint32_t)lay.offsets.size(), s, &plan);
   };
   hq rc = ch.draw_felt();
   int32_t st = commit_composition(air, rc);
@@ -614,30 +641,17 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   }
   const size_t n_cols = lay.col_first.size() - 1;
   const size_t n_samples = lay.sample_off.size();
+  if (plan_st) return plan_st;
+  STWO_REQUIRE(n_samples > 0 && plan.d, "no OODS samples");
 
-  // Batched OODS evaluation of every sampled polynomial (pcs/prover.rs:89-101).
-  std::vector<const uint32_t*> polys(n_cols);
-  std::vector<uint32_t> plogs(n_cols), poly_of(n_samples);
-  std::vector<const uint32_t*> ceval(n_cols);
-  std::vector<uint32_t> clog(n_cols);
-  std::vector<stwo_qm31_point> qpts(n_samples);
-  for (size_t t = 0; t < trees.size(); t++)
-    for (uint32_t c = lay.tree_first[t]; c < lay.tree_first[t + 1]; c++) {
-      const uint32_t lc = c - lay.tree_first[t];
-      polys[c] = trees[t].polys[lc];
-      plogs[c] = trees[t].poly_logs[lc];
-      ceval[c] = trees[t].evals[lc];
-      clog[c] = trees[t].eval_logs[lc];
-      for (uint32_t e = lay.col_first[c]; e < lay.col_first[c + 1]; e++) {
-        poly_of[e] = c;
-        const HPointQ& q = upts[pid[lay.sample_off[e]]];
-        qpts[e] = {to_sq(q.x), to_sq(q.y)};
-      }
-    }
+  // Batched OODS evaluation of every sampled polynomial (pcs/prover.rs:89-101): the plan's
+  // evaluations take the point of their mask offset.
+  std::vector<stwo_qm31_point> opts(lay.offsets.size());
+  for (size_t i = 0; i < lay.offsets.size(); i++) opts[i] = {to_sq(upts[pid[i]].x), to_sq(upts[pid[i]].y)};
   std::vector<stwo_qm31> svals(n_samples);
   StageScope stage_oods("Evaluate columns out of domain", s);
-  st = eval_at_points(polys.data(), plogs.data(), (uint32_t)n_cols, poly_of.data(), qpts.data(),
-                      (uint32_t)n_samples, svals.data(), s);
+  st = eval_plan_run(plan, opts.data(), svals.data(), s);
+  eval_plan_free(plan, s);
   if (st) return st;
   std::vector<hq> flat(n_samples);
   for (size_t e = 0; e < n_samples; e++) flat[e] = from_sq(svals[e]);

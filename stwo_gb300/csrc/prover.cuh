@@ -10,7 +10,6 @@
 
 namespace stwo {
 
-// Stream-ordered device allocations released together (one proof's working set).
 // Device memory of one proof, released together at its end. Small requests are carved from
 // 32 MiB chunks (256-byte aligned) so that a proof makes a few dozen pool allocations rather
 // than hundreds; large ones get their own.
