@@ -100,17 +100,26 @@ uint32_t* Arena::alloc(size_t words) {
 }
 
 // ------------------------------------------------------------------------------------------------
-// Gather of words from HBM: each request is (device pointer, element index), 1 or 8 words.
-// Every requested word (values) and 8-word hash, in one launch: request i < nv reads one word,
-// the others one hash. Requests and results live in mapped host memory.
-__global__ void k_gather(const unsigned long long* req, uint32_t nv, uint32_t nh, uint32_t* vout, uint32_t* hout) {
+// Gather of words from HBM in one launch. Threads [0, nv) read one value each, [nv, nv + nh) one
+// 8-word hash each; then one block per run reads its `count` strided words. Requests and results
+// live in mapped host memory.
+__global__ void k_gather(const unsigned long long* vreq, uint32_t nv, const unsigned long long* hreq, uint32_t nh,
+                         const unsigned long long* rreq, uint32_t first_run_block, uint32_t* vout, uint32_t* hout) {
   pdl_enter();
+  if (blockIdx.x >= first_run_block) {
+    const unsigned long long* r = rreq + 4 * (size_t)(blockIdx.x - first_run_block);
+    const uint32_t* base = reinterpret_cast<const uint32_t*>(r[0]);
+    const size_t stride = r[1], idx = r[2];
+    const uint32_t slot = (uint32_t)r[3], count = (uint32_t)(r[3] >> 32);
+    for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) vout[slot + k] = base[(size_t)k * stride + idx];
+    return;
+  }
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nv) {
-    vout[i] = reinterpret_cast<const uint32_t*>(req[2 * i])[req[2 * i + 1]];
+    vout[vreq[3 * i + 2]] = reinterpret_cast<const uint32_t*>(vreq[3 * i])[vreq[3 * i + 1]];
   } else if (i < nv + nh) {
     const uint32_t j = i - nv;
-    const uint4* p = reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(req[2 * i]) + req[2 * i + 1] * 8);
+    const uint4* p = reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(hreq[2 * j]) + hreq[2 * j + 1] * 8);
     uint4 a = p[0], b = p[1];
     uint32_t* o = hout + (size_t)j * 8;
     o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
@@ -119,25 +128,27 @@ __global__ void k_gather(const unsigned long long* req, uint32_t nv, uint32_t nh
 }
 
 int32_t Gather::run(cudaStream_t s) {
-  const size_t nv = vptr.size(), nh = hptr.size();
-  vres.assign(nv, 0);
+  const size_t nv = vreq.size() / 3, nh = hptr.size(), nr = rreq.size() / 4;
+  vres.assign(n_slots, 0);
   hres.assign(nh * 8, 0);
-  if (nv + nh == 0) return STWO_OK;
+  if (nv + nh + nr == 0) return STWO_OK;
   Mapped mp;
-  int32_t st = mapped_words(4 * (nv + nh) + nv + 8 * nh, mp);
+  const size_t w_req = 2 * (3 * nv + 2 * nh + 4 * nr);  // request words (u64 = 2 words)
+  int32_t st = mapped_words(w_req + n_slots + 8 * nh, mp);
   if (st) return st;
   unsigned long long* req = reinterpret_cast<unsigned long long*>(mp.host);
-  for (size_t i = 0; i < nv; i++) {
-    req[2 * i] = vptr[i];
-    req[2 * i + 1] = vidx[i];
-  }
+  std::memcpy(req, vreq.data(), vreq.size() * 8);
+  unsigned long long* hq_ = req + 3 * nv;
   for (size_t i = 0; i < nh; i++) {
-    req[2 * (nv + i)] = hptr[i];
-    req[2 * (nv + i) + 1] = hidx[i];
+    hq_[2 * i] = hptr[i];
+    hq_[2 * i + 1] = hidx[i];
   }
-  uint32_t* dres = mp.dev + 4 * (nv + nh);
-  launch_pdl(k_gather, dim3((uint32_t)((nv + nh + 127) / 128)), dim3(128), 0, s,
-             reinterpret_cast<const unsigned long long*>(mp.dev), (uint32_t)nv, (uint32_t)nh, dres, dres + nv);
+  std::memcpy(hq_ + 2 * nh, rreq.data(), rreq.size() * 8);
+  const unsigned long long* dreq = reinterpret_cast<const unsigned long long*>(mp.dev);
+  uint32_t* dres = mp.dev + w_req;
+  const uint32_t single_blocks = (uint32_t)((nv + nh + 127) / 128);
+  launch_pdl(k_gather, dim3(single_blocks + (uint32_t)nr), dim3(128), 0, s, dreq, (uint32_t)nv, dreq + 3 * nv,
+             (uint32_t)nh, dreq + 3 * nv + 2 * nh, single_blocks, dres, dres + n_slots);
   note_launch();
   cudaError_t e = cudaGetLastError();
   if (!e) e = cudaStreamSynchronize(s);
@@ -145,9 +156,9 @@ int32_t Gather::run(cudaStream_t s) {
     set_error("gather: %s", cudaGetErrorString(e));
     return STWO_ERR_CUDA;
   }
-  const uint32_t* hres_p = mp.host + 4 * (nv + nh);
-  std::memcpy(vres.data(), hres_p, nv * 4);
-  std::memcpy(hres.data(), hres_p + nv, nh * 32);
+  const uint32_t* res = mp.host + w_req;
+  std::memcpy(vres.data(), res, n_slots * 4);
+  std::memcpy(hres.data(), res + n_slots, nh * 32);
   return STWO_OK;
 }
 
@@ -169,6 +180,13 @@ int32_t DevMerkle::commit(const std::vector<ColRef>& columns, Arena& arena, cuda
   while (lg >= 0) {
     std::vector<const uint32_t*> lc;
     while (ci < sorted.size() && sorted[ci].log == (uint32_t)lg) lc.push_back(sorted[ci++].p);
+    // Columns that lie a fixed stride apart (one column block) are gathered as one run per node.
+    size_t stride = 0;
+    if (lc.size() >= 8 && lc[1] > lc[0]) {
+      stride = (size_t)(lc[1] - lc[0]);
+      for (size_t k = 2; k < lc.size() && stride; k++)
+        if (lc[k] != lc[0] + k * stride) stride = 0;
+    }
     const uint32_t* prev = (uint32_t)lg < max_log ? layers[lg + 1] : nullptr;
     if (!lc.empty() || !prev) {
       int32_t st = merkle_commit_layer((uint32_t)lg, prev, lc.data(), (uint32_t)lc.size(), layers[lg], s);
@@ -228,6 +246,13 @@ void DevMerkle::decommit(const std::map<uint32_t, std::vector<size_t>>& queries,
   for (int lg = (int)layers.size() - 1; lg >= 0; lg--) {
     std::vector<const uint32_t*> lc;
     while (ci < sorted.size() && sorted[ci].log == (uint32_t)lg) lc.push_back(sorted[ci++].p);
+    // Columns that lie a fixed stride apart (one column block) are gathered as one run per node.
+    size_t stride = 0;
+    if (lc.size() >= 8 && lc[1] > lc[0]) {
+      stride = (size_t)(lc[1] - lc[0]);
+      for (size_t k = 2; k < lc.size() && stride; k++)
+        if (lc[k] != lc[0] + k * stride) stride = 0;
+    }
     const uint32_t* prev = (size_t)lg + 1 < layers.size() ? layers[lg + 1] : nullptr;
     auto it = queries.find((uint32_t)lg);
     const std::vector<size_t>& cq = it == queries.end() ? empty : it->second;
@@ -247,7 +272,13 @@ void DevMerkle::decommit(const std::map<uint32_t, std::vector<size_t>>& queries,
       }
       bool q = qi < cq.size() && cq[qi] == node;
       if (q) qi++;
-      for (auto* c : lc) (q ? out.queried : out.column_witness).push_back(g.val(c, node));
+      std::vector<size_t>& dst = q ? out.queried : out.column_witness;
+      if (stride) {
+        const size_t first = g.vals_strided(lc[0], stride, (uint32_t)lc.size(), node);
+        for (size_t k = 0; k < lc.size(); k++) dst.push_back(first + k);
+      } else {
+        for (auto* c : lc) dst.push_back(g.val(c, node));
+      }
       total.push_back(node);
     }
     last = total;
@@ -279,7 +310,12 @@ struct ByteWriter {
   }
   void vals(const std::vector<size_t>& idx, const Gather& g) {
     u64(idx.size());
-    for (size_t i : idx) u32(g.vres[i]);
+    size_t o = b.size();
+    b.resize(o + 4 * idx.size());
+    for (size_t i : idx) {
+      const uint32_t v = g.vres[i];
+      for (int k = 0; k < 4; k++) b[o++] = (uint8_t)(v >> (8 * k));
+    }
   }
   void dec(const DecommitRecipe& d, const Gather& g) {
     hashes(d.hash_witness, g);

@@ -27,13 +27,29 @@ struct Arena {
 
 // Words to read back from HBM, collected while walking decommitment structures on the host and
 // fetched in one launch per word size.
+// A value request takes one result slot of vres; a run of `count` columns that lie `stride` words
+// apart (one column block) takes `count` consecutive slots with one request.
 struct Gather {
-  std::vector<unsigned long long> vptr, vidx, hptr, hidx;
+  std::vector<unsigned long long> vreq;  // (column, index, slot) per single value
+  std::vector<unsigned long long> rreq;  // (first column, stride, index, slot | count << 32) per run
+  std::vector<unsigned long long> hptr, hidx;
   std::vector<uint32_t> vres, hres;
+  size_t n_slots = 0;
   size_t val(const uint32_t* col, size_t i) {
-    vptr.push_back((unsigned long long)(uintptr_t)col);
-    vidx.push_back(i);
-    return vptr.size() - 1;
+    vreq.push_back((unsigned long long)(uintptr_t)col);
+    vreq.push_back(i);
+    vreq.push_back(n_slots);
+    return n_slots++;
+  }
+  // Slots of col0[i], col0[stride + i], ..., col0[(count - 1) stride + i]: the first is returned.
+  size_t vals_strided(const uint32_t* col0, size_t stride, uint32_t count, size_t i) {
+    rreq.push_back((unsigned long long)(uintptr_t)col0);
+    rreq.push_back(stride);
+    rreq.push_back(i);
+    rreq.push_back((unsigned long long)n_slots | ((unsigned long long)count << 32));
+    const size_t first = n_slots;
+    n_slots += count;
+    return first;
   }
   size_t hash(const uint32_t* layer, size_t node) {
     hptr.push_back((unsigned long long)(uintptr_t)layer);
