@@ -433,9 +433,11 @@ __global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
   pdl_enter();
   __shared__ uint32_t s_coeffs[4 * PS_N_CONSTRAINTS];
   __shared__ uint32_t s_part[PS_REPS][4][PC_ROWS];
+  extern __shared__ uint32_t s_masks[];  // per warp: 2 slots x 16 columns x 32 rows
   for (uint32_t i = threadIdx.x; i < 4 * PS_N_CONSTRAINTS; i += blockDim.x) s_coeffs[i] = coeffs[i];
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31, rep = threadIdx.x >> 5;
+  uint32_t* const mb = s_masks + rep * (2 * PS_ST * PC_ROWS) + lane;
   const uint32_t el = pp.eval_log;
   const uint32_t n_tiles = (n_rows + PC_ROWS - 1) / PC_ROWS;
   auto col = [&](const uint32_t* base, uint32_t c, uint32_t row) { return __ldg(base + ((size_t)c << el) + row); };
@@ -462,32 +464,51 @@ __global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
       }
     };
     const uint32_t c0 = rep * PS_COLS_PER_REP;
+    // First mask column of full round k (four before the partial rounds, four after).
+    auto full_col = [&](uint32_t k) {
+      return c0 + PS_ST * (1 + k) + (k >= PS_HALF ? PS_PARTIAL : 0u);
+    };
+    // A full round's 16 mask columns go to this warp's shared-memory slot by cp.async, one round
+    // ahead of their use: each lane copies (and later reads) its own row's words, so the copies need
+    // no barrier, only the lane's own wait_group.
+    auto issue_full = [&](uint32_t slot, uint32_t col0) {
+#pragma unroll
+      for (int i = 0; i < PS_ST; i++) {
+        const uint32_t* g = trace + ((size_t)(col0 + i) << el) + r;
+        const uint32_t sa = (uint32_t)__cvta_generic_to_shared(mb + (slot * PS_ST + i) * 32);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(g) : "memory");
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    issue_full(0, full_col(0));
     uint32_t s[PS_ST];
 #pragma unroll
     for (int i = 0; i < PS_ST; i++) s[i] = col(trace, c0 + i, r);
     // The lookup value of the initial state, taken now so that the state need not be kept.
     const qm31 d0 = combine16(pp.lc, s);
-    uint32_t mc = c0 + PS_ST;
-    // Each round's masks are loaded before its arithmetic so that their latency hides behind the
-    // matrix and S-box work.
-    auto full_round = [&]() {
-      uint32_t m[PS_ST];
-#pragma unroll
-      for (int i = 0; i < PS_ST; i++) m[i] = col(trace, mc + i, r);
-      mc += PS_ST;
+    uint32_t mc = c0 + PS_ST * (1 + PS_HALF);  // the first partial round's column
+    auto full_round = [&](uint32_t k) {
+      if (k + 1 < 2 * PS_HALF) {
+        issue_full((k + 1) & 1, full_col(k + 1));
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      }
+      const uint32_t* m = mb + (k & 1) * PS_ST * 32;
 #pragma unroll
       for (int i = 0; i < PS_ST; i++) s[i] = m31_add(s[i], PS_RC);
       external_matrix(s);
 #pragma unroll
       for (int i = 0; i < PS_ST; i++) {
-        acc(m31_sub(pow5(s[i]), m[i]));
-        s[i] = m[i];
+        const uint32_t mi = m[i * 32];
+        acc(m31_sub(pow5(s[i]), mi));
+        s[i] = mi;
       }
     };
     // The rounds stay loops: fully unrolled, the kernel outgrew the instruction cache and stalled
     // on instruction fetch.
 #pragma unroll 1
-    for (int round = 0; round < PS_HALF; round++) full_round();
+    for (uint32_t round = 0; round < PS_HALF; round++) full_round(round);
     // A partial round has little arithmetic to hide its one load behind: the mask of the next
     // round is fetched one round ahead.
     uint32_t m_next = col(trace, mc, r);
@@ -500,9 +521,8 @@ __global__ void __launch_bounds__(PC_THREADS, PC_BLOCKS_PER_SM)
       acc(m31_sub(pow5(s[0]), m));
       s[0] = m;
     }
-    mc += PS_PARTIAL;
 #pragma unroll 1
-    for (int round = 0; round < PS_HALF; round++) full_round();
+    for (uint32_t round = PS_HALF; round < 2 * PS_HALF; round++) full_round(round);
     // LogUp batch `rep`: fraction (1/d0 - 1/d1) = (d1 - d0) / (d0 d1), against the cumulative
     // column of this batch minus that of the previous one (for the last batch: minus its value at
     // the previous trace row and plus claimed_sum / 2^trace_log).
@@ -602,8 +622,27 @@ struct PoseidonGpuAir : GpuAir {
     uint32_t n_rows = 1u << pp.eval_log;
     const uint32_t n_tiles = (n_rows + PC_ROWS - 1) / PC_ROWS;
     const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)sm_count() * PC_BLOCKS_PER_SM);
-    launch_pdl(k_poseidon_composition, dim3(grid), dim3(PC_THREADS), 0, s, cols[1][0], cols[2][0], n_rows, pp, coeffs,
-               dinv, acc[0], acc[1], acc[2], acc[3]);
+    // 22.4 KB of static shared memory plus the 32 KB of mask slots: above the default 48 KB, so
+    // the dynamic part needs the opt-in attribute (once per device, with the carveout).
+    constexpr size_t mask_smem = (size_t)PS_REPS * 2 * PS_ST * PC_ROWS * 4;
+    {
+      static std::mutex mu;
+      static bool done[256] = {};
+      int dev = 0;
+      STWO_CHECK_CUDA(cudaGetDevice(&dev));
+      STWO_REQUIRE(dev >= 0 && dev < 256, "device ordinal %d out of range", dev);
+      std::lock_guard<std::mutex> g(mu);
+      if (!done[dev]) {
+        STWO_CHECK_CUDA(cudaFuncSetAttribute(k_poseidon_composition, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)mask_smem));
+        // Four blocks of 54.4 KB need the largest shared-memory carveout of the SM.
+        STWO_CHECK_CUDA(cudaFuncSetAttribute(k_poseidon_composition, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             (int)cudaSharedmemCarveoutMaxShared));
+        done[dev] = true;
+      }
+    }
+    launch_pdl(k_poseidon_composition, dim3(grid), dim3(PC_THREADS), mask_smem, s, cols[1][0], cols[2][0], n_rows, pp,
+               coeffs, dinv, acc[0], acc[1], acc[2], acc[3]);
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e) {
