@@ -264,16 +264,40 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
 // evaluation takes, are known before the points are: eval_plan_build lays out and uploads the job
 // tables (stream-ordered, while the device still works on earlier stages), eval_plan_run takes the
 // points and evaluates, eval_plan_free releases the device block.
+// At most this many distinct points (mask offsets) per planned evaluation or quotient group.
+constexpr uint32_t EP_MAX_POINTS = 8;
 struct EvalPlan {
   uint32_t n_evals = 0, n_points = 0, n_blocks = 0;
   unsigned char* d = nullptr;
-  size_t off_polyof = 0, off_pointof = 0, off_work = 0, off_acc = 0, off_tables = 0;
+  size_t off_polyof = 0, off_pointof = 0, off_work = 0, off_acc = 0, off_vals = 0, off_tables = 0;
 };
 int32_t eval_plan_build(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
                         const uint32_t* poly_of, const uint32_t* point_of, uint32_t n_evals, uint32_t n_points,
                         cudaStream_t s, EvalPlan* plan);
+// Also leaves the values in device memory (eval_plan_values: 4 words per evaluation) until freed.
 int32_t eval_plan_run(const EvalPlan& plan, const stwo_qm31_point* points, stwo_qm31* out, cudaStream_t s);
+inline const uint32_t* eval_plan_values(const EvalPlan& plan) {
+  return reinterpret_cast<const uint32_t*>(plan.d + plan.off_vals);
+}
 void eval_plan_free(EvalPlan& plan, cudaStream_t s);
+
+// A quotient group (accumulate_quotients) whose samples — which column at which point id, and
+// which planned OODS evaluation holds its value — are known before the points are: quot_plan_build
+// uploads them; quot_plan_run takes the points, the batch order (point ids in the reference's order
+// of point values), the random coefficient and the values in device memory.
+struct QuotPlan {
+  uint32_t log_n = 0, log_blowup = 0, n_points = 0, n_samples = 0;
+  std::vector<const uint32_t*> cols;
+  std::vector<uint32_t> s_first;
+  unsigned char* d = nullptr;
+  size_t off_samples = 0, off_batches = 0, off_entries = 0, off_sub = 0;
+};
+int32_t quot_plan_build(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, const uint32_t* sample_col,
+                        const uint32_t* sample_eval, const uint32_t* sample_point, uint32_t n_samples, uint32_t n_points,
+                        uint32_t log_blowup, cudaStream_t s, QuotPlan* plan);
+int32_t quot_plan_run(const QuotPlan& plan, const uint32_t* d_vals, const stwo_qm31_point* points, const uint32_t* order,
+                      uint32_t n_batches, stwo_qm31 rc, uint32_t* const out[4], cudaStream_t s);
+void quot_plan_free(QuotPlan& plan, cudaStream_t s);
 
 // Pinned host words mapped into the device address space, one growable buffer per host thread:
 // kernels write small results straight into host memory, read after a stream synchronisation.

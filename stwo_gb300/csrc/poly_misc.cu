@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256) k_point_tables(const stwo_qm31_point* __r
   point_tables_block(points[blockIdx.x], tables);
 }
 // The same with the points in the launch parameters (at most EP_PARAM_POINTS).
-constexpr uint32_t EP_PARAM_POINTS = 8;
+constexpr uint32_t EP_PARAM_POINTS = EP_MAX_POINTS;
 struct EvalPoints {
   stwo_qm31_point p[EP_PARAM_POINTS];
 };
@@ -200,7 +200,8 @@ __global__ void __launch_bounds__(256) k_eval_at_point(const EvalJob* __restrict
   }
 }
 
-__global__ void k_reduce_acc(const unsigned long long* acc, uint32_t n, uint32_t* out) {
+// Canonical words of the 64-bit accumulators into out (and into dev_out when it is set).
+__global__ void k_reduce_acc(const unsigned long long* acc, uint32_t n, uint32_t* out, uint32_t* dev_out = nullptr) {
   pdl_enter();
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -208,7 +209,9 @@ __global__ void k_reduce_acc(const unsigned long long* acc, uint32_t n, uint32_t
   x = (x & P) + (x >> 31);
   x = (x & P) + (x >> 31);
   uint32_t r = (uint32_t)x;
-  out[i] = r >= P ? r - P : r;
+  r = r >= P ? r - P : r;
+  out[i] = r;
+  if (dev_out) dev_out[i] = r;
 }
 
 int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes, uint32_t n_polys,
@@ -292,7 +295,8 @@ int32_t eval_at_points(const uint32_t* const* coeffs, const uint32_t* log_sizes,
     err = cudaGetLastError();
   }
   if (!err) {
-    launch_pdl(k_reduce_acc, dim3((n_evals * 4 + 255) / 256), dim3(256), 0, s, acc, n_evals * 4, dev(h_out));
+    launch_pdl(k_reduce_acc, dim3((n_evals * 4 + 255) / 256), dim3(256), 0, s, acc, n_evals * 4, dev(h_out),
+               nullptr);
     note_launch();
     err = cudaGetLastError();
   }
@@ -340,7 +344,8 @@ int32_t eval_plan_build(const uint32_t* const* coeffs, const uint32_t* log_sizes
   p.off_pointof = p.off_polyof + up16((size_t)n_evals * 4);
   p.off_work = p.off_pointof + up16((size_t)n_evals * 4);
   p.off_acc = p.off_work + up16(work.size() * 4);
-  p.off_tables = p.off_acc + (size_t)n_evals * 32;
+  p.off_vals = p.off_acc + (size_t)n_evals * 32;
+  p.off_tables = p.off_vals + up16((size_t)n_evals * 16);
   const size_t bytes = p.off_tables + (size_t)n_points * EP_TABLE * sizeof(qm31);
   std::vector<unsigned char> host(p.off_acc, 0);
   std::memcpy(host.data(), jobs.data(), jobs.size() * sizeof(EvalJob));
@@ -383,7 +388,8 @@ int32_t eval_plan_run(const EvalPlan& p, const stwo_qm31_point* points, stwo_qm3
     err = cudaGetLastError();
   }
   if (!err) {
-    launch_pdl(k_reduce_acc, dim3((p.n_evals * 4 + 255) / 256), dim3(256), 0, s, acc, p.n_evals * 4, mp.dev);
+    launch_pdl(k_reduce_acc, dim3((p.n_evals * 4 + 255) / 256), dim3(256), 0, s, acc, p.n_evals * 4, mp.dev,
+               reinterpret_cast<uint32_t*>(p.d + p.off_vals));
     note_launch();
     err = cudaGetLastError();
   }
@@ -475,7 +481,7 @@ int32_t eval_at_points_noalloc(const uint32_t* const* coeffs, const uint32_t* lo
   if (!err) {
     launch_pdl(k_reduce_acc, dim3((n_evals * 4 + 255) / 256), dim3(256), 0, s,
                reinterpret_cast<unsigned long long*>(buf + NA_OFF_ACC), n_evals * 4,
-               reinterpret_cast<uint32_t*>(buf + NA_OFF_OUT));
+               reinterpret_cast<uint32_t*>(buf + NA_OFF_OUT), nullptr);
     note_launch();
     err = cudaGetLastError();
   }

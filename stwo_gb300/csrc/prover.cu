@@ -625,11 +625,17 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   std::vector<const uint32_t*> polys, ceval;
   std::vector<uint32_t> plogs, clog, poly_of;
   EvalPlan plan;
+  std::vector<QuotPlan> qplans;
+  std::vector<uint32_t> qorder;
   struct PlanRelease {
     EvalPlan& p;
+    std::vector<QuotPlan>& q;
     cudaStream_t s;
-    ~PlanRelease() { eval_plan_free(p, s); }
-  } plan_release{plan, s};
+    ~PlanRelease() {
+      eval_plan_free(p, s);
+      for (QuotPlan& x : q) quot_plan_free(x, s);
+    }
+  } plan_release{plan, qplans, s};
   int32_t plan_st = STWO_OK;
   before_root_wait = [&] {
     lay = sample_layout(air, trees);
@@ -652,6 +658,30 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
     if (!lay.sample_off.empty())
       plan_st = eval_plan_build(polys.data(), plogs.data(), (uint32_t)n_cols, poly_of.data(), lay.sample_off.data(),
                                 (uint32_t)lay.sample_off.size(), (uint32_t)lay.offsets.size(), s, &plan);
+    // The FRI quotient groups: columns by evaluation log size, descending (pcs/quotients.rs:76-101),
+    // tree order within a size; each group's samples (local column, OODS evaluation, offset id).
+    qorder.resize(n_cols);
+    for (uint32_t c = 0; c < n_cols; c++) qorder[c] = (uint32_t)c;
+    std::stable_sort(qorder.begin(), qorder.end(), [&](uint32_t a, uint32_t b) { return clog[a] > clog[b]; });
+    for (size_t i = 0; i < n_cols && !plan_st;) {
+      size_t j = i;
+      while (j < n_cols && clog[qorder[j]] == clog[qorder[i]]) j++;
+      std::vector<const uint32_t*> gc(j - i);
+      std::vector<uint32_t> scol, seval, spt;
+      for (size_t k = i; k < j; k++) {
+        gc[k - i] = ceval[qorder[k]];
+        for (uint32_t e = lay.col_first[qorder[k]]; e < lay.col_first[qorder[k] + 1]; e++) {
+          scol.push_back((uint32_t)(k - i));
+          seval.push_back(e);
+          spt.push_back(lay.sample_off[e]);
+        }
+      }
+      qplans.emplace_back();
+      plan_st = quot_plan_build(clog[qorder[i]], gc.data(), (uint32_t)gc.size(), scol.data(), seval.data(), spt.data(),
+                                (uint32_t)scol.size(), (uint32_t)lay.offsets.size(), cfg.log_blowup_factor, s,
+                                &qplans.back());
+      i = j;
+    }
   };
   hq rc = ch.draw_felt();
   int32_t st = commit_composition(air, rc);
@@ -687,7 +717,6 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
   std::vector<stwo_qm31> svals(n_samples);
   StageScope stage_oods("Evaluate columns out of domain", s);
   st = eval_plan_run(plan, opts.data(), svals.data(), s);
-  eval_plan_free(plan, s);
   if (st) return st;
   std::vector<hq> flat(n_samples);
   for (size_t e = 0; e < n_samples; e++) flat[e] = from_sq(svals[e]);
@@ -726,14 +755,33 @@ int32_t Prover::prove(const GpuAir& air, std::vector<uint8_t>& out) {
 
   // FRI quotients per log size, descending (pcs/quotients.rs:76-101); columns of one log size
   // keep their tree order.
-  std::vector<uint32_t> order(n_cols);
-  for (uint32_t c = 0; c < n_cols; c++) order[c] = c;
-  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return clog[a] > clog[b]; });
+  const std::vector<uint32_t>& order = qorder;
   hq qrc = ch.draw_felt();
   StageScope stage_q("Compute FRI quotients", s);
   std::vector<SecureCols> quotients;
   std::vector<uint32_t> qlogs;
-  for (size_t i = 0; i < n_cols;) {
+  // The planned path needs each mask offset on its own point (always so in practice: offsets
+  // are a few rows apart); otherwise offsets that share a point form one batch, as the reference
+  // groups samples by point value, and the tables are built here.
+  const bool planned = upts.size() == lay.offsets.size();
+  for (size_t g = 0; planned && g < qplans.size(); g++) {
+    const QuotPlan& qp = qplans[g];
+    std::vector<uint32_t> bord;  // offset ids present in the group, in the order of their points
+    for (uint32_t q = 0; q < qp.n_points; q++)
+      if (qp.s_first[q + 1] > qp.s_first[q]) bord.push_back(q);
+    std::sort(bord.begin(), bord.end(), [&](uint32_t a, uint32_t b) { return hpq_less(upts[pid[a]], upts[pid[b]]); });
+    const uint32_t glog = qp.log_n;
+    SecureCols q;
+    for (int k = 0; k < 4; k++) {
+      q.c[k] = arena.alloc((size_t)1 << glog);
+      if (!q.c[k]) return STWO_ERR_OOM;
+    }
+    st = quot_plan_run(qp, eval_plan_values(plan), opts.data(), bord.data(), (uint32_t)bord.size(), to_sq(qrc), q.c, s);
+    if (st) return st;
+    quotients.push_back(q);
+    qlogs.push_back(glog);
+  }
+  for (size_t i = 0; !planned && i < n_cols;) {
     size_t j = i;
     while (j < n_cols && clog[order[j]] == clog[order[i]]) j++;
     // ColumnSampleBatch::new_vec: group by point in CirclePoint<QM31> order.

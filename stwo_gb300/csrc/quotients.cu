@@ -386,6 +386,50 @@ __global__ void __launch_bounds__(Q_SLICES * 32) k_quotient_rows4(uint32_t rows,
   }
 }
 
+// The per-row pass over the columns (with the line coefficients already in d_b / d_e) and, above
+// a sub-domain of 2^6 points, the extension of the sub-domain result to the full domain. d_sub
+// holds 4 x 2^(log_n - log_blowup) words (unused when the rows are computed directly).
+static int32_t quotient_rows_and_extend(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, const QBatch* d_b,
+                                        uint32_t n_batches, const QEntry* d_e, uint32_t log_blowup, uint32_t* d_sub,
+                                        uint32_t* const out[4], cudaStream_t s) {
+  stwo_coset dom_half = canonic_half_coset(log_n);
+  const uint32_t sub_log = log_n - log_blowup;
+  const bool direct = sub_log < 6;
+  const uint32_t rows = 1u << (direct ? log_n : sub_log);
+  QCols qc;
+  for (uint32_t c = 0; c < n_cols; c++) qc.p[c] = cols[c];
+  uint32_t* o[4];
+  for (int q = 0; q < 4; q++) o[q] = direct ? out[q] : d_sub + (size_t)q * rows;
+  // Four rows per lane once the domain gives at least four 128-row blocks per SM, else two.
+  const int rpl = rows >= 4u * 128u * (uint32_t)sm_count() ? 4 : 2;
+  bool aligned = rows % (32 * rpl) == 0;
+  for (uint32_t c = 0; c < n_cols && aligned; c++)
+    aligned = (reinterpret_cast<uintptr_t>(cols[c]) & (4 * rpl - 1)) == 0;
+  if (aligned && rpl == 4)
+    launch_pdl(k_quotient_rows4<4>, dim3(rows / 128), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
+               dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
+  else if (aligned)
+    launch_pdl(k_quotient_rows4<2>, dim3(rows / 64), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
+               dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
+  else
+    launch_pdl(k_quotient_rows, dim3((rows + Q_ROWS - 1) / Q_ROWS), dim3(Q_SLICES * 32), 0, s, rows, log_n,
+               dom_half.initial_index, dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
+  note_launch();
+  if (cudaGetLastError() != cudaSuccess) return STWO_ERR_CUDA;
+
+  if (!direct) {
+    // Interpolate on the sub-domain (its own tree), then evaluate on the full canonic domain.
+    stwo_coset sub_half = coset_new(dom_half.initial_index, sub_log - 1);
+    TwiddleTree* t_sub = nullptr;
+    TwiddleTree* t_dom = nullptr;
+    int32_t st = get_tree(sub_half, s, &t_sub);
+    if (!st) st = get_tree(dom_half, s, &t_dom);
+    if (!st) st = fft_interpolate_evaluate(t_sub, sub_half, o, 4, t_dom, dom_half, out, s);
+    if (st) return st;
+  }
+  return STWO_OK;
+}
+
 int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, stwo_qm31 rc_in,
                              const stwo_sample_batch* batches, uint32_t n_batches, uint32_t log_blowup,
                              uint32_t* const out[4], cudaStream_t s) {
@@ -417,7 +461,6 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
     B.e1 = (uint32_t)hs.size();
   }
   std::vector<QEntry> he(hs.size());
-  stwo_coset dom_half = canonic_half_coset(log_n);
   uint32_t sub_log = log_n - log_blowup;
   bool direct = sub_log < 6;
   uint32_t rows = 1u << (direct ? log_n : sub_log);
@@ -446,39 +489,141 @@ int32_t accumulate_quotients(uint32_t log_n, const uint32_t* const* cols, uint32
     if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
   }
 
-  QCols qc;
-  for (uint32_t c = 0; c < n_cols; c++) qc.p[c] = cols[c];
-  uint32_t* o[4];
-  for (int q = 0; q < 4; q++) o[q] = direct ? out[q] : d_sub + (size_t)q * rows;
-  // Four rows per lane once the domain gives at least four 128-row blocks per SM, else two.
-  const int rpl = rows >= 4u * 128u * (uint32_t)sm_count() ? 4 : 2;
-  bool aligned = rows % (32 * rpl) == 0;
-  for (uint32_t c = 0; c < n_cols && aligned; c++)
-    aligned = (reinterpret_cast<uintptr_t>(cols[c]) & (4 * rpl - 1)) == 0;
-  if (aligned && rpl == 4)
-    launch_pdl(k_quotient_rows4<4>, dim3(rows / 128), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
-               dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
-  else if (aligned)
-    launch_pdl(k_quotient_rows4<2>, dim3(rows / 64), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
-               dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
-  else
-    launch_pdl(k_quotient_rows, dim3((rows + Q_ROWS - 1) / Q_ROWS), dim3(Q_SLICES * 32), 0, s, rows, log_n,
-               dom_half.initial_index, dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
-  note_launch();
-  if (cudaGetLastError() != cudaSuccess) return fail(STWO_ERR_CUDA);
-
-  if (!direct) {
-    // Interpolate on the sub-domain (its own tree), then evaluate on the full canonic domain.
-    stwo_coset sub_half = coset_new(dom_half.initial_index, sub_log - 1);
-    TwiddleTree* t_sub = nullptr;
-    TwiddleTree* t_dom = nullptr;
-    st = get_tree(sub_half, s, &t_sub);
-    if (!st) st = get_tree(dom_half, s, &t_dom);
-    if (!st) st = fft_interpolate_evaluate(t_sub, sub_half, o, 4, t_dom, dom_half, out, s);
-    if (st) return fail(st);
-  }
+  st = quotient_rows_and_extend(log_n, cols, n_cols, d_b, n_batches, d_e, log_blowup, d_sub, out, s);
+  if (st) return fail(st);
   scratch_free(scratch, s);
   return STWO_OK;
+}
+
+// ---------------------------------------------------------------- planned quotients (the prover's)
+// The prover knows, before the OODS point is drawn, which columns of a quotient group are sampled
+// at which mask offset and which OODS evaluation holds each value; only the points, their order
+// (the reference orders batches by point value) and the random coefficient come later. So the
+// sample table is uploaded while the device still works on earlier stages, and at run time one
+// launch assembles the batch tables from it and from the OODS values left in device memory.
+struct QPlanSample {
+  uint32_t col, eval;
+};
+struct QPlanParams {
+  uint32_t order[EP_MAX_POINTS];        // point id of batch b
+  uint32_t e_first[EP_MAX_POINTS + 1];  // entries of batch b: [e_first[b], e_first[b + 1])
+  uint32_t s_first[EP_MAX_POINTS + 1];  // the plan's samples at point id p: [s_first[p], s_first[p + 1])
+  uint32_t pt[EP_MAX_POINTS][8];        // point id p: CM31 parts prx, pix, pry, piy
+};
+
+// Block b: batch b's header and its samples, in the order k_quotient_coeffs reads them.
+__global__ void k_quotient_gather(const QPlanSample* __restrict__ ps, const uint32_t* __restrict__ vals,
+                                  QPlanParams pp, QSample* samples, QBatch* batches) {
+  pdl_enter();
+  const uint32_t b = blockIdx.x, p = pp.order[b];
+  const uint32_t s0 = pp.s_first[p], n = pp.s_first[p + 1] - s0, e0 = pp.e_first[b];
+  for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+    const QPlanSample q = ps[s0 + j];
+    QSample o;
+    o.col = q.col;
+    for (int k = 0; k < 4; k++) o.v[k] = vals[4 * q.eval + k];
+    samples[e0 + j] = o;
+  }
+  if (threadIdx.x == 0) {
+    QBatch B = {};
+    B.prx[0] = pp.pt[p][0]; B.prx[1] = pp.pt[p][1]; B.pix[0] = pp.pt[p][2]; B.pix[1] = pp.pt[p][3];
+    B.pry[0] = pp.pt[p][4]; B.pry[1] = pp.pt[p][5]; B.piy[0] = pp.pt[p][6]; B.piy[1] = pp.pt[p][7];
+    B.e0 = e0;
+    B.e1 = e0 + n;
+    batches[b] = B;
+  }
+}
+
+int32_t quot_plan_build(uint32_t log_n, const uint32_t* const* cols, uint32_t n_cols, const uint32_t* sample_col,
+                        const uint32_t* sample_eval, const uint32_t* sample_point, uint32_t n_samples, uint32_t n_points,
+                        uint32_t log_blowup, cudaStream_t s, QuotPlan* plan) {
+  STWO_REQUIRE(plan && (n_cols == 0 || cols) && (n_samples == 0 || (sample_col && sample_eval && sample_point)),
+               "null argument");
+  STWO_REQUIRE(log_n >= 1 && log_n <= 30, "bad domain log size %u", log_n);
+  STWO_REQUIRE(log_blowup < log_n, "log_blowup_factor %u >= domain log size %u", log_blowup, log_n);
+  STWO_REQUIRE(n_cols <= Q_MAX_COLS, "more than %d columns in one quotient group", Q_MAX_COLS);
+  STWO_REQUIRE(n_points >= 1 && n_points <= EP_MAX_POINTS, "%u points (at most %u)", n_points, EP_MAX_POINTS);
+  QuotPlan p;
+  p.log_n = log_n;
+  p.log_blowup = log_blowup;
+  p.n_points = n_points;
+  p.n_samples = n_samples;
+  p.cols.assign(cols, cols + n_cols);
+  // Samples bucketed by point id, each bucket in sample order (column, then offset).
+  std::vector<uint32_t> count(n_points + 1, 0);
+  for (uint32_t j = 0; j < n_samples; j++) {
+    STWO_REQUIRE(sample_col[j] < n_cols && sample_point[j] < n_points, "sample %u: index out of range", j);
+    count[sample_point[j] + 1]++;
+  }
+  for (uint32_t q = 0; q < n_points; q++) count[q + 1] += count[q];
+  p.s_first.assign(count.begin(), count.end());
+  std::vector<QPlanSample> hs(n_samples);
+  for (uint32_t j = 0; j < n_samples; j++) hs[count[sample_point[j]]++] = {sample_col[j], sample_eval[j]};
+  const uint32_t sub_log = log_n - log_blowup;
+  const uint32_t rows = 1u << (sub_log < 6 ? log_n : sub_log);
+  auto up256 = [](size_t b) { return (b + 255) / 256 * 256; };
+  p.off_samples = up256(n_samples * sizeof(QPlanSample));
+  p.off_batches = p.off_samples + up256((size_t)n_samples * sizeof(QSample));
+  p.off_entries = p.off_batches + up256((size_t)n_points * sizeof(QBatch));
+  p.off_sub = p.off_entries + up256((size_t)n_samples * sizeof(QEntry));
+  const size_t bytes = p.off_sub + (size_t)4 * rows * 4;
+  int32_t st = scratch_alloc((void**)&p.d, bytes, s);
+  if (st) return st;
+  if (n_samples) {
+    cudaError_t err = cudaMemcpyAsync(p.d, hs.data(), hs.size() * sizeof(QPlanSample), cudaMemcpyHostToDevice, s);
+    if (err) {
+      scratch_free(p.d, s);
+      set_error("quot_plan_build: %s", cudaGetErrorString(err));
+      return STWO_ERR_CUDA;
+    }
+  }
+  *plan = std::move(p);
+  return STWO_OK;
+}
+
+int32_t quot_plan_run(const QuotPlan& p, const uint32_t* d_vals, const stwo_qm31_point* points, const uint32_t* order,
+                      uint32_t n_batches, stwo_qm31 rc_in, uint32_t* const out[4], cudaStream_t s) {
+  STWO_REQUIRE(p.d && d_vals && points && (n_batches == 0 || order), "null argument");
+  STWO_REQUIRE(n_batches <= p.n_points, "%u batches for %u points", n_batches, p.n_points);
+  QPlanParams pp{};
+  uint32_t e = 0;
+  for (uint32_t b = 0; b < n_batches; b++) {
+    const uint32_t q = order[b];
+    STWO_REQUIRE(q < p.n_points, "batch %u: point id out of range", b);
+    pp.order[b] = q;
+    pp.e_first[b] = e;
+    e += p.s_first[q + 1] - p.s_first[q];
+  }
+  pp.e_first[n_batches] = e;
+  STWO_REQUIRE(e == p.n_samples, "the batch order must take every sampled point once");
+  for (uint32_t q = 0; q <= p.n_points; q++) pp.s_first[q] = p.s_first[q];
+  for (uint32_t q = 0; q < p.n_points; q++) {
+    const stwo_qm31_point& pt = points[q];
+    STWO_REQUIRE(!(pt.y.v[2] == 0 && pt.y.v[3] == 0), "Cannot evaluate a line with a single point");
+    const uint32_t w[8] = {pt.x.v[0], pt.x.v[1], pt.x.v[2], pt.x.v[3], pt.y.v[0], pt.y.v[1], pt.y.v[2], pt.y.v[3]};
+    for (int k = 0; k < 8; k++) pp.pt[q][k] = w[k];
+  }
+  const hq rc = hq_from(rc_in);
+  const QPlanSample* d_ps = reinterpret_cast<const QPlanSample*>(p.d);
+  QSample* d_s = reinterpret_cast<QSample*>(p.d + p.off_samples);
+  QBatch* d_b = reinterpret_cast<QBatch*>(p.d + p.off_batches);
+  QEntry* d_e = reinterpret_cast<QEntry*>(p.d + p.off_entries);
+  if (n_batches) {
+    launch_pdl(k_quotient_gather, dim3(n_batches), dim3(256), 0, s, d_ps, d_vals, pp, d_s, d_b);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return STWO_ERR_CUDA;
+    launch_pdl(k_quotient_coeffs, dim3(n_batches), dim3(QC_THREADS), 0, s, d_s, d_b, d_e,
+               qm31{{rc.v[0], rc.v[1]}, {rc.v[2], rc.v[3]}});
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return STWO_ERR_CUDA;
+  }
+  return quotient_rows_and_extend(p.log_n, p.cols.data(), (uint32_t)p.cols.size(), d_b, n_batches, d_e,
+                                  p.log_blowup, reinterpret_cast<uint32_t*>(p.d + p.off_sub), out, s);
+}
+
+void quot_plan_free(QuotPlan& p, cudaStream_t s) {
+  if (p.d) scratch_free(p.d, s);
+  p.d = nullptr;
 }
 
 }  // namespace stwo
