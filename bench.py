@@ -113,6 +113,20 @@ class ClockSampler:
                 "samples": len(sm), "period_ms": self.period_ms}
 
 
+def autotune_pass(run_once):
+    """One untimed run with the library's autotuner measuring the launch shapes of every size it
+    meets (results unchanged), then the table in use for everything after."""
+    from stwo_gb300 import autotune
+
+    autotune.set_mode(autotune.TUNE)
+    try:
+        run_once()
+    finally:
+        autotune.set_mode(autotune.USE)
+    return {"entries": len(autotune.entries()), "choices": autotune.summary(),
+            "note": "launch shapes timed once per size before the warm-up, then used"}
+
+
 def int_bound(kind, achieved, clocks, local):
     """Integer-datapath bound of a stage from the library's register-only probe of its inner
     operation (`kind` "butterfly" or "blake2s"): the probe's issue cost in SM cycles per warp-wide
@@ -516,6 +530,7 @@ def run_batch(args, world, rank, local, lib, barrier, max_over_ranks, emit=True)
         torch.cuda.synchronize()
         return time.perf_counter() - t0, res
 
+    tuned = autotune_pass(lambda: run(1))  # one worker: each shape timed with the GPU to itself
     for _ in range(args.warmup):
         run(workers)
     barrier()
@@ -563,6 +578,7 @@ def run_batch(args, world, rank, local, lib, barrier, max_over_ranks, emit=True)
                 "d2h_bytes_per_step": sum(len(r.proof) for r in res)},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
+        "autotune": tuned,
     }
     if not emit:
         return line
@@ -959,7 +975,7 @@ def run_gb300(args):
         b = run_batch(side, world, rank, local, lib, barrier, max_over_ranks, emit=False)
         line["batch"] = {k: b[k] for k in ("metric", "value", "unit", "ms_per_step", "plain", "speedup_vs_plain",
                                            "plain_breakdown", "proofs_identical_to_plain", "e2e", "gpu_launches",
-                                           "clocks")}
+                                           "clocks", "autotune")}
         side = argparse.Namespace(**{**vars(args), "steps": 3, "warmup": 1})
         v = run_serve(side, world, rank, local, lib, barrier, max_over_ranks, emit=False)
         line["serve"] = {k: v[k] for k in ("metric", "value", "unit", "p50_ms", "plain", "p99_vs_plain",

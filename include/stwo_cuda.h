@@ -72,6 +72,18 @@ uint64_t stwo_kernel_launches(void);
  * returns the number of distinct stages and fills up to `cap` names / summed milliseconds. */
 stwo_status stwo_set_stage_timing(int enable);
 uint32_t stwo_stage_times(const char** names, float* ms, uint32_t cap);
+/* Autotuner without a reference counterpart: launch shapes of some operations (a Merkle leaf
+ * layer's kernel variant and block size; rows per lane of the quotient pass) chosen per size key.
+ * mode 0: the built-in choices; 1: the table's entry where there is one; 2: as 1, and a key not in
+ * the table is measured on the call's own data (each candidate timed as the best of three runs after
+ * a warm-up; another shape replaces the built-in one when it is at least 3% faster; the operation's
+ * results are unchanged). The table is process-wide:
+ * stwo_autotune_entries copies up to `cap` entries and returns how many there are, set_entry adds
+ * or replaces one (entries saved by a caller can be loaded back), clear empties it. */
+stwo_status stwo_autotune_mode(int mode);
+uint32_t stwo_autotune_entries(uint32_t* sites, uint64_t* keys, uint32_t* choices, uint32_t cap);
+stwo_status stwo_autotune_set_entry(uint32_t site, uint64_t key, uint32_t choice);
+stwo_status stwo_autotune_clear(void);
 /* Diagnostic without a reference counterpart: the circle-FFT butterfly of the library's FFT
  * kernels with every operand in registers (one full wave of blocks, `rounds` rounds of 32
  * butterflies per thread, on `stream`). `h_butterflies_per_s` is its rate from event timing;

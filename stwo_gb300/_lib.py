@@ -77,6 +77,10 @@ SIGNATURES = {
     "stwo_set_stage_timing": (C.c_int32, [C.c_int]),
     "stwo_butterfly_rate": (C.c_int32, [U32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), VP]),
     "stwo_blake2s_rate": (C.c_int32, [U32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), VP]),
+    "stwo_autotune_mode": (C.c_int32, [C.c_int]),
+    "stwo_autotune_entries": (U32, [C.POINTER(U32), C.POINTER(C.c_uint64), C.POINTER(U32), U32]),
+    "stwo_autotune_set_entry": (C.c_int32, [U32, C.c_uint64, U32]),
+    "stwo_autotune_clear": (C.c_int32, []),
     "stwo_stage_times": (C.c_uint32, [C.POINTER(C.c_char_p), C.POINTER(C.c_float), U32]),
     "stwo_buf_alloc": (C.c_int32, [PVP, C.c_size_t, VP]),
     "stwo_buf_free": (C.c_int32, [VP, VP]),

@@ -11,6 +11,7 @@
 #include <vector>
 #include <tuple>
 #include <algorithm>
+#include <atomic>
 #include "../../include/stwo_cuda.h"
 #include "field.cuh"
 
@@ -264,6 +265,73 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
 // evaluation takes, are known before the points are: eval_plan_build lays out and uploads the job
 // tables (stream-ordered, while the device still works on earlier stages), eval_plan_run takes the
 // points and evaluates, eval_plan_free releases the device block.
+// Autotuner. Some launch shapes depend on the sizes in ways a fixed rule only approximates (a
+// Merkle leaf layer's kernel variant and block size, how many rows a quotient lane takes). At such
+// a site the library asks tune_choice: with tuning off it returns the built-in choice; in "use"
+// mode it returns the table's entry for (site, key) when there is one; in "tune" mode a key not yet
+// in the table is measured on the caller's own data first — each candidate timed with events on
+// the stream — and the choice recorded. Only operations that
+// recompute their whole output from their inputs are tuned this way, so the measuring leaves the
+// results as they would be. The table is process-wide; the host saves and loads it as entries.
+constexpr uint32_t TUNE_MERKLE_LAYER = 1, TUNE_QUOTIENT_ROWS = 2;
+struct TuneState {
+  std::atomic<int> mode{0};
+  std::mutex mu;
+  std::map<std::pair<uint32_t, uint64_t>, uint32_t> table;
+};
+TuneState& tune_state();
+int tune_mode();  // 0 off, 1 use the table, 2 tune keys not in it
+bool tune_lookup(uint32_t site, uint64_t key, uint32_t* choice);
+void tune_record(uint32_t site, uint64_t key, uint32_t choice);
+// Candidates are timed as the best of three runs after a warm-up; another shape replaces the
+// built-in one only when it is at least 3% faster, so that timing noise does not move the choice.
+template <class Launch>
+int32_t tune_choice(uint32_t site, uint64_t key, uint32_t builtin, const uint32_t* cands, uint32_t n_cands,
+                    cudaStream_t s, Launch&& launch, uint32_t* choice) {
+  *choice = builtin;
+  const int mode = tune_mode();
+  if (mode == 0) return STWO_OK;
+  if (tune_lookup(site, key, choice)) return STWO_OK;
+  if (mode != 2) return STWO_OK;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  STWO_CHECK_CUDA(cudaEventCreate(&e0));
+  STWO_CHECK_CUDA(cudaEventCreate(&e1));
+  auto time_of = [&](uint32_t c, float* best_ms) -> int32_t {
+    int32_t st = launch(c);  // warm
+    *best_ms = 0.f;
+    for (int r = 0; r < 3 && !st; r++) {
+      float ms = 0.f;
+      if (cudaEventRecord(e0, s) != cudaSuccess) return STWO_ERR_CUDA;
+      st = launch(c);
+      if (st) break;
+      if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        return STWO_ERR_CUDA;
+      if (r == 0 || ms < *best_ms) *best_ms = ms;
+    }
+    return st;
+  };
+  float base = 0.f, best = 0.f;
+  uint32_t pick = builtin;
+  int32_t st = time_of(builtin, &base);
+  best = base;
+  for (uint32_t i = 0; i < n_cands && !st; i++) {
+    if (cands[i] == builtin) continue;
+    float ms = 0.f;
+    st = time_of(cands[i], &ms);
+    if (!st && ms < best) {
+      best = ms;
+      pick = cands[i];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  *choice = best < 0.97f * base ? pick : builtin;
+  tune_record(site, key, *choice);
+  return STWO_OK;
+}
+
 // At most this many distinct points (mask offsets) per planned evaluation or quotient group.
 constexpr uint32_t EP_MAX_POINTS = 8;
 struct EvalPlan {

@@ -115,18 +115,19 @@ int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint3
     int32_t st = scratch_alloc((void**)&state, (size_t)n * 9 * 4, s);
     if (st) return st;
   }
-  // A small layer goes out as one-warp blocks, so that its few warps land on different SMs
-  // instead of sharing the issue slots of one. Larger layers use two-warp blocks: a layer of
-  // 2^17 nodes is then 2,048 blocks, 13-14 per SM, where 256-thread blocks (3 or 4 per SM) left
-  // the SMs with three blocks idle for a quarter of the launch.
-  const uint32_t threads = n <= MERKLE_LAT_NODES ? 32 : 64;
-  const uint32_t blocks = (n + threads - 1) / threads;
-  for (uint32_t l = 0; l < n_launch; l++) {
-    uint32_t c0 = l * per_launch;
-    uint32_t nc = n_cols - c0 < per_launch ? n_cols - c0 : per_launch;
+  // Built-in shape: a small layer goes out as one-warp blocks of the latency kernel, so that its
+  // few warps land on different SMs instead of sharing the issue slots of one. Larger layers use
+  // two-warp blocks: a layer of 2^17 nodes is then 2,048 blocks, 13-14 per SM, where 256-thread
+  // blocks (3 or 4 per SM) left the SMs with three blocks idle for a quarter of the launch.
+  // Shape c: 0 = latency kernel, 32 threads; 1..4 = throughput kernel, 32 << (c - 1) threads.
+  auto launch_shape = [&](uint32_t shape, uint32_t l) -> int32_t {
+    const uint32_t c0 = l * per_launch;
+    const uint32_t nc = n_cols - c0 < per_launch ? n_cols - c0 : per_launch;
     MerkleCols mc;
     for (uint32_t q = 0; q < nc; q++) mc.p[q] = cols[c0 + q];
-    if (n <= MERKLE_LAT_NODES)
+    const uint32_t threads = shape == 0 ? 32u : 32u << (shape - 1);
+    const uint32_t blocks = (n + threads - 1) / threads;
+    if (shape == 0)
       launch_pdl(k_merkle_layer<true>, dim3(blocks), dim3(threads), 0, s, n, prev, mc, nc, out, state, l == 0,
                  l + 1 == n_launch, 1u);
     else
@@ -135,13 +136,23 @@ int32_t merkle_commit_layer(uint32_t log_size, const uint32_t* prev, const uint3
     note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
-      scratch_free(state, s);
       set_error("merkle launch: %s", cudaGetErrorString(e));
       return STWO_ERR_CUDA;
     }
+    return STWO_OK;
+  };
+  uint32_t shape = n <= MERKLE_LAT_NODES ? 0u : 2u;
+  int32_t st = STWO_OK;
+  if (n_launch == 1 && log_size >= 10) {
+    // One launch recomputes the layer from its inputs, so it can be timed in place.
+    static const uint32_t cands[] = {0, 1, 2, 3, 4};
+    const uint64_t comps = (n_cols + 15) / 16 + (prev ? 1 : 0);
+    st = tune_choice(TUNE_MERKLE_LAYER, ((uint64_t)log_size << 32) | comps, shape, cands, 5, s,
+                     [&](uint32_t c) { return launch_shape(c, 0); }, &shape);
   }
+  for (uint32_t l = 0; l < n_launch && !st; l++) st = launch_shape(shape, l);
   scratch_free(state, s);
-  return STWO_OK;
+  return st;
 }
 
 // ---------------------------------------------------------------- node subtrees

@@ -400,29 +400,49 @@ static int32_t quotient_rows_and_extend(uint32_t log_n, const uint32_t* const* c
   for (uint32_t c = 0; c < n_cols; c++) qc.p[c] = cols[c];
   uint32_t* o[4];
   for (int q = 0; q < 4; q++) o[q] = direct ? out[q] : d_sub + (size_t)q * rows;
-  // Four rows per lane once the domain gives at least four 128-row blocks per SM, else two.
-  const int rpl = rows >= 4u * 128u * (uint32_t)sm_count() ? 4 : 2;
-  bool aligned = rows % (32 * rpl) == 0;
-  for (uint32_t c = 0; c < n_cols && aligned; c++)
-    aligned = (reinterpret_cast<uintptr_t>(cols[c]) & (4 * rpl - 1)) == 0;
-  if (aligned && rpl == 4)
-    launch_pdl(k_quotient_rows4<4>, dim3(rows / 128), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
-               dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
-  else if (aligned)
-    launch_pdl(k_quotient_rows4<2>, dim3(rows / 64), dim3(Q_SLICES * 32), 0, s, rows, log_n, dom_half.initial_index,
-               dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
-  else
-    launch_pdl(k_quotient_rows, dim3((rows + Q_ROWS - 1) / Q_ROWS), dim3(Q_SLICES * 32), 0, s, rows, log_n,
-               dom_half.initial_index, dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
-  note_launch();
-  if (cudaGetLastError() != cudaSuccess) return STWO_ERR_CUDA;
+  // Rows per lane: 4 or 2 (16- or 8-byte column loads; needs that alignment and a multiple of
+  // 32 x that many rows), or 1 (the 32-row kernel). Built in: four once the domain gives at least
+  // four 128-row blocks per SM, else two.
+  auto fits = [&](uint32_t rpl) {
+    if (rpl == 1) return true;
+    bool ok = rows % (32 * rpl) == 0;
+    for (uint32_t c = 0; c < n_cols && ok; c++) ok = (reinterpret_cast<uintptr_t>(cols[c]) & (4 * rpl - 1)) == 0;
+    return ok;
+  };
+  auto launch_rows = [&](uint32_t rpl) -> int32_t {
+    if (rpl == 4)
+      launch_pdl(k_quotient_rows4<4>, dim3(rows / 128), dim3(Q_SLICES * 32), 0, s, rows, log_n,
+                 dom_half.initial_index, dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
+    else if (rpl == 2)
+      launch_pdl(k_quotient_rows4<2>, dim3(rows / 64), dim3(Q_SLICES * 32), 0, s, rows, log_n,
+                 dom_half.initial_index, dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
+    else
+      launch_pdl(k_quotient_rows, dim3((rows + Q_ROWS - 1) / Q_ROWS), dim3(Q_SLICES * 32), 0, s, rows, log_n,
+                 dom_half.initial_index, dom_half.step_size, qc, d_b, n_batches, d_e, o[0], o[1], o[2], o[3]);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? STWO_OK : STWO_ERR_CUDA;
+  };
+  uint32_t rpl = rows >= 4u * 128u * (uint32_t)sm_count() ? 4 : 2;
+  if (!fits(rpl)) rpl = fits(2) ? 2 : 1;
+  uint32_t cands[3], n_cands = 0;
+  for (uint32_t c : {4u, 2u, 1u})
+    if (fits(c)) cands[n_cands++] = c;
+  int32_t st = STWO_OK;
+  if (rows >= 1024) {
+    // The row pass recomputes its outputs from the columns, so it can be timed in place.
+    const uint64_t key = ((uint64_t)log_n << 40) | ((uint64_t)log_blowup << 32) | n_cols;
+    st = tune_choice(TUNE_QUOTIENT_ROWS, key, rpl, cands, n_cands, s, launch_rows, &rpl);
+    if (st) return st;
+  }
+  st = launch_rows(rpl);
+  if (st) return st;
 
   if (!direct) {
     // Interpolate on the sub-domain (its own tree), then evaluate on the full canonic domain.
     stwo_coset sub_half = coset_new(dom_half.initial_index, sub_log - 1);
     TwiddleTree* t_sub = nullptr;
     TwiddleTree* t_dom = nullptr;
-    int32_t st = get_tree(sub_half, s, &t_sub);
+    st = get_tree(sub_half, s, &t_sub);
     if (!st) st = get_tree(dom_half, s, &t_dom);
     if (!st) st = fft_interpolate_evaluate(t_sub, sub_half, o, 4, t_dom, dom_half, out, s);
     if (st) return st;

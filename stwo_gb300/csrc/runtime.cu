@@ -49,6 +49,25 @@ DeviceContext& ctx() {
   return c;
 }
 
+TuneState& tune_state() {
+  static TuneState t;
+  return t;
+}
+int tune_mode() { return tune_state().mode.load(); }
+bool tune_lookup(uint32_t site, uint64_t key, uint32_t* choice) {
+  TuneState& t = tune_state();
+  std::lock_guard<std::mutex> g(t.mu);
+  auto it = t.table.find({site, key});
+  if (it == t.table.end()) return false;
+  *choice = it->second;
+  return true;
+}
+void tune_record(uint32_t site, uint64_t key, uint32_t choice) {
+  TuneState& t = tune_state();
+  std::lock_guard<std::mutex> g(t.mu);
+  t.table[{site, key}] = choice;
+}
+
 int sm_count() {
   static const int n = [] {
     int dev = 0, v = 0;
@@ -334,6 +353,36 @@ const char* stwo_status_string(stwo_status s) {
 const char* stwo_last_error(void) { return g_err; }
 
 uint64_t stwo_kernel_launches(void) { return g_launches.load(); }
+
+stwo_status stwo_autotune_mode(int mode) {
+  STWO_REQUIRE(mode >= 0 && mode <= 2, "autotune mode %d (0 off, 1 use, 2 tune)", mode);
+  tune_state().mode.store(mode);
+  return STWO_OK;
+}
+stwo_status stwo_autotune_set_entry(uint32_t site, uint64_t key, uint32_t choice) {
+  tune_record(site, key, choice);
+  return STWO_OK;
+}
+uint32_t stwo_autotune_entries(uint32_t* sites, uint64_t* keys, uint32_t* choices, uint32_t cap) {
+  TuneState& t = tune_state();
+  std::lock_guard<std::mutex> g(t.mu);
+  uint32_t i = 0;
+  for (const auto& kv : t.table) {
+    if (i < cap && sites && keys && choices) {
+      sites[i] = kv.first.first;
+      keys[i] = kv.first.second;
+      choices[i] = kv.second;
+    }
+    i++;
+  }
+  return i;
+}
+stwo_status stwo_autotune_clear(void) {
+  TuneState& t = tune_state();
+  std::lock_guard<std::mutex> g(t.mu);
+  t.table.clear();
+  return STWO_OK;
+}
 
 stwo_status stwo_set_stage_timing(int enable) {
   g_stage_on = enable != 0;

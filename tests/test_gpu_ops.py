@@ -300,3 +300,44 @@ def test_blake2s_rate_diagnostic(cuda):
     assert rate.value > 0 and 100.0 < cyc.value < 20000.0 and 100.0 < mhz.value < 3000.0
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     assert rate.value <= 4 * sms * mhz.value * 1.05e6 * 32 / cyc.value
+
+
+def test_autotuned_shapes_give_the_same_results(cuda, oracle):
+    """In tune mode the Merkle layer and the quotient row pass time their candidate shapes on the
+    call's own data; the results still equal the oracle's, and the table records one of the
+    candidates for each size."""
+    import torch
+    from stwo_gb300 import autotune
+
+    autotune.clear()
+    autotune.set_mode(autotune.TUNE)
+    try:
+        rng = np.random.default_rng(4242)
+        for log, ncols in [(11, 20), (14, 5)]:
+            n = 1 << log
+            cols = [F.rand_m31(rng, n) for _ in range(ncols)]
+            got = cuda.commit_on_layer(log, None, [dev(c) for c in cols])
+            torch.cuda.synchronize()
+            assert np.array_equal(host(got).reshape(-1, 8), oracle.commit_on_layer(log, None, cols))
+        log_n, blowup = 13, 1
+        cols = [F.rand_m31(rng, 1 << log_n) for _ in range(6)]
+        pts = sorted(rand_point(oracle, rng) for _ in range(2))
+        batches = [(pts[0], [(c, rq(rng)) for c in range(6)]), (pts[1], [(c, rq(rng)) for c in range(0, 6, 2)])]
+        rc = rq(rng)
+        out = cuda.accumulate_quotients(log_n, [dev(c) for c in cols], rc, batches, blowup)
+        want = oracle.accumulate_quotients(log_n, cols, rc, batches, blowup)
+        for k in range(4):
+            assert np.array_equal(host(out.cols[k]), want[k])
+        table = autotune.entries()
+        merkle = [e for e in table if e["site"] == 1]
+        quot = [e for e in table if e["site"] == 2]
+        assert len(merkle) == 2 and all(e["choice"] in (0, 1, 2, 3, 4) for e in merkle)
+        assert len(quot) == 1 and quot[0]["choice"] in (1, 2, 4)
+        # With the table in use, the same calls give the same results again.
+        autotune.set_mode(autotune.USE)
+        out2 = cuda.accumulate_quotients(log_n, [dev(c) for c in cols], rc, batches, blowup)
+        for k in range(4):
+            assert np.array_equal(host(out2.cols[k]), want[k])
+    finally:
+        autotune.set_mode(autotune.OFF)
+        autotune.clear()
