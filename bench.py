@@ -1090,7 +1090,7 @@ def run_kernels(args, world, rank, local, lib, barrier, max_over_ranks):
                    "l2": "inputs (1 GiB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
         "stages_ms": {"interpolate": stage_ms[0], "evaluate": stage_ms[1], "merkle_leaves": stage_ms[2],
                       "merkle_nodes": stage_ms[3], "fri_folds": stage_ms[4]},
-        "roofline": {"bound": "hbm", "kernel": "k_fft_pass<evaluate> (2 passes per call)",
+        "roofline": {"bound": "hbm", "kernel": "evaluate 2^20 -> 2^22: k_fft_reg + k_fft_tile passes (integer-bound: see int_bound)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_call": eval_bytes},

@@ -459,7 +459,7 @@ int32_t Prover::commit_evals(const std::vector<uint32_t*>& cols, uint32_t log_si
   // Interpolate in place (the evaluation is consumed, as PolyOps::interpolate takes it by value),
   // then evaluate on the blown-up domain; the pass the two transforms share runs fused where it
   // can (fft_interpolate_extend_begin), so the coefficients are read back from HBM once less.
-  if (cols.empty()) return commit_polys(cols, {});
+  if (cols.empty()) return commit_polys({}, {});
   const uint32_t el = log_size + cfg.log_blowup_factor;
   uint32_t* block = arena.alloc(cols.size() << el);
   if (!block) return STWO_ERR_OOM;
