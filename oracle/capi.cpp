@@ -475,6 +475,7 @@ void oracle_channel_draw_felts(size_t n, uint32_t* out) {
 #include "air_blake_round.h"
 #include "air_examples.h"
 #include "components.h"
+#include "air_blake_full.h"
 
 extern "C" {
 
@@ -565,6 +566,12 @@ int oracle_eval_constraints(uint32_t air_id, uint32_t log_n, uint32_t n_cols, co
     };
     std::unique_ptr<Air> air;
     std::vector<size_t> tree_cols;
+    BlakeAllElements all;  // outlives the Blake scheduler / XOR-table AIRs, which point into it
+    auto set_rel = [&](auto& r, int k, size_t n) {
+      r.z = q_of(elements + 8 * k);
+      r.alpha = q_of(elements + 8 * k + 4);
+      rel_powers(r.alpha, r.alpha_powers, n);
+    };
     if (air_id == 0) {
       air.reset(new WideFibAir(log_n, n_cols));
       tree_cols = {0, n_cols};
@@ -605,6 +612,22 @@ int oracle_eval_constraints(uint32_t air_id, uint32_t log_n, uint32_t n_cols, co
         air.reset(new StateTransitionAir(air_id - 4, log_n, r, q_of(claimed_sum)));
         tree_cols = {0, 2, 4};
       }
+    } else if (air_id == 6) {
+      // The full Blake example's scheduler: elements (Blake, Round).
+      if (n_elements != 4) return 1;
+      set_rel(all.blake, 0, BR_ROUND_FELTS);
+      set_rel(all.round.round, 1, BR_ROUND_FELTS);
+      air.reset(new BlakeSchedulerAir(log_n, &all, q_of(claimed_sum)));
+      tree_cols = {0, BF_SCHED_COLS, 4 * BF_SCHED_BATCHES};
+    } else if (air_id == 7) {
+      // An XOR table of the full Blake example: n_cols = its element bits; elements (XorElements).
+      if (n_elements != 2) return 1;
+      size_t t = xor_table_index(n_cols);
+      const XorTableShape& sh = BF_XOR_TABLES[t];
+      Relation<3>& r = const_cast<Relation<3>&>(all.round.xor_.of(n_cols));
+      set_rel(r, 0, 3);
+      air.reset(new XorTableAir(sh, &r, q_of(claimed_sum)));
+      tree_cols = {3, sh.n_mult_cols(), 4 * sh.n_batches()};
     } else {
       return 1;
     }
@@ -730,6 +753,63 @@ size_t oracle_prove_state_machine(uint32_t log_n, const uint32_t initial[2], con
     return bytes.size();
   } catch (const std::exception& e) {
     snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// prove_blake (blake/air.rs:308-460) for 2^log_n instances: the stark proof's canonical bytes and
+// the eight claimed sums (scheduler, round 0, round 1, XOR tables 12, 9, 8, 7, 4).
+size_t oracle_prove_blake(uint32_t log_n, const uint32_t cfg[4], uint8_t* out, size_t cap, uint32_t sums[32],
+                          char* err, size_t err_cap) {
+  try {
+    QM31 cs[8];
+    std::vector<uint8_t> bytes = serialize(prove_blake(log_n, PcsConfig{cfg[0], cfg[1], cfg[2], cfg[3]}, cs));
+    if (bytes.size() > cap) throw std::runtime_error("output buffer too small");
+    std::memcpy(out, bytes.data(), bytes.size());
+    for (int i = 0; i < 8; i++) q_to(cs[i], sums + 4 * i);
+    return bytes.size();
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+// verify_blake (blake/air.rs:462-520) given the eight claimed sums.
+int oracle_verify_blake(uint32_t log_n, const uint32_t sums[32], const uint8_t* proof, size_t len, char* err,
+                        size_t err_cap) {
+  try {
+    StarkProof p;
+    if (!deserialize(proof, len, p)) throw std::runtime_error("malformed proof bytes");
+    QM31 cs[8];
+    for (int i = 0; i < 8; i++) cs[i] = q_of(sums + 4 * i);
+    std::string r = verify_blake(log_n, cs, p);
+    if (!r.empty()) throw std::runtime_error(r);
+    return 1;
+  } catch (const std::exception& e) {
+    snprintf(err, err_cap, "%s", e.what());
+    return 0;
+  }
+}
+
+// The trace tree of prove_blake (the preprocessed columns, then the trace columns), in commit order,
+// written to `out` column after column; returns the number of words (0 on error or if cap is short).
+size_t oracle_blake_traces(uint32_t log_n, uint32_t* out, size_t cap, uint32_t* n_cols) {
+  try {
+    BlakeFullTraces T = blake_full_traces(log_n);
+    size_t w = 0, k = 0;
+    for (const auto* tree : {&T.preprocessed, &T.trace})
+      for (const Column& c : *tree) {
+        if (w + c.size() > cap) return 0;
+        for (const M31& x : c) out[w++] = x.v;
+        k++;
+      }
+    *n_cols = (uint32_t)k;
+    return w;
+  } catch (...) {
     return 0;
   }
 }

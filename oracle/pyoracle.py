@@ -254,6 +254,43 @@ def prove_state_machine(log_n, initial=(0, 0), config=(5, 1, 0, 3)):
     return bytes(out[:n]), (tuple(int(x) for x in cs[:4]), tuple(int(x) for x in cs[4:]))
 
 
+def prove_blake(log_n, config=(5, 1, 0, 3)):
+    """(stark proof bytes, eight claimed sums) of prove_blake (blake/air.rs:308-460) for 2^log_n
+    instances: scheduler, round 0, round 1, XOR tables 12, 9, 8, 7, 4."""
+    cap = 256 << 20
+    out = np.zeros(cap, np.uint8)
+    cs = np.zeros(32, np.uint32)
+    err = C.create_string_buffer(512)
+    f = lib().oracle_prove_blake
+    f.restype = C.c_size_t
+    cfg = _u32(config)
+    n = f(C.c_uint32(log_n), _p(cfg), _p(out), C.c_size_t(cap), _p(cs), err, C.c_size_t(512))
+    if n == 0:
+        raise RuntimeError("oracle prove failed: " + err.value.decode())
+    return bytes(out[:n]), [tuple(int(x) for x in cs[4 * i:4 * i + 4]) for i in range(8)]
+
+
+def verify_blake(log_n, sums, proof: bytes):
+    buf = np.frombuffer(proof, dtype=np.uint8).copy()
+    err = C.create_string_buffer(512)
+    cs = _u32([x for q in sums for x in q])
+    ok = lib().oracle_verify_blake(C.c_uint32(log_n), _p(cs), _p(buf), C.c_size_t(len(proof)), err, C.c_size_t(512))
+    return bool(ok), err.value.decode()
+
+
+def blake_traces(log_n):
+    """The preprocessed and trace columns of prove_blake, in commit order, as one word array."""
+    cap = 64 << 20
+    out = np.zeros(cap, np.uint32)
+    k = C.c_uint32(0)
+    f = lib().oracle_blake_traces
+    f.restype = C.c_size_t
+    n = f(C.c_uint32(log_n), _p(out), C.c_size_t(cap), C.byref(k))
+    if n == 0:
+        raise RuntimeError("oracle blake_traces failed")
+    return out[:n].copy(), k.value
+
+
 def verify_plonk(log_n, claimed_sum, proof: bytes):
     buf = np.frombuffer(proof, dtype=np.uint8).copy()
     err = C.create_string_buffer(512)

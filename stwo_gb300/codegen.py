@@ -39,6 +39,31 @@ from .expr import BaseExpr, Expr, ExprEvaluator
 SMEM_BUDGET = 40 * 1024  # shared memory for the column table and the powers, bytes
 
 
+# A row-loop body of more straight-line statements than this (no repeated group became a loop) is
+# compiled for compile time: NVRTC's default pipeline is superlinear in the size of one basic block
+# (a 2,700-statement Blake2s round body took minutes), so such a body is cut into blocks of
+# FLAT_BLOCK statements by branches the compiler cannot remove, and the source asks for
+# --Ofast-compile=max (FAST_COMPILE_MARK, read by the library's NVRTC call).
+FLAT_SPLIT_MIN = 1000
+FLAT_BLOCK = 40
+FAST_COMPILE_MARK = "// stwo-codegen: fast-compile"
+
+
+def _split_flat(body: List[str]) -> Tuple[List[str], bool]:
+    """`body` with a block boundary after every FLAT_BLOCK top-level statements when it has more
+    than FLAT_SPLIT_MIN of them; and whether it was split."""
+    top = [i for i, x in enumerate(body) if not x.startswith((" ", "#", "for ", "}"))]
+    if len(top) <= FLAT_SPLIT_MIN:
+        return body, False
+    cut = set(top[FLAT_BLOCK - 1::FLAT_BLOCK])
+    out = []
+    for i, x in enumerate(body):
+        out.append(x)
+        if i in cut:
+            out.append('if (a.trace_log == 0xFFFFFFFFu) asm volatile("");')
+    return out, True
+
+
 class _Gen:
     def __init__(self, ev: ExprEvaluator):
         self.ev = ev
@@ -159,6 +184,8 @@ class _Gen:
                 tok = ("c", slots.setdefault(t, len(slots)), c.offset)
             elif n.kind in ("const", "param"):
                 tok = (n.kind, n.is_ext, n.val)
+            elif n.kind == "combine":
+                tok = (n.kind, n.is_ext, n.val) + tuple(canon[a.uid] for a in n.args)
             else:
                 tok = (n.kind, n.is_ext) + tuple(canon[a.uid] for a in n.args)
             canon[n.uid] = len(toks)
@@ -214,6 +241,20 @@ class _Gen:
                 dest.append(f"const uint32_t {code} = __ldg(a.params + {4 * k});")
         return (code, "q" if is_ext else "b", out is None)
 
+    def _param_block(self, name: str, size: int) -> int:
+        """The parameter index of <name>_alpha0, with <name>_alpha0 .. <name>_alpha{size-1}
+        registered as consecutive parameters (gen_combine reads them by index)."""
+        first = f"{name}_alpha0"
+        if first not in self.param_index:
+            for i in range(size):
+                nm = f"{name}_alpha{i}"
+                assert nm not in self.param_index, nm
+                self.param_index[nm] = len(self.params)
+                self.params.append((nm, True))
+        k0 = self.param_index[first]
+        assert all(self.param_index.get(f"{name}_alpha{i}") == k0 + i for i in range(size)), name
+        return k0
+
     def _offset(self, off: int) -> str:
         rv = self.offsets.get(off)
         if rv is None:
@@ -257,6 +298,17 @@ class _Gen:
             return (name, "b", False)
         uni = self.uniform.get(n.uid, False)
         args = [self._ref(a, memo, out, uni) for a in n.args]
+        if k == "combine":
+            name, size = n.val
+            k0 = self._param_block(name, size)
+            zname = f"{name}_z"
+            if zname not in self.param_index:
+                self.param_index[zname] = len(self.params)
+                self.params.append((zname, True))
+            arr = f"v{n.uid}"
+            (self.pre if uni else out).append(f"const uint32_t {arr}[{len(args)}] = {{{', '.join(a[0] for a in args)}}};")
+            return self._stmt(uni, "q", f"gen_combine(a.params, {k0}, {arr}, {len(args)}, {self.param_index[zname]})",
+                              n.uid, out)
         if k == "secure_col":
             zero = BaseExpr.zero()
             if all(a is zero for a in n.args[1:]):
@@ -354,10 +406,12 @@ class _Gen:
             body.append(f"for (int g = 0; g < {m}; g++) {{")
             body += ["  " + x for x in inner]
             body.append("}")
+        body, flat = _split_flat(body)
         nc = max(self.n_cols, 1)
         threads = rows_per_iter = 128
         lines = [
             "// Generated from a constraint-framework component by stwo_gb300/codegen.py.",
+        ] + ([FAST_COMPILE_MARK] if flat else []) + [
             '#include "codegen_rt.cuh"',
             "using namespace stwo;",
             "typedef unsigned short uint16_t;",
@@ -438,9 +492,11 @@ class _FracGen(_Gen):
             body.append(f"prev = qm31_add(prev, qm31_mul({lift(num)}, qm31_inv({lift(den)})));")
             for j, c in enumerate(("prev.a.a", "prev.a.b", "prev.b.a", "prev.b.b")):
                 body.append(f"a.acc0[(size_t){4 * b + j} * n_rows + row] = {c};")
+        body, flat = _split_flat(body)
         nc = max(self.n_cols, 1)
         lines = [
             "// Generated from a constraint-framework component by stwo_gb300/codegen.py.",
+        ] + ([FAST_COMPILE_MARK] if flat else []) + [
             '#include "codegen_rt.cuh"',
             "using namespace stwo;",
             'extern "C" __constant__ uint32_t stwo_generated_layout[2] = {128, 128};',

@@ -14,6 +14,7 @@
 // it reverses the accumulator's slice of random-coefficient powers, computes the bit-reversed
 // vanishing inverses and launches the kernel, which adds row_res * denom_inv to the column.
 #include "common.cuh"
+#include <cstring>
 #include "prover.cuh"
 #include "codegen_rt.cuh"
 #include <nvrtc.h>
@@ -44,8 +45,11 @@ static int32_t nvrtc_compile(const char* src, std::string& cubin) {
     set_error("nvrtcCreateProgram: %s", nvrtcGetErrorString(r));
     return STWO_ERR_CUDA;
   }
-  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo"};
-  r = nvrtcCompileProgram(prog, 3, opts);
+  // A source that marks itself (a long straight-line body, cut into blocks by the generator) is
+  // compiled with the fast-compile pipeline: the default one takes minutes on such a body.
+  const bool fast = std::strstr(src, "// stwo-codegen: fast-compile\n") != nullptr;
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--Ofast-compile=max"};
+  r = nvrtcCompileProgram(prog, fast ? 4 : 3, opts);
   if (r != NVRTC_SUCCESS) {
     size_t n = 0;
     nvrtcGetProgramLogSize(prog, &n);

@@ -72,5 +72,22 @@ __device__ __forceinline__ void gen_fold(uint64_t acc[4]) {
   for (int j = 0; j < 4; j++) acc[j] = m31_fold64(acc[j]);
 }
 __device__ __forceinline__ qm31 gen_q_of_u4(const uint4& p) { return qm31_from_u32(p.x, p.y, p.z, p.w); }
+// A relation entry sum_i alpha_i v_i - z over n base values, the alpha powers being parameters
+// k0 .. k0 + n - 1 and z parameter kz: four 64-bit coordinate sums folded every third product, in
+// a loop kept rolled so that a wide entry (96 values) is a few instructions of code, not 96
+// inlined QM31 products.
+__device__ __forceinline__ qm31 gen_combine(const uint32_t* p, int k0, const uint32_t* v, int n, int kz) {
+  uint64_t acc[4] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll 1
+  for (int i = 0; i < n; i++) {
+    const uint32_t* al = p + 4 * (k0 + i);
+    gen_acc_base(acc, make_uint4(__ldg(al), __ldg(al + 1), __ldg(al + 2), __ldg(al + 3)), v[i]);
+    if (i % 3 == 2) gen_fold(acc);
+  }
+  gen_fold(acc);
+  const qm31 s = qm31_from_u32(m31_reduce64(acc[0]), m31_reduce64(acc[1]), m31_reduce64(acc[2]),
+                               m31_reduce64(acc[3]));
+  return qm31_sub(s, gen_param_q(p, kz));
+}
 
 }  // namespace stwo

@@ -92,8 +92,9 @@ _SIMPLIFIED: Dict[int, "Expr"] = {}
 
 class Expr:
     """Common base of BaseExpr and ExtExpr. `kind` is one of col, const, param, add, sub, mul,
-    neg, inv (base only) and secure_col (extension only); `args` are child nodes; `val` holds a
-    constant (int for base, 4-tuple for extension), a parameter name, or a ColumnExpr."""
+    neg, inv (base only), secure_col and combine (extension only); `args` are child nodes; `val`
+    holds a constant (int for base, 4-tuple for extension), a parameter name, a ColumnExpr, or a
+    combine node's (relation name, relation size)."""
 
     __slots__ = ("kind", "args", "val", "uid")
     is_ext = False
@@ -318,6 +319,16 @@ class ExtExpr(Expr):
         return ExtExpr.secure_col(*(BaseExpr.const(x) for x in v))
 
     @staticmethod
+    def combine(relation: "Relation", values: Sequence["BaseExpr"]) -> "ExtExpr":
+        """The relation entry value[0] * <name>_alpha0 + ... - <name>_z as one node, whose kernel
+        code is a loop over the values rather than one product per value."""
+        return ExtExpr("combine", tuple(_as_base(v) for v in values[:relation.size]), (relation.name, relation.size))
+
+    def expanded(self) -> "ExtExpr":
+        """A combine node written out as combine_formal's sum."""
+        return combine_formal(Relation(*self.val), self.args)
+
+    @staticmethod
     def zero() -> "ExtExpr":
         return ExtExpr.from_base(BaseExpr.zero())
 
@@ -357,6 +368,8 @@ class ExtExpr(Expr):
         return done
 
     def _simplify(self) -> "ExtExpr":
+        if self.kind == "combine":
+            return ExtExpr("combine", tuple(a.simplify() for a in self.args), self.val)
         s = _simplify_arith(self)
         if s.kind == "secure_col":
             parts = [p.simplify() for p in s.args]
@@ -383,6 +396,8 @@ class ExtExpr(Expr):
             return f"qm31({v[0]}, {v[1]}, {v[2]}, {v[3]})"
         if k == "param":
             return self.val
+        if k == "combine":
+            return self.expanded().format_expr()
         a = self.args
         if k == "add":
             return f"{a[0].format_expr()} + {a[1].format_expr()}"
@@ -403,6 +418,8 @@ class ExtExpr(Expr):
 
     def _degree(self, named: "NamedExprs") -> int:
         k = self.kind
+        if k == "combine":
+            return self.expanded().degree_bound(named)
         if k == "secure_col":
             return max(p.degree_bound(named) for p in self.args)
         if k == "const":
@@ -584,6 +601,9 @@ def combine_formal(relation: Relation, values: Sequence[BaseExpr]) -> ExtExpr:
 
 
 PREPROCESSED_TRACE_IDX, ORIGINAL_TRACE_IDX, INTERACTION_TRACE_IDX = 0, 1, 2
+# Relations wider than this are recorded as combine nodes (a loop in the kernel); narrower ones as
+# combine_formal's sum, which the kernel evaluates inline.
+COMBINE_LOOP_MIN = 16
 
 
 class ExprEvaluator:
@@ -659,7 +679,9 @@ class ExprEvaluator:
 
     # ---- LogUp (evaluator.rs:203-215 and logup_proxy, constraint_framework/mod.rs:165-240)
     def add_to_relation(self, relation: Relation, multiplicity, values: Sequence[BaseExpr]) -> None:
-        inter = self.add_extension_intermediate(combine_formal(relation, values))
+        combined = ExtExpr.combine(relation, values) if relation.size > COMBINE_LOOP_MIN else combine_formal(relation,
+                                                                                                          values)
+        inter = self.add_extension_intermediate(combined)
         self.write_logup_frac(Fraction(_as_ext(multiplicity), inter))
 
     def write_logup_frac(self, frac: Fraction) -> None:
@@ -758,6 +780,14 @@ def eval_expr(e: Expr, cols, params: Dict[str, object], memo: Optional[dict] = N
                 v = q_inv(a[0])
             elif k == "secure_col":
                 v = q_from_partial_evals(a)
+            elif k == "combine":
+                name, _ = n.val
+                v = (0, 0, 0, 0)
+                for i, x in enumerate(a):
+                    al = params[f"{name}_alpha{i}"]
+                    v = q_add(v, q_mul((al % P, 0, 0, 0) if isinstance(al, int) else tuple(al), x))
+                z = params[f"{name}_z"]
+                v = q_sub(v, (z % P, 0, 0, 0) if isinstance(z, int) else tuple(z))
             else:
                 raise AssertionError(k)
         if isinstance(v, int):

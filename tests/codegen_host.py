@@ -103,6 +103,13 @@ def accumulate(air, cols, params, coeff_powers, acc):
                 v = (np.array([pow(int(x), P - 2, P) for x in base], np.int64), 0, 0, 0)
             elif k == "secure_col":
                 v = tuple(p[0] for p in a)
+            elif k == "combine":
+                name, _ = node.val
+                v = (0, 0, 0, 0)
+                for i, x in enumerate(a):
+                    t = _qmul(vals[f"{name}_alpha{i}"], x)
+                    v = tuple(_m(p + q) for p, q in zip(v, t))
+                v = tuple(_m(p - q) for p, q in zip(v, vals[f"{name}_z"]))
             else:
                 raise AssertionError(k)
         memo[node.uid] = v

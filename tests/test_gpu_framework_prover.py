@@ -1,8 +1,10 @@
 """Whole proofs of the reference's examples that have no hand-written device prover, from their
-constraint-framework definitions alone: the Plonk example (preprocessed columns, LogUp in pairs)
-and the state machine (two components of different sizes in one proof). Constraint evaluation
-and the LogUp interaction trace run in generated kernels; the proof bytes equal the oracle's
-restatement of prove_fibonacci_plonk / prove_state_machine (oracle/components.h)."""
+constraint-framework definitions alone: the Plonk example (preprocessed columns, LogUp in pairs),
+the state machine (two components of different sizes in one proof) and the full Blake example
+(eight components of five sizes, preprocessed XOR tables). Constraint evaluation and the LogUp
+interaction trace run in generated kernels; the proof bytes equal the oracle's restatement of
+prove_fibonacci_plonk / prove_state_machine / prove_blake (oracle/components.h,
+oracle/air_blake_full.h)."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -30,4 +32,19 @@ def test_state_machine_proof_matches_oracle(cuda, oracle, log_n, initial, cfg):
     assert sums == want_sums
     assert got == want
     ok, why = oracle.verify_state_machine(log_n, sums, got)
+    assert ok, why
+
+
+@pytest.mark.parametrize("log_n,cfg", [(4, (5, 1, 0, 3)), (5, (6, 2, 1, 4))])
+def test_blake_proof_matches_oracle(cuda, oracle, log_n, cfg):
+    """The full Blake example (scheduler, two round components, five XOR tables, preprocessed XOR
+    tables) from its framework definitions: the claimed sums and the proof bytes equal the
+    oracle's restatement of prove_blake, and the oracle's verify_blake accepts the proof."""
+    from stwo_gb300 import framework_prover
+
+    got, sums = framework_prover.prove_blake(log_n, cfg)
+    want, want_sums = oracle.prove_blake(log_n, cfg)
+    assert sums == want_sums
+    assert got == want
+    ok, why = oracle.verify_blake(log_n, sums, got)
     assert ok, why

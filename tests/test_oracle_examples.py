@@ -21,3 +21,24 @@ def test_state_machine_prove_verify(oracle, log_n, initial):
     bad[-40] ^= 1
     assert not oracle.verify_state_machine(log_n, sums, bytes(bad))[0]
     assert not oracle.verify_state_machine(log_n, (sums[1], sums[0]), proof)[0]
+
+
+def test_blake_prove_verify(oracle):
+    """The full Blake example (scheduler, two round components, five XOR tables): the eight claimed
+    sums add to zero, so every round and XOR lookup is balanced by the scheduler and the tables;
+    the proof verifies; a flipped byte or a changed sum is rejected."""
+    P = (1 << 31) - 1
+    proof, sums = oracle.prove_blake(4)
+    total = [sum(q[k] for q in sums) % P for k in range(4)]
+    assert total == [0, 0, 0, 0]
+    assert all(q != (0, 0, 0, 0) for q in sums)
+    assert oracle.verify_blake(4, sums, proof) == (True, "")
+    bad = bytearray(proof)
+    bad[len(bad) // 3] ^= 1
+    assert not oracle.verify_blake(4, sums, bytes(bad))[0]
+    moved = [list(q) for q in sums]
+    moved[0][0] = (moved[0][0] + 1) % P
+    moved[3][0] = (moved[3][0] - 1) % P  # still sums to zero, but not the traces' sums
+    ok, why = oracle.verify_blake(4, [tuple(q) for q in moved], proof)
+    assert not ok
+    assert oracle.verify_blake(4, [sums[1], sums[0]] + sums[2:], proof)[0] is False
