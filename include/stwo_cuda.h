@@ -318,6 +318,15 @@ stwo_status stwo_prove_blake_round(uint32_t log_n_rows, const uint32_t* d_inputs
                                    uint8_t* h_proof, size_t capacity, size_t* h_len, stwo_qm31* h_claimed_sum,
                                    void* stream);
 
+/* The trace of the full Blake example (prove_blake, crates/prover/src/examples/blake/air.rs:363-400;
+ * generators scheduler/gen.rs:45-118, round/gen.rs:206-235, xor_table/mod.rs:60-90) for 2^log_n
+ * BLAKE2s instances, generated in HBM. d_trace receives, column after column in commit order, the
+ * scheduler's 384 columns of 2^log_n words, the two round components' 384 columns of 2^(log_n+3)
+ * and 2^(log_n+1) words, then the XOR tables' multiplicity columns (12/4: 256 of 2^16 words,
+ * 9/2: 16 of 2^14, 8/2: 16 of 2^12, 7/2: 16 of 2^10, 4/0: 1 of 2^8): 4224 * 2^log_n + 17,121,536
+ * words. d_scratch holds the round inputs, 320 * 2^log_n words. log_n in [4, 20]. */
+stwo_status stwo_gen_blake_example_trace(uint32_t log_n, uint32_t* d_trace, uint32_t* d_scratch, void* stream);
+
 /* ------------------------------------------------------------------ batched and served proving */
 /* No counterpart in the reference, which proves one statement per call (prover/mod.rs:27-79).
  * A server owns a pool of host workers, each with its own CUDA stream, that run whole-proof jobs

@@ -121,6 +121,7 @@ SIGNATURES = {
                                         VP]),
     "stwo_prove_blake_round": (C.c_int32, [U32, VP, PcsConfig, VP, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(QM31),
                                         VP]),
+    "stwo_gen_blake_example_trace": (C.c_int32, [U32, VP, VP, VP]),
     "stwo_server_create": (C.c_int32, [U32, C.c_size_t, C.c_int, PVP]),
     "stwo_server_submit": (C.c_int32, [VP, C.POINTER(ProofJob), C.POINTER(C.c_uint64)]),
     "stwo_server_wait": (C.c_int32, [VP, C.c_uint64, C.POINTER(ProofResult)]),

@@ -850,9 +850,166 @@ GpuAir* new_blake_round_air(uint32_t log_n, const hq* z_alpha, const hq& claimed
   return new BlakeRoundGpuAir(log_n, el, claimed_sum);
 }
 
+// ------------------------------------------------------------------ the full Blake example's trace
+// prove_blake's trace (blake/air.rs:331-400) for 2^L instances, one thread per row:
+//   k_bf_scheduler  the scheduler's 384 columns (messages, then the 11 states, as 16-bit limbs;
+//                   scheduler/gen.rs:45-118) and the round inputs it hands on: input
+//                   p = 10 vec_row + r holds, lane by lane, the state before round r of instance
+//                   16 vec_row + lane and its SIGMA[r]-permuted messages, i.e. row 16 p + lane;
+//   k_bf_rounds     one round component's 384 columns from those inputs (br_round, as k_br_trace)
+//                   and every XOR lookup counted into the tables' multiplicity columns, column
+//                   (ah << e) + bh, row (al << limb) + bl (xor_table/mod.rs:60-90).
+// Instance 16 vec_row + lane has every state word vec_row + 2 lane and every message word one
+// more (air.rs:331-338).
+__constant__ uint8_t c_bf_sigma[10][16] = {
+    {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15},
+    {14, 10, 4, 8, 9, 15, 13, 6, 1, 12, 0, 2, 11, 7, 5, 3},
+    {11, 8, 12, 0, 5, 2, 15, 13, 10, 14, 3, 6, 7, 1, 9, 4},
+    {7, 9, 3, 1, 13, 12, 11, 14, 2, 6, 5, 10, 4, 0, 15, 8},
+    {9, 0, 5, 7, 2, 4, 10, 15, 14, 1, 11, 12, 6, 8, 3, 13},
+    {2, 12, 6, 10, 0, 11, 8, 3, 4, 13, 7, 5, 15, 14, 1, 9},
+    {12, 5, 1, 15, 14, 13, 4, 10, 0, 7, 6, 3, 9, 2, 8, 11},
+    {13, 11, 7, 14, 12, 1, 3, 9, 5, 0, 15, 4, 8, 6, 2, 10},
+    {6, 15, 14, 9, 11, 3, 0, 8, 12, 2, 13, 7, 1, 4, 10, 5},
+    {10, 2, 8, 4, 7, 6, 1, 5, 15, 11, 9, 14, 3, 12, 13, 0},
+};
+constexpr uint32_t BF_ROUNDS = 10;
+constexpr uint32_t BF_SCHED_COLS = 384;
+
+__device__ __forceinline__ uint32_t bf_rotr(uint32_t x, uint32_t r) { return (x >> r) | (x << (32 - r)); }
+
+__global__ void __launch_bounds__(128) k_bf_scheduler(uint32_t log_n, uint32_t* __restrict__ trace,
+                                                      uint32_t* __restrict__ round_inputs) {
+  pdl_enter();
+  const size_t n = (size_t)1 << log_n;
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t vec_row = s >> 4, lane = s & 15;
+  uint32_t v[BR_ST], m[BR_ST];
+#pragma unroll
+  for (int k = 0; k < BR_ST; k++) {
+    v[k] = vec_row + 2 * lane;
+    m[k] = v[k] + 1;
+  }
+  uint32_t col = 0;
+  auto put = [&](const uint32_t* w) {
+#pragma unroll
+    for (int k = 0; k < BR_ST; k++) {
+      trace[(size_t)col++ * n + s] = w[k] & 0xffffu;
+      trace[(size_t)col++ * n + s] = w[k] >> 16;
+    }
+  };
+  put(m);
+  put(v);
+#pragma unroll 1
+  for (uint32_t r = 0; r < BF_ROUNDS; r++) {
+    uint32_t* in = round_inputs + ((((size_t)vec_row * BF_ROUNDS + r) << 4) + lane) * 32;
+#pragma unroll
+    for (int k = 0; k < BR_ST; k++) {
+      in[k] = v[k];
+      in[BR_ST + k] = m[c_bf_sigma[r][k]];
+    }
+    auto g = [&](int a, int b, int c, int d, uint32_t x, uint32_t y) {
+      v[a] = v[a] + v[b] + x;
+      v[d] = bf_rotr(v[d] ^ v[a], 16);
+      v[c] = v[c] + v[d];
+      v[b] = bf_rotr(v[b] ^ v[c], 12);
+      v[a] = v[a] + v[b] + y;
+      v[d] = bf_rotr(v[d] ^ v[a], 8);
+      v[c] = v[c] + v[d];
+      v[b] = bf_rotr(v[b] ^ v[c], 7);
+    };
+    const uint8_t* sg = c_bf_sigma[r];
+    g(0, 4, 8, 12, m[sg[0]], m[sg[1]]);
+    g(1, 5, 9, 13, m[sg[2]], m[sg[3]]);
+    g(2, 6, 10, 14, m[sg[4]], m[sg[5]]);
+    g(3, 7, 11, 15, m[sg[6]], m[sg[7]]);
+    g(0, 5, 10, 15, m[sg[8]], m[sg[9]]);
+    g(1, 6, 11, 12, m[sg[10]], m[sg[11]]);
+    g(2, 7, 8, 13, m[sg[12]], m[sg[13]]);
+    g(3, 4, 9, 14, m[sg[14]], m[sg[15]]);
+    put(v);
+  }
+}
+
+// The XOR tables' multiplicity columns, one block per table in the order 12/4, 9/2, 8/2, 7/2,
+// 4/0; table t starts at word offset bf_xor_offset(t).
+struct BfXorTables {
+  uint32_t* base;
+  __device__ __forceinline__ void lookup(uint32_t w, uint32_t a, uint32_t b, uint32_t) const {
+    uint32_t e, off;
+    switch (w) {
+      case 12: e = 4, off = 0; break;
+      case 9: e = 2, off = 1u << 24; break;
+      case 8: e = 2, off = (1u << 24) + (1u << 18); break;
+      case 7: e = 2, off = (1u << 24) + (1u << 18) + (1u << 16); break;
+      default: e = 0, off = (1u << 24) + (1u << 18) + (1u << 16) + (1u << 14); break;
+    }
+    const uint32_t lb = w - e, mask = (1u << lb) - 1;
+    const uint32_t column = ((a >> lb) << e) + (b >> lb);
+    const uint32_t row = ((a & mask) << lb) + (b & mask);
+    atomicAdd(base + off + ((size_t)column << (2 * lb)) + row, 1u);
+  }
+};
+constexpr size_t BF_XOR_WORDS = (1u << 24) + (1u << 18) + (1u << 16) + (1u << 14) + (1u << 8);
+
+struct BfRoundWriter {
+  uint32_t* trace;
+  size_t n;
+  uint32_t r;
+  BfXorTables xt;
+  uint32_t col = 0;
+  __device__ void felt(uint32_t x) { trace[(size_t)col++ * n + r] = x; }
+  __device__ void lookup(uint32_t w, uint32_t a, uint32_t b, uint32_t c) { xt.lookup(w, a, b, c); }
+};
+
+__global__ void __launch_bounds__(128) k_bf_rounds(uint32_t n_rows, const uint32_t* __restrict__ inputs,
+                                                   uint32_t* __restrict__ trace, uint32_t* __restrict__ xor_tables) {
+  pdl_enter();
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  uint32_t v[BR_ST];
+  BfRoundWriter w{trace, n_rows, r, BfXorTables{xor_tables}};
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    v[i] = __ldg(inputs + (size_t)r * 32 + i);
+    w.felt(v[i] & 0xffffu);
+    w.felt(v[i] >> 16);
+  }
+#pragma unroll
+  for (int i = 0; i < BR_ST; i++) {
+    const uint32_t m = __ldg(inputs + (size_t)r * 32 + BR_ST + i);
+    w.felt(m & 0xffffu);
+    w.felt(m >> 16);
+  }
+  br_round(v, [&](int i) { return __ldg(inputs + (size_t)r * 32 + BR_ST + i); }, w);
+}
+
 }  // namespace stwo
 
 using namespace stwo;
+
+extern "C" stwo_status stwo_gen_blake_example_trace(uint32_t log_n, uint32_t* d_trace, uint32_t* d_scratch,
+                                                    void* stream) {
+  STWO_REQUIRE(log_n >= 4 && log_n <= 20, "log_n out of [4, 20]");
+  STWO_REQUIRE(d_trace && d_scratch, "null buffer");
+  cudaStream_t s = as_stream(stream);
+  const size_t n = (size_t)1 << log_n;
+  uint32_t* sched = d_trace;
+  uint32_t* round0 = sched + BF_SCHED_COLS * n;
+  uint32_t* round1 = round0 + (size_t)BR_COLS * (8 * n);
+  uint32_t* xors = round1 + (size_t)BR_COLS * (2 * n);
+  if (cudaMemsetAsync(xors, 0, BF_XOR_WORDS * 4, s) != cudaSuccess) return STWO_ERR_CUDA;
+  launch_pdl(k_bf_scheduler, dim3((uint32_t)((n + 127) / 128)), dim3(128), 0, s, log_n, sched, d_scratch);
+  launch_pdl(k_bf_rounds, dim3((uint32_t)((8 * n + 127) / 128)), dim3(128), 0, s, (uint32_t)(8 * n),
+             (const uint32_t*)d_scratch, round0, xors);
+  launch_pdl(k_bf_rounds, dim3((uint32_t)((2 * n + 127) / 128)), dim3(128), 0, s, (uint32_t)(2 * n),
+             (const uint32_t*)(d_scratch + 8 * n * 32), round1, xors);
+  note_launch();
+  note_launch();
+  note_launch();
+  return cudaGetLastError() == cudaSuccess ? STWO_OK : STWO_ERR_CUDA;
+}
 
 extern "C" stwo_status stwo_prove_blake_round(uint32_t log_n_rows, const uint32_t* d_inputs, stwo_pcs_config cfg,
                                               uint8_t* h_proof, size_t capacity, size_t* h_len,

@@ -14,8 +14,9 @@ and the two examples without a hand-written device prover:
   prove_blake                    crates/prover/src/examples/blake/air.rs:308-460
 Every O(trace) step after trace generation runs on the device: the generated constraint kernels,
 the generated LogUp interaction kernels, and the backend operations of host_prover (FFT, Merkle,
-quotients, FRI, grind). The examples' circuits and traces are built on the host, as the
-reference's examples build them before prove(): numpy, vectorised over rows.
+quotients, FRI, grind). The Plonk circuit and the state-machine traces are built on the host, as
+the reference's examples build them before prove(); the full Blake example's trace is generated
+on the device (stwo_gen_blake_example_trace).
 """
 from __future__ import annotations
 
@@ -294,169 +295,11 @@ def prove_state_machine(log_n: int, initial: Sequence[int], cfg=(5, 1, 0, 3)) ->
 
 
 # ------------------------------------------------------------------ the full Blake example
-
-
-def _rotr(x: np.ndarray, r: int) -> np.ndarray:
-    return (x >> np.uint32(r)) | (x << np.uint32(32 - r))
-
-
-def _blake_round_words(v: List[np.ndarray], m: List[np.ndarray], r: int) -> None:
-    """One BLAKE2s round on 16 word arrays, messages by the round's SIGMA (simd/blake2s.rs:180-270)."""
-    from .airs import BLAKE2S_SIGMA
-
-    s = BLAKE2S_SIGMA[r]
-
-    def g(a, b, c, d, x, y):
-        v[a] = v[a] + v[b] + x
-        v[d] = _rotr(v[d] ^ v[a], 16)
-        v[c] = v[c] + v[d]
-        v[b] = _rotr(v[b] ^ v[c], 12)
-        v[a] = v[a] + v[b] + y
-        v[d] = _rotr(v[d] ^ v[a], 8)
-        v[c] = v[c] + v[d]
-        v[b] = _rotr(v[b] ^ v[c], 7)
-
-    for k, (a, b, c, d) in enumerate(((0, 4, 8, 12), (1, 5, 9, 13), (2, 6, 10, 14), (3, 7, 11, 15),
-                                      (0, 5, 10, 15), (1, 6, 11, 12), (2, 7, 8, 13), (3, 4, 9, 14))):
-        g(a, b, c, d, m[s[2 * k]], m[s[2 * k + 1]])
-
-
-class _RoundTrace:
-    """The round component's trace generator (round/gen.rs:75-235) over all rows at once: the 384
-    columns in the order the constraints read them, and every XOR lookup's (width, a, b)."""
-
-    def __init__(self):
-        self.cols: List[np.ndarray] = []
-        self.xors: List[Tuple[int, np.ndarray, np.ndarray]] = []
-
-    def felt(self, x):
-        self.cols.append(x.astype(np.uint32))
-
-    def u32(self, x):
-        self.felt(x & np.uint32(0xFFFF))
-        self.felt(x >> np.uint32(16))
-
-    def add(self, *xs):
-        s = xs[0]
-        for x in xs[1:]:
-            s = s + x
-        self.u32(s)
-        return s
-
-    def split(self, a, r):
-        self.felt(a >> np.uint32(r))
-        return a & np.uint32((1 << r) - 1), a >> np.uint32(r)
-
-    def xor1(self, w, a, b):
-        self.felt(a ^ b)
-        self.xors.append((w, a, b))
-
-    def xor_rotr(self, a, b, r):
-        all_, alh = self.split(a & np.uint32(0xFFFF), r)
-        ahl, ahh = self.split(a >> np.uint32(16), r)
-        bll, blh = self.split(b & np.uint32(0xFFFF), r)
-        bhl, bhh = self.split(b >> np.uint32(16), r)
-        self.xor1(r, all_, bll)
-        self.xor1(r, ahl, bhl)
-        self.xor1(16 - r, alh, blh)
-        self.xor1(16 - r, ahh, bhh)
-        return _rotr(a ^ b, r)
-
-    def g(self, v, ia, ib, ic, id_, m0, m1):
-        a, b, c, d = v[ia], v[ib], v[ic], v[id_]
-        a = self.add(a, b, m0)
-        d = self.xor_rotr16(a, d)
-        c = self.add(c, d)
-        b = self.xor_rotr(b, c, 12)
-        a = self.add(a, b, m1)
-        d = self.xor_rotr(a, d, 8)
-        c = self.add(c, d)
-        b = self.xor_rotr(b, c, 7)
-        v[ia], v[ib], v[ic], v[id_] = a, b, c, d
-
-    def xor_rotr16(self, a, b):
-        all_, alh = self.split(a & np.uint32(0xFFFF), 8)
-        ahl, ahh = self.split(a >> np.uint32(16), 8)
-        bll, blh = self.split(b & np.uint32(0xFFFF), 8)
-        bhl, bhh = self.split(b >> np.uint32(16), 8)
-        self.xor1(8, all_, bll)
-        self.xor1(8, ahl, bhl)
-        self.xor1(8, alh, blh)
-        self.xor1(8, ahh, bhh)
-        return _rotr(a ^ b, 16)
-
-    def generate(self, vin: np.ndarray, m: np.ndarray) -> None:
-        """vin, m: (16, rows) word arrays."""
-        v = [vin[i].copy() for i in range(16)]
-        mm = [m[i] for i in range(16)]
-        for i in range(16):
-            self.u32(v[i])
-        for i in range(16):
-            self.u32(mm[i])
-        for k, idx in enumerate(((0, 4, 8, 12), (1, 5, 9, 13), (2, 6, 10, 14), (3, 7, 11, 15),
-                                 (0, 5, 10, 15), (1, 6, 11, 12), (2, 7, 8, 13), (3, 4, 9, 14))):
-            self.g(v, *idx, mm[2 * k], mm[2 * k + 1])
-
-
-def blake_traces(log_n: int) -> Tuple[List[np.ndarray], List[np.ndarray]]:
-    """The preprocessed and trace columns of prove_blake (blake/air.rs:331-400) for 2^log_n
-    instances, each as the evaluation in bit-reversed order that the reference's generators write:
-      preprocessed  IsFirst(L), IsFirst(L+3), IsFirst(L+1), then per XOR table (al, bl, al ^ bl)
-                    and IsFirst of its size (preprocessed_columns.rs:58-82);
-      scheduler     messages, then the 11 states, as 16-bit limbs (scheduler/gen.rs:45-118);
-      rounds        ROUND_LOG_SPLIT = [3, 1]: the first 2^(L+3) round inputs, then 2^(L+1);
-                    round input p = 10 vec_row + r holds lane by lane the state before round r of
-                    instance 16 vec_row + lane and its SIGMA[r]-permuted messages;
-      XOR tables    multiplicities of every round XOR lookup, column (ah << e) + bh, row
-                    (al << limb) + bl (xor_table/mod.rs:60-90).
-    Instance 16 vec_row + lane has every state word vec_row + 2 lane and every message word one
-    more (air.rs:331-338)."""
-    from .airs import BLAKE2S_SIGMA, XOR_TABLES
-
-    if log_n < 4:
-        raise ValueError("prove_blake needs log_n >= 4")
-    n = 1 << log_n
-    s = np.arange(n, dtype=np.uint32)
-    vec_row, lane = s >> np.uint32(4), s & np.uint32(15)
-    v = [(vec_row + np.uint32(2) * lane).astype(np.uint32) for _ in range(16)]
-    m = [x + np.uint32(1) for x in v]
-    sched: List[np.ndarray] = []
-
-    def put(words):
-        for w in words:
-            sched.append(w & np.uint32(0xFFFF))
-            sched.append(w >> np.uint32(16))
-
-    put(m)
-    put(v)
-    rin_v = np.zeros((16, 10 * n), np.uint32)
-    rin_m = np.zeros((16, 10 * n), np.uint32)
-    for r in range(10):
-        rows = ((vec_row.astype(np.int64) * 10 + r) << 4) + lane
-        rin_v[:, rows] = np.stack(v)
-        rin_m[:, rows] = np.stack([m[k] for k in BLAKE2S_SIGMA[r]])
-        _blake_round_words(v, m, r)
-        put(v)
-    rounds, first = [], 0
-    xors = []
-    for k in (3, 1):
-        cnt = 1 << (log_n + k)
-        gen = _RoundTrace()
-        gen.generate(rin_v[:, first:first + cnt], rin_m[:, first:first + cnt])
-        rounds.append(gen.cols)
-        xors += gen.xors
-        first += cnt
-    widths = {w: i for i, (w, _) in enumerate(XOR_TABLES)}
-    mults = []
-    for w, e in XOR_TABLES:
-        lb = w - e
-        size = 1 << (2 * lb)
-        idx = [((a >> np.uint32(lb)).astype(np.int64) << e | (b >> np.uint32(lb)).astype(np.int64)) * size
-               + (((a & np.uint32((1 << lb) - 1)).astype(np.int64) << lb) | (b & np.uint32((1 << lb) - 1)))
-               for ww, a, b in xors if ww == w]
-        counts = np.bincount(np.concatenate(idx), minlength=size << (2 * e)) if idx else np.zeros(size << (2 * e))
-        mults += [counts[c * size:(c + 1) * size].astype(np.uint32) for c in range(1 << (2 * e))]
-    assert len(widths) == 5
+def blake_preprocessed(log_n: int) -> List[np.ndarray]:
+    """The preprocessed columns of prove_blake (air.rs:343-361): IsFirst(L), IsFirst(L+3),
+    IsFirst(L+1), then per XOR table (al, bl, al ^ bl) in natural order and IsFirst of its size
+    (blake/preprocessed_columns.rs:58-82)."""
+    from .airs import XOR_TABLES
 
     def is_first(log):
         c = np.zeros(1 << log, np.uint32)
@@ -469,26 +312,49 @@ def blake_traces(log_n: int) -> Tuple[List[np.ndarray], List[np.ndarray]]:
         i = np.arange(1 << (2 * lb), dtype=np.uint32)
         al, bl = i >> np.uint32(lb), i & np.uint32((1 << lb) - 1)
         pre += [al, bl, al ^ bl, is_first(2 * lb)]
-    return pre, sched + rounds[0] + rounds[1] + mults
+    return pre
+
+
+def blake_device_trace(log_n: int) -> List[Buf]:
+    """prove_blake's trace columns generated in HBM (stwo_gen_blake_example_trace), in commit
+    order, as views of one block: the scheduler, the two round components, the XOR tables'
+    multiplicity columns."""
+    from .airs import XOR_TABLES
+
+    n = 1 << log_n
+    sizes = [n] * 384 + [8 * n] * 384 + [2 * n] * 384
+    for w, e in XOR_TABLES:
+        sizes += [1 << (2 * (w - e))] * (1 << (2 * e))
+    block = Buf(sum(sizes))
+    scratch = Buf(320 * n)
+    call("stwo_gen_blake_example_trace", log_n, block.ptr, scratch.ptr, None)
+    out, at = [], 0
+    for sz in sizes:
+        out.append(Buf.view(block, at, sz))
+        at += sz
+    return out
 
 
 def prove_blake(log_n: int, cfg=(5, 1, 0, 3)) -> Tuple[bytes, List[Q]]:
     """prove_blake (blake/air.rs:308-460) on the device for 2^log_n BLAKE2s instances: the
     scheduler, two round components (2^(L+3) and 2^(L+1) rows) and the XOR tables 12, 9, 8, 7, 4
     in one proof. Returns the stark proof's canonical bytes and the eight claimed sums (scheduler,
-    round 0, round 1, XOR 12, 9, 8, 7, 4), which add to zero. The traces come from blake_traces
-    (host), everything after them runs in generated and library kernels."""
+    round 0, round 1, XOR 12, 9, 8, 7, 4), which add to zero. The trace is generated in HBM
+    (blake_device_trace) and everything after it runs in generated and library kernels; the
+    preprocessed XOR tables are host constants."""
     from .airs import (BlakeRoundEval, BlakeSchedulerEval, XOR_TABLES, XorTableEval, is_first_id,
                        xor_table_id)
 
-    pre, trace = blake_traces(log_n)
+    pre = blake_preprocessed(log_n)
+    trace = blake_device_trace(log_n)
     n_sched, n_round = 384, 384
     log_max_rows = max(log_n + 3, 16)
     pcs = CommitmentSchemeProver(cfg, log_max_rows + 1 + cfg[1])
     ch = Blake2sChannel()
     _commit_evals(pcs, _upload(pre), ch)
     ch.mix_u64(log_n)
-    _commit_evals(pcs, _upload(trace), ch)
+    _commit_evals(pcs, trace, ch)
+    trace = blake_device_trace(log_n)  # the committed columns were interpolated in place
     # AllElements::draw (air.rs:119-133): Blake, Round, then the XOR relations 12, 9, 8, 7, 4.
     el = {"blake": tuple(ch.draw_felts(2)), "round": tuple(ch.draw_felts(2))}
     for w, _ in XOR_TABLES:
@@ -512,8 +378,8 @@ def prove_blake(log_n: int, cfg=(5, 1, 0, 3)) -> Tuple[bytes, List[Q]]:
     for k, air in enumerate(evals()):
         gc = GeneratedComponent(air)
         a, b = spans[k]
-        pre_cols = [pre[3 + 4 * (k - 3) + j] for j in range(3)] if k >= 3 else []
-        cols = _upload(pre_cols + trace[a:b])
+        pre_cols = _upload([pre[3 + 4 * (k - 3) + j] for j in range(3)]) if k >= 3 else []
+        cols = pre_cols + trace[a:b]
         block = Buf(gc.n_interaction_columns() << air.log_size())
         sums.append(gc.interaction([c.ptr for c in cols], block.ptr))
         inter += _split(block, gc.n_interaction_columns(), 1 << air.log_size())

@@ -48,3 +48,33 @@ def test_blake_proof_matches_oracle(cuda, oracle, log_n, cfg):
     assert got == want
     ok, why = oracle.verify_blake(log_n, sums, got)
     assert ok, why
+
+
+@pytest.mark.parametrize("log_n", [4, 6])
+def test_blake_device_trace_matches_oracle(cuda, oracle, log_n):
+    """stwo_gen_blake_example_trace (scheduler, round components, XOR multiplicities counted with
+    atomics) equals the oracle's trace of prove_blake column for column."""
+    import numpy as np
+
+    from stwo_gb300 import framework_prover
+
+    cols = framework_prover.blake_device_trace(log_n)
+    got = np.concatenate([_download(c) for c in cols])
+    pre = framework_prover.blake_preprocessed(log_n)
+    want, k = oracle.blake_traces(log_n)
+    assert k == len(pre) + len(cols)
+    n_pre = sum(len(p) for p in pre)
+    assert np.array_equal(np.concatenate(pre), want[:n_pre])
+    assert np.array_equal(got, want[n_pre:])
+
+
+def _download(buf):
+    import ctypes as C
+
+    import numpy as np
+
+    from stwo_gb300.host_prover import call
+
+    out = np.zeros(buf.n, np.uint32)
+    call("stwo_buf_download", out.ctypes.data_as(C.c_void_p), buf.ptr, buf.n * 4, None)
+    return out
