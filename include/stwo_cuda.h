@@ -111,6 +111,10 @@ stwo_status stwo_buf_zero(void* d_dst, size_t bytes, void* stream);
  * crates/prover/src/core/vcs/prover.rs:80-149). */
 stwo_status stwo_read_words(const uint32_t* d_col, const uint64_t* h_idx, size_t n, uint32_t* h_out,
                             void* stream);
+/* Column::at for the same indices of several columns, in one transfer: h_out[c * n + i] =
+ * h_cols[c][h_idx[i]] (the values a Merkle layer's decommitment reads, vcs/prover.rs:80-149). */
+stwo_status stwo_read_words_cols(const uint32_t* const* h_cols, size_t n_cols, const uint64_t* h_idx, size_t n,
+                                 uint32_t* h_out, void* stream);
 
 /* ------------------------------------------------------------------ twiddles */
 /* PolyOps::precompute_twiddles (crates/prover/src/core/poly/circle/ops.rs:68;

@@ -88,6 +88,8 @@ SIGNATURES = {
     "stwo_buf_download": (C.c_int32, [VP, VP, C.c_size_t, VP]),
     "stwo_buf_zero": (C.c_int32, [VP, C.c_size_t, VP]),
     "stwo_read_words": (C.c_int32, [VP, C.POINTER(C.c_uint64), C.c_size_t, C.POINTER(C.c_uint32), VP]),
+    "stwo_read_words_cols": (C.c_int32, [VP, C.c_size_t, C.POINTER(C.c_uint64), C.c_size_t, C.POINTER(C.c_uint32),
+                                         VP]),
     "stwo_twiddles_precompute": (C.c_int32, [Coset, PVP, VP]),
     "stwo_twiddles_free": (C.c_int32, [VP]),
     "stwo_twiddles_info": (C.c_int32, [VP, C.POINTER(Coset), PVP, PVP, C.POINTER(C.c_size_t)]),

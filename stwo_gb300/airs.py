@@ -5,7 +5,8 @@ hand-written.
 Each class has the FrameworkEval surface (crates/prover/src/constraint_framework/component.rs:
 33-47): `log_size()`, `max_constraint_log_degree_bound()` and `evaluate(eval)`, plus `params()`,
 the values of the formal parameters its constraints name (relation elements, claimed sum, column
-size). `evaluate` restates the example's own `evaluate` step for step:
+size), and `shape_key()`, which names what the recorded expressions depend on (not the log size,
+the elements or the claimed sum), so that components of one shape share one generated kernel. `evaluate` restates the example's own `evaluate` step for step:
   WideFibonacciEval   crates/prover/src/examples/wide_fibonacci/mod.rs:25-44
   PoseidonEval        crates/prover/src/examples/poseidon/mod.rs:53-197 (constants all 1234)
   PlonkEval           crates/prover/src/examples/plonk/mod.rs:40-95
@@ -37,6 +38,9 @@ def _logup_params(claimed_sum: Q, log_size: int) -> Dict[str, object]:
 class WideFibonacciEval:
     def __init__(self, log_n_rows: int, n_cols: int):
         self.log_n_rows, self.n_cols = log_n_rows, n_cols
+
+    def shape_key(self) -> tuple:
+        return ("wide_fib", self.n_cols)
 
     def log_size(self) -> int:
         return self.log_n_rows
@@ -109,6 +113,9 @@ class PoseidonEval:
     def __init__(self, log_n_rows: int, elements: Optional[tuple] = None, claimed_sum: Q = (0, 0, 0, 0)):
         self.log_n_rows, self.elements, self.claimed_sum = log_n_rows, elements, claimed_sum
 
+    def shape_key(self) -> tuple:
+        return ("poseidon",)
+
     def log_size(self) -> int:
         return self.log_n_rows
 
@@ -160,6 +167,9 @@ class PlonkEval:
     def __init__(self, log_n_rows: int, elements: Optional[tuple] = None, claimed_sum: Q = (0, 0, 0, 0)):
         self.log_n_rows, self.elements, self.claimed_sum = log_n_rows, elements, claimed_sum
 
+    def shape_key(self) -> tuple:
+        return ("plonk",)
+
     def log_size(self) -> int:
         return self.log_n_rows
 
@@ -194,6 +204,9 @@ class StateTransitionEval:
                  claimed_sum: Q = (0, 0, 0, 0)):
         self.coordinate, self.log_n_rows = coordinate, log_n_rows
         self.elements, self.claimed_sum = elements, claimed_sum
+
+    def shape_key(self) -> tuple:
+        return ("state_transition", self.coordinate)
 
     def log_size(self) -> int:
         return self.log_n_rows
@@ -265,6 +278,9 @@ class BlakeSchedulerEval:
     def __init__(self, log_n_rows: int, elements: Optional[dict] = None, claimed_sum: Q = (0, 0, 0, 0)):
         self.log_n_rows, self.elements, self.claimed_sum = log_n_rows, elements, claimed_sum
 
+    def shape_key(self) -> tuple:
+        return ("blake_scheduler",)
+
     def log_size(self) -> int:
         return self.log_n_rows
 
@@ -299,6 +315,9 @@ class BlakeRoundEval:
 
     def __init__(self, log_n_rows: int, elements: Optional[dict] = None, claimed_sum: Q = (0, 0, 0, 0)):
         self.log_n_rows, self.elements, self.claimed_sum = log_n_rows, elements, claimed_sum
+
+    def shape_key(self) -> tuple:
+        return ("blake_round",)
 
     def log_size(self) -> int:
         return self.log_n_rows
@@ -401,6 +420,9 @@ class XorTableEval:
 
     def limb_bits(self) -> int:
         return self.elem_bits - self.expand_bits
+
+    def shape_key(self) -> tuple:
+        return ("xor_table", self.elem_bits, self.expand_bits)
 
     def log_size(self) -> int:
         return 2 * self.limb_bits()

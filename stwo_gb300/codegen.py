@@ -43,10 +43,12 @@ SMEM_BUDGET = 40 * 1024  # shared memory for the column table and the powers, by
 # compiled for compile time: NVRTC's default pipeline is superlinear in the size of one basic block
 # (a 2,700-statement Blake2s round body took minutes), so such a body is cut into blocks of
 # FLAT_BLOCK statements by branches the compiler cannot remove, and the source asks for
-# --Ofast-compile=max (FAST_COMPILE_MARK, read by the library's NVRTC call).
+# --Ofast-compile=mid (FAST_COMPILE_MARK, read by the library's NVRTC call).
 FLAT_SPLIT_MIN = 1000
 FLAT_BLOCK = 40
 FAST_COMPILE_MARK = "// stwo-codegen: fast-compile"
+# The library's NVRTC options (codegen.cu), part of the cubin cache key.
+NVRTC_FLAGS = b"--gpu-architecture=sm_103a -std=c++17 -lineinfo; marked: --Ofast-compile=mid"
 
 
 def _split_flat(body: List[str]) -> Tuple[List[str], bool]:
@@ -541,7 +543,7 @@ def _compiled(source: str, sizes: Tuple[int, int, int], load: bool = True) -> in
     disk, or NVRTC."""
     from . import _lib
 
-    key = hashlib.sha256(source.encode() + repr(sizes).encode() + _runtime_headers()).hexdigest()
+    key = hashlib.sha256(source.encode() + repr(sizes).encode() + _runtime_headers() + NVRTC_FLAGS).hexdigest()
     h = _CACHE.get(key)
     if h is None:
         out = C.c_void_p()
@@ -576,20 +578,31 @@ def _store_cubin(handle: int, path: str) -> None:
     os.replace(tmp, path)
 
 
+# Recorded components by the AIR's shape_key(): the expressions, the kernel source and handle, and
+# the interaction kernel, shared by every component of that shape (the recording does not depend on
+# the log size, the relation elements or the claimed sum, which reach the kernels as parameters).
+_RECORDED: Dict[tuple, dict] = {}
+
+
 class GeneratedComponent:
     """A FrameworkEval-like object (`log_size`, `max_constraint_log_degree_bound`, `evaluate`,
     `params`) with its generated constraint kernel."""
 
     def __init__(self, air, load: bool = True):
-        from . import _lib
-
         self.air = air
-        self.ev = air.evaluate(ExprEvaluator())
-        self.source, self.param_names = generate(self.ev)
-        self.n_cols = sum(len(m) for m in self.ev.mask)
-        self.n_constraints = len(self.ev.constraints)
-        self.handle = _compiled(self.source, (self.n_cols, len(self.param_names), self.n_constraints), load)
-        self._frac = None
+        key = air.shape_key() if hasattr(air, "shape_key") else None
+        rec = _RECORDED.get((key, load)) if key is not None else None
+        if rec is None:
+            ev = air.evaluate(ExprEvaluator())
+            source, names = generate(ev)
+            n_cols = sum(len(m) for m in ev.mask)
+            rec = {"ev": ev, "source": source, "names": names, "n_cols": n_cols, "n_constraints": len(ev.constraints),
+                   "handle": _compiled(source, (n_cols, len(names), len(ev.constraints)), load), "frac": None}
+            if key is not None:
+                _RECORDED[(key, load)] = rec
+        self._rec = rec
+        self.ev, self.source, self.param_names = rec["ev"], rec["source"], rec["names"]
+        self.n_cols, self.n_constraints, self.handle = rec["n_cols"], rec["n_constraints"], rec["handle"]
 
     def log_size(self) -> int:
         return self.air.log_size()
@@ -638,11 +651,11 @@ class GeneratedComponent:
         from . import _lib
         from ._lib import QM31
 
-        if self._frac is None:
+        if self._rec["frac"] is None:
             src, names = generate_fractions(self.ev)
             n_in = len(self.ev.mask[0]) + len(self.ev.mask[1])
-            self._frac = (_compiled(src, (n_in, len(names), len(self.ev.logup_batches))), names, n_in)
-        h, names, n_in = self._frac
+            self._rec["frac"] = (_compiled(src, (n_in, len(names), len(self.ev.logup_batches))), names, n_in)
+        h, names, n_in = self._rec["frac"]
         vals = dict(params or {})
         vals.setdefault("claimed_sum", (0, 0, 0, 0))
         tab = (C.c_void_p * max(len(cols), 1))(*cols)

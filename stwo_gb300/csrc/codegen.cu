@@ -48,7 +48,7 @@ static int32_t nvrtc_compile(const char* src, std::string& cubin) {
   // A source that marks itself (a long straight-line body, cut into blocks by the generator) is
   // compiled with the fast-compile pipeline: the default one takes minutes on such a body.
   const bool fast = std::strstr(src, "// stwo-codegen: fast-compile\n") != nullptr;
-  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--Ofast-compile=max"};
+  const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "--Ofast-compile=mid"};
   r = nvrtcCompileProgram(prog, fast ? 4 : 3, opts);
   if (r != NVRTC_SUCCESS) {
     size_t n = 0;

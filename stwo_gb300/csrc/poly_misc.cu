@@ -551,6 +551,13 @@ __global__ void k_gather(const uint32_t* col, const unsigned long long* idx, siz
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i < n) out[i] = col[idx[i]];
 }
+// out[c * n + i] = cols[c][idx[i]] over total = n_cols * n words (decommitment reads of a
+// Merkle layer's columns at the same positions).
+__global__ void k_gather_cols(const uint32_t* const* cols, const unsigned long long* idx, size_t n, size_t total,
+                              uint32_t* out) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < total) out[t] = __ldg(cols[t / n] + idx[t % n]);
+}
 
 static uint32_t grid_cap(size_t n, uint32_t threads) {
   size_t b = (n + threads - 1) / threads;
@@ -619,6 +626,36 @@ stwo_status stwo_generate_secure_powers(stwo_qm31 felt, uint32_t n_powers, stwo_
   if (!e) e = cudaStreamSynchronize(s);
   if (e) {
     set_error("secure powers: %s", cudaGetErrorString(e));
+    return STWO_ERR_CUDA;
+  }
+  return STWO_OK;
+}
+
+stwo_status stwo_read_words_cols(const uint32_t* const* h_cols, size_t n_cols, const uint64_t* h_idx, size_t n,
+                                 uint32_t* h_out, void* stream) {
+  if (n == 0 || n_cols == 0) return STWO_OK;
+  STWO_REQUIRE(h_cols && h_idx && h_out, "null argument");
+  STWO_REQUIRE(n_cols * n <= ((size_t)1 << 31), "too many words");
+  cudaStream_t s = as_stream(stream);
+  const size_t tab = n_cols * 8, idx = n * 8, out = n_cols * n * 4;
+  char* buf = nullptr;
+  int32_t st = scratch_alloc((void**)&buf, tab + idx + out + 16, s);
+  if (st) return st;
+  const uint32_t** d_cols = reinterpret_cast<const uint32_t**>(buf);
+  unsigned long long* d_idx = reinterpret_cast<unsigned long long*>(buf + tab);
+  uint32_t* d_out = reinterpret_cast<uint32_t*>(buf + tab + idx);
+  cudaError_t e = cudaMemcpyAsync(d_cols, h_cols, tab, cudaMemcpyHostToDevice, s);
+  if (!e) e = cudaMemcpyAsync(d_idx, h_idx, idx, cudaMemcpyHostToDevice, s);
+  if (!e) {
+    const size_t total = n_cols * n;
+    k_gather_cols<<<(uint32_t)((total + 255) / 256), 256, 0, s>>>(d_cols, d_idx, n, total, d_out); note_launch();
+    e = cudaGetLastError();
+  }
+  if (!e) e = cudaMemcpyAsync(h_out, d_out, out, cudaMemcpyDeviceToHost, s);
+  scratch_free(buf, s);
+  if (!e) e = cudaStreamSynchronize(s);
+  if (e) {
+    set_error("read_words_cols: %s", cudaGetErrorString(e));
     return STWO_ERR_CUDA;
   }
   return STWO_OK;

@@ -29,8 +29,8 @@ from . import _lib
 from ._lib import QM31, QM31Point, call
 from .circle import canonic_half_coset, coset, subgroup_gen
 from .codegen import GeneratedComponent
-from .host_prover import (Blake2sChannel, Buf, CommitmentSchemeProver, SecureCol, _coset_vanishing, _finish_proof,
-                          _log2, _ptr4, _ptrs, index_to_point, q_add, q_inv, q_m31, q_mul, q_sub)
+from .host_prover import (Blake2sChannel, Buf, CommitmentSchemeProver, SecureCol, _block_views, _coset_vanishing,
+                          _finish_proof, _log2, _ptr4, _ptrs, index_to_point, q_add, q_inv, q_m31, q_mul, q_sub)
 
 P = (1 << 31) - 1
 Q = Tuple[int, int, int, int]
@@ -110,7 +110,7 @@ def prove(components: Sequence[PlacedComponent], pcs: CommitmentSchemeProver, ch
             polys = c.polys(pcs, t)
             if not polys:
                 continue
-            ext = [Buf(1 << eval_log) for _ in polys]  # the component's "Extension" (component.rs:305-322)
+            ext = _block_views([1 << eval_log] * len(polys))  # the component's "Extension" (component.rs:305-322)
             call("stwo_evaluate_columns", pcs.tw, canonic_half_coset(eval_log), _ptrs(polys), log, _ptrs(ext),
                  len(ext), None)
             cols += ext

@@ -253,6 +253,30 @@ class Buf:
         return list(out)
 
 
+def _read_cols(cols: Sequence[Buf], idx: Sequence[int]) -> List[List[int]]:
+    """Column::at of the same indices in every column, one transfer (stwo_read_words_cols)."""
+    if not cols or not idx:
+        return [[] for _ in cols]
+    n = len(idx)
+    out = (C.c_uint32 * (len(cols) * n))()
+    call("stwo_read_words_cols", _ptrs(cols), len(cols), (C.c_uint64 * n)(*idx), n, out, None)
+    flat = list(out)
+    return [flat[c * n:(c + 1) * n] for c in range(len(cols))]
+
+
+def _block_views(sizes: Sequence[int]) -> List[Buf]:
+    """Columns of the given word counts as views of one device block: one allocation for a tree's
+    or a component's columns instead of one per column."""
+    if not sizes:
+        return []
+    block = Buf(sum(sizes))
+    out, at = [], 0
+    for n in sizes:
+        out.append(Buf.view(block, at, n))
+        at += n
+    return out
+
+
 def _ptrs(bufs: Sequence[Buf]):
     return (C.c_void_p * max(1, len(bufs)))(*[b.ptr for b in bufs])
 
@@ -342,7 +366,7 @@ class MerkleTree:
             hnodes = [n for k, n in wants if k == "h"]
             hashes = dict(zip(hnodes, self._hashes(log + 1, hnodes))) if hnodes else {}
             vnodes = [n for k, n in wants if k != "h"]
-            vals = [c.at(vnodes) for c in lc]
+            vals = _read_cols(lc, vnodes)
             vi = 0
             for kind, node in wants:
                 if kind == "h":
@@ -378,7 +402,7 @@ class CommitmentSchemeProver:
 
     def commit_polys(self, polys: Sequence[Buf], ch: Blake2sChannel):
         """TreeBuilder::extend_polys + commit (pcs/prover.rs:208-227)."""
-        evals = [Buf(p.n << self.log_blowup) for p in polys]
+        evals = _block_views([p.n << self.log_blowup for p in polys])
         for log in sorted({_log2(p.n) for p in polys}):
             idx = [i for i, p in enumerate(polys) if _log2(p.n) == log]
             call("stwo_evaluate_columns", self.tw, canonic_half_coset(log + self.log_blowup),

@@ -146,6 +146,9 @@ extern "C" {
     pub fn stwo_logup_interaction_codegen(component: Codegen, log_size: u32, d_cols: *const *const u32,
                                           n_cols: u32, h_params: *const StwoQm31, n_params: u32, d_out: *mut u32,
                                           h_claimed_sum: *mut StwoQm31, stream: Stream) -> Status;
+    // The full Blake example's trace in HBM (examples/blake/air.rs:363-400).
+    pub fn stwo_gen_blake_example_trace(log_n: u32, d_trace: *mut u32, d_scratch: *mut u32, stream: Stream)
+                                        -> Status;
 }
 
 /// The reference panics on contract violations (`assert!`); the binding does the same with the

@@ -1,6 +1,7 @@
 """The column model through the C ABI: Column::zeros / uninitialized / to_cpu / at
 (crates/prover/src/core/backend/mod.rs:46-65) as stwo_buf_alloc / stwo_buf_zero /
-stwo_buf_upload / stwo_buf_download / stwo_read_words / stwo_buf_free.
+stwo_buf_upload / stwo_buf_download / stwo_read_words (stwo_read_words_cols for several columns)
+/ stwo_buf_free.
 
 `at` backs the Merkle decommitment's queried values (crates/prover/src/core/vcs/prover.rs:80-149):
 the words read at arbitrary indices must be those of the column, including the first and last.
@@ -43,6 +44,30 @@ def test_alloc_upload_read_words_download_free(cuda, log):
     assert np.array_equal(back, words)
     assert lib.stwo_buf_free(d, None) == 0
     assert lib.stwo_sync(None) == 0
+
+
+@pytest.mark.parametrize("n_cols,log", [(1, 4), (7, 12), (300, 10)])
+def test_read_words_cols_matches_per_column_reads(cuda, n_cols, log):
+    """stwo_read_words_cols (one transfer for a layer's columns) returns, column by column, the
+    words at the same indices, including the first and last."""
+    from stwo_gb300 import _lib
+
+    lib = _lib.load()
+    n = 1 << log
+    rng = np.random.default_rng(1300 + n_cols)
+    cols = [F.rand_m31(rng, n) for _ in range(n_cols)]
+    bufs = [_alloc(lib, n * 4) for _ in range(n_cols)]
+    for b, w in zip(bufs, cols):
+        assert lib.stwo_buf_upload(b, w.ctypes.data_as(C.c_void_p), n * 4, None) == 0
+    idx = np.unique(np.concatenate([[0, n - 1], rng.integers(0, n, size=40)])).astype(np.uint64)
+    out = np.zeros(n_cols * idx.size, np.uint32)
+    tab = (C.c_void_p * n_cols)(*[b.value for b in bufs])
+    assert lib.stwo_read_words_cols(tab, n_cols, idx.ctypes.data_as(C.POINTER(C.c_uint64)), idx.size,
+                                    out.ctypes.data_as(C.POINTER(C.c_uint32)), None) == 0
+    for c in range(n_cols):
+        assert np.array_equal(out[c * idx.size:(c + 1) * idx.size], cols[c][idx.astype(np.int64)]), c
+    for b in bufs:
+        assert lib.stwo_buf_free(b, None) == 0
 
 
 def test_zero_part_of_a_column_and_read_back(cuda):
