@@ -148,3 +148,49 @@ def test_simplify_rules():
     assert ExtExpr.from_secure((1, 2, 3, 4)).simplify() is ExtExpr.const((1, 2, 3, 4))
     with pytest.raises(ValueError):
         (c.inverse()).degree_bound(X.NamedExprs({}, {}))
+
+
+def test_wide_relation_entry_is_one_combine_node():
+    """A relation wider than COMBINE_LOOP_MIN is recorded as one combine node; its format, degree
+    bound and value equal combine_formal's sum of alpha powers times values minus z."""
+    rel = Relation("Wide", X.COMBINE_LOOP_MIN + 4)
+    ev = ExprEvaluator()
+    vals = [ev.next_trace_mask() * BaseExpr.const(k + 1) for k in range(rel.size)]
+    ev.add_to_relation(rel, ExtExpr.one(), vals)
+    ev.finalize_logup_in_pairs()
+    node = next(e for e in ev.ext_intermediates.values() if e.kind == "combine")
+    formal = X.combine_formal(rel, vals)
+    assert node.format_expr() == formal.format_expr()
+    named = X.NamedExprs(dict(ev.intermediates), dict(ev.ext_intermediates))
+    assert node.degree_bound(named) == formal.degree_bound(named)
+    rng = random.Random(5)
+    cols = {}
+    params = rel.param_values(tuple(rng.randrange(X.P) for _ in range(4)), tuple(rng.randrange(X.P) for _ in range(4)))
+
+    def col(c):
+        return cols.setdefault(c, (rng.randrange(X.P), 0, 0, 0))
+
+    assert X.eval_expr(node, col, params) == X.eval_expr(formal, col, params)
+    assert node.simplify().kind == "combine"
+    narrow = ExprEvaluator()
+    narrow.add_to_relation(Relation("Narrow", X.COMBINE_LOOP_MIN), ExtExpr.one(),
+                           [narrow.next_trace_mask() for _ in range(X.COMBINE_LOOP_MIN)])
+    assert all(e.kind != "combine" for e in narrow.ext_intermediates.values())
+
+
+def test_long_flat_body_is_cut_into_blocks_and_marked():
+    """A generated body of more than FLAT_SPLIT_MIN straight-line statements gets a block boundary
+    every FLAT_BLOCK statements and the fast-compile mark; a shorter one, or one made of a loop,
+    is left alone."""
+    from stwo_gb300 import codegen as G
+
+    body = [f"const uint32_t t{i} = {i}u;" for i in range(G.FLAT_SPLIT_MIN + 1)]
+    out, flat = G._split_flat(body)
+    assert flat
+    cuts = [i for i, x in enumerate(out) if "asm volatile" in x]
+    assert len(cuts) == (G.FLAT_SPLIT_MIN + 1) // G.FLAT_BLOCK
+    assert [x for x in out if "asm volatile" not in x] == body
+    short, flat = G._split_flat(body[:G.FLAT_SPLIT_MIN])
+    assert not flat and short == body[:G.FLAT_SPLIT_MIN]
+    loop = ["#pragma unroll 1", "for (int g = 0; g < 8; g++) {"] + ["  " + x for x in body] + ["}"]
+    assert G._split_flat(loop) == (loop, False)
