@@ -795,6 +795,12 @@ int oracle_verify_blake(uint32_t log_n, const uint32_t sums[32], const uint8_t* 
   }
 }
 
+// r rounds of BLAKE2s on the 16-word state v with message m (the scheduler's round function),
+// in place.
+void oracle_blake2s_rounds(uint32_t v[16], const uint32_t m[16], uint32_t rounds) {
+  for (uint32_t r = 0; r < rounds; r++) blake2s_round_words(v, m, r);
+}
+
 // The trace tree of prove_blake (the preprocessed columns, then the trace columns), in commit order,
 // written to `out` column after column; returns the number of words (0 on error or if cap is short).
 size_t oracle_blake_traces(uint32_t log_n, uint32_t* out, size_t cap, uint32_t* n_cols) {

@@ -278,6 +278,13 @@ def verify_blake(log_n, sums, proof: bytes):
     return bool(ok), err.value.decode()
 
 
+def blake2s_rounds(v, m, rounds=10):
+    """The full Blake example's scheduler round function applied `rounds` times."""
+    vv = _u32(v).copy()
+    lib().oracle_blake2s_rounds(_p(vv), _p(_u32(m)), C.c_uint32(rounds))
+    return [int(x) for x in vv]
+
+
 def blake_traces(log_n):
     """The preprocessed and trace columns of prove_blake, in commit order, as one word array."""
     cap = 64 << 20

@@ -42,3 +42,21 @@ def test_blake_prove_verify(oracle):
     ok, why = oracle.verify_blake(4, [tuple(q) for q in moved], proof)
     assert not ok
     assert oracle.verify_blake(4, [sums[1], sums[0]] + sums[2:], proof)[0] is False
+
+
+def test_blake_scheduler_rounds_are_blake2s(oracle):
+    """Pins the scheduler's round function to BLAKE2s itself: ten rounds on the compression's
+    working vector (h, IV ^ (t, f)), finalised as h ^ v[0..8] ^ v[8..16], give hashlib's BLAKE2s-256
+    of a one-block 64-byte message (RFC 7693: parameter block 0x01010020, t = 64, last block)."""
+    import hashlib
+    import struct
+
+    iv = [0x6A09E667, 0xBB67AE85, 0x3C6EF372, 0xA54FF53A, 0x510E527F, 0x9B05688C, 0x1F83D9AB, 0x5BE0CD19]
+    for seed in range(3):
+        msg = bytes((seed * 97 + 13 * i) & 0xFF for i in range(64))
+        m = list(struct.unpack("<16I", msg))
+        h = [iv[0] ^ 0x01010020] + iv[1:]
+        v = h + iv[:4] + [iv[4] ^ 64, iv[5], iv[6] ^ 0xFFFFFFFF, iv[7]]
+        out = oracle.blake2s_rounds(v, m)
+        digest = struct.pack("<8I", *[h[i] ^ out[i] ^ out[i + 8] for i in range(8)])
+        assert digest == hashlib.blake2s(msg).digest()
