@@ -578,6 +578,83 @@ def _store_cubin(handle: int, path: str) -> None:
     os.replace(tmp, path)
 
 
+def _point_function(ev: ExprEvaluator):
+    """The component's constraints at a point as one straight-line Python function f(M, V) -> the
+    constraint values in order, M[interaction][local column][offset index] the sampled mask values
+    and V the parameters (QM31 tuples): the intermediates in definition order, then the
+    constraints, each node computed once. It gives eval_expr's values without its per-node
+    interpretation, for components of thousands of nodes."""
+    lines = ["def f(M, V):"]
+    names: Dict[int, str] = {}
+    inter = {name: f"I{k}" for k, name in enumerate(ev.ordered_intermediates)}
+
+    def leaf(n: Expr) -> str:
+        if n.kind == "col":
+            c = n.val
+            return f"M[{c.interaction}][{c.local}][{ev.mask[c.interaction][c.local].index(c.offset)}]"
+        if n.kind == "const":
+            v = n.val
+            return repr((v % X.P, 0, 0, 0)) if isinstance(v, int) else repr(tuple(v))
+        name = n.val
+        if name in inter:
+            return inter[name]
+        if name in ev.preprocessed:
+            return f"M[0][{ev.preprocessed.index(name)}][0]"
+        return f"V[{name!r}]"
+
+    def emit(root: Expr) -> str:
+        stack = [root]
+        while stack:
+            n = stack[-1]
+            if n.uid in names:
+                stack.pop()
+                continue
+            if n.kind in ("col", "const", "param"):
+                names[n.uid] = leaf(n)
+                stack.pop()
+                continue
+            pending = [a for a in n.args if a.uid not in names]
+            if pending:
+                stack.extend(pending)
+                continue
+            stack.pop()
+            a = [names[x.uid] for x in n.args]
+            k, var = n.kind, f"t{n.uid}"
+            if k in ("add", "sub", "mul"):
+                code = f"{ {'add': 'qa', 'sub': 'qs', 'mul': 'qm'}[k]}({a[0]}, {a[1]})"
+            elif k == "neg":
+                code = f"qn({a[0]})"
+            elif k == "inv":
+                code = f"qi({a[0]})"
+            elif k == "secure_col":
+                code = f"qp(({', '.join(a)},))"
+            elif k == "combine":
+                rel, _ = n.val
+                terms = ", ".join(f"qm(V[{rel + '_alpha' + str(i)!r}], {x})" for i, x in enumerate(a))
+                code = f"qs(qsum(({terms},)), V[{rel + '_z'!r}])"
+            else:
+                raise AssertionError(k)
+            lines.append(f"    {var} = {code}")
+            names[n.uid] = var
+        return names[root.uid]
+
+    for name in ev.ordered_intermediates:
+        lines.append(f"    {inter[name]} = {emit(ev.intermediate(name))}")
+    outs = [emit(c) for c in ev.constraints]
+    lines.append(f"    return [{', '.join(outs)}]")
+
+    def qsum(vs):
+        acc = (0, 0, 0, 0)
+        for v in vs:
+            acc = X.q_add(acc, v)
+        return acc
+
+    scope = {"qa": X.q_add, "qs": X.q_sub, "qm": X.q_mul, "qn": X.q_neg, "qi": X.q_inv,
+             "qp": X.q_from_partial_evals, "qsum": qsum}
+    exec(compile("\n".join(lines), "<point evaluation>", "exec"), scope)
+    return scope["f"]
+
+
 # Recorded components by the AIR's shape_key(): the expressions, the kernel source and handle, and
 # the interaction kernel, shared by every component of that shape (the recording does not depend on
 # the log size, the relation elements or the claimed sum, which reach the kernels as parameters).
@@ -672,18 +749,11 @@ class GeneratedComponent:
         vals = dict(self.air.params())
         if params:
             vals.update(params)
-        ev = self.ev
-
-        def col(c):
-            offs = ev.mask[c.interaction][c.local]
-            return tuple(mask_values[c.interaction][c.local][offs.index(c.offset)])
-
-        for k, name in enumerate(ev.preprocessed):
-            vals.setdefault(name, tuple(mask_values[0][ev.preprocessed.index(name)][0]))
         vals = {k: ((v % X.P, 0, 0, 0) if isinstance(v, int) else tuple(v)) for k, v in vals.items()}
-        vals = X.with_intermediates(ev, col, vals)
-        memo: dict = {}
-        for c in ev.constraints:
-            v = X.eval_expr(c, col, vals, memo)
+        fn = self._rec.get("point")
+        if fn is None:
+            fn = self._rec["point"] = _point_function(self.ev)
+        m = [[[tuple(v) for v in offs] for offs in tree] for tree in mask_values]
+        for v in fn(m, vals):
             acc = X.q_add(X.q_mul(acc, rc), X.q_mul(denom_inv, v))
         return acc

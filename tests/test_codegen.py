@@ -128,3 +128,36 @@ def test_compile_error_is_reported():
     st = _lib.load().stwo_codegen_compile(b"this is not CUDA", 1, 0, 1, 0, C.byref(out))
     assert st == 1
     assert b"does not compile" in _lib.load().stwo_last_error()
+
+
+@pytest.mark.parametrize("kind", ["wide_fib", "poseidon", "plonk", "state_machine_x", "scheduler", "round", "xor12",
+                                  "xor4"])
+def test_point_evaluation_matches_interpreter(kind):
+    """GeneratedComponent.eval_at_point (a straight-line function per component shape) equals the
+    expression interpreter (with_intermediates + eval_expr) at random mask values."""
+    import random
+
+    if kind in CASES:
+        air = make_case(kind)[1]
+    elif kind == "xor12":
+        air = airs.XorTableEval(12, 4, ((1, 2, 3, 4), (5, 6, 7, 8)), (9, 9, 9, 9))
+    else:
+        air = make_blake_case(kind)[0]
+    gc = codegen.GeneratedComponent(air, load=False)
+    ev = gc.ev
+    rng = random.Random(11)
+    mask = [[[tuple(rng.randrange(P) for _ in range(4)) for _ in offs] for offs in tree] for tree in ev.mask]
+    rc, dinv = (3, 1, 4, 1), (5, 9, 2, 6)
+    got = gc.eval_at_point(mask, rc, dinv)
+    vals = {k: ((v % P, 0, 0, 0) if isinstance(v, int) else tuple(v)) for k, v in air.params().items()}
+    for name in ev.preprocessed:
+        vals.setdefault(name, mask[0][ev.preprocessed.index(name)][0])
+
+    def col(c):
+        return mask[c.interaction][c.local][ev.mask[c.interaction][c.local].index(c.offset)]
+
+    vals = X.with_intermediates(ev, col, vals)
+    want, memo = (0, 0, 0, 0), {}
+    for c in ev.constraints:
+        want = X.q_add(X.q_mul(want, rc), X.q_mul(dinv, X.eval_expr(c, col, vals, memo)))
+    assert got == want
