@@ -297,7 +297,7 @@ class SecureCol:
         self.n = n
 
     def at(self, idx: Sequence[int]) -> List[Q]:
-        c = [b.at(idx) for b in self.cols]
+        c = _read_cols(self.cols, idx)
         return [(c[0][i], c[1][i], c[2][i], c[3][i]) for i in range(len(idx))]
 
 
