@@ -35,7 +35,7 @@ def test_state_machine_proof_matches_oracle(cuda, oracle, log_n, initial, cfg):
     assert ok, why
 
 
-@pytest.mark.parametrize("log_n,cfg", [(4, (5, 1, 0, 3)), (5, (6, 2, 1, 4))])
+@pytest.mark.parametrize("log_n,cfg", [(4, (5, 1, 0, 3)), (5, (6, 2, 1, 4)), (7, (10, 2, 2, 8))])
 def test_blake_proof_matches_oracle(cuda, oracle, log_n, cfg):
     """The full Blake example (scheduler, two round components, five XOR tables, preprocessed XOR
     tables) from its framework definitions: the claimed sums and the proof bytes equal the
@@ -50,7 +50,7 @@ def test_blake_proof_matches_oracle(cuda, oracle, log_n, cfg):
     assert ok, why
 
 
-@pytest.mark.parametrize("log_n", [4, 6])
+@pytest.mark.parametrize("log_n", [4, 6, 10])
 def test_blake_device_trace_matches_oracle(cuda, oracle, log_n):
     """stwo_gen_blake_example_trace (scheduler, round components, XOR multiplicities counted with
     atomics) equals the oracle's trace of prove_blake column for column."""
