@@ -674,12 +674,21 @@ class GeneratedComponent:
             source, names = generate(ev)
             n_cols = sum(len(m) for m in ev.mask)
             rec = {"ev": ev, "source": source, "names": names, "n_cols": n_cols, "n_constraints": len(ev.constraints),
-                   "handle": _compiled(source, (n_cols, len(names), len(ev.constraints)), load), "frac": None}
+                   "load": load, "handle": None, "frac": None}
             if key is not None:
                 _RECORDED[(key, load)] = rec
         self._rec = rec
         self.ev, self.source, self.param_names = rec["ev"], rec["source"], rec["names"]
-        self.n_cols, self.n_constraints, self.handle = rec["n_cols"], rec["n_constraints"], rec["handle"]
+        self.n_cols, self.n_constraints = rec["n_cols"], rec["n_constraints"]
+
+    @property
+    def handle(self) -> int:
+        """The compiled constraint kernel, compiled (or loaded from the cubin cache) on first use."""
+        rec = self._rec
+        if rec["handle"] is None:
+            rec["handle"] = _compiled(rec["source"], (rec["n_cols"], len(rec["names"]), rec["n_constraints"]),
+                                      rec["load"])
+        return rec["handle"]
 
     def log_size(self) -> int:
         return self.air.log_size()

@@ -29,6 +29,8 @@ from . import _lib
 from ._lib import QM31, QM31Point, call
 from .circle import canonic_half_coset, coset, subgroup_gen
 from .codegen import GeneratedComponent
+
+STWO_AIR_BLAKE_ROUND = 2  # include/stwo_cuda.h
 from .host_prover import (Blake2sChannel, Buf, CommitmentSchemeProver, SecureCol, _block_views, _coset_vanishing,
                           _finish_proof, _log2, _ptr4, _ptrs, index_to_point, q_add, q_inv, q_m31, q_mul, q_sub)
 
@@ -294,6 +296,25 @@ def prove_state_machine(log_n: int, initial: Sequence[int], cfg=(5, 1, 0, 3)) ->
     return prove(comps, pcs, ch, cfg), (sums[0], sums[1])
 
 
+class HandWrittenComponent(GeneratedComponent):
+    """A framework component whose evaluation on the domain runs one of the library's hand-written
+    kernels (stwo_eval_constraints, as the Rust crate's CudaAir components do); its recorded
+    expressions still give its mask, its LogUp interaction kernel and its evaluation at a point.
+    `air_id` is STWO_AIR_*, `elements` the QM31 values that entry point takes for it."""
+
+    def __init__(self, air, air_id: int, elements: Sequence[Q]):
+        super().__init__(air)
+        self.air_id, self.elements = air_id, [tuple(e) for e in elements]
+
+    def eval_constraints(self, cols: Sequence[int], coeff_powers, accum4: Sequence[int], stream=None,
+                         params: Dict[str, object] = None) -> None:
+        el = (QM31 * len(self.elements))(*[QM31(e) for e in self.elements])
+        comp = _lib.Component(self.air_id, self.log_size(), 0, QM31(tuple(self.air.claimed_sum)), el,
+                              len(self.elements))
+        call("stwo_eval_constraints", C.byref(comp), (C.c_void_p * max(len(cols), 1))(*cols), len(cols), coeff_powers,
+             self.n_constraints, (C.c_void_p * 4)(*accum4), stream)
+
+
 # ------------------------------------------------------------------ the full Blake example
 def blake_preprocessed(log_n: int) -> List[np.ndarray]:
     """The preprocessed columns of prove_blake (air.rs:343-361): IsFirst(L), IsFirst(L+3),
@@ -390,5 +411,9 @@ def prove_blake(log_n: int, cfg=(5, 1, 0, 3)) -> Tuple[bytes, List[Q]]:
     alloc.preprocessed = [is_first_id(log_n), is_first_id(log_n + 3), is_first_id(log_n + 1)]
     for w, e in XOR_TABLES:
         alloc.preprocessed += [xor_table_id(w, e, j) for j in range(3)] + [is_first_id(2 * (w - e))]
-    comps = [alloc.place(GeneratedComponent(air)) for air in evals(sums)]
+    # The round components run the hand-written round kernel (STWO_AIR_BLAKE_ROUND: Round, then
+    # the XOR relations 12, 9, 8, 7, 4), the others their generated kernels.
+    round_el = [q for key in ("round",) + tuple(w for w, _ in XOR_TABLES) for q in el[key]]
+    comps = [alloc.place(HandWrittenComponent(air, STWO_AIR_BLAKE_ROUND, round_el) if isinstance(air, BlakeRoundEval)
+                         else GeneratedComponent(air)) for air in evals(sums)]
     return prove(comps, pcs, ch, cfg), sums
