@@ -1226,6 +1226,25 @@ def run_reference(args):
         unit = "leaves/s"
         config = {"workload": "GKR batch proof, one LogUp-generic layer of 2^20 leaves (Poseidon2 relation shape "
                               "at 2^16 rows)", "log_leaves": 20}
+    elif args.workload == "blake_full":
+        import oracle.pyoracle as O
+
+        log = args.log_rows or 10
+
+        def one():
+            t0 = time.perf_counter()
+            O.prove_blake(log, (5, 1, 0, 3))
+            dt = time.perf_counter() - t0
+            return {"value": (1 << log) / dt, "unit": "BLAKE2s instances/s", "proof_s": dt,
+                    "cores": os.cpu_count(), "kind": "port",
+                    "sample": f"one whole prove_blake of 2^{log} instances"}
+
+        for _ in range(min(args.warmup, 1)):
+            one()
+        vals = [one() for _ in range(args.steps)]
+        metric = f"full Blake example proof s & BLAKE2s instances/s (2^{log} instances)"
+        unit = "BLAKE2s instances/s"
+        config = {"workload": f"prove_blake, 2^{log} instances", "log_instances": log, "pcs_config": [5, 1, 0, 3]}
     else:
         # Each step is one whole proof of the benchmarked configuration (2^16 rows: ~2-3 s on 16
         # cores), so both arms time the same work.
