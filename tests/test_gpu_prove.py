@@ -35,6 +35,34 @@ def test_wide_fib_proof_bytes_match_oracle(cuda, oracle, log_n, n_cols, cfg):
     assert ok, why
 
 
+def _random_cases(n, seed):
+    """Seeded (log_n, n_cols, (pow_bits, log_blowup, log_last_layer, n_queries)) combinations that
+    the reference's FRI verifier accepts: every column's line degree bound (log_n - 1 for the trace)
+    above the last layer's (FriVerifier::commit, crates/prover/src/core/fri.rs:356-420)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        log_n = int(rng.integers(2, 13))
+        out.append((log_n, int(rng.integers(4, 151)),
+                    (int(rng.integers(0, 13)), int(rng.integers(1, 4)), int(rng.integers(0, min(3, log_n - 1))),
+                     int(rng.integers(1, 21)))))
+    return out
+
+
+@pytest.mark.parametrize("log_n,n_cols,cfg", _random_cases(8, 2026))
+def test_wide_fib_random_configurations_match_oracle(cuda, oracle, log_n, n_cols, cfg):
+    """Seeded random sizes, widths and PcsConfigs: bytes equal to the oracle's, verifier accepts."""
+    from stwo_gb300.prover import prove_wide_fib, wide_fib_trace
+
+    rng = np.random.default_rng(log_n * 7919 + n_cols)
+    a = F.rand_m31(rng, 1 << log_n)
+    b = F.rand_m31(rng, 1 << log_n)
+    want = oracle.prove_wide_fib(log_n, n_cols, a, b, cfg)
+    assert prove_wide_fib(log_n, wide_fib_trace(log_n, n_cols, dev(a), dev(b)), cfg) == want
+    ok, why = oracle.verify_wide_fib(log_n, n_cols, want)
+    assert ok, why
+
+
 def test_wide_fib_reference_inputs(cuda, oracle):
     # The reference test's inputs (a = 1, b = row index) at log 2..6.
     from stwo_gb300.prover import prove_wide_fib, wide_fib_trace
