@@ -93,6 +93,32 @@ def test_poseidon_proof_bytes_match_oracle(cuda, oracle, log_n, seeded, cfg):
     assert ok, why
 
 
+def _random_poseidon_cases(n, seed):
+    """Seeded (log_n, cfg) for Poseidon2 proofs within the verifier's rule (last layer bound below
+    log_n - 1)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        log_n = int(rng.integers(4, 10))
+        out.append((log_n, (int(rng.integers(0, 13)), int(rng.integers(1, 4)), int(rng.integers(0, 3)),
+                            int(rng.integers(1, 21)))))
+    return out
+
+
+@pytest.mark.parametrize("log_n,cfg", _random_poseidon_cases(4, 2027))
+def test_poseidon_random_configurations_match_oracle(cuda, oracle, log_n, cfg):
+    """Seeded random sizes and PcsConfigs over seeded initial states: bytes and claimed sum equal to
+    the oracle's, verifier accepts."""
+    from stwo_gb300.prover import prove_poseidon
+
+    init = F.rand_m31(np.random.default_rng(log_n * 31 + cfg[3]), (1 << log_n) * 8 * 16)
+    want, want_cs = oracle.prove_poseidon(log_n, init, cfg)
+    got, cs = prove_poseidon(log_n, dev(init), cfg)
+    assert (got, cs) == (want, want_cs)
+    ok, why = oracle.verify_poseidon(log_n, cs, got)
+    assert ok, why
+
+
 @pytest.mark.parametrize("log_n", [4, 9])
 def test_poseidon_initial_states_from_pinned_host_memory(cuda, oracle, log_n):
     # The trace kernel reads the initial states straight from pinned host memory (16 rows: half a
