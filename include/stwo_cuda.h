@@ -322,6 +322,13 @@ stwo_status stwo_prove_blake_round(uint32_t log_n_rows, const uint32_t* d_inputs
                                    uint8_t* h_proof, size_t capacity, size_t* h_len, stwo_qm31* h_claimed_sum,
                                    void* stream);
 
+/* A framework component's constraints at one point (constraint_framework/point.rs:15-70), on the
+ * host, from its recorded expressions compiled to a small program (values: inputs, then one per
+ * op; ops add, sub, mul, neg, inv, partial-evals, relation combine); *acc = acc * rc + denom_inv * c
+ * for each output constraint c. The program format is written beside the function. */
+stwo_status stwo_point_program_eval(const uint32_t* program, size_t program_len, const stwo_qm31* inputs,
+                                    size_t n_inputs, stwo_qm31 rc, stwo_qm31 denom_inv, stwo_qm31* acc);
+
 /* The trace of the full Blake example (prove_blake, crates/prover/src/examples/blake/air.rs:363-400;
  * generators scheduler/gen.rs:45-118, round/gen.rs:206-235, xor_table/mod.rs:60-90) for 2^log_n
  * BLAKE2s instances, generated in HBM. d_trace receives, column after column in commit order, the

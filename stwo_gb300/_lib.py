@@ -124,6 +124,8 @@ SIGNATURES = {
     "stwo_prove_blake_round": (C.c_int32, [U32, VP, PcsConfig, VP, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(QM31),
                                         VP]),
     "stwo_gen_blake_example_trace": (C.c_int32, [U32, VP, VP, VP]),
+    "stwo_point_program_eval": (C.c_int32, [C.POINTER(C.c_uint32), C.c_size_t, C.POINTER(QM31), C.c_size_t, QM31, QM31,
+                                            C.POINTER(QM31)]),
     "stwo_server_create": (C.c_int32, [U32, C.c_size_t, C.c_int, PVP]),
     "stwo_server_submit": (C.c_int32, [VP, C.POINTER(ProofJob), C.POINTER(C.c_uint64)]),
     "stwo_server_wait": (C.c_int32, [VP, C.c_uint64, C.POINTER(ProofResult)]),

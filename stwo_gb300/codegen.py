@@ -578,81 +578,83 @@ def _store_cubin(handle: int, path: str) -> None:
     os.replace(tmp, path)
 
 
-def _point_function(ev: ExprEvaluator):
-    """The component's constraints at a point as one straight-line Python function f(M, V) -> the
-    constraint values in order, M[interaction][local column][offset index] the sampled mask values
-    and V the parameters (QM31 tuples): the intermediates in definition order, then the
-    constraints, each node computed once. It gives eval_expr's values without its per-node
-    interpretation, for components of thousands of nodes."""
-    lines = ["def f(M, V):"]
-    names: Dict[int, str] = {}
-    inter = {name: f"I{k}" for k, name in enumerate(ev.ordered_intermediates)}
+def _point_program(ev: ExprEvaluator):
+    """The component's constraints at a point as a program for stwo_point_program_eval: the
+    intermediates in definition order, then the constraints, each node one op. Returns the program
+    (uint32 words) and its inputs, in order: ("mask", interaction, local column, offset index),
+    ("param", name) or ("const", QM31). A relation entry's alpha powers are consecutive inputs."""
+    inputs: List[tuple] = []
+    index: Dict[tuple, int] = {}
+    ops: List[List[tuple]] = []  # each op: its words, operands as ("i", input) or ("o", op)
+    ref: Dict[int, tuple] = {}
+    inter: Dict[str, tuple] = {}
 
-    def leaf(n: Expr) -> str:
+    def inp(key) -> tuple:
+        if key not in index:
+            index[key] = len(inputs)
+            inputs.append(key)
+        return ("i", index[key])
+
+    def leaf(n: Expr) -> tuple:
         if n.kind == "col":
             c = n.val
-            return f"M[{c.interaction}][{c.local}][{ev.mask[c.interaction][c.local].index(c.offset)}]"
+            return inp(("mask", c.interaction, c.local, ev.mask[c.interaction][c.local].index(c.offset)))
         if n.kind == "const":
             v = n.val
-            return repr((v % X.P, 0, 0, 0)) if isinstance(v, int) else repr(tuple(v))
+            return inp(("const", (v % X.P, 0, 0, 0) if isinstance(v, int) else tuple(v)))
         name = n.val
         if name in inter:
             return inter[name]
         if name in ev.preprocessed:
-            return f"M[0][{ev.preprocessed.index(name)}][0]"
-        return f"V[{name!r}]"
+            return inp(("mask", 0, ev.preprocessed.index(name), 0))
+        return inp(("param", name))
 
-    def emit(root: Expr) -> str:
+    def emit(root: Expr) -> tuple:
         stack = [root]
         while stack:
             n = stack[-1]
-            if n.uid in names:
+            if n.uid in ref:
                 stack.pop()
                 continue
             if n.kind in ("col", "const", "param"):
-                names[n.uid] = leaf(n)
+                ref[n.uid] = leaf(n)
                 stack.pop()
                 continue
-            pending = [a for a in n.args if a.uid not in names]
+            pending = [a for a in n.args if a.uid not in ref]
             if pending:
                 stack.extend(pending)
                 continue
             stack.pop()
-            a = [names[x.uid] for x in n.args]
-            k, var = n.kind, f"t{n.uid}"
-            if k in ("add", "sub", "mul"):
-                code = f"{ {'add': 'qa', 'sub': 'qs', 'mul': 'qm'}[k]}({a[0]}, {a[1]})"
-            elif k == "neg":
-                code = f"qn({a[0]})"
-            elif k == "inv":
-                code = f"qi({a[0]})"
-            elif k == "secure_col":
-                code = f"qp(({', '.join(a)},))"
-            elif k == "combine":
-                rel, _ = n.val
-                terms = ", ".join(f"qm(V[{rel + '_alpha' + str(i)!r}], {x})" for i, x in enumerate(a))
-                code = f"qs(qsum(({terms},)), V[{rel + '_z'!r}])"
+            args = [ref[x.uid] for x in n.args]
+            k = n.kind
+            if k == "combine":
+                rel, size = n.val
+                first = ("param", f"{rel}_alpha0")
+                if first not in index:
+                    for i in range(size):
+                        inp(("param", f"{rel}_alpha{i}"))
+                k0 = index[first]
+                assert all(index.get(("param", f"{rel}_alpha{i}")) == k0 + i for i in range(size)), rel
+                words = [7, len(args), ("a", k0), inp(("param", f"{rel}_z"))] + args
             else:
-                raise AssertionError(k)
-            lines.append(f"    {var} = {code}")
-            names[n.uid] = var
-        return names[root.uid]
+                words = [{"add": 1, "sub": 2, "mul": 3, "neg": 4, "inv": 5, "secure_col": 6}[k]] + args
+            ops.append(words)
+            ref[n.uid] = ("o", len(ops) - 1)
+        return ref[root.uid]
 
     for name in ev.ordered_intermediates:
-        lines.append(f"    {inter[name]} = {emit(ev.intermediate(name))}")
+        inter[name] = emit(ev.intermediate(name))
     outs = [emit(c) for c in ev.constraints]
-    lines.append(f"    return [{', '.join(outs)}]")
+    n_in = len(inputs)
 
-    def qsum(vs):
-        acc = (0, 0, 0, 0)
-        for v in vs:
-            acc = X.q_add(acc, v)
-        return acc
+    def word(w):
+        if isinstance(w, int):
+            return w
+        kind, k = w
+        return k if kind in ("i", "a") else n_in + k
 
-    scope = {"qa": X.q_add, "qs": X.q_sub, "qm": X.q_mul, "qn": X.q_neg, "qi": X.q_inv,
-             "qp": X.q_from_partial_evals, "qsum": qsum}
-    exec(compile("\n".join(lines), "<point evaluation>", "exec"), scope)
-    return scope["f"]
+    prog = [len(ops)] + [word(w) for op in ops for w in op] + [len(outs)] + [word(o) for o in outs]
+    return (C.c_uint32 * len(prog))(*prog), len(prog), inputs
 
 
 # Recorded components by the AIR's shape_key(): the expressions, the kernel source and handle, and
@@ -753,16 +755,29 @@ class GeneratedComponent:
     def eval_at_point(self, mask_values: Sequence[Sequence[Sequence[X.Q]]], rc: X.Q, denom_inv: X.Q,
                       params: Dict[str, object] = None, acc: X.Q = (0, 0, 0, 0)) -> X.Q:
         """PointEvaluator (constraint_framework/point.rs:15-70): acc = acc * rc + denom_inv * c
-        for every constraint in order. `mask_values[interaction][local column][offset index]` are
-        the sampled values; preprocessed columns are interaction 0 in request order."""
+        for every constraint in order, by the library on the host (stwo_point_program_eval, from
+        the component's recorded expressions). `mask_values[interaction][local column][offset
+        index]` are the sampled values; preprocessed columns are interaction 0 in request order."""
         vals = dict(self.air.params())
         if params:
             vals.update(params)
         vals = {k: ((v % X.P, 0, 0, 0) if isinstance(v, int) else tuple(v)) for k, v in vals.items()}
-        fn = self._rec.get("point")
-        if fn is None:
-            fn = self._rec["point"] = _point_function(self.ev)
-        m = [[[tuple(v) for v in offs] for offs in tree] for tree in mask_values]
-        for v in fn(m, vals):
-            acc = X.q_add(X.q_mul(acc, rc), X.q_mul(denom_inv, v))
-        return acc
+        from . import _lib
+        from ._lib import QM31
+
+        prog = self._rec.get("point")
+        if prog is None:
+            prog = self._rec["point"] = _point_program(self.ev)
+        words, n_words, inputs = prog
+        arr = (QM31 * max(len(inputs), 1))()
+        for i, key in enumerate(inputs):
+            if key[0] == "mask":
+                arr[i] = QM31(tuple(mask_values[key[1]][key[2]][key[3]]))
+            elif key[0] == "param":
+                arr[i] = QM31(vals[key[1]])
+            else:
+                arr[i] = QM31(key[1])
+        out = QM31(tuple(acc))
+        _lib.call("stwo_point_program_eval", words, n_words, arr, len(inputs), QM31(tuple(rc)), QM31(tuple(denom_inv)),
+                  C.byref(out))
+        return tuple(out.v)

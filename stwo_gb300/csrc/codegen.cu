@@ -20,6 +20,7 @@
 #include <nvrtc.h>
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "codegen_headers.inc"  // kFieldCuh, kCodegenRtCuh: the two headers, as text
 
@@ -279,6 +280,80 @@ stwo_status stwo_logup_interaction_codegen(stwo_codegen_component comp, uint32_t
   if (st) return st;
   if (h_claimed_sum)
     for (int j = 0; j < 4; j++) h_claimed_sum->v[j] = claimed.v[j];
+  return STWO_OK;
+}
+
+// A component's constraints at one point, from its recorded expressions compiled to a program
+// (stwo_gb300/codegen.py, _point_program): the PointEvaluator of constraint_framework/point.rs,
+// on the host. Values 0 .. n_inputs - 1 are the inputs (mask values, parameters, constants); each
+// op appends one value:
+//   1 add a b | 2 sub a b | 3 mul a b | 4 neg a | 5 inv a | 6 partial a b c d (a + b i + c u + d iu)
+//   7 combine n alpha0 z v_0 .. v_{n-1} (sum alpha_{alpha0 + k} v_k - z, the relation entry)
+// then n_out and the output value indices; *acc becomes acc * rc + denom_inv * c for each output c
+// in order.
+stwo_status stwo_point_program_eval(const uint32_t* program, size_t program_len, const stwo_qm31* inputs,
+                                    size_t n_inputs, stwo_qm31 rc, stwo_qm31 denom_inv, stwo_qm31* acc) {
+  STWO_REQUIRE(program && acc && (inputs || n_inputs == 0), "null argument");
+  std::vector<hq> val(n_inputs);
+  for (size_t i = 0; i < n_inputs; i++) val[i] = hq_from(inputs[i]);
+  size_t pc = 0;
+  auto next = [&](uint32_t& w) {
+    if (pc >= program_len) return false;
+    w = program[pc++];
+    return true;
+  };
+  auto arg = [&](hq& out) {
+    uint32_t i;
+    if (!next(i) || i >= val.size()) return false;
+    out = val[i];
+    return true;
+  };
+  uint32_t n_ops;
+  STWO_REQUIRE(next(n_ops), "truncated program");
+  val.reserve(n_inputs + n_ops);
+  for (uint32_t k = 0; k < n_ops; k++) {
+    uint32_t op;
+    STWO_REQUIRE(next(op), "truncated program");
+    hq a, b, c, d, r;
+    switch (op) {
+      case 1: case 2: case 3:
+        STWO_REQUIRE(arg(a) && arg(b), "bad operand at op %u", k);
+        r = op == 1 ? hq_add(a, b) : op == 2 ? hq_sub(a, b) : hq_mul(a, b);
+        break;
+      case 4: case 5:
+        STWO_REQUIRE(arg(a), "bad operand at op %u", k);
+        r = op == 4 ? hq_sub(hq_make(0, 0, 0, 0), a) : hq_inv(a);
+        break;
+      case 6:
+        STWO_REQUIRE(arg(a) && arg(b) && arg(c) && arg(d), "bad operand at op %u", k);
+        r = hq_add(hq_add(a, hq_mul(b, hq_make(0, 1, 0, 0))),
+                   hq_add(hq_mul(c, hq_make(0, 0, 1, 0)), hq_mul(d, hq_make(0, 0, 0, 1))));
+        break;
+      case 7: {
+        uint32_t n, alpha0;
+        STWO_REQUIRE(next(n) && next(alpha0) && arg(b) && (size_t)alpha0 + n <= val.size(), "bad combine at op %u", k);
+        r = hq_make(0, 0, 0, 0);
+        for (uint32_t j = 0; j < n; j++) {
+          STWO_REQUIRE(arg(a), "bad combine operand at op %u", k);
+          r = hq_add(r, hq_mul(val[alpha0 + j], a));
+        }
+        r = hq_sub(r, b);
+        break;
+      }
+      default:
+        STWO_REQUIRE(false, "unknown op %u at %u", op, k);
+    }
+    val.push_back(r);
+  }
+  uint32_t n_out;
+  STWO_REQUIRE(next(n_out), "truncated program");
+  hq ac = hq_from(*acc), rcq = hq_from(rc), dq = hq_from(denom_inv);
+  for (uint32_t k = 0; k < n_out; k++) {
+    hq v;
+    STWO_REQUIRE(arg(v), "bad output %u", k);
+    ac = hq_add(hq_mul(ac, rcq), hq_mul(dq, v));
+  }
+  for (int i = 0; i < 4; i++) acc->v[i] = ac.v[i];
   return STWO_OK;
 }
 

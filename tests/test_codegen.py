@@ -133,8 +133,9 @@ def test_compile_error_is_reported():
 @pytest.mark.parametrize("kind", ["wide_fib", "poseidon", "plonk", "state_machine_x", "scheduler", "round", "xor12",
                                   "xor4"])
 def test_point_evaluation_matches_interpreter(kind):
-    """GeneratedComponent.eval_at_point (a straight-line function per component shape) equals the
-    expression interpreter (with_intermediates + eval_expr) at random mask values."""
+    """GeneratedComponent.eval_at_point (the library's stwo_point_program_eval running the
+    component's compiled point program, on the host) equals the expression interpreter
+    (with_intermediates + eval_expr) at random mask values."""
     import random
 
     if kind in CASES:
