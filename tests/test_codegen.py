@@ -162,3 +162,28 @@ def test_point_evaluation_matches_interpreter(kind):
     for c in ev.constraints:
         want = X.q_add(X.q_mul(want, rc), X.q_mul(dinv, X.eval_expr(c, col, vals, memo)))
     assert got == want
+
+
+def test_point_program_rejects_malformed_programs():
+    """stwo_point_program_eval checks every operand and length: a truncated program, an operand
+    past the values, an unknown op or a combine reaching past the inputs is INVALID_ARG, not a read
+    out of bounds."""
+    from stwo_gb300 import _lib
+    from stwo_gb300._lib import QM31
+
+    lib = _lib.load()
+    inputs = (QM31 * 2)(QM31((1, 2, 3, 4)), QM31((5, 6, 7, 8)))
+
+    def run(words):
+        arr = (C.c_uint32 * max(len(words), 1))(*words)
+        acc = QM31((0, 0, 0, 0))
+        return lib.stwo_point_program_eval(arr, len(words), inputs, 2, QM31((1, 0, 0, 0)), QM31((1, 0, 0, 0)),
+                                           C.byref(acc)), tuple(acc.v)
+
+    st, acc = run([1, 1, 0, 1, 1, 2])  # one add (v2 = v0 + v1), output v2
+    assert st == 0 and acc == (6, 8, 10, 12)
+    assert run([1, 1, 0])[0] == 1           # truncated add
+    assert run([1, 1, 0, 5, 1, 2])[0] == 1  # operand past the values
+    assert run([1, 9, 0, 1, 1, 2])[0] == 1  # unknown op
+    assert run([1, 7, 3, 0, 1, 0, 1, 0, 1, 2])[0] == 1  # combine alphas past the values
+    assert run([0, 1, 7])[0] == 1           # output past the values
