@@ -55,3 +55,19 @@ def test_rust_binding_matches_header():
     for name, n in decls.items():
         assert name in header, name
         assert header[name] == n, (name, header[name], n)
+
+
+def test_new_entry_points_check_arguments_before_any_device_work():
+    """Argument errors come back as INVALID_ARG from host checks, with no device call (CPU)."""
+    from stwo_gb300 import _lib
+
+    lib = _lib.load()
+    buf = (ctypes.c_uint32 * 4)()
+    # The full Blake example's trace: log_n outside [4, 20], or a null buffer.
+    assert lib.stwo_gen_blake_example_trace(3, buf, buf, None) == 1
+    assert lib.stwo_gen_blake_example_trace(21, buf, buf, None) == 1
+    assert lib.stwo_gen_blake_example_trace(4, None, buf, None) == 1
+    # Multi-column reads: nothing to read is a no-op; null arguments are rejected.
+    assert lib.stwo_read_words_cols(None, 0, None, 0, None, None) == 0
+    assert lib.stwo_read_words_cols(None, 2, None, 3, None, None) == 1
+    assert b"null" in lib.stwo_last_error()
