@@ -134,6 +134,16 @@ def prove(components: Sequence[PlacedComponent], pcs: CommitmentSchemeProver, ch
     px, py = ch.random_point()
     oods = (px, py)
     points: List[List[list]] = [[[] for _ in tr.polys] for tr in pcs.trees]
+    shifted: Dict[Tuple[int, int], tuple] = {}
+
+    def mask_pt(log_size: int, offset: int):
+        """oods shifted by `offset` steps of the log_size coset; the same for every column that
+        asks for it."""
+        key = (log_size, offset)
+        if key not in shifted:
+            shifted[key] = _mask_point(oods, log_size, offset)
+        return shifted[key]
+
     for c in components:
         for i in c.preprocessed:
             points[0][i] = [oods]
@@ -142,7 +152,7 @@ def prove(components: Sequence[PlacedComponent], pcs: CommitmentSchemeProver, ch
                 continue
             a, _ = c.spans[t]
             for k, offs in enumerate(offs_per_col):
-                points[t][a + k] = [_mask_point(oods, c.gc.log_size(), o) for o in offs]
+                points[t][a + k] = [mask_pt(c.gc.log_size(), o) for o in offs]
     points[-1] = [[oods]] * 4
     polys = [p for tr in pcs.trees for p in tr.polys]
     poly_of, pts = [], []
@@ -196,8 +206,11 @@ def _upload(cols: Sequence[np.ndarray]) -> List[Buf]:
 
 def _commit_evals(pcs: CommitmentSchemeProver, evals: Sequence[Buf], ch: Blake2sChannel) -> None:
     """TreeBuilder::extend_evals + commit for columns of any sizes (interpolated in place)."""
-    for log in sorted({_log2(e.n) for e in evals}):
-        grp = [e for e in evals if _log2(e.n) == log]
+    by_log: Dict[int, List[Buf]] = {}
+    for e in evals:
+        by_log.setdefault(_log2(e.n), []).append(e)
+    for log in sorted(by_log):
+        grp = by_log[log]
         call("stwo_interpolate_columns", pcs.tw, canonic_half_coset(log), _ptrs(grp), len(grp), None)
     pcs.commit_polys(list(evals), ch)
 

@@ -403,8 +403,11 @@ class CommitmentSchemeProver:
     def commit_polys(self, polys: Sequence[Buf], ch: Blake2sChannel):
         """TreeBuilder::extend_polys + commit (pcs/prover.rs:208-227)."""
         evals = _block_views([p.n << self.log_blowup for p in polys])
-        for log in sorted({_log2(p.n) for p in polys}):
-            idx = [i for i, p in enumerate(polys) if _log2(p.n) == log]
+        by_log: Dict[int, List[int]] = {}
+        for i, p in enumerate(polys):
+            by_log.setdefault(_log2(p.n), []).append(i)
+        for log in sorted(by_log):
+            idx = by_log[log]
             call("stwo_evaluate_columns", self.tw, canonic_half_coset(log + self.log_blowup),
                  _ptrs([polys[i] for i in idx]), log, _ptrs([evals[i] for i in idx]), len(idx), None)
         t = CommitmentTree(polys, evals)
